@@ -1,0 +1,300 @@
+"""Benchmark: seg-seg pair interactions/s on one GB300 (FP64 plain method).
+
+Workload "gpu65k": 65,536 segments = 8192 closed square loops (shear and
+prismatic, BCC {110}<111> slip systems, L ~ U(20, 200) b, centres uniform in a
+20,000^3 b cube, 5% shifted / tilted near-parallel neighbours), seed 0.
+A step is one all-pairs calcSegSegForce: N(N-1)/2 = 2.147e9 pair interactions.
+
+value: device-resident path (packed segments already in HBM, forces left in
+       HBM), CUDA events on the launching stream over K steps, L2 flushed
+       (a 512 MB write) before every step.
+e2e:   the reference-facing C-ABI call with host buffers (ddd_segseg_force):
+       host -> device copies of the network arrays, compute, device -> host copy
+       of the 3 x 2 x N forces, all inside the timed region.
+cpu_baseline: the C++/OpenMP port of the reference's threaded path
+       (calcSegSegForcePar: contiguous i-chunks, one atomic add per output
+       component) on the host's cores, on a bounded sub-network of the workload.
+
+--impl reference: times that CPU port alone (the reference itself is Julia and
+cannot run here), same metric and workload, each step a bounded sub-network.
+
+Multi-GPU (--gpus N under torchrun): independent replicas (the path needs no
+exchange between GPUs here); value = all ranks' pairs / max rank time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# Algorithmic FLOPs per unit (add/sub/mul/div/sqrt/log/atan = 1 each), from the
+# op-counting instantiation of the oracle (oracle/ddd_oracle.cpp, opcount_*):
+OPS_GENERAL_PAIR = 1511  # general branch: 626 add, 840 mul, 23 div, 10 sqrt, 8 log, 4 atan
+OPS_PARALLEL_PAIR = 985  # near-parallel branch without core corrections
+# Each near-parallel side that needs core corrections adds two general evaluations.
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.idx = device_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_par_sample(pkg, synth, oracle, p, b, k5, target_s):
+    """Times the OpenMP port of calcSegSegForcePar on the first n segments of the
+    workload, n chosen so that one run takes about target_s seconds."""
+    threads = cpu_threads()
+    coord, bvec, seg = synth.network_arrays(p[:256], b[:256])
+    net = pkg.DislocationNetwork(coord, bvec, seg)
+    t0 = time.perf_counter()
+    oracle.segseg_par_atomic(k5, net, threads)
+    dt = time.perf_counter() - t0
+    rate = net.numSeg * (net.numSeg - 1) / 2 / dt
+    n_loops = int(min(p.shape[0], max(256, np.sqrt(2 * rate * target_s) / 8)))
+    coord, bvec, seg = synth.network_arrays(p[:n_loops], b[:n_loops])
+    net = pkg.DislocationNetwork(coord, bvec, seg)
+    t0 = time.perf_counter()
+    oracle.segseg_par_atomic(k5, net, threads)
+    dt = time.perf_counter() - t0
+    n = net.numSeg
+    return {"value": n * (n - 1) / 2 / dt, "unit": "pair-interactions/s", "cores": threads, "kind": "port",
+            "sample": "all %d pairs of the first %d segments (%d loops) of the workload, %.1f s" %
+                      (n * (n - 1) // 2, n, n_loops, dt)}
+
+
+def run_reference(args, pkg, synth, oracle):
+    ws, rank = _dist()
+    if rank != 0:
+        return
+    p, b, cfg = synth.make(args.workload, seed=0)
+    k5 = np.array([1.0, 1 / (4 * np.pi), 1 / (8 * np.pi), 1 / (4 * np.pi) / (1 - synth.NU),
+                   synth.NU / (4 * np.pi) / (1 - synth.NU)])
+    times, vals = [], []
+    info = None
+    for it in range(args.warmup + args.steps):
+        info = cpu_par_sample(pkg, synth, oracle, p, b, k5, args.ref_step_s)
+        if it >= args.warmup:
+            vals.append(info["value"])
+    v = statistics.median(vals)
+    n = p.shape[0] * 8
+    out = {
+        "impl": "reference", "metric": "seg-seg pair interactions/s at 65k segs (FP64 plain)",
+        "value": v, "unit": "pair-interactions/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * (n * (n - 1) / 2) / v, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": "%s: %d segments, %d loops" % (args.workload, n, p.shape[0]),
+                   "ms_per_step_note": "extrapolated to the full workload from the sampled pairs/s"},
+        "cpu_baseline": {"kind": "port", "cores": info["cores"], "sample": info["sample"], "value": v,
+                         "unit": "pair-interactions/s",
+                         "what": "C++/OpenMP restatement of calcSegSegForcePar (DislocationForces.jl:719-777); "
+                                 "the Julia reference cannot run on this box (no Julia runtime)"},
+        "e2e": {"value": v, "unit": "pair-interactions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="gpu65k")
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--cpu-target-s", type=float, default=15.0)
+    ap.add_argument("--ref-step-s", type=float, default=4.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+
+    import __graft_entry__ as graft
+    pkg = graft.load_package()
+    oracle, _ = graft.load_oracle()
+    import ddd_gb300.synth as synth
+
+    if args.impl == "reference":
+        run_reference(args, pkg, synth, oracle)
+        return
+
+    import torch
+    ws, rank = _dist()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    p, b, cfg = synth.make(args.workload, seed=0)
+    n = p.shape[0] * 8
+    pairs = n * (n - 1) // 2
+    dln = pkg.DislocationParameters(coreRad=synth.CORE_RAD)
+    mat = pkg.MaterialParameters(mu=synth.MU, nu=synth.NU)
+    k = pkg.consts_of(dln, mat)
+    ctx = pkg.Context(local)
+
+    stream = torch.cuda.Stream()
+    soa = torch.from_numpy(synth.packed_soa(p, b)).cuda()
+    force = torch.zeros(6 * n, dtype=torch.float64, device="cuda")
+    flush = torch.empty(512 * 2 ** 20 // 4, dtype=torch.float32, device="cuda")
+    sptr = stream.cuda_stream
+
+    # One reported call: branch statistics for the algorithmic FLOP count.
+    rep = ctx.segseg_force_device(k, soa.data_ptr(), n, n, force.data_ptr(), stream=sptr, report=True)
+    flops_per_step = (rep["pairs_general"] * OPS_GENERAL_PAIR + rep["pairs_parallel"] * OPS_PARALLEL_PAIR
+                      + rep["core_sides"] * 2 * OPS_GENERAL_PAIR)
+    fp64_peak = ctx.probe_fma_peak(64)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            flush.zero_()
+            ctx.segseg_force_device(k, soa.data_ptr(), n, n, force.data_ptr(), stream=sptr)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        with ClockSampler(local) as clocks:
+            ev0.record(stream)
+            for s in range(args.steps):
+                flush.zero_()
+                kev[s][0].record(stream)
+                ctx.segseg_force_device(k, soa.data_ptr(), n, n, force.data_ptr(), stream=sptr)
+                kev[s][1].record(stream)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+        ms_total = ev0.elapsed_time(ev1)
+        ms_kernel = [a.elapsed_time(b_) for a, b_ in kev]
+    t_rank = torch.tensor([ms_total], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(t_rank, op=dist.ReduceOp.MAX)
+        dist.barrier()
+    ms_step = t_rank.item() / args.steps
+    value = ws * pairs / (ms_step * 1e-3)
+
+    # End to end through the reference-facing C-ABI call with host arrays.
+    coord, bvec, seg = synth.network_arrays(p, b)
+    net = pkg.DislocationNetwork(coord, bvec, seg)
+    e2e_steps = args.e2e_steps if args.e2e_steps is not None else max(1, min(args.steps, 3))
+    pkg_ctx = ctx
+    pkg_ctx.segseg_force(k, net)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        out = pkg_ctx.segseg_force(k, net)
+    t_e2e = (time.perf_counter() - t0) / e2e_steps
+    erep = pkg_ctx.last_report
+    e2e_value = ws * pairs / t_e2e
+    # Same forces as the device-resident path.
+    same = bool(np.array_equal(out.ravel(order="F"), force.cpu().numpy()))
+
+    if rank != 0:
+        return
+    achieved = flops_per_step / (statistics.mean(ms_kernel) * 1e-3)
+    line = {
+        "metric": "seg-seg pair interactions/s at 65k segs (FP64 plain)",
+        "value": value, "unit": "pair-interactions/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded generator, seed 0)",
+        "config": {"workload": "%s: %d segments, %d closed 8-segment square loops, L~U(%g,%g) b, %g^3 b cube, "
+                               "%d%% near-parallel neighbours" % (args.workload, n, p.shape[0], cfg["lmin"],
+                                                                  cfg["lmax"], cfg["cube"],
+                                                                  round(100 * cfg["parallel_fraction"])),
+                   "pairs_per_step": pairs, "l2": "flushed before every step (512 MB write)",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
+                     "frac": achieved / fp64_peak, "traffic": None,
+                     "kernel": "segseg_tile_f64<0>",
+                     "peak_source": "measured FP64 FMA-chain probe on this GPU (ddd_probe_fma_peak); "
+                                    "MEASURED_PEAKS.json holds no FP64 figure",
+                     "flops_per_step": flops_per_step,
+                     "branches": {k_: rep[k_] for k_ in ("pairs_general", "pairs_parallel", "core_sides")}},
+        "e2e": {"value": e2e_value, "unit": "pair-interactions/s", "h2d_bytes_per_step": erep["h2d_bytes"],
+                "d2h_bytes_per_step": erep["d2h_bytes"], "steps": e2e_steps, "matches_device_path": same},
+        "gpu_launches": 3 * args.steps,
+        "kernel_ms_per_step": statistics.mean(ms_kernel),
+    }
+    cs = clocks.summary()
+    if cs:
+        line["clocks"] = cs
+    if not args.no_cpu:
+        k5 = np.array([dln.coreRadSq, mat.μ4π, mat.μ8π, mat.μ4πν, mat.νμ4πν])
+        line["cpu_baseline"] = cpu_par_sample(pkg, synth, oracle, p, b, k5, args.cpu_target_s)
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,342 @@
+"""ddd_gb300 — host-side mirror of DDD.jl's seg-seg force / σ̃ interface over
+the C-ABI library libddd_gb300.so (include/ddd_gb300.h).
+
+The reference is Julia; its drop-in is a `ccall` shim (julia/DDDGB300.jl).
+This module is the same binding written with ctypes so the path can be driven
+and tested from Python: the functions keep the reference's names, argument
+order, array layouts and semantics:
+
+  calcSegSegForce(dlnParams, matParams, network, idx=None)        DislocationForces.jl:470-561
+  calcSegSegForce_inplace(dlnParams, matParams, network, idx=None) calcSegSegForce!  :576-669
+  calc_σTilde(x0, dlnParams, matParams, network, idx=None)        DislocationFEM.jl:24-41
+  calc_σTilde_inplace(σ, x0, dlnParams, matParams, network, idx=None) calc_σTilde! :67-84
+
+All computation runs on the GPU.  There is no CPU fallback: if the library is
+not built or no GPU is usable, calls raise.
+"""
+import ctypes
+import math
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libddd_gb300.so")
+
+DDD_OK, DDD_EINVAL, DDD_ERANGE, DDD_ENONFINITE, DDD_EDEVICE, DDD_ENOMEM = 0, -1, -2, -3, -4, -5
+
+# Every symbol include/ddd_gb300.h declares.
+EXPORTED_SYMBOLS = (
+    "ddd_create", "ddd_destroy", "ddd_last_error", "ddd_version",
+    "ddd_segseg_force", "ddd_segseg_force_inplace", "ddd_sigma_tilde",
+    "ddd_segseg_force_device", "ddd_sigma_tilde_device", "ddd_probe_fma_peak",
+)
+
+
+class DDDError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (code %d)" % (msg, code))
+        self.code = code
+
+
+class ddd_consts(ctypes.Structure):
+    _fields_ = [("aSq", ctypes.c_double), ("mu4pi", ctypes.c_double), ("mu8pi", ctypes.c_double),
+                ("mu4pinu", ctypes.c_double), ("nuMu4pinu", ctypes.c_double)]
+
+
+class ddd_report(ctypes.Structure):
+    _fields_ = [("pairs_general", ctypes.c_int64), ("pairs_parallel", ctypes.c_int64),
+                ("core_sides", ctypes.c_int64), ("kernel_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
+                ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int64)
+_up = ctypes.POINTER(ctypes.c_uint8)
+_vp = ctypes.c_void_p
+_i64 = ctypes.c_int64
+
+
+def build(verbose=False):
+    """Compile libddd_gb300.so for sm_103a (nvcc; works without a GPU)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_ddd_gb300_build", os.path.join(HERE, "build.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    return m.build(verbose=verbose)
+
+
+def library():
+    """The loaded C-ABI library (ctypes.CDLL).  Raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libddd_gb300.so is not built (run __graft_entry__.build() or build()); "
+                               "there is no CPU fallback")
+        L = ctypes.CDLL(LIB_PATH)
+        cp = ctypes.POINTER(ddd_consts)
+        rp = ctypes.POINTER(ddd_report)
+        L.ddd_create.argtypes = [ctypes.c_int]
+        L.ddd_create.restype = _vp
+        L.ddd_destroy.argtypes = [_vp]
+        L.ddd_destroy.restype = None
+        L.ddd_last_error.argtypes = [_vp]
+        L.ddd_last_error.restype = ctypes.c_char_p
+        L.ddd_version.argtypes = []
+        L.ddd_segseg_force.argtypes = [_vp, cp, _dp, _i64, _dp, _i64, _ip, _i64, _up, _i64, _ip, _i64, _dp, rp]
+        L.ddd_segseg_force_inplace.argtypes = [_vp, cp, _dp, _i64, _dp, _i64, _ip, _i64, _up, _i64, _ip, _i64, _dp,
+                                               _i64, rp]
+        L.ddd_sigma_tilde.argtypes = [_vp, cp, _dp, _i64, _dp, _i64, _dp, _i64, _ip, _i64, _i64, _ip, _i64, _dp, rp]
+        L.ddd_segseg_force_device.argtypes = [_vp, cp, _vp, _i64, _vp, _i64, _vp, _vp, rp]
+        L.ddd_sigma_tilde_device.argtypes = [_vp, cp, _vp, _i64, _vp, _i64, _i64, _vp, _vp, rp]
+        L.ddd_probe_fma_peak.argtypes = [_vp, ctypes.c_int, _dp]
+        _lib = L
+    return _lib
+
+
+# ---------------------------------------------------------------------------
+# Parameter and network types (fields as in src/Type/*.jl).
+
+class MaterialParameters:
+    """MaterialParameters (src/Type/MaterialConstructor.jl:42-101): derived constants from μ and ν."""
+
+    def __init__(self, *, crystalStruct="BCC", mu=1.0, muMag=1.0, nu=0.2, sigmaPN=0.0):
+        self.crystalStruct = crystalStruct
+        self.μ = self.mu = float(mu)
+        self.μMag = float(muMag)
+        self.ν = self.nu = float(nu)
+        self.omνInv = 1.0 / (1.0 - self.nu)
+        self.opνInv = 1.0 / (1.0 + self.nu)
+        self.νomνInv = self.nu * self.omνInv
+        self.νopνInv = self.nu * self.opνInv
+        self.μ4π = self.mu / (4.0 * math.pi)
+        self.μ8π = self.μ4π / 2.0
+        self.μ4πν = self.μ4π * self.omνInv
+        self.νμ4πν = self.nu * self.μ4πν
+        self.omνInv8π = self.omνInv / (8.0 * math.pi)
+        self.om2νomνInv8π = (1.0 - 2.0 * self.nu) * self.omνInv8π
+        self.σPN = float(sigmaPN)
+
+
+class DislocationParameters:
+    """The DislocationParameters fields this path reads (src/Type/DislocationConstructor.jl:55-105)."""
+
+    def __init__(self, *, coreRad=1.0, coreRadMag=1.0, minSegLen=None, maxSegLen=None, parCPU=False,
+                 parGPU=True, **other):
+        self.coreRad = float(coreRad)
+        self.coreRadSq = self.coreRad * self.coreRad
+        self.coreRadMag = float(coreRadMag)
+        self.minSegLen = 2 * self.coreRad if minSegLen is None else float(minSegLen)
+        self.maxSegLen = 20 * self.coreRad if maxSegLen is None else float(maxSegLen)
+        self.parCPU = bool(parCPU)
+        self.parGPU = bool(parGPU)
+        for k, v in other.items():
+            setattr(self, k, v)
+
+
+class DislocationNetwork:
+    """The DislocationNetwork arrays this path reads and writes (src/Type/DislocationType.jl:324-340).
+
+    coord (3×nodeBuf), bVec (3×linkBuf), segIdx (linkBuf×3; link, node1, node2;
+    1-based), extSeg (linkBuf), segForce (3×2×linkBuf), numSeg.  Stored
+    Fortran-ordered, which is the Julia memory image.
+    """
+
+    def __init__(self, coord, bVec, segIdx, numSeg=None, extSeg=None, segForce=None):
+        self.coord = np.asfortranarray(coord, dtype=np.float64)
+        self.bVec = np.asfortranarray(bVec, dtype=np.float64)
+        self.segIdx = np.asfortranarray(segIdx, dtype=np.int64)
+        ld = self.segIdx.shape[0]
+        self.numSeg = int(ld if numSeg is None else numSeg)
+        self.extSeg = (np.zeros(ld, np.uint8) if extSeg is None else np.ascontiguousarray(extSeg, dtype=np.uint8))
+        self.segForce = (np.zeros((3, 2, self.bVec.shape[1]), np.float64, order="F") if segForce is None
+                         else np.asfortranarray(segForce, dtype=np.float64))
+
+
+def consts_of(dlnParams, matParams):
+    k = ddd_consts()
+    k.aSq = dlnParams.coreRadSq
+    k.mu4pi = matParams.μ4π
+    k.mu8pi = matParams.μ8π
+    k.mu4pinu = matParams.μ4πν
+    k.nuMu4pinu = matParams.νμ4πν
+    return k
+
+
+# ---------------------------------------------------------------------------
+# Context.
+
+class Context:
+    """Owns one ddd_ctx (device buffers, stream) on one CUDA device."""
+
+    def __init__(self, device=0):
+        L = library()
+        self._L = L
+        self._h = L.ddd_create(int(device))
+        if not self._h:
+            raise DDDError(DDD_EDEVICE, "ddd_create(%d) failed: %s" % (device, L.ddd_last_error(None).decode()))
+        self.device = device
+        self.last_report = None
+
+    def close(self):
+        if self._h:
+            self._L.ddd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != DDD_OK:
+            msg = self._L.ddd_last_error(self._h).decode()
+            if rc == DDD_ERANGE:
+                raise IndexError(msg)
+            if rc in (DDD_EINVAL, DDD_ENONFINITE):
+                raise ValueError(msg)
+            raise DDDError(rc, msg)
+
+    @staticmethod
+    def _net(network):
+        coord = np.require(network.coord, np.float64, ["F"])
+        bvec = np.require(network.bVec, np.float64, ["F"])
+        seg = np.require(network.segIdx, np.int64, ["F"])
+        ext = np.require(network.extSeg, np.uint8, ["C"])
+        if coord.ndim != 2 or coord.shape[0] != 3 or bvec.ndim != 2 or bvec.shape[0] != 3:
+            raise ValueError("coord and bVec must be 3×n")
+        if seg.ndim != 2 or seg.shape[1] != 3:
+            raise ValueError("segIdx must be n×3")
+        if ext.shape[0] < network.numSeg:
+            raise ValueError("extSeg shorter than numSeg")
+        return coord, bvec, seg, ext
+
+    @staticmethod
+    def _idx(idx):
+        if idx is None:
+            return None
+        return np.ascontiguousarray(np.atleast_1d(np.asarray(idx)), dtype=np.int64)
+
+    def segseg_force(self, k, network, idx=None, out=None):
+        coord, bvec, seg, ext = self._net(network)
+        idx = self._idx(idx)
+        n = network.numSeg if idx is None else len(idx)
+        if out is None:
+            out = np.zeros((3, 2, n), np.float64, order="F")
+        rep = ddd_report()
+        rc = self._L.ddd_segseg_force(
+            self._h, ctypes.byref(k), coord.ctypes.data_as(_dp), coord.shape[1], bvec.ctypes.data_as(_dp),
+            bvec.shape[1], seg.ctypes.data_as(_ip), seg.shape[0], ext.ctypes.data_as(_up), network.numSeg,
+            None if idx is None else idx.ctypes.data_as(_ip), 0 if idx is None else len(idx),
+            out.ctypes.data_as(_dp), ctypes.byref(rep))
+        self._check(rc)
+        self.last_report = rep.as_dict()
+        return out
+
+    def segseg_force_inplace(self, k, network, idx=None):
+        coord, bvec, seg, ext = self._net(network)
+        idx = self._idx(idx)
+        sf = network.segForce
+        if not (sf.flags.f_contiguous and sf.dtype == np.float64 and sf.shape[:2] == (3, 2)):
+            raise ValueError("segForce must be a Fortran-ordered float64 3×2×n array")
+        rep = ddd_report()
+        rc = self._L.ddd_segseg_force_inplace(
+            self._h, ctypes.byref(k), coord.ctypes.data_as(_dp), coord.shape[1], bvec.ctypes.data_as(_dp),
+            bvec.shape[1], seg.ctypes.data_as(_ip), seg.shape[0], ext.ctypes.data_as(_up), network.numSeg,
+            None if idx is None else idx.ctypes.data_as(_ip), 0 if idx is None else len(idx),
+            sf.ctypes.data_as(_dp), sf.shape[2], ctypes.byref(rep))
+        self._check(rc)
+        self.last_report = rep.as_dict()
+
+    def sigma_tilde(self, k, x0, network, idx=None, out=None):
+        coord, bvec, seg, _ = self._net(network)
+        x0 = np.require(x0, np.float64, ["F"])
+        if x0.ndim == 1:
+            x0 = x0.reshape(3, -1, order="F")
+        if x0.shape[0] != 3:
+            raise ValueError("x0 must be 3×M")
+        M = x0.shape[1]
+        idx = self._idx(idx)
+        if out is None:
+            out = np.zeros((6, M), np.float64, order="F")
+        rep = ddd_report()
+        rc = self._L.ddd_sigma_tilde(
+            self._h, ctypes.byref(k), x0.ctypes.data_as(_dp), M, coord.ctypes.data_as(_dp), coord.shape[1],
+            bvec.ctypes.data_as(_dp), bvec.shape[1], seg.ctypes.data_as(_ip), seg.shape[0], network.numSeg,
+            None if idx is None else idx.ctypes.data_as(_ip), 0 if idx is None else len(idx),
+            out.ctypes.data_as(_dp), ctypes.byref(rep))
+        self._check(rc)
+        self.last_report = rep.as_dict()
+        return out
+
+    def segseg_force_device(self, k, segs_ptr, ld, numSeg, force_ptr, ext_ptr=None, stream=None, report=False):
+        """Device-resident all-pairs call; pointers are raw device addresses (ints)."""
+        rep = ddd_report() if report else None
+        rc = self._L.ddd_segseg_force_device(self._h, ctypes.byref(k), segs_ptr, ld, ext_ptr, numSeg, force_ptr,
+                                             stream, ctypes.byref(rep) if report else None)
+        self._check(rc)
+        return rep.as_dict() if report else None
+
+    def sigma_tilde_device(self, k, x0_ptr, M, segs_ptr, ld, numSeg, sigma_ptr, stream=None, report=False):
+        rep = ddd_report() if report else None
+        rc = self._L.ddd_sigma_tilde_device(self._h, ctypes.byref(k), x0_ptr, M, segs_ptr, ld, numSeg, sigma_ptr,
+                                            stream, ctypes.byref(rep) if report else None)
+        self._check(rc)
+        return rep.as_dict() if report else None
+
+    def probe_fma_peak(self, precision=64):
+        v = ctypes.c_double(0)
+        self._check(self._L.ddd_probe_fma_peak(self._h, int(precision), ctypes.byref(v)))
+        return v.value
+
+
+_contexts = {}
+
+
+def get_context(device=0):
+    if device not in _contexts:
+        _contexts[device] = Context(device)
+    return _contexts[device]
+
+
+# ---------------------------------------------------------------------------
+# The reference's interface.
+
+def calcSegSegForce(dlnParams, matParams, network, idx=None):
+    """calcSegSegForce (DislocationForces.jl:470-561): a fresh 3×2×numSeg array
+    (or 3×2×length(idx) for an index list)."""
+    return get_context().segseg_force(consts_of(dlnParams, matParams), network, idx)
+
+
+def calcSegSegForce_inplace(dlnParams, matParams, network, idx=None):
+    """calcSegSegForce! (DislocationForces.jl:576-669): adds into network.segForce."""
+    get_context().segseg_force_inplace(consts_of(dlnParams, matParams), network, idx)
+    return None
+
+
+def calc_σTilde(x0, dlnParams, matParams, network, idx=None):
+    """calc_σTilde (DislocationFEM.jl:24-41): 6×M stresses, or a 6-vector for one point."""
+    x0 = np.asarray(x0, dtype=np.float64)
+    sig = get_context().sigma_tilde(consts_of(dlnParams, matParams), x0.reshape(3, -1, order="F"), network, idx)
+    return sig[:, 0].copy() if sig.shape[1] == 1 else sig
+
+
+def calc_σTilde_inplace(σ, x0, dlnParams, matParams, network, idx=None):
+    """calc_σTilde! (DislocationFEM.jl:67-84): asserts the shapes, then overwrites σ."""
+    x0 = np.asarray(x0, dtype=np.float64)
+    if not (σ.ndim == x0.ndim and σ.shape[0] == 6):
+        raise AssertionError("ndims(σ) == ndims(x0) && size(σ, 1) == 6")
+    if σ.ndim == 2 and σ.shape[1] != x0.shape[1]:
+        raise AssertionError("size(σ, 2) == size(x0, 2)")
+    sig = get_context().sigma_tilde(consts_of(dlnParams, matParams), x0.reshape(3, -1, order="F"), network, idx)
+    σ[...] = sig.reshape(σ.shape, order="F")
+    return σ
+
+
+calc_sigmaTilde = calc_σTilde
+calc_sigmaTilde_inplace = calc_σTilde_inplace

@@ -1,0 +1,495 @@
+// C-ABI layer of libddd_gb300.so: validation, device buffers, copies, launch
+// sequencing.  Declared in include/ddd_gb300.h.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/ddd_gb300.h"
+#include "ddd_internal.h"
+#include "pair_f64.cuh"
+
+namespace {
+
+std::string g_create_error;
+std::mutex g_create_mu;
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = bytes + bytes / 8 + 256;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return e;
+    }
+    cap = want;
+    return cudaSuccess;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <class T> T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+}  // namespace
+
+struct ddd_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  std::mutex mu;
+  std::string err;
+  DevBuf coord, bvec, segidx, ext, soa, skip, partial, out, rows, x0, sigma, counters, probe;
+  std::vector<double> hostTmp;
+};
+
+namespace {
+
+int fail(ddd_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int cuda_fail(ddd_ctx* c, cudaError_t e, const char* where) {
+  std::string m = std::string(where) + ": " + cudaGetErrorName(e) + ": " + cudaGetErrorString(e);
+  return fail(c, e == cudaErrorMemoryAllocation ? DDD_ENOMEM : DDD_EDEVICE, m);
+}
+
+#define CK(call, where)                              \
+  do {                                               \
+    cudaError_t _e = (call);                         \
+    if (_e != cudaSuccess) return cuda_fail(ctx, _e, where); \
+  } while (0)
+
+bool finite3(const double* p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
+
+int check_consts(ddd_ctx* ctx, const ddd_consts* k, ddd::KConsts& K) {
+  if (!k) return fail(ctx, DDD_EINVAL, "consts is NULL");
+  const double v[5] = {k->aSq, k->mu4pi, k->mu8pi, k->mu4pinu, k->nuMu4pinu};
+  for (double x : v)
+    if (!std::isfinite(x)) return fail(ctx, DDD_ENONFINITE, "non-finite material/core constant");
+  if (!(k->aSq > 0.0)) return fail(ctx, DDD_EINVAL, "aSq (coreRadSq) must be > 0");
+  K.aSq = k->aSq;
+  K.mu4pi = k->mu4pi;
+  K.mu8pi = k->mu8pi;
+  K.mu4pinu = k->mu4pinu;
+  K.nuMu4pinu = k->nuMu4pinu;
+  K.mu8piaSq = k->aSq * k->mu8pi;      // DislocationForces.jl:681
+  K.mu4pinuaSq = k->aSq * k->mu4pinu;  // DislocationForces.jl:682
+  return DDD_OK;
+}
+
+// Checks one segIdx row (0-based row r): link/node indices in range, finite
+// data, non-zero length.
+int check_row(ddd_ctx* ctx, const double* coord, int64_t coordCols, const double* bVec, int64_t bVecCols,
+              const int64_t* segIdx, int64_t ld, int64_t r) {
+  const int64_t l = segIdx[r], a = segIdx[r + ld], b = segIdx[r + 2 * ld];
+  char buf[160];
+  if (l < 1 || l > bVecCols || a < 1 || a > coordCols || b < 1 || b > coordCols) {
+    snprintf(buf, sizeof buf, "segIdx row %lld = (%lld, %lld, %lld) out of range (bVec cols %lld, coord cols %lld)",
+             (long long)(r + 1), (long long)l, (long long)a, (long long)b, (long long)bVecCols,
+             (long long)coordCols);
+    return fail(ctx, DDD_ERANGE, buf);
+  }
+  const double* p1 = coord + 3 * (a - 1);
+  const double* p2 = coord + 3 * (b - 1);
+  const double* bv = bVec + 3 * (l - 1);
+  if (!finite3(p1) || !finite3(p2) || !finite3(bv)) {
+    snprintf(buf, sizeof buf, "segment %lld has a non-finite coordinate or Burgers vector", (long long)(r + 1));
+    return fail(ctx, DDD_ENONFINITE, buf);
+  }
+  if (p1[0] == p2[0] && p1[1] == p2[1] && p1[2] == p2[2]) {
+    snprintf(buf, sizeof buf, "segment %lld has zero length", (long long)(r + 1));
+    return fail(ctx, DDD_ENONFINITE, buf);
+  }
+  return DDD_OK;
+}
+
+int check_network(ddd_ctx* ctx, const double* coord, int64_t coordCols, const double* bVec, int64_t bVecCols,
+                  const int64_t* segIdx, int64_t ld, int64_t numSeg) {
+  if (numSeg < 0 || coordCols < 0 || bVecCols < 0 || ld < 0) return fail(ctx, DDD_EINVAL, "negative size");
+  if (numSeg > ld) return fail(ctx, DDD_EINVAL, "numSeg exceeds the rows of segIdx (ldSegIdx)");
+  if (numSeg > 0 && (!coord || !bVec || !segIdx)) return fail(ctx, DDD_EINVAL, "network array is NULL");
+  for (int64_t r = 0; r < numSeg; ++r) {
+    int rc = check_row(ctx, coord, coordCols, bVec, bVecCols, segIdx, ld, r);
+    if (rc) return rc;
+  }
+  return DDD_OK;
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms;
+}
+
+// Uploads the network and builds the packed SoA; returns npad.
+int upload_network(ddd_ctx* ctx, const double* coord, int64_t coordCols, const double* bVec, int64_t bVecCols,
+                   const int64_t* segIdx, int64_t ld, const uint8_t* extSeg, int64_t numSeg, int64_t& npad,
+                   int64_t& h2d) {
+  npad = ddd::segseg_npad(numSeg);
+  const size_t cB = (size_t)coordCols * 3 * sizeof(double), bB = (size_t)bVecCols * 3 * sizeof(double);
+  const size_t sB = (size_t)ld * 3 * sizeof(int64_t), eB = extSeg ? (size_t)numSeg : 0;
+  CK(ctx->coord.ensure(cB), "alloc coord");
+  CK(ctx->bvec.ensure(bB), "alloc bVec");
+  CK(ctx->segidx.ensure(sB), "alloc segIdx");
+  if (eB) CK(ctx->ext.ensure(eB), "alloc extSeg");
+  CK(ctx->soa.ensure(ddd::segseg_soa_bytes(npad)), "alloc segment SoA");
+  CK(ctx->skip.ensure((size_t)npad), "alloc skip flags");
+  CK(cudaMemcpyAsync(ctx->coord.p, coord, cB, cudaMemcpyHostToDevice, ctx->stream), "copy coord");
+  CK(cudaMemcpyAsync(ctx->bvec.p, bVec, bB, cudaMemcpyHostToDevice, ctx->stream), "copy bVec");
+  CK(cudaMemcpyAsync(ctx->segidx.p, segIdx, sB, cudaMemcpyHostToDevice, ctx->stream), "copy segIdx");
+  if (eB) CK(cudaMemcpyAsync(ctx->ext.p, extSeg, eB, cudaMemcpyHostToDevice, ctx->stream), "copy extSeg");
+  h2d += (int64_t)(cB + bB + sB + eB);
+  CK(ddd::launch_prep_segments(ctx->coord.as<double>(), ctx->bvec.as<double>(), ctx->segidx.as<int64_t>(), ld,
+                               eB ? ctx->ext.as<uint8_t>() : nullptr, numSeg, npad, ctx->soa.as<double>(),
+                               ctx->skip.as<uint8_t>(), ctx->stream),
+     "prep_segments");
+  return DDD_OK;
+}
+
+// Shared body of ddd_segseg_force / _inplace: computes into ctx->hostTmp
+// (6 × (numSeg or nIdx)).
+int segseg_compute(ddd_ctx* ctx, const ddd_consts* k, const double* coord, int64_t coordCols, const double* bVec,
+                   int64_t bVecCols, const int64_t* segIdx, int64_t ld, const uint8_t* extSeg, int64_t numSeg,
+                   const int64_t* idx, int64_t nIdx, ddd_report* rep) {
+  ddd::KConsts K;
+  int rc = check_consts(ctx, k, K);
+  if (rc) return rc;
+  rc = check_network(ctx, coord, coordCols, bVec, bVecCols, segIdx, ld, numSeg);
+  if (rc) return rc;
+  const bool rowsMode = idx != nullptr;
+  if (rowsMode) {
+    if (nIdx < 0) return fail(ctx, DDD_EINVAL, "nIdx < 0");
+    for (int64_t q = 0; q < nIdx; ++q)
+      if (idx[q] < 1 || idx[q] > numSeg) {
+        char buf[96];
+        snprintf(buf, sizeof buf, "idx[%lld] = %lld outside 1..numSeg=%lld", (long long)q, (long long)idx[q],
+                 (long long)numSeg);
+        return fail(ctx, DDD_ERANGE, buf);
+      }
+  }
+  const int64_t nOut = rowsMode ? nIdx : numSeg;
+  ctx->hostTmp.assign((size_t)nOut * 6, 0.0);
+  if (rep) memset(rep, 0, sizeof *rep);
+  if (nOut == 0 || numSeg == 0) return DDD_OK;
+
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  int64_t h2d = 0, npad = 0;
+  CK(cudaEventRecord(ctx->ev[0], ctx->stream), "event");
+  rc = upload_network(ctx, coord, coordCols, bVec, bVecCols, segIdx, ld, extSeg, numSeg, npad, h2d);
+  if (rc) return rc;
+  CK(ctx->counters.ensure(3 * sizeof(unsigned long long)), "alloc counters");
+  CK(cudaMemsetAsync(ctx->counters.p, 0, 3 * sizeof(unsigned long long), ctx->stream), "memset counters");
+  CK(ctx->out.ensure((size_t)nOut * 6 * sizeof(double)), "alloc output");
+  if (!rowsMode) {
+    CK(ctx->partial.ensure(ddd::segseg_partial_bytes_all(npad)), "alloc partial sums");
+    CK(cudaEventRecord(ctx->ev[1], ctx->stream), "event");
+    CK(ddd::launch_segseg_all_f64(K, ctx->soa.as<double>(), ctx->skip.as<uint8_t>(), npad, ctx->partial.as<double>(),
+                                  ctx->out.as<double>(), numSeg, ctx->counters.as<unsigned long long>(), ctx->stream),
+       "segseg_all_f64");
+  } else {
+    std::vector<int64_t> rows0((size_t)nIdx);
+    for (int64_t q = 0; q < nIdx; ++q) rows0[q] = idx[q] - 1;
+    CK(ctx->rows.ensure((size_t)nIdx * sizeof(int64_t)), "alloc rows");
+    CK(cudaMemcpyAsync(ctx->rows.p, rows0.data(), (size_t)nIdx * sizeof(int64_t), cudaMemcpyHostToDevice,
+                       ctx->stream),
+       "copy idx");
+    h2d += nIdx * (int64_t)sizeof(int64_t);
+    CK(ctx->partial.ensure(ddd::segseg_partial_bytes_rows(nIdx, npad)), "alloc partial sums");
+    CK(cudaEventRecord(ctx->ev[1], ctx->stream), "event");
+    CK(ddd::launch_segseg_rows_f64(K, ctx->soa.as<double>(), ctx->skip.as<uint8_t>(), npad, ctx->rows.as<int64_t>(),
+                                   nIdx, ctx->partial.as<double>(), ctx->out.as<double>(),
+                                   ctx->counters.as<unsigned long long>(), ctx->stream),
+       "segseg_rows_f64");
+  }
+  CK(cudaEventRecord(ctx->ev[2], ctx->stream), "event");
+  unsigned long long cnt[3] = {0, 0, 0};
+  CK(cudaMemcpyAsync(ctx->hostTmp.data(), ctx->out.p, (size_t)nOut * 6 * sizeof(double), cudaMemcpyDeviceToHost,
+                     ctx->stream),
+     "copy forces");
+  CK(cudaMemcpyAsync(cnt, ctx->counters.p, sizeof cnt, cudaMemcpyDeviceToHost, ctx->stream), "copy counters");
+  CK(cudaEventRecord(ctx->ev[3], ctx->stream), "event");
+  CK(cudaStreamSynchronize(ctx->stream), "segseg_force");
+  if (rep) {
+    rep->pairs_general = (int64_t)cnt[0];
+    rep->pairs_parallel = (int64_t)cnt[1];
+    rep->core_sides = (int64_t)cnt[2];
+    rep->kernel_ms = elapsed(ctx->ev[1], ctx->ev[2]);
+    rep->total_ms = elapsed(ctx->ev[0], ctx->ev[3]);
+    rep->h2d_bytes = h2d;
+    rep->d2h_bytes = nOut * 6 * (int64_t)sizeof(double);
+  }
+  return DDD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ddd_version(void) { return 100; }
+
+ddd_ctx* ddd_create(int device) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  auto bad = [&](const std::string& m) -> ddd_ctx* {
+    std::lock_guard<std::mutex> g(g_create_mu);
+    g_create_error = m;
+    return nullptr;
+  };
+  if (e != cudaSuccess) return bad(std::string("cudaGetDeviceCount: ") + cudaGetErrorString(e));
+  if (device < 0 || device >= n) return bad("no CUDA device " + std::to_string(device));
+  e = cudaSetDevice(device);
+  if (e != cudaSuccess) return bad(std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+  ddd_ctx* c = new ddd_ctx();
+  c->device = device;
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
+  if (e != cudaSuccess) {
+    ddd_destroy(c);
+    return bad(std::string("stream/event creation: ") + cudaGetErrorString(e));
+  }
+  return c;
+}
+
+void ddd_destroy(ddd_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (DevBuf* b : {&c->coord, &c->bvec, &c->segidx, &c->ext, &c->soa, &c->skip, &c->partial, &c->out, &c->rows,
+                    &c->x0, &c->sigma, &c->counters, &c->probe})
+    b->release();
+  for (auto& ev : c->ev)
+    if (ev) cudaEventDestroy(ev);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char* ddd_last_error(const ddd_ctx* c) {
+  if (!c) return g_create_error.c_str();
+  return c->err.c_str();
+}
+
+int ddd_segseg_force(ddd_ctx* ctx, const ddd_consts* k, const double* coord, int64_t coordCols, const double* bVec,
+                     int64_t bVecCols, const int64_t* segIdx, int64_t ldSegIdx, const uint8_t* extSeg,
+                     int64_t numSeg, const int64_t* idx, int64_t nIdx, double* force, ddd_report* rep) {
+  if (!ctx) return DDD_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  const int64_t nOut = idx ? nIdx : numSeg;
+  if (nOut > 0 && !force) return fail(ctx, DDD_EINVAL, "force is NULL");
+  int rc = segseg_compute(ctx, k, coord, coordCols, bVec, bVecCols, segIdx, ldSegIdx, extSeg, numSeg, idx, nIdx, rep);
+  if (rc) return rc;
+  if (nOut > 0) memcpy(force, ctx->hostTmp.data(), (size_t)nOut * 6 * sizeof(double));
+  return DDD_OK;
+}
+
+int ddd_segseg_force_inplace(ddd_ctx* ctx, const ddd_consts* k, const double* coord, int64_t coordCols,
+                             const double* bVec, int64_t bVecCols, const int64_t* segIdx, int64_t ldSegIdx,
+                             const uint8_t* extSeg, int64_t numSeg, const int64_t* idx, int64_t nIdx,
+                             double* segForce, int64_t segForceCols, ddd_report* rep) {
+  if (!ctx) return DDD_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (segForceCols < numSeg) return fail(ctx, DDD_EINVAL, "segForce has fewer columns than numSeg");
+  const int64_t nOut = idx ? nIdx : numSeg;
+  if (nOut > 0 && !segForce) return fail(ctx, DDD_EINVAL, "segForce is NULL");
+  int rc = segseg_compute(ctx, k, coord, coordCols, bVec, bVecCols, segIdx, ldSegIdx, extSeg, numSeg, idx, nIdx, rep);
+  if (rc) return rc;
+  const double* F = ctx->hostTmp.data();
+  if (!idx) {
+    for (int64_t q = 0; q < 6 * numSeg; ++q) segForce[q] += F[q];
+  } else {
+    // calcSegSegForce!'s idx loop (DislocationForces.jl:640-667): skip external,
+    // add into column idx[k]; a repeated index adds again.
+    for (int64_t q = 0; q < nIdx; ++q) {
+      const int64_t i = idx[q] - 1;
+      if (extSeg && extSeg[i]) continue;
+      for (int c = 0; c < 6; ++c) segForce[6 * i + c] += F[6 * q + c];
+    }
+  }
+  return DDD_OK;
+}
+
+int ddd_sigma_tilde(ddd_ctx* ctx, const ddd_consts* k, const double* x0, int64_t numPoints, const double* coord,
+                    int64_t coordCols, const double* bVec, int64_t bVecCols, const int64_t* segIdx,
+                    int64_t ldSegIdx, int64_t numSeg, const int64_t* idx, int64_t nIdx, double* sigma,
+                    ddd_report* rep) {
+  if (!ctx) return DDD_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  ddd::KConsts K;
+  int rc = check_consts(ctx, k, K);
+  if (rc) return rc;
+  if (numPoints < 0 || numSeg < 0 || ldSegIdx < 0 || (idx && nIdx < 0))
+    return fail(ctx, DDD_EINVAL, "negative size");
+  if (numPoints > 0 && (!x0 || !sigma)) return fail(ctx, DDD_EINVAL, "x0 or sigma is NULL");
+  if (numSeg > ldSegIdx) return fail(ctx, DDD_EINVAL, "numSeg exceeds the rows of segIdx (ldSegIdx)");
+  const int64_t nSel = idx ? nIdx : numSeg;
+  if (nSel > 0 && (!coord || !bVec || !segIdx)) return fail(ctx, DDD_EINVAL, "network array is NULL");
+  // Selected rows, gathered into a compact nSel × 3 segIdx (DislocationFEM.jl:108-118).
+  std::vector<int64_t> sel((size_t)nSel * 3);
+  for (int64_t q = 0; q < nSel; ++q) {
+    int64_t r = q;
+    if (idx) {
+      if (idx[q] < 1 || idx[q] > ldSegIdx) {
+        char buf[96];
+        snprintf(buf, sizeof buf, "idx[%lld] = %lld outside 1..%lld", (long long)q, (long long)idx[q],
+                 (long long)ldSegIdx);
+        return fail(ctx, DDD_ERANGE, buf);
+      }
+      r = idx[q] - 1;
+    }
+    rc = check_row(ctx, coord, coordCols, bVec, bVecCols, segIdx, ldSegIdx, r);
+    if (rc) return rc;
+    sel[q] = segIdx[r];
+    sel[q + nSel] = segIdx[r + ldSegIdx];
+    sel[q + 2 * nSel] = segIdx[r + 2 * ldSegIdx];
+  }
+  for (int64_t j = 0; j < numPoints; ++j)
+    if (!finite3(x0 + 3 * j)) return fail(ctx, DDD_ENONFINITE, "non-finite field point");
+  if (rep) memset(rep, 0, sizeof *rep);
+  if (numPoints == 0) return DDD_OK;
+  if (nSel == 0) {
+    memset(sigma, 0, (size_t)numPoints * 6 * sizeof(double));
+    return DDD_OK;
+  }
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  int64_t h2d = 0, npad = 0;
+  CK(cudaEventRecord(ctx->ev[0], ctx->stream), "event");
+  rc = upload_network(ctx, coord, coordCols, bVec, bVecCols, sel.data(), nSel, nullptr, nSel, npad, h2d);
+  if (rc) return rc;
+  const size_t xB = (size_t)numPoints * 3 * sizeof(double), sB = (size_t)numPoints * 6 * sizeof(double);
+  CK(ctx->x0.ensure(xB), "alloc points");
+  CK(ctx->sigma.ensure(sB), "alloc sigma");
+  CK(cudaMemcpyAsync(ctx->x0.p, x0, xB, cudaMemcpyHostToDevice, ctx->stream), "copy points");
+  h2d += (int64_t)xB;
+  CK(cudaEventRecord(ctx->ev[1], ctx->stream), "event");
+  CK(ddd::launch_sigma_f64(K, ctx->soa.as<double>(), npad, nSel, ctx->x0.as<double>(), numPoints,
+                           ctx->sigma.as<double>(), ctx->stream),
+     "sigma_tilde_f64");
+  CK(cudaEventRecord(ctx->ev[2], ctx->stream), "event");
+  CK(cudaMemcpyAsync(sigma, ctx->sigma.p, sB, cudaMemcpyDeviceToHost, ctx->stream), "copy sigma");
+  CK(cudaEventRecord(ctx->ev[3], ctx->stream), "event");
+  CK(cudaStreamSynchronize(ctx->stream), "sigma_tilde");
+  if (rep) {
+    rep->kernel_ms = elapsed(ctx->ev[1], ctx->ev[2]);
+    rep->total_ms = elapsed(ctx->ev[0], ctx->ev[3]);
+    rep->h2d_bytes = h2d;
+    rep->d2h_bytes = (int64_t)sB;
+  }
+  return DDD_OK;
+}
+
+int ddd_segseg_force_device(ddd_ctx* ctx, const ddd_consts* k, const double* segs, int64_t ldSegs,
+                            const uint8_t* ext, int64_t numSeg, double* force, void* stream, ddd_report* rep) {
+  if (!ctx) return DDD_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  ddd::KConsts K;
+  int rc = check_consts(ctx, k, K);
+  if (rc) return rc;
+  if (numSeg < 0 || ldSegs < numSeg) return fail(ctx, DDD_EINVAL, "bad numSeg / ldSegs");
+  if (numSeg > 0 && (!segs || !force)) return fail(ctx, DDD_EINVAL, "segs or force is NULL");
+  if (rep) memset(rep, 0, sizeof *rep);
+  if (numSeg == 0) return DDD_OK;
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  const int64_t npad = ddd::segseg_npad(numSeg);
+  CK(ctx->soa.ensure(ddd::segseg_soa_bytes(npad)), "alloc segment SoA");
+  CK(ctx->skip.ensure((size_t)npad), "alloc skip flags");
+  CK(ctx->partial.ensure(ddd::segseg_partial_bytes_all(npad)), "alloc partial sums");
+  CK(ctx->counters.ensure(3 * sizeof(unsigned long long)), "alloc counters");
+  if (rep) CK(cudaMemsetAsync(ctx->counters.p, 0, 3 * sizeof(unsigned long long), st), "memset counters");
+  if (rep) CK(cudaEventRecord(ctx->ev[1], st), "event");
+  CK(ddd::launch_prep_segments_packed(segs, ldSegs, ext, numSeg, npad, ctx->soa.as<double>(),
+                                      ctx->skip.as<uint8_t>(), st),
+     "prep_segments_packed");
+  CK(ddd::launch_segseg_all_f64(K, ctx->soa.as<double>(), ctx->skip.as<uint8_t>(), npad, ctx->partial.as<double>(),
+                                force, numSeg, rep ? ctx->counters.as<unsigned long long>() : nullptr, st),
+     "segseg_all_f64");
+  if (rep) {
+    unsigned long long cnt[3] = {0, 0, 0};
+    CK(cudaEventRecord(ctx->ev[2], st), "event");
+    CK(cudaMemcpyAsync(cnt, ctx->counters.p, sizeof cnt, cudaMemcpyDeviceToHost, st), "copy counters");
+    CK(cudaStreamSynchronize(st), "segseg_force_device");
+    rep->pairs_general = (int64_t)cnt[0];
+    rep->pairs_parallel = (int64_t)cnt[1];
+    rep->core_sides = (int64_t)cnt[2];
+    rep->kernel_ms = elapsed(ctx->ev[1], ctx->ev[2]);
+    rep->total_ms = rep->kernel_ms;
+  }
+  return DDD_OK;
+}
+
+int ddd_sigma_tilde_device(ddd_ctx* ctx, const ddd_consts* k, const double* x0, int64_t numPoints,
+                           const double* segs, int64_t ldSegs, int64_t numSeg, double* sigma, void* stream,
+                           ddd_report* rep) {
+  if (!ctx) return DDD_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  ddd::KConsts K;
+  int rc = check_consts(ctx, k, K);
+  if (rc) return rc;
+  if (numSeg < 0 || ldSegs < numSeg || numPoints < 0) return fail(ctx, DDD_EINVAL, "bad sizes");
+  if (numPoints > 0 && (!x0 || !sigma)) return fail(ctx, DDD_EINVAL, "x0 or sigma is NULL");
+  if (numSeg > 0 && !segs) return fail(ctx, DDD_EINVAL, "segs is NULL");
+  if (rep) memset(rep, 0, sizeof *rep);
+  if (numPoints == 0) return DDD_OK;
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  if (numSeg == 0) {
+    CK(cudaMemsetAsync(sigma, 0, (size_t)numPoints * 6 * sizeof(double), st), "memset sigma");
+    return DDD_OK;
+  }
+  const int64_t npad = ddd::segseg_npad(numSeg);
+  CK(ctx->soa.ensure(ddd::segseg_soa_bytes(npad)), "alloc segment SoA");
+  CK(ctx->skip.ensure((size_t)npad), "alloc skip flags");
+  if (rep) CK(cudaEventRecord(ctx->ev[1], st), "event");
+  CK(ddd::launch_prep_segments_packed(segs, ldSegs, nullptr, numSeg, npad, ctx->soa.as<double>(),
+                                      ctx->skip.as<uint8_t>(), st),
+     "prep_segments_packed");
+  CK(ddd::launch_sigma_f64(K, ctx->soa.as<double>(), npad, numSeg, x0, numPoints, sigma, st), "sigma_tilde_f64");
+  if (rep) {
+    CK(cudaEventRecord(ctx->ev[2], st), "event");
+    CK(cudaStreamSynchronize(st), "sigma_tilde_device");
+    rep->kernel_ms = elapsed(ctx->ev[1], ctx->ev[2]);
+    rep->total_ms = rep->kernel_ms;
+  }
+  return DDD_OK;
+}
+
+int ddd_probe_fma_peak(ddd_ctx* ctx, int precision, double* flops_per_s) {
+  if (!ctx || !flops_per_s) return DDD_EINVAL;
+  if (precision != 64 && precision != 32) return fail(ctx, DDD_EINVAL, "precision must be 64 or 32");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  int sms = 0;
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device), "attr");
+  const int threads = 256, blocks = sms * 8;
+  const int iters = precision == 64 ? 4096 : 65536;
+  CK(ctx->probe.ensure((size_t)blocks * threads * sizeof(double)), "alloc probe");
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; ++rep) {
+    CK(cudaEventRecord(ctx->ev[0], ctx->stream), "event");
+    if (precision == 64)
+      CK(ddd::launch_fp64_peak_probe(ctx->probe.as<double>(), iters, blocks, threads, ctx->stream), "probe");
+    else
+      CK(ddd::launch_fp32_peak_probe(ctx->probe.as<float>(), iters, blocks, threads, ctx->stream), "probe");
+    CK(cudaEventRecord(ctx->ev[1], ctx->stream), "event");
+    CK(cudaStreamSynchronize(ctx->stream), "probe");
+    float ms = elapsed(ctx->ev[0], ctx->ev[1]);
+    if (rep > 0 && ms < best) best = ms;
+  }
+  *flops_per_s = 2.0 * 8.0 * (double)iters * (double)threads * (double)blocks / (best * 1e-3);
+  return DDD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,56 @@
+// FP64 field-point stress σ̃ (calc_σTilde, DislocationFEM.jl:86-303).
+//
+// One thread per field point; segments stream through shared memory in tiles
+// of SIG_TILE, every thread reading the same segment at the same time (a
+// broadcast).  Each point's six components accumulate in registers over the
+// segments in list order — the same per-point summation order as the
+// reference's segment-outer loop — and are written once (48 B/point), so σ
+// never round-trips through memory per segment as it does on the CPU.
+#include <cuda_runtime.h>
+
+#include "ddd_internal.h"
+#include "pair_f64.cuh"
+
+namespace ddd {
+
+constexpr int SIG_TILE = 128;
+
+__global__ void __launch_bounds__(SIG_TILE)
+sigma_tilde_f64(KConsts K, const double* __restrict__ soa, int64_t npad, int64_t nSeg, const double* __restrict__ x0,
+                int64_t M, double* __restrict__ sigma) {
+  __shared__ double seg[12][SIG_TILE];
+  const int t = threadIdx.x;
+  const int64_t j = blockIdx.x * (int64_t)SIG_TILE + t;
+  D3 x = {0, 0, 0};
+  if (j < M) x = {x0[3 * j], x0[3 * j + 1], x0[3 * j + 2]};
+  double sig[6] = {0, 0, 0, 0, 0, 0};
+  for (int64_t s0 = 0; s0 < nSeg; s0 += SIG_TILE) {
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 12; ++k) seg[k][t] = soa[k * npad + s0 + t];
+    __syncthreads();
+    const int n = (int)min((int64_t)SIG_TILE, nSeg - s0);
+    if (j < M) {
+      for (int q = 0; q < n; ++q) {
+        D3 n1 = {seg[0][q], seg[1][q], seg[2][q]};
+        D3 n2 = {seg[3][q], seg[4][q], seg[5][q]};
+        D3 b = {seg[6][q], seg[7][q], seg[8][q]};
+        D3 tt = {seg[9][q], seg[10][q], seg[11][q]};
+        sigma_point(K, b, n1, n2, tt, x, sig);
+      }
+    }
+  }
+  if (j < M) {
+#pragma unroll
+    for (int c = 0; c < 6; ++c) sigma[6 * j + c] = sig[c];
+  }
+}
+
+cudaError_t launch_sigma_f64(const KConsts& K, const double* soa, int64_t npad, int64_t nSeg, const double* x0,
+                             int64_t M, double* sigma, cudaStream_t st) {
+  if (M == 0) return cudaSuccess;
+  sigma_tilde_f64<<<(unsigned)((M + SIG_TILE - 1) / SIG_TILE), SIG_TILE, 0, st>>>(K, soa, npad, nSeg, x0, M, sigma);
+  return cudaGetLastError();
+}
+
+}  // namespace ddd

@@ -1,0 +1,132 @@
+/* ddd_gb300 — C ABI of the GB300 implementation of DDD.jl's O(N^2) elastic
+ * interaction hot path: the non-singular segment–segment force and the
+ * field-point stress of a dislocation network.
+ *
+ * Every array argument uses the memory image of the corresponding Julia field
+ * of DDD.jl's DislocationNetwork (src/Type/DislocationType.jl:324-340):
+ * column-major, 1-based indices, Float64 / Int64 / Bool(1 byte):
+ *
+ *   coord    double[3 * coordCols]      network.coord      (3 × nodeBuf)
+ *   bVec     double[3 * bVecCols]       network.bVec       (3 × linkBuf)
+ *   segIdx   int64 [ldSegIdx * 3]       network.segIdx     (linkBuf × 3: link, node1, node2)
+ *   extSeg   uint8 [numSeg]             network.extSeg     (may be NULL = no external segments)
+ *   force    double[3 * 2 * n]          segForce layout    F[k + 3*(node + 2*s)]
+ *   x0       double[3 * numPoints]      field points       (3 × M)
+ *   sigma    double[6 * numPoints]      (xx, yy, zz, xy, xz, yz) per point
+ *   idx      int64 [nIdx]               1-based segment numbers, NULL = all segments
+ *
+ * The caller owns all host arrays; the library copies in, computes on the GPU
+ * and copies out before returning.  No pointer is kept after a call returns.
+ * Device scratch belongs to the context and is reused across calls (grow-only).
+ * Calls on one context are serialised by an internal mutex; separate contexts
+ * are independent.  There is no CPU fallback: with no usable GPU, ddd_create
+ * returns NULL and every call reports DDD_EDEVICE.
+ *
+ * Return codes: DDD_OK (0) or a negative DDD_E* code; ddd_last_error() gives
+ * the message.  Nothing aborts, traps or exits the process.
+ */
+#ifndef DDD_GB300_H
+#define DDD_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DDD_OK 0
+#define DDD_EINVAL (-1)     /* null pointer, negative or inconsistent size */
+#define DDD_ERANGE (-2)     /* an index (segIdx entry or idx entry) out of range */
+#define DDD_ENONFINITE (-3) /* a non-finite coordinate / Burgers vector / constant, or a zero-length segment */
+#define DDD_EDEVICE (-4)    /* CUDA error (message in ddd_last_error) */
+#define DDD_ENOMEM (-5)     /* device allocation failed */
+
+typedef struct ddd_ctx ddd_ctx;
+
+/* Constants of the path.  The reference computes them in
+ * MaterialParameters (src/Type/MaterialConstructor.jl:66-82) and
+ * DislocationParameters (src/Type/DislocationConstructor.jl:83). */
+typedef struct ddd_consts {
+  double aSq;       /* dlnParams.coreRadSq = coreRad^2 */
+  double mu4pi;     /* matParams.μ4π  = μ / (4π) */
+  double mu8pi;     /* matParams.μ8π  = μ4π / 2 */
+  double mu4pinu;   /* matParams.μ4πν = μ4π / (1 - ν) */
+  double nuMu4pinu; /* matParams.νμ4πν = ν μ4πν (σ̃ only) */
+} ddd_consts;
+
+/* Optional per-call report (pass NULL to skip). */
+typedef struct ddd_report {
+  int64_t pairs_general;   /* pairs evaluated on the general branch */
+  int64_t pairs_parallel;  /* pairs routed to the near-parallel branch (1 - c^2 <= sqrt(eps)) */
+  int64_t core_sides;      /* near-parallel sides that needed the two core-correction evaluations */
+  double kernel_ms;        /* device time of the compute kernels */
+  double total_ms;         /* device time of the call including host<->device copies */
+  int64_t h2d_bytes;       /* bytes copied host -> device */
+  int64_t d2h_bytes;       /* bytes copied device -> host */
+} ddd_report;
+
+/* Context on CUDA device `device`; NULL on failure (ddd_last_error(NULL)). */
+ddd_ctx* ddd_create(int device);
+void ddd_destroy(ddd_ctx* ctx);
+/* Message of the last failed call on ctx (or of the last failed ddd_create when ctx is NULL). */
+const char* ddd_last_error(const ddd_ctx* ctx);
+/* ABI version, 100 * major + minor. */
+int ddd_version(void);
+
+/* calcSegSegForce(dlnParams, matParams, network, idx = nothing)
+ *   src/Processing/DislocationForces.jl:470-561 (dispatch :497-561, Ser :778-829,
+ *   Par :719-777, idx form :528-557 + calcSegSegForceIdx! :831-877).
+ * idx == NULL: all unordered pairs i < j, both skipped when extSeg; force is
+ *   3 × 2 × numSeg and is overwritten.
+ * idx != NULL: for each k, i = idx[k] (1-based, duplicates allowed), the sum over
+ *   all j != i (non-external) of the forces on segment i's two nodes; force is
+ *   3 × 2 × nIdx and is overwritten; column k stays 0 when segment i is external. */
+int ddd_segseg_force(ddd_ctx* ctx, const ddd_consts* k, const double* coord, int64_t coordCols, const double* bVec,
+                     int64_t bVecCols, const int64_t* segIdx, int64_t ldSegIdx, const uint8_t* extSeg,
+                     int64_t numSeg, const int64_t* idx, int64_t nIdx, double* force, ddd_report* rep);
+
+/* calcSegSegForce!(dlnParams, matParams, network, idx = nothing)
+ *   src/Processing/DislocationForces.jl:576-669.
+ * Adds into segForce (3 × 2 × segForceCols, segForceCols >= numSeg):
+ * idx == NULL: columns 1:numSeg += all-pairs forces;
+ * idx != NULL: for each k, column idx[k] += that segment's forces (a repeated
+ *   index adds repeatedly, as the reference's loop does). */
+int ddd_segseg_force_inplace(ddd_ctx* ctx, const ddd_consts* k, const double* coord, int64_t coordCols,
+                             const double* bVec, int64_t bVecCols, const int64_t* segIdx, int64_t ldSegIdx,
+                             const uint8_t* extSeg, int64_t numSeg, const int64_t* idx, int64_t nIdx,
+                             double* segForce, int64_t segForceCols, ddd_report* rep);
+
+/* calc_σTilde(x0, dlnParams, matParams, network, idx = nothing) and
+ * calc_σTilde!(σ, x0, ...) — src/Processing/DislocationFEM.jl:24-84, kernel
+ * _calc_σTilde! :86-303.  Both write sigma (6 × numPoints) fresh.  Segments are
+ * rows 1:numSeg of segIdx, or the rows listed in idx (1-based, <= ldSegIdx);
+ * extSeg is ignored, as in the reference. */
+int ddd_sigma_tilde(ddd_ctx* ctx, const ddd_consts* k, const double* x0, int64_t numPoints, const double* coord,
+                    int64_t coordCols, const double* bVec, int64_t bVecCols, const int64_t* segIdx,
+                    int64_t ldSegIdx, int64_t numSeg, const int64_t* idx, int64_t nIdx, double* sigma,
+                    ddd_report* rep);
+
+/* Device-resident forms, for callers whose network already lives in GPU memory.
+ * segs is a packed structure-of-arrays of 9 rows × ldSegs (device pointer):
+ * rows n1x n1y n1z n2x n2y n2z bx by bz, segment s in column s (0-based).
+ * ext (device, may be NULL) marks external segments.  force / sigma are device
+ * pointers in the layouts above.  The work is enqueued on `stream`
+ * (a cudaStream_t, NULL = the context's stream) and the call returns without
+ * waiting unless rep != NULL.  Same semantics as ddd_segseg_force (idx == NULL)
+ * and ddd_sigma_tilde (idx == NULL). */
+int ddd_segseg_force_device(ddd_ctx* ctx, const ddd_consts* k, const double* segs, int64_t ldSegs,
+                            const uint8_t* ext, int64_t numSeg, double* force, void* stream, ddd_report* rep);
+int ddd_sigma_tilde_device(ddd_ctx* ctx, const ddd_consts* k, const double* x0, int64_t numPoints,
+                           const double* segs, int64_t ldSegs, int64_t numSeg, double* sigma, void* stream,
+                           ddd_report* rep);
+
+/* Measurement utility (no reference counterpart): FP64 or FP32 FMA-pipe
+ * throughput of this GPU in FLOP/s, measured with CUDA events over an
+ * FMA-chain kernel filling every SM.  precision: 64 or 32. */
+int ddd_probe_fma_peak(ddd_ctx* ctx, int precision, double* flops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DDD_GB300_H */

@@ -1,0 +1,329 @@
+// CPU ORACLE — test infrastructure only (see ddd_oracle.hpp).  C entry points
+// over the templated restatement, for ctypes (oracle/oracle.py).
+//
+// Network layout (Julia column-major, 1-based indices, as DislocationNetwork
+// stores it: src/Type/DislocationType.jl:324-340):
+//   coord   double[3 * coordCols]       coord[3*(node-1) + k]
+//   bVec    double[3 * bVecCols]        bVec[3*(link-1) + k]
+//   segIdx  int64[ldSegIdx * 3]          segIdx[(i-1) + ldSegIdx*c] = (link, node1, node2)
+//   extSeg  uint8[numSeg]                Julia Vector{Bool}
+//   forces  double[3 * 2 * n]            F[k + 3*(node + 2*s)]  (segForce layout)
+//   sigma   double[6 * M]                (xx, yy, zz, xy, xz, yz) per point
+#include "ddd_oracle.hpp"
+
+#include <omp.h>
+
+#include <atomic>
+#include <cstring>
+#include <vector>
+
+using namespace ddd_oracle;
+
+namespace {
+
+struct Seg {
+  V3<double> b, n1, n2;
+};
+
+Consts<double> make_consts(const double* k5) {
+  // k5 = (aSq, μ4π, μ8π, μ4πν, νμ4πν)
+  Consts<double> K;
+  K.aSq = k5[0];
+  K.mu4pi = k5[1];
+  K.mu8pi = k5[2];
+  K.mu4pinu = k5[3];
+  K.nuMu4pinu = k5[4];
+  K.mu8piaSq = K.aSq * K.mu8pi;      // DislocationForces.jl:681
+  K.mu4pinuaSq = K.aSq * K.mu4pinu;  // DislocationForces.jl:682
+  return K;
+}
+
+inline V3<double> col3(const double* a, int64_t col1) {
+  const double* p = a + 3 * (col1 - 1);
+  return {p[0], p[1], p[2]};
+}
+
+// segSegForceUnroll's gathers (DislocationForces.jl:692-697).
+std::vector<Seg> gather(const double* coord, const double* bVec, const int64_t* segIdx, int64_t ld, int64_t numSeg) {
+  std::vector<Seg> s(numSeg);
+  for (int64_t i = 0; i < numSeg; ++i) {
+    s[i].b = col3(bVec, segIdx[i]);
+    s[i].n1 = col3(coord, segIdx[i + ld]);
+    s[i].n2 = col3(coord, segIdx[i + 2 * ld]);
+  }
+  return s;
+}
+
+inline void add3(double* dst, const V3<double>& v) {
+  dst[0] = dst[0] + v.x;
+  dst[1] = dst[1] + v.y;
+  dst[2] = dst[2] + v.z;
+}
+
+}  // namespace
+
+extern "C" {
+
+// One pair: F[12] = (Fnode1, Fnode2, Fnode3, Fnode4).  DislocationForces.jl:879.
+void oracle_segseg_pair(const double* k5, const double* b1, const double* n11, const double* n12, const double* b2,
+                        const double* n21, const double* n22, double* F) {
+  Consts<double> K = make_consts(k5);
+  V3<double> out[4];
+  seg_seg_force<double>(K, {b1[0], b1[1], b1[2]}, {n11[0], n11[1], n11[2]}, {n12[0], n12[1], n12[2]},
+                        {b2[0], b2[1], b2[2]}, {n21[0], n21[1], n21[2]}, {n22[0], n22[1], n22[2]}, out);
+  for (int q = 0; q < 4; ++q) {
+    F[3 * q + 0] = out[q].x;
+    F[3 * q + 1] = out[q].y;
+    F[3 * q + 2] = out[q].z;
+  }
+}
+
+// Same pair in single precision (for the reduced-precision error studies).
+void oracle_segseg_pair_f32(const double* k5, const double* b1, const double* n11, const double* n12,
+                            const double* b2, const double* n21, const double* n22, double* F) {
+  Consts<float> K;
+  K.aSq = (float)k5[0];
+  K.mu4pi = (float)k5[1];
+  K.mu8pi = (float)k5[2];
+  K.mu4pinu = (float)k5[3];
+  K.nuMu4pinu = (float)k5[4];
+  K.mu8piaSq = K.aSq * K.mu8pi;
+  K.mu4pinuaSq = K.aSq * K.mu4pinu;
+  auto f = [](const double* p) { return V3<float>{(float)p[0], (float)p[1], (float)p[2]}; };
+  V3<float> out[4];
+  seg_seg_force<float>(K, f(b1), f(n11), f(n12), f(b2), f(n21), f(n22), out);
+  for (int q = 0; q < 4; ++q) {
+    F[3 * q + 0] = out[q].x;
+    F[3 * q + 1] = out[q].y;
+    F[3 * q + 2] = out[q].z;
+  }
+}
+
+// calcSegSegForceSer! (DislocationForces.jl:778-829): accumulates into F
+// (3×2×numSeg), which the caller zeroes for the non-mutating form.
+void oracle_segseg_ser(const double* k5, const double* coord, const double* bVec, const int64_t* segIdx, int64_t ld,
+                       const uint8_t* extSeg, int64_t numSeg, double* F) {
+  Consts<double> K = make_consts(k5);
+  std::vector<Seg> s = gather(coord, bVec, segIdx, ld, numSeg);
+  V3<double> out[4];
+  for (int64_t i = 0; i < numSeg; ++i) {
+    if (extSeg[i]) continue;
+    for (int64_t j = i + 1; j < numSeg; ++j) {
+      if (extSeg[j]) continue;
+      seg_seg_force<double>(K, s[i].b, s[i].n1, s[i].n2, s[j].b, s[j].n1, s[j].n2, out);
+      add3(F + 6 * i, out[0]);
+      add3(F + 6 * i + 3, out[1]);
+      add3(F + 6 * j, out[2]);
+      add3(F + 6 * j + 3, out[3]);
+    }
+  }
+}
+
+// calcSegSegForcePar (DislocationForces.jl:719-777): contiguous i-chunks
+// start = 1 + ((tid-1)·N)÷T, stop = (tid·N)÷T per thread, j > i, one atomic
+// add per output component.  Overwrites F (3×2×numSeg).
+void oracle_segseg_par_atomic(const double* k5, const double* coord, const double* bVec, const int64_t* segIdx,
+                              int64_t ld, const uint8_t* extSeg, int64_t numSeg, double* F, int nthreads) {
+  Consts<double> K = make_consts(k5);
+  std::vector<Seg> s = gather(coord, bVec, segIdx, ld, numSeg);
+  std::vector<std::atomic<double>> acc(6 * numSeg);
+  for (auto& a : acc) a.store(0.0, std::memory_order_relaxed);
+#pragma omp parallel num_threads(nthreads)
+  {
+    const int64_t T = omp_get_num_threads();
+    const int64_t tid = omp_get_thread_num() + 1;
+    const int64_t start = 1 + ((tid - 1) * numSeg) / T;
+    const int64_t stop = (tid * numSeg) / T;
+    V3<double> out[4];
+    for (int64_t i1 = start; i1 <= stop; ++i1) {
+      const int64_t i = i1 - 1;
+      if (extSeg[i]) continue;
+      for (int64_t j = i + 1; j < numSeg; ++j) {
+        if (extSeg[j]) continue;
+        seg_seg_force<double>(K, s[i].b, s[i].n1, s[i].n2, s[j].b, s[j].n1, s[j].n2, out);
+        const double* o = &out[0].x;
+        (void)o;
+        const V3<double>* q = out;
+        acc[6 * i + 0].fetch_add(q[0].x, std::memory_order_relaxed);
+        acc[6 * i + 1].fetch_add(q[0].y, std::memory_order_relaxed);
+        acc[6 * i + 2].fetch_add(q[0].z, std::memory_order_relaxed);
+        acc[6 * i + 3].fetch_add(q[1].x, std::memory_order_relaxed);
+        acc[6 * i + 4].fetch_add(q[1].y, std::memory_order_relaxed);
+        acc[6 * i + 5].fetch_add(q[1].z, std::memory_order_relaxed);
+        acc[6 * j + 0].fetch_add(q[2].x, std::memory_order_relaxed);
+        acc[6 * j + 1].fetch_add(q[2].y, std::memory_order_relaxed);
+        acc[6 * j + 2].fetch_add(q[2].z, std::memory_order_relaxed);
+        acc[6 * j + 3].fetch_add(q[3].x, std::memory_order_relaxed);
+        acc[6 * j + 4].fetch_add(q[3].y, std::memory_order_relaxed);
+        acc[6 * j + 5].fetch_add(q[3].z, std::memory_order_relaxed);
+      }
+    }
+  }
+  for (int64_t k = 0; k < 6 * numSeg; ++k) F[k] = acc[k].load(std::memory_order_relaxed);
+}
+
+// Rows of the all-pairs (Ser) result for the segments in rows[] (0-based):
+// F_s = Σ_{j<s} Fnode3,4(j, s) + Σ_{j>s} Fnode1,2(s, j), added in that order,
+// which is exactly the order calcSegSegForceSer! adds into column s.  Used to
+// check large networks on sampled segments.  Overwrites F (3×2×nRows).
+void oracle_segseg_rows(const double* k5, const double* coord, const double* bVec, const int64_t* segIdx, int64_t ld,
+                        const uint8_t* extSeg, int64_t numSeg, const int64_t* rows, int64_t nRows, double* F,
+                        int nthreads) {
+  Consts<double> K = make_consts(k5);
+  std::vector<Seg> s = gather(coord, bVec, segIdx, ld, numSeg);
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+  for (int64_t r = 0; r < nRows; ++r) {
+    const int64_t i = rows[r];
+    double* dst = F + 6 * r;
+    for (int k = 0; k < 6; ++k) dst[k] = 0.0;
+    if (extSeg[i]) continue;
+    V3<double> out[4];
+    for (int64_t j = 0; j < i; ++j) {
+      if (extSeg[j]) continue;
+      seg_seg_force<double>(K, s[j].b, s[j].n1, s[j].n2, s[i].b, s[i].n1, s[i].n2, out);
+      add3(dst, out[2]);
+      add3(dst + 3, out[3]);
+    }
+    for (int64_t j = i + 1; j < numSeg; ++j) {
+      if (extSeg[j]) continue;
+      seg_seg_force<double>(K, s[i].b, s[i].n1, s[i].n2, s[j].b, s[j].n1, s[j].n2, out);
+      add3(dst, out[0]);
+      add3(dst + 3, out[1]);
+    }
+  }
+}
+
+// Index-list form (DislocationForces.jl:528-557 and calcSegSegForceIdx! :831-877):
+// for k, i = idx[k] (1-based), skip ext i; F[:,:,k] += Σ_{j≠i, !ext j} Fnode1,2(i, j).
+// F is 3×2×nIdx and accumulated into (the caller zeroes it for the fresh form).
+void oracle_segseg_idx(const double* k5, const double* coord, const double* bVec, const int64_t* segIdx, int64_t ld,
+                       const uint8_t* extSeg, int64_t numSeg, const int64_t* idx, int64_t nIdx, double* F,
+                       int nthreads) {
+  Consts<double> K = make_consts(k5);
+  std::vector<Seg> s = gather(coord, bVec, segIdx, ld, numSeg);
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+  for (int64_t k = 0; k < nIdx; ++k) {
+    const int64_t i = idx[k] - 1;
+    if (extSeg[i]) continue;
+    double* dst = F + 6 * k;
+    V3<double> out[4];
+    for (int64_t j = 0; j < numSeg; ++j) {
+      if (i == j || extSeg[j]) continue;
+      seg_seg_force<double>(K, s[i].b, s[i].n1, s[i].n2, s[j].b, s[j].n1, s[j].n2, out);
+      add3(dst, out[0]);
+      add3(dst + 3, out[1]);
+    }
+  }
+}
+
+// _calc_σTilde! (DislocationFEM.jl:86-303) for an array of points x0 (3×M).
+// idx (1-based rows of segIdx) selects segments, NULL = 1:numSeg.  Overwrites
+// sigma (6×M).  The reference loops segments outside and points inside; each
+// point's sum is taken over segments in order either way, so the threaded
+// form (points split over threads) returns bitwise the same values.
+void oracle_sigma_tilde(const double* k5, const double* x0, int64_t M, const double* coord, const double* bVec,
+                        const int64_t* segIdx, int64_t ld, int64_t numSeg, const int64_t* idx, int64_t nIdx,
+                        double* sigma, int nthreads) {
+  Consts<double> K = make_consts(k5);
+  int64_t nS = idx ? nIdx : numSeg;
+  std::vector<Seg> s(nS);
+  std::vector<V3<double>> t(nS);
+  for (int64_t q = 0; q < nS; ++q) {
+    int64_t i = idx ? idx[q] - 1 : q;
+    s[q].b = col3(bVec, segIdx[i]);
+    s[q].n1 = col3(coord, segIdx[i + ld]);
+    s[q].n2 = col3(coord, segIdx[i + 2 * ld]);
+    t[q] = normalize(s[q].n2 - s[q].n1);
+  }
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+  for (int64_t j = 0; j < M; ++j) {
+    double sig[6] = {0, 0, 0, 0, 0, 0};
+    V3<double> x = {x0[3 * j], x0[3 * j + 1], x0[3 * j + 2]};
+    for (int64_t q = 0; q < nS; ++q) sigma_tilde_point<double>(K, s[q].b, s[q].n1, s[q].n2, t[q], x, sig);
+    for (int k = 0; k < 6; ++k) sigma[6 * j + k] = sig[k];
+  }
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Operation counting.  The same templates instantiated with a scalar that
+// counts every arithmetic operation give the algorithmic work of one pair or
+// one (segment, point) evaluation.  Convention: add/sub/mul each 1; div, sqrt,
+// log, atan counted separately; sign flips free.  Since the reference never
+// fuses, the FLOP count is add + mul + div + sqrt + log + atan.
+namespace {
+struct OpCounts {
+  long long add, mul, div, sqrt, log, atan, cmp;
+};
+thread_local OpCounts g_ops;
+
+struct OD {
+  double v;
+  OD() = default;
+  constexpr OD(double x) : v(x) {}
+};
+inline OD operator+(OD a, OD b) { ++g_ops.add; return OD(a.v + b.v); }
+inline OD operator-(OD a, OD b) { ++g_ops.add; return OD(a.v - b.v); }
+inline OD operator-(OD a) { return OD(-a.v); }
+inline OD operator*(OD a, OD b) { ++g_ops.mul; return OD(a.v * b.v); }
+inline OD operator/(OD a, OD b) { ++g_ops.div; return OD(a.v / b.v); }
+inline bool operator>(OD a, OD b) { ++g_ops.cmp; return a.v > b.v; }
+inline bool operator<(OD a, OD b) { ++g_ops.cmp; return a.v < b.v; }
+inline OD sqrt(OD a) { ++g_ops.sqrt; return OD(std::sqrt(a.v)); }
+inline OD log(OD a) { ++g_ops.log; return OD(std::log(a.v)); }
+inline OD atan(OD a) { ++g_ops.atan; return OD(std::atan(a.v)); }
+
+Consts<OD> make_consts_od(const double* k5) {
+  Consts<OD> K;
+  K.aSq = k5[0];
+  K.mu4pi = k5[1];
+  K.mu8pi = k5[2];
+  K.mu4pinu = k5[3];
+  K.nuMu4pinu = k5[4];
+  K.mu8piaSq = k5[0] * k5[2];
+  K.mu4pinuaSq = k5[0] * k5[3];
+  return K;
+}
+inline V3<OD> v3od(const double* p) { return {OD(p[0]), OD(p[1]), OD(p[2])}; }
+void store_counts(long long* c) {
+  c[0] = g_ops.add;
+  c[1] = g_ops.mul;
+  c[2] = g_ops.div;
+  c[3] = g_ops.sqrt;
+  c[4] = g_ops.log;
+  c[5] = g_ops.atan;
+  c[6] = g_ops.cmp;
+}
+}  // namespace
+
+extern "C" {
+// counts[7] = (add/sub, mul, div, sqrt, log, atan, compare) for one pair; F[12] out.
+void oracle_opcount_pair(const double* k5, const double* b1, const double* n11, const double* n12, const double* b2,
+                         const double* n21, const double* n22, long long* counts, double* F) {
+  g_ops = OpCounts{0, 0, 0, 0, 0, 0, 0};
+  Consts<OD> K = make_consts_od(k5);
+  V3<OD> out[4];
+  seg_seg_force<OD>(K, v3od(b1), v3od(n11), v3od(n12), v3od(b2), v3od(n21), v3od(n22), out);
+  store_counts(counts);
+  for (int q = 0; q < 4; ++q) {
+    F[3 * q + 0] = out[q].x.v;
+    F[3 * q + 1] = out[q].y.v;
+    F[3 * q + 2] = out[q].z.v;
+  }
+}
+
+// counts[7] for one (segment, point) σ̃ evaluation, excluding the per-segment
+// normalisation of t (done once per segment in the reference).
+void oracle_opcount_sigma(const double* k5, const double* b, const double* n1, const double* n2, const double* x,
+                          long long* counts, double* sig6) {
+  Consts<OD> K = make_consts_od(k5);
+  V3<OD> bb = v3od(b), a1 = v3od(n1), a2 = v3od(n2), xx = v3od(x);
+  V3<OD> t = normalize(a2 - a1);
+  OD sig[6] = {0, 0, 0, 0, 0, 0};
+  g_ops = OpCounts{0, 0, 0, 0, 0, 0, 0};
+  sigma_tilde_point<OD>(K, bb, a1, a2, t, xx, sig);
+  store_counts(counts);
+  for (int k = 0; k < 6; ++k) sig6[k] = sig[k].v;
+}
+}  // extern "C"

@@ -1,0 +1,171 @@
+"""Test fixtures: the reference's loop and network generators, restated in Python.
+
+Test infrastructure only.  Rebuilds the exact networks the reference's golden
+tests are computed on, so the oracle (and through it the GPU path) can be
+checked against those goldens.
+
+Restated from (paths within the DDD.jl project):
+  src/Misc/Misc.jl:143-207                    internalAngle / externalAngle / rot3D
+  src/Type/DislocationConstructor.jl:196-298  DislocationLoop (loopPure: prism / shear)
+  src/Type/DislocationConstructor.jl:477-551  DislocationNetwork(sources; memBuffer)
+  src/Type/DislocationConstructor.jl:645-688  makeNetwork!
+  src/Type/DislocationUtil.jl:96-152          loopDistribution(Zeros), limits!, translatePoints!
+  src/Type/DislocationUtil.jl:161-164         makeSegment(segEdge)
+  src/Type/DislocationUtil.jl:253-295         getSegmentIdx
+  src/Type/MaterialConstructor.jl:42-82       MaterialParameters derived constants
+"""
+import math
+
+import numpy as np
+
+EXT_DLN = 5  # nodeTypeDln.extDln (src/Type/DislocationType.jl:24-32)
+
+
+def material_constants(mu, nu):
+    """(μ4π, μ8π, μ4πν, νμ4πν) as MaterialParameters computes them (MaterialConstructor.jl:66-82)."""
+    om_nu_inv = 1.0 / (1.0 - nu)
+    mu4pi = mu / (4.0 * math.pi)
+    mu8pi = mu4pi / 2.0
+    mu4pinu = mu4pi * om_nu_inv
+    nu_mu4pinu = nu * mu4pinu
+    return mu4pi, mu8pi, mu4pinu, nu_mu4pinu
+
+
+def consts5(core_rad, mu, nu):
+    """Oracle constant vector (aSq, μ4π, μ8π, μ4πν, νμ4πν); aSq = coreRad^2 (DislocationConstructor.jl:83)."""
+    mu4pi, mu8pi, mu4pinu, nu_mu4pinu = material_constants(mu, nu)
+    return np.array([core_rad * core_rad, mu4pi, mu8pi, mu4pinu, nu_mu4pinu], dtype=np.float64)
+
+
+def _norm3(v):
+    return math.sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2])
+
+
+def external_angle(n):
+    internal = (n - 2) * math.pi / n
+    return math.pi - internal
+
+
+def rot3D(xyz, uvw, abc, theta):
+    """Rotate xyz about the axis uvw through abc by theta (Misc.jl:185-207)."""
+    inv = 1.0 / _norm3(uvw)
+    u = [inv * uvw[0], inv * uvw[1], inv * uvw[2]]
+    c = math.cos(theta)
+    omc = 1.0 - c
+    s = math.sin(theta)
+    xdu = xyz[0] * u[0] + xyz[1] * u[1] + xyz[2] * u[2]
+    return [
+        (abc[0] * (u[1] * u[1] + u[2] * u[2]) - u[0] * (abc[1] * u[1] + abc[2] * u[2] - xdu)) * omc
+        + xyz[0] * c
+        + s * (-abc[2] * u[1] + abc[1] * u[2] - u[2] * xyz[1] + u[1] * xyz[2]),
+        (abc[1] * (u[0] * u[0] + u[2] * u[2]) - u[1] * (abc[0] * u[0] + abc[2] * u[2] - xdu)) * omc
+        + xyz[1] * c
+        + s * (abc[2] * u[0] - abc[0] * u[2] + u[2] * xyz[0] - u[0] * xyz[2]),
+        (abc[2] * (u[0] * u[0] + u[1] * u[1]) - u[2] * (abc[0] * u[0] + abc[1] * u[1] - xdu)) * omc
+        + xyz[2] * c
+        + s * (-abc[1] * u[0] + abc[0] * u[1] - u[1] * xyz[0] + u[0] * xyz[1]),
+    ]
+
+
+def make_loop(loop_type, num_sides, node_side, seg_len, slip_plane, b_vec):
+    """Coordinates (nodeTotal×3) of one centred loop (DislocationConstructor.jl:196-298)."""
+    node_total = num_sides * node_side
+    if np.isscalar(seg_len):
+        seg_len = [float(seg_len)] * node_total
+    n_len = len(seg_len)
+    n = [float(v) for v in slip_plane]
+    b = [float(v) for v in b_vec]
+    nn, nb = _norm3(n), _norm3(b)
+    n = [v / nn for v in n]
+    b = [v / nb for v in b]
+    rot_axis = n if loop_type == "shear" else b
+    # makeSegment(segEdge(), n, b) = (n × b) / |n × b|
+    e = [n[1] * b[2] - n[2] * b[1], n[2] * b[0] - n[0] * b[2], n[0] * b[1] - n[1] * b[0]]
+    ne = _norm3(e)
+    e = [v / ne for v in e]
+    segs = [[e[0] * L, e[1] * L, e[2] * L] for L in seg_len]
+    theta = external_angle(num_sides)
+    coord = [[0.0, 0.0, 0.0] for _ in range(node_total)]
+    for i in range(1, num_sides + 1):
+        idx = (i - 1) * node_side
+        mod_idx = (i - 1) % n_len
+        rseg = rot3D(segs[mod_idx], rot_axis, [0.0, 0.0, 0.0], theta * (i - 1))
+        for j in range(1, node_side + 1):
+            if i == j == 1:
+                coord[0] = [0.0, 0.0, 0.0]
+                continue
+            if idx + j <= node_total:
+                prev = coord[idx + j - 2]
+                cur = coord[idx + j - 1]
+                coord[idx + j - 1] = [cur[k] + (prev[k] + rseg[k]) for k in range(3)]
+    mean = [0.0, 0.0, 0.0]
+    for p in coord:
+        for k in range(3):
+            mean[k] += p[k]
+    mean = [m / node_total for m in mean]
+    coord = [[p[k] - mean[k] for k in range(3)] for p in coord]
+    return coord, b
+
+
+class Network:
+    """Arrays in the reference's DislocationNetwork layout, column-major, 1-based indices.
+
+    coord (3×nodeBuf), bVec (3×linkBuf), segIdx (linkBuf×3: link, node1, node2),
+    extSeg (linkBuf bools), numSeg.  numpy stores them Fortran-ordered so
+    `.ravel(order="F")` is the exact Julia memory image.
+    """
+
+    def __init__(self, coord, bvec, seg_idx, ext_seg, num_seg, label=None):
+        self.coord = np.asfortranarray(coord, dtype=np.float64)
+        self.bVec = np.asfortranarray(bvec, dtype=np.float64)
+        self.segIdx = np.asfortranarray(seg_idx, dtype=np.int64)
+        self.extSeg = np.ascontiguousarray(ext_seg, dtype=np.uint8)
+        self.numSeg = int(num_seg)
+        self.label = label
+        self.segForce = np.zeros((3, 2, self.bVec.shape[1]), dtype=np.float64, order="F")
+
+
+def make_network(loops, slip_systems, ranges, shift=None):
+    """DislocationNetwork(loops; memBuffer=1) with dist = Zeros() and buffer = 0.
+
+    Zeros() puts every loop's centre at the lower corner of `range`
+    (DislocationUtil.jl:130-152).
+    """
+    coords, bvecs, links, labels = [], [], [], []
+    base = 0
+    for L in loops:
+        sp = slip_systems["slipPlane"][L["slipSystemIdx"] - 1]
+        bv = slip_systems["bVec"][L["slipSystemIdx"] - 1]
+        c, b = make_loop(L["type"], L["numSides"], L["nodeSide"], L["segLen"], sp, bv)
+        nl = len(c)
+        for _ in range(L["numLoops"]):
+            for q in range(nl):
+                p = c[q]
+                coords.append([p[k] + (ranges[k][0] + (ranges[k][1] - ranges[k][0]) * 0.0) for k in range(3)])
+                bvecs.append(list(b))
+                labels.append(L["label"][q])
+                links.append((base + q + 1, base + (q + 1) % nl + 1))
+            base += nl
+    n = len(coords)
+    coord = np.array(coords, dtype=np.float64).T
+    if shift is not None:
+        coord[:, shift["fromNode"] - 1:] += np.array(shift["by"], dtype=np.float64)[:, None]
+    bvec = np.array(bvecs, dtype=np.float64).T
+    seg_idx = np.zeros((n, 3), dtype=np.int64)
+    ext = np.zeros(n, dtype=np.uint8)
+    for i, (n1, n2) in enumerate(links):
+        seg_idx[i] = (i + 1, n1, n2)
+        ext[i] = 1 if (labels[n1 - 1] == EXT_DLN or labels[n2 - 1] == EXT_DLN) else 0
+    return Network(coord, bvec, seg_idx, ext, n, label=np.array(labels))
+
+
+def sigma_case_network(case):
+    """The single-segment network of DislocationFEMTest.jl:5-155 and its 3×3 grid of points."""
+    coord = np.array(case["coord"], dtype=np.float64).T
+    nseg = len(case["links"])
+    bvec = np.tile(np.array(case["b"], dtype=np.float64)[:, None], (1, nseg))
+    seg_idx = np.array([[i + 1, l[0], l[1]] for i, l in enumerate(case["links"])], dtype=np.int64)
+    net = Network(coord, bvec, seg_idx, np.zeros(nseg, np.uint8), nseg)
+    r = [-300.0, 0.0, 300.0]
+    pts = np.array([[x, y, 0.0] for x in r for y in r], dtype=np.float64).T  # x outer, y inner
+    return net, np.asfortranarray(pts)

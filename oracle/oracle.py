@@ -1,0 +1,158 @@
+"""ctypes wrapper of the CPU oracle (liboracle.so built from ddd_oracle.cpp).
+
+Test infrastructure only: tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline load it, always as the checker, never as the thing measured or shipped.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+
+_lib = None
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int64)
+_up = ctypes.POINTER(ctypes.c_uint8)
+_llp = ctypes.POINTER(ctypes.c_longlong)
+
+
+def build(force=False):
+    """Compile liboracle.so with g++ (no -march flags: the same build runs on x86 and Arm)."""
+    src = os.path.join(HERE, "ddd_oracle.cpp")
+    hdr = os.path.join(HERE, "ddd_oracle.hpp")
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= max(
+            os.path.getmtime(src), os.path.getmtime(hdr)):
+        return LIB_PATH
+    import subprocess
+    tmp = LIB_PATH + ".tmp"
+    cmd = ["g++", "-std=c++20", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-o", tmp, src]
+    subprocess.check_call(cmd)
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        L.oracle_segseg_pair.argtypes = [_dp] * 8
+        L.oracle_segseg_pair_f32.argtypes = [_dp] * 8
+        L.oracle_segseg_ser.argtypes = [_dp, _dp, _dp, _ip, ctypes.c_int64, _up, ctypes.c_int64, _dp]
+        L.oracle_segseg_par_atomic.argtypes = [_dp, _dp, _dp, _ip, ctypes.c_int64, _up, ctypes.c_int64, _dp,
+                                               ctypes.c_int]
+        L.oracle_segseg_rows.argtypes = [_dp, _dp, _dp, _ip, ctypes.c_int64, _up, ctypes.c_int64, _ip,
+                                         ctypes.c_int64, _dp, ctypes.c_int]
+        L.oracle_segseg_idx.argtypes = [_dp, _dp, _dp, _ip, ctypes.c_int64, _up, ctypes.c_int64, _ip,
+                                        ctypes.c_int64, _dp, ctypes.c_int]
+        L.oracle_sigma_tilde.argtypes = [_dp, _dp, ctypes.c_int64, _dp, _dp, _ip, ctypes.c_int64, ctypes.c_int64,
+                                         _ip, ctypes.c_int64, _dp, ctypes.c_int]
+        L.oracle_opcount_pair.argtypes = [_dp] * 7 + [_llp, _dp]
+        L.oracle_opcount_sigma.argtypes = [_dp] * 5 + [_llp, _dp]
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+def _f64(a):
+    return np.require(a, np.float64, ["F", "A"])
+
+
+def _net_arrays(net):
+    coord = np.require(net.coord, np.float64, ["F"])
+    bvec = np.require(net.bVec, np.float64, ["F"])
+    seg = np.require(net.segIdx, np.int64, ["F"])
+    ext = np.require(net.extSeg, np.uint8, ["C"])
+    return coord, bvec, seg, ext, seg.shape[0]
+
+
+def pair(k5, b1, n11, n12, b2, n21, n22, f32=False):
+    """Fnode1..4 (4×3) of one pair."""
+    args = [np.ascontiguousarray(v, np.float64) for v in (k5, b1, n11, n12, b2, n21, n22)]
+    F = np.zeros(12)
+    fn = lib().oracle_segseg_pair_f32 if f32 else lib().oracle_segseg_pair
+    fn(*[_d(a) for a in args], _d(F))
+    return F.reshape(4, 3)
+
+
+def segseg_ser(k5, net):
+    """calcSegSegForceSer! into a fresh 3×2×numSeg array (Fortran order)."""
+    coord, bvec, seg, ext, ld = _net_arrays(net)
+    F = np.zeros((3, 2, net.numSeg), np.float64, order="F")
+    lib().oracle_segseg_ser(_d(np.ascontiguousarray(k5, np.float64)), _d(coord), _d(bvec), _i(seg), ld,
+                            ext.ctypes.data_as(_up), net.numSeg, _d(F))
+    return F
+
+
+def segseg_par_atomic(k5, net, nthreads):
+    coord, bvec, seg, ext, ld = _net_arrays(net)
+    F = np.zeros((3, 2, net.numSeg), np.float64, order="F")
+    lib().oracle_segseg_par_atomic(_d(np.ascontiguousarray(k5, np.float64)), _d(coord), _d(bvec), _i(seg), ld,
+                                   ext.ctypes.data_as(_up), net.numSeg, _d(F), int(nthreads))
+    return F
+
+
+def segseg_rows(k5, net, rows, nthreads=1):
+    """All-pairs result restricted to the given 0-based segment rows (3×2×len(rows))."""
+    coord, bvec, seg, ext, ld = _net_arrays(net)
+    rows = np.ascontiguousarray(rows, np.int64)
+    F = np.zeros((3, 2, len(rows)), np.float64, order="F")
+    lib().oracle_segseg_rows(_d(np.ascontiguousarray(k5, np.float64)), _d(coord), _d(bvec), _i(seg), ld,
+                             ext.ctypes.data_as(_up), net.numSeg, _i(rows), len(rows), _d(F), int(nthreads))
+    return F
+
+
+def segseg_idx(k5, net, idx, nthreads=1):
+    """Index-list form (idx 1-based) into a fresh 3×2×len(idx) array."""
+    coord, bvec, seg, ext, ld = _net_arrays(net)
+    idx = np.ascontiguousarray(idx, np.int64)
+    F = np.zeros((3, 2, len(idx)), np.float64, order="F")
+    lib().oracle_segseg_idx(_d(np.ascontiguousarray(k5, np.float64)), _d(coord), _d(bvec), _i(seg), ld,
+                            ext.ctypes.data_as(_up), net.numSeg, _i(idx), len(idx), _d(F), int(nthreads))
+    return F
+
+
+def sigma_tilde(k5, x0, net, idx=None, nthreads=1):
+    """σ̃ (6×M, Fortran order) at the points x0 (3×M)."""
+    coord, bvec, seg, ext, ld = _net_arrays(net)
+    x0 = np.require(x0, np.float64, ["F"])
+    M = x0.shape[1]
+    sig = np.zeros((6, M), np.float64, order="F")
+    if idx is None:
+        ip, n = None, 0
+    else:
+        idx = np.ascontiguousarray(idx, np.int64)
+        ip, n = _i(idx), len(idx)
+    lib().oracle_sigma_tilde(_d(np.ascontiguousarray(k5, np.float64)), _d(x0), M, _d(coord), _d(bvec), _i(seg), ld,
+                             net.numSeg, ip, n, _d(sig), int(nthreads))
+    return sig
+
+
+OPCOUNT_FIELDS = ("add", "mul", "div", "sqrt", "log", "atan", "cmp")
+
+
+def opcount_pair(k5, b1, n11, n12, b2, n21, n22):
+    args = [np.ascontiguousarray(v, np.float64) for v in (k5, b1, n11, n12, b2, n21, n22)]
+    c = np.zeros(7, np.int64)
+    F = np.zeros(12)
+    lib().oracle_opcount_pair(*[_d(a) for a in args], c.ctypes.data_as(_llp), _d(F))
+    return dict(zip(OPCOUNT_FIELDS, (int(v) for v in c)))
+
+
+def opcount_sigma(k5, b, n1, n2, x):
+    args = [np.ascontiguousarray(v, np.float64) for v in (k5, b, n1, n2, x)]
+    c = np.zeros(7, np.int64)
+    s = np.zeros(6)
+    lib().oracle_opcount_sigma(*[_d(a) for a in args], c.ctypes.data_as(_llp), _d(s))
+    return dict(zip(OPCOUNT_FIELDS, (int(v) for v in c)))

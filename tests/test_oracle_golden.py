@@ -1,0 +1,130 @@
+"""The CPU oracle against the reference's own golden vectors (CPU only).
+
+Goldens: test/SegmentForcesTest.jl:281-443 (seg-seg, three networks) and
+test/DislocationFEMTest.jl:5-155 (σ̃, edge and screw segment), extracted as
+text by tests/golden/extract_goldens.py.  The goldens are printed with 15
+decimals (absolute 5e-16 on values ~1e-3) and the networks are rebuilt here
+with libm's sin/cos instead of Julia's, so the bound is:
+  elementwise |Δ| <= 2e-14 and ||Δ|| / ||golden|| <= 1e-11
+(the reference test itself uses isapprox, rtol = sqrt(eps) ≈ 1.5e-8).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+ABS_TOL = 2e-14
+REL_TOL = 1e-11
+
+
+def _segseg_cases():
+    g = json.load(open(os.path.join(GOLDEN, "segseg_goldens.json")))
+    return g, [c["name"] for c in g["cases"]]
+
+
+G_SEG, SEG_NAMES = _segseg_cases()
+G_SIG = json.load(open(os.path.join(GOLDEN, "sigma_goldens.json")))
+
+
+def _seg_case(fixtures, name):
+    c = next(c for c in G_SEG["cases"] if c["name"] == name)
+    p = G_SEG["params"]
+    net = fixtures.make_network(c["loops"], G_SEG["slipSystems"], c["range"], c["shift"])
+    k5 = fixtures.consts5(p["coreRad"], p["mu"], p["nu"])
+    return c, net, k5
+
+
+def _close(ours, gold):
+    d = ours - gold
+    assert np.abs(d).max() <= ABS_TOL, np.abs(d).max()
+    assert np.linalg.norm(d) <= REL_TOL * np.linalg.norm(gold), np.linalg.norm(d) / np.linalg.norm(gold)
+
+
+@pytest.mark.parametrize("name", SEG_NAMES)
+def test_segseg_serial_matches_golden(oracle, fixtures, name):
+    c, net, k5 = _seg_case(fixtures, name)
+    F = oracle.segseg_ser(k5, net)
+    _close(F[:, 0, :].T, np.array(c["f1"]))
+    _close(F[:, 1, :].T, np.array(c["f2"]))
+
+
+@pytest.mark.parametrize("name", SEG_NAMES)
+def test_segseg_threaded_matches_golden(oracle, fixtures, name):
+    """calcSegSegForcePar restatement (contiguous i-chunks, atomic adds)."""
+    c, net, k5 = _seg_case(fixtures, name)
+    for nt in (1, 3, 4):
+        F = oracle.segseg_par_atomic(k5, net, nt)
+        _close(F[:, 0, :].T, np.array(c["f1"]))
+        _close(F[:, 1, :].T, np.array(c["f2"]))
+
+
+@pytest.mark.parametrize("name", SEG_NAMES)
+def test_segseg_rows_equal_serial_bitwise(oracle, fixtures, name):
+    """The sampled-row form adds each segment's contributions in Ser's order."""
+    _, net, k5 = _seg_case(fixtures, name)
+    F = oracle.segseg_ser(k5, net)
+    rows = np.arange(net.numSeg)
+    R = oracle.segseg_rows(k5, net, rows, 2)
+    assert np.array_equal(F, R)
+
+
+def test_segseg_idx_form_matches_all_pairs(oracle, fixtures):
+    """SegmentForcesTest.jl:372-380: the idx form equals the all-pairs columns."""
+    _, net, k5 = _seg_case(fixtures, "pentagons_shifted")
+    F = oracle.segseg_ser(k5, net)
+    rng = np.random.default_rng(3)
+    idx = rng.integers(1, net.numSeg + 1, net.numSeg // 2)
+    Fi = oracle.segseg_idx(k5, net, idx)
+    # The idx form evaluates every pair with segment i first, the all-pairs
+    # form with the lower index first: same forces up to rounding.
+    d = Fi - F[:, :, idx - 1]
+    assert np.linalg.norm(d) <= 1e-10 * np.linalg.norm(Fi)
+
+
+def test_segseg_ext_segments_skipped(oracle, fixtures):
+    _, net, k5 = _seg_case(fixtures, "hexagons_prism_shear")
+    net.extSeg[[2, 7]] = 1
+    F = oracle.segseg_ser(k5, net)
+    assert np.all(F[:, :, [2, 7]] == 0)
+    keep = [i for i in range(net.numSeg) if i not in (2, 7)]
+    # Equivalent to dropping the two segments from the network.
+    from oracle.fixtures import Network
+    sub = Network(net.coord, net.bVec[:, keep], np.c_[np.arange(1, len(keep) + 1), net.segIdx[keep, 1:]],
+                  np.zeros(len(keep), np.uint8), len(keep))
+    np.testing.assert_allclose(F[:, :, keep], oracle.segseg_ser(k5, sub), rtol=1e-12, atol=1e-18)
+
+
+@pytest.mark.parametrize("case", [c["name"] for c in G_SIG["cases"]])
+def test_sigma_tilde_matches_golden(oracle, fixtures, case):
+    c = next(c for c in G_SIG["cases"] if c["name"] == case)
+    net, pts = fixtures.sigma_case_network(c)
+    k5 = fixtures.consts5(c["coreRad"], c["mu"], c["nu"])
+    sig = oracle.sigma_tilde(k5, pts, net)
+    gold = np.array(c["golden"])
+    ours = sig.T[:, [0, 1, 2, 3, 5, 4]]  # golden columns are (xx, yy, zz, xy, yz, xz)
+    _close(ours, gold)
+
+
+def test_sigma_threaded_bitwise_equal(oracle, fixtures):
+    c = G_SIG["cases"][0]
+    net, _ = fixtures.sigma_case_network(c)
+    k5 = fixtures.consts5(c["coreRad"], c["mu"], c["nu"])
+    rng = np.random.default_rng(0)
+    pts = np.asfortranarray(rng.uniform(-400, 400, (3, 500)))
+    assert np.array_equal(oracle.sigma_tilde(k5, pts, net, nthreads=1), oracle.sigma_tilde(k5, pts, net, nthreads=4))
+
+
+def test_opcount_constants(oracle, fixtures):
+    """Algorithmic work per unit, from the op-counting instantiation."""
+    k5 = fixtures.consts5(1.0, 1.0, 0.28)
+    rng = np.random.default_rng(1)
+    a = [rng.normal(size=3) * 100 for _ in range(6)]
+    c = oracle.opcount_pair(k5, *a)
+    flops = c["add"] + c["mul"] + c["div"] + c["sqrt"] + c["log"] + c["atan"]
+    assert c["log"] == 8 and c["atan"] == 4 and c["sqrt"] == 10
+    assert 1000 < flops < 2000
+    s = oracle.opcount_sigma(k5, a[0], a[1], a[2], a[3])
+    assert s["sqrt"] == 2 and s["div"] == 3

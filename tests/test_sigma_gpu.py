@@ -1,0 +1,133 @@
+"""Field-point stress σ̃ on the GPU (through the C ABI) against the oracle and goldens.
+
+Tolerance: each point's six components are sums over segments in the same
+order as the oracle; per point |Δσ| <= 1e-10 |σ| + 1e-12 max|σ| (Frobenius
+norms of the 6-vectors), and the golden cases as in the oracle's test.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, k5_of
+
+pytestmark = pytest.mark.gpu
+
+G_SIG = json.load(open(os.path.join(GOLDEN, "sigma_goldens.json")))
+
+
+def assert_sigma_close(S, ref, rel=1e-10, floor=1e-12, smax=None):
+    """smax: the largest point stress of the whole field (default: of ref)."""
+    d = np.linalg.norm(S - ref, axis=0)
+    n = np.linalg.norm(ref, axis=0)
+    assert np.all(d <= rel * n + floor * (n.max() if smax is None else smax)), np.max(d / (n + 1e-300))
+
+
+def _fem_net(pkg, c):
+    coord = np.array(c["coord"], dtype=np.float64).T
+    nseg = len(c["links"])
+    bvec = np.tile(np.array(c["b"], dtype=np.float64)[:, None], (1, nseg))
+    seg = np.array([[i + 1, l[0], l[1]] for i, l in enumerate(c["links"])], dtype=np.int64)
+    return pkg.DislocationNetwork(coord, bvec, seg)
+
+
+@pytest.mark.parametrize("case", [c["name"] for c in G_SIG["cases"]])
+def test_golden(pkg, fixtures, case):
+    c = next(c for c in G_SIG["cases"] if c["name"] == case)
+    net = _fem_net(pkg, c)
+    _, pts = fixtures.sigma_case_network(c)
+    dln = pkg.DislocationParameters(coreRad=c["coreRad"])
+    mat = pkg.MaterialParameters(mu=c["mu"], nu=c["nu"])
+    S = pkg.calc_σTilde(pts, dln, mat, net)
+    ours = S.T[:, [0, 1, 2, 3, 5, 4]]
+    gold = np.array(c["golden"])
+    d = ours - gold
+    assert np.abs(d).max() <= 5e-14
+    assert np.linalg.norm(d) <= 1e-11 * np.linalg.norm(gold)
+    # calc_σTilde! gives the identical array (DislocationFEMTest.jl:76-78).
+    sig = np.full((6, pts.shape[1]), 7.0, order="F")
+    pkg.calc_σTilde_inplace(sig, pts, dln, mat, net)
+    assert np.array_equal(sig, S)
+
+
+@pytest.mark.parametrize("b", [[0.0, 0.0, 1.0], [1.0, 0.0, 0.0]])
+def test_line_of_49_segments(pkg, oracle, b):
+    """DislocationFEMTest.jl:157-268: 49 collinear segments, 51 x 51 points in z = 0."""
+    r = np.linspace(-300, 300, 51)
+    coord = np.asfortranarray(np.stack([np.zeros(51), np.zeros(51), r]))
+    bvec = np.tile(np.array(b)[:, None], (1, 49))
+    seg = np.array([[i + 1, i + 1, i + 2] for i in range(49)], dtype=np.int64)
+    net = pkg.DislocationNetwork(coord, bvec, seg)
+    pts = np.asfortranarray(np.array([[x, y, 0.0] for x in r for y in r]).T)
+    dln = pkg.DislocationParameters(coreRad=5.0)
+    mat = pkg.MaterialParameters(mu=1.0, nu=0.28)
+    S = pkg.calc_σTilde(pts, dln, mat, net)
+    sig = np.zeros((6, pts.shape[1]), order="F")
+    pkg.calc_σTilde_inplace(sig, pts, dln, mat, net)
+    assert np.array_equal(sig, S)
+    assert_sigma_close(S, oracle.sigma_tilde(k5_of(dln, mat), pts, net))
+
+
+@pytest.mark.parametrize("num_loops,npts", [(1, 1), (8, 100), (40, 1000), (64, 4096)])
+def test_random_vs_oracle(pkg, synth, oracle, num_loops, npts):
+    p, b = synth.square_loops(num_loops, num_loops, 50.0, 200.0, 2000.0, 0.5, 0.1)
+    coord, bvec, seg = synth.network_arrays(p, b)
+    net = pkg.DislocationNetwork(coord, bvec, seg)
+    net.extSeg[::7] = 1  # σ̃ ignores extSeg
+    rng = np.random.default_rng(npts)
+    pts = np.asfortranarray(rng.uniform(0, 2000.0, (3, npts)))
+    dln = pkg.DislocationParameters(coreRad=1.0)
+    mat = pkg.MaterialParameters(mu=1.0, nu=0.28)
+    S = pkg.calc_σTilde(pts, dln, mat, net)
+    ref = oracle.sigma_tilde(k5_of(dln, mat), pts, net)
+    if npts == 1:
+        assert S.shape == (6,)
+        S = S[:, None]
+    assert_sigma_close(S, ref)
+
+
+def test_idx_selection(pkg, synth, oracle):
+    p, b = synth.square_loops(30, 5, 50.0, 200.0, 2000.0, 0.5, 0.0)
+    coord, bvec, seg = synth.network_arrays(p, b)
+    net = pkg.DislocationNetwork(coord, bvec, seg)
+    rng = np.random.default_rng(2)
+    idx = rng.integers(1, net.numSeg + 1, 70)
+    pts = np.asfortranarray(rng.uniform(0, 2000.0, (3, 333)))
+    dln = pkg.DislocationParameters(coreRad=1.0)
+    mat = pkg.MaterialParameters(mu=1.0, nu=0.28)
+    S = pkg.calc_σTilde(pts, dln, mat, net, idx)
+    assert_sigma_close(S, oracle.sigma_tilde(k5_of(dln, mat), pts, net, idx=idx))
+
+
+def test_grid_32k_sampled(pkg, synth, oracle):
+    """σ̃ of 32,768 segments on 4096 grid points; 64 points against the oracle."""
+    p, b, cfg = synth.make("gpu32k", seed=4)
+    coord, bvec, seg = synth.network_arrays(p, b)
+    net = pkg.DislocationNetwork(coord, bvec, seg)
+    pts = synth.grid_points(16, cfg["cube"])
+    dln = pkg.DislocationParameters(coreRad=1.0)
+    mat = pkg.MaterialParameters(mu=1.0, nu=0.28)
+    S = pkg.calc_σTilde(pts, dln, mat, net)
+    pick = np.random.default_rng(0).choice(pts.shape[1], 64, replace=False)
+    ref = oracle.sigma_tilde(k5_of(dln, mat), np.asfortranarray(pts[:, pick]), net, nthreads=os.cpu_count() or 1)
+    assert_sigma_close(S[:, pick], ref, smax=np.linalg.norm(S, axis=0).max())
+
+
+def test_device_form(pkg, synth):
+    torch = pytest.importorskip("torch")
+    p, b = synth.square_loops(20, 9, 50.0, 200.0, 2000.0, 0.5, 0.0)
+    coord, bvec, seg = synth.network_arrays(p, b)
+    net = pkg.DislocationNetwork(coord, bvec, seg)
+    pts = synth.grid_points(8, 2000.0)
+    dln = pkg.DislocationParameters(coreRad=1.0)
+    mat = pkg.MaterialParameters(mu=1.0, nu=0.28)
+    host = pkg.calc_σTilde(pts, dln, mat, net)
+    soa = torch.from_numpy(synth.packed_soa(p, b)).cuda()
+    x0 = torch.from_numpy(np.ascontiguousarray(pts.T)).cuda()  # point-major = 3×M column-major
+    out = torch.zeros(6 * pts.shape[1], dtype=torch.float64, device="cuda")
+    pkg.get_context().sigma_tilde_device(pkg.consts_of(dln, mat), x0.data_ptr(), pts.shape[1], soa.data_ptr(),
+                                         soa.shape[1], net.numSeg, out.data_ptr(),
+                                         stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy().reshape(6, -1, order="F"), host)
