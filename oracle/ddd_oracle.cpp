@@ -327,3 +327,41 @@ void oracle_opcount_sigma(const double* k5, const double* b, const double* n1, c
   for (int k = 0; k < 6; ++k) sig6[k] = sig[k].v;
 }
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Extended-precision all-pairs (long double), to measure the rounding noise of
+// the Float64 algorithm itself: |F_f64 - F_ld| is the reference's own error.
+// rows (0-based, may be NULL = all) selects the segments returned; F is 3×2×nRows.
+extern "C" void oracle_segseg_ser_ld(const double* k5, const double* coord, const double* bVec, const int64_t* segIdx,
+                                     int64_t ld, const uint8_t* extSeg, int64_t numSeg, const int64_t* rows,
+                                     int64_t nRows, double* F, int nthreads) {
+  typedef long double L;
+  Consts<L> K;
+  K.aSq = k5[0];
+  K.mu4pi = k5[1];
+  K.mu8pi = k5[2];
+  K.mu4pinu = k5[3];
+  K.nuMu4pinu = k5[4];
+  K.mu8piaSq = (L)k5[0] * (L)k5[2];
+  K.mu4pinuaSq = (L)k5[0] * (L)k5[3];
+  std::vector<Seg> s = gather(coord, bVec, segIdx, ld, numSeg);
+  auto cv = [](const V3<double>& v) { return V3<L>{(L)v.x, (L)v.y, (L)v.z}; };
+  const int64_t nOut = rows ? nRows : numSeg;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+  for (int64_t r = 0; r < nOut; ++r) {
+    const int64_t i = rows ? rows[r] : r;
+    L acc[6] = {0, 0, 0, 0, 0, 0};
+    if (!extSeg[i]) {
+      V3<L> out[4];
+      for (int64_t j = 0; j < numSeg; ++j) {
+        if (j == i || extSeg[j]) continue;
+        const int64_t a = i < j ? i : j, b = i < j ? j : i;
+        seg_seg_force<L>(K, cv(s[a].b), cv(s[a].n1), cv(s[a].n2), cv(s[b].b), cv(s[b].n1), cv(s[b].n2), out);
+        const V3<L>* q = (i < j) ? out : out + 2;
+        acc[0] += q[0].x; acc[1] += q[0].y; acc[2] += q[0].z;
+        acc[3] += q[1].x; acc[4] += q[1].y; acc[5] += q[1].z;
+      }
+    }
+    for (int c = 0; c < 6; ++c) F[6 * r + c] = (double)acc[c];
+  }
+}

@@ -51,6 +51,8 @@ def lib():
                                         ctypes.c_int64, _dp, ctypes.c_int]
         L.oracle_sigma_tilde.argtypes = [_dp, _dp, ctypes.c_int64, _dp, _dp, _ip, ctypes.c_int64, ctypes.c_int64,
                                          _ip, ctypes.c_int64, _dp, ctypes.c_int]
+        L.oracle_segseg_ser_ld.argtypes = [_dp, _dp, _dp, _ip, ctypes.c_int64, _up, ctypes.c_int64, _ip,
+                                           ctypes.c_int64, _dp, ctypes.c_int]
         L.oracle_opcount_pair.argtypes = [_dp] * 7 + [_llp, _dp]
         L.oracle_opcount_sigma.argtypes = [_dp] * 5 + [_llp, _dp]
         _lib = L
@@ -92,6 +94,21 @@ def segseg_ser(k5, net):
     F = np.zeros((3, 2, net.numSeg), np.float64, order="F")
     lib().oracle_segseg_ser(_d(np.ascontiguousarray(k5, np.float64)), _d(coord), _d(bvec), _i(seg), ld,
                             ext.ctypes.data_as(_up), net.numSeg, _d(F))
+    return F
+
+
+def segseg_ser_ld(k5, net, rows=None, nthreads=1):
+    """All-pairs forces with every operation in long double (rounded to double at
+    the end), for all segments or the given 0-based rows.  Its distance from the
+    Float64 result is the rounding error of the reference's own arithmetic."""
+    coord, bvec, seg, ext, ld = _net_arrays(net)
+    if rows is not None:
+        rows = np.ascontiguousarray(rows, np.int64)
+    n = net.numSeg if rows is None else len(rows)
+    F = np.zeros((3, 2, n), np.float64, order="F")
+    lib().oracle_segseg_ser_ld(_d(np.ascontiguousarray(k5, np.float64)), _d(coord), _d(bvec), _i(seg), ld,
+                               ext.ctypes.data_as(_up), net.numSeg, None if rows is None else _i(rows),
+                               0 if rows is None else len(rows), _d(F), int(nthreads))
     return F
 
 

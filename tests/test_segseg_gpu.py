@@ -2,11 +2,18 @@
 
 Tolerances (FP64 path):
   * golden networks: |Δ| <= 5e-14 elementwise and ||Δ|| <= 1e-11 ||golden||
-    (the oracle meets 2e-14 / 1e-11; the kernel adds FMA contraction);
-  * against the oracle: ||Δ|| <= 1e-10 ||F|| over the whole array, and per node
-    force vector |ΔF_n| <= 1e-10 |F_n| + 1e-12 max_n |F_n| — node forces are
-    sums of O(N) contributions that cancel (closed loops), so the absolute
-    floor is set by the largest force in the network, not by the node itself.
+    (the oracle meets 2e-14 / 1e-11; the kernel adds FMA contraction).
+  * against the oracle, per node force vector:
+        |F_gpu - F_ref| <= 1e-10 |F_ref| + 4 * noise
+    where noise = max over nodes of |F_ref - F_ext|, F_ext being the same
+    algorithm evaluated in long double: the worst rounding error of the
+    reference's own Float64 arithmetic on this network.  Node forces are sums of
+    O(N) contributions that cancel (closed loops), so a node whose force is small
+    carries an absolute error set by the large terms, and two correct Float64
+    evaluations differ by about that much (up to ~3e-10 relative, measured).
+    Over the whole array ||ΔF|| <= 1e-10 ||F||.
+  * accuracy: max over nodes of |F_gpu - F_ext| <= 3 * noise: the kernel is as
+    accurate as the reference's arithmetic.
 """
 import json
 import os
@@ -37,17 +44,31 @@ def _synthetic(pkg, synth, num_loops, seed, config="gpu32k", parallel_fraction=N
     return pkg.DislocationNetwork(coord, bvec, seg)
 
 
-def assert_forces_close(F, ref, rel=1e-10, floor=1e-12, fmax=None):
-    """fmax: the largest node force of the whole network (default: of ref)."""
-    assert F.shape == ref.shape
-    d = F - ref
-    scale = np.linalg.norm(ref)
-    assert np.linalg.norm(d) <= rel * scale + 1e-300, np.linalg.norm(d) / scale
-    dn = np.linalg.norm(d, axis=0)
-    fn = np.linalg.norm(ref, axis=0)
-    bound = rel * fn + floor * (fn.max() if fmax is None else fmax)
-    worst = np.max(dn - bound)
-    assert worst <= 0, "node-force error exceeds bound by %g (max rel %g)" % (worst, np.max(dn / (fn + 1e-300)))
+def check_forces(F, oracle, k5, net, rows=None, ref=None):
+    """F: GPU forces of all segments (or of the 0-based `rows`); ref: the oracle's
+    Float64 forces for the same columns (computed here when None)."""
+    nt = os.cpu_count() or 1
+    if ref is None:
+        ref = oracle.segseg_ser(k5, net) if rows is None else oracle.segseg_rows(k5, net, rows, nt)
+    ext = oracle.segseg_ser_ld(k5, net, rows, nthreads=nt)
+    assert F.shape == ref.shape == ext.shape
+    norm = lambda a: np.linalg.norm(a, axis=0)
+    # A few ulps of the largest force: the floor for tiny networks whose noise is 0.
+    ulps = 4 * np.finfo(np.float64).eps * norm(ext).max()
+    noise = norm(ref - ext).max()
+    d = norm(F - ref)
+    gpu_err = norm(F - ext).max()
+    if os.environ.get("DDD_TEST_STATS"):
+        with open(os.environ["DDD_TEST_STATS"], "a") as fh:
+            fh.write("%s n=%d noise=%.3e gpu_err=%.3e max_rel_diff=%.3e\n" % (
+                os.environ.get("PYTEST_CURRENT_TEST", "?"), F.shape[2], noise, gpu_err,
+                np.max(d / (norm(ref) + 1e-300))))
+    assert np.linalg.norm(F - ref) <= 1e-10 * np.linalg.norm(ref) + ulps
+    excess = np.max(d - (1e-10 * norm(ref) + 4 * noise + ulps))
+    assert excess <= 0, "node-force difference exceeds bound by %g (noise %g, max rel %g)" % (
+        excess, noise, np.max(d / (norm(ref) + 1e-300)))
+    assert gpu_err <= 3 * noise + ulps, "kernel error %g vs reference arithmetic %g" % (gpu_err, noise)
+    return noise, gpu_err
 
 
 @pytest.mark.parametrize("name", [c["name"] for c in G_SEG["cases"]])
@@ -63,7 +84,7 @@ def test_golden_networks(pkg, fixtures, oracle, name):
         d = F[:, node, :].T - gold
         assert np.abs(d).max() <= 5e-14, np.abs(d).max()
         assert np.linalg.norm(d) <= 1e-11 * np.linalg.norm(gold)
-    assert_forces_close(F, oracle.segseg_ser(k5_of(dln, mat), net))
+    check_forces(F, oracle, k5_of(dln, mat), net)
     rep = pkg.get_context().last_report
     n = net.numSeg
     assert rep["pairs_general"] + rep["pairs_parallel"] == n * (n - 1) // 2
@@ -76,7 +97,7 @@ def test_random_networks_vs_oracle(pkg, synth, oracle, num_loops, seed):
     net = _synthetic(pkg, synth, num_loops, seed, cube=3000.0)
     dln, mat = _params(pkg)
     F = pkg.calcSegSegForce(dln, mat, net)
-    assert_forces_close(F, oracle.segseg_ser(k5_of(dln, mat), net))
+    check_forces(F, oracle, k5_of(dln, mat), net)
 
 
 @pytest.mark.parametrize("n", [1, 2, 3, 127, 129, 255, 257])
@@ -86,11 +107,10 @@ def test_ragged_sizes(pkg, synth, oracle, n):
     net.numSeg = n
     dln, mat = _params(pkg)
     F = pkg.calcSegSegForce(dln, mat, net)
-    ref = oracle.segseg_ser(k5_of(dln, mat), net)
     if n == 1:
         assert np.all(F == 0)
     else:
-        assert_forces_close(F, ref)
+        check_forces(F, oracle, k5_of(dln, mat), net)
 
 
 def test_empty_network(pkg, synth):
@@ -108,7 +128,7 @@ def test_near_parallel_heavy(pkg, synth, oracle):
     F = pkg.calcSegSegForce(dln, mat, net)
     rep = pkg.get_context().last_report
     assert rep["pairs_parallel"] > 0.05 * (rep["pairs_parallel"] + rep["pairs_general"])
-    assert_forces_close(F, oracle.segseg_ser(k5_of(dln, mat), net))
+    check_forces(F, oracle, k5_of(dln, mat), net)
 
 
 def test_external_segments(pkg, synth, oracle):
@@ -118,7 +138,7 @@ def test_external_segments(pkg, synth, oracle):
     dln, mat = _params(pkg)
     F = pkg.calcSegSegForce(dln, mat, net)
     assert np.all(F[:, :, net.extSeg[:net.numSeg] == 1] == 0)
-    assert_forces_close(F, oracle.segseg_ser(k5_of(dln, mat), net))
+    check_forces(F, oracle, k5_of(dln, mat), net)
 
 
 def test_deterministic(pkg, synth):
@@ -139,14 +159,13 @@ def test_idx_form(pkg, synth, oracle):
     idx = rng.integers(1, net.numSeg + 1, net.numSeg // 2)
     idx[:3] = [4, 4, 101]  # a repeated index and external segments
     Fi = pkg.calcSegSegForce(dln, mat, net, idx)
-    ref = oracle.segseg_idx(k5, net, idx)
     assert np.all(Fi[:, :, 2] == 0)
-    assert_forces_close(Fi, ref)
+    check_forces(Fi, oracle, k5, net, rows=idx - 1, ref=oracle.segseg_idx(k5, net, idx))
     Fall = pkg.calcSegSegForce(dln, mat, net)
     assert np.linalg.norm(Fi - Fall[:, :, idx - 1]) <= 1e-10 * np.linalg.norm(Fall[:, :, idx - 1])
     one = pkg.calcSegSegForce(dln, mat, net, 17)
     assert one.shape == (3, 2, 1)
-    assert_forces_close(one, oracle.segseg_idx(k5, net, [17]))
+    check_forces(one, oracle, k5, net, rows=[16], ref=oracle.segseg_idx(k5, net, [17]))
 
 
 def test_inplace_forms(pkg, synth, oracle):
@@ -180,8 +199,7 @@ def test_large_sampled_rows(pkg, synth, oracle):
     assert rep["pairs_general"] + rep["pairs_parallel"] == n * (n - 1) // 2
     rng = np.random.default_rng(9)
     rows = np.sort(rng.choice(n, 24, replace=False))
-    ref = oracle.segseg_rows(k5_of(dln, mat), net, rows, nthreads=os.cpu_count() or 1)
-    assert_forces_close(F[:, :, rows], ref, fmax=np.linalg.norm(F, axis=0).max())
+    check_forces(F[:, :, rows], oracle, k5_of(dln, mat), net, rows=rows)
 
 
 def test_errors(pkg, synth):
