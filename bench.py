@@ -175,6 +175,7 @@ def main():
     ap.add_argument("--cpu-target-s", type=float, default=15.0)
     ap.add_argument("--ref-step-s", type=float, default=4.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-variants", action="store_true")
     args = ap.parse_args()
 
     import __graft_entry__ as graft
@@ -243,6 +244,31 @@ def main():
     ms_step = t_rank.item() / args.steps
     value = ws * pairs / (ms_step * 1e-3)
 
+    # The FMA variant of the same kernel, for comparison (same workload, same timing).
+    variants = {}
+    if not args.no_variants:
+        ctx.mode = "fp64_fma"
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            ctx.segseg_force_device(k, soa.data_ptr(), n, n, force.data_ptr(), stream=sptr)
+            torch.cuda.synchronize()
+            vms = []
+            for s_ in range(max(1, min(args.steps, 2))):
+                flush.zero_()
+                a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a_.record(stream)
+                ctx.segseg_force_device(k, soa.data_ptr(), n, n, force.data_ptr(), stream=sptr)
+                b_.record(stream)
+                torch.cuda.synchronize()
+                vms.append(a_.elapsed_time(b_))
+        ctx.mode = "fp64"
+        variants["fp64_fma"] = {"value": pairs / (statistics.mean(vms) * 1e-3), "unit": "pair-interactions/s",
+                                "ms_per_step": statistics.mean(vms),
+                                "frac_fp64_peak": flops_per_step / (statistics.mean(vms) * 1e-3) / fp64_peak}
+        with torch.cuda.stream(stream):
+            ctx.segseg_force_device(k, soa.data_ptr(), n, n, force.data_ptr(), stream=sptr)
+            torch.cuda.synchronize()
+
     # End to end through the reference-facing C-ABI call with host arrays.
     coord, bvec, seg = synth.network_arrays(p, b)
     net = pkg.DislocationNetwork(coord, bvec, seg)
@@ -283,6 +309,8 @@ def main():
         "e2e": {"value": e2e_value, "unit": "pair-interactions/s", "h2d_bytes_per_step": erep["h2d_bytes"],
                 "d2h_bytes_per_step": erep["d2h_bytes"], "steps": e2e_steps, "matches_device_path": same},
         "gpu_launches": 3 * args.steps,
+        "mode": "fp64 (strict: every multiply and add rounded separately, as the reference)",
+        "variants": variants,
         "kernel_ms_per_step": statistics.mean(ms_kernel),
     }
     cs = clocks.summary()

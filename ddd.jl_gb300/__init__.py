@@ -29,8 +29,12 @@ DDD_OK, DDD_EINVAL, DDD_ERANGE, DDD_ENONFINITE, DDD_EDEVICE, DDD_ENOMEM = 0, -1,
 EXPORTED_SYMBOLS = (
     "ddd_create", "ddd_destroy", "ddd_last_error", "ddd_version",
     "ddd_segseg_force", "ddd_segseg_force_inplace", "ddd_sigma_tilde",
-    "ddd_segseg_force_device", "ddd_sigma_tilde_device", "ddd_probe_fma_peak",
+    "ddd_segseg_force_device", "ddd_sigma_tilde_device", "ddd_set_mode", "ddd_get_mode", "ddd_probe_fma_peak",
 )
+
+# Arithmetic modes (ddd_set_mode).
+MODE_FP64, MODE_FP64_FMA = 0, 1
+MODES = {"fp64": MODE_FP64, "fp64_fma": MODE_FP64_FMA}
 
 
 class DDDError(RuntimeError):
@@ -93,6 +97,8 @@ def library():
         L.ddd_sigma_tilde.argtypes = [_vp, cp, _dp, _i64, _dp, _i64, _dp, _i64, _ip, _i64, _i64, _ip, _i64, _dp, rp]
         L.ddd_segseg_force_device.argtypes = [_vp, cp, _vp, _i64, _vp, _i64, _vp, _vp, rp]
         L.ddd_sigma_tilde_device.argtypes = [_vp, cp, _vp, _i64, _vp, _i64, _i64, _vp, _vp, rp]
+        L.ddd_set_mode.argtypes = [_vp, ctypes.c_int]
+        L.ddd_get_mode.argtypes = [_vp]
         L.ddd_probe_fma_peak.argtypes = [_vp, ctypes.c_int, _dp]
         _lib = L
     return _lib
@@ -288,6 +294,14 @@ class Context:
                                             stream, ctypes.byref(rep) if report else None)
         self._check(rc)
         return rep.as_dict() if report else None
+
+    @property
+    def mode(self):
+        return self._L.ddd_get_mode(self._h)
+
+    @mode.setter
+    def mode(self, m):
+        self._check(self._L.ddd_set_mode(self._h, MODES.get(m, m) if isinstance(m, str) else int(m)))
 
     def probe_fma_peak(self, precision=64):
         v = ctypes.c_double(0)

@@ -18,8 +18,26 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 
 
+# Translation units compiled more than once: (object suffix, extra flags).
+VARIANTS = {
+    "segseg_f64.cu": [("strict", ["-DDDD_VARIANT=strict", "--fmad=false"]), ("fast", ["-DDDD_VARIANT=fast"])],
+    "sigma_f64.cu": [("strict", ["-DDDD_VARIANT=strict", "--fmad=false"]), ("fast", ["-DDDD_VARIANT=fast"])],
+}
+
+
 def sources():
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+
+
+def units():
+    """(source, object, extra flags) for every object of the library."""
+    out = []
+    for src in sources():
+        base = os.path.basename(src)[:-3]
+        for suffix, flags in VARIANTS.get(os.path.basename(src), [("", [])]):
+            obj = os.path.join(BUILD, base + ("_" + suffix if suffix else "") + ".o")
+            out.append((src, obj, flags))
+    return out
 
 
 def _headers():
@@ -35,8 +53,7 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def _compile(src, extra, verbose):
-    obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+def _compile(src, obj, extra, verbose):
     if not _stale(obj, [src] + _headers() + [__file__]):
         return obj, ""
     cmd = [NVCC] + ARCH + FLAGS + extra + ["-c", src, "-o", obj]
@@ -49,9 +66,9 @@ def _compile(src, extra, verbose):
 def build(verbose=False, ptxas_info=False):
     os.makedirs(BUILD, exist_ok=True)
     extra = ["-Xptxas", "-v"] if ptxas_info else []
-    srcs = sources()
-    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
-        results = list(ex.map(lambda s: _compile(s, extra, verbose or ptxas_info), srcs))
+    us = units()
+    with cf.ThreadPoolExecutor(max_workers=min(8, len(us))) as ex:
+        results = list(ex.map(lambda u: _compile(u[0], u[1], u[2] + extra, verbose or ptxas_info), us))
     objs = [o for o, _ in results]
     logs = "".join(l for _, l in results)
     if _stale(LIB, objs):

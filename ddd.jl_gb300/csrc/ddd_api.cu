@@ -47,6 +47,7 @@ struct DevBuf {
 
 struct ddd_ctx {
   int device = 0;
+  int mode = DDD_MODE_FP64;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   std::mutex mu;
@@ -72,6 +73,31 @@ int cuda_fail(ddd_ctx* c, cudaError_t e, const char* where) {
     cudaError_t _e = (call);                         \
     if (_e != cudaSuccess) return cuda_fail(ctx, _e, where); \
   } while (0)
+
+// FP64 kernel variant of the context's mode.  Segment preparation (direction
+// and inverse length) always uses the strict build, so t and 1/|l| are the
+// reference's values in both modes.
+bool use_fma(const ddd_ctx* c) { return c->mode == DDD_MODE_FP64_FMA; }
+
+cudaError_t run_segseg_all(const ddd_ctx* c, const ddd::KConsts& K, const double* soa, const uint8_t* skip,
+                           int64_t npad, double* partial, double* out, int64_t numSeg, unsigned long long* cnt,
+                           cudaStream_t st) {
+  return use_fma(c) ? ddd::fast::launch_segseg_all_f64(K, soa, skip, npad, partial, out, numSeg, cnt, st)
+                    : ddd::strict::launch_segseg_all_f64(K, soa, skip, npad, partial, out, numSeg, cnt, st);
+}
+
+cudaError_t run_segseg_rows(const ddd_ctx* c, const ddd::KConsts& K, const double* soa, const uint8_t* skip,
+                            int64_t npad, const int64_t* rows, int64_t nRows, double* partial, double* out,
+                            unsigned long long* cnt, cudaStream_t st) {
+  return use_fma(c) ? ddd::fast::launch_segseg_rows_f64(K, soa, skip, npad, rows, nRows, partial, out, cnt, st)
+                    : ddd::strict::launch_segseg_rows_f64(K, soa, skip, npad, rows, nRows, partial, out, cnt, st);
+}
+
+cudaError_t run_sigma(const ddd_ctx* c, const ddd::KConsts& K, const double* soa, int64_t npad, int64_t nSeg,
+                      const double* x0, int64_t M, double* sigma, cudaStream_t st) {
+  return use_fma(c) ? ddd::fast::launch_sigma_f64(K, soa, npad, nSeg, x0, M, sigma, st)
+                    : ddd::strict::launch_sigma_f64(K, soa, npad, nSeg, x0, M, sigma, st);
+}
 
 bool finite3(const double* p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
 
@@ -139,21 +165,21 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
 int upload_network(ddd_ctx* ctx, const double* coord, int64_t coordCols, const double* bVec, int64_t bVecCols,
                    const int64_t* segIdx, int64_t ld, const uint8_t* extSeg, int64_t numSeg, int64_t& npad,
                    int64_t& h2d) {
-  npad = ddd::segseg_npad(numSeg);
+  npad = ddd::strict::segseg_npad(numSeg);
   const size_t cB = (size_t)coordCols * 3 * sizeof(double), bB = (size_t)bVecCols * 3 * sizeof(double);
   const size_t sB = (size_t)ld * 3 * sizeof(int64_t), eB = extSeg ? (size_t)numSeg : 0;
   CK(ctx->coord.ensure(cB), "alloc coord");
   CK(ctx->bvec.ensure(bB), "alloc bVec");
   CK(ctx->segidx.ensure(sB), "alloc segIdx");
   if (eB) CK(ctx->ext.ensure(eB), "alloc extSeg");
-  CK(ctx->soa.ensure(ddd::segseg_soa_bytes(npad)), "alloc segment SoA");
+  CK(ctx->soa.ensure(ddd::strict::segseg_soa_bytes(npad)), "alloc segment SoA");
   CK(ctx->skip.ensure((size_t)npad), "alloc skip flags");
   CK(cudaMemcpyAsync(ctx->coord.p, coord, cB, cudaMemcpyHostToDevice, ctx->stream), "copy coord");
   CK(cudaMemcpyAsync(ctx->bvec.p, bVec, bB, cudaMemcpyHostToDevice, ctx->stream), "copy bVec");
   CK(cudaMemcpyAsync(ctx->segidx.p, segIdx, sB, cudaMemcpyHostToDevice, ctx->stream), "copy segIdx");
   if (eB) CK(cudaMemcpyAsync(ctx->ext.p, extSeg, eB, cudaMemcpyHostToDevice, ctx->stream), "copy extSeg");
   h2d += (int64_t)(cB + bB + sB + eB);
-  CK(ddd::launch_prep_segments(ctx->coord.as<double>(), ctx->bvec.as<double>(), ctx->segidx.as<int64_t>(), ld,
+  CK(ddd::strict::launch_prep_segments(ctx->coord.as<double>(), ctx->bvec.as<double>(), ctx->segidx.as<int64_t>(), ld,
                                eB ? ctx->ext.as<uint8_t>() : nullptr, numSeg, npad, ctx->soa.as<double>(),
                                ctx->skip.as<uint8_t>(), ctx->stream),
      "prep_segments");
@@ -195,9 +221,9 @@ int segseg_compute(ddd_ctx* ctx, const ddd_consts* k, const double* coord, int64
   CK(cudaMemsetAsync(ctx->counters.p, 0, 3 * sizeof(unsigned long long), ctx->stream), "memset counters");
   CK(ctx->out.ensure((size_t)nOut * 6 * sizeof(double)), "alloc output");
   if (!rowsMode) {
-    CK(ctx->partial.ensure(ddd::segseg_partial_bytes_all(npad)), "alloc partial sums");
+    CK(ctx->partial.ensure(ddd::strict::segseg_partial_bytes_all(npad)), "alloc partial sums");
     CK(cudaEventRecord(ctx->ev[1], ctx->stream), "event");
-    CK(ddd::launch_segseg_all_f64(K, ctx->soa.as<double>(), ctx->skip.as<uint8_t>(), npad, ctx->partial.as<double>(),
+    CK(run_segseg_all(ctx, K, ctx->soa.as<double>(), ctx->skip.as<uint8_t>(), npad, ctx->partial.as<double>(),
                                   ctx->out.as<double>(), numSeg, ctx->counters.as<unsigned long long>(), ctx->stream),
        "segseg_all_f64");
   } else {
@@ -208,9 +234,9 @@ int segseg_compute(ddd_ctx* ctx, const ddd_consts* k, const double* coord, int64
                        ctx->stream),
        "copy idx");
     h2d += nIdx * (int64_t)sizeof(int64_t);
-    CK(ctx->partial.ensure(ddd::segseg_partial_bytes_rows(nIdx, npad)), "alloc partial sums");
+    CK(ctx->partial.ensure(ddd::strict::segseg_partial_bytes_rows(nIdx, npad)), "alloc partial sums");
     CK(cudaEventRecord(ctx->ev[1], ctx->stream), "event");
-    CK(ddd::launch_segseg_rows_f64(K, ctx->soa.as<double>(), ctx->skip.as<uint8_t>(), npad, ctx->rows.as<int64_t>(),
+    CK(run_segseg_rows(ctx, K, ctx->soa.as<double>(), ctx->skip.as<uint8_t>(), npad, ctx->rows.as<int64_t>(),
                                    nIdx, ctx->partial.as<double>(), ctx->out.as<double>(),
                                    ctx->counters.as<unsigned long long>(), ctx->stream),
        "segseg_rows_f64");
@@ -374,7 +400,7 @@ int ddd_sigma_tilde(ddd_ctx* ctx, const ddd_consts* k, const double* x0, int64_t
   CK(cudaMemcpyAsync(ctx->x0.p, x0, xB, cudaMemcpyHostToDevice, ctx->stream), "copy points");
   h2d += (int64_t)xB;
   CK(cudaEventRecord(ctx->ev[1], ctx->stream), "event");
-  CK(ddd::launch_sigma_f64(K, ctx->soa.as<double>(), npad, nSel, ctx->x0.as<double>(), numPoints,
+  CK(run_sigma(ctx, K, ctx->soa.as<double>(), npad, nSel, ctx->x0.as<double>(), numPoints,
                            ctx->sigma.as<double>(), ctx->stream),
      "sigma_tilde_f64");
   CK(cudaEventRecord(ctx->ev[2], ctx->stream), "event");
@@ -403,17 +429,17 @@ int ddd_segseg_force_device(ddd_ctx* ctx, const ddd_consts* k, const double* seg
   if (numSeg == 0) return DDD_OK;
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
   CK(cudaSetDevice(ctx->device), "cudaSetDevice");
-  const int64_t npad = ddd::segseg_npad(numSeg);
-  CK(ctx->soa.ensure(ddd::segseg_soa_bytes(npad)), "alloc segment SoA");
+  const int64_t npad = ddd::strict::segseg_npad(numSeg);
+  CK(ctx->soa.ensure(ddd::strict::segseg_soa_bytes(npad)), "alloc segment SoA");
   CK(ctx->skip.ensure((size_t)npad), "alloc skip flags");
-  CK(ctx->partial.ensure(ddd::segseg_partial_bytes_all(npad)), "alloc partial sums");
+  CK(ctx->partial.ensure(ddd::strict::segseg_partial_bytes_all(npad)), "alloc partial sums");
   CK(ctx->counters.ensure(3 * sizeof(unsigned long long)), "alloc counters");
   if (rep) CK(cudaMemsetAsync(ctx->counters.p, 0, 3 * sizeof(unsigned long long), st), "memset counters");
   if (rep) CK(cudaEventRecord(ctx->ev[1], st), "event");
-  CK(ddd::launch_prep_segments_packed(segs, ldSegs, ext, numSeg, npad, ctx->soa.as<double>(),
+  CK(ddd::strict::launch_prep_segments_packed(segs, ldSegs, ext, numSeg, npad, ctx->soa.as<double>(),
                                       ctx->skip.as<uint8_t>(), st),
      "prep_segments_packed");
-  CK(ddd::launch_segseg_all_f64(K, ctx->soa.as<double>(), ctx->skip.as<uint8_t>(), npad, ctx->partial.as<double>(),
+  CK(run_segseg_all(ctx, K, ctx->soa.as<double>(), ctx->skip.as<uint8_t>(), npad, ctx->partial.as<double>(),
                                 force, numSeg, rep ? ctx->counters.as<unsigned long long>() : nullptr, st),
      "segseg_all_f64");
   if (rep) {
@@ -449,14 +475,14 @@ int ddd_sigma_tilde_device(ddd_ctx* ctx, const ddd_consts* k, const double* x0, 
     CK(cudaMemsetAsync(sigma, 0, (size_t)numPoints * 6 * sizeof(double), st), "memset sigma");
     return DDD_OK;
   }
-  const int64_t npad = ddd::segseg_npad(numSeg);
-  CK(ctx->soa.ensure(ddd::segseg_soa_bytes(npad)), "alloc segment SoA");
+  const int64_t npad = ddd::strict::segseg_npad(numSeg);
+  CK(ctx->soa.ensure(ddd::strict::segseg_soa_bytes(npad)), "alloc segment SoA");
   CK(ctx->skip.ensure((size_t)npad), "alloc skip flags");
   if (rep) CK(cudaEventRecord(ctx->ev[1], st), "event");
-  CK(ddd::launch_prep_segments_packed(segs, ldSegs, nullptr, numSeg, npad, ctx->soa.as<double>(),
+  CK(ddd::strict::launch_prep_segments_packed(segs, ldSegs, nullptr, numSeg, npad, ctx->soa.as<double>(),
                                       ctx->skip.as<uint8_t>(), st),
      "prep_segments_packed");
-  CK(ddd::launch_sigma_f64(K, ctx->soa.as<double>(), npad, numSeg, x0, numPoints, sigma, st), "sigma_tilde_f64");
+  CK(run_sigma(ctx, K, ctx->soa.as<double>(), npad, numSeg, x0, numPoints, sigma, st), "sigma_tilde_f64");
   if (rep) {
     CK(cudaEventRecord(ctx->ev[2], st), "event");
     CK(cudaStreamSynchronize(st), "sigma_tilde_device");
@@ -465,6 +491,16 @@ int ddd_sigma_tilde_device(ddd_ctx* ctx, const ddd_consts* k, const double* x0, 
   }
   return DDD_OK;
 }
+
+int ddd_set_mode(ddd_ctx* ctx, int mode) {
+  if (!ctx) return DDD_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (mode != DDD_MODE_FP64 && mode != DDD_MODE_FP64_FMA) return fail(ctx, DDD_EINVAL, "unknown mode");
+  ctx->mode = mode;
+  return DDD_OK;
+}
+
+int ddd_get_mode(const ddd_ctx* ctx) { return ctx ? ctx->mode : DDD_EINVAL; }
 
 int ddd_probe_fma_peak(ddd_ctx* ctx, int precision, double* flops_per_s) {
   if (!ctx || !flops_per_s) return DDD_EINVAL;

@@ -9,26 +9,34 @@ namespace ddd {
 
 struct KConsts;
 
-// segseg_f64.cu
-int64_t segseg_npad(int64_t numSeg);
-size_t segseg_soa_bytes(int64_t npad);
-size_t segseg_partial_bytes_all(int64_t npad);
-size_t segseg_partial_bytes_rows(int64_t nRows, int64_t npad);
-cudaError_t launch_prep_segments(const double* coord, const double* bVec, const int64_t* segIdx, int64_t ld,
-                                 const uint8_t* extSeg, int64_t numSeg, int64_t npad, double* soa, uint8_t* skip,
-                                 cudaStream_t st);
-cudaError_t launch_prep_segments_packed(const double* in, int64_t ldIn, const uint8_t* extSeg, int64_t numSeg,
-                                        int64_t npad, double* soa, uint8_t* skip, cudaStream_t st);
-cudaError_t launch_segseg_all_f64(const KConsts& K, const double* soa, const uint8_t* skip, int64_t npad,
-                                  double* partial, double* out, int64_t numSeg, unsigned long long* counters,
-                                  cudaStream_t st);
-cudaError_t launch_segseg_rows_f64(const KConsts& K, const double* soa, const uint8_t* skip, int64_t npad,
-                                   const int64_t* rows, int64_t nRows, double* partial, double* out,
-                                   unsigned long long* counters, cudaStream_t st);
+// segseg_f64.cu and sigma_f64.cu, each compiled as two variants:
+//   strict: --fmad=false, every operation rounded as in the reference;
+//   fast:   FMA contraction.
+#define DDD_F64_DECLS \
+  int64_t segseg_npad(int64_t numSeg); \
+  size_t segseg_soa_bytes(int64_t npad); \
+  size_t segseg_partial_bytes_all(int64_t npad); \
+  size_t segseg_partial_bytes_rows(int64_t nRows, int64_t npad); \
+  cudaError_t launch_prep_segments(const double* coord, const double* bVec, const int64_t* segIdx, int64_t ld, \
+                                   const uint8_t* extSeg, int64_t numSeg, int64_t npad, double* soa, uint8_t* skip, \
+                                   cudaStream_t st); \
+  cudaError_t launch_prep_segments_packed(const double* in, int64_t ldIn, const uint8_t* extSeg, int64_t numSeg, \
+                                          int64_t npad, double* soa, uint8_t* skip, cudaStream_t st); \
+  cudaError_t launch_segseg_all_f64(const KConsts& K, const double* soa, const uint8_t* skip, int64_t npad, \
+                                    double* partial, double* out, int64_t numSeg, unsigned long long* counters, \
+                                    cudaStream_t st); \
+  cudaError_t launch_segseg_rows_f64(const KConsts& K, const double* soa, const uint8_t* skip, int64_t npad, \
+                                     const int64_t* rows, int64_t nRows, double* partial, double* out, \
+                                     unsigned long long* counters, cudaStream_t st); \
+  cudaError_t launch_sigma_f64(const KConsts& K, const double* soa, int64_t npad, int64_t nSeg, const double* x0, \
+                               int64_t M, double* sigma, cudaStream_t st);
 
-// sigma_f64.cu
-cudaError_t launch_sigma_f64(const KConsts& K, const double* soa, int64_t npad, int64_t nSeg, const double* x0,
-                             int64_t M, double* sigma, cudaStream_t st);
+namespace strict {
+DDD_F64_DECLS
+}
+namespace fast {
+DDD_F64_DECLS
+}
 
 // probes.cu
 cudaError_t launch_fp64_peak_probe(double* sink, int iters, int blocks, int threads, cudaStream_t st);

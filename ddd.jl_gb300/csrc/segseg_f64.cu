@@ -25,7 +25,15 @@
 #include "ddd_internal.h"
 #include "pair_f64.cuh"
 
+// This file is compiled twice: DDD_VARIANT=strict with --fmad=false (every
+// multiply and add rounded separately, as the reference's Julia code does) and
+// DDD_VARIANT=fast with FMA contraction.
+#ifndef DDD_VARIANT
+#define DDD_VARIANT strict
+#endif
+
 namespace ddd {
+namespace DDD_VARIANT {
 
 constexpr int TILE = 128;
 constexpr int NWARP = TILE / 32;
@@ -466,4 +474,5 @@ cudaError_t launch_segseg_rows_f64(const KConsts& K, const double* soa, const ui
   return cudaGetLastError();
 }
 
+}  // namespace DDD_VARIANT
 }  // namespace ddd

@@ -11,7 +11,13 @@
 #include "ddd_internal.h"
 #include "pair_f64.cuh"
 
+// Compiled twice, like segseg_f64.cu: strict (--fmad=false) and fast (FMA).
+#ifndef DDD_VARIANT
+#define DDD_VARIANT strict
+#endif
+
 namespace ddd {
+namespace DDD_VARIANT {
 
 constexpr int SIG_TILE = 128;
 
@@ -53,4 +59,5 @@ cudaError_t launch_sigma_f64(const KConsts& K, const double* soa, int64_t npad, 
   return cudaGetLastError();
 }
 
+}  // namespace DDD_VARIANT
 }  // namespace ddd

@@ -43,6 +43,14 @@ extern "C" {
 
 typedef struct ddd_ctx ddd_ctx;
 
+/* Arithmetic modes of a context (ddd_set_mode).  The reference has one method,
+ * Float64 with every multiply and add rounded separately; DDD_MODE_FP64 is
+ * that method and the default.  DDD_MODE_FP64_FMA evaluates the same formulas
+ * with fused multiply-adds (faster; its rounding differs at the level of the
+ * algorithm's own Float64 noise). */
+#define DDD_MODE_FP64 0
+#define DDD_MODE_FP64_FMA 1
+
 /* Constants of the path.  The reference computes them in
  * MaterialParameters (src/Type/MaterialConstructor.jl:66-82) and
  * DislocationParameters (src/Type/DislocationConstructor.jl:83). */
@@ -119,6 +127,11 @@ int ddd_segseg_force_device(ddd_ctx* ctx, const ddd_consts* k, const double* seg
 int ddd_sigma_tilde_device(ddd_ctx* ctx, const ddd_consts* k, const double* x0, int64_t numPoints,
                            const double* segs, int64_t ldSegs, int64_t numSeg, double* sigma, void* stream,
                            ddd_report* rep);
+
+/* Select / query the arithmetic mode of ctx (DDD_MODE_*).  No reference
+ * counterpart: the reference's dispatch flags are parCPU / parGPU only. */
+int ddd_set_mode(ddd_ctx* ctx, int mode);
+int ddd_get_mode(const ddd_ctx* ctx);
 
 /* Measurement utility (no reference counterpart): FP64 or FP32 FMA-pipe
  * throughput of this GPU in FLOP/s, measured with CUDA events over an

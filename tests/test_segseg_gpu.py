@@ -44,7 +44,7 @@ def _synthetic(pkg, synth, num_loops, seed, config="gpu32k", parallel_fraction=N
     return pkg.DislocationNetwork(coord, bvec, seg)
 
 
-def check_forces(F, oracle, k5, net, rows=None, ref=None):
+def check_forces(F, oracle, k5, net, rows=None, ref=None, factor=(4, 3)):
     """F: GPU forces of all segments (or of the 0-based `rows`); ref: the oracle's
     Float64 forces for the same columns (computed here when None)."""
     nt = os.cpu_count() or 1
@@ -64,10 +64,10 @@ def check_forces(F, oracle, k5, net, rows=None, ref=None):
                 os.environ.get("PYTEST_CURRENT_TEST", "?"), F.shape[2], noise, gpu_err,
                 np.max(d / (norm(ref) + 1e-300))))
     assert np.linalg.norm(F - ref) <= 1e-10 * np.linalg.norm(ref) + ulps
-    excess = np.max(d - (1e-10 * norm(ref) + 4 * noise + ulps))
+    excess = np.max(d - (1e-10 * norm(ref) + factor[0] * noise + ulps))
     assert excess <= 0, "node-force difference exceeds bound by %g (noise %g, max rel %g)" % (
         excess, noise, np.max(d / (norm(ref) + 1e-300)))
-    assert gpu_err <= 3 * noise + ulps, "kernel error %g vs reference arithmetic %g" % (gpu_err, noise)
+    assert gpu_err <= factor[1] * noise + ulps, "kernel error %g vs reference arithmetic %g" % (gpu_err, noise)
     return noise, gpu_err
 
 
@@ -241,3 +241,23 @@ def test_device_resident_form(pkg, synth):
     dev = out.cpu().numpy().reshape(3, 2, -1, order="F")
     assert np.array_equal(dev, host)
     assert rep["pairs_general"] + rep["pairs_parallel"] == net.numSeg * (net.numSeg - 1) // 2
+
+
+@pytest.mark.parametrize("num_loops,seed", [(64, 4), (150, 5)])
+def test_fma_mode(pkg, synth, oracle, num_loops, seed):
+    """DDD_MODE_FP64_FMA: same formulas with fused multiply-adds.  Its rounding
+    differs from the reference's arithmetic by up to ~4x that arithmetic's own
+    noise (measured: the same happens to the oracle compiled with FMA on a CPU),
+    so the bounds are 8x / 6x the noise."""
+    net = _synthetic(pkg, synth, num_loops, seed, cube=3000.0)
+    dln, mat = _params(pkg)
+    ctx = pkg.get_context()
+    ctx.mode = "fp64_fma"
+    try:
+        F = pkg.calcSegSegForce(dln, mat, net)
+    finally:
+        ctx.mode = "fp64"
+    assert ctx.mode == pkg.MODE_FP64
+    check_forces(F, oracle, k5_of(dln, mat), net, factor=(8, 6))
+    S = pkg.calcSegSegForce(dln, mat, net)
+    assert not np.array_equal(F, S)  # a different kernel ran
