@@ -137,7 +137,7 @@ def run_reference(args, pkg, synth, oracle):
     ws, rank = _dist()
     if rank != 0:
         return
-    p, b, cfg = synth.make(args.workload, seed=0)
+    p, b, cfg = synth.make(args.workload, seed=0, num_loops=args.loops)
     k5 = np.array([1.0, 1 / (4 * np.pi), 1 / (8 * np.pi), 1 / (4 * np.pi) / (1 - synth.NU),
                    synth.NU / (4 * np.pi) / (1 - synth.NU)])
     times, vals = [], []
@@ -171,6 +171,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="gpu65k")
+    ap.add_argument("--loops", type=int, default=None,
+                    help="override the loop count of the workload (8 segments per loop), for small profiling runs")
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--cpu-target-s", type=float, default=15.0)
     ap.add_argument("--ref-step-s", type=float, default=4.0)
@@ -196,7 +198,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
-    p, b, cfg = synth.make(args.workload, seed=0)
+    p, b, cfg = synth.make(args.workload, seed=0, num_loops=args.loops)
     n = p.shape[0] * 8
     pairs = n * (n - 1) // 2
     dln = pkg.DislocationParameters(coreRad=synth.CORE_RAD)
