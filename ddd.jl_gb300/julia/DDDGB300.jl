@@ -1,0 +1,116 @@
+# DDDGB300.jl — Julia binding of libddd_gb300.so (include/ddd_gb300.h) for DDD.jl.
+#
+# Drop-in for the O(N^2) hot path: calcSegSegForce / calcSegSegForce! /
+# calc_σTilde / calc_σTilde! keep DDD.jl's signatures and array layouts; the
+# network's own arrays are passed to the library without copies.  Select it
+# with the existing DislocationParameters field parGPU (src/Type/DislocationType.jl:254):
+# the dispatch lines to add to DDD.jl are shown in INTEGRATION.md.
+#
+# Julia is not installed in the environment this library was built in, so this
+# file has not been executed there; the C ABI it binds is exercised by the
+# Python mirror (ddd.jl_gb300/__init__.py) and its tests.
+module DDDGB300
+
+export calcSegSegForceGPU, calcSegSegForceGPU!, calc_σTildeGPU, calc_σTildeGPU!
+
+const libddd = joinpath(@__DIR__, "..", "libddd_gb300.so")
+
+struct DDDConsts
+    aSq::Float64
+    mu4pi::Float64
+    mu8pi::Float64
+    mu4pinu::Float64
+    nuMu4pinu::Float64
+end
+
+const CTX = Ref{Ptr{Cvoid}}(C_NULL)
+
+function context()
+    if CTX[] == C_NULL
+        p = ccall((:ddd_create, libddd), Ptr{Cvoid}, (Cint,), 0)
+        p == C_NULL && error("ddd_create: " * unsafe_string(ccall((:ddd_last_error, libddd), Cstring, (Ptr{Cvoid},), C_NULL)))
+        CTX[] = p
+        atexit(() -> ccall((:ddd_destroy, libddd), Cvoid, (Ptr{Cvoid},), CTX[]))
+    end
+    return CTX[]
+end
+
+consts(dlnParams, matParams) =
+    DDDConsts(dlnParams.coreRadSq, matParams.μ4π, matParams.μ8π, matParams.μ4πν, matParams.νμ4πν)
+
+function check(rc)
+    rc == 0 && return nothing
+    msg = unsafe_string(ccall((:ddd_last_error, libddd), Cstring, (Ptr{Cvoid},), context()))
+    rc == -2 && throw(BoundsError(msg))
+    (rc == -1 || rc == -3) && throw(ArgumentError(msg))
+    error("libddd_gb300 error $rc: $msg")
+end
+
+idxvec(idx) = isnothing(idx) ? Int64[] : collect(Int64, idx)
+
+# calcSegSegForce (src/Processing/DislocationForces.jl:470-561)
+function calcSegSegForceGPU(dlnParams, matParams, network, idx = nothing)
+    numSeg = network.numSeg[1]
+    iv = idxvec(idx)
+    n = isnothing(idx) ? numSeg : length(iv)
+    out = zeros(3, 2, n)
+    k = Ref(consts(dlnParams, matParams))
+    coord, bVec, segIdx, extSeg = network.coord, network.bVec, network.segIdx, network.extSeg
+    GC.@preserve coord bVec segIdx extSeg iv out begin
+        rc = ccall((:ddd_segseg_force, libddd), Cint,
+            (Ptr{Cvoid}, Ref{DDDConsts}, Ptr{Float64}, Int64, Ptr{Float64}, Int64, Ptr{Int64}, Int64,
+             Ptr{Bool}, Int64, Ptr{Int64}, Int64, Ptr{Float64}, Ptr{Cvoid}),
+            context(), k, coord, size(coord, 2), bVec, size(bVec, 2), segIdx, size(segIdx, 1),
+            extSeg, numSeg, isnothing(idx) ? C_NULL : pointer(iv), length(iv), out, C_NULL)
+    end
+    check(rc)
+    return out
+end
+
+# calcSegSegForce! (src/Processing/DislocationForces.jl:576-669)
+function calcSegSegForceGPU!(dlnParams, matParams, network, idx = nothing)
+    numSeg = network.numSeg[1]
+    iv = idxvec(idx)
+    k = Ref(consts(dlnParams, matParams))
+    coord, bVec, segIdx, extSeg, segForce = network.coord, network.bVec, network.segIdx, network.extSeg, network.segForce
+    GC.@preserve coord bVec segIdx extSeg segForce iv begin
+        rc = ccall((:ddd_segseg_force_inplace, libddd), Cint,
+            (Ptr{Cvoid}, Ref{DDDConsts}, Ptr{Float64}, Int64, Ptr{Float64}, Int64, Ptr{Int64}, Int64,
+             Ptr{Bool}, Int64, Ptr{Int64}, Int64, Ptr{Float64}, Int64, Ptr{Cvoid}),
+            context(), k, coord, size(coord, 2), bVec, size(bVec, 2), segIdx, size(segIdx, 1),
+            extSeg, numSeg, isnothing(idx) ? C_NULL : pointer(iv), length(iv), segForce, size(segForce, 3), C_NULL)
+    end
+    check(rc)
+    return nothing
+end
+
+# calc_σTilde! (src/Processing/DislocationFEM.jl:67-84); x0 must be a 3×M array.
+function calc_σTildeGPU!(σ, x0, dlnParams, matParams, network, idx = nothing)
+    @assert ndims(σ) == ndims(x0) && size(σ, 1) == 6
+    @assert size(σ, 2) == size(x0, 2)
+    iv = idxvec(idx)
+    k = Ref(consts(dlnParams, matParams))
+    coord, bVec, segIdx = network.coord, network.bVec, network.segIdx
+    xs = convert(Array{Float64}, x0)
+    GC.@preserve coord bVec segIdx xs σ iv begin
+        rc = ccall((:ddd_sigma_tilde, libddd), Cint,
+            (Ptr{Cvoid}, Ref{DDDConsts}, Ptr{Float64}, Int64, Ptr{Float64}, Int64, Ptr{Float64}, Int64,
+             Ptr{Int64}, Int64, Int64, Ptr{Int64}, Int64, Ptr{Float64}, Ptr{Cvoid}),
+            context(), k, xs, size(xs, 2), coord, size(coord, 2), bVec, size(bVec, 2), segIdx, size(segIdx, 1),
+            network.numSeg[1], isnothing(idx) ? C_NULL : pointer(iv), length(iv), σ, C_NULL)
+    end
+    check(rc)
+    return σ
+end
+
+# calc_σTilde (src/Processing/DislocationFEM.jl:24-41)
+function calc_σTildeGPU(x0, dlnParams, matParams, network, idx = nothing)
+    xs = x0 isa Base.Iterators.ProductIterator ? reduce(hcat, [collect(p) for p in x0]) : x0
+    numPoints = div(length(xs), 3)
+    xs = reshape(convert(Array{Float64}, xs), 3, numPoints)
+    σ = zeros(6, numPoints)
+    calc_σTildeGPU!(σ, xs, dlnParams, matParams, network, idx)
+    return numPoints == 1 ? σ[:, 1] : σ
+end
+
+end # module
