@@ -23,13 +23,16 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libddd_gb300.so")
 
-DDD_OK, DDD_EINVAL, DDD_ERANGE, DDD_ENONFINITE, DDD_EDEVICE, DDD_ENOMEM = 0, -1, -2, -3, -4, -5
+DDD_OK, DDD_EINVAL, DDD_ERANGE, DDD_ENONFINITE, DDD_EDEVICE, DDD_ENOMEM, DDD_ETOOBIG = 0, -1, -2, -3, -4, -5, -6
+# Largest network ddd_segseg_force_device_noalloc accepts (include/ddd_gb300.h).
+NOALLOC_MAX_SEGMENTS = 4096
 
 # Every symbol include/ddd_gb300.h declares.
 EXPORTED_SYMBOLS = (
     "ddd_create", "ddd_destroy", "ddd_last_error", "ddd_version",
     "ddd_segseg_force", "ddd_segseg_force_inplace", "ddd_sigma_tilde",
     "ddd_segseg_force_device", "ddd_sigma_tilde_device", "ddd_set_mode", "ddd_get_mode", "ddd_probe_fma_peak",
+    "ddd_segseg_force_device_noalloc",
 )
 
 # Arithmetic modes (ddd_set_mode).
@@ -97,6 +100,7 @@ def library():
         L.ddd_sigma_tilde.argtypes = [_vp, cp, _dp, _i64, _dp, _i64, _dp, _i64, _ip, _i64, _i64, _ip, _i64, _dp, rp]
         L.ddd_segseg_force_device.argtypes = [_vp, cp, _vp, _i64, _vp, _i64, _vp, _vp, rp]
         L.ddd_sigma_tilde_device.argtypes = [_vp, cp, _vp, _i64, _vp, _i64, _i64, _vp, _vp, rp]
+        L.ddd_segseg_force_device_noalloc.argtypes = [cp, _vp, _i64, _vp, _i64, _vp, _vp]
         L.ddd_set_mode.argtypes = [_vp, ctypes.c_int]
         L.ddd_get_mode.argtypes = [_vp]
         L.ddd_probe_fma_peak.argtypes = [_vp, ctypes.c_int, _dp]

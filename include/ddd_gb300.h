@@ -40,6 +40,7 @@ extern "C" {
 #define DDD_ENONFINITE (-3) /* a non-finite coordinate / Burgers vector / constant, or a zero-length segment */
 #define DDD_EDEVICE (-4)    /* CUDA error (message in ddd_last_error) */
 #define DDD_ENOMEM (-5)     /* device allocation failed */
+#define DDD_ETOOBIG (-6)    /* more segments than ddd_segseg_force_device_noalloc accepts */
 
 typedef struct ddd_ctx ddd_ctx;
 
@@ -127,6 +128,27 @@ int ddd_segseg_force_device(ddd_ctx* ctx, const ddd_consts* k, const double* seg
 int ddd_sigma_tilde_device(ddd_ctx* ctx, const ddd_consts* k, const double* x0, int64_t numPoints,
                            const double* segs, int64_t ldSegs, int64_t numSeg, double* sigma, void* stream,
                            ddd_report* rep);
+
+/* Allocation-free form of ddd_segseg_force_device (no counterpart in the
+ * reference, which has no device memory): for callers that cannot let this
+ * library allocate device memory — an application whose GPU memory is owned by
+ * its own pool allocator, or a time-stepping loop that cannot afford the
+ * device-wide synchronisation of cudaMalloc/cudaFree.  Inputs and output are
+ * the caller's device buffers (layouts as ddd_segseg_force_device; ext may be
+ * NULL); the work runs on the current CUDA device, on `stream` (a
+ * cudaStream_t; NULL = the legacy default stream), in DDD_MODE_FP64 arithmetic,
+ * and the call returns without waiting.  It calls no cudaMalloc, cudaFree or
+ * other allocating routine: its scratch is a fixed device array of about
+ * 6.9 MB that exists on every GPU that loads the library, for the life of the
+ * process.  Limits: numSeg <= DDD_NOALLOC_MAX_SEGMENTS, else DDD_ETOOBIG.
+ * Every call shares that array (it keeps the last call's contents; each call
+ * writes every element it reads first), so calls that overlap on the GPU race:
+ * serialise them.  The first call on each device looks up the array's device
+ * address; make it before any stream capture that contains later calls.
+ * Returns DDD_OK, DDD_EINVAL, DDD_ETOOBIG or DDD_EDEVICE (no message). */
+#define DDD_NOALLOC_MAX_SEGMENTS 4096
+int ddd_segseg_force_device_noalloc(const ddd_consts* k, const double* segs, int64_t ldSegs, const uint8_t* ext,
+                                    int64_t numSeg, double* force, void* stream);
 
 /* Select / query the arithmetic mode of ctx (DDD_MODE_*).  No reference
  * counterpart: the reference's dispatch flags are parCPU / parGPU only. */
