@@ -39,6 +39,7 @@ sys.path.insert(0, ROOT)
 # op-counting instantiation of the oracle (oracle/ddd_oracle.cpp, opcount_*):
 OPS_GENERAL_PAIR = 1511  # general branch: 626 add, 840 mul, 23 div, 10 sqrt, 8 log, 4 atan
 OPS_PARALLEL_PAIR = 985  # near-parallel branch without core corrections
+OPS_SIGMA_EVAL = 289  # one (segment, field point) σ̃ evaluation: 101 add, 183 mul, 3 div, 2 sqrt
 # Each near-parallel side that needs core corrections adds two general evaluations.
 
 
@@ -178,6 +179,8 @@ def main():
     ap.add_argument("--ref-step-s", type=float, default=4.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--no-sigma", action="store_true")
+    ap.add_argument("--sigma-grid", type=int, default=32)
     args = ap.parse_args()
 
     import __graft_entry__ as graft
@@ -271,6 +274,32 @@ def main():
             ctx.segseg_force_device(k, soa.data_ptr(), n, n, force.data_ptr(), stream=sptr)
             torch.cuda.synchronize()
 
+    # Field-point stress σ̃ of the same network on a 32^3 grid over the cube.
+    sigma = None
+    if not args.no_sigma:
+        pts = synth.grid_points(args.sigma_grid, cfg["cube"])
+        M = pts.shape[1]
+        x0 = torch.from_numpy(np.ascontiguousarray(pts.T)).cuda()
+        sig = torch.zeros(6 * M, dtype=torch.float64, device="cuda")
+        with torch.cuda.stream(stream):
+            ctx.sigma_tilde_device(k, x0.data_ptr(), M, soa.data_ptr(), n, n, sig.data_ptr(), stream=sptr)
+            torch.cuda.synchronize()
+            sms = []
+            for _ in range(2):
+                flush.zero_()
+                a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a_.record(stream)
+                ctx.sigma_tilde_device(k, x0.data_ptr(), M, soa.data_ptr(), n, n, sig.data_ptr(), stream=sptr)
+                b_.record(stream)
+                torch.cuda.synchronize()
+                sms.append(a_.elapsed_time(b_))
+        ms_sig = statistics.mean(sms)
+        evals = n * M
+        sigma = {"value": evals / (ms_sig * 1e-3), "unit": "seg-point evaluations/s",
+                 "points_per_s": M / (ms_sig * 1e-3), "ms": ms_sig,
+                 "config": "%d segments x %d points (%d^3 grid over the cube), FP64 strict" % (n, M, args.sigma_grid),
+                 "frac_fp64_peak": evals * OPS_SIGMA_EVAL / (ms_sig * 1e-3) / fp64_peak}
+
     # End to end through the reference-facing C-ABI call with host arrays.
     coord, bvec, seg = synth.network_arrays(p, b)
     net = pkg.DislocationNetwork(coord, bvec, seg)
@@ -313,6 +342,7 @@ def main():
         "gpu_launches": 3 * args.steps,
         "mode": "fp64 (strict: every multiply and add rounded separately, as the reference)",
         "variants": variants,
+        "sigma_tilde": sigma,
         "kernel_ms_per_step": statistics.mean(ms_kernel),
     }
     cs = clocks.summary()

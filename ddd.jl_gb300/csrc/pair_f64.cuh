@@ -53,9 +53,15 @@ __device__ __forceinline__ void seg_direction(D3 n1, D3 n2, D3& t, double& tN) {
   t = t * tN;
 }
 
-// SegSegInteg at one corner, added with sign s (+1/-1) into integ[19].
+// v with its sign flipped when sm is the sign-bit mask (integer pipe, exact).
+__device__ __forceinline__ double sgn(double v, unsigned long long sm) {
+  return __longlong_as_double(__double_as_longlong(v) ^ (long long)sm);
+}
+
+// SegSegInteg at one corner, added (sm = 0) or subtracted (sm = sign bit) into integ[19].
 __device__ __forceinline__ void seg_seg_integ_acc(double aSq, double d, double c, double cSq, double omcSq,
-                                                  double omcSqI, double x, double y, double s, double* integ) {
+                                                  double omcSqI, double x, double y, unsigned long long sm,
+                                                  double* integ) {
   double aSq_dSq = aSq + d * d * omcSq;
   double xSq = x * x;
   double ySq = y * y;
@@ -102,25 +108,25 @@ __device__ __forceinline__ void seg_seg_integ_acc(double aSq, double d, double c
 
   double c15_18_19 = 2.0 * integ4;
 
-  integ[0] += s * integ1;
-  integ[1] += s * integ2;
-  integ[2] += s * integ3;
-  integ[3] += s * integ4;
-  integ[4] += s * integ5;
-  integ[5] += s * integ6;
-  integ[6] += s * ((integ1 - xRaSq_R_t1_I - yRaSq_R_t2_I) / (aSq_dSq));
-  integ[7] += s * ((RaSq_R_t1_I - c * RaSq_R_t2_I) * omcSqI);
-  integ[8] += s * ((RaSq_R_t2_I - c * RaSq_R_t1_I) * omcSqI);
-  integ[9] += s * ((RaInv - c * (xRaSq_R_t1_I + yRaSq_R_t2_I + integ1)) * omcSqI);
-  integ[10] += s * ((xRaSq_R_t1_I + cSq * yRaSq_R_t2_I + c_11_12) * omcSqI);
-  integ[11] += s * ((yRaSq_R_t2_I + cSq * xRaSq_R_t1_I + c_11_12) * omcSqI);
-  integ[12] += s * ((integ3 - x_13_14 + c * (y_13_14 - integ2)) * omcSqI);
-  integ[13] += s * ((integ2 - y_13_14 + c * (x_13_14 - integ3)) * omcSqI);
-  integ[14] += s * ((integ5 - z_15_18 + c * (xSq * c_15_18 - c15_18_19)) * omcSqI);
-  integ[15] += s * ((xSqRaSq_R_t1_I + c * c_16 + 2.0 * integ2) * omcSqI);
-  integ[16] += s * ((ySqRaSq_R_t2_I + c * c_17_19 + 2.0 * integ3) * omcSqI);
-  integ[17] += s * ((c15_18_19 - xSq * c_15_18 + c * (z_15_18 - integ5)) * omcSqI);
-  integ[18] += s * ((c15_18_19 - ySq * c_19 + c * (x * c_17_19 - integ6)) * omcSqI);
+  integ[0] += sgn(integ1, sm);
+  integ[1] += sgn(integ2, sm);
+  integ[2] += sgn(integ3, sm);
+  integ[3] += sgn(integ4, sm);
+  integ[4] += sgn(integ5, sm);
+  integ[5] += sgn(integ6, sm);
+  integ[6] += sgn(((integ1 - xRaSq_R_t1_I - yRaSq_R_t2_I) / (aSq_dSq)), sm);
+  integ[7] += sgn(((RaSq_R_t1_I - c * RaSq_R_t2_I) * omcSqI), sm);
+  integ[8] += sgn(((RaSq_R_t2_I - c * RaSq_R_t1_I) * omcSqI), sm);
+  integ[9] += sgn(((RaInv - c * (xRaSq_R_t1_I + yRaSq_R_t2_I + integ1)) * omcSqI), sm);
+  integ[10] += sgn(((xRaSq_R_t1_I + cSq * yRaSq_R_t2_I + c_11_12) * omcSqI), sm);
+  integ[11] += sgn(((yRaSq_R_t2_I + cSq * xRaSq_R_t1_I + c_11_12) * omcSqI), sm);
+  integ[12] += sgn(((integ3 - x_13_14 + c * (y_13_14 - integ2)) * omcSqI), sm);
+  integ[13] += sgn(((integ2 - y_13_14 + c * (x_13_14 - integ3)) * omcSqI), sm);
+  integ[14] += sgn(((integ5 - z_15_18 + c * (xSq * c_15_18 - c15_18_19)) * omcSqI), sm);
+  integ[15] += sgn(((xSqRaSq_R_t1_I + c * c_16 + 2.0 * integ2) * omcSqI), sm);
+  integ[16] += sgn(((ySqRaSq_R_t2_I + c * c_17_19 + 2.0 * integ3) * omcSqI), sm);
+  integ[17] += sgn(((c15_18_19 - xSq * c_15_18 + c * (z_15_18 - integ5)) * omcSqI), sm);
+  integ[18] += sgn(((c15_18_19 - ySq * c_19 + c * (x * c_17_19 - integ6)) * omcSqI), sm);
 }
 
 __device__ __forceinline__ D3 fsum11(const D3* V, const double* F) {
@@ -195,8 +201,8 @@ __device__ __forceinline__ void general_pair(const KConsts& K, D3 b1, D3 n11, D3
   for (int q = 0; q < 4; ++q) {
     double x = (q & 2) ? x2 : x1;
     double y = (q & 1) ? y2 : y1;
-    double s = (q == 1 || q == 2) ? -1.0 : 1.0;
-    seg_seg_integ_acc(K.aSq, d, c, cSq, omcSq, omcSqI, x, y, s, integ);
+    unsigned long long sm = (q == 1 || q == 2) ? 0x8000000000000000ull : 0ull;
+    seg_seg_integ_acc(K.aSq, d, c, cSq, omcSq, omcSqI, x, y, sm, integ);
   }
 
   D3 V[11];
@@ -324,9 +330,9 @@ __device__ __forceinline__ void general_pair(const KConsts& K, D3 b1, D3 n11, D3
   }
 }
 
-// ParSegSegInteg at one corner, added with sign s into integ[12].
-__device__ __forceinline__ void par_seg_seg_integ_acc(double aSq_dSq, double aSq_dSqI, double x, double y, double s,
-                                                      double* integ) {
+// ParSegSegInteg at one corner, added or subtracted (sm) into integ[12].
+__device__ __forceinline__ void par_seg_seg_integ_acc(double aSq_dSq, double aSq_dSqI, double x, double y,
+                                                      unsigned long long sm, double* integ) {
   double xpy = x + y;
   double xmy = x - y;
   double Ra = sqrt(aSq_dSq + xpy * xpy);
@@ -334,18 +340,18 @@ __device__ __forceinline__ void par_seg_seg_integ_acc(double aSq_dSq, double aSq
   double Log_Ra_ypz = log(Ra + xpy);
   double tmp = xmy * Ra * aSq_dSqI;
   double i10 = -aSq_dSqI * xpy * RaInv;
-  integ[0] += s * (Ra * aSq_dSqI);
-  integ[1] += s * (-0.5 * (Log_Ra_ypz - tmp));
-  integ[2] += s * (-0.5 * (Log_Ra_ypz + tmp));
-  integ[3] += s * (-Log_Ra_ypz);
-  integ[4] += s * (y * Log_Ra_ypz - Ra);
-  integ[5] += s * (x * Log_Ra_ypz - Ra);
-  integ[6] += s * (aSq_dSqI * (2.0 * aSq_dSqI * Ra - RaInv));
-  integ[7] += s * (aSq_dSqI * (tmp - x * RaInv));
-  integ[8] += s * (-aSq_dSqI * (tmp + y * RaInv));
-  integ[9] += s * i10;
-  integ[10] += s * (RaInv - y * i10);
-  integ[11] += s * (RaInv - x * i10);
+  integ[0] += sgn((Ra * aSq_dSqI), sm);
+  integ[1] += sgn((-0.5 * (Log_Ra_ypz - tmp)), sm);
+  integ[2] += sgn((-0.5 * (Log_Ra_ypz + tmp)), sm);
+  integ[3] += sgn((-Log_Ra_ypz), sm);
+  integ[4] += sgn((y * Log_Ra_ypz - Ra), sm);
+  integ[5] += sgn((x * Log_Ra_ypz - Ra), sm);
+  integ[6] += sgn((aSq_dSqI * (2.0 * aSq_dSqI * Ra - RaInv)), sm);
+  integ[7] += sgn((aSq_dSqI * (tmp - x * RaInv)), sm);
+  integ[8] += sgn((-aSq_dSqI * (tmp + y * RaInv)), sm);
+  integ[9] += sgn(i10, sm);
+  integ[10] += sgn((RaInv - y * i10), sm);
+  integ[11] += sgn((RaInv - x * i10), sm);
 }
 
 // One side of calcParSegSegForce: the analytic parallel part on segment "a"
@@ -410,8 +416,8 @@ __device__ __forceinline__ int par_side(const KConsts& K, D3 na1, D3 na2, D3 ta,
   for (int q = 0; q < 4; ++q) {
     double x = (q & 2) ? x2 : x1;
     double y = (q & 1) ? y2 : y1;
-    double s = (q == 1 || q == 2) ? -1.0 : 1.0;
-    par_seg_seg_integ_acc(aSq_dSq, aSq_dSqI, x, y, s, integ);
+    unsigned long long sm = (q == 1 || q == 2) ? 0x8000000000000000ull : 0ull;
+    par_seg_seg_integ_acc(aSq_dSq, aSq_dSqI, x, y, sm, integ);
   }
 
   tmp = tadba * tadbb;
