@@ -249,30 +249,41 @@ def main():
     ms_step = t_rank.item() / args.steps
     value = ws * pairs / (ms_step * 1e-3)
 
-    # The FMA variant of the same kernel, for comparison (same workload, same timing).
+    # Other arithmetic modes of the same path, same workload and timing: the FMA
+    # build of the FP64 kernel and the df64 precision form.  Each reports its
+    # error against the strict FP64 result (itself parity-checked).
     variants = {}
+    ref_force = force.cpu().numpy().reshape(3, 2, -1, order="F")
     if not args.no_variants:
-        ctx.mode = "fp64_fma"
-        with torch.cuda.stream(stream):
-            flush.zero_()
-            ctx.segseg_force_device(k, soa.data_ptr(), n, n, force.data_ptr(), stream=sptr)
-            torch.cuda.synchronize()
-            vms = []
-            for s_ in range(max(1, min(args.steps, 2))):
-                flush.zero_()
-                a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                a_.record(stream)
-                ctx.segseg_force_device(k, soa.data_ptr(), n, n, force.data_ptr(), stream=sptr)
-                b_.record(stream)
-                torch.cuda.synchronize()
-                vms.append(a_.elapsed_time(b_))
-        ctx.mode = "fp64"
-        variants["fp64_fma"] = {"value": pairs / (statistics.mean(vms) * 1e-3), "unit": "pair-interactions/s",
-                                "ms_per_step": statistics.mean(vms),
-                                "frac_fp64_peak": flops_per_step / (statistics.mean(vms) * 1e-3) / fp64_peak}
-        with torch.cuda.stream(stream):
-            ctx.segseg_force_device(k, soa.data_ptr(), n, n, force.data_ptr(), stream=sptr)
-            torch.cuda.synchronize()
+        for mode in ("fp64_fma", "df64"):
+            ctx.mode = mode
+            out_v = torch.zeros_like(force)
+            with torch.cuda.stream(stream):
+                rep_v = ctx.segseg_force_device(k, soa.data_ptr(), n, n, out_v.data_ptr(), stream=sptr, report=True)
+                vms = []
+                for s_ in range(max(1, min(args.steps, 2))):
+                    flush.zero_()
+                    a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    a_.record(stream)
+                    ctx.segseg_force_device(k, soa.data_ptr(), n, n, out_v.data_ptr(), stream=sptr)
+                    b_.record(stream)
+                    torch.cuda.synchronize()
+                    vms.append(a_.elapsed_time(b_))
+            ctx.mode = "fp64"
+            Fv = out_v.cpu().numpy().reshape(3, 2, -1, order="F")
+            dn = np.linalg.norm(Fv - ref_force, axis=0)
+            fn = np.linalg.norm(ref_force, axis=0)
+            variants[mode] = {
+                "value": pairs / (statistics.mean(vms) * 1e-3), "unit": "pair-interactions/s",
+                "ms_per_step": statistics.mean(vms),
+                "speedup_vs_fp64": ms_step / statistics.mean(vms),
+                "frac_fp64_peak_algorithmic": flops_per_step / (statistics.mean(vms) * 1e-3) / fp64_peak,
+                "error_vs_fp64": {"rel_rms": float(np.linalg.norm(Fv - ref_force) / np.linalg.norm(ref_force)),
+                                  "max_node_over_max_force": float(dn.max() / fn.max()),
+                                  "max_rel_node": float(np.max(dn / np.maximum(fn, 1e-300)))},
+                "branches_match_fp64": (rep_v["pairs_general"], rep_v["pairs_parallel"]) ==
+                                       (rep["pairs_general"], rep["pairs_parallel"]),
+            }
 
     # Field-point stress σ̃ of the same network on a 32^3 grid over the cube.
     sigma = None
@@ -351,6 +362,20 @@ def main():
     if not args.no_cpu:
         k5 = np.array([dln.coreRadSq, mat.μ4π, mat.μ8π, mat.μ4πν, mat.νμ4πν])
         line["cpu_baseline"] = cpu_par_sample(pkg, synth, oracle, p, b, k5, args.cpu_target_s)
+        # Parity of the timed result on sampled segments: the oracle's Float64 rows
+        # and the same rows in long double (the reference arithmetic's own error).
+        rows = np.sort(np.random.default_rng(0).choice(n, 16, replace=False))
+        nt_ = cpu_threads()
+        ref_rows = oracle.segseg_rows(k5, net, rows, nt_)
+        ext_rows = oracle.segseg_ser_ld(k5, net, rows, nthreads=nt_)
+        nrm = lambda a: np.linalg.norm(a, axis=0)
+        par = {"rows": len(rows), "fp64_max_rel_node": float(np.max(nrm(ref_force[:, :, rows] - ref_rows) /
+                                                                   nrm(ref_rows))),
+               "fp64_err_vs_longdouble": float(nrm(ref_force[:, :, rows] - ext_rows).max()),
+               "reference_arith_err_vs_longdouble": float(nrm(ref_rows - ext_rows).max())}
+        for mode in variants:
+            pass
+        line["parity_sample"] = par
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

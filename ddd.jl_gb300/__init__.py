@@ -36,8 +36,8 @@ EXPORTED_SYMBOLS = (
 )
 
 # Arithmetic modes (ddd_set_mode).
-MODE_FP64, MODE_FP64_FMA = 0, 1
-MODES = {"fp64": MODE_FP64, "fp64_fma": MODE_FP64_FMA}
+MODE_FP64, MODE_FP64_FMA, MODE_DF64 = 0, 1, 2
+MODES = {"fp64": MODE_FP64, "fp64_fma": MODE_FP64_FMA, "df64": MODE_DF64}
 
 
 class DDDError(RuntimeError):

@@ -22,6 +22,8 @@ FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", 
 VARIANTS = {
     "segseg_f64.cu": [("strict", ["-DDDD_VARIANT=strict", "--fmad=false"]), ("fast", ["-DDDD_VARIANT=fast"])],
     "sigma_f64.cu": [("strict", ["-DDDD_VARIANT=strict", "--fmad=false"]), ("fast", ["-DDDD_VARIANT=fast"])],
+    # df64 needs exact error-free transformations: no contraction.
+    "segseg_df.cu": [("", ["--fmad=false"])],
 }
 
 

@@ -52,7 +52,7 @@ struct ddd_ctx {
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   std::mutex mu;
   std::string err;
-  DevBuf coord, bvec, segidx, ext, soa, skip, partial, out, rows, x0, sigma, counters, probe;
+  DevBuf coord, bvec, segidx, ext, soa, soadf, skip, partial, out, rows, x0, sigma, counters, probe;
   std::vector<double> hostTmp;
 };
 
@@ -78,22 +78,40 @@ int cuda_fail(ddd_ctx* c, cudaError_t e, const char* where) {
 // and inverse length) always uses the strict build, so t and 1/|l| are the
 // reference's values in both modes.
 bool use_fma(const ddd_ctx* c) { return c->mode == DDD_MODE_FP64_FMA; }
+bool use_df(const ddd_ctx* c) { return c->mode == DDD_MODE_DF64; }
 
-cudaError_t run_segseg_all(const ddd_ctx* c, const ddd::KConsts& K, const double* soa, const uint8_t* skip,
-                           int64_t npad, double* partial, double* out, int64_t numSeg, unsigned long long* cnt,
-                           cudaStream_t st) {
+// For DDD_MODE_DF64 the df64 copy of the segment SoA is built first (ctx->soadf).
+cudaError_t prep_df_if_needed(ddd_ctx* c, int64_t npad, cudaStream_t st) {
+  if (!use_df(c)) return cudaSuccess;
+  cudaError_t e = c->soadf.ensure(ddd::segseg_df_soa_bytes(npad));
+  if (e != cudaSuccess) return e;
+  return ddd::launch_prep_df(c->soa.as<double>(), npad, c->soadf.as<float>(), st);
+}
+
+cudaError_t run_segseg_all(ddd_ctx* c, const ddd::KConsts& K, const double* soa, const uint8_t* skip, int64_t npad,
+                           double* partial, double* out, int64_t numSeg, unsigned long long* cnt, cudaStream_t st) {
+  if (use_df(c)) {
+    cudaError_t e = prep_df_if_needed(c, npad, st);
+    if (e != cudaSuccess) return e;
+    return ddd::launch_segseg_all_df(K, soa, c->soadf.as<float>(), skip, npad, partial, out, numSeg, cnt, st);
+  }
   return use_fma(c) ? ddd::fast::launch_segseg_all_f64(K, soa, skip, npad, partial, out, numSeg, cnt, st)
                     : ddd::strict::launch_segseg_all_f64(K, soa, skip, npad, partial, out, numSeg, cnt, st);
 }
 
-cudaError_t run_segseg_rows(const ddd_ctx* c, const ddd::KConsts& K, const double* soa, const uint8_t* skip,
-                            int64_t npad, const int64_t* rows, int64_t nRows, double* partial, double* out,
+cudaError_t run_segseg_rows(ddd_ctx* c, const ddd::KConsts& K, const double* soa, const uint8_t* skip, int64_t npad,
+                            const int64_t* rows, int64_t nRows, double* partial, double* out,
                             unsigned long long* cnt, cudaStream_t st) {
+  if (use_df(c)) {
+    cudaError_t e = prep_df_if_needed(c, npad, st);
+    if (e != cudaSuccess) return e;
+    return ddd::launch_segseg_rows_df(K, soa, c->soadf.as<float>(), skip, npad, rows, nRows, partial, out, cnt, st);
+  }
   return use_fma(c) ? ddd::fast::launch_segseg_rows_f64(K, soa, skip, npad, rows, nRows, partial, out, cnt, st)
                     : ddd::strict::launch_segseg_rows_f64(K, soa, skip, npad, rows, nRows, partial, out, cnt, st);
 }
 
-cudaError_t run_sigma(const ddd_ctx* c, const ddd::KConsts& K, const double* soa, int64_t npad, int64_t nSeg,
+cudaError_t run_sigma(ddd_ctx* c, const ddd::KConsts& K, const double* soa, int64_t npad, int64_t nSeg,
                       const double* x0, int64_t M, double* sigma, cudaStream_t st) {
   return use_fma(c) ? ddd::fast::launch_sigma_f64(K, soa, npad, nSeg, x0, M, sigma, st)
                     : ddd::strict::launch_sigma_f64(K, soa, npad, nSeg, x0, M, sigma, st);
@@ -294,7 +312,7 @@ void ddd_destroy(ddd_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  for (DevBuf* b : {&c->coord, &c->bvec, &c->segidx, &c->ext, &c->soa, &c->skip, &c->partial, &c->out, &c->rows,
+  for (DevBuf* b : {&c->coord, &c->bvec, &c->segidx, &c->ext, &c->soa, &c->soadf, &c->skip, &c->partial, &c->out, &c->rows,
                     &c->x0, &c->sigma, &c->counters, &c->probe})
     b->release();
   for (auto& ev : c->ev)
@@ -495,7 +513,8 @@ int ddd_sigma_tilde_device(ddd_ctx* ctx, const ddd_consts* k, const double* x0, 
 int ddd_set_mode(ddd_ctx* ctx, int mode) {
   if (!ctx) return DDD_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
-  if (mode != DDD_MODE_FP64 && mode != DDD_MODE_FP64_FMA) return fail(ctx, DDD_EINVAL, "unknown mode");
+  if (mode != DDD_MODE_FP64 && mode != DDD_MODE_FP64_FMA && mode != DDD_MODE_DF64)
+    return fail(ctx, DDD_EINVAL, "unknown mode");
   ctx->mode = mode;
   return DDD_OK;
 }

@@ -29,7 +29,9 @@ struct KConsts;
                                      const int64_t* rows, int64_t nRows, double* partial, double* out, \
                                      unsigned long long* counters, cudaStream_t st); \
   cudaError_t launch_sigma_f64(const KConsts& K, const double* soa, int64_t npad, int64_t nSeg, const double* x0, \
-                               int64_t M, double* sigma, cudaStream_t st);
+                               int64_t M, double* sigma, cudaStream_t st); \
+  cudaError_t launch_reduce_all(const double* partial, int64_t npad, int64_t numSeg, double* out, cudaStream_t st); \
+  cudaError_t launch_reduce_rows(const double* partial, int64_t npad, int64_t nRows, double* out, cudaStream_t st);
 
 namespace strict {
 DDD_F64_DECLS
@@ -37,6 +39,17 @@ DDD_F64_DECLS
 namespace fast {
 DDD_F64_DECLS
 }
+
+// segseg_df.cu: the general branch in df64 (pairs of FP32) on the FP32 pipes,
+// near-parallel pairs and the cross-tile reduction in FP64 (strict).
+size_t segseg_df_soa_bytes(int64_t npad);
+cudaError_t launch_prep_df(const double* soa, int64_t npad, float* soadf, cudaStream_t st);
+cudaError_t launch_segseg_all_df(const KConsts& K, const double* soa, const float* soadf, const uint8_t* skip,
+                                 int64_t npad, double* partial, double* out, int64_t numSeg,
+                                 unsigned long long* counters, cudaStream_t st);
+cudaError_t launch_segseg_rows_df(const KConsts& K, const double* soa, const float* soadf, const uint8_t* skip,
+                                  int64_t npad, const int64_t* rows, int64_t nRows, double* partial, double* out,
+                                  unsigned long long* counters, cudaStream_t st);
 
 // probes.cu
 cudaError_t launch_fp64_peak_probe(double* sink, int iters, int blocks, int threads, cudaStream_t st);

@@ -444,6 +444,16 @@ static cudaError_t set_attr() {
   return cudaSuccess;
 }
 
+cudaError_t launch_reduce_all(const double* partial, int64_t npad, int64_t numSeg, double* out, cudaStream_t st) {
+  segseg_reduce_all<<<(unsigned)((numSeg + 127) / 128), 128, 0, st>>>(partial, npad / TILE, numSeg, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_reduce_rows(const double* partial, int64_t npad, int64_t nRows, double* out, cudaStream_t st) {
+  segseg_reduce_rows<<<(unsigned)((nRows + 127) / 128), 128, 0, st>>>(partial, npad / TILE, nRows, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_segseg_all_f64(const KConsts& K, const double* soa, const uint8_t* skip, int64_t npad,
                                   double* partial, double* out, int64_t numSeg, unsigned long long* counters,
                                   cudaStream_t st) {

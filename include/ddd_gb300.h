@@ -51,6 +51,13 @@ typedef struct ddd_ctx ddd_ctx;
  * algorithm's own Float64 noise). */
 #define DDD_MODE_FP64 0
 #define DDD_MODE_FP64_FMA 1
+/* DDD_MODE_DF64, the precision form of the seg-seg force: the general-branch
+ * pair arithmetic as double-float (pairs of FP32, ~48-bit significands) on the
+ * FP32 pipes; the near-parallel branch, the branch decision and the per-node
+ * accumulation stay FP64.  Its error is of the order of 2^6 times the FP64
+ * form's own rounding error (FP32-pair vs FP64 unit roundoff).  The field
+ * stress (ddd_sigma_tilde*) runs in DDD_MODE_FP64 arithmetic in this mode. */
+#define DDD_MODE_DF64 2
 
 /* Constants of the path.  The reference computes them in
  * MaterialParameters (src/Type/MaterialConstructor.jl:66-82) and

@@ -261,3 +261,25 @@ def test_fma_mode(pkg, synth, oracle, num_loops, seed):
     check_forces(F, oracle, k5_of(dln, mat), net, factor=(8, 6))
     S = pkg.calcSegSegForce(dln, mat, net)
     assert not np.array_equal(F, S)  # a different kernel ran
+
+
+@pytest.mark.parametrize("num_loops,seed,pf", [(64, 4, 0.05), (150, 5, 0.05), (96, 21, 0.5)])
+def test_df64_mode(pkg, synth, oracle, num_loops, seed, pf):
+    """DDD_MODE_DF64 (double-float general branch, FP64 near-parallel branch and
+    accumulation): its error is bounded by 2^6 x the FP64 arithmetic's own error
+    (the ratio of the two unit roundoffs), and pairs take the same branches."""
+    net = _synthetic(pkg, synth, num_loops, seed, parallel_fraction=pf, cube=3000.0)
+    dln, mat = _params(pkg)
+    ctx = pkg.get_context()
+    S = pkg.calcSegSegForce(dln, mat, net)
+    rep_s = dict(ctx.last_report)
+    ctx.mode = "df64"
+    try:
+        F = pkg.calcSegSegForce(dln, mat, net)
+        rep_d = dict(ctx.last_report)
+        Fi = pkg.calcSegSegForce(dln, mat, net, [3, 77, 77])
+    finally:
+        ctx.mode = "fp64"
+    assert (rep_d["pairs_general"], rep_d["pairs_parallel"]) == (rep_s["pairs_general"], rep_s["pairs_parallel"])
+    check_forces(F, oracle, k5_of(dln, mat), net, factor=(64, 64))
+    check_forces(Fi, oracle, k5_of(dln, mat), net, rows=[2, 76, 76], factor=(64, 64))
