@@ -373,8 +373,6 @@ def main():
                                                                    nrm(ref_rows))),
                "fp64_err_vs_longdouble": float(nrm(ref_force[:, :, rows] - ext_rows).max()),
                "reference_arith_err_vs_longdouble": float(nrm(ref_rows - ext_rows).max())}
-        for mode in variants:
-            pass
         line["parity_sample"] = par
     print(json.dumps(line), flush=True)
     if dist:
