@@ -255,7 +255,7 @@ def main():
     variants = {}
     ref_force = force.cpu().numpy().reshape(3, 2, -1, order="F")
     if not args.no_variants:
-        for mode in ("fp64_fma", "df64"):
+        for mode in ("fp64_fma", "df64", "f32c"):
             ctx.mode = mode
             out_v = torch.zeros_like(force)
             with torch.cuda.stream(stream):

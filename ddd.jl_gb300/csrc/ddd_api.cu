@@ -78,7 +78,8 @@ int cuda_fail(ddd_ctx* c, cudaError_t e, const char* where) {
 // and inverse length) always uses the strict build, so t and 1/|l| are the
 // reference's values in both modes.
 bool use_fma(const ddd_ctx* c) { return c->mode == DDD_MODE_FP64_FMA; }
-bool use_df(const ddd_ctx* c) { return c->mode == DDD_MODE_DF64; }
+bool use_df(const ddd_ctx* c) { return c->mode == DDD_MODE_DF64 || c->mode == DDD_MODE_F32C; }
+int df_form(const ddd_ctx* c) { return c->mode == DDD_MODE_F32C ? 1 : 0; }
 
 // For DDD_MODE_DF64 the df64 copy of the segment SoA is built first (ctx->soadf).
 cudaError_t prep_df_if_needed(ddd_ctx* c, int64_t npad, cudaStream_t st) {
@@ -93,7 +94,8 @@ cudaError_t run_segseg_all(ddd_ctx* c, const ddd::KConsts& K, const double* soa,
   if (use_df(c)) {
     cudaError_t e = prep_df_if_needed(c, npad, st);
     if (e != cudaSuccess) return e;
-    return ddd::launch_segseg_all_df(K, soa, c->soadf.as<float>(), skip, npad, partial, out, numSeg, cnt, st);
+    return ddd::launch_segseg_all_df(K, soa, c->soadf.as<float>(), skip, npad, partial, out, numSeg, cnt, st,
+                                     df_form(c));
   }
   return use_fma(c) ? ddd::fast::launch_segseg_all_f64(K, soa, skip, npad, partial, out, numSeg, cnt, st)
                     : ddd::strict::launch_segseg_all_f64(K, soa, skip, npad, partial, out, numSeg, cnt, st);
@@ -105,7 +107,8 @@ cudaError_t run_segseg_rows(ddd_ctx* c, const ddd::KConsts& K, const double* soa
   if (use_df(c)) {
     cudaError_t e = prep_df_if_needed(c, npad, st);
     if (e != cudaSuccess) return e;
-    return ddd::launch_segseg_rows_df(K, soa, c->soadf.as<float>(), skip, npad, rows, nRows, partial, out, cnt, st);
+    return ddd::launch_segseg_rows_df(K, soa, c->soadf.as<float>(), skip, npad, rows, nRows, partial, out, cnt, st,
+                                      df_form(c));
   }
   return use_fma(c) ? ddd::fast::launch_segseg_rows_f64(K, soa, skip, npad, rows, nRows, partial, out, cnt, st)
                     : ddd::strict::launch_segseg_rows_f64(K, soa, skip, npad, rows, nRows, partial, out, cnt, st);
@@ -513,7 +516,7 @@ int ddd_sigma_tilde_device(ddd_ctx* ctx, const ddd_consts* k, const double* x0, 
 int ddd_set_mode(ddd_ctx* ctx, int mode) {
   if (!ctx) return DDD_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
-  if (mode != DDD_MODE_FP64 && mode != DDD_MODE_FP64_FMA && mode != DDD_MODE_DF64)
+  if (mode != DDD_MODE_FP64 && mode != DDD_MODE_FP64_FMA && mode != DDD_MODE_DF64 && mode != DDD_MODE_F32C)
     return fail(ctx, DDD_EINVAL, "unknown mode");
   ctx->mode = mode;
   return DDD_OK;

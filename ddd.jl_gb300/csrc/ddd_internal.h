@@ -40,16 +40,17 @@ namespace fast {
 DDD_F64_DECLS
 }
 
-// segseg_df.cu: the general branch in df64 (pairs of FP32) on the FP32 pipes,
+// segseg_df.cu: the general branch in df64 (pairs of FP32) on the FP32 pipes
+// (form 0), or df64 corner integrals with FP32 assembly (form 1, mixed);
 // near-parallel pairs and the cross-tile reduction in FP64 (strict).
 size_t segseg_df_soa_bytes(int64_t npad);
 cudaError_t launch_prep_df(const double* soa, int64_t npad, float* soadf, cudaStream_t st);
 cudaError_t launch_segseg_all_df(const KConsts& K, const double* soa, const float* soadf, const uint8_t* skip,
                                  int64_t npad, double* partial, double* out, int64_t numSeg,
-                                 unsigned long long* counters, cudaStream_t st);
+                                 unsigned long long* counters, cudaStream_t st, int form);
 cudaError_t launch_segseg_rows_df(const KConsts& K, const double* soa, const float* soadf, const uint8_t* skip,
                                   int64_t npad, const int64_t* rows, int64_t nRows, double* partial, double* out,
-                                  unsigned long long* counters, cudaStream_t st);
+                                  unsigned long long* counters, cudaStream_t st, int form);
 
 // probes.cu
 cudaError_t launch_fp64_peak_probe(double* sink, int iters, int blocks, int threads, cudaStream_t st);

@@ -59,10 +59,10 @@ __device__ __forceinline__ double sgn(double v, unsigned long long sm) {
 }
 
 // SegSegInteg at one corner, added (sm = 0) or subtracted (sm = sign bit) into integ[19].
-__device__ __forceinline__ void seg_seg_integ_acc(double aSq, double d, double c, double cSq, double omcSq,
-                                                  double omcSqI, double x, double y, unsigned long long sm,
-                                                  double* integ) {
-  double aSq_dSq = aSq + d * d * omcSq;
+// aSq_dSq = aSq + d^2 (1 - c^2) and den = 1 / sqrt((1 - c^2) aSq_dSq) do not depend
+// on the corner; the caller computes them once per pair with the same operations.
+__device__ __forceinline__ void seg_seg_integ_acc(double aSq_dSq, double den, double c, double cSq, double omcSqI,
+                                                  double x, double y, unsigned long long sm, double* integ) {
   double xSq = x * x;
   double ySq = y * y;
   double Ra = sqrt(aSq_dSq + xSq + ySq + 2.0 * x * y * c);
@@ -83,8 +83,6 @@ __device__ __forceinline__ void seg_seg_integ_acc(double aSq, double d, double c
   double RaSq_R_t2_I = RaInv / Ra_Rd_t2;
   double yRaSq_R_t2_I = y * RaSq_R_t2_I;
   double ySqRaSq_R_t2_I = y * yRaSq_R_t2_I;
-
-  double den = 1.0 / sqrt(omcSq * aSq_dSq);
 
   double integ1 = -2.0 * den * atan((1.0 + c) * (Ra + x + y) * den);
 
@@ -196,13 +194,15 @@ __device__ __forceinline__ void general_pair(const KConsts& K, D3 b1, D3 n11, D3
   double integ[19];
 #pragma unroll
   for (int k = 0; k < 19; ++k) integ[k] = 0.0;
+  const double aSq_dSq = K.aSq + d * d * omcSq;
+  const double den = 1.0 / sqrt(omcSq * aSq_dSq);
   // ((I(x1,y1) - I(x1,y2)) - I(x2,y1)) + I(x2,y2), DislocationForces.jl:948-951.
 #pragma unroll 1
   for (int q = 0; q < 4; ++q) {
     double x = (q & 2) ? x2 : x1;
     double y = (q & 1) ? y2 : y1;
     unsigned long long sm = (q == 1 || q == 2) ? 0x8000000000000000ull : 0ull;
-    seg_seg_integ_acc(K.aSq, d, c, cSq, omcSq, omcSqI, x, y, sm, integ);
+    seg_seg_integ_acc(aSq_dSq, den, c, cSq, omcSqI, x, y, sm, integ);
   }
 
   D3 V[11];

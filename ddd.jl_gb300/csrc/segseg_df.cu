@@ -1,4 +1,4 @@
-// Precision form of the all-pairs and index-list seg-seg force: the general
+// Precision forms of the all-pairs and index-list seg-seg force: the general
 // branch (the bulk of the pair arithmetic, ~95% of pairs) in df64 — pairs of
 // FP32 on the FP32 pipes, ~48-bit significands — while FP64 is kept for
 //   * the near-parallel branch (calcParSegSegForce, the strict FP64 code),
@@ -91,9 +91,12 @@ __device__ __forceinline__ void add_df(float2& acc, df64 v) {
   acc.y = s.lo;
 }
 
-template <int MODE>
+// FORM 0: every general-pair operation in df64.  FORM 1 (mixed): the corner
+// antiderivatives and their moments in df64, V-vector assembly and node sums
+// in FP32 (general_pair_mixed).
+template <int MODE, int FORM>
 __global__ void __launch_bounds__(TILE, 2)
-segseg_tile_df(KConsts K64, KConstsDF K, const double* __restrict__ soa, const float* __restrict__ soadf,
+segseg_tile_df(KConsts K64, KConstsDF K, KConstsF KF, const double* __restrict__ soa, const float* __restrict__ soadf,
                const uint8_t* __restrict__ skipArr, int64_t npad, const int64_t* __restrict__ rows, int64_t nRows,
                int64_t nJt, double* __restrict__ partial, unsigned long long* __restrict__ counters) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -169,8 +172,12 @@ segseg_tile_df(KConsts K64, KConstsDF K, const double* __restrict__ soa, const f
       if (general) {
         DV3 F1, F2, F3, F4;
         if (MODE == 0) {
-          general_pair_df<true, true>(K, si.b, si.n1, si.n2, si.t, si.tN, sj.b, sj.n1, sj.n2, sj.t, sj.tN, c, F1,
-                                      F2, F3, F4);
+          if (FORM == 0)
+            general_pair_df<true, true>(K, si.b, si.n1, si.n2, si.t, si.tN, sj.b, sj.n1, sj.n2, sj.t, sj.tN, c, F1,
+                                        F2, F3, F4);
+          else
+            general_pair_mixed<true, true, true>(K, KF, f3(si.b), si.n1, si.n2, si.t, si.tN.hi, f3(sj.b), sj.n1,
+                                                 sj.n2, sj.t, sj.tN.hi, c, F1, F2, F3, F4);
           add_df(sm.fj[warp][0][jl], F3.x);
           add_df(sm.fj[warp][1][jl], F3.y);
           add_df(sm.fj[warp][2][jl], F3.z);
@@ -178,8 +185,12 @@ segseg_tile_df(KConsts K64, KConstsDF K, const double* __restrict__ soa, const f
           add_df(sm.fj[warp][4][jl], F4.y);
           add_df(sm.fj[warp][5][jl], F4.z);
         } else {
-          general_pair_df<true, false>(K, si.b, si.n1, si.n2, si.t, si.tN, sj.b, sj.n1, sj.n2, sj.t, sj.tN, c, F1,
-                                       F2, F3, F4);
+          if (FORM == 0)
+            general_pair_df<true, false>(K, si.b, si.n1, si.n2, si.t, si.tN, sj.b, sj.n1, sj.n2, sj.t, sj.tN, c, F1,
+                                         F2, F3, F4);
+          else
+            general_pair_mixed<true, false, true>(K, KF, f3(si.b), si.n1, si.n2, si.t, si.tN.hi, f3(sj.b), sj.n1,
+                                                  sj.n2, sj.t, sj.tN.hi, c, F1, F2, F3, F4);
         }
         fi1 = fi1 + F1;
         fi2 = fi2 + F2;
@@ -311,15 +322,19 @@ KConstsDF to_df(const KConsts& K) {
   return KConstsDF{s(K.aSq), s(K.mu4pi), s(K.mu4pinu), s(K.mu8piaSq), s(K.mu4pinuaSq)};
 }
 
-bool g_attr_df[2] = {false, false};
+KConstsF to_f(const KConsts& K) {
+  return KConstsF{(float)K.mu4pi, (float)K.mu4pinu, (float)K.mu8piaSq, (float)K.mu4pinuaSq};
+}
 
-template <int MODE>
+bool g_attr_df[2][2] = {{false, false}, {false, false}};
+
+template <int MODE, int FORM>
 cudaError_t set_attr_df() {
-  if (!g_attr_df[MODE]) {
-    cudaError_t e = cudaFuncSetAttribute(segseg_tile_df<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if (!g_attr_df[MODE][FORM]) {
+    cudaError_t e = cudaFuncSetAttribute(segseg_tile_df<MODE, FORM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)sizeof(TileSmemDF));
     if (e != cudaSuccess) return e;
-    g_attr_df[MODE] = true;
+    g_attr_df[MODE][FORM] = true;
   }
   return cudaSuccess;
 }
@@ -335,13 +350,17 @@ cudaError_t launch_prep_df(const double* soa, int64_t npad, float* soadf, cudaSt
 
 cudaError_t launch_segseg_all_df(const KConsts& K, const double* soa, const float* soadf, const uint8_t* skip,
                                  int64_t npad, double* partial, double* out, int64_t numSeg,
-                                 unsigned long long* counters, cudaStream_t st) {
-  cudaError_t e = set_attr_df<0>();
+                                 unsigned long long* counters, cudaStream_t st, int form) {
+  cudaError_t e = form ? set_attr_df<0, 1>() : set_attr_df<0, 0>();
   if (e != cudaSuccess) return e;
   const int64_t nt = npad / TILE;
   const int64_t nb = nt * (nt + 1) / 2;
-  segseg_tile_df<0><<<(unsigned)nb, TILE, sizeof(TileSmemDF), st>>>(K, to_df(K), soa, soadf, skip, npad, nullptr, 0,
-                                                                      0, partial, counters);
+  if (form)
+    segseg_tile_df<0, 1><<<(unsigned)nb, TILE, sizeof(TileSmemDF), st>>>(K, to_df(K), to_f(K), soa, soadf, skip, npad,
+                                                                         nullptr, 0, 0, partial, counters);
+  else
+    segseg_tile_df<0, 0><<<(unsigned)nb, TILE, sizeof(TileSmemDF), st>>>(K, to_df(K), to_f(K), soa, soadf, skip, npad,
+                                                                         nullptr, 0, 0, partial, counters);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   return strict::launch_reduce_all(partial, npad, numSeg, out, st);
@@ -349,13 +368,18 @@ cudaError_t launch_segseg_all_df(const KConsts& K, const double* soa, const floa
 
 cudaError_t launch_segseg_rows_df(const KConsts& K, const double* soa, const float* soadf, const uint8_t* skip,
                                   int64_t npad, const int64_t* rows, int64_t nRows, double* partial, double* out,
-                                  unsigned long long* counters, cudaStream_t st) {
-  cudaError_t e = set_attr_df<1>();
+                                  unsigned long long* counters, cudaStream_t st, int form) {
+  cudaError_t e = form ? set_attr_df<1, 1>() : set_attr_df<1, 0>();
   if (e != cudaSuccess) return e;
   const int64_t nJt = npad / TILE;
   const int64_t nrt = (nRows + TILE - 1) / TILE;
-  segseg_tile_df<1><<<(unsigned)(nrt * nJt), TILE, sizeof(TileSmemDF), st>>>(K, to_df(K), soa, soadf, skip, npad,
-                                                                              rows, nRows, nJt, partial, counters);
+  const unsigned grid = (unsigned)(nrt * nJt);
+  if (form)
+    segseg_tile_df<1, 1><<<grid, TILE, sizeof(TileSmemDF), st>>>(K, to_df(K), to_f(K), soa, soadf, skip, npad, rows,
+                                                                 nRows, nJt, partial, counters);
+  else
+    segseg_tile_df<1, 0><<<grid, TILE, sizeof(TileSmemDF), st>>>(K, to_df(K), to_f(K), soa, soadf, skip, npad, rows,
+                                                                 nRows, nJt, partial, counters);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   return strict::launch_reduce_rows(partial, npad, nRows, out, st);

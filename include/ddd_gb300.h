@@ -58,6 +58,13 @@ typedef struct ddd_ctx ddd_ctx;
  * form's own rounding error (FP32-pair vs FP64 unit roundoff).  The field
  * stress (ddd_sigma_tilde*) runs in DDD_MODE_FP64 arithmetic in this mode. */
 #define DDD_MODE_DF64 2
+/* DDD_MODE_F32C, the FP32 form with compensated terms: the integration-domain
+ * geometry, the four corner antiderivatives (their logs, arctangents, roots and
+ * quotients) and their first moments in double-float, where the formula
+ * cancels; the V-vector assembly and node sums in plain FP32; near-parallel
+ * branch, branch decision and per-node accumulation in FP64 as in
+ * DDD_MODE_DF64.  Measured node-force error ~5e-8 relative RMS. */
+#define DDD_MODE_F32C 3
 
 /* Constants of the path.  The reference computes them in
  * MaterialParameters (src/Type/MaterialConstructor.jl:66-82) and

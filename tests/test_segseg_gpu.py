@@ -289,3 +289,35 @@ def test_df64_mode(pkg, synth, oracle, num_loops, seed, pf):
     check_forces(Fi, oracle, k5_of(dln, mat), net, rows=[2, 76, 76], factor=(1000, 1000), normwise=1e-8)
     ext = oracle.segseg_ser_ld(k5_of(dln, mat), net, nthreads=os.cpu_count() or 1)
     assert np.linalg.norm(F - ext) <= 1e-8 * np.linalg.norm(ext)
+
+
+@pytest.mark.parametrize("num_loops,seed,pf,cube", [(64, 4, 0.05, 3000.0), (150, 5, 0.05, 3000.0),
+                                                    (300, 7, 0.05, 20000.0)])
+def test_f32c_mode(pkg, synth, oracle, num_loops, seed, pf, cube):
+    """DDD_MODE_F32C: df64 corner antiderivatives and moments, FP32 assembly.
+    Measured (the same code compiled for a CPU) ~5e-8 normwise relative error
+    against the long-double evaluation; bounds: normwise <= 2e-7, per node
+    |ΔF_n| <= 1e-4 |F_n| + 1e-6 max|F|; same branches as the FP64 kernel."""
+    net = _synthetic(pkg, synth, num_loops, seed, parallel_fraction=pf, cube=cube)
+    dln, mat = _params(pkg)
+    ctx = pkg.get_context()
+    pkg.calcSegSegForce(dln, mat, net)
+    rep_s = dict(ctx.last_report)
+    ctx.mode = "f32c"
+    try:
+        F = pkg.calcSegSegForce(dln, mat, net)
+        rep_c = dict(ctx.last_report)
+        Fi = pkg.calcSegSegForce(dln, mat, net, [5, 9, 9])
+    finally:
+        ctx.mode = "fp64"
+    assert (rep_c["pairs_general"], rep_c["pairs_parallel"]) == (rep_s["pairs_general"], rep_s["pairs_parallel"])
+    ext = oracle.segseg_ser_ld(k5_of(dln, mat), net, nthreads=os.cpu_count() or 1)
+    nrm = lambda a: np.linalg.norm(a, axis=0)
+    if os.environ.get("DDD_TEST_STATS"):
+        with open(os.environ["DDD_TEST_STATS"], "a") as fh:
+            fh.write("f32c n=%d normwise=%.3e max_node_over_max=%.3e\n" % (
+                net.numSeg, np.linalg.norm(F - ext) / np.linalg.norm(ext), nrm(F - ext).max() / nrm(ext).max()))
+    assert np.linalg.norm(F - ext) <= 2e-7 * np.linalg.norm(ext)
+    assert np.all(nrm(F - ext) <= 1e-4 * nrm(ext) + 1e-6 * nrm(ext).max())
+    exti = ext[:, :, [4, 8, 8]]
+    assert np.all(nrm(Fi - exti) <= 1e-4 * nrm(exti) + 1e-6 * nrm(ext).max())
