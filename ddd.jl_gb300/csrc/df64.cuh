@@ -6,7 +6,7 @@
 // Algorithms (published methods, restated):
 //   TwoSum (Knuth), FastTwoSum (Dekker), TwoProd via FMA;
 //   add / mul / div / sqrt as in Hida, Li & Bailey, "Library for double-double
-//   and quad-double arithmetic" (2001): the accurate (IEEE-style) addition,
+//   and quad-double arithmetic" (2001): the "sloppy" or IEEE-style addition,
 //   the FMA product, division by two Newton-style corrections, sqrt by one
 //   Newton step on an FP32 root;
 //   log: x = 2^e m, m reduced by a 64-entry table to m/c_j in [1 - 2^-7, 1 + 2^-7],
@@ -112,13 +112,23 @@ DF_HD double df_to_double(df64 a) { return (double)a.hi + (double)a.lo; }
 
 DF_HD df64 operator-(df64 a) { return {-a.hi, -a.lo}; }
 
+// Addition.  DDD_DF_ACCURATE_ADD selects the IEEE-style form (error relative to
+// the result); the default is the "sloppy" form (error <= ~2^-47 (|a| + |b|)),
+// which is as accurate as the operands themselves whenever they carry their own
+// rounding error of that size — every computed df64 value does.
 DF_HD df64 operator+(df64 a, df64 b) {
+#ifdef DDD_DF_ACCURATE_ADD
   df64 s = two_sum(a.hi, b.hi);
   df64 t = two_sum(a.lo, b.lo);
   s.lo += t.hi;
   s = fast_two_sum(s.hi, s.lo);
   s.lo += t.lo;
   return fast_two_sum(s.hi, s.lo);
+#else
+  df64 s = two_sum(a.hi, b.hi);
+  s.lo += a.lo + b.lo;
+  return fast_two_sum(s.hi, s.lo);
+#endif
 }
 DF_HD df64 operator-(df64 a, df64 b) { return a + (-b); }
 DF_HD df64 operator+(df64 a, float b) {
