@@ -180,6 +180,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-sigma", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--sigma-grid", type=int, default=32)
     args = ap.parse_args()
 
@@ -311,6 +312,37 @@ def main():
                  "config": "%d segments x %d points (%d^3 grid over the cube), FP64 strict" % (n, M, args.sigma_grid),
                  "frac_fp64_peak": evals * OPS_SIGMA_EVAL / (ms_sig * 1e-3) / fp64_peak}
 
+    # Batched form: 256 independent networks (segment counts log-uniform in
+    # [64, 8192], own seeds, cubes 2000-20000 b, slip-system subsets) in one
+    # persistent launch replayed from a CUDA graph.  The f32c plan is autotuned
+    # (tile 64/128 x work order); the FP64 plan uses the default tile 128.
+    batched = None
+    if not args.no_batched:
+        nets = synth.batch_networks(256, seed=0)
+        sizes = [p_.shape[0] * 8 for p_, _ in nets]
+        bsegs = torch.from_numpy(np.ascontiguousarray(np.concatenate([synth.packed_soa(p_, b_) for p_, b_ in nets],
+                                                                     axis=1))).cuda()
+        bforce = torch.zeros(6 * bsegs.shape[1], dtype=torch.float64, device="cuda")
+        bpairs = sum(n_ * (n_ - 1) // 2 for n_ in sizes)
+        batched = {"networks": len(sizes), "segments": int(sum(sizes)), "pairs_per_run": int(bpairs)}
+        for mode, tune in (("f32c", True), ("fp64", False)):
+            plan = pkg.Batch(ctx, sizes, mode=mode, tune=tune)
+            with torch.cuda.stream(stream):
+                plan.run(k, bsegs.data_ptr(), bforce.data_ptr(), stream=sptr)  # tune (if asked) + graph capture
+                torch.cuda.synchronize()
+                a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a_.record(stream)
+                for _ in range(2):
+                    plan.run(k, bsegs.data_ptr(), bforce.data_ptr(), stream=sptr)
+                b_.record(stream)
+                torch.cuda.synchronize()
+            ms_b = a_.elapsed_time(b_) / 2
+            inf = plan.info()
+            batched[mode] = {"value": bpairs / (ms_b * 1e-3), "unit": "pair-interactions/s", "ms_per_run": ms_b,
+                             "tile": inf["tile"], "order": inf["order"], "work_items": inf["work_items"],
+                             "tune_ms": inf["tune_ms"] if tune else None, "graph_launches": inf["graph_launches"]}
+            plan.close()
+
     # End to end through the reference-facing C-ABI call with host arrays.
     coord, bvec, seg = synth.network_arrays(p, b)
     net = pkg.DislocationNetwork(coord, bvec, seg)
@@ -354,6 +386,7 @@ def main():
         "mode": "fp64 (strict: every multiply and add rounded separately, as the reference)",
         "variants": variants,
         "sigma_tilde": sigma,
+        "batched": batched,
         "kernel_ms_per_step": statistics.mean(ms_kernel),
     }
     cs = clocks.summary()

@@ -33,6 +33,7 @@ EXPORTED_SYMBOLS = (
     "ddd_segseg_force", "ddd_segseg_force_inplace", "ddd_sigma_tilde",
     "ddd_segseg_force_device", "ddd_sigma_tilde_device", "ddd_set_mode", "ddd_get_mode", "ddd_probe_fma_peak",
     "ddd_segseg_force_device_noalloc",
+    "ddd_batch_create", "ddd_batch_run", "ddd_batch_info", "ddd_batch_last_error", "ddd_batch_destroy",
 )
 
 # Arithmetic modes (ddd_set_mode).
@@ -49,6 +50,17 @@ class DDDError(RuntimeError):
 class ddd_consts(ctypes.Structure):
     _fields_ = [("aSq", ctypes.c_double), ("mu4pi", ctypes.c_double), ("mu8pi", ctypes.c_double),
                 ("mu4pinu", ctypes.c_double), ("nuMu4pinu", ctypes.c_double)]
+
+
+class ddd_batch_info_t(ctypes.Structure):
+    _fields_ = [("tile", ctypes.c_int), ("order", ctypes.c_int), ("work_items", ctypes.c_int64),
+                ("total_segments", ctypes.c_int64), ("graph_launches", ctypes.c_int64),
+                ("tune_ms", ctypes.c_double * 4)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "tune_ms"}
+        d["tune_ms"] = list(self.tune_ms)
+        return d
 
 
 class ddd_report(ctypes.Structure):
@@ -101,6 +113,14 @@ def library():
         L.ddd_segseg_force_device.argtypes = [_vp, cp, _vp, _i64, _vp, _i64, _vp, _vp, rp]
         L.ddd_sigma_tilde_device.argtypes = [_vp, cp, _vp, _i64, _vp, _i64, _i64, _vp, _vp, rp]
         L.ddd_segseg_force_device_noalloc.argtypes = [cp, _vp, _i64, _vp, _i64, _vp, _vp]
+        L.ddd_batch_create.argtypes = [_vp, _i64, _ip, ctypes.c_int, ctypes.c_int]
+        L.ddd_batch_create.restype = _vp
+        L.ddd_batch_run.argtypes = [_vp, cp, _vp, _vp, _vp, _vp]
+        L.ddd_batch_info.argtypes = [_vp, ctypes.POINTER(ddd_batch_info_t)]
+        L.ddd_batch_last_error.argtypes = [_vp]
+        L.ddd_batch_last_error.restype = ctypes.c_char_p
+        L.ddd_batch_destroy.argtypes = [_vp]
+        L.ddd_batch_destroy.restype = None
         L.ddd_set_mode.argtypes = [_vp, ctypes.c_int]
         L.ddd_get_mode.argtypes = [_vp]
         L.ddd_probe_fma_peak.argtypes = [_vp, ctypes.c_int, _dp]
@@ -311,6 +331,42 @@ class Context:
         v = ctypes.c_double(0)
         self._check(self._L.ddd_probe_fma_peak(self._h, int(precision), ctypes.byref(v)))
         return v.value
+
+
+class Batch:
+    """A batch plan (ddd_batch_*): many networks, one persistent launch in a CUDA graph."""
+
+    def __init__(self, ctx, num_seg, mode="fp64", tune=False):
+        self._L = ctx._L
+        self.ctx = ctx
+        sizes = np.ascontiguousarray(num_seg, dtype=np.int64)
+        m = MODES.get(mode, mode) if isinstance(mode, str) else int(mode)
+        self._h = self._L.ddd_batch_create(ctx._h, len(sizes), sizes.ctypes.data_as(_ip), m, 1 if tune else 0)
+        if not self._h:
+            raise DDDError(DDD_EINVAL, "ddd_batch_create failed (sizes or mode)")
+        self.num_seg = sizes
+        self.total = int(sizes.sum())
+
+    def run(self, k, segs_ptr, force_ptr, ext_ptr=None, stream=None):
+        rc = self._L.ddd_batch_run(self._h, ctypes.byref(k), segs_ptr, ext_ptr, force_ptr, stream)
+        if rc != DDD_OK:
+            raise DDDError(rc, self._L.ddd_batch_last_error(self._h).decode())
+
+    def info(self):
+        i = ddd_batch_info_t()
+        self._L.ddd_batch_info(self._h, ctypes.byref(i))
+        return i.as_dict()
+
+    def close(self):
+        if self._h:
+            self._L.ddd_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 _contexts = {}

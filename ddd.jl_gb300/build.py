@@ -24,6 +24,7 @@ VARIANTS = {
     "sigma_f64.cu": [("strict", ["-DDDD_VARIANT=strict", "--fmad=false"]), ("fast", ["-DDDD_VARIANT=fast"])],
     # df64 needs exact error-free transformations: no contraction.
     "segseg_df.cu": [("", ["--fmad=false"])],
+    "segseg_batch.cu": [("", ["--fmad=false"])],
 }
 
 

@@ -56,6 +56,8 @@ struct ddd_ctx {
   std::vector<double> hostTmp;
 };
 
+int ddd::ctx_device(const ddd_ctx* c) { return c->device; }
+
 namespace {
 
 int fail(ddd_ctx* c, int code, const std::string& msg) {

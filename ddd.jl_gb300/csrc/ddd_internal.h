@@ -5,6 +5,8 @@
 #include <cstddef>
 #include <cstdint>
 
+struct ddd_ctx;
+
 namespace ddd {
 
 struct KConsts;
@@ -51,6 +53,9 @@ cudaError_t launch_segseg_all_df(const KConsts& K, const double* soa, const floa
 cudaError_t launch_segseg_rows_df(const KConsts& K, const double* soa, const float* soadf, const uint8_t* skip,
                                   int64_t npad, const int64_t* rows, int64_t nRows, double* partial, double* out,
                                   unsigned long long* counters, cudaStream_t st, int form);
+
+// ddd_api.cu: context accessors for the other C-ABI files.
+int ctx_device(const ddd_ctx* c);
 
 // probes.cu
 cudaError_t launch_fp64_peak_probe(double* sink, int iters, int blocks, int threads, cudaStream_t st);

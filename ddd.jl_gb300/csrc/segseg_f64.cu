@@ -24,6 +24,7 @@
 
 #include "ddd_internal.h"
 #include "pair_f64.cuh"
+#include "tile_body.cuh"
 
 // This file is compiled twice: DDD_VARIANT=strict with --fmad=false (every
 // multiply and add rounded separately, as the reference's Julia code does) and
@@ -36,8 +37,6 @@ namespace ddd {
 namespace DDD_VARIANT {
 
 constexpr int TILE = 128;
-constexpr int NWARP = TILE / 32;
-constexpr int CHUNK = TILE;  // near-parallel pairs evaluated per round
 
 // ---------------------------------------------------------------------------
 // Gather the caller's network arrays (Julia column-major, 1-based) into the
@@ -107,35 +106,6 @@ __global__ void prep_segments_packed(const double* __restrict__ in, int64_t ldIn
   skip[i] = sk;
 }
 
-__device__ __forceinline__ SegF64 load_seg_global(const double* __restrict__ soa, int64_t npad, int64_t i) {
-  SegF64 s;
-  s.n1 = {soa[i], soa[npad + i], soa[2 * npad + i]};
-  s.n2 = {soa[3 * npad + i], soa[4 * npad + i], soa[5 * npad + i]};
-  s.b = {soa[6 * npad + i], soa[7 * npad + i], soa[8 * npad + i]};
-  s.t = {soa[9 * npad + i], soa[10 * npad + i], soa[11 * npad + i]};
-  s.tN = soa[12 * npad + i];
-  return s;
-}
-
-struct TileSmem {
-  double seg[13][TILE];           // J tile, SoA
-  double fj[NWARP][6][TILE];      // per-warp j-side forces
-  double cf[CHUNK][12];           // near-parallel chunk results
-  uint16_t plist[TILE * TILE];    // near-parallel list: (i_local << 8) | j_local
-  int cnt[TILE];                  // near-parallel count per i thread (prefix-summed)
-  uint8_t skip[TILE];
-};
-
-__device__ __forceinline__ SegF64 load_seg_smem(const TileSmem& sm, int j) {
-  SegF64 s;
-  s.n1 = {sm.seg[0][j], sm.seg[1][j], sm.seg[2][j]};
-  s.n2 = {sm.seg[3][j], sm.seg[4][j], sm.seg[5][j]};
-  s.b = {sm.seg[6][j], sm.seg[7][j], sm.seg[8][j]};
-  s.t = {sm.seg[9][j], sm.seg[10][j], sm.seg[11][j]};
-  s.tN = sm.seg[12][j];
-  return s;
-}
-
 __device__ __forceinline__ void tile_index(int64_t b, int64_t& I, int64_t& J) {
   // b enumerates (I <= J) column by column: J-th column holds I = 0..J.
   int64_t Jc = (int64_t)((sqrt(8.0 * (double)b + 1.0) - 1.0) * 0.5);
@@ -145,17 +115,14 @@ __device__ __forceinline__ void tile_index(int64_t b, int64_t& I, int64_t& J) {
   I = b - Jc * (Jc + 1) / 2;
 }
 
-// MODE 0: all pairs (symmetric, i < j).  MODE 1: index rows (all j != i, F12 only).
+// MODE 0: all pairs (symmetric, i < j), one CTA per tile pair I <= J.
+// MODE 1: index rows (all j != i, F12 only), one CTA per (row tile, column tile).
 template <int MODE>
 __global__ void __launch_bounds__(TILE, 2)
-segseg_tile_f64(KConsts K, const double* __restrict__ soa, const uint8_t* __restrict__ skipArr, int64_t npad,
-                const int64_t* __restrict__ rows, int64_t nRows, int64_t nJt, double* __restrict__ partial,
+segseg_tile_f64(TileArgs A, const int64_t* __restrict__ rows, int64_t nRows, int64_t nJt, double* __restrict__ partial,
                 unsigned long long* __restrict__ counters) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  TileSmem& sm = *reinterpret_cast<TileSmem*>(smem_raw);
-  const int t = threadIdx.x;
-  const int warp = t >> 5;
-
+  auto& sm = *reinterpret_cast<TileSmemT<TILE, PolF64>*>(smem_raw);
   int64_t I, J;
   if (MODE == 0) {
     tile_index(blockIdx.x, I, J);
@@ -163,201 +130,8 @@ segseg_tile_f64(KConsts K, const double* __restrict__ soa, const uint8_t* __rest
     I = blockIdx.x / nJt;
     J = blockIdx.x % nJt;
   }
-  const bool diag = (MODE == 0) && (I == J);
-
-  // Row segment of this thread.
-  int64_t gi;
-  bool iActive;
-  if (MODE == 0) {
-    gi = I * TILE + t;
-    iActive = skipArr[gi] == 0;
-  } else {
-    int64_t r = I * TILE + t;
-    iActive = r < nRows;
-    gi = iActive ? rows[r] : 0;
-    iActive = iActive && skipArr[gi] == 0;
-  }
-  SegF64 si = load_seg_global(soa, npad, gi);
-
-  // J tile into shared memory.
-  const int64_t j0 = J * TILE;
-#pragma unroll
-  for (int k = 0; k < 13; ++k) sm.seg[k][t] = soa[k * npad + j0 + t];
-  sm.skip[t] = skipArr[j0 + t];
-#pragma unroll
-  for (int w = 0; w < NWARP; ++w)
-#pragma unroll
-    for (int c = 0; c < 6; ++c) sm.fj[w][c][t] = 0.0;
-  __syncthreads();
-
-  D3 fi1 = {0, 0, 0}, fi2 = {0, 0, 0};
-  uint32_t pmask[TILE / 32] = {0, 0, 0, 0};
-  unsigned long long nGeneral = 0;
-
-  // ---- Sweep: general pairs now, near-parallel pairs flagged. ----
-  for (int k = 0; k < TILE; ++k) {
-    const int jl = (t + k) & (TILE - 1);
-    bool act = iActive && sm.skip[jl] == 0;
-    if (MODE == 0) act = act && (!diag || jl > t);
-    if (MODE == 1) act = act && (j0 + jl != gi);
-    if (act) {
-      SegF64 sj = load_seg_smem(sm, jl);
-      double c = dot(si.t, sj.t);
-      double omcSq = 1.0 - c * c;
-      if (omcSq > kSqrtEps) {
-        D3 F1, F2, F3, F4;
-        if (MODE == 0) {
-          general_pair<true, true>(K, si.b, si.n1, si.n2, si.t, si.tN, sj.b, sj.n1, sj.n2, sj.t, sj.tN, c, F1, F2,
-                                   F3, F4);
-          double* fj = &sm.fj[warp][0][0];
-          fj[0 * TILE + jl] += F3.x;
-          fj[1 * TILE + jl] += F3.y;
-          fj[2 * TILE + jl] += F3.z;
-          fj[3 * TILE + jl] += F4.x;
-          fj[4 * TILE + jl] += F4.y;
-          fj[5 * TILE + jl] += F4.z;
-        } else {
-          general_pair<true, false>(K, si.b, si.n1, si.n2, si.t, si.tN, sj.b, sj.n1, sj.n2, sj.t, sj.tN, c, F1, F2,
-                                    F3, F4);
-        }
-        fi1 = fi1 + F1;
-        fi2 = fi2 + F2;
-        ++nGeneral;
-      } else {
-        pmask[jl >> 5] |= 1u << (jl & 31);
-      }
-    }
-    __syncwarp();
-  }
-
-  // ---- Near-parallel pairs: compact, then evaluate densely. ----
-  int myCnt = __popc(pmask[0]) + __popc(pmask[1]) + __popc(pmask[2]) + __popc(pmask[3]);
-  sm.cnt[t] = myCnt;
-  __syncthreads();
-  // Exclusive scan over 128 counts (one warp, deterministic).
-  if (warp == 0) {
-    int v[4];
-    int s = 0;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      v[q] = sm.cnt[4 * t + q];
-      s += v[q];
-    }
-    int incl = s;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      int n = __shfl_up_sync(0xffffffffu, incl, o);
-      if ((t & 31) >= o) incl += n;
-    }
-    int excl = incl - s;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      sm.cnt[4 * t + q] = excl;
-      excl += v[q];
-    }
-  }
-  __syncthreads();
-  const int myOff = sm.cnt[t];
-  // Total = offset of the last thread + its own count.
-  __shared__ int sTotal;
-  if (t == TILE - 1) sTotal = myOff + myCnt;
-  {
-    int o = myOff;
-    for (int k = 0; k < TILE; ++k) {
-      const int jl = (t + k) & (TILE - 1);
-      if (pmask[jl >> 5] & (1u << (jl & 31))) sm.plist[o++] = (uint16_t)((t << 8) | jl);
-    }
-  }
-  __syncthreads();
-  const int nPar = sTotal;
-  D3 fjp3 = {0, 0, 0}, fjp4 = {0, 0, 0};  // near-parallel forces on j = t
-  unsigned long long nCore = 0;
-  for (int base = 0; base < nPar; base += CHUNK) {
-    const int e = base + t;
-    if (e < nPar) {
-      const int il = sm.plist[e] >> 8, jl = sm.plist[e] & 0xff;
-      SegF64 a, b;
-      if (MODE == 0) {
-        a = load_seg_global(soa, npad, I * TILE + il);
-      } else {
-        a = load_seg_global(soa, npad, rows[I * TILE + il]);
-      }
-      b = load_seg_smem(sm, jl);
-      double c = dot(a.t, b.t);
-      D3 F1, F2, F3 = {0, 0, 0}, F4 = {0, 0, 0};
-      if (MODE == 0)
-        nCore += parallel_pair<true>(K, a.b, a.n1, a.n2, a.t, a.tN, b.b, b.n1, b.n2, b.t, b.tN, c, F1, F2, F3, F4);
-      else
-        nCore += parallel_pair<false>(K, a.b, a.n1, a.n2, a.t, a.tN, b.b, b.n1, b.n2, b.t, b.tN, c, F1, F2, F3, F4);
-      sm.cf[t][0] = F1.x; sm.cf[t][1] = F1.y; sm.cf[t][2] = F1.z;
-      sm.cf[t][3] = F2.x; sm.cf[t][4] = F2.y; sm.cf[t][5] = F2.z;
-      sm.cf[t][6] = F3.x; sm.cf[t][7] = F3.y; sm.cf[t][8] = F3.z;
-      sm.cf[t][9] = F4.x; sm.cf[t][10] = F4.y; sm.cf[t][11] = F4.z;
-    }
-    __syncthreads();
-    const int lim = min(CHUNK, nPar - base);
-    // i-side: this thread's entries are contiguous in the list.
-    int lo = max(myOff, base), hi = min(myOff + myCnt, base + lim);
-    for (int e2 = lo; e2 < hi; ++e2) {
-      const double* f = sm.cf[e2 - base];
-      fi1 = fi1 + D3{f[0], f[1], f[2]};
-      fi2 = fi2 + D3{f[3], f[4], f[5]};
-    }
-    if (MODE == 0) {
-      // j-side: scan the chunk for entries whose j is this thread's slot.
-      for (int q = 0; q < lim; ++q) {
-        if ((sm.plist[base + q] & 0xff) == t) {
-          const double* f = sm.cf[q];
-          fjp3 = fjp3 + D3{f[6], f[7], f[8]};
-          fjp4 = fjp4 + D3{f[9], f[10], f[11]};
-        }
-      }
-    }
-    __syncthreads();
-  }
-
-  // ---- Write partials: [block][side][6][TILE], side 0 = row tile, 1 = col tile. ----
-  double* p = partial + (int64_t)blockIdx.x * (MODE == 0 ? 12 : 6) * TILE;
-  p[0 * TILE + t] = fi1.x;
-  p[1 * TILE + t] = fi1.y;
-  p[2 * TILE + t] = fi1.z;
-  p[3 * TILE + t] = fi2.x;
-  p[4 * TILE + t] = fi2.y;
-  p[5 * TILE + t] = fi2.z;
-  if (MODE == 0) {
-    double acc[6];
-#pragma unroll
-    for (int c = 0; c < 6; ++c) {
-      double s = sm.fj[0][c][t];
-#pragma unroll
-      for (int w = 1; w < NWARP; ++w) s += sm.fj[w][c][t];
-      acc[c] = s;
-    }
-    acc[0] += fjp3.x;
-    acc[1] += fjp3.y;
-    acc[2] += fjp3.z;
-    acc[3] += fjp4.x;
-    acc[4] += fjp4.y;
-    acc[5] += fjp4.z;
-#pragma unroll
-    for (int c = 0; c < 6; ++c) p[(6 + c) * TILE + t] = acc[c];
-  }
-
-  // Branch statistics: pairs on the general path, pairs on the near-parallel
-  // path, near-parallel sides that needed the two core-correction evaluations.
-  if (counters) {
-    unsigned long long g = nGeneral, cc = nCore;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      g += __shfl_down_sync(0xffffffffu, g, o);
-      cc += __shfl_down_sync(0xffffffffu, cc, o);
-    }
-    if ((t & 31) == 0) {
-      atomicAdd(&counters[0], g);
-      atomicAdd(&counters[2], cc);
-    }
-    if (t == 0) atomicAdd(&counters[1], (unsigned long long)nPar);
-  }
+  tile_body<TILE, MODE, PolF64>(A, PolF64::Consts{}, sm, I * TILE, J * TILE, MODE == 0 && I == J, rows, nRows,
+                                partial + (int64_t)blockIdx.x * (MODE == 0 ? 12 : 6) * TILE, counters);
 }
 
 // Sum the partial blocks of each segment in a fixed order and write the
@@ -437,7 +211,7 @@ template <int MODE>
 static cudaError_t set_attr() {
   if (!g_attr_set[MODE]) {
     cudaError_t e = cudaFuncSetAttribute(segseg_tile_f64<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sizeof(TileSmem));
+                                         (int)sizeof(TileSmemT<TILE, PolF64>));
     if (e != cudaSuccess) return e;
     g_attr_set[MODE] = true;
   }
@@ -461,8 +235,9 @@ cudaError_t launch_segseg_all_f64(const KConsts& K, const double* soa, const uin
   if (e != cudaSuccess) return e;
   const int64_t nt = npad / TILE;
   const int64_t nb = nt * (nt + 1) / 2;
-  segseg_tile_f64<0><<<(unsigned)nb, TILE, sizeof(TileSmem), st>>>(K, soa, skip, npad, nullptr, 0, 0, partial,
-                                                                    counters);
+  const TileArgs A{K, soa, skip, npad, nullptr, nullptr};
+  segseg_tile_f64<0><<<(unsigned)nb, TILE, sizeof(TileSmemT<TILE, PolF64>), st>>>(A, nullptr, 0, 0, partial,
+                                                                                  counters);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   segseg_reduce_all<<<(unsigned)((numSeg + 127) / 128), 128, 0, st>>>(partial, nt, numSeg, out);
@@ -476,8 +251,9 @@ cudaError_t launch_segseg_rows_f64(const KConsts& K, const double* soa, const ui
   if (e != cudaSuccess) return e;
   const int64_t nJt = npad / TILE;
   const int64_t nrt = (nRows + TILE - 1) / TILE;
-  segseg_tile_f64<1><<<(unsigned)(nrt * nJt), TILE, sizeof(TileSmem), st>>>(K, soa, skip, npad, rows, nRows, nJt,
-                                                                             partial, counters);
+  const TileArgs A{K, soa, skip, npad, nullptr, nullptr};
+  segseg_tile_f64<1><<<(unsigned)(nrt * nJt), TILE, sizeof(TileSmemT<TILE, PolF64>), st>>>(A, rows, nRows, nJt,
+                                                                                           partial, counters);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   segseg_reduce_rows<<<(unsigned)((nRows + 127) / 128), 128, 0, st>>>(partial, nJt, nRows, out);

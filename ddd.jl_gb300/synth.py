@@ -127,3 +127,20 @@ def make(config, seed=0, num_loops=None):
     p, b = square_loops(cfg["num_loops"], seed, cfg["lmin"], cfg["lmax"], cfg["cube"], cfg["shear_fraction"],
                         cfg["parallel_fraction"])
     return p, b, cfg
+
+
+def batch_networks(num_networks=256, seed=0, nmin=64, nmax=8192):
+    """Independent networks for the batched form: segment counts log-uniform in
+    [nmin, nmax] (rounded to whole 8-segment loops), each with its own seed, its
+    own cube edge uniform in [2000, 20000] b and a random subset of the 12 slip
+    systems; same loop generator otherwise.  Returns a list of (p, b)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(num_networks):
+        n = int(np.exp(rng.uniform(np.log(nmin), np.log(nmax))))
+        loops = max(1, n // 8)
+        cube = rng.uniform(2000.0, 20000.0)
+        subset = np.sort(rng.choice(12, rng.integers(1, 13), replace=False))
+        p, b = square_loops(loops, int(rng.integers(1 << 31)), 20.0, 200.0, cube, 0.5, 0.05, slip_subset=subset)
+        out.append((p, b))
+    return out

@@ -164,6 +164,36 @@ int ddd_sigma_tilde_device(ddd_ctx* ctx, const ddd_consts* k, const double* x0, 
 int ddd_segseg_force_device_noalloc(const ddd_consts* k, const double* segs, int64_t ldSegs, const uint8_t* ext,
                                     int64_t numSeg, double* force, void* stream);
 
+/* Batched form (no reference counterpart: the reference evaluates one network
+ * per call).  Many independent networks of uneven sizes in one persistent
+ * launch replayed from a captured CUDA graph.  A batch plan is made for a list
+ * of network sizes and a mode (DDD_MODE_FP64, DDD_MODE_DF64 or DDD_MODE_F32C);
+ * with tune != 0 its first run times the candidate tile sizes (64, 128) and
+ * work orders on the actual inputs and keeps the fastest (remembered per size
+ * list and mode for the rest of the process).  Inputs: all networks
+ * concatenated as one packed 9 × sum(numSeg) device array (rows n1 n2 b,
+ * network n in consecutive columns), ext (device, may be NULL); output the
+ * forces in the same order (3 × 2 × sum(numSeg), device).  The first run with a
+ * given (consts, segs, ext, force, stream) captures the work into a CUDA graph;
+ * later runs with the same arguments replay it.  Runs are asynchronous on
+ * `stream` (NULL = the plan's own stream).  A plan must not be run
+ * concurrently with itself. */
+typedef struct ddd_batch ddd_batch;
+typedef struct ddd_batch_info_t {
+  int tile;                /* chosen tile size (segments per side) */
+  int order;               /* chosen work order: 0 network order, 1 largest networks first */
+  int64_t work_items;      /* tile pairs in the chosen layout */
+  int64_t total_segments;  /* sum of numSeg */
+  int64_t graph_launches;  /* runs replayed from the captured graph */
+  double tune_ms[4];       /* timings of (128, largest first), (128, network order), (64, …), (64, …); -1 if untuned */
+} ddd_batch_info_t;
+ddd_batch* ddd_batch_create(ddd_ctx* ctx, int64_t nNet, const int64_t* numSeg, int mode, int tune);
+int ddd_batch_run(ddd_batch* b, const ddd_consts* k, const double* segs, const uint8_t* ext, double* force,
+                  void* stream);
+int ddd_batch_info(const ddd_batch* b, ddd_batch_info_t* out);
+const char* ddd_batch_last_error(const ddd_batch* b);
+void ddd_batch_destroy(ddd_batch* b);
+
 /* Select / query the arithmetic mode of ctx (DDD_MODE_*).  No reference
  * counterpart: the reference's dispatch flags are parCPU / parGPU only. */
 int ddd_set_mode(ddd_ctx* ctx, int mode);
