@@ -24,6 +24,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libddd_gb300.so")
 
 DDD_OK, DDD_EINVAL, DDD_ERANGE, DDD_ENONFINITE, DDD_EDEVICE, DDD_ENOMEM, DDD_ETOOBIG = 0, -1, -2, -3, -4, -5, -6
+DDD_ETIMEOUT = -7
 # Largest network ddd_segseg_force_device_noalloc accepts (include/ddd_gb300.h).
 NOALLOC_MAX_SEGMENTS = 4096
 
@@ -34,6 +35,7 @@ EXPORTED_SYMBOLS = (
     "ddd_segseg_force_device", "ddd_sigma_tilde_device", "ddd_set_mode", "ddd_get_mode", "ddd_probe_fma_peak",
     "ddd_segseg_force_device_noalloc",
     "ddd_batch_create", "ddd_batch_run", "ddd_batch_info", "ddd_batch_last_error", "ddd_batch_destroy",
+    "ddd_tc_gemm_bf16",
 )
 
 # Arithmetic modes (ddd_set_mode).
@@ -121,6 +123,7 @@ def library():
         L.ddd_batch_last_error.restype = ctypes.c_char_p
         L.ddd_batch_destroy.argtypes = [_vp]
         L.ddd_batch_destroy.restype = None
+        L.ddd_tc_gemm_bf16.argtypes = [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp]
         L.ddd_set_mode.argtypes = [_vp, ctypes.c_int]
         L.ddd_get_mode.argtypes = [_vp]
         L.ddd_probe_fma_peak.argtypes = [_vp, ctypes.c_int, _dp]
@@ -326,6 +329,10 @@ class Context:
     @mode.setter
     def mode(self, m):
         self._check(self._L.ddd_set_mode(self._h, MODES.get(m, m) if isinstance(m, str) else int(m)))
+
+    def tc_gemm_bf16(self, M, N, K, a_ptr, b_ptr, d_ptr, stream=None):
+        """D[M×N] fp32 = A[M×K] · B[N×K]^T on tcgen05 (device pointers)."""
+        self._check(self._L.ddd_tc_gemm_bf16(self._h, M, N, K, a_ptr, b_ptr, d_ptr, stream))
 
     def probe_fma_peak(self, precision=64):
         v = ctypes.c_double(0)

@@ -52,7 +52,7 @@ struct ddd_ctx {
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   std::mutex mu;
   std::string err;
-  DevBuf coord, bvec, segidx, ext, soa, soadf, skip, partial, out, rows, x0, sigma, counters, probe;
+  DevBuf coord, bvec, segidx, ext, soa, soadf, skip, partial, out, rows, x0, sigma, counters, probe, errflag;
   std::vector<double> hostTmp;
 };
 
@@ -318,7 +318,7 @@ void ddd_destroy(ddd_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (DevBuf* b : {&c->coord, &c->bvec, &c->segidx, &c->ext, &c->soa, &c->soadf, &c->skip, &c->partial, &c->out, &c->rows,
-                    &c->x0, &c->sigma, &c->counters, &c->probe})
+                    &c->x0, &c->sigma, &c->counters, &c->probe, &c->errflag})
     b->release();
   for (auto& ev : c->ev)
     if (ev) cudaEventDestroy(ev);
@@ -525,6 +525,25 @@ int ddd_set_mode(ddd_ctx* ctx, int mode) {
 }
 
 int ddd_get_mode(const ddd_ctx* ctx) { return ctx ? ctx->mode : DDD_EINVAL; }
+
+int ddd_tc_gemm_bf16(ddd_ctx* ctx, int M, int N, int K, const void* A, const void* B, float* D, void* stream) {
+  if (!ctx) return DDD_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (M <= 0 || M % 128 || N < 16 || N > 256 || N % 16 || K <= 0 || K % 16)
+    return fail(ctx, DDD_EINVAL, "shape must be M % 128 == 0, N in [16, 256] multiple of 16, K multiple of 16");
+  if (!A || !B || !D) return fail(ctx, DDD_EINVAL, "null pointer");
+  if (((uintptr_t)A | (uintptr_t)B) & 15) return fail(ctx, DDD_EINVAL, "A and B must be 16-byte aligned");
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  CK(ctx->errflag.ensure(sizeof(int)), "alloc error flag");
+  CK(cudaMemsetAsync(ctx->errflag.p, 0, sizeof(int), st), "memset");
+  CK(ddd::launch_tc_gemm_bf16(M, N, K, A, B, D, ctx->errflag.as<int>(), st), "tc_gemm_bf16");
+  int flag = 0;
+  CK(cudaMemcpyAsync(&flag, ctx->errflag.p, sizeof(int), cudaMemcpyDeviceToHost, st), "copy flag");
+  CK(cudaStreamSynchronize(st), "tc_gemm_bf16");
+  if (flag) return fail(ctx, DDD_ETIMEOUT, "tensor-core GEMM: mbarrier wait timed out");
+  return DDD_OK;
+}
 
 int ddd_probe_fma_peak(ddd_ctx* ctx, int precision, double* flops_per_s) {
   if (!ctx || !flops_per_s) return DDD_EINVAL;

@@ -54,6 +54,11 @@ cudaError_t launch_segseg_rows_df(const KConsts& K, const double* soa, const flo
                                   int64_t npad, const int64_t* rows, int64_t nRows, double* partial, double* out,
                                   unsigned long long* counters, cudaStream_t st, int form);
 
+// tc_gemm.cu: tcgen05 BF16 GEMM, D = A * B^T (both K-major).
+size_t tc_gemm_smem_bytes(int N);
+cudaError_t launch_tc_gemm_bf16(int M, int N, int K, const void* A, const void* B, float* D, int* err,
+                                cudaStream_t st);
+
 // ddd_api.cu: context accessors for the other C-ABI files.
 int ctx_device(const ddd_ctx* c);
 

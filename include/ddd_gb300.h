@@ -41,6 +41,7 @@ extern "C" {
 #define DDD_EDEVICE (-4)    /* CUDA error (message in ddd_last_error) */
 #define DDD_ENOMEM (-5)     /* device allocation failed */
 #define DDD_ETOOBIG (-6)    /* more segments than ddd_segseg_force_device_noalloc accepts */
+#define DDD_ETIMEOUT (-7)   /* a bounded wait inside a kernel gave up (the kernel returned early) */
 
 typedef struct ddd_ctx ddd_ctx;
 
@@ -198,6 +199,13 @@ void ddd_batch_destroy(ddd_batch* b);
  * counterpart: the reference's dispatch flags are parCPU / parGPU only. */
 int ddd_set_mode(ddd_ctx* ctx, int mode);
 int ddd_get_mode(const ddd_ctx* ctx);
+
+/* Tensor-core building block of the learned surrogate (no reference
+ * counterpart): D[M x N] (FP32) = A[M x K] * B[N x K]^T with BF16 A and B,
+ * row-major with K contiguous, on tcgen05 (accumulators in TMEM).  M a multiple
+ * of 128, N a multiple of 16 in [16, 256], K a multiple of 16; device pointers,
+ * 16-byte aligned.  Synchronous; DDD_ETIMEOUT if a bounded wait gave up. */
+int ddd_tc_gemm_bf16(ddd_ctx* ctx, int M, int N, int K, const void* A, const void* B, float* D, void* stream);
 
 /* Measurement utility (no reference counterpart): FP64 or FP32 FMA-pipe
  * throughput of this GPU in FLOP/s, measured with CUDA events over an
