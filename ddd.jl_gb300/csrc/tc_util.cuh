@@ -83,10 +83,12 @@ __device__ __forceinline__ void mbar_init(uint64_t* mbar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(mbar)), "r"(count) : "memory");
 }
 
-// Waits for the phase with the given parity to complete; false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint32_t max_iter = 1u << 24) {
+// Waits for the phase with the given parity to complete; false once about two
+// seconds (4e9 SM clocks) have passed without it.
+__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, long long max_clocks = 4000000000LL) {
   const uint32_t a = smem_addr(mbar);
-  for (uint32_t it = 0; it < max_iter; ++it) {
+  const long long start = clock64();
+  for (;;) {
     uint32_t done;
     asm volatile(
         "{\n"
@@ -98,8 +100,8 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint3
         : "r"(a), "r"(parity)
         : "memory");
     if (done) return true;
+    if (clock64() - start > max_clocks) return false;
   }
-  return false;
 }
 
 // 16 consecutive FP32 accumulator columns of this thread's TMEM lane.
