@@ -36,6 +36,8 @@ EXPORTED_SYMBOLS = (
     "ddd_segseg_force_device_noalloc",
     "ddd_batch_create", "ddd_batch_run", "ddd_batch_info", "ddd_batch_last_error", "ddd_batch_destroy",
     "ddd_tc_gemm_bf16",
+    "ddd_surrogate_create", "ddd_surrogate_destroy", "ddd_surrogate_num_params", "ddd_surrogate_params",
+    "ddd_surrogate_make_data", "ddd_surrogate_train", "ddd_surrogate_forward", "ddd_surrogate_grads",
 )
 
 # Arithmetic modes (ddd_set_mode).
@@ -124,6 +126,17 @@ def library():
         L.ddd_batch_destroy.argtypes = [_vp]
         L.ddd_batch_destroy.restype = None
         L.ddd_tc_gemm_bf16.argtypes = [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp]
+        L.ddd_surrogate_create.argtypes = [_vp, ctypes.c_uint64]
+        L.ddd_surrogate_create.restype = _vp
+        L.ddd_surrogate_destroy.argtypes = [_vp]
+        L.ddd_surrogate_destroy.restype = None
+        L.ddd_surrogate_num_params.argtypes = []
+        L.ddd_surrogate_params.argtypes = [_vp, ctypes.POINTER(ctypes.c_float), ctypes.c_int]
+        L.ddd_surrogate_make_data.argtypes = [_vp, cp, _vp, _i64, _vp, _i64, _vp, _vp, _vp]
+        L.ddd_surrogate_train.argtypes = [_vp, _vp, _vp, _i64, _i64, ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                          _dp]
+        L.ddd_surrogate_forward.argtypes = [_vp, _vp, _i64, _vp]
+        L.ddd_surrogate_grads.argtypes = [_vp, _vp, _vp, _i64, _dp, ctypes.POINTER(ctypes.c_float)]
         L.ddd_set_mode.argtypes = [_vp, ctypes.c_int]
         L.ddd_get_mode.argtypes = [_vp]
         L.ddd_probe_fma_peak.argtypes = [_vp, ctypes.c_int, _dp]
@@ -367,6 +380,65 @@ class Batch:
     def close(self):
         if self._h:
             self._L.ddd_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Surrogate:
+    """The learned far-field surrogate (ddd_surrogate_*): training and evaluation on the GPU."""
+
+    def __init__(self, ctx, seed=0):
+        self._L = ctx._L
+        self.ctx = ctx
+        self._h = self._L.ddd_surrogate_create(ctx._h, int(seed))
+        if not self._h:
+            raise DDDError(DDD_EDEVICE, "ddd_surrogate_create failed")
+        self.num_params = self._L.ddd_surrogate_num_params()
+
+    def _rc(self, rc, what):
+        if rc != DDD_OK:
+            raise DDDError(rc, what)
+
+    def params(self):
+        out = np.zeros(self.num_params, np.float32)
+        self._rc(self._L.ddd_surrogate_params(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), 0),
+                 "params")
+        return out
+
+    def set_params(self, flat):
+        flat = np.ascontiguousarray(flat, np.float32)
+        assert flat.size == self.num_params
+        self._rc(self._L.ddd_surrogate_params(self._h, flat.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), 1),
+                 "set_params")
+
+    def make_data(self, k, segs_ptr, n, pairs_ptr, P, X_ptr, T_ptr, F_ptr=None):
+        self.ctx._check(self._L.ddd_surrogate_make_data(self.ctx._h, ctypes.byref(k), segs_ptr, n, pairs_ptr, P,
+                                                        X_ptr, T_ptr, F_ptr))
+
+    def train(self, X_ptr, T_ptr, P, batch, epochs, lr=1e-3, weight_decay=0.0):
+        hist = np.zeros(epochs)
+        self._rc(self._L.ddd_surrogate_train(self._h, X_ptr, T_ptr, P, batch, epochs, lr, weight_decay,
+                                             hist.ctypes.data_as(_dp)), "train")
+        return hist
+
+    def forward(self, X_ptr, P, Y_ptr):
+        self._rc(self._L.ddd_surrogate_forward(self._h, X_ptr, P, Y_ptr), "forward")
+
+    def grads(self, X_ptr, T_ptr, B):
+        loss = ctypes.c_double(0)
+        g = np.zeros(self.num_params, np.float32)
+        self._rc(self._L.ddd_surrogate_grads(self._h, X_ptr, T_ptr, B, ctypes.byref(loss),
+                                             g.ctypes.data_as(ctypes.POINTER(ctypes.c_float))), "grads")
+        return loss.value, g
+
+    def close(self):
+        if self._h:
+            self._L.ddd_surrogate_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -25,6 +25,7 @@ VARIANTS = {
     # df64 needs exact error-free transformations: no contraction.
     "segseg_df.cu": [("", ["--fmad=false"])],
     "segseg_batch.cu": [("", ["--fmad=false"])],
+    "surrogate_data.cu": [("", ["--fmad=false"])],
 }
 
 

@@ -207,6 +207,34 @@ int ddd_get_mode(const ddd_ctx* ctx);
  * 16-byte aligned.  Synchronous; DDD_ETIMEOUT if a bounded wait gave up. */
 int ddd_tc_gemm_bf16(ddd_ctx* ctx, int M, int N, int K, const void* A, const void* B, float* D, void* stream);
 
+/* Learned far-field surrogate (no reference counterpart; the north-star
+ * extension).  A small MLP (16 -> 128 -> 128 -> 128 -> 16, GELU, BF16 operands,
+ * FP32 accumulation) predicts the four node forces of a far segment pair in the
+ * pair's own frame, scaled by mu4pi L_i L_j / R^2 (features and frame:
+ * csrc/surrogate.cuh).  It is trained on the GPU by this library's kernels
+ * (tcgen05 GEMMs, Adam) on pairs whose exact forces the FP64 kernel computes.
+ *   make_data: features X (BF16, P x 16) and scaled exact targets T (FP32,
+ *     P x 16) of the pairs (i, j) in `pairs` (device int32, 2 x P: all i, then
+ *     all j; 0-based columns of the packed 9 x n device array segs); F (device,
+ *     P x 12, may be NULL) receives the exact forces.
+ *   train: Adam over P samples in batches of B (P % B == 0, B % 128 == 0),
+ *     cosine learning-rate decay; per-epoch mean loss into lossHistory.
+ *   forward: Y = MLP(X) for P % 128 == 0 rows (device).
+ *   grads: one forward and backward pass (no update): loss and the flat
+ *     gradient (host), for checks against a CPU evaluation.
+ *   params: copy the flat FP32 parameters to (set = 0) or from (set = 1) the host. */
+typedef struct ddd_surrogate ddd_surrogate;
+ddd_surrogate* ddd_surrogate_create(ddd_ctx* ctx, uint64_t seed);
+void ddd_surrogate_destroy(ddd_surrogate* s);
+int ddd_surrogate_num_params(void);
+int ddd_surrogate_params(ddd_surrogate* s, float* host, int set);
+int ddd_surrogate_make_data(ddd_ctx* ctx, const ddd_consts* k, const double* segs, int64_t n, const int32_t* pairs,
+                            int64_t P, void* X, float* T, double* F);
+int ddd_surrogate_train(ddd_surrogate* s, const void* X, const float* T, int64_t P, int64_t B, int epochs, float lr,
+                        float weightDecay, double* lossHistory);
+int ddd_surrogate_forward(ddd_surrogate* s, const void* X, int64_t P, float* Y);
+int ddd_surrogate_grads(ddd_surrogate* s, const void* X, const float* T, int64_t B, double* loss, float* grads);
+
 /* Measurement utility (no reference counterpart): FP64 or FP32 FMA-pipe
  * throughput of this GPU in FLOP/s, measured with CUDA events over an
  * FMA-chain kernel filling every SM.  precision: 64 or 32. */
