@@ -535,6 +535,7 @@ int ddd_surrogate_make_data(ddd_ctx* ctx, const ddd_consts* k, const double* seg
   if (rc) return rc;
   if (n <= 0 || P < 0 || !segs || (P > 0 && (!pairs || !X || !T))) return fail(ctx, DDD_EINVAL, "bad arguments");
   CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  CK(cudaDeviceSynchronize(), "wait for the caller's device inputs");
   const int64_t npad = ddd::strict::segseg_npad(n);
   CK(ctx->soa.ensure(ddd::strict::segseg_soa_bytes(npad)), "alloc segment SoA");
   CK(ctx->skip.ensure((size_t)npad), "alloc skip flags");

@@ -361,7 +361,8 @@ void ddd_surrogate_destroy(ddd_surrogate* s) {
 int ddd_surrogate_params(ddd_surrogate* s, float* host, int set) {
   if (!s || !host) return DDD_EINVAL;
   cudaSetDevice(s->device);
-  cudaError_t e;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return DDD_EDEVICE;
   if (set) {
     e = cudaMemcpy(s->P, host, kNumParams * sizeof(float), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = refresh_weights(s, s->own);
@@ -379,6 +380,7 @@ int ddd_surrogate_num_params(void) { return kNumParams; }
 int ddd_surrogate_grads(ddd_surrogate* s, const void* X, const float* T, int64_t B, double* loss, float* grads) {
   if (!s || !X || !T || B <= 0 || B % 128) return DDD_EINVAL;
   cudaSetDevice(s->device);
+  if (cudaDeviceSynchronize() != cudaSuccess) return DDD_EDEVICE;  // caller's inputs are ready
   cudaStream_t st = s->own;
   cudaError_t e = ensure_batch(s, B);
   if (e == cudaSuccess) e = cudaMemsetAsync(s->loss, 0, sizeof(double), st);
@@ -402,6 +404,7 @@ int ddd_surrogate_train(ddd_surrogate* s, const void* X, const float* T, int64_t
                         float weightDecay, double* lossHistory) {
   if (!s || !X || !T || B <= 0 || B % 128 || P < B || P % B || epochs <= 0) return DDD_EINVAL;
   cudaSetDevice(s->device);
+  if (cudaDeviceSynchronize() != cudaSuccess) return DDD_EDEVICE;  // caller's inputs are ready
   cudaStream_t st = s->own;
   cudaError_t e = ensure_batch(s, B);
   if (e == cudaSuccess) e = cudaMemsetAsync(s->err, 0, sizeof(int), st);
@@ -441,6 +444,7 @@ int ddd_surrogate_train(ddd_surrogate* s, const void* X, const float* T, int64_t
 int ddd_surrogate_forward(ddd_surrogate* s, const void* X, int64_t P, float* Y) {
   if (!s || !X || !Y || P <= 0 || P % 128) return DDD_EINVAL;
   cudaSetDevice(s->device);
+  if (cudaDeviceSynchronize() != cudaSuccess) return DDD_EDEVICE;  // caller's inputs are ready
   cudaStream_t st = s->own;
   const int64_t B = P < 65536 ? P : 65536;
   cudaError_t e = ensure_batch(s, B);

@@ -222,7 +222,10 @@ int ddd_tc_gemm_bf16(ddd_ctx* ctx, int M, int N, int K, const void* A, const voi
  *   forward: Y = MLP(X) for P % 128 == 0 rows (device).
  *   grads: one forward and backward pass (no update): loss and the flat
  *     gradient (host), for checks against a CPU evaluation.
- *   params: copy the flat FP32 parameters to (set = 0) or from (set = 1) the host. */
+ *   params: copy the flat FP32 parameters to (set = 0) or from (set = 1) the host.
+ * These calls are synchronous: each first waits for all work already queued on
+ * the device (so inputs the caller is still producing on its own stream are
+ * complete) and returns when its results are ready. */
 typedef struct ddd_surrogate ddd_surrogate;
 ddd_surrogate* ddd_surrogate_create(ddd_ctx* ctx, uint64_t seed);
 void ddd_surrogate_destroy(ddd_surrogate* s);

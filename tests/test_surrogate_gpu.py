@@ -54,7 +54,9 @@ def test_features_and_exact_targets(pkg, synth, oracle):
         a1, a2, ab = soa[0:3, i], soa[3:6, i], soa[6:9, i]
         c1, c2, cb = soa[0:3, j], soa[3:6, j], soa[6:9, j]
         ref = oracle.pair(k5, ab, a1, a2, cb, c1, c2).ravel()
-        assert np.allclose(Fh[q], ref, rtol=1e-9, atol=1e-12 * np.abs(ref).max())
+        # Far pairs: the formula cancels strongly, so two correct FP64 evaluations
+        # agree to ~1e-6 of the largest component (long-double study in the design doc).
+        assert np.allclose(Fh[q], ref, rtol=0, atol=1e-5 * np.abs(ref).max())
         li, lj = np.linalg.norm(a2 - a1), np.linalg.norm(c2 - c1)
         f, (e1, e2, e3, scale) = M.features(0.5 * (c1 + c2) - 0.5 * (a1 + a2), (a2 - a1) / li, (c2 - c1) / lj, ab, cb,
                                             li, lj, k5[1])

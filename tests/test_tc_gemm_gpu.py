@@ -12,7 +12,8 @@ def test_tc_gemm_matches_torch(pkg, M, N, K):
     A = torch.randn(M, K, generator=g).to(torch.bfloat16).cuda()
     B = torch.randn(N, K, generator=g).to(torch.bfloat16).cuda()
     D = torch.full((M, N), float("nan"), dtype=torch.float32, device="cuda")
-    pkg.get_context().tc_gemm_bf16(M, N, K, A.data_ptr(), B.data_ptr(), D.data_ptr())
+    pkg.get_context().tc_gemm_bf16(M, N, K, A.data_ptr(), B.data_ptr(), D.data_ptr(),
+                                   stream=torch.cuda.current_stream().cuda_stream)
     ref = A.float() @ B.float().t()
     err = (D - ref).abs().max().item()
     assert err <= 1e-3 * ref.abs().max().item() + 1e-3, err
