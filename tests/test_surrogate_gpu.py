@@ -102,8 +102,9 @@ def test_training_reduces_loss_and_forward_matches(pkg, synth):
     sur = pkg.Surrogate(ctx, seed=1)
     X = torch.zeros((P, 16), dtype=torch.bfloat16, device="cuda")
     T = torch.zeros((P, 16), dtype=torch.float32, device="cuda")
-    sur.make_data(_k(pkg), torch.from_numpy(soa).cuda().data_ptr(), soa.shape[1],
-                  torch.from_numpy(pairs).cuda().data_ptr(), P, X.data_ptr(), T.data_ptr())
+    dsoa, dpairs = torch.from_numpy(soa).cuda(), torch.from_numpy(pairs).cuda()  # kept alive across the call
+    sur.make_data(_k(pkg), dsoa.data_ptr(), soa.shape[1], dpairs.data_ptr(), P, X.data_ptr(), T.data_ptr())
+    assert torch.isfinite(X.float()).all() and torch.isfinite(T).all()
     hist = sur.train(X.data_ptr(), T.data_ptr(), P, 1024, 8, lr=2e-3)
     assert np.all(np.isfinite(hist)) and hist[-1] < 0.2 * hist[0]
     Y = torch.zeros((P, 16), dtype=torch.float32, device="cuda")
