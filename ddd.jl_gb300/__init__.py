@@ -38,6 +38,7 @@ EXPORTED_SYMBOLS = (
     "ddd_tc_gemm_bf16",
     "ddd_surrogate_create", "ddd_surrogate_destroy", "ddd_surrogate_num_params", "ddd_surrogate_params",
     "ddd_surrogate_make_data", "ddd_surrogate_train", "ddd_surrogate_forward", "ddd_surrogate_grads",
+    "ddd_surrogate_force", "ddd_surrogate_last_error",
 )
 
 # Arithmetic modes (ddd_set_mode).
@@ -71,6 +72,23 @@ class ddd_report(ctypes.Structure):
     _fields_ = [("pairs_general", ctypes.c_int64), ("pairs_parallel", ctypes.c_int64),
                 ("core_sides", ctypes.c_int64), ("kernel_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
                 ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ddd_sur_opts(ctypes.Structure):
+    _fields_ = [("kappa", ctypes.c_double), ("audit_fraction", ctypes.c_double), ("audit_tol", ctypes.c_double)]
+
+
+class ddd_sur_report(ctypes.Structure):
+    _fields_ = [("pairs_total", ctypes.c_int64), ("pairs_near_general", ctypes.c_int64),
+                ("pairs_near_parallel", ctypes.c_int64), ("tiles_total", ctypes.c_int64),
+                ("tiles_near", ctypes.c_int64), ("tiles_audit", ctypes.c_int64),
+                ("audit_rel_rms", ctypes.c_double), ("audit_rel_max", ctypes.c_double),
+                ("audit_node_rel_rms", ctypes.c_double), ("fallback", ctypes.c_int),
+                ("ms_prep", ctypes.c_double), ("ms_network", ctypes.c_double), ("ms_audit", ctypes.c_double),
+                ("ms_near", ctypes.c_double), ("ms_reduce", ctypes.c_double), ("ms_total", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -137,6 +155,10 @@ def library():
                                           _dp]
         L.ddd_surrogate_forward.argtypes = [_vp, _vp, _i64, _vp]
         L.ddd_surrogate_grads.argtypes = [_vp, _vp, _vp, _i64, _dp, ctypes.POINTER(ctypes.c_float)]
+        L.ddd_surrogate_force.argtypes = [_vp, cp, _vp, _i64, _vp, _i64, _vp, _vp, ctypes.POINTER(ddd_sur_opts),
+                                          ctypes.POINTER(ddd_sur_report)]
+        L.ddd_surrogate_last_error.argtypes = [_vp]
+        L.ddd_surrogate_last_error.restype = ctypes.c_char_p
         L.ddd_set_mode.argtypes = [_vp, ctypes.c_int]
         L.ddd_get_mode.argtypes = [_vp]
         L.ddd_probe_fma_peak.argtypes = [_vp, ctypes.c_int, _dp]
@@ -389,8 +411,58 @@ class Batch:
             pass
 
 
+# Flat parameter layout of the surrogate (csrc/surrogate.cuh): name -> (offset, size).
+_PARAM_OFF = {}
+_o = 0
+for _name, _size in (("W1", 128 * 16), ("b1", 128), ("W2", 128 * 128), ("b2", 128), ("W3", 128 * 128), ("b3", 128),
+                     ("W4", 16 * 128), ("b4", 16)):
+    _PARAM_OFF[_name] = (_o, _size)
+    _o += _size
+del _o, _name, _size
+
+SURROGATE_MAGIC = b"DDDGBSUR"
+SURROGATE_VERSION = 1
+
+
+def packed_segments(network):
+    """Packed 9 × numSeg segment array (n1 xyz, n2 xyz, b xyz per segment) of a
+    DislocationNetwork, in segIdx row order (the layout of the device entry points)."""
+    n = network.numSeg
+    si = network.segIdx[:n]
+    n1 = network.coord[:, si[:, 1] - 1]
+    n2 = network.coord[:, si[:, 2] - 1]
+    b = network.bVec[:, si[:, 0] - 1]
+    return np.ascontiguousarray(np.concatenate([n1, n2, b], axis=0))
+
+
+def _nu_of(k):
+    """Poisson ratio from the derived constants (mu4pinu = mu4pi / (1 - nu))."""
+    return 1.0 - k.mu4pi / k.mu4pinu
+
+
+def sample_far_pairs(segs, count, kappa, rng):
+    """`count` random pairs (i != j) of the packed segments with midpoint
+    separation R >= kappa * max(L_i, L_j): int32 array 2 × count."""
+    n = segs.shape[1]
+    m = 0.5 * (segs[0:3] + segs[3:6])
+    L = np.linalg.norm(segs[3:6] - segs[0:3], axis=0)
+    out, have = [], 0
+    while have < count:
+        ij = rng.integers(0, n, (2, max(1024, 2 * (count - have))))
+        d2 = ((m[:, ij[1]] - m[:, ij[0]]) ** 2).sum(0)
+        ok = (ij[0] != ij[1]) & (d2 >= (kappa * np.maximum(L[ij[0]], L[ij[1]])) ** 2)
+        out.append(ij[:, ok])
+        have += int(ok.sum())
+    return np.ascontiguousarray(np.concatenate(out, axis=1)[:, :count].astype(np.int32))
+
+
 class Surrogate:
-    """The learned far-field surrogate (ddd_surrogate_*): training and evaluation on the GPU."""
+    """The learned far-field surrogate (ddd_surrogate_*): training and evaluation on the GPU.
+
+    kappa is the trust-region factor the network was trained for (far pairs:
+    R >= kappa max(L_i, L_j)); nu the Poisson ratio of its training data (the
+    scaled pair forces depend on nu, not on mu).  Both travel with save/load.
+    """
 
     def __init__(self, ctx, seed=0):
         self._L = ctx._L
@@ -399,10 +471,129 @@ class Surrogate:
         if not self._h:
             raise DDDError(DDD_EDEVICE, "ddd_surrogate_create failed")
         self.num_params = self._L.ddd_surrogate_num_params()
+        self.kappa = 20.0
+        self.nu = None
+        self.aSq = None
 
     def _rc(self, rc, what):
         if rc != DDD_OK:
-            raise DDDError(rc, what)
+            detail = self._L.ddd_surrogate_last_error(self._h)
+            raise DDDError(rc, what + (": " + detail.decode() if detail else ""))
+
+    # -- training (the product path: sampling, output normalisation, folding) --
+    def fit(self, k, networks, pairs_per_network=1 << 20, epochs=30, batch=4096, lr=2e-3, kappa=20.0,
+            kappa_train=None, seed=0, weight_decay=0.0):
+        """Train on far pairs of `networks` (packed 9 × n float64 arrays) with
+        the exact FP64 forces as targets.  Pairs are sampled uniformly among the
+        pairs with R >= kappa_train max(L_i, L_j) (default 0.9 kappa, a margin
+        around the trust region's edge).  Each of the 12 scaled outputs is
+        normalised by its standard deviation for training; the scales are folded
+        into the last layer afterwards, so evaluation needs no extra step.
+        Returns {"loss": per-epoch history, "samples": P, "sigma": scales}."""
+        import torch
+        kt = 0.9 * kappa if kappa_train is None else kappa_train
+        rng = np.random.default_rng(seed)
+        Xs, Ts = [], []
+        for segs in networks:
+            segs = np.ascontiguousarray(segs, dtype=np.float64)
+            pairs = sample_far_pairs(segs, pairs_per_network, kt, rng)
+            P = pairs.shape[1]
+            X = torch.zeros((P, 16), dtype=torch.bfloat16, device="cuda")
+            T = torch.zeros((P, 16), dtype=torch.float32, device="cuda")
+            dsegs, dpairs = torch.from_numpy(segs).cuda(), torch.from_numpy(pairs).cuda()
+            self.make_data(k, dsegs.data_ptr(), segs.shape[1], dpairs.data_ptr(), P, X.data_ptr(), T.data_ptr())
+            Xs.append(X)
+            Ts.append(T)
+            del dsegs, dpairs
+        X, T = torch.cat(Xs), torch.cat(Ts)
+        del Xs, Ts
+        g = torch.Generator().manual_seed(int(seed))
+        perm = torch.randperm(X.shape[0], generator=g).cuda()
+        P = (X.shape[0] // batch) * batch
+        X, T = X[perm[:P]].contiguous(), T[perm[:P]].contiguous()
+        sig = T[:, :12].double().std(0).clamp_min(1e-12).float()
+        sig16 = torch.ones(16, device="cuda")
+        sig16[:12] = sig
+        Tn = (T / sig16).contiguous()
+        hist = self.train(X.data_ptr(), Tn.data_ptr(), P, batch, epochs, lr=lr, weight_decay=weight_decay)
+        flat = self.params()
+        s16 = sig16.cpu().numpy()
+        o, n = _PARAM_OFF["W4"]
+        flat[o:o + n] = (flat[o:o + n].reshape(16, 128) * s16[:, None]).ravel()
+        o, n = _PARAM_OFF["b4"]
+        flat[o:o + n] *= s16
+        self.set_params(flat)
+        self.kappa, self.nu, self.aSq = float(kappa), _nu_of(k), float(k.aSq)
+        return {"loss": hist, "samples": P, "sigma": s16[:12].copy()}
+
+    # -- forces ---------------------------------------------------------------
+    def force(self, k, segs, ext=None, kappa=None, audit_fraction=0.01, audit_tol=1e-3, out=None, stream=None):
+        """ddd_surrogate_force on packed 9 × n segments (a CUDA float64 tensor or
+        a numpy array).  Returns (forces as a CUDA tensor n × 6 = the 3 × 2 × n
+        column-major array, report dict)."""
+        import torch
+        if self.nu is not None and abs(_nu_of(k) - self.nu) > 1e-9:
+            raise DDDError(DDD_EINVAL, "surrogate trained for nu = %.6g, called with nu = %.6g"
+                           % (self.nu, _nu_of(k)))
+        if not isinstance(segs, torch.Tensor):
+            segs = torch.from_numpy(np.ascontiguousarray(segs, dtype=np.float64)).cuda()
+        assert segs.dtype == torch.float64 and segs.is_cuda and segs.dim() == 2 and segs.shape[0] == 9
+        segs = segs.contiguous()
+        n = segs.shape[1]
+        if ext is not None and not isinstance(ext, torch.Tensor):
+            ext = torch.from_numpy(np.ascontiguousarray(ext, dtype=np.uint8)).cuda()
+        if out is None:
+            out = torch.empty((n, 6), dtype=torch.float64, device=segs.device)
+        o = ddd_sur_opts(self.kappa if kappa is None else float(kappa), float(audit_fraction), float(audit_tol))
+        rep = ddd_sur_report()
+        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        self._rc(self._L.ddd_surrogate_force(self._h, ctypes.byref(k), segs.data_ptr(), n,
+                                             ext.data_ptr() if ext is not None else None, n, out.data_ptr(), st,
+                                             ctypes.byref(o), ctypes.byref(rep)), "surrogate force")
+        return out, rep.as_dict()
+
+    def force_network(self, dlnParams, matParams, network, **kw):
+        """The surrogate's calcSegSegForce: a 3×2×numSeg array for a DislocationNetwork."""
+        n = network.numSeg
+        ext = network.extSeg[network.segIdx[:n, 0] - 1]
+        f, rep = self.force(consts_of(dlnParams, matParams), packed_segments(network), ext=ext, **kw)
+        return np.asfortranarray(f.cpu().numpy().reshape(n, 2, 3).transpose(2, 1, 0)), rep
+
+    # -- checkpoints ------------------------------------------------------------
+    def save(self, path):
+        """Versioned checkpoint: magic, version, parameter count, kappa, nu, aSq,
+        FP32 parameters, CRC-32 of everything before it."""
+        import struct
+        import zlib
+        flat = self.params()
+        head = SURROGATE_MAGIC + struct.pack("<IIddd", SURROGATE_VERSION, flat.size, self.kappa,
+                                             np.nan if self.nu is None else self.nu,
+                                             np.nan if self.aSq is None else self.aSq)
+        body = head + flat.astype("<f4").tobytes()
+        with open(path, "wb") as f:
+            f.write(body + struct.pack("<I", zlib.crc32(body) & 0xFFFFFFFF))
+
+    def load(self, path):
+        import struct
+        import zlib
+        with open(path, "rb") as f:
+            data = f.read()
+        hl = len(SURROGATE_MAGIC) + struct.calcsize("<IIddd")
+        if len(data) < hl + 4 or data[:len(SURROGATE_MAGIC)] != SURROGATE_MAGIC:
+            raise DDDError(DDD_EINVAL, "not a surrogate checkpoint: %s" % path)
+        ver, n, kappa, nu, aSq = struct.unpack("<IIddd", data[len(SURROGATE_MAGIC):hl])
+        if ver != SURROGATE_VERSION:
+            raise DDDError(DDD_EINVAL, "checkpoint version %d, expected %d" % (ver, SURROGATE_VERSION))
+        if n != self.num_params or len(data) != hl + 4 * n + 4:
+            raise DDDError(DDD_EINVAL, "checkpoint size mismatch")
+        (crc,) = struct.unpack("<I", data[-4:])
+        if zlib.crc32(data[:-4]) & 0xFFFFFFFF != crc:
+            raise DDDError(DDD_EINVAL, "checkpoint CRC mismatch: %s" % path)
+        self.set_params(np.frombuffer(data[hl:hl + 4 * n], dtype="<f4").astype(np.float32))
+        self.kappa = kappa
+        self.nu = None if math.isnan(nu) else nu
+        self.aSq = None if math.isnan(aSq) else aSq
+        return self
 
     def params(self):
         out = np.zeros(self.num_params, np.float32)

@@ -26,6 +26,7 @@ VARIANTS = {
     "segseg_df.cu": [("", ["--fmad=false"])],
     "segseg_batch.cu": [("", ["--fmad=false"])],
     "surrogate_data.cu": [("", ["--fmad=false"])],
+    "surrogate_force.cu": [("", ["--fmad=false"])],
 }
 
 

@@ -112,6 +112,28 @@ __host__ __device__ __forceinline__ float gelu_grad(float x) {
   return 0.5f * (1.0f + th) + 0.5f * x * (1.0f - th * th) * du;
 }
 
+// Per-segment data of the force path (10 rows of npad floats, sorted order):
+// midpoint xyz, direction xyz, length (0 for an external or padding segment),
+// Burgers vector xyz.
+constexpr int kMsRows = 10;
+constexpr int kMsM = 0, kMsT = 3, kMsL = 6, kMsB = 7;
+
+// Trust region of the surrogate: a pair is evaluated by the network when both
+// segments are active and its midpoint separation R satisfies
+// R^2 >= kappa^2 max(L_i, L_j)^2.  Every kernel that classifies pairs calls this
+// function on the same FP32 data; the explicit round-to-nearest intrinsics keep
+// the result identical whatever the contraction flags of the translation unit,
+// so each pair is counted by exactly one of the network and the exact pass.
+__device__ __forceinline__ bool pair_is_far(float mix, float miy, float miz, float Li, float mjx, float mjy,
+                                            float mjz, float Lj, float kappa2, float& dx, float& dy, float& dz) {
+  dx = __fsub_rn(mjx, mix);
+  dy = __fsub_rn(mjy, miy);
+  dz = __fsub_rn(mjz, miz);
+  const float R2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+  const float Lm = fmaxf(Li, Lj);
+  return Li > 0.0f && Lj > 0.0f && R2 >= __fmul_rn(kappa2, __fmul_rn(Lm, Lm));
+}
+
 // Flat parameter layout (FP32 master copy): W1 [128 x 16], b1 [128],
 // W2 [128 x 128], b2, W3 [128 x 128], b3, W4 [16 x 128], b4 [16]; every W is
 // [out x in] (row-major, input contiguous).

@@ -22,6 +22,7 @@
 #include "../../include/ddd_gb300.h"
 #include "ddd_internal.h"
 #include "surrogate.cuh"
+#include "surrogate_state.h"
 
 using namespace ddd::sur;
 
@@ -161,25 +162,6 @@ inline unsigned blocks(int64_t n, int t = 256) { return (unsigned)((n + t - 1) /
 }  // namespace ddd
 
 using namespace ddd;
-
-struct ddd_surrogate {
-  int device = 0;
-  cudaStream_t own = nullptr;
-  // parameters, gradients, Adam moments (FP32, flat layout of surrogate.cuh)
-  float *P = nullptr, *G = nullptr, *M1 = nullptr, *M2 = nullptr;
-  // BF16 weights [out x in] and transposes [in x out]
-  __nv_bfloat16 *W1 = nullptr, *W2 = nullptr, *W3 = nullptr, *W4 = nullptr;
-  __nv_bfloat16 *W2T = nullptr, *W3T = nullptr, *W4T = nullptr;
-  int64_t step = 0;
-  // activations for the current batch capacity
-  int64_t cap = 0;
-  float *Z1 = nullptr, *Z2 = nullptr, *Z3 = nullptr, *Y = nullptr, *dH = nullptr, *dZf = nullptr, *dYf = nullptr;
-  __nv_bfloat16 *H1 = nullptr, *H2 = nullptr, *H3 = nullptr, *dY = nullptr, *dZ = nullptr, *AT = nullptr,
-                *BT = nullptr;
-  float *gT = nullptr, *colpart = nullptr;
-  double *lossPart = nullptr, *loss = nullptr;
-  int* err = nullptr;
-};
 
 namespace {
 
@@ -348,6 +330,7 @@ void ddd_surrogate_destroy(ddd_surrogate* s) {
   if (!s) return;
   cudaSetDevice(s->device);
   if (s->own) cudaStreamSynchronize(s->own);
+  ddd::destroy_force_plan(s->plan);
   for (void* p : {(void*)s->P, (void*)s->G, (void*)s->M1, (void*)s->M2, (void*)s->W1, (void*)s->W2, (void*)s->W3,
                   (void*)s->W4, (void*)s->W2T, (void*)s->W3T, (void*)s->W4T, (void*)s->Z1, (void*)s->Z2,
                   (void*)s->Z3, (void*)s->Y, (void*)s->dH, (void*)s->dZf, (void*)s->dYf, (void*)s->H1, (void*)s->H2,

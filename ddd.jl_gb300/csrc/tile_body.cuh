@@ -2,7 +2,9 @@
 // (all-pairs, index rows, batched persistent), templated on
 //   T     tile size (segments per side = threads per CTA; 64 or 128),
 //   MODE  0 = unordered pairs i < j (both sides' forces), 1 = index rows (all
-//         j != i, forces on the row segment only),
+//         j != i, forces on the row segment only), 2 = the pairs i < j outside
+//         the surrogate's trust region (near pairs; forces added to `p`),
+//         3 = the pairs i < j inside it (far pairs; forces written to `p`),
 //   P     arithmetic policy (FP64, df64, mixed FP32; pair_f64.cuh / pair_df.cuh).
 //
 // Thread t owns row segment i (registers); the column tile sits in shared
@@ -15,12 +17,16 @@
 // segment — are written to `p` as [side][component][T] doubles.  No
 // floating-point atomics: the result is deterministic.
 //
+// In MODES 2 and 3 every selected pair goes through the compacted dense pass,
+// in the FP64 general or near-parallel branch as the reference chooses it.
+//
 // Data: `soa` is the FP64 structure of arrays (13 rows of npad doubles: n1xyz,
 // n2xyz, bxyz, txyz, 1/|l|), `skip` one byte per segment (external or padding).
 #pragma once
 #include <cstdint>
 
 #include "pair_f64.cuh"
+#include "surrogate.cuh"
 
 namespace ddd {
 
@@ -31,6 +37,8 @@ struct TileArgs {
   int64_t npad;          // row stride of the SoA
   const float* soadf;    // df64 SoA (policies that use it)
   const void* kd;        // policy constants (df64 / FP32), device-side copy in the kernel parameters
+  const float* ms = nullptr;  // MODES 2-3: FP32 segment data of the trust-region test (surrogate.cuh)
+  float farK2 = 0.0f;         // MODES 2-3: kappa^2 of the trust region
 };
 
 __device__ __forceinline__ SegF64 tb_load_seg64(const double* __restrict__ soa, int64_t npad, int64_t i) {
@@ -67,7 +75,7 @@ __device__ __forceinline__ void tile_body(const TileArgs& A, const typename P::C
 
   int64_t gi;
   bool iActive;
-  if (MODE == 0) {
+  if (MODE != 1) {
     gi = iBase + t;
     iActive = A.skip[gi] == 0;
   } else {
@@ -76,25 +84,46 @@ __device__ __forceinline__ void tile_body(const TileArgs& A, const typename P::C
     gi = iActive ? rows[r] : 0;
     iActive = iActive && A.skip[gi] == 0;
   }
-  typename P::Seg si = P::load_global(A, gi);
+  constexpr bool CLS = MODE >= 2;  // classified modes: dense pass only
+  typename P::Seg si;
+  if (!CLS) si = P::load_global(A, gi);
+  float mi[3] = {0, 0, 0}, Li = 0.0f;
+  if (CLS) {
+    const int64_t n = A.npad;
+    mi[0] = A.ms[(sur::kMsM + 0) * n + gi];
+    mi[1] = A.ms[(sur::kMsM + 1) * n + gi];
+    mi[2] = A.ms[(sur::kMsM + 2) * n + gi];
+    Li = A.ms[sur::kMsL * n + gi];
+  }
 
-  P::template load_tile<T>(A, sm.pol, j0, t);
+  if (!CLS) {
+    P::template load_tile<T>(A, sm.pol, j0, t);
+    P::template zero_cols<T>(sm.pol, t);
+  }
   sm.skip[t] = A.skip[j0 + t];
-  P::template zero_cols<T>(sm.pol, t);
   __syncthreads();
 
   typename P::Acc fi1 = P::acc_zero(), fi2 = P::acc_zero();
   uint32_t pmask[NW];
 #pragma unroll
   for (int w = 0; w < NW; ++w) pmask[w] = 0;
-  unsigned long long nGeneral = 0;
+  unsigned long long nGeneral = 0, nDenseParallel = 0;
 
   for (int k = 0; k < T; ++k) {
     const int jl = (t + k) & (T - 1);
     bool act = iActive && sm.skip[jl] == 0;
-    if (MODE == 0) act = act && (!diag || jl > t);
+    if (MODE != 1) act = act && (!diag || jl > t);
     if (MODE == 1) act = act && (j0 + jl != gi);
-    if (act) {
+    if (CLS) {
+      if (act) {
+        const int64_t n = A.npad, gj = j0 + jl;
+        float dx, dy, dz;
+        const bool far = sur::pair_is_far(mi[0], mi[1], mi[2], Li, A.ms[(sur::kMsM + 0) * n + gj],
+                                          A.ms[(sur::kMsM + 1) * n + gj], A.ms[(sur::kMsM + 2) * n + gj],
+                                          A.ms[sur::kMsL * n + gj], A.farK2, dx, dy, dz);
+        if (far == (MODE == 3)) pmask[jl >> 5] |= 1u << (jl & 31);
+      }
+    } else if (act) {
       typename P::Seg sj = P::template load_smem<T>(sm.pol, jl);
       typename P::Scalar c;
       if (P::is_general(A, si, sj, gi, j0 + jl, c)) {
@@ -161,14 +190,19 @@ __device__ __forceinline__ void tile_body(const TileArgs& A, const typename P::C
     const int e = base + t;
     if (e < nPar) {
       const int il = sm.plist[e] >> 8, jl = sm.plist[e] & 0xff;
-      SegF64 a = tb_load_seg64(A.soa, A.npad, MODE == 0 ? iBase + il : rows[iBase + il]);
+      SegF64 a = tb_load_seg64(A.soa, A.npad, MODE != 1 ? iBase + il : rows[iBase + il]);
       SegF64 b = tb_load_seg64(A.soa, A.npad, j0 + jl);
       double c = dot(a.t, b.t);
       D3 F1, F2, F3 = {0, 0, 0}, F4 = {0, 0, 0};
-      if (MODE == 0)
+      if (CLS && 1.0 - c * c > kSqrtEps) {
+        general_pair<true, true>(A.K, a.b, a.n1, a.n2, a.t, a.tN, b.b, b.n1, b.n2, b.t, b.tN, c, F1, F2, F3, F4);
+        ++nGeneral;
+      } else if (MODE != 1) {
+        ++nDenseParallel;
         nCore += parallel_pair<true>(A.K, a.b, a.n1, a.n2, a.t, a.tN, b.b, b.n1, b.n2, b.t, b.tN, c, F1, F2, F3, F4);
-      else
+      } else {
         nCore += parallel_pair<false>(A.K, a.b, a.n1, a.n2, a.t, a.tN, b.b, b.n1, b.n2, b.t, b.tN, c, F1, F2, F3, F4);
+      }
       sm.cf[t][0] = F1.x; sm.cf[t][1] = F1.y; sm.cf[t][2] = F1.z;
       sm.cf[t][3] = F2.x; sm.cf[t][4] = F2.y; sm.cf[t][5] = F2.z;
       sm.cf[t][6] = F3.x; sm.cf[t][7] = F3.y; sm.cf[t][8] = F3.z;
@@ -182,7 +216,7 @@ __device__ __forceinline__ void tile_body(const TileArgs& A, const typename P::C
       fp1 = fp1 + D3{f[0], f[1], f[2]};
       fp2 = fp2 + D3{f[3], f[4], f[5]};
     }
-    if (MODE == 0) {
+    if (MODE != 1) {
       for (int q = 0; q < lim; ++q) {
         if ((sm.plist[base + q] & 0xff) == t) {
           const double* f = sm.cf[q];
@@ -195,6 +229,26 @@ __device__ __forceinline__ void tile_body(const TileArgs& A, const typename P::C
   }
 
   // ---- Partials: [side][component][T]; side 0 = row segments, 1 = column segments. ----
+  if (CLS) {
+    const double v[12] = {fp1.x, fp1.y, fp1.z, fp2.x, fp2.y, fp2.z, fjp3.x, fjp3.y, fjp3.z, fjp4.x, fjp4.y, fjp4.z};
+#pragma unroll
+    for (int c = 0; c < 12; ++c) p[c * T + t] = (MODE == 2 ? p[c * T + t] : 0.0) + v[c];
+  }
+  if (counters && CLS) {
+    unsigned long long g = nGeneral, pp = nDenseParallel, cc = nCore;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      g += __shfl_down_sync(0xffffffffu, g, o);
+      pp += __shfl_down_sync(0xffffffffu, pp, o);
+      cc += __shfl_down_sync(0xffffffffu, cc, o);
+    }
+    if ((t & 31) == 0) {
+      atomicAdd(&counters[0], g);
+      atomicAdd(&counters[1], pp);
+      atomicAdd(&counters[2], cc);
+    }
+  }
+  if (CLS) return;
   const D3 r1 = P::acc_to_d3(fi1), r2 = P::acc_to_d3(fi2);
   p[0 * T + t] = r1.x + fp1.x;
   p[1 * T + t] = r1.y + fp1.y;

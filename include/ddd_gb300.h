@@ -238,6 +238,51 @@ int ddd_surrogate_train(ddd_surrogate* s, const void* X, const float* T, int64_t
 int ddd_surrogate_forward(ddd_surrogate* s, const void* X, int64_t P, float* Y);
 int ddd_surrogate_grads(ddd_surrogate* s, const void* X, const float* T, int64_t B, double* loss, float* grads);
 
+/* Seg-seg forces with the surrogate for far pairs: the same inputs and output
+ * as ddd_segseg_force_device (packed 9 x ldSegs device segments n1, n2, b; ext
+ * device bytes or NULL; force device 3 x 2 x numSeg), the same pair set as
+ * calcSegSegForce (DislocationForces.jl:574-657, every unordered pair of active
+ * segments), split into
+ *   far pairs  R^2 >= kappa^2 max(L_i, L_j)^2 (R: midpoint separation, L:
+ *              lengths) -> the network, fused tcgen05 kernel;
+ *   near pairs (every other active pair) -> the exact FP64 pair force
+ *              (calcSegSegForce's general or near-parallel branch, strict
+ *              rounding), evaluated in full.
+ * Segments are Morton-sorted by midpoint first, so near pairs fall in few tile
+ * pairs; the result is returned in the caller's order and is deterministic.
+ * Audit: a deterministic sample of about audit_fraction of the tile pairs is
+ * also evaluated exactly on its far pairs.  From the network's errors there the
+ * call estimates the node-force relative RMS error of the whole result
+ * (sqrt(sum of squared slot errors / sampled fraction) / ||F||); when that
+ * exceeds audit_tol, the whole call is recomputed with the exact FP64 kernel
+ * (fallback = 1).
+ * opts may be NULL (kappa 20, audit_fraction 0.01, audit_tol 1e-3); rep may be
+ * NULL.  Synchronous: the work is queued on `stream` (NULL: the surrogate's own
+ * stream, after waiting for all work already queued on the device) and the
+ * call returns when the forces are complete. */
+typedef struct {
+  double kappa;          /* trust-region factor; the network's training range sets it (> 0) */
+  double audit_fraction; /* in [0, 1]; 0 disables the audit */
+  double audit_tol;      /* bound of the estimated node-force relative RMS error; <= 0: no fallback */
+} ddd_sur_opts;
+typedef struct {
+  int64_t pairs_total;          /* unordered pairs of active segments */
+  int64_t pairs_near_general;   /* near pairs, general branch (exact) */
+  int64_t pairs_near_parallel;  /* near pairs, near-parallel branch (exact) */
+  int64_t tiles_total;          /* tile pairs (128 x 128) of the network pass */
+  int64_t tiles_near;           /* tile pairs visited by the exact near pass */
+  int64_t tiles_audit;          /* tile pairs audited */
+  double audit_rel_rms;         /* sqrt(sum |net - exact|^2 / sum |exact|^2) over audited tile sums */
+  double audit_rel_max;         /* largest per-tile-pair relative error among them */
+  double audit_node_rel_rms;    /* estimated node-force relative RMS error of the result */
+  int fallback;                 /* 1 when the exact recomputation replaced the network's result */
+  double ms_prep, ms_network, ms_audit, ms_near, ms_reduce, ms_total;
+} ddd_sur_report;
+int ddd_surrogate_force(ddd_surrogate* s, const ddd_consts* k, const double* segs, int64_t ldSegs,
+                        const uint8_t* ext, int64_t numSeg, double* force, void* stream, const ddd_sur_opts* opts,
+                        ddd_sur_report* rep);
+const char* ddd_surrogate_last_error(const ddd_surrogate* s);
+
 /* Measurement utility (no reference counterpart): FP64 or FP32 FMA-pipe
  * throughput of this GPU in FLOP/s, measured with CUDA events over an
  * FMA-chain kernel filling every SM.  precision: 64 or 32. */

@@ -1,0 +1,213 @@
+"""Surrogate force path (ddd_surrogate_force) on the GPU.
+
+Partition: every unordered pair of active segments is evaluated once, either by
+the network (R^2 >= kappa^2 max(L_i, L_j)^2, FP32 test) or exactly (all other
+pairs).  Checked three ways:
+  * network output forced to zero: the result must be the exact forces of the
+    near pairs alone, summed here with the CPU oracle over the pairs that the
+    same FP32 test (restated in numpy, identical rounding) calls near;
+  * kappa so large that every pair is near: the result must be the exact FP64
+    all-pairs forces (the library's FP64 path and the oracle);
+  * an untrained network: the audit sees a large error and the call falls back
+    to the exact forces.
+Accuracy and speed with a trained network: node-force relative RMS error
+against the exact FP64 forces below 5e-4 on a 32,768-segment network the
+network never saw, and at least 5x faster than the exact FP64 path there.
+
+Tolerances of the exact parts: the near pass computes each pair with the same
+FP64 code as the exact kernel (strict rounding), but after the Morton sort a
+pair may be evaluated with its two segments' roles swapped, and CUDA's and the C
+library's log / atan differ by an ulp; both change the rounding at the level of
+the algorithm's own FP64 noise, amplified by the cancellation in node sums.  So
+the all-pairs comparison uses the FP64 parity check of test_segseg_gpu (per
+node: 1e-10 |F| + 4 x the long-double-measured noise; normwise 3e-10), and the
+near-pairs comparison ||dF|| <= 1e-10 ||F||, per node <= 1e-9 max |F|.
+"""
+import os
+import time
+
+import numpy as np
+import pytest
+
+from conftest import k5_of
+from test_segseg_gpu import check_forces
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def _params(pkg):
+    return pkg.DislocationParameters(coreRad=1.0), pkg.MaterialParameters(mu=1.0, nu=0.28)
+
+
+def _k(pkg):
+    return pkg.consts_of(*_params(pkg))
+
+
+def _network(pkg, synth, loops, seed, cube=20000.0, config="gpu32k"):
+    cfg = synth.CONFIGS[config]
+    p, b = synth.square_loops(loops, seed, cfg["lmin"], cfg["lmax"], cube, cfg["shear_fraction"],
+                              cfg["parallel_fraction"])
+    coord, bvec, seg = synth.network_arrays(p, b)
+    return pkg.DislocationNetwork(coord, bvec, seg), synth.packed_soa(p, b)
+
+
+def _exact_device(pkg, segs, ext=None):
+    ctx = pkg.get_context()
+    k = _k(pkg)
+    n = segs.shape[1]
+    d = torch.from_numpy(segs).cuda()
+    e = torch.from_numpy(ext).cuda() if ext is not None else None
+    out = torch.zeros((n, 6), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    ctx.segseg_force_device(k, d.data_ptr(), n, n, out.data_ptr(), e.data_ptr() if e is not None else None)
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+def _near_mask_rows(segs, kappa):
+    """Per row i, the columns j > i that the FP32 trust-region test calls near
+    (the library's pair_is_far, restated with numpy float32 rounding)."""
+    n1, n2 = segs[0:3], segs[3:6]
+    m = (0.5 * (n1 + n2)).astype(np.float32)
+    t = n2 - n1
+    tN = 1.0 / np.sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2])
+    L = (1.0 / tN).astype(np.float32)
+    k2 = np.float32(kappa) * np.float32(kappa)
+    n = segs.shape[1]
+    for i in range(n - 1):
+        j = np.arange(i + 1, n)
+        dx = m[0, j] - m[0, i]
+        dy = m[1, j] - m[1, i]
+        dz = m[2, j] - m[2, i]
+        R2 = (dx * dx + dy * dy) + dz * dz
+        Lm = np.maximum(L[j], L[i])
+        yield i, j[~(R2 >= k2 * (Lm * Lm))]
+
+
+def _zero_surrogate(pkg):
+    sur = pkg.Surrogate(pkg.get_context(), seed=0)
+    sur.set_params(np.zeros(sur.num_params, np.float32))
+    return sur
+
+
+def test_zero_network_leaves_exact_near_pairs(pkg, synth, oracle):
+    dln, mat = _params(pkg)
+    k5 = k5_of(dln, mat)
+    net, segs = _network(pkg, synth, 256, seed=31, cube=8000.0)
+    sur = _zero_surrogate(pkg)
+    F, rep = sur.force(_k(pkg), segs, kappa=20.0, audit_fraction=0.0)
+    F = F.cpu().numpy()
+    ref = np.zeros_like(F)
+    near = 0
+    for i, js in _near_mask_rows(segs, 20.0):
+        for j in js:
+            f = oracle.pair(k5, segs[6:9, i], segs[0:3, i], segs[3:6, i], segs[6:9, j], segs[0:3, j],
+                            segs[3:6, j]).ravel()
+            ref[i] += f[0:6]
+            ref[j] += f[6:12]
+            near += 1
+    assert near > 1000  # the network places both near and far pairs
+    assert rep["pairs_near_general"] + rep["pairs_near_parallel"] == near
+    assert rep["pairs_total"] == segs.shape[1] * (segs.shape[1] - 1) // 2
+    assert np.linalg.norm(F - ref) <= 1e-10 * np.linalg.norm(ref)
+    assert np.abs(F - ref).max() <= 1e-9 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("with_ext", [False, True])
+def test_all_pairs_near_is_exact(pkg, synth, oracle, with_ext):
+    dln, mat = _params(pkg)
+    net, segs = _network(pkg, synth, 300, seed=32, cube=6000.0)  # 2,400 segments: padded last tile
+    n = segs.shape[1]
+    ext = (np.arange(n) % 7 == 3).astype(np.uint8) if with_ext else None
+    sur = _zero_surrogate(pkg)
+    F, rep = sur.force(_k(pkg), segs, ext=ext, kappa=1e30, audit_fraction=0.0)
+    F = F.cpu().numpy()
+    na = n - (int(ext.sum()) if with_ext else 0)
+    assert rep["pairs_near_general"] + rep["pairs_near_parallel"] == na * (na - 1) // 2
+    ex = _exact_device(pkg, segs, ext)
+    assert np.linalg.norm(F - ex) <= 3e-10 * np.linalg.norm(ex)
+    if with_ext:
+        assert np.all(F[ext == 1] == 0.0)
+        net.extSeg[:] = ext
+    F3 = np.asfortranarray(F.reshape(n, 2, 3).transpose(2, 1, 0))
+    check_forces(F3, oracle, k5_of(dln, mat), net, normwise=3e-10)
+
+
+def test_untrained_network_falls_back_to_exact(pkg, synth, oracle):
+    # Sparse network: mostly far pairs, whose FP64 evaluation cancels strongly,
+    # so the per-node bound (long-double-calibrated noise) carries the check.
+    dln, mat = _params(pkg)
+    net, segs = _network(pkg, synth, 512, seed=33, cube=10000.0)
+    n = segs.shape[1]
+    sur = pkg.Surrogate(pkg.get_context(), seed=5)  # random weights
+    F, rep = sur.force(_k(pkg), segs, kappa=20.0, audit_fraction=0.05, audit_tol=1e-3)
+    assert rep["tiles_audit"] > 0 and rep["audit_node_rel_rms"] > 1e-3
+    assert rep["fallback"] == 1
+    F3 = np.asfortranarray(F.cpu().numpy().reshape(n, 2, 3).transpose(2, 1, 0))
+    check_forces(F3, oracle, k5_of(dln, mat), net, normwise=1e-8)
+
+
+@pytest.fixture(scope="module")
+def trained(pkg, synth):
+    sur = pkg.Surrogate(pkg.get_context(), seed=1)
+    cfg = synth.CONFIGS["gpu32k"]
+    nets = [synth.packed_soa(*synth.square_loops(4096, s, cfg["lmin"], cfg["lmax"], cfg["cube"],
+                                                  cfg["shear_fraction"], cfg["parallel_fraction"]))
+            for s in (101, 102)]
+    info = sur.fit(_k(pkg), nets, pairs_per_network=1 << 20, epochs=10, batch=4096, lr=2e-3, kappa=20.0, seed=3)
+    assert np.all(np.isfinite(info["loss"])) and info["loss"][-1] < 0.05 * info["loss"][0]
+    return sur
+
+
+def test_trained_surrogate_accuracy_and_gain(pkg, synth, trained):
+    net, segs = _network(pkg, synth, 4096, seed=0)  # 32,768 segments, not in the training set
+    k = _k(pkg)
+    ctx = pkg.get_context()
+    d = torch.from_numpy(segs).cuda()
+    n = segs.shape[1]
+    ex = torch.zeros((n, 6), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ctx.segseg_force_device(k, d.data_ptr(), n, n, ex.data_ptr())
+    torch.cuda.synchronize()
+    t_exact = time.perf_counter() - t0
+    F, rep = trained.force(k, d)  # first call: plan set-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    F, rep = trained.force(k, d)
+    torch.cuda.synchronize()
+    t_sur = time.perf_counter() - t0
+    err = (torch.linalg.norm(F - ex) / torch.linalg.norm(ex)).item()
+    if os.environ.get("DDD_TEST_STATS"):
+        with open(os.environ["DDD_TEST_STATS"], "a") as fh:
+            fh.write("surrogate 32k: rel rms %.3e audit %.3e/%.3e exact %.3f s surrogate %.3f s %s\n"
+                     % (err, rep["audit_rel_rms"], rep["audit_rel_max"], t_exact, t_sur, rep))
+    assert rep["fallback"] == 0
+    assert err < 5e-4, err
+    # The audit's node-level estimate is of the right size.
+    assert err / 4 < rep["audit_node_rel_rms"] < 4 * err
+    assert t_exact / t_sur > 5.0, (t_exact, t_sur)
+    F2, _ = trained.force(k, d)
+    assert torch.equal(F, F2)  # deterministic
+
+
+def test_checkpoint_round_trip(pkg, synth, trained, tmp_path):
+    path = str(tmp_path / "sur.bin")
+    trained.save(path)
+    other = pkg.Surrogate(pkg.get_context(), seed=9).load(path)
+    assert np.array_equal(other.params(), trained.params())
+    assert other.kappa == trained.kappa and other.nu == trained.nu
+    net, segs = _network(pkg, synth, 512, seed=34)
+    a, _ = trained.force(_k(pkg), segs)
+    b, _ = other.force(_k(pkg), segs)
+    assert torch.equal(a, b)
+    raw = bytearray(open(path, "rb").read())
+    raw[100] ^= 1
+    open(path, "wb").write(bytes(raw))
+    with pytest.raises(pkg.DDDError):
+        pkg.Surrogate(pkg.get_context(), seed=9).load(path)
+    # A network trained for another Poisson ratio is refused.
+    k = pkg.consts_of(pkg.DislocationParameters(coreRad=1.0), pkg.MaterialParameters(mu=1.0, nu=0.3))
+    with pytest.raises(pkg.DDDError):
+        trained.force(k, segs)

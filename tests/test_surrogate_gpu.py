@@ -105,7 +105,11 @@ def test_training_reduces_loss_and_forward_matches(pkg, synth):
     dsoa, dpairs = torch.from_numpy(soa).cuda(), torch.from_numpy(pairs).cuda()  # kept alive across the call
     sur.make_data(_k(pkg), dsoa.data_ptr(), soa.shape[1], dpairs.data_ptr(), P, X.data_ptr(), T.data_ptr())
     assert torch.isfinite(X.float()).all() and torch.isfinite(T).all()
-    hist = sur.train(X.data_ptr(), T.data_ptr(), P, 1024, 8, lr=2e-3)
+    # Per-output normalisation, as Surrogate.fit trains.
+    sig = torch.ones(16, device="cuda")
+    sig[:12] = T[:, :12].std(0)
+    Tn = (T / sig).contiguous()
+    hist = sur.train(X.data_ptr(), Tn.data_ptr(), P, 1024, 8, lr=2e-3)
     assert np.all(np.isfinite(hist)) and hist[-1] < 0.2 * hist[0]
     Y = torch.zeros((P, 16), dtype=torch.float32, device="cuda")
     sur.forward(X.data_ptr(), P, Y.data_ptr())
