@@ -150,11 +150,11 @@ def library():
         L.ddd_surrogate_destroy.restype = None
         L.ddd_surrogate_num_params.argtypes = []
         L.ddd_surrogate_params.argtypes = [_vp, ctypes.POINTER(ctypes.c_float), ctypes.c_int]
-        L.ddd_surrogate_make_data.argtypes = [_vp, cp, _vp, _i64, _vp, _i64, _vp, _vp, _vp]
-        L.ddd_surrogate_train.argtypes = [_vp, _vp, _vp, _i64, _i64, ctypes.c_int, ctypes.c_float, ctypes.c_float,
-                                          _dp]
-        L.ddd_surrogate_forward.argtypes = [_vp, _vp, _i64, _vp]
-        L.ddd_surrogate_grads.argtypes = [_vp, _vp, _vp, _i64, _dp, ctypes.POINTER(ctypes.c_float)]
+        L.ddd_surrogate_make_data.argtypes = [_vp, cp, _vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp]
+        L.ddd_surrogate_train.argtypes = [_vp, _vp, _vp, _vp, _i64, _i64, ctypes.c_int, ctypes.c_float,
+                                          ctypes.c_float, _dp]
+        L.ddd_surrogate_forward.argtypes = [_vp, _vp, _vp, _i64, _vp]
+        L.ddd_surrogate_grads.argtypes = [_vp, _vp, _vp, _vp, _i64, _dp, ctypes.POINTER(ctypes.c_float)]
         L.ddd_surrogate_force.argtypes = [_vp, cp, _vp, _i64, _vp, _i64, _vp, _vp, ctypes.POINTER(ddd_sur_opts),
                                           ctypes.POINTER(ddd_sur_report)]
         L.ddd_surrogate_last_error.argtypes = [_vp]
@@ -414,8 +414,8 @@ class Batch:
 # Flat parameter layout of the surrogate (csrc/surrogate.cuh): name -> (offset, size).
 _PARAM_OFF = {}
 _o = 0
-for _name, _size in (("W1", 128 * 16), ("b1", 128), ("W2", 128 * 128), ("b2", 128), ("W3", 128 * 128), ("b3", 128),
-                     ("W4", 16 * 128), ("b4", 16)):
+for _name, _size in (("W1", 128 * 8), ("b1", 128), ("W2", 128 * 128), ("b2", 128), ("W3", 128 * 128), ("b3", 128),
+                     ("W4", 112 * 128), ("b4", 112)):
     _PARAM_OFF[_name] = (_o, _size)
     _o += _size
 del _o, _name, _size
@@ -440,9 +440,12 @@ def _nu_of(k):
     return 1.0 - k.mu4pi / k.mu4pinu
 
 
-def sample_far_pairs(segs, count, kappa, rng):
+def sample_far_pairs(segs, count, kappa, rng, focus=0.0):
     """`count` random pairs (i != j) of the packed segments with midpoint
-    separation R >= kappa * max(L_i, L_j): int32 array 2 × count."""
+    separation R >= kappa * max(L_i, L_j): int32 array 2 × count.  focus > 0
+    keeps a uniformly drawn far pair with probability (kappa max(L_i, L_j) / R)^focus,
+    moving samples toward the trust region's edge, where a pair's force (and so
+    its share of the node-force error) is largest."""
     n = segs.shape[1]
     m = 0.5 * (segs[0:3] + segs[3:6])
     L = np.linalg.norm(segs[3:6] - segs[0:3], axis=0)
@@ -450,7 +453,10 @@ def sample_far_pairs(segs, count, kappa, rng):
     while have < count:
         ij = rng.integers(0, n, (2, max(1024, 2 * (count - have))))
         d2 = ((m[:, ij[1]] - m[:, ij[0]]) ** 2).sum(0)
-        ok = (ij[0] != ij[1]) & (d2 >= (kappa * np.maximum(L[ij[0]], L[ij[1]])) ** 2)
+        r02 = (kappa * np.maximum(L[ij[0]], L[ij[1]])) ** 2
+        ok = (ij[0] != ij[1]) & (d2 >= r02)
+        if focus > 0:
+            ok &= rng.random(ok.shape) < (r02 / np.maximum(d2, r02)) ** (0.5 * focus)
         out.append(ij[:, ok])
         have += int(ok.sum())
     return np.ascontiguousarray(np.concatenate(out, axis=1)[:, :count].astype(np.int32))
@@ -482,49 +488,57 @@ class Surrogate:
 
     # -- training (the product path: sampling, output normalisation, folding) --
     def fit(self, k, networks, pairs_per_network=1 << 20, epochs=30, batch=4096, lr=2e-3, kappa=20.0,
-            kappa_train=None, seed=0, weight_decay=0.0):
+            kappa_train=None, seed=0, weight_decay=0.0, focus=0.0):
         """Train on far pairs of `networks` (packed 9 × n float64 arrays) with
-        the exact FP64 forces as targets.  Pairs are sampled uniformly among the
-        pairs with R >= kappa_train max(L_i, L_j) (default 0.9 kappa, a margin
-        around the trust region's edge).  Each of the 12 scaled outputs is
+        the exact FP64 forces as targets.  Pairs are sampled among the pairs with
+        R >= kappa_train max(L_i, L_j) (default 0.9 kappa, a margin around the
+        trust region's edge), uniformly or, with focus > 0, weighted toward that
+        edge (sample_far_pairs).  Each of the 12 scaled outputs is
         normalised by its standard deviation for training; the scales are folded
         into the last layer afterwards, so evaluation needs no extra step.
         Returns {"loss": per-epoch history, "samples": P, "sigma": scales}."""
         import torch
         kt = 0.9 * kappa if kappa_train is None else kappa_train
         rng = np.random.default_rng(seed)
-        Xs, Ts = [], []
+        Xs, Bs, Ts = [], [], []
         for segs in networks:
             segs = np.ascontiguousarray(segs, dtype=np.float64)
-            pairs = sample_far_pairs(segs, pairs_per_network, kt, rng)
+            pairs = sample_far_pairs(segs, pairs_per_network, kt, rng, focus)
             P = pairs.shape[1]
-            X = torch.zeros((P, 16), dtype=torch.bfloat16, device="cuda")
+            X = torch.zeros((P, 16), dtype=torch.bfloat16, device="cuda")  # hi and lo feature parts
+            Bp = torch.zeros((P, 16), dtype=torch.float32, device="cuda")
             T = torch.zeros((P, 16), dtype=torch.float32, device="cuda")
             dsegs, dpairs = torch.from_numpy(segs).cuda(), torch.from_numpy(pairs).cuda()
-            self.make_data(k, dsegs.data_ptr(), segs.shape[1], dpairs.data_ptr(), P, X.data_ptr(), T.data_ptr())
+            self.make_data(k, dsegs.data_ptr(), segs.shape[1], dpairs.data_ptr(), P, X.data_ptr(), Bp.data_ptr(),
+                           T.data_ptr())
             Xs.append(X)
+            Bs.append(Bp)
             Ts.append(T)
             del dsegs, dpairs
-        X, T = torch.cat(Xs), torch.cat(Ts)
-        del Xs, Ts
+        X, Bp, T = torch.cat(Xs), torch.cat(Bs), torch.cat(Ts)
+        del Xs, Bs, Ts
         g = torch.Generator().manual_seed(int(seed))
         perm = torch.randperm(X.shape[0], generator=g).cuda()
         P = (X.shape[0] // batch) * batch
-        X, T = X[perm[:P]].contiguous(), T[perm[:P]].contiguous()
+        X, Bp, T = X[perm[:P]].contiguous(), Bp[perm[:P]].contiguous(), T[perm[:P]].contiguous()
         sig = T[:, :12].double().std(0).clamp_min(1e-12).float()
         sig16 = torch.ones(16, device="cuda")
         sig16[:12] = sig
         Tn = (T / sig16).contiguous()
-        hist = self.train(X.data_ptr(), Tn.data_ptr(), P, batch, epochs, lr=lr, weight_decay=weight_decay)
+        hist = self.train(X.data_ptr(), Bp.data_ptr(), Tn.data_ptr(), P, batch, epochs, lr=lr,
+                          weight_decay=weight_decay)
+        # Fold the output scales into the last layer: coefficient row 12 ac + o scales by sigma_o.
         flat = self.params()
-        s16 = sig16.cpu().numpy()
+        s12 = sig.cpu().numpy().astype(np.float64)
+        rows = np.ones(112)
+        rows[:108] = np.tile(s12, 9)
         o, n = _PARAM_OFF["W4"]
-        flat[o:o + n] = (flat[o:o + n].reshape(16, 128) * s16[:, None]).ravel()
+        flat[o:o + n] = (flat[o:o + n].reshape(112, 128) * rows[:, None]).ravel()
         o, n = _PARAM_OFF["b4"]
-        flat[o:o + n] *= s16
+        flat[o:o + n] *= rows
         self.set_params(flat)
         self.kappa, self.nu, self.aSq = float(kappa), _nu_of(k), float(k.aSq)
-        return {"loss": hist, "samples": P, "sigma": s16[:12].copy()}
+        return {"loss": hist, "samples": P, "sigma": s12}
 
     # -- forces ---------------------------------------------------------------
     def force(self, k, segs, ext=None, kappa=None, audit_fraction=0.01, audit_tol=1e-3, out=None, stream=None):
@@ -607,23 +621,25 @@ class Surrogate:
         self._rc(self._L.ddd_surrogate_params(self._h, flat.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), 1),
                  "set_params")
 
-    def make_data(self, k, segs_ptr, n, pairs_ptr, P, X_ptr, T_ptr, F_ptr=None):
+    def make_data(self, k, segs_ptr, n, pairs_ptr, P, X_ptr, Bp_ptr, T_ptr, F_ptr=None):
+        """Features X (P x 16 BF16), Burgers-vector products Bp and scaled exact
+        targets T (P x 16 FP32 each) of P pairs (device pointers)."""
         self.ctx._check(self._L.ddd_surrogate_make_data(self.ctx._h, ctypes.byref(k), segs_ptr, n, pairs_ptr, P,
-                                                        X_ptr, T_ptr, F_ptr))
+                                                        X_ptr, Bp_ptr, T_ptr, F_ptr))
 
-    def train(self, X_ptr, T_ptr, P, batch, epochs, lr=1e-3, weight_decay=0.0):
+    def train(self, X_ptr, Bp_ptr, T_ptr, P, batch, epochs, lr=1e-3, weight_decay=0.0):
         hist = np.zeros(epochs)
-        self._rc(self._L.ddd_surrogate_train(self._h, X_ptr, T_ptr, P, batch, epochs, lr, weight_decay,
+        self._rc(self._L.ddd_surrogate_train(self._h, X_ptr, Bp_ptr, T_ptr, P, batch, epochs, lr, weight_decay,
                                              hist.ctypes.data_as(_dp)), "train")
         return hist
 
-    def forward(self, X_ptr, P, Y_ptr):
-        self._rc(self._L.ddd_surrogate_forward(self._h, X_ptr, P, Y_ptr), "forward")
+    def forward(self, X_ptr, Bp_ptr, P, O_ptr):
+        self._rc(self._L.ddd_surrogate_forward(self._h, X_ptr, Bp_ptr, P, O_ptr), "forward")
 
-    def grads(self, X_ptr, T_ptr, B):
+    def grads(self, X_ptr, Bp_ptr, T_ptr, B):
         loss = ctypes.c_double(0)
         g = np.zeros(self.num_params, np.float32)
-        self._rc(self._L.ddd_surrogate_grads(self._h, X_ptr, T_ptr, B, ctypes.byref(loss),
+        self._rc(self._L.ddd_surrogate_grads(self._h, X_ptr, Bp_ptr, T_ptr, B, ctypes.byref(loss),
                                              g.ctypes.data_as(ctypes.POINTER(ctypes.c_float))), "grads")
         return loss.value, g
 

@@ -527,13 +527,13 @@ int ddd_set_mode(ddd_ctx* ctx, int mode) {
 int ddd_get_mode(const ddd_ctx* ctx) { return ctx ? ctx->mode : DDD_EINVAL; }
 
 int ddd_surrogate_make_data(ddd_ctx* ctx, const ddd_consts* k, const double* segs, int64_t n, const int32_t* pairs,
-                            int64_t P, void* X, float* T, double* F) {
+                            int64_t P, void* X, float* Bp, float* T, double* F) {
   if (!ctx) return DDD_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
   ddd::KConsts K;
   int rc = check_consts(ctx, k, K);
   if (rc) return rc;
-  if (n <= 0 || P < 0 || !segs || (P > 0 && (!pairs || !X || !T))) return fail(ctx, DDD_EINVAL, "bad arguments");
+  if (n <= 0 || P < 0 || !segs || (P > 0 && (!pairs || !X || !Bp || !T))) return fail(ctx, DDD_EINVAL, "bad arguments");
   CK(cudaSetDevice(ctx->device), "cudaSetDevice");
   CK(cudaDeviceSynchronize(), "wait for the caller's device inputs");
   const int64_t npad = ddd::strict::segseg_npad(n);
@@ -542,7 +542,7 @@ int ddd_surrogate_make_data(ddd_ctx* ctx, const ddd_consts* k, const double* seg
   CK(ddd::strict::launch_prep_segments_packed(segs, n, nullptr, n, npad, ctx->soa.as<double>(),
                                               ctx->skip.as<uint8_t>(), ctx->stream),
      "prep_segments_packed");
-  CK(ddd::launch_pair_data(K, ctx->soa.as<double>(), npad, pairs, P, X, T, F, ctx->stream), "pair_data");
+  CK(ddd::launch_pair_data(K, ctx->soa.as<double>(), npad, pairs, P, X, Bp, T, F, ctx->stream), "pair_data");
   CK(cudaStreamSynchronize(ctx->stream), "surrogate_make_data");
   return DDD_OK;
 }

@@ -61,7 +61,7 @@ cudaError_t launch_tc_gemm_bf16(int M, int N, int K, const void* A, const void* 
 
 // surrogate_data.cu: features and exact scaled targets of a pair list.
 cudaError_t launch_pair_data(const KConsts& K, const double* soa, int64_t npad, const int32_t* pairs, int64_t P,
-                             void* X, float* T, double* F, cudaStream_t st);
+                             void* X, float* Bp, float* T, double* F, cudaStream_t st);
 
 // ddd_api.cu: context accessors for the other C-ABI files.
 int ctx_device(const ddd_ctx* c);

@@ -1,26 +1,40 @@
-// Learned far-field surrogate: pair features and output frame.
+// Learned far-field surrogate: pair features, output frame and the bilinear
+// Burgers-vector contraction.
 //
 // A far pair (midpoint separation R well above the segment lengths) is
 // described in its own frame: e3 along the midpoint separation r = m_j - m_i,
-// e1 along the part of t_i perpendicular to e3, e2 = e3 x e1.  Features
-// (dimensionless, 13 used of 16):
-//   t_i.e1, t_i.e3, t_j.e1, t_j.e2, t_j.e3, b_i.(e1,e2,e3), b_j.(e1,e2,e3),
-//   10 L_i/R, 10 L_j/R (scaled to O(0.1-1) like the others).
-// Outputs: the four node forces (Fnode1, Fnode2 on segment i, Fnode3, Fnode4 on
-// segment j) in the (e1, e2, e3) frame divided by the far-field scale
-// mu4pi * L_i * L_j / R^2 (the order of the force between two segments at
-// distance R for unit Burgers vectors).  Equivariance under rotations is built
-// in; the network only learns the angular and L/R dependence.
+// e1 along the part of t_i perpendicular to e3, e2 = e3 x e1.
+//
+// The pair force is exactly bilinear in the two Burgers vectors (the stress of
+// segment j is linear in b_j, the Peach-Koehler force on segment i linear in
+// b_i), so the network only sees the geometry and the Burgers vectors enter
+// through an exact contraction:
+//   geometric features (7 used of 8):  t_i.e1, t_i.e3, t_j.e1, t_j.e2, t_j.e3,
+//                                      10 L_i / R, 10 L_j / R;
+//   network outputs: 108 coefficients C[ac][o] (ac = 3 a + c, o = 0..11);
+//   scaled node forces: out[o] = sum_ac (b_i.e_a)(b_j.e_c) C[ac][o].
+// out holds the four node forces (Fnode1, Fnode2 on segment i, Fnode3, Fnode4
+// on segment j) in the (e1, e2, e3) frame divided by the far-field scale
+// mu4pi L_i L_j / R^2.  Rotation equivariance and the Burgers-vector linearity
+// are built in; the network learns the angular and L/R dependence.
 #pragma once
+#include <cuda_bf16.h>
 
 namespace ddd {
 namespace sur {
 
-constexpr int kFeat = 16;  // padded feature count (K of layer 1)
-constexpr int kUsedFeat = 13;
+constexpr int kGeo = 8;      // geometric features (7 used, padded)
+constexpr int kUsedGeo = 7;
+// Layer-1 input: each feature as two BF16 numbers, hi = bf16(f) and
+// lo = bf16(f - hi) (columns 0-7 and 8-15), against the weights [W1 | W1]:
+// the product sees the features to ~16 significant bits instead of BF16's 8.
+constexpr int kFeatIn = 2 * kGeo;  // 16
 constexpr int kHidden = 128;
-constexpr int kOut = 16;  // padded output count (N of layer 4)
-constexpr int kUsedOut = 12;
+constexpr int kUsedOut = 12;       // node-force components (4 nodes x 3)
+constexpr int kBProd = 9;          // (b_i.e_a)(b_j.e_c)
+constexpr int kCoef = kBProd * kUsedOut;  // 108 network outputs used
+constexpr int kOut = 112;          // layer-4 width (108 padded to a multiple of 16)
+constexpr int kRow = 16;           // padded per-sample row of the b-product and target buffers
 
 struct Frame {
   float e1[3], e2[3], e3[3];
@@ -28,10 +42,11 @@ struct Frame {
 };
 
 // r: midpoint separation (already in FP32), ti/tj: unit directions, bi/bj:
-// Burgers vectors, Li/Lj: lengths, mu4pi: mu / (4 pi).
+// Burgers vectors, Li/Lj: lengths, mu4pi: mu / (4 pi).  f: the 8 geometric
+// features; bp: the 9 Burgers-vector products; fr: the frame and scale.
 __host__ __device__ __forceinline__ void pair_features(const float r[3], const float ti[3], const float tj[3],
                                                        const float bi[3], const float bj[3], float Li, float Lj,
-                                                       float mu4pi, float* f, Frame& fr) {
+                                                       float mu4pi, float* f, float* bp, Frame& fr) {
   const float R2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
   const float invR = 1.0f / sqrtf(R2);
   float e3[3] = {r[0] * invR, r[1] * invR, r[2] * invR};
@@ -57,21 +72,29 @@ __host__ __device__ __forceinline__ void pair_features(const float r[3], const f
   f[2] = d(tj, e1);
   f[3] = d(tj, e2);
   f[4] = d(tj, e3);
-  f[5] = d(bi, e1);
-  f[6] = d(bi, e2);
-  f[7] = d(bi, e3);
-  f[8] = d(bj, e1);
-  f[9] = d(bj, e2);
-  f[10] = d(bj, e3);
-  f[11] = 10.0f * Li * invR;
-  f[12] = 10.0f * Lj * invR;
-  f[13] = f[14] = f[15] = 0.0f;
+  f[5] = 10.0f * Li * invR;
+  f[6] = 10.0f * Lj * invR;
+  f[7] = 0.0f;
+  const float bl[3] = {d(bi, e1), d(bi, e2), d(bi, e3)};
+  const float br[3] = {d(bj, e1), d(bj, e2), d(bj, e3)};
+  for (int p = 0; p < 3; ++p)
+    for (int q = 0; q < 3; ++q) bp[3 * p + q] = bl[p] * br[q];
   for (int k = 0; k < 3; ++k) {
     fr.e1[k] = e1[k];
     fr.e2[k] = e2[k];
     fr.e3[k] = e3[k];
   }
   fr.scale = mu4pi * Li * Lj * invR * invR;
+}
+
+// The features of one pair as the layer-1 operand row: hi parts, then lo parts.
+__device__ __forceinline__ void split_features(const float* f, float* row) {
+#pragma unroll
+  for (int k = 0; k < kGeo; ++k) {
+    const float hi = __bfloat162float(__float2bfloat16_rn(f[k]));
+    row[k] = hi;
+    row[kGeo + k] = f[k] - hi;
+  }
 }
 
 // Global-frame force from a scaled local output triple.
@@ -134,11 +157,12 @@ __device__ __forceinline__ bool pair_is_far(float mix, float miy, float miz, flo
   return Li > 0.0f && Lj > 0.0f && R2 >= __fmul_rn(kappa2, __fmul_rn(Lm, Lm));
 }
 
-// Flat parameter layout (FP32 master copy): W1 [128 x 16], b1 [128],
-// W2 [128 x 128], b2, W3 [128 x 128], b3, W4 [16 x 128], b4 [16]; every W is
-// [out x in] (row-major, input contiguous).
+// Flat parameter layout (FP32 master copy): W1 [128 x 8], b1 [128],
+// W2 [128 x 128], b2, W3 [128 x 128], b3, W4 [112 x 128], b4 [112]; every W is
+// [out x in] (row-major, input contiguous); output row 12 ac + o of W4 / b4 is
+// coefficient C[ac][o] (rows 108-111 are padding).
 constexpr int kOffW1 = 0;
-constexpr int kOffB1 = kOffW1 + kHidden * kFeat;
+constexpr int kOffB1 = kOffW1 + kHidden * kGeo;
 constexpr int kOffW2 = kOffB1 + kHidden;
 constexpr int kOffB2 = kOffW2 + kHidden * kHidden;
 constexpr int kOffW3 = kOffB2 + kHidden;

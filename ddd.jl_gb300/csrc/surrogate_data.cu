@@ -1,7 +1,8 @@
 // Training data of the far-field surrogate: for a list of segment pairs, the
-// pair features (BF16, surrogate.cuh) and the exact node forces from the FP64
-// analytic kernel (general or near-parallel branch, DislocationForces.jl
-// :879-1442), expressed as the surrogate's scaled local outputs.  Compiled
+// layer-1 operand (hi and lo BF16 parts of the geometric features), the
+// Burgers-vector products, and the exact node forces from the FP64 analytic
+// kernel (general or near-parallel branch, DislocationForces.jl :879-1442)
+// expressed as the surrogate's scaled local outputs (surrogate.cuh).  Compiled
 // with --fmad=false so the forces are the strict FP64 ones.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -25,8 +26,10 @@ __device__ __forceinline__ SegF64 seg_at(const double* __restrict__ soa, int64_t
 }
 
 // pairs: 2 x P int32 (row i, then row j; 0-based segment indices of the SoA).
+// X [P x 16] BF16, Bp [P x 16] FP32 (9 used), T [P x 16] FP32 (12 used), F [P x 12].
 __global__ void pair_data(KConsts K, const double* __restrict__ soa, int64_t npad, const int32_t* __restrict__ pairs,
-                          int64_t P, __nv_bfloat16* __restrict__ X, float* __restrict__ T, double* __restrict__ F) {
+                          int64_t P, __nv_bfloat16* __restrict__ X, float* __restrict__ Bp, float* __restrict__ T,
+                          double* __restrict__ F) {
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (p >= P) return;
   const SegF64 a = seg_at(soa, npad, pairs[p]);
@@ -42,13 +45,16 @@ __global__ void pair_data(KConsts K, const double* __restrict__ soa, int64_t npa
   const float r[3] = {(float)rd.x, (float)rd.y, (float)rd.z};
   const float ti[3] = {(float)a.t.x, (float)a.t.y, (float)a.t.z}, tj[3] = {(float)b.t.x, (float)b.t.y, (float)b.t.z};
   const float bi[3] = {(float)a.b.x, (float)a.b.y, (float)a.b.z}, bj[3] = {(float)b.b.x, (float)b.b.y, (float)b.b.z};
-  float f[sur::kFeat];
+  float f[sur::kGeo], bp[sur::kBProd], row[sur::kFeatIn];
   sur::Frame fr;
-  sur::pair_features(r, ti, tj, bi, bj, (float)(1.0 / a.tN), (float)(1.0 / b.tN), (float)K.mu4pi, f, fr);
+  sur::pair_features(r, ti, tj, bi, bj, (float)(1.0 / a.tN), (float)(1.0 / b.tN), (float)K.mu4pi, f, bp, fr);
+  sur::split_features(f, row);
 #pragma unroll
-  for (int k = 0; k < sur::kFeat; ++k) X[p * sur::kFeat + k] = __float2bfloat16_rn(f[k]);
+  for (int k = 0; k < sur::kFeatIn; ++k) X[p * sur::kFeatIn + k] = __float2bfloat16_rn(row[k]);
+#pragma unroll
+  for (int k = 0; k < sur::kRow; ++k) Bp[p * sur::kRow + k] = k < sur::kBProd ? bp[k] : 0.0f;
   const D3 Fs[4] = {F1, F2, F3, F4};
-  float* tp = T + p * sur::kOut;
+  float* tp = T + p * sur::kRow;
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const double g[3] = {Fs[q].x, Fs[q].y, Fs[q].z};
@@ -60,15 +66,15 @@ __global__ void pair_data(KConsts K, const double* __restrict__ soa, int64_t npa
     }
   }
 #pragma unroll
-  for (int k = sur::kUsedOut; k < sur::kOut; ++k) tp[k] = 0.0f;
+  for (int k = sur::kUsedOut; k < sur::kRow; ++k) tp[k] = 0.0f;
 }
 
 }  // namespace
 
 cudaError_t launch_pair_data(const KConsts& K, const double* soa, int64_t npad, const int32_t* pairs, int64_t P,
-                             void* X, float* T, double* F, cudaStream_t st) {
+                             void* X, float* Bp, float* T, double* F, cudaStream_t st) {
   if (P == 0) return cudaSuccess;
-  pair_data<<<(unsigned)((P + 127) / 128), 128, 0, st>>>(K, soa, npad, pairs, P, (__nv_bfloat16*)X, T, F);
+  pair_data<<<(unsigned)((P + 127) / 128), 128, 0, st>>>(K, soa, npad, pairs, P, (__nv_bfloat16*)X, Bp, T, F);
   return cudaGetLastError();
 }
 

@@ -1,21 +1,23 @@
 // Fused inference of the far-field surrogate over tile pairs.
 //
-// A persistent CTA (one per SM, 4 warpgroups = 512 threads) takes tile pairs
+// A persistent CTA (one per SM, 3 warpgroups = 384 threads) takes tile pairs
 // (I <= J, 128 sorted segments a side) from a work list.  The MLP weights (BF16,
-// 72 KB) stay in shared memory for the CTA's lifetime; each warpgroup has its
+// 96 KB) stay in shared memory for the CTA's lifetime; each warpgroup has its
 // own 32 KB activation buffer, its own 128 TMEM columns and its own mbarrier, so
-// the four warpgroups run independent layer pipelines and the tensor core works
-// on one warpgroup's layer while the others run their epilogues.
+// the warpgroups run independent layer pipelines and the tensor core works on
+// one warpgroup's layer while the others run their epilogues.
 //
-// Warpgroup g handles the steps k = g, g + 4, ... of the tile pair.  At step k
-// thread t forms pair (row t, column (t + k) mod 128), writes its 16 features
-// as row t of a 128 x 16 BF16 operand, and the layer chain runs as
-//   X (128x16) W1^T -> TMEM (128x128 FP32) -> +b1, GELU, BF16 -> H (smem)
-//   H W2^T -> TMEM -> ... -> H W3^T -> TMEM -> ... -> H W4^T -> TMEM (128x16)
+// Warpgroup g handles the steps k = g, g + 3, ... of the tile pair.  At step k
+// thread t forms pair (row t, column (t + k) mod 128), writes its 8 geometric
+// features (hi and lo BF16 parts) as row t of a 128 x 16 BF16 operand, and the
+// layer chain runs as
+//   X (128x16) [W1|W1]^T -> TMEM (128x128 FP32) -> +b1, GELU, BF16 -> H (smem)
+//   H W2^T -> TMEM -> ... -> H W3^T -> TMEM -> ... -> H W4^T -> TMEM (128x112)
 // one thread issuing the tcgen05.mma instructions, the warpgroup waiting on its
 // mbarrier (bounded), each thread reading back its own accumulator row
-// (tcgen05.ld) for the epilogue.  The 12 outputs become the pair's four node
-// forces in the global frame.  Pairs outside the trust region (pair_is_far
+// (tcgen05.ld) for the epilogue.  The 108 coefficients, contracted with the
+// pair's Burgers-vector products, give the 12 scaled outputs, which become the
+// pair's four node forces in the global frame.  Pairs outside the trust region (pair_is_far
 // false), inactive segments and the lower half of diagonal tiles produce zero
 // force here; the exact pass adds the near pairs afterwards.
 //
@@ -37,21 +39,21 @@ namespace ddd {
 namespace {
 
 constexpr int TT = 128;  // tile size (segments)
-constexpr int NWG = 4;   // warpgroups per CTA
+constexpr int NWG = 3;   // warpgroups per CTA
 constexpr int kThreads = NWG * 128;
 // Shared-memory layout (bytes).  The X operand of a step (128 x 16 BF16) sits
 // at the start of the warpgroup's H buffer: layer 1 has read it before the
 // first epilogue overwrites it.
 constexpr int kW1 = 0;                            // 128 x 16 BF16, K-major
-constexpr int kW2 = kW1 + kHidden * kFeat * 2;    // 128 x 128
+constexpr int kW2 = kW1 + kHidden * kFeatIn * 2;  // 128 x 128
 constexpr int kW3 = kW2 + kHidden * kHidden * 2;  // 128 x 128
-constexpr int kW4 = kW3 + kHidden * kHidden * 2;  // 16 x 128
+constexpr int kW4 = kW3 + kHidden * kHidden * 2;  // 112 x 128
 constexpr int kHBytes = TT * kHidden * 2;
 constexpr int kH = kW4 + kOut * kHidden * 2;             // NWG x (128 x 128)
 constexpr int kJ = kH + NWG * kHBytes;                   // kMsRows x 128 FP32 column-tile data
 constexpr int kFJ = kJ + kMsRows * TT * 4;               // NWG x 6 x 128 FP32 column forces
-constexpr int kBias = kFJ + NWG * 6 * TT * 4;            // b1, b2, b3 (128 each), b4 (16)
-constexpr int kSmem = kBias + (3 * kHidden + kOut) * 4;  // 223,808 B
+constexpr int kBias = kFJ + NWG * 6 * TT * 4;            // b1, b2, b3 (128 each), b4 (112)
+constexpr int kSmem = kBias + (3 * kHidden + kOut) * 4;  // 212,928 B
 static_assert(kSmem <= 227 * 1024, "shared memory");
 static_assert(6 * TT * 4 <= kHBytes, "row-sum staging fits in one H buffer");
 
@@ -174,7 +176,7 @@ mlp_far_tiles(const float* __restrict__ ms, int64_t npad, const int4* __restrict
           *reinterpret_cast<const uint4*>(W + (size_t)r * K + kb * 8);
     }
   };
-  stage(W1, kHidden, kFeat, kW1);
+  stage(W1, kHidden, kFeatIn, kW1);
   stage(W2, kHidden, kHidden, kW2);
   stage(W3, kHidden, kHidden, kW3);
   stage(W4, kOut, kHidden, kW4);
@@ -221,7 +223,7 @@ mlp_far_tiles(const float* __restrict__ ms, int64_t npad, const int4* __restrict
 
     for (int k = wg; k < TT; k += NWG) {
       const int jl = (t + k) & (TT - 1);
-      float f[kFeat];
+      float f[kGeo], bp[kBProd];
       Frame fr;
       float r[3];
       const bool far = pair_is_far(mi[0], mi[1], mi[2], Li, sJ[(kMsM + 0) * TT + jl], sJ[(kMsM + 1) * TT + jl],
@@ -229,35 +231,49 @@ mlp_far_tiles(const float* __restrict__ ms, int64_t npad, const int4* __restrict
       if (far && (!diag || jl > t)) {
         const float tj[3] = {sJ[(kMsT + 0) * TT + jl], sJ[(kMsT + 1) * TT + jl], sJ[(kMsT + 2) * TT + jl]};
         const float bj[3] = {sJ[(kMsB + 0) * TT + jl], sJ[(kMsB + 1) * TT + jl], sJ[(kMsB + 2) * TT + jl]};
-        pair_features(r, ti, tj, bi, bj, Li, sJ[kMsL * TT + jl], mu4pi, f, fr);
+        pair_features(r, ti, tj, bi, bj, Li, sJ[kMsL * TT + jl], mu4pi, f, bp, fr);
       } else {
 #pragma unroll
-        for (int c = 0; c < kFeat; ++c) f[c] = 0.0f;
+        for (int c = 0; c < kGeo; ++c) f[c] = 0.0f;
+#pragma unroll
+        for (int c = 0; c < kBProd; ++c) bp[c] = 0.0f;
         fr.scale = 0.0f;
 #pragma unroll
         for (int c = 0; c < 3; ++c) fr.e1[c] = fr.e2[c] = fr.e3[c] = 0.0f;
       }
-      store_bf16x16(H, t, 0, kFeat, f);
+      float row[kFeatIn];
+      split_features(f, row);
+      store_bf16x16(H, t, 0, kFeatIn, row);
 
-      if (!(ok = layer(tm, H, smem + kW1, kFeat, kHidden, &mbar[wg], phase, leader, bar))) break;
+      if (!(ok = layer(tm, H, smem + kW1, kFeatIn, kHidden, &mbar[wg], phase, leader, bar))) break;
       hidden_epilogue(tm_row, sBias, H, t);
       if (!(ok = layer(tm, H, smem + kW2, kHidden, kHidden, &mbar[wg], phase, leader, bar))) break;
       hidden_epilogue(tm_row, sBias + kHidden, H, t);
       if (!(ok = layer(tm, H, smem + kW3, kHidden, kHidden, &mbar[wg], phase, leader, bar))) break;
       hidden_epilogue(tm_row, sBias + 2 * kHidden, H, t);
       if (!(ok = layer(tm, H, smem + kW4, kHidden, kOut, &mbar[wg], phase, leader, bar))) break;
-      uint32_t yr[16];
-      tmem_ld16_async(tm_row, yr);
-      tmem_wait_ld();
+      // Contraction: out[o] = sum_ac bp[ac] (Y[12 ac + o] + b4[12 ac + o]).
       const float* b4 = sBias + 3 * kHidden;
+      float out[kUsedOut];
+#pragma unroll
+      for (int o = 0; o < kUsedOut; ++o) out[o] = 0.0f;
+#pragma unroll
+      for (int c0 = 0; c0 < kCoef; c0 += 16) {
+        uint32_t yr[16];
+        tmem_ld16_async(tm_row + (uint32_t)c0, yr);
+        tmem_wait_ld();
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const int j = c0 + i;
+          if (j < kCoef) out[j % kUsedOut] += bp[j / kUsedOut] * (__uint_as_float(yr[i]) + b4[j]);
+        }
+      }
       float F[12];
 #pragma unroll
       for (int n = 0; n < 4; ++n) {
-        const float y0 = __uint_as_float(yr[3 * n]) + b4[3 * n];
-        const float y1 = __uint_as_float(yr[3 * n + 1]) + b4[3 * n + 1];
-        const float y2 = __uint_as_float(yr[3 * n + 2]) + b4[3 * n + 2];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) F[3 * n + c] = fr.scale * (y0 * fr.e1[c] + y1 * fr.e2[c] + y2 * fr.e3[c]);
+        for (int c = 0; c < 3; ++c)
+          F[3 * n + c] = fr.scale * (out[3 * n] * fr.e1[c] + out[3 * n + 1] * fr.e2[c] + out[3 * n + 2] * fr.e3[c]);
       }
 #pragma unroll
       for (int c = 0; c < 6; ++c) fi[c] += F[c];

@@ -1,16 +1,22 @@
 // Training and batched evaluation of the far-field surrogate MLP
-// (16 -> 128 -> 128 -> 128 -> 16, GELU, BF16 operands, FP32 accumulation) on
-// the GPU with the project's own kernels: every matrix product is the tcgen05
-// GEMM (tc_gemm.cu); activations, losses, transposes, bias gradients and the
-// Adam update are small elementwise / reduction kernels here.
+// (16 -> 128 -> 128 -> 128 -> 112, GELU, BF16 operands, FP32 accumulation) and
+// its Burgers-vector contraction (surrogate.cuh) on the GPU with the project's
+// own kernels: every matrix product is the tcgen05 GEMM (tc_gemm.cu);
+// activations, the contraction, losses, transposes, bias gradients and the Adam
+// update are small elementwise / reduction kernels here.
 //
-// Forward (batch B, X [B x 16] BF16):  Z_l = H_{l-1} W_l^T + b_l,  H_l = GELU(Z_l)
-//   (H_0 = X), Y = H_3 W_4^T + b_4.  Loss = mean over the 12 used outputs of
-//   (Y - T)^2.
-// Backward: dY = 2 (Y - T) / (12 B);  dW_4 = dY^T H_3 (computed as (H_3^T dY)^T),
-//   dH_{l} = dZ_{l+1} W_{l+1},  dZ_l = dH_l * GELU'(Z_l),  dW_l = dZ_l^T H_{l-1},
-//   db_l = column sums of dZ_l.  GEMM operands are BF16 (transposed copies where
-//   the GEMM needs K contiguous); accumulations, bias grads and Adam are FP32.
+// Forward (batch B; X [B x 16] BF16: hi and lo parts of the 8 geometric
+// features; Bp [B x 16] FP32: the 9 Burgers-vector products):
+//   Z_1 = X [W_1 | W_1]^T + b_1 (= (X_hi + X_lo) W_1^T + b_1),
+//   Z_l = H_{l-1} W_l^T + b_l,  H_l = GELU(Z_l),  Y = H_3 W_4^T + b_4 (112 wide),
+//   out[o] = sum_ac Bp[ac] Y[12 ac + o]  (o < 12).
+//   Loss = mean over the 12 outputs of (out - T)^2.
+// Backward: dout = 2 (out - T) / (12 B);  dY[12 ac + o] = Bp[ac] dout[o];
+//   dW_4 = dY^T H_3 (computed as (H_3^T dY)^T),  dH_l = dZ_{l+1} W_{l+1},
+//   dZ_l = dH_l * GELU'(Z_l),  dW_l = dZ_l^T H_{l-1},  db_l = column sums of dZ_l;
+//   dW_1 = sum of the two 8-column halves of dZ_1^T X.  GEMM operands are BF16
+//   (transposed copies where the GEMM needs K contiguous); accumulations, bias
+//   grads and Adam are FP32.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -38,24 +44,53 @@ __global__ void bias_gelu_fwd(float* __restrict__ Z, const float* __restrict__ b
   H[i] = __float2bfloat16_rn(gelu(z));
 }
 
-// Y += b4; loss partial sums per block; dY = 2 (Y - T) / (12 B) on the used outputs.
-__global__ void out_loss(float* __restrict__ Y, const float* __restrict__ b4, const float* __restrict__ T,
-                         __nv_bfloat16* __restrict__ dY, int64_t B, double* __restrict__ lossPart) {
+// Per sample p: y = Y[p] + b4, out[o] = sum_ac Bp[p][ac] y[12 ac + o].  With T:
+// the block's loss partial sum, dout = 2 (out - T) / (12 B) and
+// dY[p][12 ac + o] = Bp[p][ac] dout[o] (FP32 and BF16; padding columns 0).
+// With O: out into O[p] (16 wide, 12 used).
+__global__ void contract(const float* __restrict__ Y, const float* __restrict__ b4, const float* __restrict__ Bp,
+                         const float* __restrict__ T, int64_t B, float* __restrict__ O, float* __restrict__ dYf,
+                         __nv_bfloat16* __restrict__ dY, double* __restrict__ lossPart) {
   __shared__ double red[256];
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   double l = 0.0;
-  if (i < B * kOut) {
-    const int c = (int)(i % kOut);
-    const float y = Y[i] + b4[c];
-    Y[i] = y;
-    float g = 0.0f;
-    if (c < kUsedOut) {
-      const float d = y - T[i];
-      l = (double)d * d;
-      g = 2.0f * d / (12.0f * (float)B);
+  if (p < B) {
+    const float* y = Y + p * kOut;
+    float bp[kBProd], out[kUsedOut];
+#pragma unroll
+    for (int ac = 0; ac < kBProd; ++ac) bp[ac] = Bp[p * kRow + ac];
+#pragma unroll
+    for (int o = 0; o < kUsedOut; ++o) out[o] = 0.0f;
+#pragma unroll
+    for (int ac = 0; ac < kBProd; ++ac)
+#pragma unroll
+      for (int o = 0; o < kUsedOut; ++o) out[o] += bp[ac] * (y[kUsedOut * ac + o] + b4[kUsedOut * ac + o]);
+    if (O)
+#pragma unroll
+      for (int o = 0; o < kRow; ++o) O[p * kRow + o] = o < kUsedOut ? out[o] : 0.0f;
+    if (T) {
+      float g[kUsedOut];
+#pragma unroll
+      for (int o = 0; o < kUsedOut; ++o) {
+        const float d = out[o] - T[p * kRow + o];
+        l += (double)d * d;
+        g[o] = 2.0f * d / (12.0f * (float)B);
+      }
+#pragma unroll
+      for (int ac = 0; ac < kBProd; ++ac)
+#pragma unroll
+        for (int o = 0; o < kUsedOut; ++o) {
+          const float v = bp[ac] * g[o];
+          dYf[p * kOut + kUsedOut * ac + o] = v;
+          dY[p * kOut + kUsedOut * ac + o] = __float2bfloat16_rn(v);
+        }
+      for (int j = kCoef; j < kOut; ++j) {
+        dYf[p * kOut + j] = 0.0f;
+        dY[p * kOut + j] = __float2bfloat16_rn(0.0f);
+      }
     }
-    dY[i] = __float2bfloat16_rn(g);
   }
+  if (!lossPart) return;
   red[threadIdx.x] = l;
   __syncthreads();
   for (int s = 128; s > 0; s >>= 1) {
@@ -106,6 +141,25 @@ __global__ void f32_to_bf16(const float* __restrict__ in, __nv_bfloat16* __restr
   if (i < n) out[i] = __float2bfloat16_rn(in[i]);
 }
 
+// [W1 | W1] (128 x 16 BF16) from W1 (128 x 8 FP32): the layer-1 weights of the
+// hi / lo feature columns.
+__global__ void w1_dup(const float* __restrict__ W1, __nv_bfloat16* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kHidden * kGeo) return;
+  const int o = i / kGeo, k = i % kGeo;
+  const __nv_bfloat16 w = __float2bfloat16_rn(W1[i]);
+  out[o * kFeatIn + k] = w;
+  out[o * kFeatIn + kGeo + k] = w;
+}
+
+// Layer-1 weight gradient: the hi and lo columns' halves of dW1 [128 x 16] summed.
+__global__ void w1_fold(const float* __restrict__ g16, float* __restrict__ g) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kHidden * kGeo) return;
+  const int o = i / kGeo, k = i % kGeo;
+  g[i] = g16[o * kFeatIn + k] + g16[o * kFeatIn + kGeo + k];
+}
+
 // Column sums of a [rows x cols] FP32 matrix into out[cols], fixed order: block
 // b sums rows [b*chunk, (b+1)*chunk) into part[b][cols]; then one pass over b.
 __global__ void colsum_part(const float* __restrict__ m, int64_t rows, int cols, int64_t chunk,
@@ -123,12 +177,6 @@ __global__ void colsum_final(const float* __restrict__ part, int nparts, int col
   float s = 0.0f;
   for (int b = 0; b < nparts; ++b) s += part[(int64_t)b * cols + c];
   out[c] = s;
-}
-
-// dY (BF16, [B x 16]) to FP32 for the b4 gradient.
-__global__ void bf16_to_f32(const __nv_bfloat16* __restrict__ in, float* __restrict__ out, int64_t n) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < n) out[i] = __bfloat162float(in[i]);
 }
 
 // grad[out x in] = gT[in x out]^T (FP32), for W4 (computed as H3^T dY).
@@ -149,11 +197,6 @@ __global__ void adam(float* __restrict__ p, const float* __restrict__ g, float* 
   m[i] = mi;
   v[i] = vi;
   p[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
-}
-
-__global__ void add_bias(float* __restrict__ Y, const float* __restrict__ b, int64_t rows, int cols) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < rows * cols) Y[i] += b[i % cols];
 }
 
 inline unsigned blocks(int64_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
@@ -193,26 +236,31 @@ cudaError_t ensure_batch(ddd_surrogate* s, int64_t B) {
   if (e == cudaSuccess) e = dalloc(&s->AT, h);
   if (e == cudaSuccess) e = dalloc(&s->BT, h);
   if (e == cudaSuccess) e = dalloc(&s->colpart, (size_t)(B / 128 + 1) * kHidden);
-  if (e == cudaSuccess) e = dalloc(&s->lossPart, (size_t)(B * kOut / 256 + 1));
+  if (e == cudaSuccess) e = dalloc(&s->lossPart, (size_t)(B / 256 + 1));
   if (e == cudaSuccess) s->cap = B;
   return e;
 }
 
-// BF16 weights and transposes from the FP32 master copy.
-cudaError_t refresh_weights(ddd_surrogate* s, cudaStream_t st) {
-  f32_to_bf16<<<blocks(kHidden * kFeat), 256, 0, st>>>(s->P + kOffW1, s->W1, kHidden * kFeat);
-  f32_to_bf16<<<blocks(kHidden * kHidden), 256, 0, st>>>(s->P + kOffW2, s->W2, kHidden * kHidden);
-  f32_to_bf16<<<blocks(kHidden * kHidden), 256, 0, st>>>(s->P + kOffW3, s->W3, kHidden * kHidden);
-  f32_to_bf16<<<blocks(kOut * kHidden), 256, 0, st>>>(s->P + kOffW4, s->W4, kOut * kHidden);
-  dim3 tb(32, 8);
-  transpose_bf16<<<dim3(kHidden / 32, kHidden / 32), tb, 0, st>>>(s->W2, s->W2T, kHidden, kHidden);
-  transpose_bf16<<<dim3(kHidden / 32, kHidden / 32), tb, 0, st>>>(s->W3, s->W3T, kHidden, kHidden);
-  transpose_bf16<<<dim3(1, kHidden / 32), tb, 0, st>>>(s->W4, s->W4T, kOut, kHidden);
-  return cudaGetLastError();
-}
+#define RET(x)                             \
+  do {                                     \
+    cudaError_t _e = (x);                  \
+    if (_e != cudaSuccess) return _e;      \
+  } while (0)
 
 cudaError_t transpose(const __nv_bfloat16* in, __nv_bfloat16* out, int64_t R, int C, cudaStream_t st) {
   transpose_bf16<<<dim3((unsigned)((R + 31) / 32), (unsigned)((C + 31) / 32)), dim3(32, 8), 0, st>>>(in, out, R, C);
+  return cudaGetLastError();
+}
+
+// BF16 weights and transposes from the FP32 master copy.
+cudaError_t refresh_weights(ddd_surrogate* s, cudaStream_t st) {
+  w1_dup<<<blocks(kHidden * kGeo), 256, 0, st>>>(s->P + kOffW1, s->W1);
+  f32_to_bf16<<<blocks(kHidden * kHidden), 256, 0, st>>>(s->P + kOffW2, s->W2, kHidden * kHidden);
+  f32_to_bf16<<<blocks(kHidden * kHidden), 256, 0, st>>>(s->P + kOffW3, s->W3, kHidden * kHidden);
+  f32_to_bf16<<<blocks(kOut * kHidden), 256, 0, st>>>(s->P + kOffW4, s->W4, kOut * kHidden);
+  RET(transpose(s->W2, s->W2T, kHidden, kHidden, st));
+  RET(transpose(s->W3, s->W3T, kHidden, kHidden, st));
+  RET(transpose(s->W4, s->W4T, kOut, kHidden, st));  // [128 x 112]
   return cudaGetLastError();
 }
 
@@ -224,15 +272,9 @@ cudaError_t colsum(ddd_surrogate* s, const float* m, int64_t rows, int cols, flo
   return cudaGetLastError();
 }
 
-#define RET(x)                             \
-  do {                                     \
-    cudaError_t _e = (x);                  \
-    if (_e != cudaSuccess) return _e;      \
-  } while (0)
-
 // Forward over a batch of B rows (B % 128 == 0): Z/H buffers and Y filled.
 cudaError_t forward(ddd_surrogate* s, const __nv_bfloat16* X, int64_t B, cudaStream_t st) {
-  RET(launch_tc_gemm_bf16((int)B, kHidden, kFeat, X, s->W1, s->Z1, s->err, st));
+  RET(launch_tc_gemm_bf16((int)B, kHidden, kFeatIn, X, s->W1, s->Z1, s->err, st));
   bias_gelu_fwd<<<blocks(B * kHidden), 256, 0, st>>>(s->Z1, s->P + kOffB1, s->H1, B, kHidden);
   RET(launch_tc_gemm_bf16((int)B, kHidden, kHidden, s->H1, s->W2, s->Z2, s->err, st));
   bias_gelu_fwd<<<blocks(B * kHidden), 256, 0, st>>>(s->Z2, s->P + kOffB2, s->H2, B, kHidden);
@@ -243,16 +285,16 @@ cudaError_t forward(ddd_surrogate* s, const __nv_bfloat16* X, int64_t B, cudaStr
 }
 
 // Loss (added into *s->loss, mean over the batch) and gradients into s->G.
-cudaError_t backward(ddd_surrogate* s, const __nv_bfloat16* X, const float* T, int64_t B, cudaStream_t st) {
-  const int nLoss = (int)blocks(B * kOut);
-  out_loss<<<nLoss, 256, 0, st>>>(s->Y, s->P + kOffB4, T, s->dY, B, s->lossPart);
+cudaError_t backward(ddd_surrogate* s, const __nv_bfloat16* X, const float* Bp, const float* T, int64_t B,
+                     cudaStream_t st) {
+  const int nLoss = (int)blocks(B);
+  contract<<<nLoss, 256, 0, st>>>(s->Y, s->P + kOffB4, Bp, T, B, nullptr, s->dYf, s->dY, s->lossPart);
   sum_doubles<<<1, 32, 0, st>>>(s->lossPart, nLoss, 1.0 / (12.0 * (double)B), s->loss);
   // Layer 4: dW4 = (H3^T dY)^T, db4 = colsum(dY).
   RET(transpose(s->H3, s->AT, B, kHidden, st));   // AT = H3^T [128 x B]
-  RET(transpose(s->dY, s->BT, B, kOut, st));      // BT = dY^T [16 x B]
-  RET(launch_tc_gemm_bf16(kHidden, kOut, (int)B, s->AT, s->BT, s->gT, s->err, st));  // [128 x 16]
+  RET(transpose(s->dY, s->BT, B, kOut, st));      // BT = dY^T [112 x B]
+  RET(launch_tc_gemm_bf16(kHidden, kOut, (int)B, s->AT, s->BT, s->gT, s->err, st));  // [128 x 112]
   transpose_f32_small<<<blocks(kOut * kHidden), 256, 0, st>>>(s->gT, s->G + kOffW4, kHidden, kOut);
-  bf16_to_f32<<<blocks(B * kOut), 256, 0, st>>>(s->dY, s->dYf, B * kOut);
   RET(colsum(s, s->dYf, B, kOut, s->G + kOffB4, st));
   // Layer 3.
   RET(launch_tc_gemm_bf16((int)B, kHidden, kOut, s->dY, s->W4T, s->dH, s->err, st));  // dH3 = dY W4
@@ -273,8 +315,9 @@ cudaError_t backward(ddd_surrogate* s, const __nv_bfloat16* X, const float* T, i
   gelu_bwd<<<blocks(B * kHidden), 256, 0, st>>>(s->dH, s->Z1, s->dZ, s->dZf, B * kHidden);
   RET(colsum(s, s->dZf, B, kHidden, s->G + kOffB1, st));
   RET(transpose(s->dZ, s->AT, B, kHidden, st));
-  RET(transpose(X, s->BT, B, kFeat, st));  // X^T [16 x B]
-  RET(launch_tc_gemm_bf16(kHidden, kFeat, (int)B, s->AT, s->BT, s->G + kOffW1, s->err, st));
+  RET(transpose(X, s->BT, B, kFeatIn, st));  // X^T [16 x B]
+  RET(launch_tc_gemm_bf16(kHidden, kFeatIn, (int)B, s->AT, s->BT, s->gW1, s->err, st));
+  w1_fold<<<blocks(kHidden * kGeo), 256, 0, st>>>(s->gW1, s->G + kOffW1);
   return cudaGetLastError();
 }
 
@@ -290,7 +333,7 @@ ddd_surrogate* ddd_surrogate_create(ddd_ctx* ctx, uint64_t seed) {
             cudaStreamCreateWithFlags(&s->own, cudaStreamNonBlocking) == cudaSuccess;
   ok = ok && dalloc(&s->P, kNumParams) == cudaSuccess && dalloc(&s->G, kNumParams) == cudaSuccess &&
        dalloc(&s->M1, kNumParams) == cudaSuccess && dalloc(&s->M2, kNumParams) == cudaSuccess;
-  ok = ok && dalloc(&s->W1, kHidden * kFeat) == cudaSuccess && dalloc(&s->W2, kHidden * kHidden) == cudaSuccess &&
+  ok = ok && dalloc(&s->W1, kHidden * kFeatIn) == cudaSuccess && dalloc(&s->gW1, kHidden * kFeatIn) == cudaSuccess && dalloc(&s->W2, kHidden * kHidden) == cudaSuccess &&
        dalloc(&s->W3, kHidden * kHidden) == cudaSuccess && dalloc(&s->W4, kOut * kHidden) == cudaSuccess &&
        dalloc(&s->W2T, kHidden * kHidden) == cudaSuccess && dalloc(&s->W3T, kHidden * kHidden) == cudaSuccess &&
        dalloc(&s->W4T, kHidden * kOut) == cudaSuccess && dalloc(&s->gT, kHidden * kOut) == cudaSuccess &&
@@ -308,11 +351,11 @@ ddd_surrogate* ddd_surrogate_create(ddd_ctx* ctx, uint64_t seed) {
     for (int o = 0; o < out; ++o)
       for (int k = 0; k < in; ++k) h[off + o * in + k] = k < inUsed ? U(rng) : 0.0f;
   };
-  fill(kOffW1, kHidden, kFeat, kUsedFeat);
+  fill(kOffW1, kHidden, kGeo, kUsedGeo);
   fill(kOffW2, kHidden, kHidden, kHidden);
   fill(kOffW3, kHidden, kHidden, kHidden);
   fill(kOffW4, kOut, kHidden, kHidden);
-  for (int o = kUsedOut; o < kOut; ++o)
+  for (int o = kCoef; o < kOut; ++o)
     for (int k = 0; k < kHidden; ++k) h[kOffW4 + o * kHidden + k] = 0.0f;
   ok = cudaMemcpy(s->P, h.data(), kNumParams * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess &&
        cudaMemset(s->M1, 0, kNumParams * sizeof(float)) == cudaSuccess &&
@@ -332,7 +375,7 @@ void ddd_surrogate_destroy(ddd_surrogate* s) {
   if (s->own) cudaStreamSynchronize(s->own);
   ddd::destroy_force_plan(s->plan);
   for (void* p : {(void*)s->P, (void*)s->G, (void*)s->M1, (void*)s->M2, (void*)s->W1, (void*)s->W2, (void*)s->W3,
-                  (void*)s->W4, (void*)s->W2T, (void*)s->W3T, (void*)s->W4T, (void*)s->Z1, (void*)s->Z2,
+                  (void*)s->W4, (void*)s->gW1, (void*)s->W2T, (void*)s->W3T, (void*)s->W4T, (void*)s->Z1, (void*)s->Z2,
                   (void*)s->Z3, (void*)s->Y, (void*)s->dH, (void*)s->dZf, (void*)s->dYf, (void*)s->H1, (void*)s->H2,
                   (void*)s->H3, (void*)s->dY, (void*)s->dZ, (void*)s->AT, (void*)s->BT, (void*)s->gT,
                   (void*)s->colpart, (void*)s->lossPart, (void*)s->loss, (void*)s->err})
@@ -360,8 +403,9 @@ int ddd_surrogate_num_params(void) { return kNumParams; }
 
 // One forward + backward on B rows (B % 128 == 0), no update: loss and
 // gradients (flat FP32 layout) copied to the host.
-int ddd_surrogate_grads(ddd_surrogate* s, const void* X, const float* T, int64_t B, double* loss, float* grads) {
-  if (!s || !X || !T || B <= 0 || B % 128) return DDD_EINVAL;
+int ddd_surrogate_grads(ddd_surrogate* s, const void* X, const float* Bp, const float* T, int64_t B, double* loss,
+                        float* grads) {
+  if (!s || !X || !Bp || !T || B <= 0 || B % 128) return DDD_EINVAL;
   cudaSetDevice(s->device);
   if (cudaDeviceSynchronize() != cudaSuccess) return DDD_EDEVICE;  // caller's inputs are ready
   cudaStream_t st = s->own;
@@ -369,7 +413,7 @@ int ddd_surrogate_grads(ddd_surrogate* s, const void* X, const float* T, int64_t
   if (e == cudaSuccess) e = cudaMemsetAsync(s->loss, 0, sizeof(double), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(s->err, 0, sizeof(int), st);
   if (e == cudaSuccess) e = forward(s, (const __nv_bfloat16*)X, B, st);
-  if (e == cudaSuccess) e = backward(s, (const __nv_bfloat16*)X, T, B, st);
+  if (e == cudaSuccess) e = backward(s, (const __nv_bfloat16*)X, Bp, T, B, st);
   int flag = 0;
   if (e == cudaSuccess && loss) e = cudaMemcpyAsync(loss, s->loss, sizeof(double), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess && grads)
@@ -380,12 +424,12 @@ int ddd_surrogate_grads(ddd_surrogate* s, const void* X, const float* T, int64_t
   return flag ? DDD_ETIMEOUT : DDD_OK;
 }
 
-// Adam training over P samples (X [P x 16] BF16, T [P x 16] FP32, device), in
-// batches of B (P % B == 0, B % 128 == 0), `epochs` passes in a fixed order;
-// the mean loss of each epoch goes to lossHistory (host, may be NULL).
-int ddd_surrogate_train(ddd_surrogate* s, const void* X, const float* T, int64_t P, int64_t B, int epochs, float lr,
-                        float weightDecay, double* lossHistory) {
-  if (!s || !X || !T || B <= 0 || B % 128 || P < B || P % B || epochs <= 0) return DDD_EINVAL;
+// Adam training over P samples (X [P x 16] BF16, Bp and T [P x 16] FP32,
+// device), in batches of B (P % B == 0, B % 128 == 0), `epochs` passes in a
+// fixed order; the mean loss of each epoch goes to lossHistory (host, may be NULL).
+int ddd_surrogate_train(ddd_surrogate* s, const void* X, const float* Bp, const float* T, int64_t P, int64_t B,
+                        int epochs, float lr, float weightDecay, double* lossHistory) {
+  if (!s || !X || !Bp || !T || B <= 0 || B % 128 || P < B || P % B || epochs <= 0) return DDD_EINVAL;
   cudaSetDevice(s->device);
   if (cudaDeviceSynchronize() != cudaSuccess) return DDD_EDEVICE;  // caller's inputs are ready
   cudaStream_t st = s->own;
@@ -398,10 +442,11 @@ int ddd_surrogate_train(ddd_surrogate* s, const void* X, const float* T, int64_t
     // Cosine learning-rate schedule over the epochs.
     const float lre = 0.5f * lr * (1.0f + std::cos(3.14159265f * (float)ep / (float)epochs));
     for (int64_t b = 0; b < nb && e == cudaSuccess; ++b) {
-      const __nv_bfloat16* xb = (const __nv_bfloat16*)X + b * B * kFeat;
-      const float* tb = T + b * B * kOut;
+      const __nv_bfloat16* xb = (const __nv_bfloat16*)X + b * B * kFeatIn;
+      const float* bpb = Bp + b * B * kRow;
+      const float* tb = T + b * B * kRow;
       e = forward(s, xb, B, st);
-      if (e == cudaSuccess) e = backward(s, xb, tb, B, st);
+      if (e == cudaSuccess) e = backward(s, xb, bpb, tb, B, st);
       if (e != cudaSuccess) break;
       ++s->step;
       const float bc1 = 1.0f - std::pow(b1, (float)s->step), bc2 = 1.0f - std::pow(b2, (float)s->step);
@@ -423,9 +468,10 @@ int ddd_surrogate_train(ddd_surrogate* s, const void* X, const float* T, int64_t
   return flag ? DDD_ETIMEOUT : DDD_OK;
 }
 
-// Batched evaluation (P % 128 == 0): Y [P x 16] FP32 (device) = MLP(X).
-int ddd_surrogate_forward(ddd_surrogate* s, const void* X, int64_t P, float* Y) {
-  if (!s || !X || !Y || P <= 0 || P % 128) return DDD_EINVAL;
+// Batched evaluation (P % 128 == 0): O [P x 16] FP32 (device, 12 used) = the
+// contracted scaled node forces of the rows of X and Bp.
+int ddd_surrogate_forward(ddd_surrogate* s, const void* X, const float* Bp, int64_t P, float* O) {
+  if (!s || !X || !Bp || !O || P <= 0 || P % 128) return DDD_EINVAL;
   cudaSetDevice(s->device);
   if (cudaDeviceSynchronize() != cudaSuccess) return DDD_EDEVICE;  // caller's inputs are ready
   cudaStream_t st = s->own;
@@ -434,10 +480,11 @@ int ddd_surrogate_forward(ddd_surrogate* s, const void* X, int64_t P, float* Y) 
   if (e == cudaSuccess) e = cudaMemsetAsync(s->err, 0, sizeof(int), st);
   for (int64_t off = 0; off < P && e == cudaSuccess; off += B) {
     const int64_t b = (P - off) < B ? (P - off) : B;
-    e = forward(s, (const __nv_bfloat16*)X + off * kFeat, b, st);
+    e = forward(s, (const __nv_bfloat16*)X + off * kFeatIn, b, st);
     if (e != cudaSuccess) break;
-    add_bias<<<blocks(b * kOut), 256, 0, st>>>(s->Y, s->P + kOffB4, b, kOut);
-    e = cudaMemcpyAsync(Y + off * kOut, s->Y, (size_t)b * kOut * sizeof(float), cudaMemcpyDeviceToDevice, st);
+    contract<<<blocks(b), 256, 0, st>>>(s->Y, s->P + kOffB4, Bp + off * kRow, nullptr, b, O + off * kRow, nullptr,
+                                        nullptr, nullptr);
+    e = cudaGetLastError();
   }
   int flag = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, s->err, sizeof(int), cudaMemcpyDeviceToHost, st);

@@ -17,7 +17,7 @@ struct ddd_surrogate {
   cudaStream_t own = nullptr;
   // parameters, gradients, Adam moments (FP32, flat layout of surrogate.cuh)
   float *P = nullptr, *G = nullptr, *M1 = nullptr, *M2 = nullptr;
-  // BF16 weights [out x in] and transposes [in x out]
+  // BF16 weights [out x in] (W1: [W1 | W1], 128 x 32) and transposes [in x out]
   __nv_bfloat16 *W1 = nullptr, *W2 = nullptr, *W3 = nullptr, *W4 = nullptr;
   __nv_bfloat16 *W2T = nullptr, *W3T = nullptr, *W4T = nullptr;
   int64_t step = 0;
@@ -27,6 +27,7 @@ struct ddd_surrogate {
   __nv_bfloat16 *H1 = nullptr, *H2 = nullptr, *H3 = nullptr, *dY = nullptr, *dZ = nullptr, *AT = nullptr,
                 *BT = nullptr;
   float *gT = nullptr, *colpart = nullptr;
+  float* gW1 = nullptr;  // layer-1 weight gradient before folding, 128 x 32
   double *lossPart = nullptr, *loss = nullptr;
   int* err = nullptr;
   ddd::SurForcePlan* plan = nullptr;  // buffers of the force path, per segment count

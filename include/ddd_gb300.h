@@ -208,18 +208,24 @@ int ddd_get_mode(const ddd_ctx* ctx);
 int ddd_tc_gemm_bf16(ddd_ctx* ctx, int M, int N, int K, const void* A, const void* B, float* D, void* stream);
 
 /* Learned far-field surrogate (no reference counterpart; the north-star
- * extension).  A small MLP (16 -> 128 -> 128 -> 128 -> 16, GELU, BF16 operands,
- * FP32 accumulation) predicts the four node forces of a far segment pair in the
- * pair's own frame, scaled by mu4pi L_i L_j / R^2 (features and frame:
- * csrc/surrogate.cuh).  It is trained on the GPU by this library's kernels
- * (tcgen05 GEMMs, Adam) on pairs whose exact forces the FP64 kernel computes.
- *   make_data: features X (BF16, P x 16) and scaled exact targets T (FP32,
- *     P x 16) of the pairs (i, j) in `pairs` (device int32, 2 x P: all i, then
- *     all j; 0-based columns of the packed 9 x n device array segs); F (device,
- *     P x 12, may be NULL) receives the exact forces.
+ * extension).  A pair's four node forces, in the pair's own frame and scaled by
+ * mu4pi L_i L_j / R^2, are bilinear in the two Burgers vectors; a small MLP
+ * (16 -> 128 -> 128 -> 128 -> 112, GELU, BF16 operands, FP32 accumulation) maps
+ * the pair geometry to the 108 coefficients of that bilinear form, and an exact
+ * contraction with (b_i.e_a)(b_j.e_c) gives the forces (features, frame and
+ * contraction: csrc/surrogate.cuh).  It is trained on the GPU by this library's
+ * kernels (tcgen05 GEMMs, Adam) on pairs whose exact forces the FP64 kernel
+ * computes.  Per-sample rows (device, row-major):
+ *   X  BF16 [P x 16]: the 8 geometric features' hi parts bf16(f), then their
+ *      lo parts bf16(f - hi);
+ *   Bp FP32 [P x 16]: the 9 Burgers-vector products (7 zero columns);
+ *   T  FP32 [P x 16]: the 12 scaled exact node forces (4 zero columns).
+ *   make_data: X, Bp, T of the pairs (i, j) in `pairs` (device int32, 2 x P:
+ *     all i, then all j; 0-based columns of the packed 9 x n device array segs);
+ *     F (device, P x 12, may be NULL) receives the exact forces.
  *   train: Adam over P samples in batches of B (P % B == 0, B % 128 == 0),
  *     cosine learning-rate decay; per-epoch mean loss into lossHistory.
- *   forward: Y = MLP(X) for P % 128 == 0 rows (device).
+ *   forward: O [P x 16] = the contracted outputs for P % 128 == 0 rows.
  *   grads: one forward and backward pass (no update): loss and the flat
  *     gradient (host), for checks against a CPU evaluation.
  *   params: copy the flat FP32 parameters to (set = 0) or from (set = 1) the host.
@@ -232,11 +238,12 @@ void ddd_surrogate_destroy(ddd_surrogate* s);
 int ddd_surrogate_num_params(void);
 int ddd_surrogate_params(ddd_surrogate* s, float* host, int set);
 int ddd_surrogate_make_data(ddd_ctx* ctx, const ddd_consts* k, const double* segs, int64_t n, const int32_t* pairs,
-                            int64_t P, void* X, float* T, double* F);
-int ddd_surrogate_train(ddd_surrogate* s, const void* X, const float* T, int64_t P, int64_t B, int epochs, float lr,
-                        float weightDecay, double* lossHistory);
-int ddd_surrogate_forward(ddd_surrogate* s, const void* X, int64_t P, float* Y);
-int ddd_surrogate_grads(ddd_surrogate* s, const void* X, const float* T, int64_t B, double* loss, float* grads);
+                            int64_t P, void* X, float* Bp, float* T, double* F);
+int ddd_surrogate_train(ddd_surrogate* s, const void* X, const float* Bp, const float* T, int64_t P, int64_t B,
+                        int epochs, float lr, float weightDecay, double* lossHistory);
+int ddd_surrogate_forward(ddd_surrogate* s, const void* X, const float* Bp, int64_t P, float* O);
+int ddd_surrogate_grads(ddd_surrogate* s, const void* X, const float* Bp, const float* T, int64_t B, double* loss,
+                        float* grads);
 
 /* Seg-seg forces with the surrogate for far pairs: the same inputs and output
  * as ddd_segseg_force_device (packed 9 x ldSegs device segments n1, n2, b; ext

@@ -1,23 +1,32 @@
 """CPU oracle of the far-field surrogate (test infrastructure only).
 
-A float64 NumPy restatement of the surrogate's features (csrc/surrogate.cuh)
-and of the MLP's forward pass, loss and gradients (csrc/surrogate_mlp.cu),
-rounding to BF16 at the same points as the GPU (inputs, weights, hidden
-activations, output gradient, hidden-layer gradients fed to the GEMMs), so the
-GPU's gradients can be checked against it.  GELU uses the exact tanh here; the
-GPU uses the hardware tanh approximation (relative error ~2^-11).
+A float64 NumPy restatement of the surrogate's features and Burgers-vector
+contraction (csrc/surrogate.cuh) and of the MLP's forward pass, loss and
+gradients (csrc/surrogate_mlp.cu), rounding to BF16 at the same points as the
+GPU (inputs, weights, hidden activations, the coefficient gradient, hidden-layer
+gradients fed to the GEMMs), so the GPU's gradients can be checked against it.
+GELU uses the exact tanh here; the GPU uses the hardware tanh approximation
+(relative error ~2^-11).
+
+Model: the network maps the 8 geometric features of a pair (layer 1 takes each
+as two BF16 numbers, hi = bf16(f) and lo = bf16(f - hi), against the weights
+[W1 | W1], so its product is (hi + lo) W1^T) to 112 outputs Y, of which 108 are
+the coefficients C[ac][o] = Y[12 ac + o] of the bilinear form
+    out[o] = sum_ac Bp[ac] C[ac][o],   Bp[3 a + c] = (b_i.e_a)(b_j.e_c),
+giving the 12 scaled node forces.
 """
 import numpy as np
 
-FEAT, HIDDEN, OUT, USED_OUT = 16, 128, 16, 12
+GEO, FEAT_IN, HIDDEN, OUT, USED_OUT, BPROD = 8, 16, 128, 112, 12, 9
+COEF = BPROD * USED_OUT
 OFF = {}
 _o = 0
-for name, size in (("W1", HIDDEN * FEAT), ("b1", HIDDEN), ("W2", HIDDEN * HIDDEN), ("b2", HIDDEN),
+for name, size in (("W1", HIDDEN * GEO), ("b1", HIDDEN), ("W2", HIDDEN * HIDDEN), ("b2", HIDDEN),
                    ("W3", HIDDEN * HIDDEN), ("b3", HIDDEN), ("W4", OUT * HIDDEN), ("b4", OUT)):
     OFF[name] = (_o, size)
     _o += size
 NUM_PARAMS = _o
-SHAPES = {"W1": (HIDDEN, FEAT), "W2": (HIDDEN, HIDDEN), "W3": (HIDDEN, HIDDEN), "W4": (OUT, HIDDEN),
+SHAPES = {"W1": (HIDDEN, GEO), "W2": (HIDDEN, HIDDEN), "W3": (HIDDEN, HIDDEN), "W4": (OUT, HIDDEN),
           "b1": (HIDDEN,), "b2": (HIDDEN,), "b3": (HIDDEN,), "b4": (OUT,)}
 
 
@@ -27,6 +36,16 @@ def bf16(a):
     u = f.view(np.uint32).astype(np.uint64)
     r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
     return r.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def split(f):
+    """Layer-1 operand rows (..., 16) of geometric features f (..., 8): hi = bf16(f)
+    and lo = bf16(f - hi), the difference taken in float32 (exact), as
+    split_features in csrc/surrogate.cuh."""
+    f32 = np.asarray(f, dtype=np.float32)
+    hi = bf16(f32)
+    lo = bf16(f32 - hi.astype(np.float32))
+    return np.concatenate([hi, lo], axis=-1)
 
 
 def unpack(flat):
@@ -53,7 +72,8 @@ def gelu_grad(x):
 
 
 def features(r, ti, tj, bi, bj, Li, Lj, mu4pi):
-    """Features (16) and frame of one pair, as pair_features in csrc/surrogate.cuh."""
+    """Geometric features (8), Burgers-vector products (9) and frame of one pair,
+    as pair_features in csrc/surrogate.cuh."""
     r = np.asarray(r, np.float64)
     R = np.sqrt(r @ r)
     e3 = r / R
@@ -67,16 +87,26 @@ def features(r, ti, tj, bi, bj, Li, Lj, mu4pi):
         n1 = e1 @ e1
     e1 = e1 / np.sqrt(n1)
     e2 = np.cross(e3, e1)
-    f = np.zeros(FEAT)
-    f[:13] = [ti @ e1, a, tj @ e1, tj @ e2, tj @ e3, bi @ e1, bi @ e2, bi @ e3, bj @ e1, bj @ e2, bj @ e3,
-              10 * Li / R, 10 * Lj / R]
-    return f, (e1, e2, e3, mu4pi * Li * Lj / (R * R))
+    f = np.zeros(GEO)
+    f[:7] = [ti @ e1, a, tj @ e1, tj @ e2, tj @ e3, 10 * Li / R, 10 * Lj / R]
+    E = np.stack([e1, e2, e3])
+    bp = np.outer(E @ bi, E @ bj).ravel()
+    return f, bp, (e1, e2, e3, mu4pi * Li * Lj / (R * R))
 
 
-def forward(p, X):
-    """Activations of the GPU's forward pass (BF16 rounding at the GEMM inputs)."""
+def contract(Y, Bp):
+    """out[:, o] = sum_ac Bp[:, ac] Y[:, 12 ac + o] (Y already includes b4)."""
+    C = Y[:, :COEF].reshape(-1, BPROD, USED_OUT)
+    return np.einsum("pa,pao->po", Bp[:, :BPROD], C)
+
+
+def forward(p, X, Bp=None):
+    """Activations of the GPU's forward pass (BF16 rounding at the GEMM inputs);
+    X holds layer-1 operand rows (B x 16, hi and lo parts, see split).  With Bp
+    (B x 9 or wider), also the contracted outputs `out`."""
     W = {k: bf16(p[k]) if k.startswith("W") else p[k] for k in p}
-    H0 = bf16(X)
+    X = bf16(X)
+    H0 = X[:, :GEO] + X[:, GEO:]
     Z1 = H0 @ W["W1"].T + p["b1"]
     H1 = bf16(gelu(Z1))
     Z2 = H1 @ W["W2"].T + p["b2"]
@@ -84,23 +114,28 @@ def forward(p, X):
     Z3 = H2 @ W["W3"].T + p["b3"]
     H3 = bf16(gelu(Z3))
     Y = H3 @ W["W4"].T + p["b4"]
-    return dict(W=W, H0=H0, Z1=Z1, H1=H1, Z2=Z2, H2=H2, Z3=Z3, H3=H3, Y=Y)
+    a = dict(W=W, H0=H0, Z1=Z1, H1=H1, Z2=Z2, H2=H2, Z3=Z3, H3=H3, Y=Y)
+    if Bp is not None:
+        a["out"] = contract(Y, np.asarray(Bp, np.float64))
+    return a
 
 
-def loss_and_grads(flat, X, T):
-    """Mean-square loss over the 12 used outputs and the flat gradient."""
+def loss_and_grads(flat, X, Bp, T):
+    """Mean-square loss over the 12 contracted outputs and the flat gradient."""
     p = unpack(flat)
-    a = forward(p, X)
+    Bp = np.asarray(Bp, np.float64)[:, :BPROD]
+    a = forward(p, X, Bp)
     B = X.shape[0]
-    D = (a["Y"] - T)[:, :USED_OUT]
+    D = a["out"] - np.asarray(T, np.float64)[:, :USED_OUT]
     loss = float((D * D).sum() / (12.0 * B))
+    g_out = 2.0 * D / (12.0 * B)
     dYf = np.zeros((B, OUT))
-    dYf[:, :USED_OUT] = 2.0 * D / (12.0 * B)
+    dYf[:, :COEF] = (Bp[:, :, None] * g_out[:, None, :]).reshape(B, COEF)
     dY = bf16(dYf)
     W = a["W"]
     g = {}
     g["W4"] = dY.T @ a["H3"]
-    g["b4"] = dY.sum(0)
+    g["b4"] = dYf.sum(0)
     dH = dY @ W["W4"]
     dZf = dH * gelu_grad(a["Z3"])
     dZ = bf16(dZf)

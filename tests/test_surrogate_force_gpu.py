@@ -140,7 +140,11 @@ def test_untrained_network_falls_back_to_exact(pkg, synth, oracle):
     dln, mat = _params(pkg)
     net, segs = _network(pkg, synth, 512, seed=33, cube=10000.0)
     n = segs.shape[1]
-    sur = pkg.Surrogate(pkg.get_context(), seed=5)  # random weights
+    sur = pkg.Surrogate(pkg.get_context(), seed=5)
+    flat = sur.params()
+    o4 = pkg._PARAM_OFF["b4"][0]
+    flat[o4:o4 + 108] = 10.0  # a network far off the true coefficients
+    sur.set_params(flat)
     F, rep = sur.force(_k(pkg), segs, kappa=20.0, audit_fraction=0.05, audit_tol=1e-3)
     assert rep["tiles_audit"] > 0 and rep["audit_node_rel_rms"] > 1e-3
     assert rep["fallback"] == 1
