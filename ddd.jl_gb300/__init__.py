@@ -505,7 +505,7 @@ class Surrogate:
             segs = np.ascontiguousarray(segs, dtype=np.float64)
             pairs = sample_far_pairs(segs, pairs_per_network, kt, rng, focus)
             P = pairs.shape[1]
-            X = torch.zeros((P, 16), dtype=torch.bfloat16, device="cuda")  # hi and lo feature parts
+            X = torch.zeros((P, 16), dtype=torch.float16, device="cuda")  # hi and lo feature parts
             Bp = torch.zeros((P, 16), dtype=torch.float32, device="cuda")
             T = torch.zeros((P, 16), dtype=torch.float32, device="cuda")
             dsegs, dpairs = torch.from_numpy(segs).cuda(), torch.from_numpy(pairs).cuda()

@@ -54,10 +54,12 @@ cudaError_t launch_segseg_rows_df(const KConsts& K, const double* soa, const flo
                                   int64_t npad, const int64_t* rows, int64_t nRows, double* partial, double* out,
                                   unsigned long long* counters, cudaStream_t st, int form);
 
-// tc_gemm.cu: tcgen05 BF16 GEMM, D = A * B^T (both K-major).
+// tc_gemm.cu: tcgen05 GEMM, D = A * B^T (both K-major), A and B both BF16 or both F16.
 size_t tc_gemm_smem_bytes(int N);
 cudaError_t launch_tc_gemm_bf16(int M, int N, int K, const void* A, const void* B, float* D, int* err,
                                 cudaStream_t st);
+cudaError_t launch_tc_gemm_f16(int M, int N, int K, const void* A, const void* B, float* D, int* err,
+                               cudaStream_t st);
 
 // surrogate_data.cu: features and exact scaled targets of a pair list.
 cudaError_t launch_pair_data(const KConsts& K, const double* soa, int64_t npad, const int32_t* pairs, int64_t P,

@@ -19,15 +19,20 @@
 // are built in; the network learns the angular and L/R dependence.
 #pragma once
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <cstdint>
 
 namespace ddd {
 namespace sur {
 
 constexpr int kGeo = 8;      // geometric features (7 used, padded)
 constexpr int kUsedGeo = 7;
-// Layer-1 input: each feature as two BF16 numbers, hi = bf16(f) and
-// lo = bf16(f - hi) (columns 0-7 and 8-15), against the weights [W1 | W1]:
-// the product sees the features to ~16 significant bits instead of BF16's 8.
+// Layer-1 input: each feature as two FP16 numbers, hi = f16(f) and
+// lo = f16(f - hi) (columns 0-7 and 8-15), against the weights [W1 | W1]:
+// the product sees the features to ~22 significant bits instead of FP16's 11.
+// The forward pass runs in FP16 operands (weights and activations) with FP32
+// accumulation; the GELU epilogue computes two activations per instruction.
 constexpr int kFeatIn = 2 * kGeo;  // 16
 constexpr int kHidden = 128;
 constexpr int kUsedOut = 12;       // node-force components (4 nodes x 3)
@@ -87,14 +92,35 @@ __host__ __device__ __forceinline__ void pair_features(const float r[3], const f
   fr.scale = mu4pi * Li * Lj * invR * invR;
 }
 
-// The features of one pair as the layer-1 operand row: hi parts, then lo parts.
+// The features of one pair as the layer-1 operand row: hi parts, then lo parts
+// (FP32 values that round exactly or to the nearest FP16 when stored).
 __device__ __forceinline__ void split_features(const float* f, float* row) {
 #pragma unroll
   for (int k = 0; k < kGeo; ++k) {
-    const float hi = __bfloat162float(__float2bfloat16_rn(f[k]));
+    const float hi = __half2float(__float2half_rn(f[k]));
     row[k] = hi;
     row[kGeo + k] = f[k] - hi;
   }
+}
+
+__device__ __forceinline__ uint32_t h2_bits(__half2 h) { return *reinterpret_cast<uint32_t*>(&h); }
+__device__ __forceinline__ __half2 bits_h2(uint32_t u) { return *reinterpret_cast<__half2*>(&u); }
+
+// GELU (tanh form) of two FP16 values per instruction: x (x p(x^2)) with
+// p = sqrt(2/pi) (1 + 0.044715 x^2), h = 0.5 x (1 + tanh(x p)), the hardware
+// FP16 tanh approximation.  Errors are a few FP16 ulps (~1e-3 relative), below
+// the rounding of an FP16 activation times the fan-in's averaging; overflow of
+// x^2 for |x| > 256 gives tanh = +-1, i.e. h = x or 0, as the exact function.
+// The training forward pass and the inference kernel both use this function.
+__device__ __forceinline__ __half2 gelu_h2(__half2 x) {
+  const __half2 c1 = __float2half2_rn(0.7978845608f);
+  const __half2 c2 = __float2half2_rn(0.7978845608f * 0.044715f);
+  const __half2 hf = __float2half2_rn(0.5f);
+  const __half2 p = __hfma2(c2, __hmul2(x, x), c1);
+  uint32_t th;
+  asm("tanh.approx.f16x2 %0, %1;" : "=r"(th) : "r"(h2_bits(__hmul2(x, p))));
+  const __half2 hx = __hmul2(hf, x);
+  return __hfma2(hx, bits_h2(th), hx);
 }
 
 // Global-frame force from a scaled local output triple.

@@ -1,10 +1,10 @@
 // Training data of the far-field surrogate: for a list of segment pairs, the
-// layer-1 operand (hi and lo BF16 parts of the geometric features), the
+// layer-1 operand (hi and lo FP16 parts of the geometric features), the
 // Burgers-vector products, and the exact node forces from the FP64 analytic
 // kernel (general or near-parallel branch, DislocationForces.jl :879-1442)
 // expressed as the surrogate's scaled local outputs (surrogate.cuh).  Compiled
 // with --fmad=false so the forces are the strict FP64 ones.
-#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "ddd_internal.h"
@@ -26,9 +26,9 @@ __device__ __forceinline__ SegF64 seg_at(const double* __restrict__ soa, int64_t
 }
 
 // pairs: 2 x P int32 (row i, then row j; 0-based segment indices of the SoA).
-// X [P x 16] BF16, Bp [P x 16] FP32 (9 used), T [P x 16] FP32 (12 used), F [P x 12].
+// X [P x 16] FP16, Bp [P x 16] FP32 (9 used), T [P x 16] FP32 (12 used), F [P x 12].
 __global__ void pair_data(KConsts K, const double* __restrict__ soa, int64_t npad, const int32_t* __restrict__ pairs,
-                          int64_t P, __nv_bfloat16* __restrict__ X, float* __restrict__ Bp, float* __restrict__ T,
+                          int64_t P, __half* __restrict__ X, float* __restrict__ Bp, float* __restrict__ T,
                           double* __restrict__ F) {
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (p >= P) return;
@@ -50,7 +50,7 @@ __global__ void pair_data(KConsts K, const double* __restrict__ soa, int64_t npa
   sur::pair_features(r, ti, tj, bi, bj, (float)(1.0 / a.tN), (float)(1.0 / b.tN), (float)K.mu4pi, f, bp, fr);
   sur::split_features(f, row);
 #pragma unroll
-  for (int k = 0; k < sur::kFeatIn; ++k) X[p * sur::kFeatIn + k] = __float2bfloat16_rn(row[k]);
+  for (int k = 0; k < sur::kFeatIn; ++k) X[p * sur::kFeatIn + k] = __float2half_rn(row[k]);
 #pragma unroll
   for (int k = 0; k < sur::kRow; ++k) Bp[p * sur::kRow + k] = k < sur::kBProd ? bp[k] : 0.0f;
   const D3 Fs[4] = {F1, F2, F3, F4};
@@ -74,7 +74,7 @@ __global__ void pair_data(KConsts K, const double* __restrict__ soa, int64_t npa
 cudaError_t launch_pair_data(const KConsts& K, const double* soa, int64_t npad, const int32_t* pairs, int64_t P,
                              void* X, float* Bp, float* T, double* F, cudaStream_t st) {
   if (P == 0) return cudaSuccess;
-  pair_data<<<(unsigned)((P + 127) / 128), 128, 0, st>>>(K, soa, npad, pairs, P, (__nv_bfloat16*)X, Bp, T, F);
+  pair_data<<<(unsigned)((P + 127) / 128), 128, 0, st>>>(K, soa, npad, pairs, P, (__half*)X, Bp, T, F);
   return cudaGetLastError();
 }
 

@@ -1,7 +1,7 @@
 // Fused inference of the far-field surrogate over tile pairs.
 //
 // A persistent CTA (one per SM, 3 warpgroups = 384 threads) takes tile pairs
-// (I <= J, 128 sorted segments a side) from a work list.  The MLP weights (BF16,
+// (I <= J, 128 sorted segments a side) from a work list.  The MLP weights (FP16,
 // 96 KB) stay in shared memory for the CTA's lifetime; each warpgroup has its
 // own 32 KB activation buffer, its own 128 TMEM columns and its own mbarrier, so
 // the warpgroups run independent layer pipelines and the tensor core works on
@@ -9,9 +9,10 @@
 //
 // Warpgroup g handles the steps k = g, g + 3, ... of the tile pair.  At step k
 // thread t forms pair (row t, column (t + k) mod 128), writes its 8 geometric
-// features (hi and lo BF16 parts) as row t of a 128 x 16 BF16 operand, and the
+// features (hi and lo FP16 parts) as row t of a 128 x 16 FP16 operand, and the
 // layer chain runs as
-//   X (128x16) [W1|W1]^T -> TMEM (128x128 FP32) -> +b1, GELU, BF16 -> H (smem)
+//   X (128x16) [W1|W1]^T -> TMEM (128x128 FP32) -> +b1, GELU (two per
+//   instruction, gelu_h2), FP16 -> H (smem)
 //   H W2^T -> TMEM -> ... -> H W3^T -> TMEM -> ... -> H W4^T -> TMEM (128x112)
 // one thread issuing the tcgen05.mma instructions, the warpgroup waiting on its
 // mbarrier (bounded), each thread reading back its own accumulator row
@@ -26,7 +27,7 @@
 // of the tile pair the four warpgroups' sums are added in a fixed order and
 // written, as doubles, to the tile pair's slot in the same [side][component][T]
 // layout as the exact tile kernels.  No floating-point atomics.
-#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "ddd_internal.h"
@@ -41,10 +42,10 @@ namespace {
 constexpr int TT = 128;  // tile size (segments)
 constexpr int NWG = 3;   // warpgroups per CTA
 constexpr int kThreads = NWG * 128;
-// Shared-memory layout (bytes).  The X operand of a step (128 x 16 BF16) sits
+// Shared-memory layout (bytes).  The X operand of a step (128 x 16 FP16) sits
 // at the start of the warpgroup's H buffer: layer 1 has read it before the
 // first epilogue overwrites it.
-constexpr int kW1 = 0;                            // 128 x 16 BF16, K-major
+constexpr int kW1 = 0;                            // 128 x 16 FP16, K-major
 constexpr int kW2 = kW1 + kHidden * kFeatIn * 2;  // 128 x 128
 constexpr int kW3 = kW2 + kHidden * kHidden * 2;  // 128 x 128
 constexpr int kW4 = kW3 + kHidden * kHidden * 2;  // 112 x 128
@@ -102,12 +103,10 @@ __device__ __forceinline__ void tmem_ld16_async(uint32_t taddr, uint32_t* r) {
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-__device__ __forceinline__ void store_bf16x16(unsigned char* base, int row, int c0, int KC, const float* v) {
-  __nv_bfloat162 p[8];
-#pragma unroll
-  for (int i = 0; i < 8; ++i) p[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
-  *reinterpret_cast<uint4*>(base + tc::kmajor_offset(row, c0, KC)) = *reinterpret_cast<uint4*>(&p[0]);
-  *reinterpret_cast<uint4*>(base + tc::kmajor_offset(row, c0 + 8, KC)) = *reinterpret_cast<uint4*>(&p[4]);
+// 16 FP16 values (8 packed pairs) of row `row`, columns c0..c0+15, of a K-major tile.
+__device__ __forceinline__ void store_h16(unsigned char* base, int row, int c0, int KC, const __half2* p) {
+  *reinterpret_cast<uint4*>(base + tc::kmajor_offset(row, c0, KC)) = *reinterpret_cast<const uint4*>(&p[0]);
+  *reinterpret_cast<uint4*>(base + tc::kmajor_offset(row, c0 + 8, KC)) = *reinterpret_cast<const uint4*>(&p[4]);
 }
 
 // The layer's MMAs (one thread of the warpgroup issues them) and the wait for
@@ -121,7 +120,7 @@ __device__ __forceinline__ bool layer(uint32_t tm, const unsigned char* A, const
     tc::fence_after_sync();
     const uint32_t a = tc::smem_addr(A), b = tc::smem_addr(B);
     const uint32_t sbo = (uint32_t)(K / 8) * 128u;
-    const uint32_t idesc = tc::idesc_bf16_f32(128, N);
+    const uint32_t idesc = tc::idesc_f16_f32(128, N);  // A and B both FP16
     for (int kk = 0; kk < K; kk += 16)
       tc::mma_bf16(tm, tc::smem_desc(a + (uint32_t)(kk / 8) * 128u, 128u, sbo),
                    tc::smem_desc(b + (uint32_t)(kk / 8) * 128u, 128u, sbo), idesc, kk > 0 ? 1u : 0u);
@@ -134,7 +133,8 @@ __device__ __forceinline__ bool layer(uint32_t tm, const unsigned char* A, const
   return ok;
 }
 
-// Row t of the warpgroup's 128-column accumulator + bias, GELU, BF16, into H.
+// Row t of the warpgroup's 128-column accumulator + bias (FP32), GELU on FP16
+// pairs, into H (FP16): the same arithmetic as the training forward pass.
 __device__ __forceinline__ void hidden_epilogue(uint32_t tm_row, const float* bias, unsigned char* H, int t) {
 #pragma unroll 1
   for (int c0 = 0; c0 < kHidden; c0 += 32) {
@@ -142,18 +142,20 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t tm_row, const float* bi
     tmem_ld16_async(tm_row + (uint32_t)c0, r);
     tmem_ld16_async(tm_row + (uint32_t)c0 + 16u, r + 16);
     tmem_wait_ld();
-    float v[32];
+    __half2 h[16];
 #pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = gelu(__uint_as_float(r[i]) + bias[c0 + i]);
-    store_bf16x16(H, t, c0, kHidden, v);
-    store_bf16x16(H, t, c0 + 16, kHidden, v + 16);
+    for (int i = 0; i < 16; ++i)
+      h[i] = gelu_h2(__floats2half2_rn(__uint_as_float(r[2 * i]) + bias[c0 + 2 * i],
+                                       __uint_as_float(r[2 * i + 1]) + bias[c0 + 2 * i + 1]));
+    store_h16(H, t, c0, kHidden, h);
+    store_h16(H, t, c0 + 16, kHidden, h + 8);
   }
 }
 
 __global__ void __launch_bounds__(kThreads, 1)
 mlp_far_tiles(const float* __restrict__ ms, int64_t npad, const int4* __restrict__ items, int32_t nItems,
-              int32_t* __restrict__ next, const __nv_bfloat16* __restrict__ W1, const __nv_bfloat16* __restrict__ W2,
-              const __nv_bfloat16* __restrict__ W3, const __nv_bfloat16* __restrict__ W4,
+              int32_t* __restrict__ next, const __half* __restrict__ W1, const __half* __restrict__ W2,
+              const __half* __restrict__ W3, const __half* __restrict__ W4,
               const float* __restrict__ params, float mu4pi, float kappa2, double* __restrict__ partial,
               int32_t* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -169,7 +171,7 @@ mlp_far_tiles(const float* __restrict__ ms, int64_t npad, const int4* __restrict
   unsigned char* H = smem + kH + wg * kHBytes;
 
   // Weights (K-major core-matrix layout) and biases into shared memory, once.
-  auto stage = [&](const __nv_bfloat16* W, int rows, int K, int off) {
+  auto stage = [&](const __half* W, int rows, int K, int off) {
     for (int idx = tid; idx < rows * (K / 8); idx += kThreads) {
       const int r = idx / (K / 8), kb = idx % (K / 8);
       *reinterpret_cast<uint4*>(smem + off + tc::kmajor_offset(r, kb * 8, K)) =
@@ -243,7 +245,10 @@ mlp_far_tiles(const float* __restrict__ ms, int64_t npad, const int4* __restrict
       }
       float row[kFeatIn];
       split_features(f, row);
-      store_bf16x16(H, t, 0, kFeatIn, row);
+      __half2 x[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) x[i] = __floats2half2_rn(row[2 * i], row[2 * i + 1]);
+      store_h16(H, t, 0, kFeatIn, x);
 
       if (!(ok = layer(tm, H, smem + kW1, kFeatIn, kHidden, &mbar[wg], phase, leader, bar))) break;
       hidden_epilogue(tm_row, sBias, H, t);
@@ -337,9 +342,9 @@ cudaError_t launch_mlp_far_tiles(const float* ms, int64_t npad, const int4* item
   cudaError_t e = prepare_mlp_far_tiles();
   if (e != cudaSuccess) return e;
   if (nItems <= 0) return cudaSuccess;
-  mlp_far_tiles<<<grid, kThreads, kSmem, st>>>(ms, npad, items, nItems, next, (const __nv_bfloat16*)W[0],
-                                               (const __nv_bfloat16*)W[1], (const __nv_bfloat16*)W[2],
-                                               (const __nv_bfloat16*)W[3], params, mu4pi, kappa2, partial, err);
+  mlp_far_tiles<<<grid, kThreads, kSmem, st>>>(ms, npad, items, nItems, next, (const __half*)W[0],
+                                               (const __half*)W[1], (const __half*)W[2], (const __half*)W[3],
+                                               params, mu4pi, kappa2, partial, err);
   return cudaGetLastError();
 }
 

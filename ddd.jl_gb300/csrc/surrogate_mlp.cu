@@ -1,11 +1,11 @@
 // Training and batched evaluation of the far-field surrogate MLP
-// (16 -> 128 -> 128 -> 128 -> 112, GELU, BF16 operands, FP32 accumulation) and
+// (16 -> 128 -> 128 -> 128 -> 112, GELU, FP16 operands, FP32 accumulation) and
 // its Burgers-vector contraction (surrogate.cuh) on the GPU with the project's
 // own kernels: every matrix product is the tcgen05 GEMM (tc_gemm.cu);
 // activations, the contraction, losses, transposes, bias gradients and the Adam
 // update are small elementwise / reduction kernels here.
 //
-// Forward (batch B; X [B x 16] BF16: hi and lo parts of the 8 geometric
+// Forward (batch B; X [B x 16] FP16: hi and lo parts of the 8 geometric
 // features; Bp [B x 16] FP32: the 9 Burgers-vector products):
 //   Z_1 = X [W_1 | W_1]^T + b_1 (= (X_hi + X_lo) W_1^T + b_1),
 //   Z_l = H_{l-1} W_l^T + b_l,  H_l = GELU(Z_l),  Y = H_3 W_4^T + b_4 (112 wide),
@@ -14,8 +14,10 @@
 // Backward: dout = 2 (out - T) / (12 B);  dY[12 ac + o] = Bp[ac] dout[o];
 //   dW_4 = dY^T H_3 (computed as (H_3^T dY)^T),  dH_l = dZ_{l+1} W_{l+1},
 //   dZ_l = dH_l * GELU'(Z_l),  dW_l = dZ_l^T H_{l-1},  db_l = column sums of dZ_l;
-//   dW_1 = sum of the two 8-column halves of dZ_1^T X.  GEMM operands are BF16
-//   (transposed copies where the GEMM needs K contiguous); accumulations, bias
+//   dW_1 = sum of the two 8-column halves of dZ_1^T X.  Forward GEMM operands are
+//   FP16 (weights, activations; the GELU is gelu_h2 of surrogate.cuh, as in the
+//   inference kernel), backward GEMM operands BF16 (gradients, and BF16 copies
+//   of the weights and of the transposed activations); accumulations, bias
 //   grads and Adam are FP32.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -35,13 +37,17 @@ using namespace ddd::sur;
 namespace ddd {
 namespace {
 
-__global__ void bias_gelu_fwd(float* __restrict__ Z, const float* __restrict__ bias, __nv_bfloat16* __restrict__ H,
+// Z += bias (FP32, kept for the backward pass); H = gelu_h2(f16(Z)), two
+// adjacent columns per thread (cols even).
+__global__ void bias_gelu_fwd(float* __restrict__ Z, const float* __restrict__ bias, __half* __restrict__ H,
                               int64_t rows, int cols) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t i = 2 * (blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
   if (i >= rows * cols) return;
-  const float z = Z[i] + bias[i % cols];
-  Z[i] = z;
-  H[i] = __float2bfloat16_rn(gelu(z));
+  const int c = (int)(i % cols);
+  const float z0 = Z[i] + bias[c], z1 = Z[i + 1] + bias[c + 1];
+  Z[i] = z0;
+  Z[i + 1] = z1;
+  *reinterpret_cast<__half2*>(H + i) = gelu_h2(__floats2half2_rn(z0, z1));
 }
 
 // Per sample p: y = Y[p] + b4, out[o] = sum_ac Bp[p][ac] y[12 ac + o].  With T:
@@ -117,37 +123,46 @@ __global__ void gelu_bwd(const float* __restrict__ dH, const float* __restrict__
   dZf[i] = g;
 }
 
-// out[C x R] = in[R x C]^T (BF16), 32 x 32 tiles through shared memory.
-__global__ void transpose_bf16(const __nv_bfloat16* __restrict__ in, __nv_bfloat16* __restrict__ out, int64_t R,
-                               int C) {
-  __shared__ __nv_bfloat16 tile[32][33];
+__device__ __forceinline__ float to_f(float v) { return v; }
+__device__ __forceinline__ float to_f(__half v) { return __half2float(v); }
+__device__ __forceinline__ float to_f(__nv_bfloat16 v) { return __bfloat162float(v); }
+template <class T>
+__device__ __forceinline__ T from_f(float v);
+template <>
+__device__ __forceinline__ __nv_bfloat16 from_f<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
+
+// out[C x R] = in[R x C]^T converted to BF16 (BF16 copies exact; FP16 / FP32
+// values rounded), 32 x 32 tiles through shared memory.
+template <class Tin>
+__global__ void transpose_to_bf16(const Tin* __restrict__ in, __nv_bfloat16* __restrict__ out, int64_t R, int C) {
+  __shared__ float tile[32][33];
   const int64_t r0 = blockIdx.x * 32;
   const int c0 = blockIdx.y * 32;
   for (int k = threadIdx.y; k < 32; k += blockDim.y) {
     const int64_t r = r0 + k;
     const int c = c0 + threadIdx.x;
-    if (r < R && c < C) tile[k][threadIdx.x] = in[r * C + c];
+    if (r < R && c < C) tile[k][threadIdx.x] = to_f(in[r * C + c]);
   }
   __syncthreads();
   for (int k = threadIdx.y; k < 32; k += blockDim.y) {
     const int c = c0 + k;
     const int64_t r = r0 + threadIdx.x;
-    if (r < R && c < C) out[(int64_t)c * R + r] = tile[threadIdx.x][k];
+    if (r < R && c < C) out[(int64_t)c * R + r] = from_f<__nv_bfloat16>(tile[threadIdx.x][k]);
   }
 }
 
-__global__ void f32_to_bf16(const float* __restrict__ in, __nv_bfloat16* __restrict__ out, int64_t n) {
+__global__ void f32_to_f16(const float* __restrict__ in, __half* __restrict__ out, int64_t n) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < n) out[i] = __float2bfloat16_rn(in[i]);
+  if (i < n) out[i] = __float2half_rn(in[i]);
 }
 
-// [W1 | W1] (128 x 16 BF16) from W1 (128 x 8 FP32): the layer-1 weights of the
+// [W1 | W1] (128 x 16 FP16) from W1 (128 x 8 FP32): the layer-1 weights of the
 // hi / lo feature columns.
-__global__ void w1_dup(const float* __restrict__ W1, __nv_bfloat16* __restrict__ out) {
+__global__ void w1_dup(const float* __restrict__ W1, __half* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= kHidden * kGeo) return;
   const int o = i / kGeo, k = i % kGeo;
-  const __nv_bfloat16 w = __float2bfloat16_rn(W1[i]);
+  const __half w = __float2half_rn(W1[i]);
   out[o * kFeatIn + k] = w;
   out[o * kFeatIn + kGeo + k] = w;
 }
@@ -247,20 +262,23 @@ cudaError_t ensure_batch(ddd_surrogate* s, int64_t B) {
     if (_e != cudaSuccess) return _e;      \
   } while (0)
 
-cudaError_t transpose(const __nv_bfloat16* in, __nv_bfloat16* out, int64_t R, int C, cudaStream_t st) {
-  transpose_bf16<<<dim3((unsigned)((R + 31) / 32), (unsigned)((C + 31) / 32)), dim3(32, 8), 0, st>>>(in, out, R, C);
+template <class Tin>
+cudaError_t transpose(const Tin* in, __nv_bfloat16* out, int64_t R, int C, cudaStream_t st) {
+  transpose_to_bf16<Tin><<<dim3((unsigned)((R + 31) / 32), (unsigned)((C + 31) / 32)), dim3(32, 8), 0, st>>>(in, out, R,
+                                                                                                         C);
   return cudaGetLastError();
 }
 
 // BF16 weights and transposes from the FP32 master copy.
 cudaError_t refresh_weights(ddd_surrogate* s, cudaStream_t st) {
   w1_dup<<<blocks(kHidden * kGeo), 256, 0, st>>>(s->P + kOffW1, s->W1);
-  f32_to_bf16<<<blocks(kHidden * kHidden), 256, 0, st>>>(s->P + kOffW2, s->W2, kHidden * kHidden);
-  f32_to_bf16<<<blocks(kHidden * kHidden), 256, 0, st>>>(s->P + kOffW3, s->W3, kHidden * kHidden);
-  f32_to_bf16<<<blocks(kOut * kHidden), 256, 0, st>>>(s->P + kOffW4, s->W4, kOut * kHidden);
-  RET(transpose(s->W2, s->W2T, kHidden, kHidden, st));
-  RET(transpose(s->W3, s->W3T, kHidden, kHidden, st));
-  RET(transpose(s->W4, s->W4T, kOut, kHidden, st));  // [128 x 112]
+  f32_to_f16<<<blocks(kHidden * kHidden), 256, 0, st>>>(s->P + kOffW2, s->W2, kHidden * kHidden);
+  f32_to_f16<<<blocks(kHidden * kHidden), 256, 0, st>>>(s->P + kOffW3, s->W3, kHidden * kHidden);
+  f32_to_f16<<<blocks(kOut * kHidden), 256, 0, st>>>(s->P + kOffW4, s->W4, kOut * kHidden);
+  // BF16 transposes of the FP32 master weights for the backward pass.
+  RET(transpose(s->P + kOffW2, s->W2T, kHidden, kHidden, st));
+  RET(transpose(s->P + kOffW3, s->W3T, kHidden, kHidden, st));
+  RET(transpose(s->P + kOffW4, s->W4T, kOut, kHidden, st));  // [128 x 112]
   return cudaGetLastError();
 }
 
@@ -273,19 +291,19 @@ cudaError_t colsum(ddd_surrogate* s, const float* m, int64_t rows, int cols, flo
 }
 
 // Forward over a batch of B rows (B % 128 == 0): Z/H buffers and Y filled.
-cudaError_t forward(ddd_surrogate* s, const __nv_bfloat16* X, int64_t B, cudaStream_t st) {
-  RET(launch_tc_gemm_bf16((int)B, kHidden, kFeatIn, X, s->W1, s->Z1, s->err, st));
-  bias_gelu_fwd<<<blocks(B * kHidden), 256, 0, st>>>(s->Z1, s->P + kOffB1, s->H1, B, kHidden);
-  RET(launch_tc_gemm_bf16((int)B, kHidden, kHidden, s->H1, s->W2, s->Z2, s->err, st));
-  bias_gelu_fwd<<<blocks(B * kHidden), 256, 0, st>>>(s->Z2, s->P + kOffB2, s->H2, B, kHidden);
-  RET(launch_tc_gemm_bf16((int)B, kHidden, kHidden, s->H2, s->W3, s->Z3, s->err, st));
-  bias_gelu_fwd<<<blocks(B * kHidden), 256, 0, st>>>(s->Z3, s->P + kOffB3, s->H3, B, kHidden);
-  RET(launch_tc_gemm_bf16((int)B, kOut, kHidden, s->H3, s->W4, s->Y, s->err, st));
+cudaError_t forward(ddd_surrogate* s, const __half* X, int64_t B, cudaStream_t st) {
+  RET(launch_tc_gemm_f16((int)B, kHidden, kFeatIn, X, s->W1, s->Z1, s->err, st));
+  bias_gelu_fwd<<<blocks(B * kHidden / 2), 256, 0, st>>>(s->Z1, s->P + kOffB1, s->H1, B, kHidden);
+  RET(launch_tc_gemm_f16((int)B, kHidden, kHidden, s->H1, s->W2, s->Z2, s->err, st));
+  bias_gelu_fwd<<<blocks(B * kHidden / 2), 256, 0, st>>>(s->Z2, s->P + kOffB2, s->H2, B, kHidden);
+  RET(launch_tc_gemm_f16((int)B, kHidden, kHidden, s->H2, s->W3, s->Z3, s->err, st));
+  bias_gelu_fwd<<<blocks(B * kHidden / 2), 256, 0, st>>>(s->Z3, s->P + kOffB3, s->H3, B, kHidden);
+  RET(launch_tc_gemm_f16((int)B, kOut, kHidden, s->H3, s->W4, s->Y, s->err, st));
   return cudaGetLastError();
 }
 
 // Loss (added into *s->loss, mean over the batch) and gradients into s->G.
-cudaError_t backward(ddd_surrogate* s, const __nv_bfloat16* X, const float* Bp, const float* T, int64_t B,
+cudaError_t backward(ddd_surrogate* s, const __half* X, const float* Bp, const float* T, int64_t B,
                      cudaStream_t st) {
   const int nLoss = (int)blocks(B);
   contract<<<nLoss, 256, 0, st>>>(s->Y, s->P + kOffB4, Bp, T, B, nullptr, s->dYf, s->dY, s->lossPart);
@@ -412,8 +430,8 @@ int ddd_surrogate_grads(ddd_surrogate* s, const void* X, const float* Bp, const 
   cudaError_t e = ensure_batch(s, B);
   if (e == cudaSuccess) e = cudaMemsetAsync(s->loss, 0, sizeof(double), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(s->err, 0, sizeof(int), st);
-  if (e == cudaSuccess) e = forward(s, (const __nv_bfloat16*)X, B, st);
-  if (e == cudaSuccess) e = backward(s, (const __nv_bfloat16*)X, Bp, T, B, st);
+  if (e == cudaSuccess) e = forward(s, (const __half*)X, B, st);
+  if (e == cudaSuccess) e = backward(s, (const __half*)X, Bp, T, B, st);
   int flag = 0;
   if (e == cudaSuccess && loss) e = cudaMemcpyAsync(loss, s->loss, sizeof(double), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess && grads)
@@ -442,7 +460,7 @@ int ddd_surrogate_train(ddd_surrogate* s, const void* X, const float* Bp, const 
     // Cosine learning-rate schedule over the epochs.
     const float lre = 0.5f * lr * (1.0f + std::cos(3.14159265f * (float)ep / (float)epochs));
     for (int64_t b = 0; b < nb && e == cudaSuccess; ++b) {
-      const __nv_bfloat16* xb = (const __nv_bfloat16*)X + b * B * kFeatIn;
+      const __half* xb = (const __half*)X + b * B * kFeatIn;
       const float* bpb = Bp + b * B * kRow;
       const float* tb = T + b * B * kRow;
       e = forward(s, xb, B, st);
@@ -480,7 +498,7 @@ int ddd_surrogate_forward(ddd_surrogate* s, const void* X, const float* Bp, int6
   if (e == cudaSuccess) e = cudaMemsetAsync(s->err, 0, sizeof(int), st);
   for (int64_t off = 0; off < P && e == cudaSuccess; off += B) {
     const int64_t b = (P - off) < B ? (P - off) : B;
-    e = forward(s, (const __nv_bfloat16*)X + off * kFeatIn, b, st);
+    e = forward(s, (const __half*)X + off * kFeatIn, b, st);
     if (e != cudaSuccess) break;
     contract<<<blocks(b), 256, 0, st>>>(s->Y, s->P + kOffB4, Bp + off * kRow, nullptr, b, O + off * kRow, nullptr,
                                         nullptr, nullptr);

@@ -2,6 +2,7 @@
 // and the force path (surrogate_force.cu).
 #pragma once
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -17,17 +18,18 @@ struct ddd_surrogate {
   cudaStream_t own = nullptr;
   // parameters, gradients, Adam moments (FP32, flat layout of surrogate.cuh)
   float *P = nullptr, *G = nullptr, *M1 = nullptr, *M2 = nullptr;
-  // BF16 weights [out x in] (W1: [W1 | W1], 128 x 32) and transposes [in x out]
-  __nv_bfloat16 *W1 = nullptr, *W2 = nullptr, *W3 = nullptr, *W4 = nullptr;
+  // FP16 forward weights [out x in] (W1: [W1 | W1], 128 x 16) and BF16
+  // transposes [in x out] for the backward pass
+  __half *W1 = nullptr, *W2 = nullptr, *W3 = nullptr, *W4 = nullptr;
   __nv_bfloat16 *W2T = nullptr, *W3T = nullptr, *W4T = nullptr;
   int64_t step = 0;
   // activations for the current batch capacity
   int64_t cap = 0;
   float *Z1 = nullptr, *Z2 = nullptr, *Z3 = nullptr, *Y = nullptr, *dH = nullptr, *dZf = nullptr, *dYf = nullptr;
-  __nv_bfloat16 *H1 = nullptr, *H2 = nullptr, *H3 = nullptr, *dY = nullptr, *dZ = nullptr, *AT = nullptr,
-                *BT = nullptr;
+  __half *H1 = nullptr, *H2 = nullptr, *H3 = nullptr;  // FP16 activations
+  __nv_bfloat16 *dY = nullptr, *dZ = nullptr, *AT = nullptr, *BT = nullptr;
   float *gT = nullptr, *colpart = nullptr;
-  float* gW1 = nullptr;  // layer-1 weight gradient before folding, 128 x 32
+  float* gW1 = nullptr;  // layer-1 weight gradient before folding, 128 x 16
   double *lossPart = nullptr, *loss = nullptr;
   int* err = nullptr;
   ddd::SurForcePlan* plan = nullptr;  // buffers of the force path, per segment count

@@ -1,5 +1,6 @@
-// BF16 tensor-core GEMM on tcgen05: D[M x N] (FP32) = A[M x K] * B[N x K]^T, A and
-// B row-major with K contiguous (both operands K-major), M a multiple of 128,
+// Tensor-core GEMM on tcgen05: D[M x N] (FP32) = A[M x K] * B[N x K]^T, A and B
+// both BF16 or both F16 (the instruction descriptor carries the type), row-major
+// with K contiguous (both operands K-major), M a multiple of 128,
 // N a multiple of 16 up to 256, K a multiple of 16.  The building block of the
 // surrogate's training and inference; one CTA (4 warps) per 128-row block.
 //
@@ -22,11 +23,11 @@ namespace {
 constexpr int KC = 64;
 
 __global__ void __launch_bounds__(128, 1)
-tc_gemm_bf16_tn(int M, int N, int K, const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __restrict__ B,
-                float* __restrict__ D, int* __restrict__ err) {
+tc_gemm_tn(int M, int N, int K, const uint16_t* __restrict__ A, const uint16_t* __restrict__ B,
+           float* __restrict__ D, int* __restrict__ err, uint32_t idesc) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  unsigned char* sA = smem;                 // 128 x KC bf16
-  unsigned char* sB = smem + 128 * KC * 2;  // N x KC bf16
+  unsigned char* sA = smem;                 // 128 x KC 16-bit
+  unsigned char* sB = smem + 128 * KC * 2;  // N x KC 16-bit
   __shared__ uint64_t mbar;
   __shared__ uint32_t s_taddr;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
@@ -40,7 +41,6 @@ tc_gemm_bf16_tn(int M, int N, int K, const __nv_bfloat16* __restrict__ A, const 
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t taddr = s_taddr;
-  const uint32_t idesc = tc::idesc_bf16_f32(128, N);
   uint32_t phase = 0;
   bool ok = true;
 
@@ -97,17 +97,28 @@ tc_gemm_bf16_tn(int M, int N, int K, const __nv_bfloat16* __restrict__ A, const 
 
 size_t tc_gemm_smem_bytes(int N) { return (size_t)(128 + N) * KC * 2; }
 
-cudaError_t launch_tc_gemm_bf16(int M, int N, int K, const void* A, const void* B, float* D, int* err,
-                                cudaStream_t st) {
+static cudaError_t launch_tc_gemm(int M, int N, int K, const void* A, const void* B, float* D, int* err,
+                                  cudaStream_t st, bool f16) {
   const int smem = (int)tc_gemm_smem_bytes(N);
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(tc_gemm_bf16_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
+    cudaError_t e = cudaFuncSetAttribute(tc_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  tc_gemm_bf16_tn<<<M / 128, 128, smem, st>>>(M, N, K, (const __nv_bfloat16*)A, (const __nv_bfloat16*)B, D, err);
+  tc_gemm_tn<<<M / 128, 128, smem, st>>>(M, N, K, (const uint16_t*)A, (const uint16_t*)B, D, err,
+                                         tc::idesc_f32acc(128, N, f16));
   return cudaGetLastError();
+}
+
+cudaError_t launch_tc_gemm_bf16(int M, int N, int K, const void* A, const void* B, float* D, int* err,
+                                cudaStream_t st) {
+  return launch_tc_gemm(M, N, K, A, B, D, err, st, false);
+}
+
+cudaError_t launch_tc_gemm_f16(int M, int N, int K, const void* A, const void* B, float* D, int* err,
+                               cudaStream_t st) {
+  return launch_tc_gemm(M, N, K, A, B, D, err, st, true);
 }
 
 }  // namespace ddd

@@ -1,5 +1,5 @@
 // Blackwell (sm_100-family) tensor-core primitives as inline PTX: TMEM
-// allocation, tcgen05.mma (kind::f16, BF16 inputs, FP32 accumulators in TMEM),
+// allocation, tcgen05.mma (kind::f16, BF16 or F16 inputs, FP32 accumulators in TMEM),
 // commit to an mbarrier, bounded mbarrier waits, tcgen05.ld of accumulators.
 //
 // Operand staging: K-major tiles without swizzle, built from 8 x 16-byte "core
@@ -35,17 +35,19 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
   return d;
 }
 
-// Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major,
+// Instruction descriptor, kind::f16: D = F32, A and B both BF16 (or both F16
+// with f16 = true; the two operands always share one type), both K-major,
 // dense, shape M x N (M = 128 here, N multiple of 16 up to 256).
-__host__ __device__ __forceinline__ uint32_t idesc_bf16_f32(int M, int N) {
+__host__ __device__ __forceinline__ uint32_t idesc_f32acc(int M, int N, bool f16) {
   uint32_t d = 0;
   d |= 1u << 4;                        // D format: F32
-  d |= 1u << 7;                        // A format: BF16
-  d |= 1u << 10;                       // B format: BF16
+  if (!f16) d |= (1u << 7) | (1u << 10);  // A and B format: BF16 (F16 = 0)
   d |= (uint32_t)(N >> 3) << 17;       // N / 8
   d |= (uint32_t)(M >> 4) << 24;       // M / 16
   return d;
 }
+__host__ __device__ __forceinline__ uint32_t idesc_bf16_f32(int M, int N) { return idesc_f32acc(M, N, false); }
+__host__ __device__ __forceinline__ uint32_t idesc_f16_f32(int M, int N) { return idesc_f32acc(M, N, true); }
 
 __device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols) {
   asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(dst_smem)),
@@ -61,6 +63,7 @@ __device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence
 // Makes this thread's shared-memory writes visible to the tensor core (async proxy).
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
+// The operand type is in idesc; the instruction is the same for BF16 and F16.
 __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
                                          uint32_t accumulate) {
   asm volatile(

@@ -210,14 +210,14 @@ int ddd_tc_gemm_bf16(ddd_ctx* ctx, int M, int N, int K, const void* A, const voi
 /* Learned far-field surrogate (no reference counterpart; the north-star
  * extension).  A pair's four node forces, in the pair's own frame and scaled by
  * mu4pi L_i L_j / R^2, are bilinear in the two Burgers vectors; a small MLP
- * (16 -> 128 -> 128 -> 128 -> 112, GELU, BF16 operands, FP32 accumulation) maps
+ * (16 -> 128 -> 128 -> 128 -> 112, GELU, FP16 operands, FP32 accumulation) maps
  * the pair geometry to the 108 coefficients of that bilinear form, and an exact
  * contraction with (b_i.e_a)(b_j.e_c) gives the forces (features, frame and
  * contraction: csrc/surrogate.cuh).  It is trained on the GPU by this library's
- * kernels (tcgen05 GEMMs, Adam) on pairs whose exact forces the FP64 kernel
- * computes.  Per-sample rows (device, row-major):
- *   X  BF16 [P x 16]: the 8 geometric features' hi parts bf16(f), then their
- *      lo parts bf16(f - hi);
+ * kernels (tcgen05 GEMMs: FP16 forward, BF16 backward; Adam) on pairs whose
+ * exact forces the FP64 kernel computes.  Per-sample rows (device, row-major):
+ *   X  FP16 [P x 16]: the 8 geometric features' hi parts f16(f), then their
+ *      lo parts f16(f - hi);
  *   Bp FP32 [P x 16]: the 9 Burgers-vector products (7 zero columns);
  *   T  FP32 [P x 16]: the 12 scaled exact node forces (4 zero columns).
  *   make_data: X, Bp, T of the pairs (i, j) in `pairs` (device int32, 2 x P:

@@ -2,14 +2,15 @@
 
 A float64 NumPy restatement of the surrogate's features and Burgers-vector
 contraction (csrc/surrogate.cuh) and of the MLP's forward pass, loss and
-gradients (csrc/surrogate_mlp.cu), rounding to BF16 at the same points as the
-GPU (inputs, weights, hidden activations, the coefficient gradient, hidden-layer
-gradients fed to the GEMMs), so the GPU's gradients can be checked against it.
-GELU uses the exact tanh here; the GPU uses the hardware tanh approximation
-(relative error ~2^-11).
+gradients (csrc/surrogate_mlp.cu), rounding at the same points as the GPU: the
+forward pass in FP16 (inputs, weights, hidden activations), the backward pass in
+BF16 (the coefficient gradient, hidden-layer gradients, and BF16 copies of the
+weights and activations fed to the backward GEMMs), so the GPU's gradients can
+be checked against it.  GELU is the exact function here; the GPU evaluates it
+on FP16 pairs with the hardware tanh approximation (a few FP16 ulps).
 
 Model: the network maps the 8 geometric features of a pair (layer 1 takes each
-as two BF16 numbers, hi = bf16(f) and lo = bf16(f - hi), against the weights
+as two FP16 numbers, hi = f16(f) and lo = f16(f - hi), against the weights
 [W1 | W1], so its product is (hi + lo) W1^T) to 112 outputs Y, of which 108 are
 the coefficients C[ac][o] = Y[12 ac + o] of the bilinear form
     out[o] = sum_ac Bp[ac] C[ac][o],   Bp[3 a + c] = (b_i.e_a)(b_j.e_c),
@@ -38,13 +39,18 @@ def bf16(a):
     return r.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
+def f16(a):
+    """Round to the nearest FP16 (ties to even), returned as float64."""
+    return np.asarray(a, dtype=np.float32).astype(np.float16).astype(np.float64)
+
+
 def split(f):
-    """Layer-1 operand rows (..., 16) of geometric features f (..., 8): hi = bf16(f)
-    and lo = bf16(f - hi), the difference taken in float32 (exact), as
+    """Layer-1 operand rows (..., 16) of geometric features f (..., 8): hi = f16(f)
+    and lo = f16(f - hi), the difference taken in float32 (exact), as
     split_features in csrc/surrogate.cuh."""
     f32 = np.asarray(f, dtype=np.float32)
-    hi = bf16(f32)
-    lo = bf16(f32 - hi.astype(np.float32))
+    hi = f16(f32)
+    lo = f16(f32 - hi.astype(np.float32))
     return np.concatenate([hi, lo], axis=-1)
 
 
@@ -101,20 +107,20 @@ def contract(Y, Bp):
 
 
 def forward(p, X, Bp=None):
-    """Activations of the GPU's forward pass (BF16 rounding at the GEMM inputs);
+    """Activations of the GPU's forward pass (FP16 rounding at the GEMM inputs);
     X holds layer-1 operand rows (B x 16, hi and lo parts, see split).  With Bp
     (B x 9 or wider), also the contracted outputs `out`."""
-    W = {k: bf16(p[k]) if k.startswith("W") else p[k] for k in p}
-    X = bf16(X)
+    W = {k: f16(p[k]) for k in p if k.startswith("W")}
+    X = f16(X)
     H0 = X[:, :GEO] + X[:, GEO:]
     Z1 = H0 @ W["W1"].T + p["b1"]
-    H1 = bf16(gelu(Z1))
+    H1 = f16(gelu(Z1))
     Z2 = H1 @ W["W2"].T + p["b2"]
-    H2 = bf16(gelu(Z2))
+    H2 = f16(gelu(Z2))
     Z3 = H2 @ W["W3"].T + p["b3"]
-    H3 = bf16(gelu(Z3))
+    H3 = f16(gelu(Z3))
     Y = H3 @ W["W4"].T + p["b4"]
-    a = dict(W=W, H0=H0, Z1=Z1, H1=H1, Z2=Z2, H2=H2, Z3=Z3, H3=H3, Y=Y)
+    a = dict(X=X, H0=H0, Z1=Z1, H1=H1, Z2=Z2, H2=H2, Z3=Z3, H3=H3, Y=Y)
     if Bp is not None:
         a["out"] = contract(Y, np.asarray(Bp, np.float64))
     return a
@@ -132,23 +138,24 @@ def loss_and_grads(flat, X, Bp, T):
     dYf = np.zeros((B, OUT))
     dYf[:, :COEF] = (Bp[:, :, None] * g_out[:, None, :]).reshape(B, COEF)
     dY = bf16(dYf)
-    W = a["W"]
+    Wb = {k: bf16(p[k]) for k in p if k.startswith("W")}  # BF16 copies of the FP32 master weights
+    X = a["X"]
     g = {}
-    g["W4"] = dY.T @ a["H3"]
+    g["W4"] = dY.T @ bf16(a["H3"])
     g["b4"] = dYf.sum(0)
-    dH = dY @ W["W4"]
+    dH = dY @ Wb["W4"]
     dZf = dH * gelu_grad(a["Z3"])
     dZ = bf16(dZf)
-    g["W3"] = dZ.T @ a["H2"]
+    g["W3"] = dZ.T @ bf16(a["H2"])
     g["b3"] = dZf.sum(0)
-    dH = dZ @ W["W3"]
+    dH = dZ @ Wb["W3"]
     dZf = dH * gelu_grad(a["Z2"])
     dZ = bf16(dZf)
-    g["W2"] = dZ.T @ a["H1"]
+    g["W2"] = dZ.T @ bf16(a["H1"])
     g["b2"] = dZf.sum(0)
-    dH = dZ @ W["W2"]
+    dH = dZ @ Wb["W2"]
     dZf = dH * gelu_grad(a["Z1"])
     dZ = bf16(dZf)
-    g["W1"] = dZ.T @ a["H0"]
+    g["W1"] = dZ.T @ (bf16(X[:, :GEO]) + bf16(X[:, GEO:]))
     g["b1"] = dZf.sum(0)
     return loss, pack(g)
