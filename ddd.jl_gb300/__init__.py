@@ -78,7 +78,8 @@ class ddd_report(ctypes.Structure):
 
 
 class ddd_sur_opts(ctypes.Structure):
-    _fields_ = [("kappa", ctypes.c_double), ("audit_fraction", ctypes.c_double), ("audit_tol", ctypes.c_double)]
+    _fields_ = [("kappa", ctypes.c_double), ("audit_fraction", ctypes.c_double), ("audit_tol", ctypes.c_double),
+                ("exact_mode", ctypes.c_int)]
 
 
 class ddd_sur_report(ctypes.Structure):
@@ -541,10 +542,12 @@ class Surrogate:
         return {"loss": hist, "samples": P, "sigma": s12}
 
     # -- forces ---------------------------------------------------------------
-    def force(self, k, segs, ext=None, kappa=None, audit_fraction=0.01, audit_tol=1e-3, out=None, stream=None):
+    def force(self, k, segs, ext=None, kappa=None, audit_fraction=0.01, audit_tol=1e-3, exact_mode="fp64", out=None,
+              stream=None):
         """ddd_surrogate_force on packed 9 × n segments (a CUDA float64 tensor or
-        a numpy array).  Returns (forces as a CUDA tensor n × 6 = the 3 × 2 × n
-        column-major array, report dict)."""
+        a numpy array); exact_mode: arithmetic of the exact near / audit passes
+        ("fp64", "df64" or "f32c").  Returns (forces as a CUDA tensor n × 6 = the
+        3 × 2 × n column-major array, report dict)."""
         import torch
         if self.nu is not None and abs(_nu_of(k) - self.nu) > 1e-9:
             raise DDDError(DDD_EINVAL, "surrogate trained for nu = %.6g, called with nu = %.6g"
@@ -558,7 +561,8 @@ class Surrogate:
             ext = torch.from_numpy(np.ascontiguousarray(ext, dtype=np.uint8)).cuda()
         if out is None:
             out = torch.empty((n, 6), dtype=torch.float64, device=segs.device)
-        o = ddd_sur_opts(self.kappa if kappa is None else float(kappa), float(audit_fraction), float(audit_tol))
+        o = ddd_sur_opts(self.kappa if kappa is None else float(kappa), float(audit_fraction), float(audit_tol),
+                         MODES.get(exact_mode, exact_mode) if isinstance(exact_mode, str) else int(exact_mode))
         rep = ddd_sur_report()
         st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
         self._rc(self._L.ddd_surrogate_force(self._h, ctypes.byref(k), segs.data_ptr(), n,

@@ -29,117 +29,13 @@
 #include "pair_df.cuh"
 #include "pair_f64.cuh"
 #include "tile_body.cuh"
+#include "tile_pol_df.cuh"
 
 namespace ddd {
 namespace batch {
 
-constexpr float kThrHiB = 1.4901312e-08f;
-constexpr float kThrLoB = 1.4901012e-08f;
-
-struct SegDFb {
-  DV3 b, n1, n2, t;
-  df64 tN;
-};
-
-__device__ __forceinline__ SegDFb load_df(const float* __restrict__ s, int64_t ld, int64_t i) {
-  auto g = [&](int k) { return df64{s[(2 * k) * ld + i], s[(2 * k + 1) * ld + i]}; };
-  SegDFb r;
-  r.n1 = {g(0), g(1), g(2)};
-  r.n2 = {g(3), g(4), g(5)};
-  r.b = {g(6), g(7), g(8)};
-  r.t = {g(9), g(10), g(11)};
-  r.tN = g(12);
-  return r;
-}
-
-// df64 / mixed policy (same arithmetic as segseg_df.cu).
 template <int FORM>
-struct PolDFb {
-  using Seg = SegDFb;
-  using Scalar = df64;
-  using Vec = DV3;
-  using Acc = DV3;
-  struct Consts {
-    KConstsDF K;
-    KConstsF KF;
-  };
-  template <int T>
-  struct Tile {
-    float seg[26][T];
-    float2 fj[T / 32][6][T];
-  };
-  static __device__ __forceinline__ Seg load_global(const TileArgs& A, int64_t i) { return load_df(A.soadf, A.npad, i); }
-  template <int T>
-  static __device__ __forceinline__ void load_tile(const TileArgs& A, Tile<T>& s, int64_t j0, int t) {
-#pragma unroll
-    for (int k = 0; k < 26; ++k) s.seg[k][t] = A.soadf[k * A.npad + j0 + t];
-  }
-  template <int T>
-  static __device__ __forceinline__ void zero_cols(Tile<T>& s, int t) {
-#pragma unroll
-    for (int w = 0; w < T / 32; ++w)
-#pragma unroll
-      for (int c = 0; c < 6; ++c) s.fj[w][c][t] = make_float2(0.0f, 0.0f);
-  }
-  template <int T>
-  static __device__ __forceinline__ Seg load_smem(const Tile<T>& s, int j) {
-    auto g = [&](int q) { return df64{s.seg[2 * q][j], s.seg[2 * q + 1][j]}; };
-    Seg r;
-    r.n1 = {g(0), g(1), g(2)};
-    r.n2 = {g(3), g(4), g(5)};
-    r.b = {g(6), g(7), g(8)};
-    r.t = {g(9), g(10), g(11)};
-    r.tN = g(12);
-    return r;
-  }
-  static __device__ __forceinline__ bool is_general(const TileArgs& A, const Seg& a, const Seg& b, int64_t gi,
-                                                    int64_t gj, df64& c) {
-    c = dot(a.t, b.t);
-    df64 omc = df(1.0f) - c * c;
-    if (omc.hi > kThrHiB) return true;
-    if (omc.hi < kThrLoB) return false;
-    const int64_t n = A.npad;
-    D3 ti = {A.soa[9 * n + gi], A.soa[10 * n + gi], A.soa[11 * n + gi]};
-    D3 tj = {A.soa[9 * n + gj], A.soa[10 * n + gj], A.soa[11 * n + gj]};
-    double c64 = dot(ti, tj);
-    return (1.0 - c64 * c64) > kSqrtEps;
-  }
-  template <bool BOTH>
-  static __device__ __forceinline__ void general(const Consts& KP, const TileArgs&, const Seg& a, const Seg& b,
-                                                 df64 c, DV3& F1, DV3& F2, DV3& F3, DV3& F4) {
-    if (FORM == 0)
-      general_pair_df<true, BOTH>(KP.K, a.b, a.n1, a.n2, a.t, a.tN, b.b, b.n1, b.n2, b.t, b.tN, c, F1, F2, F3, F4);
-    else
-      general_pair_mixed<true, BOTH, true>(KP.K, KP.KF, f3(a.b), a.n1, a.n2, a.t, a.tN.hi, f3(b.b), b.n1, b.n2, b.t,
-                                           b.tN.hi, c, F1, F2, F3, F4);
-  }
-  static __device__ __forceinline__ void add_df(float2& acc, df64 v) {
-    df64 s = df64{acc.x, acc.y} + v;
-    acc.x = s.hi;
-    acc.y = s.lo;
-  }
-  template <int T>
-  static __device__ __forceinline__ void add_col(Tile<T>& s, int warp, int j, const DV3& F3, const DV3& F4) {
-    add_df(s.fj[warp][0][j], F3.x);
-    add_df(s.fj[warp][1][j], F3.y);
-    add_df(s.fj[warp][2][j], F3.z);
-    add_df(s.fj[warp][3][j], F4.x);
-    add_df(s.fj[warp][4][j], F4.y);
-    add_df(s.fj[warp][5][j], F4.z);
-  }
-  static __device__ __forceinline__ DV3 acc_zero() { return {df(0.f), df(0.f), df(0.f)}; }
-  static __device__ __forceinline__ void acc_add(DV3& a, const DV3& v) { a = a + v; }
-  static __device__ __forceinline__ D3 acc_to_d3(const DV3& a) {
-    return {df_to_double(a.x), df_to_double(a.y), df_to_double(a.z)};
-  }
-  template <int T>
-  static __device__ __forceinline__ double col_sum(const Tile<T>& s, int c, int t) {
-    double v = 0.0;
-#pragma unroll
-    for (int w = 0; w < T / 32; ++w) v += (double)s.fj[w][c][t].x + (double)s.fj[w][c][t].y;
-    return v;
-  }
-};
+using PolDFb = PolDF<FORM>;  // tile_pol_df.cuh
 
 // Padded SoA from the caller's packed 9 × ld array; src[g] = source column or -1.
 __global__ void prep_batched(const double* __restrict__ in, int64_t ldIn, const uint8_t* __restrict__ ext,
@@ -172,17 +68,6 @@ __global__ void prep_batched(const double* __restrict__ in, int64_t ldIn, const 
 #pragma unroll
   for (int k = 0; k < 13; ++k) soa[k * ntot + g] = v[k];
   skip[g] = sk;
-}
-
-__global__ void prep_df_batched(const double* __restrict__ soa, int64_t ntot, float* __restrict__ soadf) {
-  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= ntot) return;
-#pragma unroll
-  for (int k = 0; k < 13; ++k) {
-    df64 v = df_from_double(soa[k * ntot + i]);
-    soadf[(2 * k) * ntot + i] = v.hi;
-    soadf[(2 * k + 1) * ntot + i] = v.lo;
-  }
 }
 
 // Work item: (slot, first row segment, first column segment, diagonal flag).
@@ -391,15 +276,6 @@ KConsts kconsts(const ddd_consts* k) {
   return K;
 }
 
-KConstsDF kdf(const KConsts& K) {
-  auto s = [](double d) {
-    float hi = (float)d;
-    return df64{hi, (float)(d - (double)hi)};
-  };
-  return KConstsDF{s(K.aSq), s(K.mu4pi), s(K.mu4pinu), s(K.mu8piaSq), s(K.mu4pinuaSq)};
-}
-KConstsF kf(const KConsts& K) { return KConstsF{(float)K.mu4pi, (float)K.mu4pinu, (float)K.mu8piaSq, (float)K.mu4pinuaSq}; }
-
 // Shared-memory attribute and grid size of the persistent kernel, set up outside
 // any stream capture.
 template <int T, class P>
@@ -441,8 +317,7 @@ cudaError_t enqueue(ddd_batch* b, Layout& L, const ddd_consts* k, const double* 
                                                                (double*)L.soa.p, (uint8_t*)L.skip.p);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (b->mode != DDD_MODE_FP64) {
-    prep_df_batched<<<(unsigned)((ntot + 255) / 256), 256, 0, st>>>((const double*)L.soa.p, ntot, (float*)L.soadf.p);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = launch_prep_df((const double*)L.soa.p, ntot, (float*)L.soadf.p, st)) != cudaSuccess) return e;
   }
   const KConsts K = kconsts(k);
   const TileArgs A{K, (const double*)L.soa.p, (const uint8_t*)L.skip.p, ntot, (const float*)L.soadf.p, nullptr};
@@ -451,11 +326,11 @@ cudaError_t enqueue(ddd_batch* b, Layout& L, const ddd_consts* k, const double* 
     e = L.T == 64 ? launch_persistent<64, PolF64>(A, PolF64::Consts{}, L, next, counters, st)
                   : launch_persistent<128, PolF64>(A, PolF64::Consts{}, L, next, counters, st);
   } else if (b->mode == DDD_MODE_DF64) {
-    const PolDFb<0>::Consts KP{kdf(K), kf(K)};
+    const PolDFb<0>::Consts KP{kconsts_df(K), kconsts_f(K)};
     e = L.T == 64 ? launch_persistent<64, PolDFb<0>>(A, KP, L, next, counters, st)
                   : launch_persistent<128, PolDFb<0>>(A, KP, L, next, counters, st);
   } else {
-    const PolDFb<1>::Consts KP{kdf(K), kf(K)};
+    const PolDFb<1>::Consts KP{kconsts_df(K), kconsts_f(K)};
     e = L.T == 64 ? launch_persistent<64, PolDFb<1>>(A, KP, L, next, counters, st)
                   : launch_persistent<128, PolDFb<1>>(A, KP, L, next, counters, st);
   }

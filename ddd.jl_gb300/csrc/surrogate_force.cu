@@ -11,8 +11,9 @@
 //      exactly on their far pairs (tile_body MODE 3), compared with the
 //      network's slot sums;
 //   4. near pass: the listed tile pairs, every pair outside the trust region
-//      evaluated exactly (tile_body MODE 2: FP64 general or near-parallel
-//      branch, strict rounding) and added to the slot;
+//      evaluated exactly (tile_body MODE 2: the reference's general or
+//      near-parallel branch, the general branch in the caller's exact_mode
+//      arithmetic: strict FP64, df64 or f32c) and added to the slot;
 //   5. reduction of each segment's slots in a fixed order, written back in the
 //      caller's order.
 // If the audited error exceeds the caller's bound, steps 2-5 are replaced by
@@ -35,6 +36,7 @@
 #include "surrogate.cuh"
 #include "surrogate_state.h"
 #include "tile_body.cuh"
+#include "tile_pol_df.cuh"
 
 namespace ddd {
 
@@ -203,14 +205,15 @@ __global__ void near_items(const int4* __restrict__ all, int32_t nAll, const flo
   if (d2 < cut * cut) out[atomicAdd(count, 1)] = it;
 }
 
-// Persistent loop of the exact tile body over a work list; the item count is
-// read from the device (nDev) when given.
-template <int MODE>
+// Persistent loop of the exact tile body (arithmetic policy P) over a work
+// list; the item count is read from the device (nDev) when given.
+template <int MODE, class P>
 __global__ void __launch_bounds__(T, 2)
-exact_tiles(TileArgs A, const int4* __restrict__ items, const int32_t* __restrict__ nDev, int32_t nHost,
-            int32_t* __restrict__ next, double* __restrict__ partial, unsigned long long* __restrict__ counters) {
+exact_tiles(TileArgs A, typename P::Consts KP, const int4* __restrict__ items, const int32_t* __restrict__ nDev,
+            int32_t nHost, int32_t* __restrict__ next, double* __restrict__ partial,
+            unsigned long long* __restrict__ counters) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  auto& sm = *reinterpret_cast<TileSmemT<T, PolF64>*>(smem_raw);
+  auto& sm = *reinterpret_cast<TileSmemT<T, P>*>(smem_raw);
   __shared__ int32_t s_item;
   const int32_t nItems = nDev ? *nDev : nHost;
   for (;;) {
@@ -220,8 +223,7 @@ exact_tiles(TileArgs A, const int4* __restrict__ items, const int32_t* __restric
     const int32_t w = s_item;
     if (w >= nItems) break;
     const int4 it = items[w];
-    tile_body<T, MODE, PolF64>(A, PolF64::Consts{}, sm, it.y, it.z, it.w != 0, nullptr, 0,
-                               partial + (int64_t)it.x * 12 * T, counters);
+    tile_body<T, MODE, P>(A, KP, sm, it.y, it.z, it.w != 0, nullptr, 0, partial + (int64_t)it.x * 12 * T, counters);
   }
 }
 
@@ -363,11 +365,11 @@ struct SurForcePlan {
   double auditFraction = -1.0;
   size_t cubBytes = 0;
   int sms = 0, gridExact = 0;
-  Buf soa, skip, ms, keysIn, keysOut, valsIn, perm, src, cubTmp, minmaxPart, box, tbox, allItems, nearItems, partial,
+  Buf soa, soadf, skip, ms, keysIn, keysOut, valsIn, perm, src, cubTmp, minmaxPart, box, tbox, allItems, nearItems, partial,
       auditItems, auditSlots, abuf, astat, small;
   cudaEvent_t ev[6] = {};
   ~SurForcePlan() {
-    for (Buf* b : {&soa, &skip, &ms, &keysIn, &keysOut, &valsIn, &perm, &src, &cubTmp, &minmaxPart, &box, &tbox,
+    for (Buf* b : {&soa, &soadf, &skip, &ms, &keysIn, &keysOut, &valsIn, &perm, &src, &cubTmp, &minmaxPart, &box, &tbox,
                    &allItems, &nearItems, &partial, &auditItems, &auditSlots, &abuf, &astat, &small})
       b->release();
     for (cudaEvent_t& e : ev)
@@ -403,24 +405,39 @@ uint32_t slot_hash(uint32_t x) {
   return x;
 }
 
-template <int MODE>
+template <int MODE, class P>
 cudaError_t set_exact_attr() {
   static bool done = false;
   if (done) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(sf::exact_tiles<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)sizeof(TileSmemT<sf::T, PolF64>));
+  cudaError_t e = cudaFuncSetAttribute(sf::exact_tiles<MODE, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)sizeof(TileSmemT<sf::T, P>));
   if (e == cudaSuccess) done = true;
   return e;
 }
 
-template <int MODE>
-cudaError_t launch_exact(const TileArgs& A, const int4* items, const int32_t* nDev, int32_t nHost, int32_t* next,
-                         double* partial, unsigned long long* counters, int grid, cudaStream_t st) {
-  cudaError_t e = set_exact_attr<MODE>();
+template <int MODE, class P>
+cudaError_t launch_exact_p(const TileArgs& A, const typename P::Consts& KP, const int4* items, const int32_t* nDev,
+                           int32_t nHost, int32_t* next, double* partial, unsigned long long* counters, int grid,
+                           cudaStream_t st) {
+  cudaError_t e = set_exact_attr<MODE, P>();
   if (e != cudaSuccess) return e;
-  sf::exact_tiles<MODE><<<grid, sf::T, sizeof(TileSmemT<sf::T, PolF64>), st>>>(A, items, nDev, nHost, next, partial,
-                                                                                counters);
+  sf::exact_tiles<MODE, P><<<grid, sf::T, sizeof(TileSmemT<sf::T, P>), st>>>(A, KP, items, nDev, nHost, next,
+                                                                             partial, counters);
   return cudaGetLastError();
+}
+
+// The exact tile pass in the arithmetic of `mode` (DDD_MODE_FP64 strict,
+// DDD_MODE_DF64 or DDD_MODE_F32C for the general branch).
+template <int MODE>
+cudaError_t launch_exact(int mode, const TileArgs& A, const int4* items, const int32_t* nDev, int32_t nHost,
+                         int32_t* next, double* partial, unsigned long long* counters, int grid, cudaStream_t st) {
+  if (mode == DDD_MODE_FP64)
+    return launch_exact_p<MODE, PolF64>(A, PolF64::Consts{}, items, nDev, nHost, next, partial, counters, grid, st);
+  const typename PolDF<0>::Consts KP{kconsts_df(A.K), kconsts_f(A.K)};
+  if (mode == DDD_MODE_DF64)
+    return launch_exact_p<MODE, PolDF<0>>(A, KP, items, nDev, nHost, next, partial, counters, grid, st);
+  return launch_exact_p<MODE, PolDF<1>>(A, typename PolDF<1>::Consts{KP.K, KP.KF}, items, nDev, nHost, next, partial,
+                                        counters, grid, st);
 }
 
 cudaError_t ensure_plan(ddd_surrogate* s, int64_t numSeg, double auditFraction) {
@@ -435,11 +452,9 @@ cudaError_t ensure_plan(ddd_surrogate* s, int64_t numSeg, double auditFraction) 
     P.nItems = P.nt * (P.nt + 1) / 2;
     P.auditFraction = -1.0;
     if ((e = cudaDeviceGetAttribute(&P.sms, cudaDevAttrMultiProcessorCount, s->device)) != cudaSuccess) return e;
-    if ((e = set_exact_attr<0>()) != cudaSuccess || (e = set_exact_attr<2>()) != cudaSuccess ||
-        (e = set_exact_attr<3>()) != cudaSuccess)
-      return e;
-    int per = 0;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sf::exact_tiles<2>, sf::T,
+    if ((e = set_exact_attr<2, PolF64>()) != cudaSuccess) return e;
+    int per = 0;  // the df64 policies use the same shared memory and register budget
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sf::exact_tiles<2, PolF64>, sf::T,
                                                            sizeof(TileSmemT<sf::T, PolF64>))) != cudaSuccess)
       return e;
     P.gridExact = P.sms * std::max(1, per);
@@ -532,8 +547,10 @@ int ddd_surrogate_force(ddd_surrogate* s, const ddd_consts* k, const double* seg
                         const uint8_t* ext, int64_t numSeg, double* force, void* stream, const ddd_sur_opts* opts,
                         ddd_sur_report* rep) {
   if (!s) return DDD_EINVAL;
-  ddd_sur_opts o{20.0, 0.01, 1e-3};
+  ddd_sur_opts o{20.0, 0.01, 1e-3, DDD_MODE_FP64};
   if (opts) o = *opts;
+  if (o.exact_mode != DDD_MODE_FP64 && o.exact_mode != DDD_MODE_DF64 && o.exact_mode != DDD_MODE_F32C)
+    return sfail(s, DDD_EINVAL, "exact_mode must be DDD_MODE_FP64, DDD_MODE_DF64 or DDD_MODE_F32C");
   if (!k) return sfail(s, DDD_EINVAL, "consts is NULL");
   const double kv[5] = {k->aSq, k->mu4pi, k->mu8pi, k->mu4pinu, k->nuMu4pinu};
   for (double x : kv)
@@ -564,7 +581,9 @@ int ddd_surrogate_force(ddd_surrogate* s, const ddd_consts* k, const double* seg
   K.mu8piaSq = k->aSq * k->mu8pi;
   K.mu4pinuaSq = k->aSq * k->mu4pinu;
   const float kappa = (float)o.kappa;
-  TileArgs A{K, P.soa.as<double>(), P.skip.as<uint8_t>(), npad, nullptr, nullptr};
+  const int xm = o.exact_mode;
+  if (xm != DDD_MODE_FP64) SCK(P.soadf.ensure((size_t)npad * 26 * sizeof(float)), "allocate df64 segments");
+  TileArgs A{K, P.soa.as<double>(), P.skip.as<uint8_t>(), npad, P.soadf.as<float>(), nullptr};
   A.ms = P.ms.as<float>();
   A.farK2 = kappa * kappa;
   const unsigned nb = (unsigned)((npad + 255) / 256);
@@ -585,6 +604,7 @@ int ddd_surrogate_force(ddd_surrogate* s, const ddd_consts* k, const double* seg
                                         P.skip.as<uint8_t>(), P.src.as<int32_t>(), &dv->active);
   SCK(cudaGetLastError(), "gather");
   SCK(launch_prep_mlp_seg(P.soa.as<double>(), P.skip.as<uint8_t>(), npad, P.ms.as<float>(), st), "prep_mlp_seg");
+  if (xm != DDD_MODE_FP64) SCK(launch_prep_df(P.soa.as<double>(), npad, P.soadf.as<float>(), st), "prep_df");
   sf::tile_boxes<<<(unsigned)nt, sf::T, 0, st>>>(P.ms.as<float>(), npad, P.tbox.as<float>());
   sf::near_items<<<(unsigned)((P.nItems + 255) / 256), 256, 0, st>>>(
       P.allItems.as<int4>(), (int32_t)P.nItems, P.tbox.as<float>(), kappa, P.nearItems.as<int4>(), &dv->nearCount);
@@ -601,7 +621,7 @@ int ddd_surrogate_force(ddd_surrogate* s, const ddd_consts* k, const double* seg
 
   // 3. audit
   if (P.nAudit > 0) {
-    SCK(launch_exact<3>(A, P.auditItems.as<int4>(), nullptr, P.nAudit, &dv->next[1], P.abuf.as<double>(), nullptr,
+    SCK(launch_exact<3>(xm, A, P.auditItems.as<int4>(), nullptr, P.nAudit, &dv->next[1], P.abuf.as<double>(), nullptr,
                         (int)std::min<int64_t>(P.gridExact, P.nAudit), st),
         "audit pass");
     sf::audit_compare<<<P.nAudit, sf::T, 0, st>>>(P.partial.as<double>(), P.abuf.as<double>(),
@@ -612,7 +632,7 @@ int ddd_surrogate_force(ddd_surrogate* s, const ddd_consts* k, const double* seg
   SCK(cudaEventRecord(P.ev[3], st), "event");
 
   // 4. near pass (in place)
-  SCK(launch_exact<2>(A, P.nearItems.as<int4>(), &dv->nearCount, 0, &dv->next[2], P.partial.as<double>(),
+  SCK(launch_exact<2>(xm, A, P.nearItems.as<int4>(), &dv->nearCount, 0, &dv->next[2], P.partial.as<double>(),
                       dv->counts, P.gridExact, st),
       "near pass");
   SCK(cudaEventRecord(P.ev[4], st), "event");
@@ -642,7 +662,7 @@ int ddd_surrogate_force(ddd_surrogate* s, const ddd_consts* k, const double* seg
     // The audit exceeded its bound: exact forces for every pair.
     cudaEvent_t e0 = P.ev[1], e1 = P.ev[2];
     SCK(cudaEventRecord(e0, st), "event");
-    SCK(launch_exact<0>(A, P.allItems.as<int4>(), nullptr, (int32_t)P.nItems, &dv->next[3], P.partial.as<double>(),
+    SCK(launch_exact<0>(xm, A, P.allItems.as<int4>(), nullptr, (int32_t)P.nItems, &dv->next[3], P.partial.as<double>(),
                         nullptr, P.gridExact, st),
         "exact fallback");
     sf::reduce_unpermute<<<nb, 256, 0, st>>>(P.partial.as<double>(), P.src.as<int32_t>(), npad, nt, force);

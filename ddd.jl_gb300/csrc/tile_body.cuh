@@ -17,8 +17,9 @@
 // segment — are written to `p` as [side][component][T] doubles.  No
 // floating-point atomics: the result is deterministic.
 //
-// In MODES 2 and 3 every selected pair goes through the compacted dense pass,
-// in the FP64 general or near-parallel branch as the reference chooses it.
+// In MODES 2 and 3 every selected pair goes through the compacted dense pass:
+// the branch is the reference's FP64 decision, the general branch uses the
+// policy's arithmetic (P::dense_general), the near-parallel branch FP64.
 //
 // Data: `soa` is the FP64 structure of arrays (13 rows of npad doubles: n1xyz,
 // n2xyz, bxyz, txyz, 1/|l|), `skip` one byte per segment (external or padding).
@@ -195,7 +196,8 @@ __device__ __forceinline__ void tile_body(const TileArgs& A, const typename P::C
       double c = dot(a.t, b.t);
       D3 F1, F2, F3 = {0, 0, 0}, F4 = {0, 0, 0};
       if (CLS && 1.0 - c * c > kSqrtEps) {
-        general_pair<true, true>(A.K, a.b, a.n1, a.n2, a.t, a.tN, b.b, b.n1, b.n2, b.t, b.tN, c, F1, F2, F3, F4);
+        // The reference's branch decision in FP64; the policy's general-branch arithmetic.
+        P::dense_general(KP, A, iBase + il, j0 + jl, F1, F2, F3, F4);
         ++nGeneral;
       } else if (MODE != 1) {
         ++nDenseParallel;
@@ -325,6 +327,12 @@ struct PolF64 {
   static __device__ __forceinline__ void general(const Consts&, const TileArgs& A, const Seg& a, const Seg& b, double c,
                                                  D3& F1, D3& F2, D3& F3, D3& F4) {
     general_pair<true, BOTH>(A.K, a.b, a.n1, a.n2, a.t, a.tN, b.b, b.n1, b.n2, b.t, b.tN, c, F1, F2, F3, F4);
+  }
+  // Dense pass of the classified modes: one general-branch pair, both sides.
+  static __device__ __forceinline__ void dense_general(const Consts& KP, const TileArgs& A, int64_t gi, int64_t gj,
+                                                       D3& F1, D3& F2, D3& F3, D3& F4) {
+    const SegF64 a = tb_load_seg64(A.soa, A.npad, gi), b = tb_load_seg64(A.soa, A.npad, gj);
+    general<true>(KP, A, a, b, dot(a.t, b.t), F1, F2, F3, F4);
   }
   template <int T>
   static __device__ __forceinline__ void add_col(Tile<T>& s, int warp, int j, const D3& F3, const D3& F4) {

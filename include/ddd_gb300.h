@@ -252,9 +252,10 @@ int ddd_surrogate_grads(ddd_surrogate* s, const void* X, const float* Bp, const 
  * segments), split into
  *   far pairs  R^2 >= kappa^2 max(L_i, L_j)^2 (R: midpoint separation, L:
  *              lengths) -> the network, fused tcgen05 kernel;
- *   near pairs (every other active pair) -> the exact FP64 pair force
- *              (calcSegSegForce's general or near-parallel branch, strict
- *              rounding), evaluated in full.
+ *   near pairs (every other active pair) -> the exact pair force
+ *              (calcSegSegForce's general or near-parallel branch; the general
+ *              branch in the arithmetic of opts->exact_mode, strict FP64 by
+ *              default), evaluated in full.
  * Segments are Morton-sorted by midpoint first, so near pairs fall in few tile
  * pairs; the result is returned in the caller's order and is deterministic.
  * Audit: a deterministic sample of about audit_fraction of the tile pairs is
@@ -263,7 +264,8 @@ int ddd_surrogate_grads(ddd_surrogate* s, const void* X, const float* Bp, const 
  * (sqrt(sum of squared slot errors / sampled fraction) / ||F||); when that
  * exceeds audit_tol, the whole call is recomputed with the exact FP64 kernel
  * (fallback = 1).
- * opts may be NULL (kappa 20, audit_fraction 0.01, audit_tol 1e-3); rep may be
+ * opts may be NULL (kappa 20, audit_fraction 0.01, audit_tol 1e-3, exact_mode
+ * DDD_MODE_FP64); rep may be
  * NULL.  Synchronous: the work is queued on `stream` (NULL: the surrogate's own
  * stream, after waiting for all work already queued on the device) and the
  * call returns when the forces are complete. */
@@ -271,6 +273,8 @@ typedef struct {
   double kappa;          /* trust-region factor; the network's training range sets it (> 0) */
   double audit_fraction; /* in [0, 1]; 0 disables the audit */
   double audit_tol;      /* bound of the estimated node-force relative RMS error; <= 0: no fallback */
+  int exact_mode;        /* arithmetic of the exact passes (near, audit, fallback): DDD_MODE_FP64 (strict),
+                            DDD_MODE_DF64 or DDD_MODE_F32C for the general branch */
 } ddd_sur_opts;
 typedef struct {
   int64_t pairs_total;          /* unordered pairs of active segments */

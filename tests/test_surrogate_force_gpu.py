@@ -134,6 +134,21 @@ def test_all_pairs_near_is_exact(pkg, synth, oracle, with_ext):
     check_forces(F3, oracle, k5_of(dln, mat), net, normwise=3e-10)
 
 
+@pytest.mark.parametrize("mode", ["f32c", "df64"])
+def test_all_pairs_near_precision_forms(pkg, synth, mode):
+    # The exact passes in the df64 / f32c arithmetic (the general branch in
+    # double-float; branch decision and near-parallel branch FP64): every pair
+    # near, against the library's FP64 path.  Bound: those forms' measured error
+    # (~5e-8 relative RMS for f32c) with margin.
+    net, segs = _network(pkg, synth, 300, seed=35, cube=6000.0)
+    sur = _zero_surrogate(pkg)
+    F, rep = sur.force(_k(pkg), segs, kappa=1e30, audit_fraction=0.0, exact_mode=mode)
+    n = segs.shape[1]
+    assert rep["pairs_near_general"] + rep["pairs_near_parallel"] == n * (n - 1) // 2
+    ex = _exact_device(pkg, segs)
+    assert np.linalg.norm(F.cpu().numpy() - ex) <= 1e-6 * np.linalg.norm(ex)
+
+
 def test_untrained_network_falls_back_to_exact(pkg, synth, oracle):
     # Sparse network: mostly far pairs, whose FP64 evaluation cancels strongly,
     # so the per-node bound (long-double-calibrated noise) carries the check.
