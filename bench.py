@@ -1,4 +1,5 @@
-"""Benchmark: seg-seg pair interactions/s on one GB300 (FP64 plain method).
+"""Benchmark: seg-seg pair interactions/s on one GB300 (FP64 plain method, and
+the FP32 + learned-surrogate form at its stated error).
 
 Workload "gpu65k": 65,536 segments = 8192 closed square loops (shear and
 prismatic, BCC {110}<111> slip systems, L ~ U(20, 200) b, centres uniform in a
@@ -14,6 +15,11 @@ e2e:   the reference-facing C-ABI call with host buffers (ddd_segseg_force):
 cpu_baseline: the C++/OpenMP port of the reference's threaded path
        (calcSegSegForcePar: contiguous i-chunks, one atomic add per output
        component) on the host's cores, on a bounded sub-network of the workload.
+
+surrogate: the same workload through ddd_surrogate_force (far pairs by the
+       tcgen05 MLP, near pairs exact in f32c or strict FP64, 1% audit), value,
+       speedup over the FP64 kernel, node-force error against the FP64 result,
+       and the network kernel's tensor throughput.
 
 --impl reference: times that CPU port alone (the reference itself is Julia and
 cannot run here), same metric and workload, each step a bounded sub-network.
@@ -134,6 +140,71 @@ def cpu_par_sample(pkg, synth, oracle, p, b, k5, target_s):
                       (n * (n - 1) // 2, n, n_loops, dt)}
 
 
+# Tensor-core FLOPs of the surrogate network per pair slot (one row of the
+# 128-row MMA tiles): 2 (16*128 + 128*128 + 128*128 + 128*112).
+OPS_MLP_PAIR = 98304
+SURROGATE_CKPT = os.path.join(ROOT, "ddd.jl_gb300", "data", "surrogate_gpu65k_nu028.bin")
+
+
+def run_surrogate(args, pkg, ctx, k, soa, ref, pairs, ms_fp64, stream, sptr, flush):
+    """The learned far-field surrogate on the same workload: far pairs through the
+    tcgen05 MLP, near pairs exact, 1% of tile pairs audited exactly.  Exact passes
+    in f32c ("FP32+surrogate") and in strict FP64.  Error: node-force relative
+    RMS against the timed FP64 result `ref`."""
+    import torch
+    sur = pkg.Surrogate(ctx, seed=0)
+    if os.path.exists(args.surrogate):
+        sur.load(args.surrogate)
+        source = "checkpoint %s (ddd.jl_gb300/train_surrogate.py: 4 networks of the generator, seeds 11-14, " \
+                 "2^21 far pairs each, 20 epochs)" % os.path.relpath(args.surrogate, ROOT)
+    else:
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("train_surrogate",
+                                                      os.path.join(ROOT, "ddd.jl_gb300", "train_surrogate.py"))
+        ts_mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(ts_mod)
+        t0 = time.time()
+        sur, info = ts_mod.train(epochs=10)
+        source = "trained in this run (%d samples, 10 epochs, %.0f s)" % (info["samples"], time.time() - t0)
+    n = soa.shape[1]
+    F = torch.empty((n, 6), dtype=torch.float64, device="cuda")
+    refv = ref.view(n, 6)
+    out = {"source": source, "kappa": sur.kappa, "audit_fraction": 0.01}
+    for xm in ("f32c", "fp64"):
+        with torch.cuda.stream(stream):
+            sur.force(k, soa, out=F, exact_mode=xm, stream=sptr)  # plan set-up
+            ts, rep = [], None
+            for _ in range(max(1, min(args.steps, 3))):
+                flush.zero_()
+                a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a_.record(stream)
+                _, rep = sur.force(k, soa, out=F, exact_mode=xm, stream=sptr)
+                b_.record(stream)
+                torch.cuda.synchronize()
+                ts.append(a_.elapsed_time(b_))
+        ms = statistics.mean(ts)
+        dn = torch.linalg.norm((F - refv).view(n, 2, 3), dim=2)
+        fn = torch.linalg.norm(refv.view(n, 2, 3), dim=2)
+        slots = rep["tiles_total"] * 128 * 128
+        tfl = slots * OPS_MLP_PAIR / (rep["ms_network"] * 1e-3) / 1e12
+        out[xm] = {
+            "value": pairs / (ms * 1e-3), "unit": "pair-interactions/s", "ms_per_step": ms,
+            "speedup_vs_fp64": ms_fp64 / ms,
+            "error_vs_fp64": {"rel_rms": (torch.linalg.norm(F - refv) / torch.linalg.norm(refv)).item(),
+                              "median_rel_node": (dn / fn).median().item(),
+                              "max_node_over_max_force": (dn.max() / fn.max()).item()},
+            "audit_estimate_rel_rms": rep["audit_node_rel_rms"], "fallback": rep["fallback"],
+            "pairs_near_exact": rep["pairs_near_general"] + rep["pairs_near_parallel"],
+            "pairs_network": rep["pairs_total"] - rep["pairs_near_general"] - rep["pairs_near_parallel"],
+            "ms": {kk: rep[kk] for kk in ("ms_prep", "ms_network", "ms_audit", "ms_near", "ms_reduce")},
+            "network_kernel": {"kernel": "mlp_far_tiles", "tensor_tflops": tfl, "bound": "tensor",
+                               "peak_tflops": None, "frac": None,
+                               "flops": "%d pair slots x %d MMA FLOPs (FP16 operands, FP32 accumulation)"
+                                        % (slots, OPS_MLP_PAIR)},
+        }
+    return out
+
+
 def run_reference(args, pkg, synth, oracle):
     ws, rank = _dist()
     if rank != 0:
@@ -150,7 +221,8 @@ def run_reference(args, pkg, synth, oracle):
     v = statistics.median(vals)
     n = p.shape[0] * 8
     out = {
-        "impl": "reference", "metric": "seg-seg pair interactions/s at 65k segs (FP64 plain)",
+        "impl": "reference",
+        "metric": "seg-seg pair interactions/s at 65k segs (FP64 plain vs FP32+surrogate) at stated error",
         "value": v, "unit": "pair-interactions/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * (n * (n - 1) / 2) / v, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
@@ -182,6 +254,8 @@ def main():
     ap.add_argument("--no-sigma", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--sigma-grid", type=int, default=32)
+    ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--surrogate", default=SURROGATE_CKPT, help="surrogate checkpoint (trained here when missing)")
     args = ap.parse_args()
 
     import __graft_entry__ as graft
@@ -286,6 +360,19 @@ def main():
                                        (rep["pairs_general"], rep["pairs_parallel"]),
             }
 
+    # Learned far-field surrogate ("FP32+surrogate"), same workload and timing.
+    surrogate = None
+    if not args.no_surrogate:
+        surrogate = run_surrogate(args, pkg, ctx, k, soa, force, pairs, ms_step, stream, sptr, flush)
+        peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+        if os.path.exists(peaks_path):
+            tp = json.load(open(peaks_path)).get("bf16_tflops")
+            for xm in ("f32c", "fp64"):
+                nk = surrogate[xm]["network_kernel"]
+                nk["peak_tflops"] = tp
+                nk["frac"] = nk["tensor_tflops"] / tp if tp else None
+                nk["peak_source"] = "MEASURED_PEAKS.json bf16_tflops (burst; FP16 dense rate is the same)"
+
     # Field-point stress σ̃ of the same network on a 32^3 grid over the cube.
     sigma = None
     if not args.no_sigma:
@@ -363,7 +450,7 @@ def main():
         return
     achieved = flops_per_step / (statistics.mean(ms_kernel) * 1e-3)
     line = {
-        "metric": "seg-seg pair interactions/s at 65k segs (FP64 plain)",
+        "metric": "seg-seg pair interactions/s at 65k segs (FP64 plain vs FP32+surrogate) at stated error",
         "value": value, "unit": "pair-interactions/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded generator, seed 0)",
@@ -385,6 +472,7 @@ def main():
         "gpu_launches": 3 * args.steps,
         "mode": "fp64 (strict: every multiply and add rounded separately, as the reference)",
         "variants": variants,
+        "surrogate": surrogate,
         "sigma_tilde": sigma,
         "batched": batched,
         "kernel_ms_per_step": statistics.mean(ms_kernel),
