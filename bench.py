@@ -255,6 +255,9 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--sigma-grid", type=int, default=32)
     ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--profile-surrogate", type=int, default=0, metavar="N",
+                    help="only run N surrogate force calls on the workload (f32c exact passes, no audit) and exit: "
+                         "the command the ncu captures of the surrogate kernels use")
     ap.add_argument("--surrogate", default=SURROGATE_CKPT, help="surrogate checkpoint (trained here when missing)")
     args = ap.parse_args()
 
@@ -283,6 +286,15 @@ def main():
     mat = pkg.MaterialParameters(mu=synth.MU, nu=synth.NU)
     k = pkg.consts_of(dln, mat)
     ctx = pkg.Context(local)
+
+    if args.profile_surrogate:
+        sur = pkg.Surrogate(ctx, seed=0).load(args.surrogate)
+        segs = torch.from_numpy(synth.packed_soa(p, b)).cuda()
+        for _ in range(args.profile_surrogate):
+            _, rep = sur.force(k, segs, exact_mode="f32c", audit_fraction=0.0)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_surrogate": args.profile_surrogate, "segments": n, "report": rep}), flush=True)
+        return
 
     stream = torch.cuda.Stream()
     soa = torch.from_numpy(synth.packed_soa(p, b)).cuda()
