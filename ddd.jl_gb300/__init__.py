@@ -38,7 +38,8 @@ EXPORTED_SYMBOLS = (
     "ddd_tc_gemm_bf16",
     "ddd_surrogate_create", "ddd_surrogate_destroy", "ddd_surrogate_num_params", "ddd_surrogate_params",
     "ddd_surrogate_make_data", "ddd_surrogate_train", "ddd_surrogate_forward", "ddd_surrogate_grads",
-    "ddd_surrogate_force", "ddd_surrogate_last_error",
+    "ddd_surrogate_force", "ddd_surrogate_force_host", "ddd_surrogate_last_error", "ddd_surrogate_save",
+    "ddd_surrogate_load",
 )
 
 # Arithmetic modes (ddd_set_mode).
@@ -158,6 +159,10 @@ def library():
         L.ddd_surrogate_grads.argtypes = [_vp, _vp, _vp, _vp, _i64, _dp, ctypes.POINTER(ctypes.c_float)]
         L.ddd_surrogate_force.argtypes = [_vp, cp, _vp, _i64, _vp, _i64, _vp, _vp, ctypes.POINTER(ddd_sur_opts),
                                           ctypes.POINTER(ddd_sur_report)]
+        L.ddd_surrogate_force_host.argtypes = [_vp, cp, _dp, _i64, _dp, _i64, _ip, _i64, _up, _i64, _dp,
+                                               ctypes.POINTER(ddd_sur_opts), ctypes.POINTER(ddd_sur_report)]
+        L.ddd_surrogate_save.argtypes = [_vp, ctypes.c_char_p, ctypes.c_double, ctypes.c_double, ctypes.c_double]
+        L.ddd_surrogate_load.argtypes = [_vp, ctypes.c_char_p, _dp, _dp, _dp]
         L.ddd_surrogate_last_error.argtypes = [_vp]
         L.ddd_surrogate_last_error.restype = ctypes.c_char_p
         L.ddd_set_mode.argtypes = [_vp, ctypes.c_int]
@@ -421,10 +426,6 @@ for _name, _size in (("W1", 128 * 8), ("b1", 128), ("W2", 128 * 128), ("b2", 128
     _o += _size
 del _o, _name, _size
 
-SURROGATE_MAGIC = b"DDDGBSUR"
-SURROGATE_VERSION = 1
-
-
 def packed_segments(network):
     """Packed 9 × numSeg segment array (n1 xyz, n2 xyz, b xyz per segment) of a
     DislocationNetwork, in segIdx row order (the layout of the device entry points)."""
@@ -549,9 +550,7 @@ class Surrogate:
         ("fp64", "df64" or "f32c").  Returns (forces as a CUDA tensor n × 6 = the
         3 × 2 × n column-major array, report dict)."""
         import torch
-        if self.nu is not None and abs(_nu_of(k) - self.nu) > 1e-9:
-            raise DDDError(DDD_EINVAL, "surrogate trained for nu = %.6g, called with nu = %.6g"
-                           % (self.nu, _nu_of(k)))
+        o = self._opts(k, kappa, audit_fraction, audit_tol, exact_mode)
         if not isinstance(segs, torch.Tensor):
             segs = torch.from_numpy(np.ascontiguousarray(segs, dtype=np.float64)).cuda()
         assert segs.dtype == torch.float64 and segs.is_cuda and segs.dim() == 2 and segs.shape[0] == 9
@@ -561,8 +560,6 @@ class Surrogate:
             ext = torch.from_numpy(np.ascontiguousarray(ext, dtype=np.uint8)).cuda()
         if out is None:
             out = torch.empty((n, 6), dtype=torch.float64, device=segs.device)
-        o = ddd_sur_opts(self.kappa if kappa is None else float(kappa), float(audit_fraction), float(audit_tol),
-                         MODES.get(exact_mode, exact_mode) if isinstance(exact_mode, str) else int(exact_mode))
         rep = ddd_sur_report()
         st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
         self._rc(self._L.ddd_surrogate_force(self._h, ctypes.byref(k), segs.data_ptr(), n,
@@ -570,47 +567,42 @@ class Surrogate:
                                              ctypes.byref(o), ctypes.byref(rep)), "surrogate force")
         return out, rep.as_dict()
 
-    def force_network(self, dlnParams, matParams, network, **kw):
-        """The surrogate's calcSegSegForce: a 3×2×numSeg array for a DislocationNetwork."""
-        n = network.numSeg
-        ext = network.extSeg[network.segIdx[:n, 0] - 1]
-        f, rep = self.force(consts_of(dlnParams, matParams), packed_segments(network), ext=ext, **kw)
-        return np.asfortranarray(f.cpu().numpy().reshape(n, 2, 3).transpose(2, 1, 0)), rep
+    def _opts(self, k, kappa, audit_fraction, audit_tol, exact_mode):
+        if self.nu is not None and abs(_nu_of(k) - self.nu) > 1e-9:
+            raise DDDError(DDD_EINVAL, "surrogate trained for nu = %.6g, called with nu = %.6g"
+                           % (self.nu, _nu_of(k)))
+        return ddd_sur_opts(self.kappa if kappa is None else float(kappa), float(audit_fraction), float(audit_tol),
+                            MODES.get(exact_mode, exact_mode) if isinstance(exact_mode, str) else int(exact_mode))
 
-    # -- checkpoints ------------------------------------------------------------
+    def force_network(self, dlnParams, matParams, network, kappa=None, audit_fraction=0.01, audit_tol=1e-3,
+                      exact_mode="fp64"):
+        """The surrogate's calcSegSegForce on a DislocationNetwork's own host arrays
+        (ddd_surrogate_force_host): a fresh 3×2×numSeg array and the report."""
+        k = consts_of(dlnParams, matParams)
+        o = self._opts(k, kappa, audit_fraction, audit_tol, exact_mode)
+        n = network.numSeg
+        F = np.zeros((3, 2, n), np.float64, order="F")
+        rep = ddd_sur_report()
+        self._rc(self._L.ddd_surrogate_force_host(
+            self._h, ctypes.byref(k), network.coord.ctypes.data_as(_dp), network.coord.shape[1],
+            network.bVec.ctypes.data_as(_dp), network.bVec.shape[1], network.segIdx.ctypes.data_as(_ip),
+            network.segIdx.shape[0], network.extSeg.ctypes.data_as(_up), n, F.ctypes.data_as(_dp),
+            ctypes.byref(o), ctypes.byref(rep)), "surrogate force")
+        return F, rep.as_dict()
+
+    # -- checkpoints (format: ddd_surrogate_save in include/ddd_gb300.h) -------
     def save(self, path):
-        """Versioned checkpoint: magic, version, parameter count, kappa, nu, aSq,
-        FP32 parameters, CRC-32 of everything before it."""
-        import struct
-        import zlib
-        flat = self.params()
-        head = SURROGATE_MAGIC + struct.pack("<IIddd", SURROGATE_VERSION, flat.size, self.kappa,
-                                             np.nan if self.nu is None else self.nu,
-                                             np.nan if self.aSq is None else self.aSq)
-        body = head + flat.astype("<f4").tobytes()
-        with open(path, "wb") as f:
-            f.write(body + struct.pack("<I", zlib.crc32(body) & 0xFFFFFFFF))
+        self._rc(self._L.ddd_surrogate_save(self._h, os.fsencode(path), self.kappa,
+                                            math.nan if self.nu is None else self.nu,
+                                            math.nan if self.aSq is None else self.aSq), "save")
 
     def load(self, path):
-        import struct
-        import zlib
-        with open(path, "rb") as f:
-            data = f.read()
-        hl = len(SURROGATE_MAGIC) + struct.calcsize("<IIddd")
-        if len(data) < hl + 4 or data[:len(SURROGATE_MAGIC)] != SURROGATE_MAGIC:
-            raise DDDError(DDD_EINVAL, "not a surrogate checkpoint: %s" % path)
-        ver, n, kappa, nu, aSq = struct.unpack("<IIddd", data[len(SURROGATE_MAGIC):hl])
-        if ver != SURROGATE_VERSION:
-            raise DDDError(DDD_EINVAL, "checkpoint version %d, expected %d" % (ver, SURROGATE_VERSION))
-        if n != self.num_params or len(data) != hl + 4 * n + 4:
-            raise DDDError(DDD_EINVAL, "checkpoint size mismatch")
-        (crc,) = struct.unpack("<I", data[-4:])
-        if zlib.crc32(data[:-4]) & 0xFFFFFFFF != crc:
-            raise DDDError(DDD_EINVAL, "checkpoint CRC mismatch: %s" % path)
-        self.set_params(np.frombuffer(data[hl:hl + 4 * n], dtype="<f4").astype(np.float32))
-        self.kappa = kappa
-        self.nu = None if math.isnan(nu) else nu
-        self.aSq = None if math.isnan(aSq) else aSq
+        kappa, nu, aSq = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        self._rc(self._L.ddd_surrogate_load(self._h, os.fsencode(path), ctypes.byref(kappa), ctypes.byref(nu),
+                                            ctypes.byref(aSq)), "load")
+        self.kappa = kappa.value
+        self.nu = None if math.isnan(nu.value) else nu.value
+        self.aSq = None if math.isnan(aSq.value) else aSq.value
         return self
 
     def params(self):

@@ -11,6 +11,7 @@
 
 #include "../../include/ddd_gb300.h"
 #include "ddd_internal.h"
+#include "net_check.h"
 #include "pair_f64.cuh"
 
 namespace {
@@ -122,7 +123,6 @@ cudaError_t run_sigma(ddd_ctx* c, const ddd::KConsts& K, const double* soa, int6
                     : ddd::strict::launch_sigma_f64(K, soa, npad, nSeg, x0, M, sigma, st);
 }
 
-bool finite3(const double* p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
 
 int check_consts(ddd_ctx* ctx, const ddd_consts* k, ddd::KConsts& K) {
   if (!k) return fail(ctx, DDD_EINVAL, "consts is NULL");
@@ -140,30 +140,12 @@ int check_consts(ddd_ctx* ctx, const ddd_consts* k, ddd::KConsts& K) {
   return DDD_OK;
 }
 
-// Checks one segIdx row (0-based row r): link/node indices in range, finite
-// data, non-zero length.
+// Checks one segIdx row (0-based row r): net_check.h.
 int check_row(ddd_ctx* ctx, const double* coord, int64_t coordCols, const double* bVec, int64_t bVecCols,
               const int64_t* segIdx, int64_t ld, int64_t r) {
-  const int64_t l = segIdx[r], a = segIdx[r + ld], b = segIdx[r + 2 * ld];
-  char buf[160];
-  if (l < 1 || l > bVecCols || a < 1 || a > coordCols || b < 1 || b > coordCols) {
-    snprintf(buf, sizeof buf, "segIdx row %lld = (%lld, %lld, %lld) out of range (bVec cols %lld, coord cols %lld)",
-             (long long)(r + 1), (long long)l, (long long)a, (long long)b, (long long)bVecCols,
-             (long long)coordCols);
-    return fail(ctx, DDD_ERANGE, buf);
-  }
-  const double* p1 = coord + 3 * (a - 1);
-  const double* p2 = coord + 3 * (b - 1);
-  const double* bv = bVec + 3 * (l - 1);
-  if (!finite3(p1) || !finite3(p2) || !finite3(bv)) {
-    snprintf(buf, sizeof buf, "segment %lld has a non-finite coordinate or Burgers vector", (long long)(r + 1));
-    return fail(ctx, DDD_ENONFINITE, buf);
-  }
-  if (p1[0] == p2[0] && p1[1] == p2[1] && p1[2] == p2[2]) {
-    snprintf(buf, sizeof buf, "segment %lld has zero length", (long long)(r + 1));
-    return fail(ctx, DDD_ENONFINITE, buf);
-  }
-  return DDD_OK;
+  std::string msg;
+  const int rc = ddd::check_segment_row(coord, coordCols, bVec, bVecCols, segIdx, ld, r, msg);
+  return rc ? fail(ctx, rc, msg) : DDD_OK;
 }
 
 int check_network(ddd_ctx* ctx, const double* coord, int64_t coordCols, const double* bVec, int64_t bVecCols,
@@ -405,7 +387,7 @@ int ddd_sigma_tilde(ddd_ctx* ctx, const ddd_consts* k, const double* x0, int64_t
     sel[q + 2 * nSel] = segIdx[r + 2 * ldSegIdx];
   }
   for (int64_t j = 0; j < numPoints; ++j)
-    if (!finite3(x0 + 3 * j)) return fail(ctx, DDD_ENONFINITE, "non-finite field point");
+    if (!ddd::finite3(x0 + 3 * j)) return fail(ctx, DDD_ENONFINITE, "non-finite field point");
   if (rep) memset(rep, 0, sizeof *rep);
   if (numPoints == 0) return DDD_OK;
   if (nSel == 0) {

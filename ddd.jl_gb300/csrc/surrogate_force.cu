@@ -32,6 +32,7 @@
 
 #include "../../include/ddd_gb300.h"
 #include "ddd_internal.h"
+#include "net_check.h"
 #include "pair_f64.cuh"
 #include "surrogate.cuh"
 #include "surrogate_state.h"
@@ -367,10 +368,12 @@ struct SurForcePlan {
   int sms = 0, gridExact = 0;
   Buf soa, soadf, skip, ms, keysIn, keysOut, valsIn, perm, src, cubTmp, minmaxPart, box, tbox, allItems, nearItems, partial,
       auditItems, auditSlots, abuf, astat, small;
+  Buf hostSegs, hostExt, hostForce;  // device copies for the host-array entry point
   cudaEvent_t ev[6] = {};
   ~SurForcePlan() {
     for (Buf* b : {&soa, &soadf, &skip, &ms, &keysIn, &keysOut, &valsIn, &perm, &src, &cubTmp, &minmaxPart, &box, &tbox,
-                   &allItems, &nearItems, &partial, &auditItems, &auditSlots, &abuf, &astat, &small})
+                   &allItems, &nearItems, &partial, &auditItems, &auditSlots, &abuf, &astat, &small, &hostSegs,
+                   &hostExt, &hostForce})
       b->release();
     for (cudaEvent_t& e : ev)
       if (e) cudaEventDestroy(e);
@@ -694,6 +697,53 @@ int ddd_surrogate_force(ddd_surrogate* s, const ddd_consts* k, const double* seg
     rep->ms_reduce = m[4];
     rep->ms_total = fallback ? (double)msFallback : (double)(m[0] + m[1] + m[2] + m[3] + m[4]);
   }
+  return DDD_OK;
+}
+
+// The network's own host arrays (the layout of ddd_segseg_force): validated and
+// packed on the host, copied in, ddd_surrogate_force on the surrogate's stream,
+// forces copied out.
+int ddd_surrogate_force_host(ddd_surrogate* s, const ddd_consts* k, const double* coord, int64_t coordCols,
+                             const double* bVec, int64_t bVecCols, const int64_t* segIdx, int64_t ldSegIdx,
+                             const uint8_t* extSeg, int64_t numSeg, double* force, const ddd_sur_opts* opts,
+                             ddd_sur_report* rep) {
+  if (!s) return DDD_EINVAL;
+  if (numSeg < 0 || coordCols < 0 || bVecCols < 0 || ldSegIdx < numSeg)
+    return sfail(s, DDD_EINVAL, "negative size or numSeg exceeds the rows of segIdx");
+  if (numSeg > 0 && (!coord || !bVec || !segIdx || !force)) return sfail(s, DDD_EINVAL, "network array is NULL");
+  if (numSeg > ((int64_t)1 << 24)) return sfail(s, DDD_ETOOBIG, "numSeg above 2^24");
+  std::vector<double> packed((size_t)numSeg * 9);
+  for (int64_t r = 0; r < numSeg; ++r) {
+    std::string msg;
+    const int rc = check_segment_row(coord, coordCols, bVec, bVecCols, segIdx, ldSegIdx, r, msg);
+    if (rc) return sfail(s, rc, msg);
+    const double* p1 = coord + 3 * (segIdx[r + ldSegIdx] - 1);
+    const double* p2 = coord + 3 * (segIdx[r + 2 * ldSegIdx] - 1);
+    const double* bv = bVec + 3 * (segIdx[r] - 1);
+    for (int c = 0; c < 3; ++c) {
+      packed[(size_t)c * numSeg + r] = p1[c];
+      packed[(size_t)(3 + c) * numSeg + r] = p2[c];
+      packed[(size_t)(6 + c) * numSeg + r] = bv[c];
+    }
+  }
+  if (rep) std::memset(rep, 0, sizeof *rep);
+  if (numSeg == 0) return DDD_OK;
+  SCK(cudaSetDevice(s->device), "cudaSetDevice");
+  if (!s->plan) s->plan = new SurForcePlan();
+  SurForcePlan& P = *s->plan;
+  SCK(P.hostSegs.ensure(packed.size() * sizeof(double)), "allocate segments");
+  SCK(P.hostForce.ensure((size_t)numSeg * 6 * sizeof(double)), "allocate forces");
+  if (extSeg) SCK(P.hostExt.ensure((size_t)numSeg), "allocate extSeg");
+  cudaStream_t st = s->own;
+  SCK(cudaMemcpyAsync(P.hostSegs.p, packed.data(), packed.size() * sizeof(double), cudaMemcpyHostToDevice, st),
+      "copy segments");
+  if (extSeg) SCK(cudaMemcpyAsync(P.hostExt.p, extSeg, (size_t)numSeg, cudaMemcpyHostToDevice, st), "copy extSeg");
+  const int rc = ddd_surrogate_force(s, k, P.hostSegs.as<double>(), numSeg, extSeg ? P.hostExt.as<uint8_t>() : nullptr,
+                                     numSeg, P.hostForce.as<double>(), st, opts, rep);
+  if (rc) return rc;
+  SCK(cudaMemcpyAsync(force, P.hostForce.p, (size_t)numSeg * 6 * sizeof(double), cudaMemcpyDeviceToHost, st),
+      "copy forces");
+  SCK(cudaStreamSynchronize(st), "surrogate force");
   return DDD_OK;
 }
 

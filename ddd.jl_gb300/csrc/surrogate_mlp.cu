@@ -23,7 +23,9 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <string>
 #include <random>
 #include <vector>
 
@@ -418,6 +420,105 @@ int ddd_surrogate_params(ddd_surrogate* s, float* host, int set) {
 }
 
 int ddd_surrogate_num_params(void) { return kNumParams; }
+
+}  // extern "C"
+
+namespace {
+
+// CRC-32 (IEEE 802.3, reflected, polynomial 0xEDB88320; the zlib checksum).
+uint32_t crc32_bytes(const unsigned char* p, size_t n) {
+  static uint32_t table[256];
+  static bool init = false;
+  if (!init) {
+    for (uint32_t i = 0; i < 256; ++i) {
+      uint32_t c = i;
+      for (int k = 0; k < 8; ++k) c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
+      table[i] = c;
+    }
+    init = true;
+  }
+  uint32_t c = 0xFFFFFFFFu;
+  for (size_t i = 0; i < n; ++i) c = table[(c ^ p[i]) & 0xFF] ^ (c >> 8);
+  return c ^ 0xFFFFFFFFu;
+}
+
+// Checkpoint layout (little-endian): "DDDGBSUR", u32 version, u32 parameter
+// count, f64 kappa, f64 nu, f64 aSq, f32 parameters, u32 CRC-32 of all that
+// precedes it.
+constexpr char kMagic[8] = {'D', 'D', 'D', 'G', 'B', 'S', 'U', 'R'};
+constexpr uint32_t kVersion = 1;
+constexpr size_t kHeader = 8 + 4 + 4 + 3 * 8;
+
+template <class T>
+void put(std::vector<unsigned char>& b, size_t off, T v) {
+  std::memcpy(b.data() + off, &v, sizeof v);
+}
+template <class T>
+T get(const std::vector<unsigned char>& b, size_t off) {
+  T v;
+  std::memcpy(&v, b.data() + off, sizeof v);
+  return v;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ddd_surrogate_save(ddd_surrogate* s, const char* path, double kappa, double nu, double aSq) {
+  if (!s || !path) return DDD_EINVAL;
+  std::vector<unsigned char> b(kHeader + (size_t)kNumParams * 4 + 4);
+  std::memcpy(b.data(), kMagic, 8);
+  put<uint32_t>(b, 8, kVersion);
+  put<uint32_t>(b, 12, (uint32_t)kNumParams);
+  put<double>(b, 16, kappa);
+  put<double>(b, 24, nu);
+  put<double>(b, 32, aSq);
+  const int rc = ddd_surrogate_params(s, reinterpret_cast<float*>(b.data() + kHeader), 0);
+  if (rc) return rc;
+  put<uint32_t>(b, b.size() - 4, crc32_bytes(b.data(), b.size() - 4));
+  FILE* f = std::fopen(path, "wb");
+  if (!f) {
+    s->lastError = std::string("cannot open for writing: ") + path;
+    return DDD_EINVAL;
+  }
+  const bool ok = std::fwrite(b.data(), 1, b.size(), f) == b.size();
+  if (std::fclose(f) != 0 || !ok) {
+    s->lastError = std::string("write failed: ") + path;
+    return DDD_EINVAL;
+  }
+  return DDD_OK;
+}
+
+int ddd_surrogate_load(ddd_surrogate* s, const char* path, double* kappa, double* nu, double* aSq) {
+  if (!s || !path) return DDD_EINVAL;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) {
+    s->lastError = std::string("cannot open: ") + path;
+    return DDD_EINVAL;
+  }
+  std::vector<unsigned char> b;
+  unsigned char chunk[65536];
+  size_t n;
+  while ((n = std::fread(chunk, 1, sizeof chunk, f)) > 0) b.insert(b.end(), chunk, chunk + n);
+  std::fclose(f);
+  auto bad = [&](const char* why) {
+    s->lastError = std::string(why) + ": " + path;
+    return DDD_EINVAL;
+  };
+  if (b.size() < kHeader + 4 || std::memcmp(b.data(), kMagic, 8) != 0) return bad("not a surrogate checkpoint");
+  if (get<uint32_t>(b, 8) != kVersion) return bad("unsupported checkpoint version");
+  if (get<uint32_t>(b, 12) != (uint32_t)kNumParams || b.size() != kHeader + (size_t)kNumParams * 4 + 4)
+    return bad("checkpoint size does not match this network");
+  if (crc32_bytes(b.data(), b.size() - 4) != get<uint32_t>(b, b.size() - 4)) return bad("checkpoint CRC mismatch");
+  std::vector<float> params((size_t)kNumParams);
+  std::memcpy(params.data(), b.data() + kHeader, params.size() * 4);
+  const int rc = ddd_surrogate_params(s, params.data(), 1);
+  if (rc) return rc;
+  if (kappa) *kappa = get<double>(b, 16);
+  if (nu) *nu = get<double>(b, 24);
+  if (aSq) *aSq = get<double>(b, 32);
+  return DDD_OK;
+}
 
 // One forward + backward on B rows (B % 128 == 0), no update: loss and
 // gradients (flat FP32 layout) copied to the host.

@@ -12,6 +12,7 @@
 module DDDGB300
 
 export calcSegSegForceGPU, calcSegSegForceGPU!, calc_σTildeGPU, calc_σTildeGPU!
+export Surrogate, loadSurrogate, calcSegSegForceSurrogateGPU
 
 const libddd = joinpath(@__DIR__, "..", "libddd_gb300.so")
 
@@ -111,6 +112,86 @@ function calc_σTildeGPU(x0, dlnParams, matParams, network, idx = nothing)
     σ = zeros(6, numPoints)
     calc_σTildeGPU!(σ, xs, dlnParams, matParams, network, idx)
     return numPoints == 1 ? σ[:, 1] : σ
+end
+
+# ---------------------------------------------------------------------------
+# Learned far-field surrogate (no reference counterpart): calcSegSegForce with
+# far pairs (R >= kappa max(L_i, L_j)) from a trained network and near pairs
+# exact; checkpoints as written by ddd_surrogate_save (e.g. the repository's
+# ddd.jl_gb300/data/surrogate_gpu65k_nu028.bin, trained for nu = 0.28).
+
+struct DDDSurOpts
+    kappa::Float64
+    audit_fraction::Float64
+    audit_tol::Float64
+    exact_mode::Cint
+end
+
+struct DDDSurReport
+    pairs_total::Int64
+    pairs_near_general::Int64
+    pairs_near_parallel::Int64
+    tiles_total::Int64
+    tiles_near::Int64
+    tiles_audit::Int64
+    audit_rel_rms::Float64
+    audit_rel_max::Float64
+    audit_node_rel_rms::Float64
+    fallback::Cint
+    ms_prep::Float64
+    ms_network::Float64
+    ms_audit::Float64
+    ms_near::Float64
+    ms_reduce::Float64
+    ms_total::Float64
+end
+
+mutable struct Surrogate
+    ptr::Ptr{Cvoid}
+    kappa::Float64
+    nu::Float64
+end
+
+function surcheck(s::Surrogate, rc)
+    rc == 0 && return nothing
+    msg = unsafe_string(ccall((:ddd_surrogate_last_error, libddd), Cstring, (Ptr{Cvoid},), s.ptr))
+    rc == -2 && throw(BoundsError(msg))
+    (rc == -1 || rc == -3) && throw(ArgumentError(msg))
+    error("libddd_gb300 surrogate error $rc: $msg")
+end
+
+function loadSurrogate(path::AbstractString)
+    p = ccall((:ddd_surrogate_create, libddd), Ptr{Cvoid}, (Ptr{Cvoid}, UInt64), context(), 0)
+    p == C_NULL && error("ddd_surrogate_create failed")
+    s = Surrogate(p, 0.0, 0.0)
+    finalizer(x -> ccall((:ddd_surrogate_destroy, libddd), Cvoid, (Ptr{Cvoid},), x.ptr), s)
+    kappa, nu, aSq = Ref(0.0), Ref(0.0), Ref(0.0)
+    surcheck(s, ccall((:ddd_surrogate_load, libddd), Cint, (Ptr{Cvoid}, Cstring, Ref{Float64}, Ref{Float64},
+                                                             Ref{Float64}), p, path, kappa, nu, aSq))
+    s.kappa, s.nu = kappa[], nu[]
+    return s
+end
+
+# exact_mode: 0 = strict FP64 (DDD_MODE_FP64), 2 = df64, 3 = f32c.
+function calcSegSegForceSurrogateGPU(s::Surrogate, dlnParams, matParams, network;
+                                     audit_fraction = 0.01, audit_tol = 1e-3, exact_mode = 0)
+    nu = 1 - matParams.μ4π / matParams.μ4πν
+    isnan(s.nu) || abs(nu - s.nu) <= 1e-9 || throw(ArgumentError("surrogate trained for nu = $(s.nu), not $nu"))
+    numSeg = network.numSeg[1]
+    out = zeros(3, 2, numSeg)
+    k = Ref(consts(dlnParams, matParams))
+    opts = Ref(DDDSurOpts(s.kappa, audit_fraction, audit_tol, exact_mode))
+    rep = Ref{DDDSurReport}()
+    coord, bVec, segIdx, extSeg = network.coord, network.bVec, network.segIdx, network.extSeg
+    GC.@preserve coord bVec segIdx extSeg out begin
+        rc = ccall((:ddd_surrogate_force_host, libddd), Cint,
+            (Ptr{Cvoid}, Ref{DDDConsts}, Ptr{Float64}, Int64, Ptr{Float64}, Int64, Ptr{Int64}, Int64,
+             Ptr{Bool}, Int64, Ptr{Float64}, Ref{DDDSurOpts}, Ref{DDDSurReport}),
+            s.ptr, k, coord, size(coord, 2), bVec, size(bVec, 2), segIdx, size(segIdx, 1),
+            extSeg, numSeg, out, opts, rep)
+    end
+    surcheck(s, rc)
+    return out, rep[]
 end
 
 end # module

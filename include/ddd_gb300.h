@@ -244,6 +244,13 @@ int ddd_surrogate_train(ddd_surrogate* s, const void* X, const float* Bp, const 
 int ddd_surrogate_forward(ddd_surrogate* s, const void* X, const float* Bp, int64_t P, float* O);
 int ddd_surrogate_grads(ddd_surrogate* s, const void* X, const float* Bp, const float* T, int64_t B, double* loss,
                         float* grads);
+/* Checkpoints (little-endian): "DDDGBSUR", u32 version 1, u32 parameter count,
+ * f64 kappa, f64 nu, f64 aSq (the trust-region factor, Poisson ratio and core
+ * radius squared the network was trained for), the f32 parameters, and the
+ * CRC-32 (zlib) of everything before it.  load refuses a wrong magic, version,
+ * size or CRC with DDD_EINVAL; kappa / nu / aSq may be NULL. */
+int ddd_surrogate_save(ddd_surrogate* s, const char* path, double kappa, double nu, double aSq);
+int ddd_surrogate_load(ddd_surrogate* s, const char* path, double* kappa, double* nu, double* aSq);
 
 /* Seg-seg forces with the surrogate for far pairs: the same inputs and output
  * as ddd_segseg_force_device (packed 9 x ldSegs device segments n1, n2, b; ext
@@ -292,6 +299,14 @@ typedef struct {
 int ddd_surrogate_force(ddd_surrogate* s, const ddd_consts* k, const double* segs, int64_t ldSegs,
                         const uint8_t* ext, int64_t numSeg, double* force, void* stream, const ddd_sur_opts* opts,
                         ddd_sur_report* rep);
+/* The same with the network's own host arrays, in the layout of
+ * ddd_segseg_force (calcSegSegForce's all-pairs form: coord 3 x coordCols,
+ * bVec 3 x bVecCols, segIdx ldSegIdx x 3 1-based, extSeg per segment row or
+ * NULL, force 3 x 2 x numSeg); validated like ddd_segseg_force. */
+int ddd_surrogate_force_host(ddd_surrogate* s, const ddd_consts* k, const double* coord, int64_t coordCols,
+                             const double* bVec, int64_t bVecCols, const int64_t* segIdx, int64_t ldSegIdx,
+                             const uint8_t* extSeg, int64_t numSeg, double* force, const ddd_sur_opts* opts,
+                             ddd_sur_report* rep);
 const char* ddd_surrogate_last_error(const ddd_surrogate* s);
 
 /* Measurement utility (no reference counterpart): FP64 or FP32 FMA-pipe

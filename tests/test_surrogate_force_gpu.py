@@ -211,6 +211,25 @@ def test_trained_surrogate_accuracy_and_gain(pkg, synth, trained):
     assert torch.equal(F, F2)  # deterministic
 
 
+def test_host_array_entry_matches_device_form(pkg, synth, trained):
+    # ddd_surrogate_force_host takes the network's own arrays (the
+    # ddd_segseg_force layout, extSeg per segment row): same result, bit for bit.
+    dln, mat = _params(pkg)
+    net, segs = _network(pkg, synth, 700, seed=36)
+    n = segs.shape[1]
+    ext = (np.arange(n) % 11 == 5).astype(np.uint8)
+    net.extSeg[:] = ext
+    Fh, rep_h = trained.force_network(dln, mat, net)
+    Fd, rep_d = trained.force(_k(pkg), segs, ext=ext)
+    assert np.array_equal(Fh, np.asfortranarray(Fd.cpu().numpy().reshape(n, 2, 3).transpose(2, 1, 0)))
+    assert rep_h["pairs_total"] == rep_d["pairs_total"] == (n - int(ext.sum())) * (n - int(ext.sum()) - 1) // 2
+    assert np.all(Fh[:, :, ext == 1] == 0.0)
+    bad = pkg.DislocationNetwork(net.coord, net.bVec, net.segIdx.copy())
+    bad.segIdx[3, 1] = 10 ** 7
+    with pytest.raises(pkg.DDDError):
+        trained.force_network(dln, mat, bad)
+
+
 def test_checkpoint_round_trip(pkg, synth, trained, tmp_path):
     path = str(tmp_path / "sur.bin")
     trained.save(path)
