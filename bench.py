@@ -410,6 +410,30 @@ def main():
                  "points_per_s": M / (ms_sig * 1e-3), "ms": ms_sig,
                  "config": "%d segments x %d points (%d^3 grid over the cube), FP64 strict" % (n, M, args.sigma_grid),
                  "frac_fp64_peak": evals * OPS_SIGMA_EVAL / (ms_sig * 1e-3) / fp64_peak}
+        # The precision form (df64 geometry and endpoint differences, FP32
+        # assembly): throughput and error against the FP64 result above.
+        sig_ref = sig.clone()
+        ctx.mode = "f32c"
+        with torch.cuda.stream(stream):
+            ctx.sigma_tilde_device(k, x0.data_ptr(), M, soa.data_ptr(), n, n, sig.data_ptr(), stream=sptr)
+            torch.cuda.synchronize()
+            sms = []
+            for _ in range(2):
+                flush.zero_()
+                a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a_.record(stream)
+                ctx.sigma_tilde_device(k, x0.data_ptr(), M, soa.data_ptr(), n, n, sig.data_ptr(), stream=sptr)
+                b_.record(stream)
+                torch.cuda.synchronize()
+                sms.append(a_.elapsed_time(b_))
+        ctx.mode = "fp64"
+        ms_mix = statistics.mean(sms)
+        dp = torch.linalg.norm((sig - sig_ref).view(M, 6), dim=1)
+        rp = torch.linalg.norm(sig_ref.view(M, 6), dim=1)
+        sigma["mixed"] = {"value": evals / (ms_mix * 1e-3), "ms": ms_mix, "speedup_vs_fp64": ms_sig / ms_mix,
+                          "error_vs_fp64": {"rel_rms": (torch.linalg.norm(sig - sig_ref) /
+                                                        torch.linalg.norm(sig_ref)).item(),
+                                            "max_point_over_max": (dp.max() / rp.max()).item()}}
 
     # Batched form: 256 independent networks (segment counts log-uniform in
     # [64, 8192], own seeds, cubes 2000-20000 b, slip-system subsets) in one

@@ -84,7 +84,7 @@ bool use_fma(const ddd_ctx* c) { return c->mode == DDD_MODE_FP64_FMA; }
 bool use_df(const ddd_ctx* c) { return c->mode == DDD_MODE_DF64 || c->mode == DDD_MODE_F32C; }
 int df_form(const ddd_ctx* c) { return c->mode == DDD_MODE_F32C ? 1 : 0; }
 
-// For DDD_MODE_DF64 the df64 copy of the segment SoA is built first (ctx->soadf).
+// For the df64 / f32c modes the df64 copy of the segment SoA is built first (ctx->soadf).
 cudaError_t prep_df_if_needed(ddd_ctx* c, int64_t npad, cudaStream_t st) {
   if (!use_df(c)) return cudaSuccess;
   cudaError_t e = c->soadf.ensure(ddd::segseg_df_soa_bytes(npad));
@@ -119,6 +119,11 @@ cudaError_t run_segseg_rows(ddd_ctx* c, const ddd::KConsts& K, const double* soa
 
 cudaError_t run_sigma(ddd_ctx* c, const ddd::KConsts& K, const double* soa, int64_t npad, int64_t nSeg,
                       const double* x0, int64_t M, double* sigma, cudaStream_t st) {
+  if (use_df(c)) {  // both precision modes: the mixed σ̃ form
+    cudaError_t e = prep_df_if_needed(c, npad, st);
+    if (e != cudaSuccess) return e;
+    return ddd::launch_sigma_mixed(K, c->soadf.as<float>(), npad, nSeg, x0, M, sigma, st);
+  }
   return use_fma(c) ? ddd::fast::launch_sigma_f64(K, soa, npad, nSeg, x0, M, sigma, st)
                     : ddd::strict::launch_sigma_f64(K, soa, npad, nSeg, x0, M, sigma, st);
 }

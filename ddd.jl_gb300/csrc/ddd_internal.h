@@ -53,6 +53,9 @@ cudaError_t launch_segseg_all_df(const KConsts& K, const double* soa, const floa
 cudaError_t launch_segseg_rows_df(const KConsts& K, const double* soa, const float* soadf, const uint8_t* skip,
                                   int64_t npad, const int64_t* rows, int64_t nRows, double* partial, double* out,
                                   unsigned long long* counters, cudaStream_t st, int form);
+// σ̃ in the mixed form: geometry and endpoint differences in df64, assembly in FP32.
+cudaError_t launch_sigma_mixed(const KConsts& K, const float* soadf, int64_t npad, int64_t nSeg, const double* x0,
+                               int64_t M, double* sigma, cudaStream_t st);
 
 // tc_gemm.cu: tcgen05 GEMM, D = A * B^T (both K-major), A and B both BF16 or both F16.
 size_t tc_gemm_smem_bytes(int N);

@@ -523,4 +523,87 @@ DF_HD void general_pair_mixed(const KConstsDF& K, const KConstsF& KF, F3 b1, DV3
   }
 }
 
+// Constants of the mixed σ̃ form.
+struct KConstsSig {
+  df64 aSq;
+  float mu4pi, mu4pinu, nuMu4pinu, aSq32, aSqMu8pi;
+};
+
+// σ̃ contribution of one segment (n1, n2, unit direction t, Burgers vector b)
+// at the point x, added into six df64 accumulators (xx, yy, zz, xy, xz, yz):
+// the reference's formulas (DislocationFEM.jl:135-299, sigma_point in
+// pair_f64.cuh), with the geometry (R, d, s1, s2), the endpoint terms and their
+// differences s_03 ... s_25 in df64 — where the two endpoints cancel — and the
+// coefficient assembly (t, d, t x b, d x b products) and the five-term sum in
+// FP32.
+DF_HD void sigma_point_mixed(const KConstsSig& K, F3 b, DV3 n1, DV3 n2, DV3 t, DV3 x, df64* sig) {
+  const DV3 R = x - n1;
+  const df64 Rdt = dot(R, t);
+  const DV3 nd = R - Rdt * t;
+  const df64 d2 = dot(nd, nd);
+  const df64 s1 = -Rdt;
+  const df64 s2 = -dot(x - n2, t);
+  const df64 a2_d2 = K.aSq + d2;
+  const df64 a2d2inv = df_recip(a2_d2);
+  df64 S[5];
+  {
+    df64 Ra = df_sqrt(a2_d2 + s1 * s1);
+    df64 Rainv = df_recip(Ra);
+    df64 Ra3inv = Rainv * Rainv * Rainv;
+    df64 sRa3inv = s1 * Ra3inv;
+    const df64 s_03a = s1 * Rainv * a2d2inv;
+    const df64 s_13a = -Rainv;
+    const df64 s_05a = (df_scale(s_03a, 2.0f) + sRa3inv) * a2d2inv;
+    const df64 s_15a = -Ra3inv;
+    const df64 s_25a = s_03a - sRa3inv;
+    Ra = df_sqrt(a2_d2 + s2 * s2);
+    Rainv = df_recip(Ra);
+    Ra3inv = Rainv * Rainv * Rainv;
+    sRa3inv = s2 * Ra3inv;
+    const df64 s_03b = s2 * Rainv * a2d2inv;
+    const df64 s_13b = -Rainv;
+    const df64 s_05b = (df_scale(s_03b, 2.0f) + sRa3inv) * a2d2inv;
+    const df64 s_15b = -Ra3inv;
+    const df64 s_25b = s_03b - sRa3inv;
+    S[0] = s_03b - s_03a;
+    S[1] = s_13b - s_13a;
+    S[2] = s_05b - s_05a;
+    S[3] = s_15b - s_15a;
+    S[4] = s_25b - s_25a;
+  }
+  float Sf[5];
+  for (int i = 0; i < 5; ++i) Sf[i] = S[i].hi + S[i].lo;
+  const F3 tf = f3(t), dv = f3(nd);
+  const F3 txb = cross(tf, b), dxb = cross(dv, b);
+  const float common = K.mu4pinu * dot(dxb, tf);
+  const float tt[3] = {tf.x, tf.y, tf.z}, dd[3] = {dv.x, dv.y, dv.z};
+  const float tb_[3] = {txb.x, txb.y, txb.z}, db_[3] = {dxb.x, dxb.y, dxb.z};
+  for (int c = 0; c < 6; ++c) {
+    const int p = (c < 3) ? c : (c == 3 ? 0 : (c == 4 ? 0 : 1));
+    const int q = (c < 3) ? c : (c == 3 ? 1 : 2);
+    float dmd, tmt, tmd, tmtxb, dmtxb, tmdxb;
+    if (c < 3) {
+      dmd = dd[p] * dd[p];
+      tmt = tt[p] * tt[p];
+      tmd = 2.0f * tt[p] * dd[p];
+      tmtxb = 2.0f * tt[p] * tb_[p];
+      dmtxb = 2.0f * dd[p] * tb_[p];
+      tmdxb = 2.0f * tt[p] * db_[p];
+    } else {
+      dmd = dd[p] * dd[q];
+      tmt = tt[p] * tt[q];
+      tmd = tt[p] * dd[q] + tt[q] * dd[p];
+      tmtxb = tt[p] * tb_[q] + tt[q] * tb_[p];
+      dmtxb = dd[p] * tb_[q] + dd[q] * tb_[p];
+      tmdxb = tt[p] * db_[q] + tt[q] * db_[p];
+    }
+    const float I03 = (c < 3) ? (common + K.mu4pinu * dmtxb - K.mu4pi * tmdxb) : (K.mu4pinu * dmtxb - K.mu4pi * tmdxb);
+    const float I13 = -K.nuMu4pinu * tmtxb;
+    const float I05 = (c < 3) ? (common * (K.aSq32 + dmd) - K.aSqMu8pi * tmdxb) : (common * dmd - K.aSqMu8pi * tmdxb);
+    const float I15 = K.aSqMu8pi * tmtxb - common * tmd;
+    const float I25 = common * tmt;
+    sig[c] = sig[c] + (I03 * Sf[0] + I13 * Sf[1] + I05 * Sf[2] + I15 * Sf[3] + I25 * Sf[4]);
+  }
+}
+
 }  // namespace ddd

@@ -76,9 +76,65 @@ cudaError_t set_attr_df() {
   return cudaSuccess;
 }
 
+// σ̃ in the mixed form (sigma_point_mixed, pair_df.cuh): one thread per point,
+// segments streamed through shared memory as df64 pairs (n1, n2, t) and FP32
+// (b), six df64 accumulators per point in the segment order of the FP64 kernel.
+constexpr int SIG_TILE = 128;
+__global__ void __launch_bounds__(SIG_TILE)
+sigma_tilde_mixed(KConstsSig K, const float* __restrict__ soadf, int64_t npad, int64_t nSeg,
+                  const double* __restrict__ x0, int64_t M, double* __restrict__ sigma) {
+  __shared__ float seg[21][SIG_TILE];  // n1 hi/lo (6), n2 hi/lo (6), b hi (3), t hi/lo (6)
+  const int t = threadIdx.x;
+  const int64_t j = blockIdx.x * (int64_t)SIG_TILE + t;
+  DV3 x = {df(0.f), df(0.f), df(0.f)};
+  if (j < M) x = {df_from_double(x0[3 * j]), df_from_double(x0[3 * j + 1]), df_from_double(x0[3 * j + 2])};
+  df64 sig[6];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) sig[c] = df(0.f);
+  for (int64_t s0 = 0; s0 < nSeg; s0 += SIG_TILE) {
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 12; ++k) seg[k][t] = soadf[k * npad + s0 + t];  // rows 0-11: n1, n2 (hi, lo)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) seg[12 + k][t] = soadf[(12 + 2 * k) * npad + s0 + t];  // b hi
+#pragma unroll
+    for (int k = 0; k < 6; ++k) seg[15 + k][t] = soadf[(18 + k) * npad + s0 + t];  // t (hi, lo)
+    __syncthreads();
+    const int n = (int)min((int64_t)SIG_TILE, nSeg - s0);
+    if (j < M) {
+      for (int q = 0; q < n; ++q) {
+        const DV3 n1 = {df64{seg[0][q], seg[1][q]}, df64{seg[2][q], seg[3][q]}, df64{seg[4][q], seg[5][q]}};
+        const DV3 n2 = {df64{seg[6][q], seg[7][q]}, df64{seg[8][q], seg[9][q]}, df64{seg[10][q], seg[11][q]}};
+        const F3 b = {seg[12][q], seg[13][q], seg[14][q]};
+        const DV3 tt = {df64{seg[15][q], seg[16][q]}, df64{seg[17][q], seg[18][q]}, df64{seg[19][q], seg[20][q]}};
+        sigma_point_mixed(K, b, n1, n2, tt, x, sig);
+      }
+    }
+  }
+  if (j < M) {
+#pragma unroll
+    for (int c = 0; c < 6; ++c) sigma[6 * j + c] = df_to_double(sig[c]);
+  }
+}
+
 }  // namespace
 
 size_t segseg_df_soa_bytes(int64_t npad) { return (size_t)npad * 26 * sizeof(float); }
+
+cudaError_t launch_sigma_mixed(const KConsts& K, const float* soadf, int64_t npad, int64_t nSeg, const double* x0,
+                               int64_t M, double* sigma, cudaStream_t st) {
+  if (M == 0) return cudaSuccess;
+  KConstsSig KS;
+  KS.aSq = kconsts_df(K).aSq;
+  KS.mu4pi = (float)K.mu4pi;
+  KS.mu4pinu = (float)K.mu4pinu;
+  KS.nuMu4pinu = (float)K.nuMu4pinu;
+  KS.aSq32 = (float)K.aSq;
+  KS.aSqMu8pi = (float)(K.aSq * K.mu8pi);
+  sigma_tilde_mixed<<<(unsigned)((M + SIG_TILE - 1) / SIG_TILE), SIG_TILE, 0, st>>>(KS, soadf, npad, nSeg, x0, M,
+                                                                                     sigma);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_prep_df(const double* soa, int64_t npad, float* soadf, cudaStream_t st) {
   prep_df<<<(unsigned)((npad + 255) / 256), 256, 0, st>>>(soa, npad, soadf);

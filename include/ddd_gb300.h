@@ -57,7 +57,9 @@ typedef struct ddd_ctx ddd_ctx;
  * FP32 pipes; the near-parallel branch, the branch decision and the per-node
  * accumulation stay FP64.  Its error is of the order of 2^6 times the FP64
  * form's own rounding error (FP32-pair vs FP64 unit roundoff).  The field
- * stress (ddd_sigma_tilde*) runs in DDD_MODE_FP64 arithmetic in this mode. */
+ * stress (ddd_sigma_tilde*) runs in the mixed form in this mode and in
+ * DDD_MODE_F32C: geometry, endpoint terms and their differences in df64,
+ * coefficient assembly in FP32, per-point sums in df64 (~1e-7 relative). */
 #define DDD_MODE_DF64 2
 /* DDD_MODE_F32C, the FP32 form with compensated terms: the integration-domain
  * geometry, the four corner antiderivatives (their logs, arctangents, roots and

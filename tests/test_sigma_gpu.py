@@ -87,6 +87,39 @@ def test_random_vs_oracle(pkg, synth, oracle, num_loops, npts):
     assert_sigma_close(S, ref)
 
 
+@pytest.mark.parametrize("mode", ["f32c", "df64"])
+@pytest.mark.parametrize("num_loops,cube,npts", [(64, 2000.0, 2048), (512, 20000.0, 1024)])
+def test_mixed_form(pkg, synth, oracle, mode, num_loops, cube, npts):
+    """σ̃ in the precision modes (the mixed form: geometry and endpoint
+    differences in df64, assembly in FP32, per-point sums in df64).  The same
+    code compiled for a CPU measures ~1.4e-7 relative RMS against long double
+    (per point up to ~4e-6 on points where the segments' contributions cancel).
+    Bounds: normwise <= 1e-6, per point <= 3e-5 |σ_p| + 1e-7 max|σ|.  idx and
+    single-point forms included."""
+    p, b = synth.square_loops(num_loops, 3, 50.0, 200.0, cube, 0.5, 0.05)
+    coord, bvec, seg = synth.network_arrays(p, b)
+    net = pkg.DislocationNetwork(coord, bvec, seg)
+    rng = np.random.default_rng(npts)
+    pts = np.asfortranarray(rng.uniform(0, cube, (3, npts)))
+    dln = pkg.DislocationParameters(coreRad=1.0)
+    mat = pkg.MaterialParameters(mu=1.0, nu=0.28)
+    ref = oracle.sigma_tilde(k5_of(dln, mat), pts, net)
+    ctx = pkg.get_context()
+    ctx.mode = mode
+    try:
+        S = pkg.calc_σTilde(pts, dln, mat, net)
+        idx = rng.integers(1, net.numSeg + 1, 50)
+        Si = pkg.calc_σTilde(pts[:, :40], dln, mat, net, idx)
+        S1 = pkg.calc_σTilde(pts[:, 7], dln, mat, net)
+    finally:
+        ctx.mode = "fp64"
+    assert np.linalg.norm(S - ref) <= 1e-6 * np.linalg.norm(ref)
+    assert_sigma_close(S, ref, rel=3e-5, floor=1e-7)
+    refi = oracle.sigma_tilde(k5_of(dln, mat), pts[:, :40], net, idx=idx)
+    assert_sigma_close(Si, refi, rel=3e-5, floor=1e-7)
+    assert np.allclose(S1, S[:, 7], rtol=0, atol=1e-12 * np.abs(S).max())
+
+
 def test_idx_selection(pkg, synth, oracle):
     p, b = synth.square_loops(30, 5, 50.0, 200.0, 2000.0, 0.5, 0.0)
     coord, bvec, seg = synth.network_arrays(p, b)
