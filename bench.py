@@ -21,6 +21,10 @@ surrogate: the same workload through ddd_surrogate_force (far pairs by the
        speedup over the FP64 kernel, node-force error against the FP64 result,
        and the network kernel's tensor throughput.
 
+precision_131k: the precision-form workload (131,072 segments, f32c force and
+       mixed-form σ̃ on 2^20 points) with errors against the FP64 kernel on
+       sampled segments and points.
+
 --impl reference: times that CPU port alone (the reference itself is Julia and
 cannot run here), same metric and workload, each step a bounded sub-network.
 
@@ -109,6 +113,16 @@ class ClockSampler:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def max_over_ranks(value, dist, device):
+    """The largest of every rank's `value` (the job's time is its slowest rank's);
+    `dist` is torch.distributed or None for one process."""
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.item()
 
 
 def cpu_threads():
@@ -205,6 +219,75 @@ def run_surrogate(args, pkg, ctx, k, soa, ref, pairs, ms_fp64, stream, sptr, flu
     return out
 
 
+def run_precision_131k(pkg, synth, ctx, k, stream, sptr, flush):
+    """The precision-form workload: 131,072 segments of the same generator, the
+    f32c all-pairs force and the mixed-form σ̃ on the 128^3 = 2^20-point grid,
+    each timed once after a warm-up; errors against the FP64 kernel (the
+    correctness oracle of the GPU forms) on 512 sampled segments (the idx form)
+    and 4,096 sampled points."""
+    import torch
+    p, b, cfg = synth.make("prec131k", seed=0)
+    n = p.shape[0] * 8
+    pairs = n * (n - 1) // 2
+    soa = torch.from_numpy(synth.packed_soa(p, b)).cuda()
+    force = torch.zeros(6 * n, dtype=torch.float64, device="cuda")
+    rng = np.random.default_rng(0)
+    rows = np.sort(rng.choice(n, 512, replace=False))
+    pts = synth.grid_points(cfg["grid"], cfg["cube"])
+    M = pts.shape[1]
+    x0 = torch.from_numpy(np.ascontiguousarray(pts.T)).cuda()
+    sig = torch.zeros(6 * M, dtype=torch.float64, device="cuda")
+
+    def timed(fn):
+        with torch.cuda.stream(stream):
+            fn()
+            torch.cuda.synchronize()
+            flush.zero_()
+            a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a_.record(stream)
+            fn()
+            b_.record(stream)
+            torch.cuda.synchronize()
+        return a_.elapsed_time(b_)
+
+    ctx.mode = "f32c"
+    try:
+        ms_f = timed(lambda: ctx.segseg_force_device(k, soa.data_ptr(), n, n, force.data_ptr(), stream=sptr))
+        ms_s = timed(lambda: ctx.sigma_tilde_device(k, x0.data_ptr(), M, soa.data_ptr(), n, n, sig.data_ptr(),
+                                                    stream=sptr))
+    finally:
+        ctx.mode = "fp64"
+    coord, bvec, seg = synth.network_arrays(p, b)
+    net = pkg.DislocationNetwork(coord, bvec, seg)
+    ref_rows = ctx.segseg_force(k, net, idx=rows + 1)  # FP64, 3 x 2 x 512
+    got = force.cpu().numpy().reshape(3, 2, n, order="F")[:, :, rows]
+    dn = np.linalg.norm(got - ref_rows, axis=0)
+    fn = np.linalg.norm(ref_rows, axis=0)
+    sp = np.sort(rng.choice(M, 4096, replace=False))
+    xs = torch.from_numpy(np.ascontiguousarray(pts[:, sp].T)).cuda()
+    sref = torch.zeros(6 * len(sp), dtype=torch.float64, device="cuda")
+    ctx.sigma_tilde_device(k, xs.data_ptr(), len(sp), soa.data_ptr(), n, n, sref.data_ptr())
+    torch.cuda.synchronize()
+    sg = sig.view(M, 6)[torch.from_numpy(sp).cuda()]
+    sr = sref.view(len(sp), 6)
+    ds = torch.linalg.norm(sg - sr, dim=1)
+    ns = torch.linalg.norm(sr, dim=1)
+    return {
+        "config": "prec131k: %d segments (%d loops, same generator), sigma on the %d^3 = %d-point grid"
+                  % (n, p.shape[0], cfg["grid"], M),
+        "force_f32c": {"value": pairs / (ms_f * 1e-3), "unit": "pair-interactions/s", "ms": ms_f,
+                       "error_vs_fp64_sampled_512_segments": {
+                           "rel_rms": float(np.linalg.norm(got - ref_rows) / np.linalg.norm(ref_rows)),
+                           "max_rel_node": float(np.max(dn / fn)),
+                           "max_node_over_max_force": float(dn.max() / fn.max())}},
+        "sigma_mixed": {"value": n * M / (ms_s * 1e-3), "unit": "seg-point evaluations/s", "ms": ms_s,
+                        "error_vs_fp64_sampled_4096_points": {
+                            "rel_rms": (torch.linalg.norm(sg - sr) / torch.linalg.norm(sr)).item(),
+                            "max_rel_point": (ds / ns).max().item(),
+                            "max_point_over_max": (ds.max() / ns.max()).item()}},
+    }
+
+
 def run_reference(args, pkg, synth, oracle):
     ws, rank = _dist()
     if rank != 0:
@@ -255,6 +338,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--sigma-grid", type=int, default=32)
     ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--no-precision131k", action="store_true")
     ap.add_argument("--profile-surrogate", type=int, default=0, metavar="N",
                     help="only run N surrogate force calls on the workload (f32c exact passes, no audit) and exit: "
                          "the command the ncu captures of the surrogate kernels use")
@@ -329,11 +413,9 @@ def main():
             torch.cuda.synchronize()
         ms_total = ev0.elapsed_time(ev1)
         ms_kernel = [a.elapsed_time(b_) for a, b_ in kev]
-    t_rank = torch.tensor([ms_total], dtype=torch.float64, device="cuda")
+    ms_step = max_over_ranks(ms_total, dist, "cuda") / args.steps
     if dist:
-        dist.all_reduce(t_rank, op=dist.ReduceOp.MAX)
         dist.barrier()
-    ms_step = t_rank.item() / args.steps
     value = ws * pairs / (ms_step * 1e-3)
 
     # Other arithmetic modes of the same path, same workload and timing: the FMA
@@ -384,6 +466,10 @@ def main():
                 nk["peak_tflops"] = tp
                 nk["frac"] = nk["tensor_tflops"] / tp if tp else None
                 nk["peak_source"] = "MEASURED_PEAKS.json bf16_tflops (burst; FP16 dense rate is the same)"
+
+    precision131k = None
+    if not args.no_precision131k and args.loops is None:
+        precision131k = run_precision_131k(pkg, synth, ctx, k, stream, sptr, flush)
 
     # Field-point stress σ̃ of the same network on a 32^3 grid over the cube.
     sigma = None
@@ -509,6 +595,7 @@ def main():
         "mode": "fp64 (strict: every multiply and add rounded separately, as the reference)",
         "variants": variants,
         "surrogate": surrogate,
+        "precision_131k": precision131k,
         "sigma_tilde": sigma,
         "batched": batched,
         "kernel_ms_per_step": statistics.mean(ms_kernel),

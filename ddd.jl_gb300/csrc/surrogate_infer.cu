@@ -134,7 +134,8 @@ __device__ __forceinline__ bool layer(uint32_t tm, const unsigned char* A, const
 }
 
 // Row t of the warpgroup's 128-column accumulator + bias (FP32), GELU on FP16
-// pairs, into H (FP16): the same arithmetic as the training forward pass.
+// pairs, into H (FP16): the same arithmetic as the training forward pass.  32
+// columns per tcgen05.wait::ld (64 measured 10% slower: register pressure).
 __device__ __forceinline__ void hidden_epilogue(uint32_t tm_row, const float* bias, unsigned char* H, int t) {
 #pragma unroll 1
   for (int c0 = 0; c0 < kHidden; c0 += 32) {
