@@ -170,7 +170,7 @@ def run_surrogate(args, pkg, ctx, k, soa, ref, pairs, ms_fp64, stream, sptr, flu
     if os.path.exists(args.surrogate):
         sur.load(args.surrogate)
         source = "checkpoint %s (ddd.jl_gb300/train_surrogate.py: 4 networks of the generator, seeds 11-14, " \
-                 "2^21 far pairs each, 20 epochs)" % os.path.relpath(args.surrogate, ROOT)
+                 "2.5e6 far pairs each, 20 epochs)" % os.path.relpath(args.surrogate, ROOT)
     else:
         import importlib.util
         spec = importlib.util.spec_from_file_location("train_surrogate",

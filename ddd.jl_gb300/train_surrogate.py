@@ -1,7 +1,7 @@
 """Train the far-field surrogate on seeded synthetic networks and save a checkpoint.
 
     python ddd.jl_gb300/train_surrogate.py --config gpu65k --seeds 11 12 13 14 \
-        --pairs 2097152 --epochs 20 --out ddd.jl_gb300/data/surrogate_gpu65k_nu028.bin
+        --pairs 2500000 --epochs 20 --out ddd.jl_gb300/data/surrogate_gpu65k_nu028.bin
 
 Every step runs on the GPU through the library: pair sampling picks far pairs
 (R >= 0.9 kappa max(L_i, L_j)) of each network, the FP64 kernel computes their
@@ -33,7 +33,7 @@ def _package():
     return mod
 
 
-def train(config="gpu65k", seeds=(11, 12, 13, 14), pairs=1 << 21, epochs=20, batch=4096, lr=2e-3, kappa=20.0,
+def train(config="gpu65k", seeds=(11, 12, 13, 14), pairs=2500000, epochs=20, batch=4096, lr=2e-3, kappa=20.0,
           out=None, seed=5, device=0):
     pkg = _package()
     import ddd_gb300.synth as synth
@@ -58,7 +58,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--config", default="gpu65k")
     ap.add_argument("--seeds", type=int, nargs="+", default=[11, 12, 13, 14])
-    ap.add_argument("--pairs", type=int, default=1 << 21, help="training pairs per network")
+    ap.add_argument("--pairs", type=int, default=2500000, help="training pairs per network (4 x 2.5e6 = 1e7)")
     ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--batch", type=int, default=4096)
     ap.add_argument("--lr", type=float, default=2e-3)
