@@ -22,7 +22,7 @@ surrogate: the same workload through ddd_surrogate_force (far pairs by the
        and the network kernel's tensor throughput.
 
 precision_131k: the precision-form workload (131,072 segments, f32c force and
-       mixed-form σ̃ on 2^20 points) with errors against the FP64 kernel on
+       mixed-form σ̃ on the 128^3 grid) with errors against the FP64 kernel on
        sampled segments and points.
 
 --impl reference: times that CPU port alone (the reference itself is Julia and
