@@ -221,7 +221,7 @@ def run_surrogate(args, pkg, ctx, k, soa, ref, pairs, ms_fp64, stream, sptr, flu
 
 def run_precision_131k(pkg, synth, ctx, k, stream, sptr, flush):
     """The precision-form workload: 131,072 segments of the same generator, the
-    f32c all-pairs force and the mixed-form σ̃ on the 128^3 = 2^20-point grid,
+    f32c all-pairs force and the mixed-form σ̃ on the 128^3-point grid,
     each timed once after a warm-up; errors against the FP64 kernel (the
     correctness oracle of the GPU forms) on 512 sampled segments (the idx form)
     and 4,096 sampled points."""
