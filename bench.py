@@ -132,27 +132,58 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
-def cpu_par_sample(pkg, synth, oracle, p, b, k5, target_s):
-    """Times the OpenMP port of calcSegSegForcePar on the first n segments of the
-    workload, n chosen so that one run takes about target_s seconds."""
+def cpu_par_sample(pkg, synth, oracle, p, b, k5, target_s, variant="atomic"):
+    """Times an OpenMP port on the first n segments of the workload, n chosen so
+    that one run takes about target_s seconds.  variant "atomic": the
+    restatement of calcSegSegForcePar (contiguous i-chunks, one atomic add per
+    output component); "private": the best-effort form (dynamic rows, per-thread
+    accumulators)."""
     threads = cpu_threads()
+    fn = oracle.segseg_par_atomic if variant == "atomic" else oracle.segseg_par_private
     coord, bvec, seg = synth.network_arrays(p[:256], b[:256])
     net = pkg.DislocationNetwork(coord, bvec, seg)
     t0 = time.perf_counter()
-    oracle.segseg_par_atomic(k5, net, threads)
+    fn(k5, net, threads)
     dt = time.perf_counter() - t0
     rate = net.numSeg * (net.numSeg - 1) / 2 / dt
     n_loops = int(min(p.shape[0], max(256, np.sqrt(2 * rate * target_s) / 8)))
     coord, bvec, seg = synth.network_arrays(p[:n_loops], b[:n_loops])
     net = pkg.DislocationNetwork(coord, bvec, seg)
     t0 = time.perf_counter()
-    oracle.segseg_par_atomic(k5, net, threads)
+    fn(k5, net, threads)
     dt = time.perf_counter() - t0
     n = net.numSeg
     return {"value": n * (n - 1) / 2 / dt, "unit": "pair-interactions/s", "cores": threads, "kind": "port",
+            "variant": variant,
             "sample": "all %d pairs of the first %d segments (%d loops) of the workload, %.1f s" %
                       (n * (n - 1) // 2, n, n_loops, dt)}
 
+
+def cpu_sigma_sample(pkg, synth, oracle, p, b, k5, cube, target_s):
+    """Times the OpenMP port of _calc_σTilde! (segment-outer order kept per
+    point, points split over threads) on all segments of the workload and a
+    sample of grid points sized to about target_s seconds."""
+    threads = cpu_threads()
+    coord, bvec, seg = synth.network_arrays(p, b)
+    net = pkg.DislocationNetwork(coord, bvec, seg)
+    pts = synth.grid_points(32, cube)
+    t0 = time.perf_counter()
+    oracle.sigma_tilde(k5, pts[:, :threads], net, nthreads=threads)
+    dt = time.perf_counter() - t0
+    m = int(min(pts.shape[1], max(threads, threads * target_s / max(dt, 1e-6))))
+    t0 = time.perf_counter()
+    oracle.sigma_tilde(k5, np.asfortranarray(pts[:, :m]), net, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": net.numSeg * m / dt, "unit": "seg-point evaluations/s", "cores": threads, "kind": "port",
+            "sample": "%d segments x %d points of the 32^3 grid, %.1f s" % (net.numSeg, m, dt)}
+
+
+# DRAM bytes per tile pair of the strict tile kernel and of the network pass,
+# from one ncu capture each at 32,768 segments (32,896 tile pairs; the partial
+# slots exceed L2 there, so traffic grows with the tile-pair count):
+# profiles/dram_traffic_tile_mlp_32k.md.
+TILE_DRAM_BYTES_PER_TILE_PAIR = (31162112 + 376273664) // 32896
+MLP_DRAM_BYTES_PER_TILE_PAIR = (12404992 + 346662144) // 32896
 
 # Tensor-core FLOPs of the surrogate network per pair slot (one row of the
 # 128-row MMA tiles): 2 (16*128 + 128*128 + 128*128 + 128*112).
@@ -213,6 +244,7 @@ def run_surrogate(args, pkg, ctx, k, soa, ref, pairs, ms_fp64, stream, sptr, flu
             "ms": {kk: rep[kk] for kk in ("ms_prep", "ms_network", "ms_audit", "ms_near", "ms_reduce")},
             "network_kernel": {"kernel": "mlp_far_tiles", "tensor_tflops": tfl, "bound": "tensor",
                                "peak_tflops": None, "frac": None,
+                               "traffic": MLP_DRAM_BYTES_PER_TILE_PAIR * rep["tiles_total"],
                                "flops": "%d pair slots x %d MMA FLOPs (FP16 operands, FP32 accumulation)"
                                         % (slots, OPS_MLP_PAIR)},
         }
@@ -583,7 +615,10 @@ def main():
                    "pairs_per_step": pairs, "l2": "flushed before every step (512 MB write)",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
-                     "frac": achieved / fp64_peak, "traffic": None,
+                     "frac": achieved / fp64_peak,
+                     "traffic": TILE_DRAM_BYTES_PER_TILE_PAIR * (n // 128) * (n // 128 + 1) // 2,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at 32,768 "
+                                       "segments, scaled by tile pairs (profiles/dram_traffic_tile_mlp_32k.md)",
                      "kernel": "segseg_tile_f64<0>",
                      "peak_source": "measured FP64 FMA-chain probe on this GPU (ddd_probe_fma_peak); "
                                     "MEASURED_PEAKS.json holds no FP64 figure",
@@ -606,6 +641,10 @@ def main():
     if not args.no_cpu:
         k5 = np.array([dln.coreRadSq, mat.μ4π, mat.μ8π, mat.μ4πν, mat.νμ4πν])
         line["cpu_baseline"] = cpu_par_sample(pkg, synth, oracle, p, b, k5, args.cpu_target_s)
+        line["cpu_baseline_private"] = cpu_par_sample(pkg, synth, oracle, p, b, k5, args.cpu_target_s / 2,
+                                                      variant="private")
+        if sigma is not None:
+            sigma["cpu_baseline"] = cpu_sigma_sample(pkg, synth, oracle, p, b, k5, cfg["cube"], 5.0)
         # Parity of the timed result on sampled segments: the oracle's Float64 rows
         # and the same rows in long double (the reference arithmetic's own error).
         rows = np.sort(np.random.default_rng(0).choice(n, 16, replace=False))

@@ -162,6 +162,40 @@ void oracle_segseg_par_atomic(const double* k5, const double* coord, const doubl
   for (int64_t k = 0; k < 6 * numSeg; ++k) F[k] = acc[k].load(std::memory_order_relaxed);
 }
 
+// The best-effort CPU form of the same all-pairs sum (not a reference code
+// path): rows handed out dynamically, every thread accumulating into its own
+// 3×2×numSeg array, the arrays summed at the end.  No atomics, balanced load;
+// the result differs from Ser / Par only by summation order.
+void oracle_segseg_par_private(const double* k5, const double* coord, const double* bVec, const int64_t* segIdx,
+                               int64_t ld, const uint8_t* extSeg, int64_t numSeg, double* F, int nthreads) {
+  Consts<double> K = make_consts(k5);
+  std::vector<Seg> s = gather(coord, bVec, segIdx, ld, numSeg);
+  const int T = nthreads > 0 ? nthreads : 1;
+  std::vector<double> priv((size_t)T * 6 * numSeg, 0.0);
+#pragma omp parallel num_threads(T)
+  {
+    double* acc = priv.data() + (size_t)omp_get_thread_num() * 6 * numSeg;
+    V3<double> out[4];
+#pragma omp for schedule(dynamic, 16)
+    for (int64_t i = 0; i < numSeg; ++i) {
+      if (extSeg[i]) continue;
+      for (int64_t j = i + 1; j < numSeg; ++j) {
+        if (extSeg[j]) continue;
+        seg_seg_force<double>(K, s[i].b, s[i].n1, s[i].n2, s[j].b, s[j].n1, s[j].n2, out);
+        add3(acc + 6 * i, out[0]);
+        add3(acc + 6 * i + 3, out[1]);
+        add3(acc + 6 * j, out[2]);
+        add3(acc + 6 * j + 3, out[3]);
+      }
+    }
+  }
+  for (int64_t k = 0; k < 6 * numSeg; ++k) {
+    double v = 0.0;
+    for (int t = 0; t < T; ++t) v += priv[(size_t)t * 6 * numSeg + k];
+    F[k] = v;
+  }
+}
+
 // Rows of the all-pairs (Ser) result for the segments in rows[] (0-based):
 // F_s = Σ_{j<s} Fnode3,4(j, s) + Σ_{j>s} Fnode1,2(s, j), added in that order,
 // which is exactly the order calcSegSegForceSer! adds into column s.  Used to

@@ -28,7 +28,7 @@ def build(force=False):
         return LIB_PATH
     import subprocess
     tmp = LIB_PATH + ".tmp"
-    cmd = ["g++", "-std=c++20", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-o", tmp, src]
+    cmd = ["g++", "-std=c++20", "-O3", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-o", tmp, src]
     subprocess.check_call(cmd)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
@@ -45,6 +45,8 @@ def lib():
         L.oracle_segseg_ser.argtypes = [_dp, _dp, _dp, _ip, ctypes.c_int64, _up, ctypes.c_int64, _dp]
         L.oracle_segseg_par_atomic.argtypes = [_dp, _dp, _dp, _ip, ctypes.c_int64, _up, ctypes.c_int64, _dp,
                                                ctypes.c_int]
+        L.oracle_segseg_par_private.argtypes = [_dp, _dp, _dp, _ip, ctypes.c_int64, _up, ctypes.c_int64, _dp,
+                                                ctypes.c_int]
         L.oracle_segseg_rows.argtypes = [_dp, _dp, _dp, _ip, ctypes.c_int64, _up, ctypes.c_int64, _ip,
                                          ctypes.c_int64, _dp, ctypes.c_int]
         L.oracle_segseg_idx.argtypes = [_dp, _dp, _dp, _ip, ctypes.c_int64, _up, ctypes.c_int64, _ip,
@@ -117,6 +119,15 @@ def segseg_par_atomic(k5, net, nthreads):
     F = np.zeros((3, 2, net.numSeg), np.float64, order="F")
     lib().oracle_segseg_par_atomic(_d(np.ascontiguousarray(k5, np.float64)), _d(coord), _d(bvec), _i(seg), ld,
                                    ext.ctypes.data_as(_up), net.numSeg, _d(F), int(nthreads))
+    return F
+
+
+def segseg_par_private(k5, net, nthreads):
+    """All-pairs forces with per-thread private accumulators (best-effort CPU form)."""
+    coord, bvec, seg, ext, ld = _net_arrays(net)
+    F = np.zeros((3, 2, net.numSeg), np.float64, order="F")
+    lib().oracle_segseg_par_private(_d(np.ascontiguousarray(k5, np.float64)), _d(coord), _d(bvec), _i(seg), ld,
+                                    ext.ctypes.data_as(_up), net.numSeg, _d(F), int(nthreads))
     return F
 
 

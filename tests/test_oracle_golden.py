@@ -59,6 +59,9 @@ def test_segseg_threaded_matches_golden(oracle, fixtures, name):
         F = oracle.segseg_par_atomic(k5, net, nt)
         _close(F[:, 0, :].T, np.array(c["f1"]))
         _close(F[:, 1, :].T, np.array(c["f2"]))
+        Fp = oracle.segseg_par_private(k5, net, nt)  # the best-effort CPU baseline form
+        _close(Fp[:, 0, :].T, np.array(c["f1"]))
+        _close(Fp[:, 1, :].T, np.array(c["f2"]))
 
 
 @pytest.mark.parametrize("name", SEG_NAMES)
