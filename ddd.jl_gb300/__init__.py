@@ -10,6 +10,9 @@ order, array layouts and semantics:
   calcSegSegForce_inplace(dlnParams, matParams, network, idx=None) calcSegSegForce!  :576-669
   calc_σTilde(x0, dlnParams, matParams, network, idx=None)        DislocationFEM.jl:24-41
   calc_σTilde_inplace(σ, x0, dlnParams, matParams, network, idx=None) calc_σTilde! :67-84
+  calcSelfForce(dlnParams, matParams, network, idx=None)          DislocationForces.jl:320-353 (and _inplace)
+  calcSegForce(dlnParams, matParams, sigmaHat, network, idx=None) DislocationForces.jl:23-46 (and _inplace;
+      sigmaHat = the FE stress at the segment midpoints, in place of mesh and forceDisplacement)
 
 All computation runs on the GPU.  There is no CPU fallback: if the library is
 not built or no GPU is usable, calls raise.
@@ -40,6 +43,7 @@ EXPORTED_SYMBOLS = (
     "ddd_surrogate_make_data", "ddd_surrogate_train", "ddd_surrogate_forward", "ddd_surrogate_grads",
     "ddd_surrogate_force", "ddd_surrogate_force_host", "ddd_surrogate_last_error", "ddd_surrogate_save",
     "ddd_surrogate_load",
+    "ddd_self_force", "ddd_self_force_inplace", "ddd_seg_force", "ddd_seg_force_inplace",
 )
 
 # Arithmetic modes (ddd_set_mode).
@@ -76,6 +80,10 @@ class ddd_report(ctypes.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ddd_self_params(ctypes.Structure):
+    _fields_ = [("coreRad", ctypes.c_double), ("coreEnergy", ctypes.c_double), ("nu", ctypes.c_double)]
 
 
 class ddd_sur_opts(ctypes.Structure):
@@ -165,6 +173,12 @@ def library():
         L.ddd_surrogate_load.argtypes = [_vp, ctypes.c_char_p, _dp, _dp, _dp]
         L.ddd_surrogate_last_error.argtypes = [_vp]
         L.ddd_surrogate_last_error.restype = ctypes.c_char_p
+        spp = ctypes.POINTER(ddd_self_params)
+        net_args = [_dp, _i64, _dp, _i64, _ip, _i64, _up, _i64]
+        L.ddd_self_force.argtypes = [_vp, cp, spp] + net_args + [_ip, _i64, _dp, _dp]
+        L.ddd_self_force_inplace.argtypes = [_vp, cp, spp] + net_args + [_ip, _i64, _dp, _i64]
+        L.ddd_seg_force.argtypes = [_vp, cp, spp] + net_args + [_dp, _ip, _i64, _dp, rp]
+        L.ddd_seg_force_inplace.argtypes = [_vp, cp, spp] + net_args + [_dp, _ip, _i64, _dp, _i64, rp]
         L.ddd_set_mode.argtypes = [_vp, ctypes.c_int]
         L.ddd_get_mode.argtypes = [_vp]
         L.ddd_probe_fma_peak.argtypes = [_vp, ctypes.c_int, _dp]
@@ -199,10 +213,12 @@ class MaterialParameters:
 class DislocationParameters:
     """The DislocationParameters fields this path reads (src/Type/DislocationConstructor.jl:55-105)."""
 
-    def __init__(self, *, coreRad=1.0, coreRadMag=1.0, minSegLen=None, maxSegLen=None, parCPU=False,
-                 parGPU=True, **other):
+    def __init__(self, *, coreRad=1.0, coreRadMag=1.0, coreEnergy=None, minSegLen=None, maxSegLen=None,
+                 parCPU=False, parGPU=True, **other):
         self.coreRad = float(coreRad)
         self.coreRadSq = self.coreRad * self.coreRad
+        self.coreEnergy = (1 / (4 * math.pi) * math.log(self.coreRad / 0.1) if coreEnergy is None
+                           else float(coreEnergy))
         self.coreRadMag = float(coreRadMag)
         self.minSegLen = 2 * self.coreRad if minSegLen is None else float(minSegLen)
         self.maxSegLen = 20 * self.coreRad if maxSegLen is None else float(maxSegLen)
@@ -229,6 +245,14 @@ class DislocationNetwork:
         self.extSeg = (np.zeros(ld, np.uint8) if extSeg is None else np.ascontiguousarray(extSeg, dtype=np.uint8))
         self.segForce = (np.zeros((3, 2, self.bVec.shape[1]), np.float64, order="F") if segForce is None
                          else np.asfortranarray(segForce, dtype=np.float64))
+
+
+def self_params_of(dlnParams, matParams):
+    sp = ddd_self_params()
+    sp.coreRad = dlnParams.coreRad
+    sp.coreEnergy = dlnParams.coreEnergy
+    sp.nu = matParams.ν
+    return sp
 
 
 def consts_of(dlnParams, matParams):
@@ -311,6 +335,74 @@ class Context:
         self._check(rc)
         self.last_report = rep.as_dict()
         return out
+
+    def _netp(self, network):
+        coord, bvec, seg, ext = self._net(network)
+        return [coord.ctypes.data_as(_dp), coord.shape[1], bvec.ctypes.data_as(_dp), bvec.shape[1],
+                seg.ctypes.data_as(_ip), seg.shape[0], ext.ctypes.data_as(_up), network.numSeg]
+
+    @staticmethod
+    def _segforce(network):
+        sf = network.segForce
+        if not (sf.flags.f_contiguous and sf.dtype == np.float64 and sf.shape[:2] == (3, 2)):
+            raise ValueError("segForce must be a Fortran-ordered float64 3×2×n array")
+        return sf
+
+    @staticmethod
+    def _sigma_hat(sigma_hat, n):
+        if sigma_hat is None:
+            return None
+        sh = np.require(sigma_hat, np.float64, ["F"])
+        if sh.shape != (6, n):
+            raise ValueError("sigmaHat must be 6×n (xx, yy, zz, xy, xz, yz per entry)")
+        return sh
+
+    def self_force(self, k, sp, network, idx=None):
+        """calcSelfForce: (F1, F2), each 3×n."""
+        idx = self._idx(idx)
+        n = network.numSeg if idx is None else len(idx)
+        F1 = np.zeros((3, n), np.float64, order="F")
+        F2 = np.zeros((3, n), np.float64, order="F")
+        self._check(self._L.ddd_self_force(self._h, ctypes.byref(k), ctypes.byref(sp), *self._netp(network),
+                                           None if idx is None else idx.ctypes.data_as(_ip),
+                                           0 if idx is None else len(idx), F1.ctypes.data_as(_dp),
+                                           F2.ctypes.data_as(_dp)))
+        return F1, F2
+
+    def self_force_inplace(self, k, sp, network, idx=None):
+        idx = self._idx(idx)
+        sf = self._segforce(network)
+        self._check(self._L.ddd_self_force_inplace(self._h, ctypes.byref(k), ctypes.byref(sp), *self._netp(network),
+                                                   None if idx is None else idx.ctypes.data_as(_ip),
+                                                   0 if idx is None else len(idx), sf.ctypes.data_as(_dp),
+                                                   sf.shape[2]))
+
+    def seg_force(self, k, sp, network, sigma_hat=None, idx=None):
+        """calcSegForce: seg-seg + self + PK/2 per node (3×2×n)."""
+        idx = self._idx(idx)
+        n = network.numSeg if idx is None else len(idx)
+        sh = self._sigma_hat(sigma_hat, n)
+        out = np.zeros((3, 2, n), np.float64, order="F")
+        rep = ddd_report()
+        self._check(self._L.ddd_seg_force(self._h, ctypes.byref(k), ctypes.byref(sp), *self._netp(network),
+                                          None if sh is None else sh.ctypes.data_as(_dp),
+                                          None if idx is None else idx.ctypes.data_as(_ip),
+                                          0 if idx is None else len(idx), out.ctypes.data_as(_dp), ctypes.byref(rep)))
+        self.last_report = rep.as_dict()
+        return out
+
+    def seg_force_inplace(self, k, sp, network, sigma_hat=None, idx=None):
+        idx = self._idx(idx)
+        n = network.numSeg if idx is None else len(idx)
+        sh = self._sigma_hat(sigma_hat, n)
+        sf = self._segforce(network)
+        rep = ddd_report()
+        self._check(self._L.ddd_seg_force_inplace(self._h, ctypes.byref(k), ctypes.byref(sp), *self._netp(network),
+                                                  None if sh is None else sh.ctypes.data_as(_dp),
+                                                  None if idx is None else idx.ctypes.data_as(_ip),
+                                                  0 if idx is None else len(idx), sf.ctypes.data_as(_dp),
+                                                  sf.shape[2], ctypes.byref(rep)))
+        self.last_report = rep.as_dict()
 
     def segseg_force_inplace(self, k, network, idx=None):
         coord, bvec, seg, ext = self._net(network)
@@ -672,6 +764,36 @@ def calcSegSegForce(dlnParams, matParams, network, idx=None):
 def calcSegSegForce_inplace(dlnParams, matParams, network, idx=None):
     """calcSegSegForce! (DislocationForces.jl:576-669): adds into network.segForce."""
     get_context().segseg_force_inplace(consts_of(dlnParams, matParams), network, idx)
+    return None
+
+
+def calcSelfForce(dlnParams, matParams, network, idx=None):
+    """calcSelfForce (DislocationForces.jl:320-353): (selfForceNode1, selfForceNode2), each 3×n."""
+    return get_context().self_force(consts_of(dlnParams, matParams), self_params_of(dlnParams, matParams), network,
+                                    idx)
+
+
+def calcSelfForce_inplace(dlnParams, matParams, network, idx=None):
+    """calcSelfForce! (DislocationForces.jl:354-387): node 1 -= s, node 2 += s in network.segForce."""
+    get_context().self_force_inplace(consts_of(dlnParams, matParams), self_params_of(dlnParams, matParams), network,
+                                     idx)
+    return None
+
+
+def calcSegForce(dlnParams, matParams, sigmaHat, network, idx=None):
+    """calcSegForce (DislocationForces.jl:23-46) with the finite-element part given
+    as data: sigmaHat (6×n: xx, yy, zz, xy, xz, yz) is calc_σHat(mesh,
+    forceDisplacement, x0) at each segment's midpoint (None: no PK term).  Returns
+    3×2×n: seg-seg + self + PK/2 per node."""
+    return get_context().seg_force(consts_of(dlnParams, matParams), self_params_of(dlnParams, matParams), network,
+                                   sigmaHat, idx)
+
+
+def calcSegForce_inplace(dlnParams, matParams, sigmaHat, network, idx=None):
+    """calcSegForce! (DislocationForces.jl:48-72): zeroes the entries' columns of
+    network.segForce, then adds PK/2, the self force and the seg-seg force."""
+    get_context().seg_force_inplace(consts_of(dlnParams, matParams), self_params_of(dlnParams, matParams), network,
+                                    sigmaHat, idx)
     return None
 
 

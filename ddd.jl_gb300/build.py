@@ -27,6 +27,7 @@ VARIANTS = {
     "segseg_batch.cu": [("", ["--fmad=false"])],
     "surrogate_data.cu": [("", ["--fmad=false"])],
     "surrogate_force.cu": [("", ["--fmad=false"])],
+    "self_force.cu": [("", ["--fmad=false"])],
 }
 
 

@@ -331,17 +331,14 @@ int ddd_segseg_force(ddd_ctx* ctx, const ddd_consts* k, const double* coord, int
   return DDD_OK;
 }
 
-int ddd_segseg_force_inplace(ddd_ctx* ctx, const ddd_consts* k, const double* coord, int64_t coordCols,
-                             const double* bVec, int64_t bVecCols, const int64_t* segIdx, int64_t ldSegIdx,
-                             const uint8_t* extSeg, int64_t numSeg, const int64_t* idx, int64_t nIdx,
-                             double* segForce, int64_t segForceCols, ddd_report* rep) {
-  if (!ctx) return DDD_EINVAL;
-  std::lock_guard<std::mutex> g(ctx->mu);
-  if (segForceCols < numSeg) return fail(ctx, DDD_EINVAL, "segForce has fewer columns than numSeg");
-  const int64_t nOut = idx ? nIdx : numSeg;
-  if (nOut > 0 && !segForce) return fail(ctx, DDD_EINVAL, "segForce is NULL");
-  int rc = segseg_compute(ctx, k, coord, coordCols, bVec, bVecCols, segIdx, ldSegIdx, extSeg, numSeg, idx, nIdx, rep);
-  if (rc) return rc;
+}  // extern "C"
+
+namespace {
+
+// Adds the seg-seg result in ctx->hostTmp into segForce the way
+// calcSegSegForce! does.
+void add_segseg_inplace(ddd_ctx* ctx, const uint8_t* extSeg, int64_t numSeg, const int64_t* idx, int64_t nIdx,
+                        double* segForce) {
   const double* F = ctx->hostTmp.data();
   if (!idx) {
     for (int64_t q = 0; q < 6 * numSeg; ++q) segForce[q] += F[q];
@@ -354,6 +351,209 @@ int ddd_segseg_force_inplace(ddd_ctx* ctx, const ddd_consts* k, const double* co
       for (int c = 0; c < 6; ++c) segForce[6 * i + c] += F[6 * q + c];
     }
   }
+}
+
+// Self force on node 2 (S) and, with sigmaHat, the PK force of each entry of
+// idx (or of every segment), on the GPU (self_force.cu), into S and PK (3 × n
+// each; PK left empty without sigmaHat).
+int self_pk_compute(ddd_ctx* ctx, const ddd_consts* k, const ddd_self_params* sp, const double* coord,
+                    int64_t coordCols, const double* bVec, int64_t bVecCols, const int64_t* segIdx, int64_t ld,
+                    const uint8_t* extSeg, int64_t numSeg, const int64_t* idx, int64_t nIdx, const double* sigmaHat,
+                    std::vector<double>& S, std::vector<double>& PK) {
+  ddd::KConsts K;
+  int rc = check_consts(ctx, k, K);
+  if (rc) return rc;
+  if (!sp) return fail(ctx, DDD_EINVAL, "self-force parameters are NULL");
+  if (!std::isfinite(sp->coreRad) || !std::isfinite(sp->coreEnergy) || !std::isfinite(sp->nu))
+    return fail(ctx, DDD_ENONFINITE, "non-finite self-force parameter");
+  if (!(sp->coreRad > 0.0) || !(sp->nu < 1.0)) return fail(ctx, DDD_EINVAL, "coreRad must be > 0 and nu < 1");
+  rc = check_network(ctx, coord, coordCols, bVec, bVecCols, segIdx, ld, numSeg);
+  if (rc) return rc;
+  if (idx) {
+    if (nIdx < 0) return fail(ctx, DDD_EINVAL, "nIdx < 0");
+    for (int64_t q = 0; q < nIdx; ++q)
+      if (idx[q] < 1 || idx[q] > numSeg) {
+        char buf[96];
+        snprintf(buf, sizeof buf, "idx[%lld] = %lld outside 1..numSeg=%lld", (long long)q, (long long)idx[q],
+                 (long long)numSeg);
+        return fail(ctx, DDD_ERANGE, buf);
+      }
+  }
+  const int64_t n = idx ? nIdx : numSeg;
+  S.assign((size_t)n * 3, 0.0);
+  PK.assign(sigmaHat ? (size_t)n * 3 : 0, 0.0);
+  if (n == 0) return DDD_OK;
+  if (sigmaHat)
+    for (int64_t q = 0; q < 6 * n; ++q)
+      if (!std::isfinite(sigmaHat[q])) return fail(ctx, DDD_ENONFINITE, "non-finite sigmaHat");
+  ddd::SelfK SK;
+  SK.a = sp->coreRad;
+  SK.aSq = k->aSq;                    // dlnParams.coreRadSq
+  SK.mu4pi = k->mu4pi;
+  SK.omNuInv = 1.0 / (1.0 - sp->nu);  // MaterialConstructor.jl:20
+  SK.nuOmNuInv = sp->nu * SK.omNuInv;  // MaterialConstructor.jl:22
+  SK.Ec = sp->coreEnergy;
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  int64_t npad = 0, h2d = 0;
+  rc = upload_network(ctx, coord, coordCols, bVec, bVecCols, segIdx, ld, extSeg, numSeg, npad, h2d);
+  if (rc) return rc;
+  if (idx) {
+    std::vector<int64_t> rows0((size_t)n);
+    for (int64_t q = 0; q < n; ++q) rows0[q] = idx[q] - 1;
+    CK(ctx->rows.ensure((size_t)n * sizeof(int64_t)), "alloc rows");
+    CK(cudaMemcpyAsync(ctx->rows.p, rows0.data(), (size_t)n * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream),
+       "copy idx");
+  }
+  if (sigmaHat) {
+    CK(ctx->sigma.ensure((size_t)n * 6 * sizeof(double)), "alloc sigmaHat");
+    CK(cudaMemcpyAsync(ctx->sigma.p, sigmaHat, (size_t)n * 6 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream),
+       "copy sigmaHat");
+  }
+  CK(ctx->out.ensure((size_t)n * 6 * sizeof(double)), "alloc output");
+  double* dS = ctx->out.as<double>();
+  CK(ddd::launch_self_pk(SK, ctx->coord.as<double>(), ctx->bvec.as<double>(), ctx->segidx.as<int64_t>(), ld,
+                         extSeg ? ctx->ext.as<uint8_t>() : nullptr, numSeg, idx ? ctx->rows.as<int64_t>() : nullptr,
+                         n, sigmaHat ? ctx->sigma.as<double>() : nullptr, dS, sigmaHat ? dS + 3 * n : nullptr,
+                         ctx->stream),
+     "self_pk_f64");
+  CK(cudaMemcpyAsync(S.data(), dS, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "copy S");
+  if (sigmaHat)
+    CK(cudaMemcpyAsync(PK.data(), dS + 3 * n, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
+       "copy PK");
+  CK(cudaStreamSynchronize(ctx->stream), "self force");
+  return DDD_OK;
+}
+
+// The reference skips entry q of its index list when extSeg[q] is set (the
+// position, DislocationForces.jl:338,376); positions past numSeg hold no
+// segment flag here and are treated as internal.
+inline bool ext_at(const uint8_t* extSeg, int64_t numSeg, int64_t q) { return extSeg && q < numSeg && extSeg[q]; }
+
+}  // namespace
+
+extern "C" {
+
+int ddd_self_force(ddd_ctx* ctx, const ddd_consts* k, const ddd_self_params* sp, const double* coord,
+                   int64_t coordCols, const double* bVec, int64_t bVecCols, const int64_t* segIdx, int64_t ldSegIdx,
+                   const uint8_t* extSeg, int64_t numSeg, const int64_t* idx, int64_t nIdx, double* F1, double* F2) {
+  if (!ctx) return DDD_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  const int64_t n = idx ? nIdx : numSeg;
+  if (n > 0 && (!F1 || !F2)) return fail(ctx, DDD_EINVAL, "F1 or F2 is NULL");
+  std::vector<double> S, PK;
+  int rc = self_pk_compute(ctx, k, sp, coord, coordCols, bVec, bVecCols, segIdx, ldSegIdx, extSeg, numSeg, idx, nIdx,
+                           nullptr, S, PK);
+  if (rc) return rc;
+  for (int64_t q = 0; q < 3 * n; ++q) {
+    F1[q] = -S[q];  // selfForceNode1 = -selfForceNode2 (:350)
+    F2[q] = S[q];
+  }
+  return DDD_OK;
+}
+
+int ddd_self_force_inplace(ddd_ctx* ctx, const ddd_consts* k, const ddd_self_params* sp, const double* coord,
+                           int64_t coordCols, const double* bVec, int64_t bVecCols, const int64_t* segIdx,
+                           int64_t ldSegIdx, const uint8_t* extSeg, int64_t numSeg, const int64_t* idx, int64_t nIdx,
+                           double* segForce, int64_t segForceCols) {
+  if (!ctx) return DDD_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (segForceCols < numSeg) return fail(ctx, DDD_EINVAL, "segForce has fewer columns than numSeg");
+  const int64_t n = idx ? nIdx : numSeg;
+  if (n > 0 && !segForce) return fail(ctx, DDD_EINVAL, "segForce is NULL");
+  std::vector<double> S, PK;
+  int rc = self_pk_compute(ctx, k, sp, coord, coordCols, bVec, bVecCols, segIdx, ldSegIdx, extSeg, numSeg, idx, nIdx,
+                           nullptr, S, PK);
+  if (rc) return rc;
+  for (int64_t q = 0; q < n; ++q) {  // calcSelfForce! (:354-387)
+    if (ext_at(extSeg, numSeg, q)) continue;
+    const int64_t i = idx ? idx[q] - 1 : q;
+    for (int c = 0; c < 3; ++c) {
+      segForce[6 * i + c] -= S[3 * q + c];
+      segForce[6 * i + 3 + c] += S[3 * q + c];
+    }
+  }
+  return DDD_OK;
+}
+
+int ddd_seg_force(ddd_ctx* ctx, const ddd_consts* k, const ddd_self_params* sp, const double* coord,
+                  int64_t coordCols, const double* bVec, int64_t bVecCols, const int64_t* segIdx, int64_t ldSegIdx,
+                  const uint8_t* extSeg, int64_t numSeg, const double* sigmaHat, const int64_t* idx, int64_t nIdx,
+                  double* force, ddd_report* rep) {
+  if (!ctx) return DDD_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  const int64_t n = idx ? nIdx : numSeg;
+  if (n > 0 && !force) return fail(ctx, DDD_EINVAL, "force is NULL");
+  std::vector<double> S, PK;
+  int rc = self_pk_compute(ctx, k, sp, coord, coordCols, bVec, bVecCols, segIdx, ldSegIdx, extSeg, numSeg, idx, nIdx,
+                           sigmaHat, S, PK);
+  if (rc) return rc;
+  rc = segseg_compute(ctx, k, coord, coordCols, bVec, bVecCols, segIdx, ldSegIdx, extSeg, numSeg, idx, nIdx, rep);
+  if (rc) return rc;
+  // calcSegForce (:23-46): segForce[k, j, i] += selfForce[j][k, i] + 0.5 * PKForce[k, i].
+  const double* F = ctx->hostTmp.data();
+  for (int64_t q = 0; q < n; ++q)
+    for (int c = 0; c < 3; ++c) {
+      const double pk = sigmaHat ? PK[3 * q + c] : 0.0;
+      force[6 * q + c] = F[6 * q + c] + (-S[3 * q + c] + 0.5 * pk);
+      force[6 * q + 3 + c] = F[6 * q + 3 + c] + (S[3 * q + c] + 0.5 * pk);
+    }
+  return DDD_OK;
+}
+
+int ddd_seg_force_inplace(ddd_ctx* ctx, const ddd_consts* k, const ddd_self_params* sp, const double* coord,
+                          int64_t coordCols, const double* bVec, int64_t bVecCols, const int64_t* segIdx,
+                          int64_t ldSegIdx, const uint8_t* extSeg, int64_t numSeg, const double* sigmaHat,
+                          const int64_t* idx, int64_t nIdx, double* segForce, int64_t segForceCols, ddd_report* rep) {
+  if (!ctx) return DDD_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (segForceCols < numSeg) return fail(ctx, DDD_EINVAL, "segForce has fewer columns than numSeg");
+  const int64_t n = idx ? nIdx : numSeg;
+  if (n > 0 && !segForce) return fail(ctx, DDD_EINVAL, "segForce is NULL");
+  std::vector<double> S, PK;
+  int rc = self_pk_compute(ctx, k, sp, coord, coordCols, bVec, bVecCols, segIdx, ldSegIdx, extSeg, numSeg, idx, nIdx,
+                           sigmaHat, S, PK);
+  if (rc) return rc;
+  rc = segseg_compute(ctx, k, coord, coordCols, bVec, bVecCols, segIdx, ldSegIdx, extSeg, numSeg, idx, nIdx, rep);
+  if (rc) return rc;
+  // calcSegForce! (:48-72): zero the range, then calcPKForce!, calcSelfForce!,
+  // calcSegSegForce!, each adding in turn.
+  for (int64_t q = 0; q < n; ++q) {
+    const int64_t i = idx ? idx[q] - 1 : q;
+    for (int c = 0; c < 6; ++c) segForce[6 * i + c] = 0.0;
+  }
+  if (sigmaHat)
+    for (int64_t q = 0; q < n; ++q) {  // calcPKForce! (:244-272)
+      if (ext_at(extSeg, numSeg, q)) continue;
+      const int64_t i = idx ? idx[q] - 1 : q;
+      for (int c = 0; c < 3; ++c) {
+        segForce[6 * i + c] += PK[3 * q + c] / 2;
+        segForce[6 * i + 3 + c] += PK[3 * q + c] / 2;
+      }
+    }
+  for (int64_t q = 0; q < n; ++q) {  // calcSelfForce! (:354-387)
+    if (ext_at(extSeg, numSeg, q)) continue;
+    const int64_t i = idx ? idx[q] - 1 : q;
+    for (int c = 0; c < 3; ++c) {
+      segForce[6 * i + c] -= S[3 * q + c];
+      segForce[6 * i + 3 + c] += S[3 * q + c];
+    }
+  }
+  add_segseg_inplace(ctx, extSeg, numSeg, idx, nIdx, segForce);
+  return DDD_OK;
+}
+
+int ddd_segseg_force_inplace(ddd_ctx* ctx, const ddd_consts* k, const double* coord, int64_t coordCols,
+                             const double* bVec, int64_t bVecCols, const int64_t* segIdx, int64_t ldSegIdx,
+                             const uint8_t* extSeg, int64_t numSeg, const int64_t* idx, int64_t nIdx,
+                             double* segForce, int64_t segForceCols, ddd_report* rep) {
+  if (!ctx) return DDD_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (segForceCols < numSeg) return fail(ctx, DDD_EINVAL, "segForce has fewer columns than numSeg");
+  const int64_t nOut = idx ? nIdx : numSeg;
+  if (nOut > 0 && !segForce) return fail(ctx, DDD_EINVAL, "segForce is NULL");
+  int rc = segseg_compute(ctx, k, coord, coordCols, bVec, bVecCols, segIdx, ldSegIdx, extSeg, numSeg, idx, nIdx, rep);
+  if (rc) return rc;
+  add_segseg_inplace(ctx, extSeg, numSeg, idx, nIdx, segForce);
   return DDD_OK;
 }
 

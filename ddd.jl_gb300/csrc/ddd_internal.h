@@ -68,6 +68,14 @@ cudaError_t launch_tc_gemm_f16(int M, int N, int K, const void* A, const void* B
 cudaError_t launch_pair_data(const KConsts& K, const double* soa, int64_t npad, const int32_t* pairs, int64_t P,
                              void* X, float* Bp, float* T, double* F, cudaStream_t st);
 
+// self_force.cu: per-segment self force (node 2) and PK force, strict FP64.
+struct SelfK {
+  double a, aSq, mu4pi, nuOmNuInv, omNuInv, Ec;
+};
+cudaError_t launch_self_pk(const SelfK& K, const double* coord, const double* bVec, const int64_t* segIdx, int64_t ld,
+                           const uint8_t* ext, int64_t nExt, const int64_t* rows, int64_t n, const double* sigmaHat,
+                           double* S, double* PK, cudaStream_t st);
+
 // ddd_api.cu: context accessors for the other C-ABI files.
 int ctx_device(const ddd_ctx* c);
 

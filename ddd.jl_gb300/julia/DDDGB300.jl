@@ -12,6 +12,7 @@
 module DDDGB300
 
 export calcSegSegForceGPU, calcSegSegForceGPU!, calc_σTildeGPU, calc_σTildeGPU!
+export calcSelfForceGPU, calcSelfForceGPU!, calcSegForceGPU, calcSegForceGPU!
 export Surrogate, loadSurrogate, calcSegSegForceSurrogateGPU
 
 const libddd = joinpath(@__DIR__, "..", "libddd_gb300.so")
@@ -112,6 +113,94 @@ function calc_σTildeGPU(x0, dlnParams, matParams, network, idx = nothing)
     σ = zeros(6, numPoints)
     calc_σTildeGPU!(σ, xs, dlnParams, matParams, network, idx)
     return numPoints == 1 ? σ[:, 1] : σ
+end
+
+# ---------------------------------------------------------------------------
+# Self force and total segment force (DislocationForces.jl:23-72, 320-455).
+
+struct DDDSelfParams
+    coreRad::Float64
+    coreEnergy::Float64
+    nu::Float64
+end
+
+selfparams(dlnParams, matParams) = DDDSelfParams(dlnParams.coreRad, dlnParams.coreEnergy, matParams.ν)
+
+# calcSelfForce: (selfForceNode1, selfForceNode2), 3×n each
+function calcSelfForceGPU(dlnParams, matParams, network, idx = nothing)
+    numSeg = network.numSeg[1]
+    iv = idxvec(idx)
+    n = isnothing(idx) ? numSeg : length(iv)
+    F1, F2 = zeros(3, n), zeros(3, n)
+    k, sp = Ref(consts(dlnParams, matParams)), Ref(selfparams(dlnParams, matParams))
+    coord, bVec, segIdx, extSeg = network.coord, network.bVec, network.segIdx, network.extSeg
+    GC.@preserve coord bVec segIdx extSeg iv F1 F2 begin
+        rc = ccall((:ddd_self_force, libddd), Cint,
+            (Ptr{Cvoid}, Ref{DDDConsts}, Ref{DDDSelfParams}, Ptr{Float64}, Int64, Ptr{Float64}, Int64, Ptr{Int64},
+             Int64, Ptr{Bool}, Int64, Ptr{Int64}, Int64, Ptr{Float64}, Ptr{Float64}),
+            context(), k, sp, coord, size(coord, 2), bVec, size(bVec, 2), segIdx, size(segIdx, 1), extSeg, numSeg,
+            isnothing(idx) ? C_NULL : pointer(iv), length(iv), F1, F2)
+    end
+    check(rc)
+    return F1, F2
+end
+
+# calcSelfForce!
+function calcSelfForceGPU!(dlnParams, matParams, network, idx = nothing)
+    numSeg = network.numSeg[1]
+    iv = idxvec(idx)
+    k, sp = Ref(consts(dlnParams, matParams)), Ref(selfparams(dlnParams, matParams))
+    coord, bVec, segIdx, extSeg, segForce = network.coord, network.bVec, network.segIdx, network.extSeg, network.segForce
+    GC.@preserve coord bVec segIdx extSeg segForce iv begin
+        rc = ccall((:ddd_self_force_inplace, libddd), Cint,
+            (Ptr{Cvoid}, Ref{DDDConsts}, Ref{DDDSelfParams}, Ptr{Float64}, Int64, Ptr{Float64}, Int64, Ptr{Int64},
+             Int64, Ptr{Bool}, Int64, Ptr{Int64}, Int64, Ptr{Float64}, Int64),
+            context(), k, sp, coord, size(coord, 2), bVec, size(bVec, 2), segIdx, size(segIdx, 1), extSeg, numSeg,
+            isnothing(idx) ? C_NULL : pointer(iv), length(iv), segForce, size(segForce, 3))
+    end
+    check(rc)
+    return nothing
+end
+
+# calcSegForce with the FE stress at the segment midpoints given as data:
+# σHat (6×n: xx, yy, zz, xy, xz, yz) = calc_σHat(mesh, forceDisplacement, midpoint)
+# for each entry, or `nothing` for no PK term.
+function calcSegForceGPU(dlnParams, matParams, σHat, network, idx = nothing)
+    numSeg = network.numSeg[1]
+    iv = idxvec(idx)
+    n = isnothing(idx) ? numSeg : length(iv)
+    out = zeros(3, 2, n)
+    sh = isnothing(σHat) ? Float64[] : convert(Array{Float64}, σHat)
+    k, sp = Ref(consts(dlnParams, matParams)), Ref(selfparams(dlnParams, matParams))
+    coord, bVec, segIdx, extSeg = network.coord, network.bVec, network.segIdx, network.extSeg
+    GC.@preserve coord bVec segIdx extSeg iv out sh begin
+        rc = ccall((:ddd_seg_force, libddd), Cint,
+            (Ptr{Cvoid}, Ref{DDDConsts}, Ref{DDDSelfParams}, Ptr{Float64}, Int64, Ptr{Float64}, Int64, Ptr{Int64},
+             Int64, Ptr{Bool}, Int64, Ptr{Float64}, Ptr{Int64}, Int64, Ptr{Float64}, Ptr{Cvoid}),
+            context(), k, sp, coord, size(coord, 2), bVec, size(bVec, 2), segIdx, size(segIdx, 1), extSeg, numSeg,
+            isnothing(σHat) ? C_NULL : pointer(sh), isnothing(idx) ? C_NULL : pointer(iv), length(iv), out, C_NULL)
+    end
+    check(rc)
+    return out
+end
+
+# calcSegForce!
+function calcSegForceGPU!(dlnParams, matParams, σHat, network, idx = nothing)
+    numSeg = network.numSeg[1]
+    iv = idxvec(idx)
+    sh = isnothing(σHat) ? Float64[] : convert(Array{Float64}, σHat)
+    k, sp = Ref(consts(dlnParams, matParams)), Ref(selfparams(dlnParams, matParams))
+    coord, bVec, segIdx, extSeg, segForce = network.coord, network.bVec, network.segIdx, network.extSeg, network.segForce
+    GC.@preserve coord bVec segIdx extSeg segForce iv sh begin
+        rc = ccall((:ddd_seg_force_inplace, libddd), Cint,
+            (Ptr{Cvoid}, Ref{DDDConsts}, Ref{DDDSelfParams}, Ptr{Float64}, Int64, Ptr{Float64}, Int64, Ptr{Int64},
+             Int64, Ptr{Bool}, Int64, Ptr{Float64}, Ptr{Int64}, Int64, Ptr{Float64}, Int64, Ptr{Cvoid}),
+            context(), k, sp, coord, size(coord, 2), bVec, size(bVec, 2), segIdx, size(segIdx, 1), extSeg, numSeg,
+            isnothing(σHat) ? C_NULL : pointer(sh), isnothing(idx) ? C_NULL : pointer(iv), length(iv), segForce,
+            size(segForce, 3), C_NULL)
+    end
+    check(rc)
+    return nothing
 end
 
 # ---------------------------------------------------------------------------

@@ -122,6 +122,50 @@ int ddd_segseg_force_inplace(ddd_ctx* ctx, const ddd_consts* k, const double* co
                              const uint8_t* extSeg, int64_t numSeg, const int64_t* idx, int64_t nIdx,
                              double* segForce, int64_t segForceCols, ddd_report* rep);
 
+/* Self force and total segment force (the next row of the hot path's callers).
+ * Parameters beyond ddd_consts: dlnParams.coreRad, dlnParams.coreEnergy and
+ * matParams.ν (omνInv = 1/(1-ν), νomνInv = ν·omνInv as MaterialConstructor.jl:20-22
+ * derives them); ddd_consts supplies coreRadSq (aSq) and μ4π. */
+typedef struct ddd_self_params {
+  double coreRad;
+  double coreEnergy;
+  double nu;
+} ddd_self_params;
+
+/* calcSelfForce(dlnParams, matParams, network, idx = nothing)
+ *   src/Processing/DislocationForces.jl:320-353, kernel _calcSelfForce :414-455.
+ * For each entry k of idx (1-based rows of segIdx) or of 1:numSeg: F1[:, k] =
+ * the force on node 1, F2[:, k] = on node 2 (3 × n each, F1 = -F2).  As in the
+ * reference, entry k is skipped (zeros) when extSeg[k] is set: the flag at the
+ * position in idx, not at the segment (positions past numSeg count as internal). */
+int ddd_self_force(ddd_ctx* ctx, const ddd_consts* k, const ddd_self_params* sp, const double* coord,
+                   int64_t coordCols, const double* bVec, int64_t bVecCols, const int64_t* segIdx, int64_t ldSegIdx,
+                   const uint8_t* extSeg, int64_t numSeg, const int64_t* idx, int64_t nIdx, double* F1, double* F2);
+
+/* calcSelfForce!(…) — :354-387: segForce[:, 1, idx[k]] -= s, segForce[:, 2, idx[k]] += s. */
+int ddd_self_force_inplace(ddd_ctx* ctx, const ddd_consts* k, const ddd_self_params* sp, const double* coord,
+                           int64_t coordCols, const double* bVec, int64_t bVecCols, const int64_t* segIdx,
+                           int64_t ldSegIdx, const uint8_t* extSeg, int64_t numSeg, const int64_t* idx, int64_t nIdx,
+                           double* segForce, int64_t segForceCols);
+
+/* calcSegForce(dlnParams, matParams, mesh, forceDisplacement, network, idx)
+ *   :23-46 — seg-seg + self + 0.5 PK per node, 3 × 2 × n fresh.  The PK force
+ *   (σ̂ b) × t (:292-300) is computed here from sigmaHat (6 × n: xx, yy, zz, xy,
+ *   xz, yz), the finite-element stress at each entry's segment midpoint that
+ *   the caller evaluates with calc_σHat(mesh, forceDisplacement, x0) — the FE
+ *   mesh is not part of this library; NULL = no PK term.
+ * ddd_seg_force_inplace: calcSegForce! :48-72 — the columns of the entries
+ *   are zeroed, then PK/2 (both nodes), the self force and the seg-seg force
+ *   are added in the reference's order. */
+int ddd_seg_force(ddd_ctx* ctx, const ddd_consts* k, const ddd_self_params* sp, const double* coord,
+                  int64_t coordCols, const double* bVec, int64_t bVecCols, const int64_t* segIdx, int64_t ldSegIdx,
+                  const uint8_t* extSeg, int64_t numSeg, const double* sigmaHat, const int64_t* idx, int64_t nIdx,
+                  double* force, ddd_report* rep);
+int ddd_seg_force_inplace(ddd_ctx* ctx, const ddd_consts* k, const ddd_self_params* sp, const double* coord,
+                          int64_t coordCols, const double* bVec, int64_t bVecCols, const int64_t* segIdx,
+                          int64_t ldSegIdx, const uint8_t* extSeg, int64_t numSeg, const double* sigmaHat,
+                          const int64_t* idx, int64_t nIdx, double* segForce, int64_t segForceCols, ddd_report* rep);
+
 /* calc_σTilde(x0, dlnParams, matParams, network, idx = nothing) and
  * calc_σTilde!(σ, x0, ...) — src/Processing/DislocationFEM.jl:24-84, kernel
  * _calc_σTilde! :86-303.  Both write sigma (6 × numPoints) fresh.  Segments are

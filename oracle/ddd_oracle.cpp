@@ -251,6 +251,56 @@ void oracle_segseg_idx(const double* k5, const double* coord, const double* bVec
 }
 
 // _calc_σTilde! (DislocationFEM.jl:86-303) for an array of points x0 (3×M).
+// calcSelfForce (DislocationForces.jl:320-353): for each k (idx[k], 1-based
+// rows of segIdx, or 1:numSeg when idx is NULL) the node forces F1 = -s,
+// F2 = s (3 × n each, overwritten).  As in the reference, the external flag
+// read for entry k is extSeg[k] (the position in idx, not the segment).
+// sc = (coreRad, coreEnergy, ν) and k5[1] = μ4π.
+void oracle_self_force(const double* k5, const double* sc, const double* coord, const double* bVec,
+                       const int64_t* segIdx, int64_t ld, const uint8_t* extSeg, int64_t numSeg, const int64_t* idx,
+                       int64_t nIdx, double* F1, double* F2) {
+  SelfConsts<double> K;
+  K.a = sc[0];
+  K.aSq = sc[0] * sc[0];  // DislocationConstructor.jl:83
+  K.mu4pi = k5[1];
+  K.omNuInv = 1.0 / (1.0 - sc[2]);  // MaterialConstructor.jl
+  K.nuOmNuInv = sc[2] * K.omNuInv;
+  K.Ec = sc[1];
+  const int64_t n = idx ? nIdx : numSeg;
+  for (int64_t q = 0; q < n; ++q) {
+    for (int c = 0; c < 3; ++c) F1[3 * q + c] = F2[3 * q + c] = 0.0;
+    if (extSeg[q]) continue;
+    const int64_t i = idx ? idx[q] - 1 : q;
+    const V3<double> n1 = col3(coord, segIdx[i + ld]), n2 = col3(coord, segIdx[i + 2 * ld]);
+    const V3<double> s = self_force_node2(K, n2 - n1, col3(bVec, segIdx[i]));
+    F1[3 * q] = -s.x;
+    F1[3 * q + 1] = -s.y;
+    F1[3 * q + 2] = -s.z;
+    F2[3 * q] = s.x;
+    F2[3 * q + 1] = s.y;
+    F2[3 * q + 2] = s.z;
+  }
+}
+
+// PK forces (σ̂ b) × (n2 - n1) of the segments in idx (or 1:numSeg) from the
+// stresses sigmaHat (6 × n, one per entry, at the segment midpoints): PK
+// (3 × n, overwritten; 0 where extSeg[k]).
+void oracle_pk_force(const double* coord, const double* bVec, const int64_t* segIdx, int64_t ld,
+                     const uint8_t* extSeg, int64_t numSeg, const int64_t* idx, int64_t nIdx, const double* sigmaHat,
+                     double* PK) {
+  const int64_t n = idx ? nIdx : numSeg;
+  for (int64_t q = 0; q < n; ++q) {
+    for (int c = 0; c < 3; ++c) PK[3 * q + c] = 0.0;
+    if (extSeg[q]) continue;
+    const int64_t i = idx ? idx[q] - 1 : q;
+    const V3<double> t = col3(coord, segIdx[i + 2 * ld]) - col3(coord, segIdx[i + ld]);
+    const V3<double> f = pk_force(sigmaHat + 6 * q, col3(bVec, segIdx[i]), t);
+    PK[3 * q] = f.x;
+    PK[3 * q + 1] = f.y;
+    PK[3 * q + 2] = f.z;
+  }
+}
+
 // idx (1-based rows of segIdx) selects segments, NULL = 1:numSeg.  Overwrites
 // sigma (6×M).  The reference loops segments outside and points inside; each
 // point's sum is taken over segments in order either way, so the threaded

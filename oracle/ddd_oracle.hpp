@@ -641,6 +641,46 @@ void par_seg_seg_force(const Consts<T>& K, V3<T> b1, V3<T> n11, V3<T> n12, V3<T>
 }
 
 // ---------------------------------------------------------------------------
+// Self force of one segment — _calcSelfForce (DislocationForces.jl:414-455):
+// the force on node 2 (node 1 gets its negative).  tVec = n2 - n1 (not
+// normalised), b the Burgers vector.  Constants: a = coreRad, aSq = coreRad²,
+// μ4π, νomνInv = ν/(1-ν), omνInv = 1/(1-ν) (MaterialConstructor.jl:73-82),
+// Ec = coreEnergy.
+template <class T> struct SelfConsts {
+  T a, aSq, mu4pi, nuOmNuInv, omNuInv, Ec;
+};
+
+template <class T>
+inline V3<T> self_force_node2(const SelfConsts<T>& K, const V3<T>& tVec, const V3<T>& b) {
+  using std::log;
+  using std::sqrt;
+  const T tVecSq = dot(tVec, tVec);
+  const T L = sqrt(tVecSq);
+  const T Linv = T(1) / L;
+  const V3<T> t = tVec * Linv;  // tVecI *= Linv
+  const T La = sqrt(tVecSq + K.aSq);
+  const T bScrew = dot(t, b);
+  const V3<T> bEdge = b - bScrew * t;
+  const T bEdgeSq = dot(bEdge, bEdge);
+  const T LaMa = La - K.a;
+  const T tor = K.mu4pi * bScrew *
+                (K.nuOmNuInv * (log((La + L) / K.a) - T(2) * LaMa * Linv) - LaMa * LaMa / (T(2) * La * L));
+  const T torCore = T(2) * K.Ec * K.nuOmNuInv * bScrew;
+  const T torTot = tor + torCore;
+  const T lonCore = (bScrew * bScrew + bEdgeSq * K.omNuInv) * K.Ec;
+  return torTot * bEdge - lonCore * t;
+}
+
+// PK force of one segment — _calcPKForce (DislocationForces.jl:292-300) for a
+// given stress at the midpoint: (σ̂ b) × t, t = n2 - n1 (not normalised),
+// sig = (xx, yy, zz, xy, xz, yz).
+template <class T> inline V3<T> pk_force(const T* sig, const V3<T>& b, const V3<T>& t) {
+  const V3<T> sb = {sig[0] * b.x + sig[3] * b.y + sig[4] * b.z, sig[3] * b.x + sig[1] * b.y + sig[5] * b.z,
+                    sig[4] * b.x + sig[5] * b.y + sig[2] * b.z};
+  return cross(sb, t);
+}
+
+// ---------------------------------------------------------------------------
 // Field-point stress of one segment at one point — body of the point loop of
 // _calc_σTilde! (DislocationFEM.jl:135-299).  Adds to sig[0..5] in the order
 // (xx, yy, zz, xy, xz, yz).  t is normalize(n2 - n1) computed once per segment

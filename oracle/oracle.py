@@ -47,6 +47,10 @@ def lib():
                                                ctypes.c_int]
         L.oracle_segseg_par_private.argtypes = [_dp, _dp, _dp, _ip, ctypes.c_int64, _up, ctypes.c_int64, _dp,
                                                 ctypes.c_int]
+        L.oracle_self_force.argtypes = [_dp, _dp, _dp, _dp, _ip, ctypes.c_int64, _up, ctypes.c_int64, _ip,
+                                        ctypes.c_int64, _dp, _dp]
+        L.oracle_pk_force.argtypes = [_dp, _dp, _ip, ctypes.c_int64, _up, ctypes.c_int64, _ip, ctypes.c_int64, _dp,
+                                      _dp]
         L.oracle_segseg_rows.argtypes = [_dp, _dp, _dp, _ip, ctypes.c_int64, _up, ctypes.c_int64, _ip,
                                          ctypes.c_int64, _dp, ctypes.c_int]
         L.oracle_segseg_idx.argtypes = [_dp, _dp, _dp, _ip, ctypes.c_int64, _up, ctypes.c_int64, _ip,
@@ -129,6 +133,32 @@ def segseg_par_private(k5, net, nthreads):
     lib().oracle_segseg_par_private(_d(np.ascontiguousarray(k5, np.float64)), _d(coord), _d(bvec), _i(seg), ld,
                                     ext.ctypes.data_as(_up), net.numSeg, _d(F), int(nthreads))
     return F
+
+
+def self_force(k5, sc, net, idx=None):
+    """calcSelfForce: (F1, F2), each 3 × n (n = numSeg or len(idx)); sc =
+    (coreRad, coreEnergy, ν)."""
+    coord, bvec, seg, ext, ld = _net_arrays(net)
+    n = net.numSeg if idx is None else len(idx)
+    F1 = np.zeros((3, n), np.float64, order="F")
+    F2 = np.zeros((3, n), np.float64, order="F")
+    ip = None if idx is None else _i(np.ascontiguousarray(idx, np.int64))
+    lib().oracle_self_force(_d(np.ascontiguousarray(k5, np.float64)), _d(np.ascontiguousarray(sc, np.float64)),
+                            _d(coord), _d(bvec), _i(seg), ld, ext.ctypes.data_as(_up), net.numSeg, ip,
+                            0 if idx is None else len(idx), _d(F1), _d(F2))
+    return F1, F2
+
+
+def pk_force(net, sigma_hat, idx=None):
+    """(σ̂ b) × (n2 - n1) per segment (3 × n) from sigma_hat (6 × n: xx, yy, zz, xy, xz, yz)."""
+    coord, bvec, seg, ext, ld = _net_arrays(net)
+    n = net.numSeg if idx is None else len(idx)
+    PK = np.zeros((3, n), np.float64, order="F")
+    sh = np.asfortranarray(sigma_hat, np.float64)
+    ip = None if idx is None else _i(np.ascontiguousarray(idx, np.int64))
+    lib().oracle_pk_force(_d(coord), _d(bvec), _i(seg), ld, ext.ctypes.data_as(_up), net.numSeg, ip,
+                          0 if idx is None else len(idx), _d(sh), _d(PK))
+    return PK
 
 
 def segseg_rows(k5, net, rows, nthreads=1):

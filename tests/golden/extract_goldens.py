@@ -6,6 +6,9 @@ matrices they assert against into JSON fixtures beside this script:
   segseg_goldens.json   test/SegmentForcesTest.jl:281-443 — three networks
                         (coincident pentagons, shifted pentagons, prismatic +
                         shear hexagons), f1 = segForce[:, 1, :]', f2 = segForce[:, 2, :]'
+  selfforce_goldens.json test/SegmentForcesTest.jl:220-267 — calcSelfForce on
+                        two prismatic pentagons (the second shifted by 10),
+                        f1 = selfForce[1]', f2 = selfForce[2]'
   sigma_goldens.json    test/DislocationFEMTest.jl:5-155 — one edge and one
                         screw segment, σ̃ at a 3×3 grid (columns 5 and 6 of the
                         golden are (yz, xz), the code's order is (xz, yz))
@@ -49,6 +52,7 @@ def main(ref):
     seg = open(os.path.join(ref, "test", "SegmentForcesTest.jl")).read()
     # The first f1/f2 pair (SegmentForcesTest.jl:244-267) holds the self-force
     # goldens; the seg-seg goldens are the next three.
+    self_f1, self_f2 = _matrices(seg, "f1")[0], _matrices(seg, "f2")[0]
     f1s = _matrices(seg, "f1")[1:]
     f2s = _matrices(seg, "f2")[1:]
     assert len(f1s) == 3 and len(f2s) == 3, (len(f1s), len(f2s))
@@ -90,6 +94,19 @@ def main(ref):
     bcc = json.load(open(os.path.join(ref, "test", "testData", "BCC.json")))
     json.dump({"params": params, "slipSystems": {"slipPlane": bcc["slipPlane"], "bVec": bcc["bVec"]},
                "cases": cases}, open(os.path.join(HERE, "segseg_goldens.json"), "w"), indent=1)
+    dpar = json.load(open(os.path.join(ref, "test", "testData", "sampleDislocationParameters.json")))
+    self_case = {
+        "name": "pentagons_shifted_10",
+        "source": "test/SegmentForcesTest.jl:220-267",
+        "loops": [{"type": "prism", "numSides": 5, "nodeSide": 1, "numLoops": 2, "segLen": 10.0,
+                   "slipSystemIdx": 4, "label": [1, 2, 1, 2, 1]}],
+        "shift": {"fromNode": 6, "by": [10.0, 10.0, 10.0]},
+        "range": [[-100.0, 100.0], [-100.0, 100.0], [-100.0, 100.0]],
+        "f1": self_f1, "f2": self_f2,
+    }
+    json.dump({"params": dict(params, coreEnergy=float(dpar["coreEnergy"])),
+               "slipSystems": {"slipPlane": bcc["slipPlane"], "bVec": bcc["bVec"]}, "cases": [self_case]},
+              open(os.path.join(HERE, "selfforce_goldens.json"), "w"), indent=1)
 
     fem = open(os.path.join(ref, "test", "DislocationFEMTest.jl")).read()
     sig = _matrices(fem, "test_σTilde")

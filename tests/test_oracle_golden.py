@@ -131,3 +131,50 @@ def test_opcount_constants(oracle, fixtures):
     assert 1000 < flops < 2000
     s = oracle.opcount_sigma(k5, a[0], a[1], a[2], a[3])
     assert s["sqrt"] == 2 and s["div"] == 3
+
+
+G_SELF = json.load(open(os.path.join(GOLDEN, "selfforce_goldens.json")))
+
+
+def _self_case(fixtures):
+    c = G_SELF["cases"][0]
+    p = G_SELF["params"]
+    net = fixtures.make_network(c["loops"], G_SELF["slipSystems"], c["range"], c["shift"])
+    k5 = fixtures.consts5(p["coreRad"], p["mu"], p["nu"])
+    return c, net, k5, np.array([p["coreRad"], p["coreEnergy"], p["nu"]])
+
+
+def test_self_force_matches_golden(oracle, fixtures):
+    """calcSelfForce (DislocationForces.jl:320-353, 414-455) against
+    test/SegmentForcesTest.jl:244-267: node 1 and node 2 forces of every segment."""
+    c, net, k5, sc = _self_case(fixtures)
+    F1, F2 = oracle.self_force(k5, sc, net)
+    _close(F1.T, np.array(c["f1"]))
+    _close(F2.T, np.array(c["f2"]))
+
+
+def test_self_force_idx_and_ext(oracle, fixtures):
+    """idx form = the selected columns of the full result (:270-278); the
+    external flag is read at the entry's position in idx, as the reference does."""
+    c, net, k5, sc = _self_case(fixtures)
+    F1, F2 = oracle.self_force(k5, sc, net)
+    idx = np.array([3, 9, 1, 3])
+    G1, G2 = oracle.self_force(k5, sc, net, idx)
+    assert np.array_equal(G1, F1[:, idx - 1]) and np.array_equal(G2, F2[:, idx - 1])
+    net.extSeg[1] = 1
+    H1, H2 = oracle.self_force(k5, sc, net, idx)
+    assert np.all(H1[:, 1] == 0) and np.all(H2[:, 1] == 0)  # entry 2 (segment 9) skipped by extSeg[2]
+    assert np.array_equal(H1[:, [0, 2, 3]], G1[:, [0, 2, 3]])
+
+
+def test_pk_force_formula(oracle, fixtures):
+    """(σ̂ b) × t for a random symmetric σ̂, against numpy."""
+    c, net, k5, sc = _self_case(fixtures)
+    rng = np.random.default_rng(3)
+    sh = rng.normal(size=(6, net.numSeg))
+    PK = oracle.pk_force(net, sh)
+    for q in range(net.numSeg):
+        S = np.array([[sh[0, q], sh[3, q], sh[4, q]], [sh[3, q], sh[1, q], sh[5, q]], [sh[4, q], sh[5, q], sh[2, q]]])
+        l, a, b = net.segIdx[q] - 1
+        t = net.coord[:, b] - net.coord[:, a]
+        assert np.allclose(PK[:, q], np.cross(S @ net.bVec[:, l], t), rtol=1e-14, atol=1e-14)
