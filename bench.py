@@ -25,6 +25,11 @@ precision_131k: the precision-form workload (131,072 segments, f32c force and
        mixed-form σ̃ on the 128^3 grid) with errors against the FP64 kernel on
        sampled segments and points.
 
+node_rows: calcSelfForce and dlnMobility (BCC) on the workload network through
+       their host-array C-ABI calls, node forces from the timed seg-seg step plus
+       the self force: e2e and kernel times, the kernel's algorithmic GB/s, the
+       single-threaded oracle's time and the largest difference from it.
+
 --impl reference: times that CPU port alone (the reference itself is Julia and
 cannot run here), same metric and workload, each step a bounded sub-network.
 
@@ -320,6 +325,66 @@ def run_precision_131k(pkg, synth, ctx, k, stream, sptr, flush):
     }
 
 
+def run_node_rows(pkg, oracle, ctx, net, dln, mat, segseg, reps=5, with_cpu=True):
+    """calcSelfForce and dlnMobility (BCC) on the workload network through the
+    host-array C-ABI calls (copies in and out included), the node forces built
+    from the timed seg-seg step plus the self force.  Beside each, the oracle
+    (single-threaded C) on the same inputs: its time and the largest difference
+    from the GPU result."""
+    k, sp = pkg.consts_of(dln, mat), pkg.self_params_of(dln, mat)
+    mp = pkg.mob_params_of(dln, mat)
+    n = net.numSeg
+
+    def best(fn):
+        fn()
+        ts, ks = [], []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            r = fn()
+            ts.append(time.perf_counter() - t0)
+            ks.append(getattr(ctx, "last_kernel_ms", 0.0))
+        return min(ts) * 1e3, min(ks), r
+
+    ms_self, k_self, (F1, F2) = best(lambda: ctx.self_force(k, sp, net))
+    net.segForce[:, :, :n] = segseg
+    net.segForce[:, 0, :n] += F1
+    net.segForce[:, 1, :n] += F2
+    ms_mob, k_mob, (Fn, Vn) = best(lambda: ctx.mobility_bcc(mp, net))
+    # Algorithmic bytes: self force reads two nodes, b and the segment row
+    # (6 + 3 doubles, 3 int64) and writes 3 doubles per segment; mobility reads
+    # per node its coordinates and connectivity row ((1 + 2 * maxConnect) int64)
+    # and per connection the link row, the far node, b and the node's force
+    # (2 int64, 9 doubles), and writes 6 doubles.
+    ld = net.connectivity.shape[0]
+    nconn = int(net.connectivity[0, :net.numNode].sum())
+    b_self = n * (9 * 8 + 3 * 8 + 3 * 8)
+    b_mob = net.numNode * (3 * 8 + ld * 8 + 6 * 8) + nconn * (2 * 8 + 9 * 8)
+    out = {"segments": n, "nodes": net.numNode, "timing": "host arrays, H2D and D2H inside, best of %d calls" % reps,
+           "self_force": {"ms_e2e": ms_self, "segments_per_s": n / (ms_self * 1e-3), "kernel_ms": k_self,
+                          "kernel_gbs": b_self / (k_self * 1e-3) / 1e9 if k_self > 0 else None,
+                          "algorithmic_bytes": b_self},
+           "mobility_bcc": {"ms_e2e": ms_mob, "nodes_per_s": net.numNode / (ms_mob * 1e-3), "kernel_ms": k_mob,
+                            "kernel_gbs": b_mob / (k_mob * 1e-3) / 1e9 if k_mob > 0 else None,
+                            "algorithmic_bytes": b_mob, "drag": dict(dln.dragCoeffs), "sigmaPN": mat.σPN}}
+    if with_cpu:
+        k5 = np.array([dln.coreRadSq, mat.μ4π, mat.μ8π, mat.μ4πν, mat.νμ4πν])
+        sc = np.array([dln.coreRad, dln.coreEnergy, mat.ν])
+        mpv = np.array([mat.σPN, *(dln.dragCoeffs[c] for c in ("edge", "screw", "climb", "line"))])
+        t0 = time.perf_counter()
+        R1, R2 = oracle.self_force(k5, sc, net)
+        cpu_self = (time.perf_counter() - t0) * 1e3
+        t0 = time.perf_counter()
+        RF, RV = oracle.mobility_bcc(mpv, net.coord, net.bVec, net.links, net.connectivity, net.segForce, net.numNode)
+        cpu_mob = (time.perf_counter() - t0) * 1e3
+        out["self_force"].update(cpu_ms=cpu_self, cpu_kind="port", cpu_cores=1,
+                                 max_rel_diff_vs_oracle=float(np.abs(np.r_[F1 - R1, F2 - R2]).max() /
+                                                              np.abs(R2).max()))
+        out["mobility_bcc"].update(cpu_ms=cpu_mob, cpu_kind="port", cpu_cores=1,
+                                   node_force_bit_equal=bool(np.array_equal(Fn, RF)),
+                                   vel_rel_diff_vs_oracle=float(np.linalg.norm(Vn - RV) / np.linalg.norm(RV)))
+    return out
+
+
 def run_reference(args, pkg, synth, oracle):
     ws, rank = _dist()
     if rank != 0:
@@ -602,6 +667,13 @@ def main():
 
     if rank != 0:
         return
+    # The node rows after the force: self force, then BCC mobility (drag
+    # coefficients of the reference's mobility test, line drag 1e-4 so the
+    # straight sides' midpoints have a regular drag).
+    dln_m = pkg.DislocationParameters(coreRad=synth.CORE_RAD, coreEnergy=1.0,
+                                      dragCoeffs=dict(edge=1.0, screw=2.0, climb=1e10, line=1e-4))
+    mat_m = pkg.MaterialParameters(mu=synth.MU, nu=synth.NU, sigmaPN=1e-4)
+    node_rows = run_node_rows(pkg, oracle, ctx, net, dln_m, mat_m, out, with_cpu=not args.no_cpu)
     achieved = flops_per_step / (statistics.mean(ms_kernel) * 1e-3)
     line = {
         "metric": "seg-seg pair interactions/s at 65k segs (FP64 plain vs FP32+surrogate) at stated error",
@@ -633,6 +705,7 @@ def main():
         "precision_131k": precision131k,
         "sigma_tilde": sigma,
         "batched": batched,
+        "node_rows": node_rows,
         "kernel_ms_per_step": statistics.mean(ms_kernel),
     }
     cs = clocks.summary()

@@ -13,6 +13,7 @@ order, array layouts and semantics:
   calcSelfForce(dlnParams, matParams, network, idx=None)          DislocationForces.jl:320-353 (and _inplace)
   calcSegForce(dlnParams, matParams, sigmaHat, network, idx=None) DislocationForces.jl:23-46 (and _inplace;
       sigmaHat = the FE stress at the segment midpoints, in place of mesh and forceDisplacement)
+  dlnMobility(dlnParams, matParams, network, idx=None)            DislocationMobility.jl:16-178, BCC (and _inplace)
 
 All computation runs on the GPU.  There is no CPU fallback: if the library is
 not built or no GPU is usable, calls raise.
@@ -33,7 +34,7 @@ NOALLOC_MAX_SEGMENTS = 4096
 
 # Every symbol include/ddd_gb300.h declares.
 EXPORTED_SYMBOLS = (
-    "ddd_create", "ddd_destroy", "ddd_last_error", "ddd_version",
+    "ddd_create", "ddd_destroy", "ddd_last_error", "ddd_last_kernel_ms", "ddd_version",
     "ddd_segseg_force", "ddd_segseg_force_inplace", "ddd_sigma_tilde",
     "ddd_segseg_force_device", "ddd_sigma_tilde_device", "ddd_set_mode", "ddd_get_mode", "ddd_probe_fma_peak",
     "ddd_segseg_force_device_noalloc",
@@ -44,6 +45,7 @@ EXPORTED_SYMBOLS = (
     "ddd_surrogate_force", "ddd_surrogate_force_host", "ddd_surrogate_last_error", "ddd_surrogate_save",
     "ddd_surrogate_load",
     "ddd_self_force", "ddd_self_force_inplace", "ddd_seg_force", "ddd_seg_force_inplace",
+    "ddd_mobility_bcc", "ddd_mobility_bcc_inplace",
 )
 
 # Arithmetic modes (ddd_set_mode).
@@ -84,6 +86,11 @@ class ddd_report(ctypes.Structure):
 
 class ddd_self_params(ctypes.Structure):
     _fields_ = [("coreRad", ctypes.c_double), ("coreEnergy", ctypes.c_double), ("nu", ctypes.c_double)]
+
+
+class ddd_mob_params(ctypes.Structure):
+    _fields_ = [("sigmaPN", ctypes.c_double), ("edgeDrag", ctypes.c_double), ("screwDrag", ctypes.c_double),
+                ("climbDrag", ctypes.c_double), ("lineDrag", ctypes.c_double)]
 
 
 class ddd_sur_opts(ctypes.Structure):
@@ -137,6 +144,8 @@ def library():
         L.ddd_destroy.restype = None
         L.ddd_last_error.argtypes = [_vp]
         L.ddd_last_error.restype = ctypes.c_char_p
+        L.ddd_last_kernel_ms.restype = ctypes.c_double
+        L.ddd_last_kernel_ms.argtypes = [ctypes.c_void_p]
         L.ddd_version.argtypes = []
         L.ddd_segseg_force.argtypes = [_vp, cp, _dp, _i64, _dp, _i64, _ip, _i64, _up, _i64, _ip, _i64, _dp, rp]
         L.ddd_segseg_force_inplace.argtypes = [_vp, cp, _dp, _i64, _dp, _i64, _ip, _i64, _up, _i64, _ip, _i64, _dp,
@@ -179,6 +188,10 @@ def library():
         L.ddd_self_force_inplace.argtypes = [_vp, cp, spp] + net_args + [_ip, _i64, _dp, _i64]
         L.ddd_seg_force.argtypes = [_vp, cp, spp] + net_args + [_dp, _ip, _i64, _dp, rp]
         L.ddd_seg_force_inplace.argtypes = [_vp, cp, spp] + net_args + [_dp, _ip, _i64, _dp, _i64, rp]
+        mob_args = [_vp, ctypes.POINTER(ddd_mob_params), _dp, _i64, _dp, _i64, _ip, _i64, _ip, _i64, _i64, _dp,
+                    _i64, _i64, _ip, _i64, _dp, _dp]
+        L.ddd_mobility_bcc.argtypes = mob_args
+        L.ddd_mobility_bcc_inplace.argtypes = mob_args + [_i64]
         L.ddd_set_mode.argtypes = [_vp, ctypes.c_int]
         L.ddd_get_mode.argtypes = [_vp]
         L.ddd_probe_fma_peak.argtypes = [_vp, ctypes.c_int, _dp]
@@ -214,7 +227,10 @@ class DislocationParameters:
     """The DislocationParameters fields this path reads (src/Type/DislocationConstructor.jl:55-105)."""
 
     def __init__(self, *, coreRad=1.0, coreRadMag=1.0, coreEnergy=None, minSegLen=None, maxSegLen=None,
-                 parCPU=False, parGPU=True, **other):
+                 parCPU=False, parGPU=True, dragCoeffs=None, **other):
+        self.dragCoeffs = dict(edge=1.0, screw=2.0, climb=1e9, line=0.0)
+        if dragCoeffs:
+            self.dragCoeffs.update({k: float(v) for k, v in dict(dragCoeffs).items()})
         self.coreRad = float(coreRad)
         self.coreRadSq = self.coreRad * self.coreRad
         self.coreEnergy = (1 / (4 * math.pi) * math.log(self.coreRad / 0.1) if coreEnergy is None
@@ -232,11 +248,15 @@ class DislocationNetwork:
     """The DislocationNetwork arrays this path reads and writes (src/Type/DislocationType.jl:324-340).
 
     coord (3×nodeBuf), bVec (3×linkBuf), segIdx (linkBuf×3; link, node1, node2;
-    1-based), extSeg (linkBuf), segForce (3×2×linkBuf), numSeg.  Stored
-    Fortran-ordered, which is the Julia memory image.
+    1-based), extSeg (linkBuf), segForce (3×2×linkBuf), numSeg; for the
+    mobility also links (2×linkBuf), connectivity ((1+2 maxConnect)×nodeBuf),
+    numNode, nodeForce and nodeVel (3×nodeBuf).  links defaults to segIdx's
+    node columns and connectivity to the one _makeConnect! builds from it.
+    Stored Fortran-ordered, which is the Julia memory image.
     """
 
-    def __init__(self, coord, bVec, segIdx, numSeg=None, extSeg=None, segForce=None):
+    def __init__(self, coord, bVec, segIdx, numSeg=None, extSeg=None, segForce=None, links=None,
+                 connectivity=None, numNode=None, nodeForce=None, nodeVel=None, maxConnect=4):
         self.coord = np.asfortranarray(coord, dtype=np.float64)
         self.bVec = np.asfortranarray(bVec, dtype=np.float64)
         self.segIdx = np.asfortranarray(segIdx, dtype=np.int64)
@@ -245,6 +265,38 @@ class DislocationNetwork:
         self.extSeg = (np.zeros(ld, np.uint8) if extSeg is None else np.ascontiguousarray(extSeg, dtype=np.uint8))
         self.segForce = (np.zeros((3, 2, self.bVec.shape[1]), np.float64, order="F") if segForce is None
                          else np.asfortranarray(segForce, dtype=np.float64))
+        self.maxConnect = int(maxConnect)
+        self.links = (np.asfortranarray(self.segIdx[:self.numSeg, 1:3].T) if links is None
+                      else np.asfortranarray(links, dtype=np.int64))
+        nodes = self.coord.shape[1]
+        self.connectivity = (make_connectivity(self.links, nodes, self.maxConnect) if connectivity is None
+                             else np.asfortranarray(connectivity, dtype=np.int64))
+        self.numNode = int(nodes if numNode is None else numNode)
+        self.nodeForce = (np.zeros((3, nodes), np.float64, order="F") if nodeForce is None
+                          else np.asfortranarray(nodeForce, dtype=np.float64))
+        self.nodeVel = (np.zeros((3, nodes), np.float64, order="F") if nodeVel is None
+                        else np.asfortranarray(nodeVel, dtype=np.float64))
+
+
+def make_connectivity(links, num_node, max_connect=4):
+    """connectivity ((1 + 2 max_connect) × num_node, 1-based) in the layout of
+    _makeConnect! (DislocationUtil.jl:213-237): row 1 counts a node's links,
+    rows 2c, 2c+1 hold its c-th link and the node's column in it; links are
+    taken in order up to the first undefined (zero) one."""
+    links = np.asarray(links, dtype=np.int64)
+    conn = np.zeros((1 + 2 * max_connect, num_node), dtype=np.int64, order="F")
+    for i in range(links.shape[1]):
+        n1, n2 = int(links[0, i]), int(links[1, i])
+        if n1 == 0:
+            break
+        for node, col in ((n1, 1), (n2, 2)):
+            conn[0, node - 1] += 1
+            c = conn[0, node - 1]
+            if 2 * c + 1 > conn.shape[0]:
+                raise ValueError("node %d has more than maxConnect = %d links" % (node, max_connect))
+            conn[2 * c - 1, node - 1] = i + 1
+            conn[2 * c, node - 1] = col
+    return conn
 
 
 def self_params_of(dlnParams, matParams):
@@ -403,6 +455,44 @@ class Context:
                                                   0 if idx is None else len(idx), sf.ctypes.data_as(_dp),
                                                   sf.shape[2], ctypes.byref(rep)))
         self.last_report = rep.as_dict()
+
+    def _mob_args(self, mp, network, idx):
+        coord = np.require(network.coord, np.float64, ["F"])
+        bvec = np.require(network.bVec, np.float64, ["F"])
+        links = np.require(network.links, np.int64, ["F"])
+        conn = np.require(network.connectivity, np.int64, ["F"])
+        sf = np.require(network.segForce, np.float64, ["F"])
+        keep = (coord, bvec, links, conn, sf)
+        args = [self._h, ctypes.byref(mp), coord.ctypes.data_as(_dp), coord.shape[1], bvec.ctypes.data_as(_dp),
+                bvec.shape[1], links.ctypes.data_as(_ip), links.shape[1], conn.ctypes.data_as(_ip), conn.shape[0],
+                conn.shape[1], sf.ctypes.data_as(_dp), sf.shape[2], network.numNode,
+                None if idx is None else idx.ctypes.data_as(_ip), 0 if idx is None else len(idx)]
+        return args, keep
+
+    @property
+    def last_kernel_ms(self):
+        """Device time of the kernel of the last self-force / segment-force / mobility call."""
+        return self._L.ddd_last_kernel_ms(self._h)
+
+    def mobility_bcc(self, mp, network, idx=None):
+        """dlnMobility (BCC): (nodeForce, nodeVel), 3×n each."""
+        idx = self._idx(idx)
+        n = network.numNode if idx is None else len(idx)
+        F = np.zeros((3, n), np.float64, order="F")
+        V = np.zeros((3, n), np.float64, order="F")
+        args, keep = self._mob_args(mp, network, idx)
+        self._check(self._L.ddd_mobility_bcc(*args, F.ctypes.data_as(_dp), V.ctypes.data_as(_dp)))
+        return F, V
+
+    def mobility_bcc_inplace(self, mp, network, idx=None):
+        idx = self._idx(idx)
+        nf, nv = network.nodeForce, network.nodeVel
+        for a in (nf, nv):
+            if not (a.flags.f_contiguous and a.dtype == np.float64 and a.shape[0] == 3):
+                raise ValueError("nodeForce / nodeVel must be Fortran-ordered float64 3×n arrays")
+        args, keep = self._mob_args(mp, network, idx)
+        self._check(self._L.ddd_mobility_bcc_inplace(*args, nf.ctypes.data_as(_dp), nv.ctypes.data_as(_dp),
+                                                     min(nf.shape[1], nv.shape[1])))
 
     def segseg_force_inplace(self, k, network, idx=None):
         coord, bvec, seg, ext = self._net(network)
@@ -795,6 +885,25 @@ def calcSegForce_inplace(dlnParams, matParams, sigmaHat, network, idx=None):
     get_context().seg_force_inplace(consts_of(dlnParams, matParams), self_params_of(dlnParams, matParams), network,
                                     sigmaHat, idx)
     return None
+
+
+def mob_params_of(dlnParams, matParams):
+    d = dlnParams.dragCoeffs
+    mp = ddd_mob_params()
+    mp.sigmaPN = matParams.σPN
+    mp.edgeDrag, mp.screwDrag, mp.climbDrag, mp.lineDrag = d["edge"], d["screw"], d["climb"], d["line"]
+    return mp
+
+
+def dlnMobility(dlnParams, matParams, network, idx=None):
+    """dlnMobility for a BCC material (DislocationMobility.jl:16-178): (nodeForce, nodeVel), 3×n each."""
+    return get_context().mobility_bcc(mob_params_of(dlnParams, matParams), network, idx)
+
+
+def dlnMobility_inplace(dlnParams, matParams, network, idx=None):
+    """dlnMobility! (DislocationMobility.jl:186-341): writes network.nodeForce and nodeVel."""
+    get_context().mobility_bcc_inplace(mob_params_of(dlnParams, matParams), network, idx)
+    return network
 
 
 def calc_σTilde(x0, dlnParams, matParams, network, idx=None):

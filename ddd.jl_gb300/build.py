@@ -28,6 +28,7 @@ VARIANTS = {
     "surrogate_data.cu": [("", ["--fmad=false"])],
     "surrogate_force.cu": [("", ["--fmad=false"])],
     "self_force.cu": [("", ["--fmad=false"])],
+    "mobility.cu": [("", ["--fmad=false"])],
 }
 
 

@@ -54,7 +54,9 @@ struct ddd_ctx {
   std::mutex mu;
   std::string err;
   DevBuf coord, bvec, segidx, ext, soa, soadf, skip, partial, out, rows, x0, sigma, counters, probe, errflag;
+  DevBuf links, conn, segforce;  // mobility inputs
   std::vector<double> hostTmp;
+  double lastKernelMs = 0.0;  // device time of the last self-force / mobility kernel
 };
 
 int ddd::ctx_device(const ddd_ctx* c) { return c->device; }
@@ -304,6 +306,7 @@ void ddd_destroy(ddd_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  for (DevBuf* b : {&c->links, &c->conn, &c->segforce}) b->release();
   for (DevBuf* b : {&c->coord, &c->bvec, &c->segidx, &c->ext, &c->soa, &c->soadf, &c->skip, &c->partial, &c->out, &c->rows,
                     &c->x0, &c->sigma, &c->counters, &c->probe, &c->errflag})
     b->release();
@@ -317,6 +320,8 @@ const char* ddd_last_error(const ddd_ctx* c) {
   if (!c) return g_create_error.c_str();
   return c->err.c_str();
 }
+
+double ddd_last_kernel_ms(const ddd_ctx* c) { return c ? c->lastKernelMs : 0.0; }
 
 int ddd_segseg_force(ddd_ctx* ctx, const ddd_consts* k, const double* coord, int64_t coordCols, const double* bVec,
                      int64_t bVecCols, const int64_t* segIdx, int64_t ldSegIdx, const uint8_t* extSeg,
@@ -411,16 +416,19 @@ int self_pk_compute(ddd_ctx* ctx, const ddd_consts* k, const ddd_self_params* sp
   }
   CK(ctx->out.ensure((size_t)n * 6 * sizeof(double)), "alloc output");
   double* dS = ctx->out.as<double>();
+  CK(cudaEventRecord(ctx->ev[1], ctx->stream), "event");
   CK(ddd::launch_self_pk(SK, ctx->coord.as<double>(), ctx->bvec.as<double>(), ctx->segidx.as<int64_t>(), ld,
                          extSeg ? ctx->ext.as<uint8_t>() : nullptr, numSeg, idx ? ctx->rows.as<int64_t>() : nullptr,
                          n, sigmaHat ? ctx->sigma.as<double>() : nullptr, dS, sigmaHat ? dS + 3 * n : nullptr,
                          ctx->stream),
      "self_pk_f64");
+  CK(cudaEventRecord(ctx->ev[2], ctx->stream), "event");
   CK(cudaMemcpyAsync(S.data(), dS, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "copy S");
   if (sigmaHat)
     CK(cudaMemcpyAsync(PK.data(), dS + 3 * n, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
        "copy PK");
   CK(cudaStreamSynchronize(ctx->stream), "self force");
+  ctx->lastKernelMs = elapsed(ctx->ev[1], ctx->ev[2]);
   return DDD_OK;
 }
 
@@ -539,6 +547,143 @@ int ddd_seg_force_inplace(ddd_ctx* ctx, const ddd_consts* k, const ddd_self_para
     }
   }
   add_segseg_inplace(ctx, extSeg, numSeg, idx, nIdx, segForce);
+  return DDD_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// dlnMobility (BCC) on the GPU for the nodes of idx (or 1:numNode) into
+// ctx->hostTmp: [nodeForce 3n | nodeVel 3n].  All indices are checked on the
+// host first.
+int mobility_compute(ddd_ctx* ctx, const ddd_mob_params* mp, const double* coord, int64_t coordCols,
+                     const double* bVec, int64_t bVecCols, const int64_t* links, int64_t linkCols,
+                     const int64_t* connectivity, int64_t ldConn, int64_t connCols, const double* segForce,
+                     int64_t segForceCols, int64_t numNode, const int64_t* idx, int64_t nIdx) {
+  if (!mp) return fail(ctx, DDD_EINVAL, "mobility parameters are NULL");
+  const double pv[5] = {mp->sigmaPN, mp->edgeDrag, mp->screwDrag, mp->climbDrag, mp->lineDrag};
+  for (double v : pv)
+    if (!std::isfinite(v)) return fail(ctx, DDD_ENONFINITE, "non-finite mobility parameter");
+  if (numNode < 0 || coordCols < 0 || bVecCols < 0 || linkCols < 0 || connCols < 0 || segForceCols < 0 ||
+      (idx && nIdx < 0))
+    return fail(ctx, DDD_EINVAL, "negative size");
+  if (ldConn < 1 || ldConn % 2 == 0) return fail(ctx, DDD_EINVAL, "connectivity must have 1 + 2 maxConnect rows");
+  if (numNode > connCols || numNode > coordCols) return fail(ctx, DDD_EINVAL, "numNode exceeds coord / connectivity");
+  if (linkCols > bVecCols || linkCols > segForceCols)
+    return fail(ctx, DDD_EINVAL, "links has more columns than bVec or segForce");
+  const int64_t n = idx ? nIdx : numNode;
+  ctx->hostTmp.assign((size_t)n * 6, 0.0);
+  if (n == 0) return DDD_OK;
+  if (!coord || !bVec || !links || !connectivity || !segForce) return fail(ctx, DDD_EINVAL, "network array is NULL");
+  char buf[160];
+  for (int64_t q = 0; q < n; ++q) {
+    const int64_t node = idx ? idx[q] : q + 1;
+    if (node < 1 || node > numNode) {
+      snprintf(buf, sizeof buf, "idx[%lld] = %lld outside 1..numNode=%lld", (long long)q, (long long)node,
+               (long long)numNode);
+      return fail(ctx, DDD_ERANGE, buf);
+    }
+    const int64_t* cn = connectivity + ldConn * (node - 1);
+    if (cn[0] < 0 || 2 * cn[0] + 1 > ldConn) {
+      snprintf(buf, sizeof buf, "node %lld: %lld connections exceed the connectivity rows", (long long)node,
+               (long long)cn[0]);
+      return fail(ctx, DDD_ERANGE, buf);
+    }
+    for (int64_t c = 1; c <= cn[0]; ++c) {
+      const int64_t link = cn[2 * c - 1], col = cn[2 * c];
+      if (link < 1 || link > linkCols || (col != 1 && col != 2)) {
+        snprintf(buf, sizeof buf, "node %lld: connection %lld = (link %lld, column %lld) out of range",
+                 (long long)node, (long long)c, (long long)link, (long long)col);
+        return fail(ctx, DDD_ERANGE, buf);
+      }
+      const int64_t other = links[2 * (link - 1) + (2 - col)];
+      if (other < 1 || other > coordCols) {
+        snprintf(buf, sizeof buf, "link %lld: node %lld outside 1..%lld", (long long)link, (long long)other,
+                 (long long)coordCols);
+        return fail(ctx, DDD_ERANGE, buf);
+      }
+    }
+  }
+  ddd::MobK P{mp->sigmaPN, mp->edgeDrag, mp->screwDrag, mp->climbDrag, mp->lineDrag};
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  cudaStream_t st = ctx->stream;
+  const size_t cB = (size_t)coordCols * 3 * 8, bB = (size_t)linkCols * 3 * 8, lB = (size_t)linkCols * 2 * 8;
+  const size_t nB = (size_t)ldConn * numNode * 8, fB = (size_t)linkCols * 6 * 8;
+  CK(ctx->coord.ensure(cB), "alloc coord");
+  CK(ctx->bvec.ensure(bB), "alloc bVec");
+  CK(ctx->links.ensure(lB), "alloc links");
+  CK(ctx->conn.ensure(nB), "alloc connectivity");
+  CK(ctx->segforce.ensure(fB), "alloc segForce");
+  CK(ctx->out.ensure((size_t)n * 6 * sizeof(double)), "alloc output");
+  CK(cudaMemcpyAsync(ctx->coord.p, coord, cB, cudaMemcpyHostToDevice, st), "copy coord");
+  CK(cudaMemcpyAsync(ctx->bvec.p, bVec, bB, cudaMemcpyHostToDevice, st), "copy bVec");
+  CK(cudaMemcpyAsync(ctx->links.p, links, lB, cudaMemcpyHostToDevice, st), "copy links");
+  CK(cudaMemcpyAsync(ctx->conn.p, connectivity, nB, cudaMemcpyHostToDevice, st), "copy connectivity");
+  CK(cudaMemcpyAsync(ctx->segforce.p, segForce, fB, cudaMemcpyHostToDevice, st), "copy segForce");
+  if (idx) {
+    std::vector<int64_t> rows0((size_t)n);
+    for (int64_t q = 0; q < n; ++q) rows0[q] = idx[q] - 1;
+    CK(ctx->rows.ensure((size_t)n * sizeof(int64_t)), "alloc rows");
+    CK(cudaMemcpyAsync(ctx->rows.p, rows0.data(), (size_t)n * sizeof(int64_t), cudaMemcpyHostToDevice, st),
+       "copy idx");
+  }
+  double* dOut = ctx->out.as<double>();
+  CK(cudaEventRecord(ctx->ev[1], st), "event");
+  CK(ddd::launch_mobility_bcc(P, ctx->coord.as<double>(), ctx->bvec.as<double>(), ctx->links.as<int64_t>(),
+                              ctx->conn.as<int64_t>(), ldConn, ctx->segforce.as<double>(),
+                              idx ? ctx->rows.as<int64_t>() : nullptr, n, dOut, dOut + 3 * n, st),
+     "mobility_bcc_f64");
+  CK(cudaEventRecord(ctx->ev[2], st), "event");
+  CK(cudaMemcpyAsync(ctx->hostTmp.data(), dOut, (size_t)n * 6 * sizeof(double), cudaMemcpyDeviceToHost, st),
+     "copy node forces and velocities");
+  CK(cudaStreamSynchronize(st), "mobility");
+  ctx->lastKernelMs = elapsed(ctx->ev[1], ctx->ev[2]);
+  return DDD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ddd_mobility_bcc(ddd_ctx* ctx, const ddd_mob_params* mp, const double* coord, int64_t coordCols,
+                     const double* bVec, int64_t bVecCols, const int64_t* links, int64_t linkCols,
+                     const int64_t* connectivity, int64_t ldConn, int64_t connCols, const double* segForce,
+                     int64_t segForceCols, int64_t numNode, const int64_t* idx, int64_t nIdx, double* nodeForce,
+                     double* nodeVel) {
+  if (!ctx) return DDD_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  const int64_t n = idx ? nIdx : numNode;
+  if (n > 0 && (!nodeForce || !nodeVel)) return fail(ctx, DDD_EINVAL, "nodeForce or nodeVel is NULL");
+  int rc = mobility_compute(ctx, mp, coord, coordCols, bVec, bVecCols, links, linkCols, connectivity, ldConn, connCols,
+                            segForce, segForceCols, numNode, idx, nIdx);
+  if (rc) return rc;
+  std::memcpy(nodeForce, ctx->hostTmp.data(), (size_t)n * 3 * sizeof(double));
+  std::memcpy(nodeVel, ctx->hostTmp.data() + 3 * n, (size_t)n * 3 * sizeof(double));
+  return DDD_OK;
+}
+
+int ddd_mobility_bcc_inplace(ddd_ctx* ctx, const ddd_mob_params* mp, const double* coord, int64_t coordCols,
+                             const double* bVec, int64_t bVecCols, const int64_t* links, int64_t linkCols,
+                             const int64_t* connectivity, int64_t ldConn, int64_t connCols, const double* segForce,
+                             int64_t segForceCols, int64_t numNode, const int64_t* idx, int64_t nIdx,
+                             double* nodeForce, double* nodeVel, int64_t nodeCols) {
+  if (!ctx) return DDD_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  const int64_t n = idx ? nIdx : numNode;
+  if (nodeCols < numNode) return fail(ctx, DDD_EINVAL, "nodeForce / nodeVel have fewer columns than numNode");
+  if (n > 0 && (!nodeForce || !nodeVel)) return fail(ctx, DDD_EINVAL, "nodeForce or nodeVel is NULL");
+  int rc = mobility_compute(ctx, mp, coord, coordCols, bVec, bVecCols, links, linkCols, connectivity, ldConn, connCols,
+                            segForce, segForceCols, numNode, idx, nIdx);
+  if (rc) return rc;
+  const double* H = ctx->hostTmp.data();
+  for (int64_t q = 0; q < n; ++q) {  // nodeForce[:, node1] = ...; nodeVel[:, node1] = ... (:338-339)
+    const int64_t node = idx ? idx[q] - 1 : q;
+    for (int c = 0; c < 3; ++c) {
+      nodeForce[3 * node + c] = H[3 * q + c];
+      nodeVel[3 * node + c] = H[3 * n + 3 * q + c];
+    }
+  }
   return DDD_OK;
 }
 

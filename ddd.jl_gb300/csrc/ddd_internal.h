@@ -76,6 +76,14 @@ cudaError_t launch_self_pk(const SelfK& K, const double* coord, const double* bV
                            const uint8_t* ext, int64_t nExt, const int64_t* rows, int64_t n, const double* sigmaHat,
                            double* S, double* PK, cudaStream_t st);
 
+// mobility.cu: BCC node velocities, strict FP64.
+struct MobK {
+  double sigmaPN, edge, screw, climb, line;
+};
+cudaError_t launch_mobility_bcc(const MobK& P, const double* coord, const double* bVec, const int64_t* links,
+                                const int64_t* conn, int64_t ldConn, const double* segForce, const int64_t* rows,
+                                int64_t n, double* nodeForce, double* nodeVel, cudaStream_t st);
+
 // ddd_api.cu: context accessors for the other C-ABI files.
 int ctx_device(const ddd_ctx* c);
 

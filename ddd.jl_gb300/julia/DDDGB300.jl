@@ -14,6 +14,7 @@ module DDDGB300
 export calcSegSegForceGPU, calcSegSegForceGPU!, calc_σTildeGPU, calc_σTildeGPU!
 export calcSelfForceGPU, calcSelfForceGPU!, calcSegForceGPU, calcSegForceGPU!
 export Surrogate, loadSurrogate, calcSegSegForceSurrogateGPU
+export dlnMobilityGPU, dlnMobilityGPU!
 
 const libddd = joinpath(@__DIR__, "..", "libddd_gb300.so")
 
@@ -198,6 +199,64 @@ function calcSegForceGPU!(dlnParams, matParams, σHat, network, idx = nothing)
             context(), k, sp, coord, size(coord, 2), bVec, size(bVec, 2), segIdx, size(segIdx, 1), extSeg, numSeg,
             isnothing(σHat) ? C_NULL : pointer(sh), isnothing(idx) ? C_NULL : pointer(iv), length(iv), segForce,
             size(segForce, 3), C_NULL)
+    end
+    check(rc)
+    return nothing
+end
+
+# ---------------------------------------------------------------------------
+# BCC mobility (DislocationMobility.jl:16-178 and dlnMobility! :186-): node
+# forces from network.segForce and node velocities from the 3×3 drag solve.
+
+struct DDDMobParams
+    sigmaPN::Float64
+    edgeDrag::Float64
+    screwDrag::Float64
+    climbDrag::Float64
+    lineDrag::Float64
+end
+
+function mobparams(dlnParams, matParams)
+    d = dlnParams.dragCoeffs
+    return DDDMobParams(matParams.σPN, d.edge, d.screw, d.climb, d.line)
+end
+
+# dlnMobility: (nodeForce, nodeVel), 3×n each
+function dlnMobilityGPU(dlnParams, matParams, network, idx = nothing)
+    numNode = network.numNode[1]
+    iv = idxvec(idx)
+    n = isnothing(idx) ? numNode : length(iv)
+    F, V = zeros(3, n), zeros(3, n)
+    mp = Ref(mobparams(dlnParams, matParams))
+    coord, bVec, links, conn, segForce = network.coord, network.bVec, network.links, network.connectivity,
+                                         network.segForce
+    GC.@preserve coord bVec links conn segForce iv F V begin
+        rc = ccall((:ddd_mobility_bcc, libddd), Cint,
+            (Ptr{Cvoid}, Ref{DDDMobParams}, Ptr{Float64}, Int64, Ptr{Float64}, Int64, Ptr{Int64}, Int64, Ptr{Int64},
+             Int64, Int64, Ptr{Float64}, Int64, Int64, Ptr{Int64}, Int64, Ptr{Float64}, Ptr{Float64}),
+            context(), mp, coord, size(coord, 2), bVec, size(bVec, 2), links, size(links, 2), conn, size(conn, 1),
+            size(conn, 2), segForce, size(segForce, 3), numNode, isnothing(idx) ? C_NULL : pointer(iv), length(iv),
+            F, V)
+    end
+    check(rc)
+    return F, V
+end
+
+# dlnMobility!: writes the nodes' columns of network.nodeForce and network.nodeVel
+function dlnMobilityGPU!(dlnParams, matParams, network, idx = nothing)
+    numNode = network.numNode[1]
+    iv = idxvec(idx)
+    mp = Ref(mobparams(dlnParams, matParams))
+    coord, bVec, links, conn, segForce = network.coord, network.bVec, network.links, network.connectivity,
+                                         network.segForce
+    nodeForce, nodeVel = network.nodeForce, network.nodeVel
+    GC.@preserve coord bVec links conn segForce nodeForce nodeVel iv begin
+        rc = ccall((:ddd_mobility_bcc_inplace, libddd), Cint,
+            (Ptr{Cvoid}, Ref{DDDMobParams}, Ptr{Float64}, Int64, Ptr{Float64}, Int64, Ptr{Int64}, Int64, Ptr{Int64},
+             Int64, Int64, Ptr{Float64}, Int64, Int64, Ptr{Int64}, Int64, Ptr{Float64}, Ptr{Float64}, Int64),
+            context(), mp, coord, size(coord, 2), bVec, size(bVec, 2), links, size(links, 2), conn, size(conn, 1),
+            size(conn, 2), segForce, size(segForce, 3), numNode, isnothing(idx) ? C_NULL : pointer(iv), length(iv),
+            nodeForce, nodeVel, size(nodeForce, 2))
     end
     check(rc)
     return nothing

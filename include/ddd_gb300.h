@@ -96,6 +96,10 @@ ddd_ctx* ddd_create(int device);
 void ddd_destroy(ddd_ctx* ctx);
 /* Message of the last failed call on ctx (or of the last failed ddd_create when ctx is NULL). */
 const char* ddd_last_error(const ddd_ctx* ctx);
+/* Device time (ms, CUDA events around the launch) of the kernel of the last
+ * successful ddd_self_force* / ddd_seg_force* / ddd_mobility_bcc* call on ctx.
+ * No reference counterpart: measurement only. */
+double ddd_last_kernel_ms(const ddd_ctx* ctx);
 /* ABI version, 100 * major + minor. */
 int ddd_version(void);
 
@@ -165,6 +169,34 @@ int ddd_seg_force_inplace(ddd_ctx* ctx, const ddd_consts* k, const ddd_self_para
                           int64_t coordCols, const double* bVec, int64_t bVecCols, const int64_t* segIdx,
                           int64_t ldSegIdx, const uint8_t* extSeg, int64_t numSeg, const double* sigmaHat,
                           const int64_t* idx, int64_t nIdx, double* segForce, int64_t segForceCols, ddd_report* rep);
+
+/* dlnMobility / dlnMobility! for a BCC material (mobBCC)
+ *   src/Processing/DislocationMobility.jl:16-178 and :186-341.
+ * For each node of idx (1-based) or of 1:numNode: the node force (sum of the
+ * forces its connected segments put on it, zeroed below the Peierls-Nabarro
+ * stress) and the velocity solving drag · v = force, the drag tensor built
+ * from every connection (edge, screw, climb and line drags; BCC screw
+ * families by the ratios of |b| components).  Arrays in the network's layout:
+ * links 2 × linkCols and connectivity ldConn × connCols (ldConn = 1 +
+ * 2 maxConnect; the _makeConnect! layout, DislocationUtil.jl:213-237), both
+ * 1-based; segForce 3 × 2 × segForceCols.  ddd_mobility_bcc writes nodeForce
+ * and nodeVel as 3 × n arrays; the _inplace form writes the nodes' columns of
+ * the network's nodeForce / nodeVel (3 × nodeCols).  A node whose drag is
+ * singular (no connections) gets NaN velocities, as the reference's solve. */
+typedef struct ddd_mob_params {
+  double sigmaPN;  /* matParams.σPN */
+  double edgeDrag, screwDrag, climbDrag, lineDrag; /* dlnParams.dragCoeffs */
+} ddd_mob_params;
+int ddd_mobility_bcc(ddd_ctx* ctx, const ddd_mob_params* mp, const double* coord, int64_t coordCols,
+                     const double* bVec, int64_t bVecCols, const int64_t* links, int64_t linkCols,
+                     const int64_t* connectivity, int64_t ldConn, int64_t connCols, const double* segForce,
+                     int64_t segForceCols, int64_t numNode, const int64_t* idx, int64_t nIdx, double* nodeForce,
+                     double* nodeVel);
+int ddd_mobility_bcc_inplace(ddd_ctx* ctx, const ddd_mob_params* mp, const double* coord, int64_t coordCols,
+                             const double* bVec, int64_t bVecCols, const int64_t* links, int64_t linkCols,
+                             const int64_t* connectivity, int64_t ldConn, int64_t connCols, const double* segForce,
+                             int64_t segForceCols, int64_t numNode, const int64_t* idx, int64_t nIdx,
+                             double* nodeForce, double* nodeVel, int64_t nodeCols);
 
 /* calc_σTilde(x0, dlnParams, matParams, network, idx = nothing) and
  * calc_σTilde!(σ, x0, ...) — src/Processing/DislocationFEM.jl:24-84, kernel

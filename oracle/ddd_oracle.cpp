@@ -282,6 +282,27 @@ void oracle_self_force(const double* k5, const double* sc, const double* coord, 
   }
 }
 
+// dlnMobility for a BCC material (DislocationMobility.jl:16-178): node forces
+// and velocities (3 × n each) of the nodes in idx (1-based) or 1:numNode.
+// mp = (σPN, edge, screw, climb, line drag).
+void oracle_mobility_bcc(const double* mp, const double* coord, const double* bVec, const int64_t* links,
+                         const int64_t* conn, int64_t ldConn, const double* segForce, int64_t numNode,
+                         const int64_t* idx, int64_t nIdx, double* nodeForce, double* nodeVel) {
+  const MobParams P{mp[0], mp[1], mp[2], mp[3], mp[4]};
+  const int64_t n = idx ? nIdx : numNode;
+  for (int64_t q = 0; q < n; ++q) {
+    const int64_t node = idx ? idx[q] - 1 : q;
+    V3<double> f, v;
+    mobility_bcc_node<double>(P, coord, bVec, links, conn, ldConn, segForce, node, f, v);
+    nodeForce[3 * q] = f.x;
+    nodeForce[3 * q + 1] = f.y;
+    nodeForce[3 * q + 2] = f.z;
+    nodeVel[3 * q] = v.x;
+    nodeVel[3 * q + 1] = v.y;
+    nodeVel[3 * q + 2] = v.z;
+  }
+}
+
 // PK forces (σ̂ b) × (n2 - n1) of the segments in idx (or 1:numSeg) from the
 // stresses sigmaHat (6 × n, one per entry, at the segment midpoints): PK
 // (3 × n, overwritten; 0 where extSeg[k]).

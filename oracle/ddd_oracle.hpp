@@ -681,6 +681,108 @@ template <class T> inline V3<T> pk_force(const T* sig, const V3<T>& b, const V3<
 }
 
 // ---------------------------------------------------------------------------
+// BCC mobility of one node — the loop body of dlnMobility
+// (DislocationMobility.jl:16-178, the ! form :186-341 is the same per node).
+// links: 2 × nLinks (1-based nodes), conn: ldConn × nodes (1-based links and
+// columns, _makeConnect! layout), segForce: 3 × 2 × nLinks.  node1 is 0-based.
+// Outer products follow ⊗(x, y) = x y' (Misc.jl:215) with the scalar applied to
+// the left vector first, as Julia's left-to-right `s * t ⊗ t` does.  The
+// velocity solves totalDrag v = f by Cramer's rule (det and adjugate).
+struct MobParams {
+  double sigmaPN, edge, screw, climb, line;
+};
+
+template <class T> struct M33 {
+  T a[3][3];
+};
+
+template <class T> inline void add_outer(M33<T>& M, T s, const V3<T>& x, const V3<T>& y, T scale, T diag) {
+  // M += scale * (diag I + (s x) y')
+  const T sx[3] = {s * x.x, s * x.y, s * x.z};
+  const T yy[3] = {y.x, y.y, y.z};
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) M.a[i][j] = M.a[i][j] + scale * ((i == j ? diag : T(0)) + sx[i] * yy[j]);
+}
+
+template <class T> inline V3<T> solve3(const M33<T>& M, const V3<T>& f) {
+  const T(&a)[3][3] = M.a;
+  const T c00 = a[1][1] * a[2][2] - a[1][2] * a[2][1];
+  const T c01 = a[1][2] * a[2][0] - a[1][0] * a[2][2];
+  const T c02 = a[1][0] * a[2][1] - a[1][1] * a[2][0];
+  const T det = a[0][0] * c00 + a[0][1] * c01 + a[0][2] * c02;
+  const T x0 = (c00 * f.x + (a[0][2] * a[2][1] - a[0][1] * a[2][2]) * f.y + (a[0][1] * a[1][2] - a[0][2] * a[1][1]) * f.z) / det;
+  const T x1 = (c01 * f.x + (a[0][0] * a[2][2] - a[0][2] * a[2][0]) * f.y + (a[0][2] * a[1][0] - a[0][0] * a[1][2]) * f.z) / det;
+  const T x2 = (c02 * f.x + (a[0][1] * a[2][0] - a[0][0] * a[2][1]) * f.y + (a[0][0] * a[1][1] - a[0][1] * a[1][0]) * f.z) / det;
+  return {x0, x1, x2};
+}
+
+template <class T>
+inline void mobility_bcc_node(const MobParams& P, const T* coord, const T* bVec, const int64_t* links,
+                              const int64_t* conn, int64_t ldConn, const T* segForce, int64_t node1, V3<T>& force,
+                              V3<T>& vel) {
+  using std::abs;
+  using std::sqrt;
+  const T eps = std::numeric_limits<T>::epsilon();
+  const T sqrtBType = sqrt(eps);
+  M33<T> drag = {};
+  force = {T(0), T(0), T(0)};
+  const int64_t numConnect = conn[ldConn * node1];
+  const V3<T> x1 = {coord[3 * node1], coord[3 * node1 + 1], coord[3 * node1 + 2]};
+  for (int64_t c = 1; c <= numConnect; ++c) {
+    const int64_t link = conn[ldConn * node1 + 2 * c - 1] - 1;
+    const int64_t colLink = conn[ldConn * node1 + 2 * c];
+    const int64_t node2 = links[2 * link + (3 - colLink) - 1] - 1;
+    V3<T> t = V3<T>{coord[3 * node2], coord[3 * node2 + 1], coord[3 * node2 + 2]} - x1;
+    const T nT = sqrt(dot(t, t));
+    if (nT < eps) continue;
+    const T tN = T(1) / nT;
+    t = t * tN;
+    V3<T> f = {segForce[6 * link + 3 * (colLink - 1)], segForce[6 * link + 3 * (colLink - 1) + 1],
+               segForce[6 * link + 3 * (colLink - 1) + 2]};
+    if (sqrt(dot(f, f)) * tN < T(P.sigmaPN)) f = {T(0), T(0), T(0)};
+    force = force + f;
+    V3<T> b = {bVec[3 * link], bVec[3 * link + 1], bVec[3 * link + 2]};
+    const T nB = sqrt(dot(b, b));
+    const T ab[3] = {abs(b.x), abs(b.y), abs(b.z)};
+    const T mn = std::min(std::min(ab[0], ab[1]), ab[2]);
+    int type1 = 0, type2 = 0, type3 = 0;
+    for (int k = 0; k < 3; ++k) {
+      const T r = ab[k] / mn;
+      type1 += abs(T(1) - r) < sqrtBType;
+      type2 += abs(T(2) - r) < sqrtBType;
+      type3 += abs(T(3) - r) < sqrtBType;
+    }
+    const bool screw = T(1) - nB < sqrtBType;
+    b = {b.x / nB, b.y / nB, b.z / nB};
+    const T nBnT_2 = nB * nT / T(2);
+    if (!((type1 == 3 && screw) || (type1 == 2 && type2 == 1 && screw) ||
+          (type1 == 1 && type2 == 1 && type3 == 1 && screw))) {
+      add_outer(drag, T(P.line) - T(P.climb), t, t, nBnT_2, T(P.climb));
+      continue;
+    }
+    const T tDb = dot(t, b);
+    const T cosSq = tDb * tDb;
+    const T sinSq = T(1) - cosSq;
+    add_outer(drag, T(P.line) - T(P.screw), t, t, nBnT_2, T(P.screw));
+    if (sinSq < eps) continue;
+    const T sq = sqrt(sinSq);
+    const V3<T> bt = cross(b, t);
+    const V3<T> p = {bt.x / sq, bt.y / sq, bt.z / sq};
+    const V3<T> q = cross(p, t);
+    const T screwSq = T(P.screw) * T(P.screw);
+    const T glide = T(1) / sqrt(sinSq / (T(P.edge) * T(P.edge)) + cosSq / screwSq);
+    const T climb = sqrt(sinSq * (T(P.climb) * T(P.climb)) + cosSq * screwSq);
+    // totalDrag += nBnT_2 * ((glide - ξs) q ⊗ q + (climb - ξs) p ⊗ p)
+    const T gq[3] = {(glide - T(P.screw)) * q.x, (glide - T(P.screw)) * q.y, (glide - T(P.screw)) * q.z};
+    const T cp[3] = {(climb - T(P.screw)) * p.x, (climb - T(P.screw)) * p.y, (climb - T(P.screw)) * p.z};
+    const T qq[3] = {q.x, q.y, q.z}, pp[3] = {p.x, p.y, p.z};
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) drag.a[i][j] = drag.a[i][j] + nBnT_2 * (gq[i] * qq[j] + cp[i] * pp[j]);
+  }
+  vel = solve3(drag, force);
+}
+
+// ---------------------------------------------------------------------------
 // Field-point stress of one segment at one point — body of the point loop of
 // _calc_σTilde! (DislocationFEM.jl:135-299).  Adds to sig[0..5] in the order
 // (xx, yy, zz, xy, xz, yz).  t is normalize(n2 - n1) computed once per segment

@@ -169,3 +169,21 @@ def sigma_case_network(case):
     r = [-300.0, 0.0, 300.0]
     pts = np.array([[x, y, 0.0] for x in r for y in r], dtype=np.float64).T  # x outer, y inner
     return net, np.asfortranarray(pts)
+
+
+def make_connectivity(links, max_connect=4):
+    """connectivity ((1 + 2 max_connect) × numNode, 1-based) as _makeConnect!
+    builds it (DislocationUtil.jl:213-237): row 1 counts a node's links, rows
+    2c and 2c+1 hold its c-th link and the node's column (1 or 2) in that link,
+    links taken in order.  links: 2 × numLinks, 1-based node numbers."""
+    links = np.asarray(links, dtype=np.int64)
+    num_node = int(links.max())
+    conn = np.zeros((1 + 2 * max_connect, num_node), dtype=np.int64, order="F")
+    for i in range(links.shape[1]):
+        n1, n2 = links[0, i] - 1, links[1, i] - 1
+        conn[0, n1] += 1
+        conn[0, n2] += 1
+        t1, t2 = 2 * conn[0, n1], 2 * conn[0, n2]
+        conn[t1 - 1:t1 + 1, n1] = (i + 1, 1)
+        conn[t2 - 1:t2 + 1, n2] = (i + 1, 2)
+    return conn

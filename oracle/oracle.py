@@ -51,6 +51,8 @@ def lib():
                                         ctypes.c_int64, _dp, _dp]
         L.oracle_pk_force.argtypes = [_dp, _dp, _ip, ctypes.c_int64, _up, ctypes.c_int64, _ip, ctypes.c_int64, _dp,
                                       _dp]
+        L.oracle_mobility_bcc.argtypes = [_dp, _dp, _dp, _ip, _ip, ctypes.c_int64, _dp, ctypes.c_int64, _ip,
+                                          ctypes.c_int64, _dp, _dp]
         L.oracle_segseg_rows.argtypes = [_dp, _dp, _dp, _ip, ctypes.c_int64, _up, ctypes.c_int64, _ip,
                                          ctypes.c_int64, _dp, ctypes.c_int]
         L.oracle_segseg_idx.argtypes = [_dp, _dp, _dp, _ip, ctypes.c_int64, _up, ctypes.c_int64, _ip,
@@ -159,6 +161,24 @@ def pk_force(net, sigma_hat, idx=None):
     lib().oracle_pk_force(_d(coord), _d(bvec), _i(seg), ld, ext.ctypes.data_as(_up), net.numSeg, ip,
                           0 if idx is None else len(idx), _d(sh), _d(PK))
     return PK
+
+
+def mobility_bcc(mp, coord, bvec, links, conn, seg_force, num_node, idx=None):
+    """dlnMobility (BCC): (nodeForce, nodeVel), 3 × n each.  mp = (σPN, edge,
+    screw, climb, line drag); links 2 × nLinks and conn ((1+2 maxConnect) ×
+    nodes) 1-based; seg_force 3 × 2 × nLinks."""
+    coord = np.require(coord, np.float64, ["F"])
+    bvec = np.require(bvec, np.float64, ["F"])
+    links = np.require(links, np.int64, ["F"])
+    conn = np.require(conn, np.int64, ["F"])
+    sf = np.require(seg_force, np.float64, ["F"])
+    n = num_node if idx is None else len(idx)
+    Fo = np.zeros((3, n), np.float64, order="F")
+    Vo = np.zeros((3, n), np.float64, order="F")
+    ip = None if idx is None else _i(np.ascontiguousarray(idx, np.int64))
+    lib().oracle_mobility_bcc(_d(np.ascontiguousarray(mp, np.float64)), _d(coord), _d(bvec), _i(links), _i(conn),
+                              conn.shape[0], _d(sf), num_node, ip, 0 if idx is None else len(idx), _d(Fo), _d(Vo))
+    return Fo, Vo
 
 
 def segseg_rows(k5, net, rows, nthreads=1):

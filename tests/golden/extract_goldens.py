@@ -9,6 +9,9 @@ matrices they assert against into JSON fixtures beside this script:
   selfforce_goldens.json test/SegmentForcesTest.jl:220-267 — calcSelfForce on
                         two prismatic pentagons (the second shifted by 10),
                         f1 = selfForce[1]', f2 = selfForce[2]'
+  mobility_goldens.json test/MobilityTest.jl:5-93 — BCC dlnMobility on a shear
+                        hexagon and a prismatic pentagon after calcSegForce!
+                        (zero FE fields, so no PK term): node forces and velocities
   sigma_goldens.json    test/DislocationFEMTest.jl:5-155 — one edge and one
                         screw segment, σ̃ at a 3×3 grid (columns 5 and 6 of the
                         golden are (yz, xz), the code's order is (xz, yz))
@@ -107,6 +110,27 @@ def main(ref):
     json.dump({"params": dict(params, coreEnergy=float(dpar["coreEnergy"])),
                "slipSystems": {"slipPlane": bcc["slipPlane"], "bVec": bcc["bVec"]}, "cases": [self_case]},
               open(os.path.join(HERE, "selfforce_goldens.json"), "w"), indent=1)
+
+    mob = open(os.path.join(ref, "test", "MobilityTest.jl")).read()
+    mvel, mforce = _matrices(mob, "testVel")[0], _matrices(mob, "testForce")[0]
+    ipar = json.load(open(os.path.join(ref, "inputs", "simParams", "sampleDislocationParameters.json")))
+    mpar = json.load(open(os.path.join(ref, "inputs", "simParams", "sampleMaterialParameters.json")))
+    json.dump({
+        "source": "test/MobilityTest.jl:5-93; parameters inputs/simParams/sample*Parameters.json",
+        "params": {"coreRad": float(ipar["coreRad"]), "coreEnergy": float(ipar["coreEnergy"]),
+                   "mu": float(mpar["μ"]), "nu": float(mpar["ν"]), "sigmaPN": float(mpar["σPN"]),
+                   "drag": {k: float(v) for k, v in ipar["dragCoeffs"].items()}},
+        "slipSystems": {"slipPlane": bcc["slipPlane"], "bVec": bcc["bVec"]},
+        "loops": [
+            {"type": "shear", "numSides": 6, "nodeSide": 1, "numLoops": 1, "segLen": 10.0, "slipSystemIdx": 4,
+             "label": [1, 2, 1, 2, 1, 1]},
+            {"type": "prism", "numSides": 5, "nodeSide": 1, "numLoops": 1, "segLen": 10.0, "slipSystemIdx": 4,
+             "label": [1, 2, 1, 2, 1]},
+        ],
+        "range": [[-100.0, 100.0], [-100.0, 100.0], [-100.0, 100.0]],
+        "maxConnect": 4,
+        "nodeVel": mvel, "nodeForce": mforce,
+    }, open(os.path.join(HERE, "mobility_goldens.json"), "w"), indent=1)
 
     fem = open(os.path.join(ref, "test", "DislocationFEMTest.jl")).read()
     sig = _matrices(fem, "test_σTilde")

@@ -178,3 +178,47 @@ def test_pk_force_formula(oracle, fixtures):
         l, a, b = net.segIdx[q] - 1
         t = net.coord[:, b] - net.coord[:, a]
         assert np.allclose(PK[:, q], np.cross(S @ net.bVec[:, l], t), rtol=1e-14, atol=1e-14)
+
+
+G_MOB = json.load(open(os.path.join(GOLDEN, "mobility_goldens.json")))
+
+
+def mobility_case(fixtures, oracle):
+    """The MobilityTest.jl network and its segment forces as calcSegForce! builds
+    them there (zero FE fields: no PK term): seg-seg plus self force."""
+    g = G_MOB
+    p = g["params"]
+    net = fixtures.make_network(g["loops"], g["slipSystems"], g["range"])
+    k5 = fixtures.consts5(p["coreRad"], p["mu"], p["nu"])
+    seg_force = oracle.segseg_ser(k5, net)
+    F1, F2 = oracle.self_force(k5, np.array([p["coreRad"], p["coreEnergy"], p["nu"]]), net)
+    seg_force[:, 0, :] += F1
+    seg_force[:, 1, :] += F2
+    links = np.asfortranarray(net.segIdx[:, 1:3].T)
+    conn = fixtures.make_connectivity(links, g["maxConnect"])
+    d = p["drag"]
+    mp = np.array([p["sigmaPN"], d["edge"], d["screw"], d["climb"], d["line"]])
+    return net, seg_force, links, conn, mp
+
+
+def test_mobility_bcc_matches_golden(oracle, fixtures):
+    """dlnMobility (BCC), DislocationMobility.jl:16-178, against
+    test/MobilityTest.jl:64-93.  Node forces to 1e-10 relative; velocities at
+    the reference test's own rtol 1e-5: the climb drag (1e10) against the glide
+    drags (1-2) makes the 3×3 solve ill-conditioned."""
+    net, seg_force, links, conn, mp = mobility_case(fixtures, oracle)
+    Fn, Vn = oracle.mobility_bcc(mp, net.coord, net.bVec, links, conn, seg_force, conn.shape[1])
+    gf, gv = np.array(G_MOB["nodeForce"]), np.array(G_MOB["nodeVel"])
+    assert np.abs(Fn.T - gf).max() <= 1e-10 * np.abs(gf).max()
+    assert np.linalg.norm(Vn.T - gv) <= 1e-5 * np.linalg.norm(gv)
+    idx = np.array([4, 1, 11, 4])
+    Fi, Vi = oracle.mobility_bcc(mp, net.coord, net.bVec, links, conn, seg_force, conn.shape[1], idx)
+    assert np.array_equal(Fi, Fn[:, idx - 1]) and np.array_equal(Vi, Vn[:, idx - 1])
+
+
+def test_connectivity_layout(fixtures):
+    """_makeConnect! (DislocationUtil.jl:213-237) on a closed 4-node loop."""
+    links = np.array([[1, 2, 3, 4], [2, 3, 4, 1]])
+    conn = fixtures.make_connectivity(links, 4)
+    assert conn[:, 0].tolist() == [2, 1, 1, 4, 2, 0, 0, 0, 0]
+    assert conn[:, 2].tolist() == [2, 2, 2, 3, 1, 0, 0, 0, 0]
