@@ -25,6 +25,10 @@ precision_131k: the precision-form workload (131,072 segments, f32c force and
        mixed-form σ̃ on the 128^3 grid) with errors against the FP64 kernel on
        sampled segments and points.
 
+collision: detectCollision on the workload network moving with the mobility
+       step's velocities: pair scans/s of the kernels and of the host call, the
+       oracle on a prefix of the network beside it, answers compared.
+
 node_rows: calcSelfForce and dlnMobility (BCC) on the workload network through
        their host-array C-ABI calls, node forces from the timed seg-seg step plus
        the self force: e2e and kernel times, the kernel's algorithmic GB/s, the
@@ -350,6 +354,7 @@ def run_node_rows(pkg, oracle, ctx, net, dln, mat, segseg, reps=5, with_cpu=True
     net.segForce[:, 0, :n] += F1
     net.segForce[:, 1, :n] += F2
     ms_mob, k_mob, (Fn, Vn) = best(lambda: ctx.mobility_bcc(mp, net))
+    net.nodeVel[:, :net.numNode] = Vn
     # Algorithmic bytes: self force reads two nodes, b and the segment row
     # (6 + 3 doubles, 3 int64) and writes 3 doubles per segment; mobility reads
     # per node its coordinates and connectivity row ((1 + 2 * maxConnect) int64)
@@ -382,6 +387,61 @@ def run_node_rows(pkg, oracle, ctx, net, dln, mat, segseg, reps=5, with_cpu=True
         out["mobility_bcc"].update(cpu_ms=cpu_mob, cpu_kind="port", cpu_cores=1,
                                    node_force_bit_equal=bool(np.array_equal(Fn, RF)),
                                    vel_rel_diff_vs_oracle=float(np.linalg.norm(Vn - RV) / np.linalg.norm(RV)))
+    return out
+
+
+def run_collision(pkg, oracle, ctx, net, synth, p, b, cd, reps=5, cpu_target_s=10.0, with_cpu=True):
+    """detectCollision on the workload network (node velocities from the
+    mobility step) through the host-array call: kernel and e2e time as pair
+    scans/s (numSeg (numSeg - 1) / 2 per call, the reference's two-line loop),
+    and beside it the oracle (the reference's serial loops) on a prefix of the
+    network sized to about cpu_target_s, with the GPU answer on that prefix
+    compared field by field."""
+    n = net.numSeg
+    pairs = n * (n - 1) // 2
+    cd2 = cd * cd
+    ctx.detect_collision(cd2, net)
+    ts, ks = [], []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        res, pair = ctx.detect_collision(cd2, net)
+        ts.append(time.perf_counter() - t0)
+        ks.append(ctx.last_kernel_ms)
+    ms_e2e, ms_k = min(ts) * 1e3, min(ks)
+    out = {"segments": n, "collisionDist": cd, "pairs_per_call": pairs,
+           "result": [res[0], res[1], *res[2:8], res[8], res[9]], "pair": pair,
+           "kernel_ms": ms_k, "value": pairs / (ms_k * 1e-3), "unit": "pair scans/s",
+           "e2e": {"ms": ms_e2e, "value": pairs / (ms_e2e * 1e-3),
+                   "h2d_bytes": int(net.numNode * (3 * 8 * 2 + 4 + 8 * net.connectivity.shape[0]) +
+                                    net.links.shape[1] * 16 + n * 24), "d2h_bytes": 96},
+           "timing": "best of %d calls; kernel = CUDA events around all collision kernels" % reps}
+    if not with_cpu:
+        return out
+
+    def prefix(loops):
+        coord, bvec, seg = synth.network_arrays(p[:loops], b[:loops])
+        sub = pkg.DislocationNetwork(coord, bvec, seg, nodeVel=net.nodeVel[:, :loops * 8])
+        return sub
+
+    def ref(sub):
+        return oracle.detect_collision(cd2, sub.coord, sub.nodeVel, sub.label, sub.links, sub.bVec, sub.connectivity,
+                                       sub.numNode, sub.numSeg)
+
+    sub = prefix(256)
+    t0 = time.perf_counter()
+    ref(sub)
+    rate = sub.numSeg * (sub.numSeg - 1) / 2 / max(time.perf_counter() - t0, 1e-6)
+    loops = int(min(p.shape[0], max(256, np.sqrt(2 * rate * cpu_target_s) / 8)))
+    sub = prefix(loops)
+    t0 = time.perf_counter()
+    rres, rpair = ref(sub)
+    dt = time.perf_counter() - t0
+    gres, gpair = ctx.detect_collision(cd2, sub)
+    m = sub.numSeg
+    out["cpu_baseline"] = {"value": m * (m - 1) / 2 / dt, "unit": "pair scans/s", "cores": 1, "kind": "port",
+                           "sample": "the first %d segments (%d loops) of the workload, %.1f s" % (m, loops, dt)}
+    out["parity_prefix"] = {"segments": m, "equal": bool(tuple(gres) == tuple(rres) and gpair == rpair),
+                            "result": [gres[0], gres[1], *gres[2:8], gres[8], gres[9]]}
     return out
 
 
@@ -674,6 +734,10 @@ def main():
                                       dragCoeffs=dict(edge=1.0, screw=2.0, climb=1e10, line=1e-4))
     mat_m = pkg.MaterialParameters(mu=synth.MU, nu=synth.NU, sigmaPN=1e-4)
     node_rows = run_node_rows(pkg, oracle, ctx, net, dln_m, mat_m, out, with_cpu=not args.no_cpu)
+    # Collision detection on the network moving with those velocities:
+    # collisionDist = minSegLen / 2 (the reference's default) with minSegLen =
+    # 20 b, the workload's shortest segment.
+    collision = run_collision(pkg, oracle, ctx, net, synth, p, b, 10.0, with_cpu=not args.no_cpu)
     achieved = flops_per_step / (statistics.mean(ms_kernel) * 1e-3)
     line = {
         "metric": "seg-seg pair interactions/s at 65k segs (FP64 plain vs FP32+surrogate) at stated error",
@@ -706,6 +770,7 @@ def main():
         "sigma_tilde": sigma,
         "batched": batched,
         "node_rows": node_rows,
+        "collision": collision,
         "kernel_ms_per_step": statistics.mean(ms_kernel),
     }
     cs = clocks.summary()

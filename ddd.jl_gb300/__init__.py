@@ -35,6 +35,7 @@ NOALLOC_MAX_SEGMENTS = 4096
 # Every symbol include/ddd_gb300.h declares.
 EXPORTED_SYMBOLS = (
     "ddd_create", "ddd_destroy", "ddd_last_error", "ddd_last_kernel_ms", "ddd_version",
+    "ddd_detect_collision", "ddd_minimum_distance",
     "ddd_segseg_force", "ddd_segseg_force_inplace", "ddd_sigma_tilde",
     "ddd_segseg_force_device", "ddd_sigma_tilde_device", "ddd_set_mode", "ddd_get_mode", "ddd_probe_fma_peak",
     "ddd_segseg_force_device_noalloc",
@@ -91,6 +92,13 @@ class ddd_self_params(ctypes.Structure):
 class ddd_mob_params(ctypes.Structure):
     _fields_ = [("sigmaPN", ctypes.c_double), ("edgeDrag", ctypes.c_double), ("screwDrag", ctypes.c_double),
                 ("climbDrag", ctypes.c_double), ("lineDrag", ctypes.c_double)]
+
+
+class ddd_collision(ctypes.Structure):
+    _fields_ = [("collision", ctypes.c_int32), ("type", ctypes.c_int32), ("n1s1", ctypes.c_int64),
+                ("n2s1", ctypes.c_int64), ("n1s2", ctypes.c_int64), ("n2s2", ctypes.c_int64), ("s1", ctypes.c_int64),
+                ("s2", ctypes.c_int64), ("L1", ctypes.c_double), ("L2", ctypes.c_double),
+                ("pairDistSq", ctypes.c_double), ("pairL1", ctypes.c_double), ("pairL2", ctypes.c_double)]
 
 
 class ddd_sur_opts(ctypes.Structure):
@@ -192,6 +200,10 @@ def library():
                     _i64, _i64, _ip, _i64, _dp, _dp]
         L.ddd_mobility_bcc.argtypes = mob_args
         L.ddd_mobility_bcc_inplace.argtypes = mob_args + [_i64]
+        L.ddd_detect_collision.argtypes = [_vp, ctypes.c_double, _dp, _i64, _dp, _i64, ctypes.POINTER(ctypes.c_int32),
+                                           _i64, _ip, _i64, _dp, _i64, _ip, _i64, _i64, _i64, _i64, _ip, _i64,
+                                           ctypes.POINTER(ddd_collision)]
+        L.ddd_minimum_distance.argtypes = [_vp, _dp, _i64, _dp]
         L.ddd_set_mode.argtypes = [_vp, ctypes.c_int]
         L.ddd_get_mode.argtypes = [_vp]
         L.ddd_probe_fma_peak.argtypes = [_vp, ctypes.c_int, _dp]
@@ -227,7 +239,7 @@ class DislocationParameters:
     """The DislocationParameters fields this path reads (src/Type/DislocationConstructor.jl:55-105)."""
 
     def __init__(self, *, coreRad=1.0, coreRadMag=1.0, coreEnergy=None, minSegLen=None, maxSegLen=None,
-                 parCPU=False, parGPU=True, dragCoeffs=None, **other):
+                 collisionDist=None, parCPU=False, parGPU=True, dragCoeffs=None, **other):
         self.dragCoeffs = dict(edge=1.0, screw=2.0, climb=1e9, line=0.0)
         if dragCoeffs:
             self.dragCoeffs.update({k: float(v) for k, v in dict(dragCoeffs).items()})
@@ -238,6 +250,8 @@ class DislocationParameters:
         self.coreRadMag = float(coreRadMag)
         self.minSegLen = 2 * self.coreRad if minSegLen is None else float(minSegLen)
         self.maxSegLen = 20 * self.coreRad if maxSegLen is None else float(maxSegLen)
+        self.collisionDist = self.minSegLen / 2 if collisionDist is None else float(collisionDist)
+        self.collisionDistSq = self.collisionDist * self.collisionDist
         self.parCPU = bool(parCPU)
         self.parGPU = bool(parGPU)
         for k, v in other.items():
@@ -250,13 +264,15 @@ class DislocationNetwork:
     coord (3×nodeBuf), bVec (3×linkBuf), segIdx (linkBuf×3; link, node1, node2;
     1-based), extSeg (linkBuf), segForce (3×2×linkBuf), numSeg; for the
     mobility also links (2×linkBuf), connectivity ((1+2 maxConnect)×nodeBuf),
-    numNode, nodeForce and nodeVel (3×nodeBuf).  links defaults to segIdx's
-    node columns and connectivity to the one _makeConnect! builds from it.
+    numNode, nodeForce and nodeVel (3×nodeBuf); for collision detection also
+    label (nodeBuf int32, the nodeTypeDln values; default 1 = intMobDln).
+    links defaults to segIdx's node columns and connectivity to the one
+    _makeConnect! builds from it.
     Stored Fortran-ordered, which is the Julia memory image.
     """
 
     def __init__(self, coord, bVec, segIdx, numSeg=None, extSeg=None, segForce=None, links=None,
-                 connectivity=None, numNode=None, nodeForce=None, nodeVel=None, maxConnect=4):
+                 connectivity=None, numNode=None, nodeForce=None, nodeVel=None, maxConnect=4, label=None):
         self.coord = np.asfortranarray(coord, dtype=np.float64)
         self.bVec = np.asfortranarray(bVec, dtype=np.float64)
         self.segIdx = np.asfortranarray(segIdx, dtype=np.int64)
@@ -276,6 +292,8 @@ class DislocationNetwork:
                           else np.asfortranarray(nodeForce, dtype=np.float64))
         self.nodeVel = (np.zeros((3, nodes), np.float64, order="F") if nodeVel is None
                         else np.asfortranarray(nodeVel, dtype=np.float64))
+        self.label = (np.ones(nodes, np.int32) if label is None
+                      else np.ascontiguousarray(np.asarray(label).astype(np.int32)))
 
 
 def make_connectivity(links, num_node, max_connect=4):
@@ -468,6 +486,36 @@ class Context:
                 conn.shape[1], sf.ctypes.data_as(_dp), sf.shape[2], network.numNode,
                 None if idx is None else idx.ctypes.data_as(_ip), 0 if idx is None else len(idx)]
         return args, keep
+
+    def detect_collision(self, collision_dist_sq, network, skip_segs=()):
+        """detectCollision: the reference's 10-tuple and a dict with the reported
+        pair's own distSq, L1 and L2."""
+        net = network
+        sk = np.ascontiguousarray(np.asarray(list(skip_segs), np.int64).reshape(-1, 2))
+        for name in ("coord", "nodeVel", "bVec", "links", "connectivity"):
+            a = getattr(net, name)
+            if not a.flags.f_contiguous:
+                raise ValueError(name + " must be Fortran-ordered")
+        lab = np.ascontiguousarray(net.label, np.int32)
+        r = ddd_collision()
+        self._check(self._L.ddd_detect_collision(
+            self._h, float(collision_dist_sq), net.coord.ctypes.data_as(_dp), net.coord.shape[1],
+            net.nodeVel.ctypes.data_as(_dp), net.nodeVel.shape[1], lab.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+            lab.shape[0], net.links.ctypes.data_as(_ip), net.links.shape[1], net.bVec.ctypes.data_as(_dp),
+            net.bVec.shape[1], net.connectivity.ctypes.data_as(_ip), net.connectivity.shape[0],
+            net.connectivity.shape[1], net.numNode, net.links.shape[1] if net.numSeg is None else net.numSeg,
+            sk.ctypes.data_as(_ip), sk.shape[0], ctypes.byref(r)))
+        res = (bool(r.collision), ("null", "hinge", "twoLine")[r.type], r.n1s1, r.n2s1, r.n1s2, r.n2s2, r.s1, r.s2,
+               r.L1, r.L2)
+        return res, {"distSq": r.pairDistSq, "L1": r.pairL1, "L2": r.pairL2}
+
+    def minimum_distance(self, pts):
+        """minimumDistance for pts (3 × 8 × n): 4 × n (distSq, dDistSqDt, L1, L2)."""
+        pts = np.require(pts, np.float64, ["F"])
+        n = pts.shape[2]
+        out = np.zeros((4, n), np.float64, order="F")
+        self._check(self._L.ddd_minimum_distance(self._h, pts.ctypes.data_as(_dp), n, out.ctypes.data_as(_dp)))
+        return out
 
     @property
     def last_kernel_ms(self):
@@ -904,6 +952,23 @@ def dlnMobility_inplace(dlnParams, matParams, network, idx=None):
     """dlnMobility! (DislocationMobility.jl:186-341): writes network.nodeForce and nodeVel."""
     get_context().mobility_bcc_inplace(mob_params_of(dlnParams, matParams), network, idx)
     return network
+
+
+def detectCollision(dlnParams, network, skipSegs=()):
+    """detectCollision (DislocationTopologyCollision.jl:1-221): (collision,
+    collisionType, n1s1, n2s1, n1s2, n2s2, s1, s2, L1, L2), collisionType one of
+    "null", "hinge", "twoLine" (the reference's symbols).  L1, L2 are the
+    reference's: those of the last pair it evaluated."""
+    return get_context().detect_collision(dlnParams.collisionDistSq, network, skipSegs)[0]
+
+
+def minimumDistance(x0, x1, y0, y1, vx0, vx1, vy0, vy1):
+    """minimumDistance (Misc.jl:314-367) for one pair of segments (3-vectors) or
+    n pairs (3 × n arrays): (distSq, dDistSqDt, L1, L2)."""
+    arrs = [np.asarray(a, np.float64).reshape(3, -1, order="F") for a in (x0, x1, y0, y1, vx0, vx1, vy0, vy1)]
+    out = get_context().minimum_distance(np.stack(arrs, axis=1))
+    single = all(np.ndim(a) == 1 for a in (x0, x1, y0, y1, vx0, vx1, vy0, vy1))
+    return tuple(float(v[0]) for v in out) if single else tuple(out)
 
 
 def calc_σTilde(x0, dlnParams, matParams, network, idx=None):

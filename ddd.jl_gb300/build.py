@@ -29,6 +29,7 @@ VARIANTS = {
     "surrogate_force.cu": [("", ["--fmad=false"])],
     "self_force.cu": [("", ["--fmad=false"])],
     "mobility.cu": [("", ["--fmad=false"])],
+    "collision.cu": [("", ["--fmad=false"])],
 }
 
 

@@ -2,6 +2,8 @@
 // sequencing.  Declared in include/ddd_gb300.h.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -55,6 +57,8 @@ struct ddd_ctx {
   std::string err;
   DevBuf coord, bvec, segidx, ext, soa, soadf, skip, partial, out, rows, x0, sigma, counters, probe, errflag;
   DevBuf links, conn, segforce;  // mobility inputs
+  DevBuf vel, label, skippairs;  // collision inputs
+  ddd::CollisionPlan* coll = nullptr;
   std::vector<double> hostTmp;
   double lastKernelMs = 0.0;  // device time of the last self-force / mobility kernel
 };
@@ -306,7 +310,8 @@ void ddd_destroy(ddd_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  for (DevBuf* b : {&c->links, &c->conn, &c->segforce}) b->release();
+  for (DevBuf* b : {&c->links, &c->conn, &c->segforce, &c->vel, &c->label, &c->skippairs}) b->release();
+  if (c->coll) ddd::collision_plan_destroy(c->coll);
   for (DevBuf* b : {&c->coord, &c->bvec, &c->segidx, &c->ext, &c->soa, &c->soadf, &c->skip, &c->partial, &c->out, &c->rows,
                     &c->x0, &c->sigma, &c->counters, &c->probe, &c->errflag})
     b->release();
@@ -921,6 +926,135 @@ int ddd_probe_fma_peak(ddd_ctx* ctx, int precision, double* flops_per_s) {
     if (rep > 0 && ms < best) best = ms;
   }
   *flops_per_s = 2.0 * 8.0 * (double)iters * (double)threads * (double)blocks / (best * 1e-3);
+  return DDD_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int ddd_detect_collision(ddd_ctx* ctx, double collisionDistSq, const double* coord, int64_t coordCols,
+                         const double* nodeVel, int64_t nodeVelCols, const int32_t* label, int64_t labelLen,
+                         const int64_t* links, int64_t linkCols, const double* bVec, int64_t bVecCols,
+                         const int64_t* connectivity, int64_t ldConn, int64_t connCols, int64_t numNode,
+                         int64_t numSeg, const int64_t* skipSegs, int64_t nSkip, ddd_collision* out) {
+  if (!ctx) return DDD_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (!out) return fail(ctx, DDD_EINVAL, "out is NULL");
+  *out = ddd_collision{};
+  if (numNode < 0 || numSeg < 0 || coordCols < 0 || nodeVelCols < 0 || labelLen < 0 || linkCols < 0 ||
+      bVecCols < 0 || connCols < 0 || nSkip < 0)
+    return fail(ctx, DDD_EINVAL, "negative size");
+  if (numNode > coordCols || numNode > nodeVelCols || numNode > labelLen || numNode > connCols)
+    return fail(ctx, DDD_EINVAL, "numNode exceeds coord / nodeVel / label / connectivity");
+  if (numSeg > linkCols || numSeg > bVecCols) return fail(ctx, DDD_EINVAL, "numSeg exceeds links / bVec");
+  if (ldConn < 1 || ldConn % 2 == 0) return fail(ctx, DDD_EINVAL, "connectivity must have 1 + 2 maxConnect rows");
+  if (numNode >= INT32_MAX || numSeg >= INT32_MAX) return fail(ctx, DDD_ETOOBIG, "more than 2^31 - 1 nodes or links");
+  if (numNode == 0) return DDD_OK;
+  if (!coord || !nodeVel || !label || !links || !connectivity || (numSeg > 0 && !bVec) || (nSkip > 0 && !skipSegs))
+    return fail(ctx, DDD_EINVAL, "network array is NULL");
+  char buf[160];
+  // Nodes: finite coordinates and velocities, their box; connections of the
+  // mobile nodes (the ones the hinge loop reads) in range.
+  double box[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+  double maxAbs = 0.0;
+  for (int64_t i = 0; i < numNode; ++i) {
+    for (int k = 0; k < 3; ++k) {
+      const double x = coord[3 * i + k], v = nodeVel[3 * i + k];
+      if (!std::isfinite(x) || !std::isfinite(v)) {
+        snprintf(buf, sizeof buf, "node %lld: non-finite coordinate or velocity", (long long)(i + 1));
+        return fail(ctx, DDD_ENONFINITE, buf);
+      }
+      box[k] = std::min(box[k], x);
+      box[3 + k] = std::max(box[3 + k], x);
+      maxAbs = std::max(maxAbs, std::fabs(x));
+    }
+    if (label[i] != 1 && label[i] != 3) continue;
+    const int64_t* cn = connectivity + ldConn * i;
+    if (cn[0] < 0 || 2 * cn[0] + 1 > ldConn) {
+      snprintf(buf, sizeof buf, "node %lld: %lld connections exceed the connectivity rows", (long long)(i + 1),
+               (long long)cn[0]);
+      return fail(ctx, DDD_ERANGE, buf);
+    }
+    for (int64_t c = 1; c <= cn[0]; ++c) {
+      const int64_t link = cn[2 * c - 1], col = cn[2 * c];
+      if (link < 1 || link > linkCols || (col != 1 && col != 2)) {
+        snprintf(buf, sizeof buf, "node %lld: connection %lld = (link %lld, column %lld) out of range",
+                 (long long)(i + 1), (long long)c, (long long)link, (long long)col);
+        return fail(ctx, DDD_ERANGE, buf);
+      }
+      const int64_t other = links[2 * (link - 1) + (2 - col)];
+      if (other < 1 || other > numNode) {
+        snprintf(buf, sizeof buf, "link %lld: node %lld outside 1..numNode=%lld", (long long)link, (long long)other,
+                 (long long)numNode);
+        return fail(ctx, DDD_ERANGE, buf);
+      }
+    }
+  }
+  for (int64_t i = 0; i < numSeg; ++i)
+    for (int k = 0; k < 2; ++k)
+      if (links[2 * i + k] < 1 || links[2 * i + k] > numNode) {
+        snprintf(buf, sizeof buf, "links[%d, %lld] = %lld outside 1..numNode=%lld", k + 1, (long long)(i + 1),
+                 (long long)links[2 * i + k], (long long)numNode);
+        return fail(ctx, DDD_ERANGE, buf);
+      }
+  // skipSegs as canonical (a <= b) sorted pairs: the reference matches either order.
+  std::vector<std::pair<int64_t, int64_t>> sk((size_t)nSkip);
+  for (int64_t q = 0; q < nSkip; ++q)
+    sk[q] = {std::min(skipSegs[2 * q], skipSegs[2 * q + 1]), std::max(skipSegs[2 * q], skipSegs[2 * q + 1])};
+  std::sort(sk.begin(), sk.end());
+  sk.erase(std::unique(sk.begin(), sk.end()), sk.end());
+  std::vector<int64_t> skFlat(2 * sk.size() + 2);
+  for (size_t q = 0; q < sk.size(); ++q) skFlat[2 * q] = sk[q].first, skFlat[2 * q + 1] = sk[q].second;
+
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  if (!ctx->coll) ctx->coll = ddd::collision_plan_create();
+  cudaStream_t st = ctx->stream;
+  const size_t cB = (size_t)numNode * 3 * 8, lB = (size_t)linkCols * 2 * 8, bB = (size_t)std::max<int64_t>(numSeg, 1) * 3 * 8;
+  const size_t nB = (size_t)ldConn * numNode * 8, kB = skFlat.size() * 8;
+  CK(ctx->coord.ensure(cB), "alloc coord");
+  CK(ctx->vel.ensure(cB), "alloc nodeVel");
+  CK(ctx->label.ensure((size_t)numNode * 4), "alloc label");
+  CK(ctx->links.ensure(lB), "alloc links");
+  CK(ctx->bvec.ensure(bB), "alloc bVec");
+  CK(ctx->conn.ensure(nB), "alloc connectivity");
+  CK(ctx->skippairs.ensure(kB), "alloc skipSegs");
+  CK(cudaMemcpyAsync(ctx->coord.p, coord, cB, cudaMemcpyHostToDevice, st), "copy coord");
+  CK(cudaMemcpyAsync(ctx->vel.p, nodeVel, cB, cudaMemcpyHostToDevice, st), "copy nodeVel");
+  CK(cudaMemcpyAsync(ctx->label.p, label, (size_t)numNode * 4, cudaMemcpyHostToDevice, st), "copy label");
+  CK(cudaMemcpyAsync(ctx->links.p, links, lB, cudaMemcpyHostToDevice, st), "copy links");
+  if (numSeg > 0) CK(cudaMemcpyAsync(ctx->bvec.p, bVec, (size_t)numSeg * 3 * 8, cudaMemcpyHostToDevice, st), "copy bVec");
+  CK(cudaMemcpyAsync(ctx->conn.p, connectivity, nB, cudaMemcpyHostToDevice, st), "copy connectivity");
+  CK(cudaMemcpyAsync(ctx->skippairs.p, skFlat.data(), kB, cudaMemcpyHostToDevice, st), "copy skipSegs");
+  ddd::CollisionOut r{};
+  CK(ddd::collision_detect(ctx->coll, collisionDistSq, ctx->coord.as<double>(), ctx->vel.as<double>(),
+                           ctx->label.as<int32_t>(), ctx->links.as<int64_t>(), ctx->bvec.as<double>(),
+                           ctx->conn.as<int64_t>(), ldConn, numNode, numSeg, ctx->skippairs.as<int64_t>(),
+                           (int64_t)sk.size(), box, maxAbs, &r, ctx->ev[1], ctx->ev[2], st),
+     "detect_collision");
+  ctx->lastKernelMs = elapsed(ctx->ev[1], ctx->ev[2]);
+  out->collision = r.collision;
+  out->type = r.type;
+  out->n1s1 = r.n1s1, out->n2s1 = r.n2s1, out->n1s2 = r.n1s2, out->n2s2 = r.n2s2, out->s1 = r.s1, out->s2 = r.s2;
+  out->L1 = r.L1, out->L2 = r.L2;
+  out->pairDistSq = r.pairDistSq, out->pairL1 = r.pairL1, out->pairL2 = r.pairL2;
+  return DDD_OK;
+}
+
+int ddd_minimum_distance(ddd_ctx* ctx, const double* pts, int64_t n, double* out) {
+  if (!ctx) return DDD_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (n < 0) return fail(ctx, DDD_EINVAL, "negative size");
+  if (n == 0) return DDD_OK;
+  if (!pts || !out) return fail(ctx, DDD_EINVAL, "array is NULL");
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  cudaStream_t st = ctx->stream;
+  CK(ctx->x0.ensure((size_t)n * 24 * 8), "alloc points");
+  CK(ctx->out.ensure((size_t)n * 4 * 8), "alloc output");
+  CK(cudaMemcpyAsync(ctx->x0.p, pts, (size_t)n * 24 * 8, cudaMemcpyHostToDevice, st), "copy points");
+  CK(ddd::launch_minimum_distance(ctx->x0.as<double>(), n, ctx->out.as<double>(), st), "minimum_distance");
+  CK(cudaMemcpyAsync(out, ctx->out.p, (size_t)n * 4 * 8, cudaMemcpyDeviceToHost, st), "copy output");
+  CK(cudaStreamSynchronize(st), "minimum_distance");
   return DDD_OK;
 }
 

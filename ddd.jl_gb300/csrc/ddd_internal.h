@@ -84,6 +84,28 @@ cudaError_t launch_mobility_bcc(const MobK& P, const double* coord, const double
                                 const int64_t* conn, int64_t ldConn, const double* segForce, const int64_t* rows,
                                 int64_t n, double* nodeForce, double* nodeVel, cudaStream_t st);
 
+// collision.cu: detectCollision and minimumDistance, strict FP64.  type: 0
+// none, 1 hinge, 2 two-line; indices 1-based; L1, L2 as the reference returns
+// them (its last evaluated pair), pair* of the reported pair.
+struct CollisionOut {
+  int32_t collision, type;
+  int64_t n1s1, n2s1, n1s2, n2s2, s1, s2;
+  double L1, L2, pairDistSq, pairL1, pairL2;
+};
+struct CollisionPlan;
+CollisionPlan* collision_plan_create();
+void collision_plan_destroy(CollisionPlan* p);
+// Device arrays in the network's layout (coord / vel / bVec 3 x n, links 2 x n
+// and conn ldConn x n 1-based); skip: nSkip canonical (a <= b), sorted pairs;
+// box: min xyz, max xyz of the node coordinates; maxAbs: max |coordinate|.
+// Writes *out (host) and synchronises st.
+cudaError_t collision_detect(CollisionPlan* P, double cd2, const double* coord, const double* vel, const int32_t* label,
+                             const int64_t* links, const double* bVec, const int64_t* conn, int64_t ldConn,
+                             int64_t numNode, int64_t numSeg, const int64_t* skip, int64_t nSkip, const double box[6],
+                             double maxAbs, CollisionOut* out, cudaEvent_t e0, cudaEvent_t e1, cudaStream_t st);
+// pts: 3 x 8 x n (x0, x1, y0, y1, vx0, vx1, vy0, vy1), out 4 x n.
+cudaError_t launch_minimum_distance(const double* pts, int64_t n, double* out, cudaStream_t st);
+
 // ddd_api.cu: context accessors for the other C-ABI files.
 int ctx_device(const ddd_ctx* c);
 

@@ -14,7 +14,7 @@ module DDDGB300
 export calcSegSegForceGPU, calcSegSegForceGPU!, calc_σTildeGPU, calc_σTildeGPU!
 export calcSelfForceGPU, calcSelfForceGPU!, calcSegForceGPU, calcSegForceGPU!
 export Surrogate, loadSurrogate, calcSegSegForceSurrogateGPU
-export dlnMobilityGPU, dlnMobilityGPU!
+export dlnMobilityGPU, dlnMobilityGPU!, detectCollisionGPU, minimumDistanceGPU
 
 const libddd = joinpath(@__DIR__, "..", "libddd_gb300.so")
 
@@ -260,6 +260,58 @@ function dlnMobilityGPU!(dlnParams, matParams, network, idx = nothing)
     end
     check(rc)
     return nothing
+end
+
+# ---------------------------------------------------------------------------
+# Collision detection (DislocationTopologyCollision.jl:1-221) and
+# minimumDistance (Misc.jl:314-367).
+
+struct DDDCollision
+    collision::Int32
+    type::Int32
+    n1s1::Int64
+    n2s1::Int64
+    n1s2::Int64
+    n2s2::Int64
+    s1::Int64
+    s2::Int64
+    L1::Float64
+    L2::Float64
+    pairDistSq::Float64
+    pairL1::Float64
+    pairL2::Float64
+end
+
+# detectCollision: the reference's 10-tuple (network.label is Int32-backed).
+function detectCollisionGPU(dlnParams, network, skipSegs = Vector{Tuple{Int, Int}}())
+    r = Ref{DDDCollision}()
+    sk = collect(Tuple{Int, Int}, skipSegs)
+    coord, nodeVel, label, links, bVec, conn = network.coord, network.nodeVel, network.label, network.links,
+                                               network.bVec, network.connectivity
+    GC.@preserve coord nodeVel label links bVec conn sk begin
+        rc = ccall((:ddd_detect_collision, libddd), Cint,
+            (Ptr{Cvoid}, Float64, Ptr{Float64}, Int64, Ptr{Float64}, Int64, Ptr{Cvoid}, Int64, Ptr{Int64}, Int64,
+             Ptr{Float64}, Int64, Ptr{Int64}, Int64, Int64, Int64, Int64, Ptr{Cvoid}, Int64, Ref{DDDCollision}),
+            context(), dlnParams.collisionDistSq, coord, size(coord, 2), nodeVel, size(nodeVel, 2), pointer(label),
+            length(label), links, size(links, 2), bVec, size(bVec, 2), conn, size(conn, 1), size(conn, 2),
+            network.numNode[1], network.numSeg[1], pointer(sk), length(sk), r)
+    end
+    check(rc)
+    c = r[]
+    return c.collision == 1, (:null, :hinge, :twoLine)[c.type + 1], c.n1s1, c.n2s1, c.n1s2, c.n2s2, c.s1, c.s2,
+           c.L1, c.L2
+end
+
+# minimumDistance for one pair of segments.
+function minimumDistanceGPU(x0, x1, y0, y1, vx0, vx1, vy0, vy1)
+    pts = Float64[x0; x1; y0; y1; vx0; vx1; vy0; vy1]
+    out = zeros(4)
+    GC.@preserve pts out begin
+        rc = ccall((:ddd_minimum_distance, libddd), Cint, (Ptr{Cvoid}, Ptr{Float64}, Int64, Ptr{Float64}),
+                   context(), pts, 1, out)
+    end
+    check(rc)
+    return out[1], out[2], out[3], out[4]
 end
 
 # ---------------------------------------------------------------------------

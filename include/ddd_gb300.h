@@ -40,7 +40,7 @@ extern "C" {
 #define DDD_ENONFINITE (-3) /* a non-finite coordinate / Burgers vector / constant, or a zero-length segment */
 #define DDD_EDEVICE (-4)    /* CUDA error (message in ddd_last_error) */
 #define DDD_ENOMEM (-5)     /* device allocation failed */
-#define DDD_ETOOBIG (-6)    /* more segments than ddd_segseg_force_device_noalloc accepts */
+#define DDD_ETOOBIG (-6)    /* input larger than the entry point accepts (noalloc segment limit, 2^31 nodes) */
 #define DDD_ETIMEOUT (-7)   /* a bounded wait inside a kernel gave up (the kernel returned early) */
 
 typedef struct ddd_ctx ddd_ctx;
@@ -197,6 +197,37 @@ int ddd_mobility_bcc_inplace(ddd_ctx* ctx, const ddd_mob_params* mp, const doubl
                              const int64_t* connectivity, int64_t ldConn, int64_t connCols, const double* segForce,
                              int64_t segForceCols, int64_t numNode, const int64_t* idx, int64_t nIdx,
                              double* nodeForce, double* nodeVel, int64_t nodeCols);
+
+/* detectCollision(dlnParams, network, skipSegs) —
+ * src/Processing/DislocationTopologyCollision.jl:1-221 (minimumDistance:
+ * src/Misc/Misc.jl:314-367).  Hinges (pairs of links at one mobile node) are
+ * checked first, then every pair of unconnected segments whose four nodes are
+ * mobile (label intMobDln = 1 or srfMobDln = 3); the reported pair is the one
+ * with the largest 1/distSq among pairs closer than collisionDist and
+ * approaching (dDistSqDt < -eps), the first in the reference's loop order on a
+ * tie.  label: numNode int32 (the nodeTypeDln enum); nodeVel 3 × nodeVelCols;
+ * links 2 × linkCols, connectivity ldConn × connCols (1-based); skipSegs: nSkip
+ * (s1, s2) link pairs (Vector{Tuple{Int,Int}}), either order.  L1, L2 are what
+ * the reference returns: the values of ITS LAST minimumDistance call (of the
+ * last pair its loops evaluated), which need not be the reported pair;
+ * pairDistSq, pairL1 and pairL2 belong to the reported pair (an extension).
+ * Non-finite coordinates or velocities: DDD_ENONFINITE. */
+typedef struct ddd_collision {
+  int32_t collision; /* 1 when a collision was found */
+  int32_t type;      /* 0 :null, 1 :hinge, 2 :twoLine */
+  int64_t n1s1, n2s1, n1s2, n2s2, s1, s2; /* 1-based node and link numbers; 0 when none */
+  double L1, L2;
+  double pairDistSq, pairL1, pairL2;
+} ddd_collision;
+int ddd_detect_collision(ddd_ctx* ctx, double collisionDistSq, const double* coord, int64_t coordCols,
+                         const double* nodeVel, int64_t nodeVelCols, const int32_t* label, int64_t labelLen,
+                         const int64_t* links, int64_t linkCols, const double* bVec, int64_t bVecCols,
+                         const int64_t* connectivity, int64_t ldConn, int64_t connCols, int64_t numNode,
+                         int64_t numSeg, const int64_t* skipSegs, int64_t nSkip, ddd_collision* out);
+/* minimumDistance(x0, x1, y0, y1, vx0, vx1, vy0, vy1) for n pairs at once:
+ * pts 3 × 8 × n (the eight points of each pair), out 4 × n (distSq,
+ * dDistSqDt, L1, L2). */
+int ddd_minimum_distance(ddd_ctx* ctx, const double* pts, int64_t n, double* out);
 
 /* calc_σTilde(x0, dlnParams, matParams, network, idx = nothing) and
  * calc_σTilde!(σ, x0, ...) — src/Processing/DislocationFEM.jl:24-84, kernel

@@ -303,6 +303,37 @@ void oracle_mobility_bcc(const double* mp, const double* coord, const double* bV
   }
 }
 
+// minimumDistance (Misc.jl:314-367) for n segment pairs: pts is 3 × 8 × n
+// (x0, x1, y0, y1, vx0, vx1, vy0, vy1 per pair), out 4 × n (distSq,
+// dDistSqDt, L1, L2).
+void oracle_minimum_distance(const double* pts, int64_t n, double* out) {
+  for (int64_t q = 0; q < n; ++q) {
+    V3<double> v[8];
+    for (int k = 0; k < 8; ++k) v[k] = {pts[24 * q + 3 * k], pts[24 * q + 3 * k + 1], pts[24 * q + 3 * k + 2]};
+    const MinDist<double> m = minimum_distance(v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7]);
+    out[4 * q] = m.distSq;
+    out[4 * q + 1] = m.dDistSqDt;
+    out[4 * q + 2] = m.L1;
+    out[4 * q + 3] = m.L2;
+  }
+}
+
+// detectCollision (DislocationTopologyCollision.jl:1-221).  iout (8): collision,
+// type (0 null, 1 hinge, 2 twoLine), n1s1, n2s1, n1s2, n2s2, s1, s2; dout (5):
+// L1, L2 (the reference's return values), pairDistSq, pairL1, pairL2.  skip holds
+// nSkip (s1, s2) link pairs.
+void oracle_detect_collision(double collisionDistSq, const double* coord, const double* nodeVel, const int32_t* label,
+                             const int64_t* links, const double* bVec, const int64_t* conn, int64_t ldConn,
+                             int64_t numNode, int64_t numSeg, const int64_t* skip, int64_t nSkip, int64_t* iout,
+                             double* dout) {
+  const Collision r = detect_collision<double>(collisionDistSq, coord, nodeVel, label, links, bVec, conn, ldConn,
+                                               numNode, numSeg, skip, nSkip);
+  const int64_t iv[8] = {r.collision, r.type, r.n1s1, r.n2s1, r.n1s2, r.n2s2, r.s1, r.s2};
+  const double dv[5] = {r.L1, r.L2, r.pairDistSq, r.pairL1, r.pairL2};
+  for (int k = 0; k < 8; ++k) iout[k] = iv[k];
+  for (int k = 0; k < 5; ++k) dout[k] = dv[k];
+}
+
 // PK forces (σ̂ b) × (n2 - n1) of the segments in idx (or 1:numSeg) from the
 // stresses sigmaHat (6 × n, one per entry, at the segment midpoints): PK
 // (3 × n, overwritten; 0 where extSeg[k]).

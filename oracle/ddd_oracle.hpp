@@ -22,10 +22,15 @@
 //   src/Processing/DislocationForces.jl:1444-1478 ParSegSegInteg
 //   src/Processing/DislocationForces.jl:1480-1561 SegSegInteg
 //   src/Processing/DislocationFEM.jl:86-303       _calc_σTilde!
+//   src/Misc/Misc.jl:314-367                      minimumDistance
+//   src/Processing/DislocationTopologyCollision.jl:1-221  detectCollision
 #pragma once
 #include <cmath>
 #include <cstdint>
 #include <limits>
+#include <utility>
+#include <vector>
+#include <algorithm>
 
 namespace ddd_oracle {
 
@@ -927,6 +932,176 @@ inline void sigma_tilde_point(const Consts<T>& K, const V3<T>& b, const V3<T>& n
   sig[3] = sig[3] + (I_03xy * s_03 + I_13xy * s_13 + I_05xy * s_05 + I_15xy * s_15 + I_25xy * s_25);
   sig[4] = sig[4] + (I_03xz * s_03 + I_13xz * s_13 + I_05xz * s_05 + I_15xz * s_15 + I_25xz * s_25);
   sig[5] = sig[5] + (I_03yz * s_03 + I_13yz * s_13 + I_05yz * s_05 + I_15yz * s_15 + I_25yz * s_25);
+}
+
+// ---------------------------------------------------------------------------
+// minimumDistance (Misc.jl:314-367): closest points of x0→x1 and y0→y1 as
+// fractions L1, L2 along each, the squared distance there and its rate of
+// change from the node velocities.  Kept as the reference writes it, including
+// the near-parallel branch's L1 = floor(idx / 2), which gives (L1, L2) = (1, 1)
+// for the second candidate (y1 - x0) — MiscTest.jl:135-140 holds that result.
+template <class T> struct MinDist {
+  T distSq, dDistSqDt, L1, L2;
+};
+
+template <class T> inline T clamp01(T x) { return x > T(1) ? T(1) : (x < T(0) ? T(0) : x); }
+
+template <class T>
+inline MinDist<T> minimum_distance(const V3<T>& x0, const V3<T>& x1, const V3<T>& y0, const V3<T>& y1,
+                                   const V3<T>& vx0, const V3<T>& vx1, const V3<T>& vy0, const V3<T>& vy1) {
+  using std::abs;
+  const T eps = std::numeric_limits<T>::epsilon();
+  const V3<T> seg1 = x1 - x0, seg2 = y1 - y0, vseg1 = vx1 - vx0, vseg2 = vy1 - vy0;
+  const T A = dot(seg1, seg1);
+  const T B = dot(T(2) * seg1, x0 - y0);
+  const T C = dot(T(2) * seg1, seg2);
+  const T D = dot(T(2) * seg2, y0 - x0);
+  const T E = dot(seg2, seg2);
+  const T G = C * C - T(4) * A * E;
+  T L1, L2;
+  if (A < eps) {
+    L1 = T(0);
+    L2 = E < eps ? T(0) : -D / E / T(2);
+  } else if (E < eps) {
+    L2 = T(0);
+    L1 = -B / A / T(2);
+  } else if (abs(G) < eps) {
+    const T d[4] = {dot(y0 - x0, y0 - x0), dot(y1 - x0, y1 - x0), dot(y0 - x1, y0 - x1), dot(y1 - x1, y1 - x1)};
+    int idx = 1;  // findmin: the first minimum (a NaN counts as the smallest)
+    for (int k = 1; k < 4 && !std::isnan(d[idx - 1]); ++k)
+      if (std::isnan(d[k]) || d[k] < d[idx - 1]) idx = k + 1;
+    L1 = std::floor(T(idx) / T(2));
+    L2 = T((idx - 1) % 2);
+  } else {
+    L2 = (T(2) * A * D + B * C) / G;
+    L1 = (C * L2 - B) / A / T(2);
+  }
+  L1 = clamp01(L1);
+  L2 = clamp01(L2);
+  const V3<T> P = x0 + seg1 * L1 - y0 - seg2 * L2;
+  const V3<T> V = vx0 + vseg1 * L1 - vy0 - vseg2 * L2;
+  return {dot(P, P), T(2) * dot(V, P), L1, L2};
+}
+
+// detectCollision (DislocationTopologyCollision.jl:1-221).  type: 0 :null,
+// 1 :hinge, 2 :twoLine.  Indices are 1-based (0 when there is no collision).
+// L1, L2 are what the reference returns: the variables its loops overwrite on
+// every minimumDistance call, i.e. those of the LAST pair it evaluated (in the
+// twoLine pass if that pass ran and evaluated a pair, else in the hinge pass),
+// not necessarily those of the reported pair; pairDistSq, pairL1, pairL2
+// belong to the reported pair.
+struct Collision {
+  int32_t collision, type;
+  int64_t n1s1, n2s1, n1s2, n2s2, s1, s2;
+  double L1, L2, pairDistSq, pairL1, pairL2;
+};
+
+inline bool mobile_label(int32_t l) { return l == 1 || l == 3; }  // intMobDln, srfMobDln
+
+// The reference scans skipSegs linearly for (a, b) in either order; the same
+// test as a lookup in the canonical (min, max) pairs, sorted.
+struct SkipSet {
+  std::vector<std::pair<int64_t, int64_t>> v;
+  SkipSet(const int64_t* skip, int64_t nSkip) {
+    for (int64_t q = 0; q < nSkip; ++q)
+      v.push_back({std::min(skip[2 * q], skip[2 * q + 1]), std::max(skip[2 * q], skip[2 * q + 1])});
+    std::sort(v.begin(), v.end());
+  }
+  bool operator()(int64_t a, int64_t b) const {
+    return !v.empty() && std::binary_search(v.begin(), v.end(), std::make_pair(std::min(a, b), std::max(a, b)));
+  }
+};
+
+template <class T>
+Collision detect_collision(T collisionDistSq, const T* coord, const T* nodeVel, const int32_t* label,
+                           const int64_t* links, const T* bVec, const int64_t* conn, int64_t ldConn, int64_t numNode,
+                           int64_t numSeg, const int64_t* skip, int64_t nSkip) {
+  const T eps = std::numeric_limits<T>::epsilon();
+  const SkipSet skipped(skip, nSkip);
+  Collision r{};
+  T smallest = T(0);
+  T L1 = T(0), L2 = T(0);
+  auto X = [&](int64_t n) { return V3<T>{coord[3 * n], coord[3 * n + 1], coord[3 * n + 2]}; };
+  auto Vn = [&](int64_t n) { return V3<T>{nodeVel[3 * n], nodeVel[3 * n + 1], nodeVel[3 * n + 2]}; };
+  // findConnectedNode (DislocationTopology.jl:22-32): (link, other node), 1-based.
+  auto connected = [&](int64_t i, int64_t c, int64_t& link, int64_t& node) {
+    link = conn[ldConn * i + 2 * c - 1];
+    const int64_t col = conn[ldConn * i + 2 * c];
+    node = links[2 * (link - 1) + (3 - col) - 1];
+  };
+  // Hinges: pairs of links at one mobile node.  link1 / node1 / tN1 persist
+  // across the k loop, swapped whenever connection k is longer (the reference
+  // assigns its j-loop variables inside the k loop).
+  for (int64_t i = 0; i < numNode; ++i) {
+    if (!mobile_label(label[i])) continue;
+    const int64_t nc = conn[ldConn * i];
+    for (int64_t j = 1; j <= nc; ++j) {
+      int64_t link1, node1;
+      connected(i, j, link1, node1);
+      V3<T> t = X(i) - X(node1 - 1);
+      T tN1 = dot(t, t);
+      for (int64_t k = j + 1; k <= nc; ++k) {
+        int64_t link2, node2;
+        connected(i, k, link2, node2);
+        t = X(i) - X(node2 - 1);
+        T tN2 = dot(t, t);
+        if (tN1 < tN2) {
+          std::swap(link1, link2);
+          std::swap(node1, node2);
+          std::swap(tN1, tN2);
+        }
+        if (skipped(link1, link2)) continue;
+        const V3<T> y0 = X(node2 - 1), vy0 = Vn(node2 - 1);
+        const MinDist<T> m = minimum_distance(X(i), X(node1 - 1), y0, y0, Vn(i), Vn(node1 - 1), vy0, vy0);
+        L1 = m.L1;
+        L2 = m.L2;
+        if (m.distSq < collisionDistSq && m.dDistSqDt < -eps) {
+          const T inv = T(1) / m.distSq;
+          if (inv > smallest) {
+            smallest = inv;
+            r = {1, 1, i + 1, node1, node2, node2, link1, link2, 0, 0, (double)m.distSq, (double)m.L1,
+                 (double)m.L2};
+          }
+        }
+      }
+    }
+  }
+  if (r.collision) {
+    r.L1 = L1;
+    r.L2 = L2;
+    return r;
+  }
+  // Two lines: unconnected pairs of segments with all four nodes mobile.
+  for (int64_t i = 0; i < numSeg; ++i) {
+    const int64_t a1 = links[2 * i], a2 = links[2 * i + 1];
+    if (!mobile_label(label[a1 - 1]) || !mobile_label(label[a2 - 1])) continue;
+    const V3<T> x0 = X(a1 - 1), x1 = X(a2 - 1), vx0 = Vn(a1 - 1), vx1 = Vn(a2 - 1);
+    const V3<T> bi = {bVec[3 * i], bVec[3 * i + 1], bVec[3 * i + 2]};
+    for (int64_t j = i + 1; j < numSeg; ++j) {
+      const int64_t c1 = links[2 * j], c2 = links[2 * j + 1];
+      if (a1 == c1 || a1 == c2 || a2 == c1 || a2 == c2) continue;
+      if (!mobile_label(label[c1 - 1]) || !mobile_label(label[c2 - 1])) continue;
+      const V3<T> y0 = X(c1 - 1), y1 = X(c2 - 1);
+      const V3<T> bj = {bVec[3 * j], bVec[3 * j + 1], bVec[3 * j + 2]};
+      const V3<T> bm = bi - bj, bp = bi + bj;
+      const T tt = dot(x1 - x0, y1 - y0);
+      if ((dot(bm, bm) < eps && tt > eps) || (dot(bp, bp) < eps && tt < eps)) continue;  // superdislocations
+      if (skipped(i + 1, j + 1)) continue;
+      const MinDist<T> m = minimum_distance(x0, x1, y0, y1, vx0, vx1, Vn(c1 - 1), Vn(c2 - 1));
+      L1 = m.L1;
+      L2 = m.L2;
+      if (m.distSq < collisionDistSq && m.dDistSqDt < -eps) {
+        const T inv = T(1) / m.distSq;
+        if (inv > smallest) {
+          smallest = inv;
+          r = {1, 2, a1, a2, c1, c2, i + 1, j + 1, 0, 0, (double)m.distSq, (double)m.L1, (double)m.L2};
+        }
+      }
+    }
+  }
+  r.L1 = L1;
+  r.L2 = L2;
+  return r;
 }
 
 }  // namespace ddd_oracle

@@ -53,6 +53,10 @@ def lib():
                                       _dp]
         L.oracle_mobility_bcc.argtypes = [_dp, _dp, _dp, _ip, _ip, ctypes.c_int64, _dp, ctypes.c_int64, _ip,
                                           ctypes.c_int64, _dp, _dp]
+        L.oracle_minimum_distance.argtypes = [_dp, ctypes.c_int64, _dp]
+        L.oracle_detect_collision.argtypes = [ctypes.c_double, _dp, _dp, ctypes.POINTER(ctypes.c_int32), _ip, _dp, _ip,
+                                              ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, _ip, ctypes.c_int64,
+                                              _ip, _dp]
         L.oracle_segseg_rows.argtypes = [_dp, _dp, _dp, _ip, ctypes.c_int64, _up, ctypes.c_int64, _ip,
                                          ctypes.c_int64, _dp, ctypes.c_int]
         L.oracle_segseg_idx.argtypes = [_dp, _dp, _dp, _ip, ctypes.c_int64, _up, ctypes.c_int64, _ip,
@@ -179,6 +183,40 @@ def mobility_bcc(mp, coord, bvec, links, conn, seg_force, num_node, idx=None):
     lib().oracle_mobility_bcc(_d(np.ascontiguousarray(mp, np.float64)), _d(coord), _d(bvec), _i(links), _i(conn),
                               conn.shape[0], _d(sf), num_node, ip, 0 if idx is None else len(idx), _d(Fo), _d(Vo))
     return Fo, Vo
+
+
+def minimum_distance(x0, x1, y0, y1, vx0, vx1, vy0, vy1):
+    """minimumDistance for n pairs: each argument 3 × n (or a 3-vector for one
+    pair); returns (distSq, dDistSqDt, L1, L2), arrays of n."""
+    arrs = [np.asarray(a, np.float64).reshape(3, -1, order="F") for a in (x0, x1, y0, y1, vx0, vx1, vy0, vy1)]
+    n = arrs[0].shape[1]
+    pts = np.asfortranarray(np.stack(arrs, axis=1))  # 3 x 8 x n
+    out = np.zeros((4, n), np.float64, order="F")
+    lib().oracle_minimum_distance(_d(pts), n, _d(out))
+    return out[0], out[1], out[2], out[3]
+
+
+_COLLISION_TYPES = ("null", "hinge", "twoLine")
+
+
+def detect_collision(collision_dist_sq, coord, node_vel, label, links, bvec, conn, num_node, num_seg, skip_segs=()):
+    """detectCollision: (collision, type, n1s1, n2s1, n1s2, n2s2, s1, s2, L1, L2)
+    as the reference returns it (type "null" / "hinge" / "twoLine"), and a dict
+    with the reported pair's own distSq, L1, L2."""
+    coord = np.require(coord, np.float64, ["F"])
+    node_vel = np.require(node_vel, np.float64, ["F"])
+    label = np.ascontiguousarray(label, np.int32)
+    links = np.require(links, np.int64, ["F"])
+    bvec = np.require(bvec, np.float64, ["F"])
+    conn = np.require(conn, np.int64, ["F"])
+    skip = np.ascontiguousarray(np.asarray(list(skip_segs), np.int64).reshape(-1, 2))
+    iout = np.zeros(8, np.int64)
+    dout = np.zeros(5, np.float64)
+    lib().oracle_detect_collision(float(collision_dist_sq), _d(coord), _d(node_vel),
+                                  label.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), _i(links), _d(bvec), _i(conn),
+                                  conn.shape[0], int(num_node), int(num_seg), _i(skip), len(skip), _i(iout), _d(dout))
+    res = (bool(iout[0]), _COLLISION_TYPES[iout[1]], *(int(v) for v in iout[2:]), float(dout[0]), float(dout[1]))
+    return res, {"distSq": float(dout[2]), "L1": float(dout[3]), "L2": float(dout[4])}
 
 
 def segseg_rows(k5, net, rows, nthreads=1):

@@ -12,6 +12,10 @@ matrices they assert against into JSON fixtures beside this script:
   mobility_goldens.json test/MobilityTest.jl:5-93 — BCC dlnMobility on a shear
                         hexagon and a prismatic pentagon after calcSegForce!
                         (zero FE fields, so no PK term): node forces and velocities
+  collision_goldens.json test/TopologyTest.jl:5-92 — detectCollision on a
+                        triangle and a 4-node loop under 17 skip lists (hinge
+                        and twoLine results), and test/MiscTest.jl:82-150 —
+                        minimumDistance on 9 segment pairs
   sigma_goldens.json    test/DislocationFEMTest.jl:5-155 — one edge and one
                         screw segment, σ̃ at a 3×3 grid (columns 5 and 6 of the
                         golden are (yz, xz), the code's order is (xz, yz))
@@ -20,6 +24,7 @@ Run once in a checkout that has the reference mounted:
     python tests/golden/extract_goldens.py /path/to/DDD.jl
 The fixtures are committed; nothing at test time reads the reference.
 """
+import ast
 import json
 import os
 import re
@@ -49,6 +54,92 @@ def _matrices(text, name):
         out.append(rows)
         pos = end
     return out
+
+
+def _julia_matrix(body):
+    """Rows of a one-line Julia matrix literal body ("1 1 2; 2 3 3")."""
+    return [[float(v) for v in row.split()] for row in body.split(";")]
+
+
+def _safe_value(expr, env):
+    """Evaluates the small vector expressions of MiscTest.jl's minimumDistance
+    block (zeros(3), ones(3), scalars times them, [1, 0, 0], eps(Float64)^2 and
+    names assigned before) by walking the parsed tree; anything else raises."""
+    import numpy as np
+
+    def ev(n):
+        if isinstance(n, ast.Constant) and isinstance(n.value, (int, float)):
+            return float(n.value)
+        if isinstance(n, ast.Name) and n.id in env:
+            return env[n.id]
+        if isinstance(n, ast.List):
+            return np.array([ev(e) for e in n.elts], dtype=np.float64)
+        if isinstance(n, ast.UnaryOp) and isinstance(n.op, ast.USub):
+            return -ev(n.operand)
+        if isinstance(n, ast.BinOp) and type(n.op) in (ast.Add, ast.Sub, ast.Mult, ast.Pow):
+            a, b = ev(n.left), ev(n.right)
+            return {ast.Add: a + b, ast.Sub: a - b, ast.Mult: a * b, ast.Pow: a ** b}[type(n.op)]
+        if isinstance(n, ast.Call) and isinstance(n.func, ast.Name) and len(n.args) == 1:
+            if n.func.id in ("zeros", "ones"):
+                k = int(ev(n.args[0]))
+                return np.zeros(k) if n.func.id == "zeros" else np.ones(k)
+            if n.func.id == "eps" and isinstance(n.args[0], ast.Name) and n.args[0].id == "Float64":
+                return float(np.finfo(np.float64).eps)
+        raise ValueError("unsupported expression: " + ast.dump(n))
+
+    return ev(expr)
+
+
+def collision_goldens(ref):
+    """detectCollision cases of TopologyTest.jl's "Collision detection" testset
+    and the minimumDistance cases of MiscTest.jl."""
+    top = open(os.path.join(ref, "test", "TopologyTest.jl")).read()
+    a = top.index('@testset "Collision detection"')
+    block = top[a:top.index("@testset", a + 10)]
+    dpar = json.load(open(os.path.join(ref, "test", "testData", "sampleDislocationParameters.json")))
+    nets = []
+    for part in block.split("network = DislocationNetwork(")[1:]:
+        fields = {}
+        for m in re.finditer(r"(\w+)\s*=\s*\w*\[([^\]]*)\]", part.split("makeConnect!")[0]):
+            fields[m.group(1)] = _julia_matrix(m.group(2))
+        cases, pending = [], []
+        tok = re.compile(r"detectCollision\(\s*dlnParams,\s*network,\s*(skipSegs|\[[^\]]*\])\s*,?\s*\)"
+                         r"|==\s*\((true|false),\s*:(\w+),([^)]*)\)")
+        for m in tok.finditer(part):
+            if m.group(1) is not None:
+                pending.append([[int(x), int(y)] for x, y in re.findall(r"\((\d+),\s*(\d+)\)", m.group(1))])
+            else:
+                nums = [v.strip() for v in m.group(4).split(",") if v.strip()]
+                exp = [m.group(2) == "true", m.group(3)] + [int(v) for v in nums[:6]] + [float(v) for v in nums[6:]]
+                cases += [{"skip": sk, "expected": exp} for sk in pending]
+                pending = []
+        nets.append({"links": fields["links"], "bVec": fields["bVec"], "coord": fields["coord"],
+                     "label": [r[0] for r in fields["label"]], "nodeVel": fields["nodeVel"], "cases": cases})
+
+    misc = open(os.path.join(ref, "test", "MiscTest.jl")).read().splitlines()
+    first = next(k for k, ln in enumerate(misc) if "minimumDistance(" in ln)
+    while not misc[first - 1].strip().startswith("@test"):
+        first -= 1
+    env, mcases, inputs = {}, [], None
+    names = ["x0", "x1", "y0", "y1", "vx0", "vx1", "vy0", "vy1"]
+    for ln in misc[first:]:
+        t = ln.strip()
+        if t.startswith("end"):
+            break
+        if "minimumDistance(" in t:
+            inputs = {k: env[k].tolist() for k in names}
+        elif t.startswith("@test (distSq, dDistSqDt, L1, L2) =="):
+            exp = ast.parse(t.split("==", 1)[1].strip(), mode="eval").body
+            mcases.append({"inputs": inputs, "expected": [_safe_value(e, {}) for e in exp.elts]})
+        elif "=" in t and not t.startswith("@"):
+            tree = ast.parse(t.replace(".+", "+").replace("^", "**"), mode="exec").body[0]
+            tg = tree.targets[0]
+            vals = tree.value.elts if isinstance(tree.value, ast.Tuple) else [tree.value]
+            tnames = [e.id for e in tg.elts] if isinstance(tg, ast.Tuple) else [tg.id]
+            for nm, v in zip(tnames, vals):
+                env[nm] = _safe_value(v, env)
+    json.dump({"collisionDist": float(dpar["collisionDist"]), "networks": nets, "minimumDistance": mcases},
+              open(os.path.join(HERE, "collision_goldens.json"), "w"), indent=1)
 
 
 def main(ref):
@@ -151,6 +242,7 @@ def main(ref):
         c["nu"] = 0.28
         c["golden_columns"] = ["xx", "yy", "zz", "xy", "yz", "xz"]
     json.dump({"cases": scases}, open(os.path.join(HERE, "sigma_goldens.json"), "w"), indent=1)
+    collision_goldens(ref)
 
 
 if __name__ == "__main__":

@@ -222,3 +222,35 @@ def test_connectivity_layout(fixtures):
     conn = fixtures.make_connectivity(links, 4)
     assert conn[:, 0].tolist() == [2, 1, 1, 4, 2, 0, 0, 0, 0]
     assert conn[:, 2].tolist() == [2, 2, 2, 3, 1, 0, 0, 0, 0]
+
+
+G_COL = json.load(open(os.path.join(GOLDEN, "collision_goldens.json")))
+
+
+def collision_net(fixtures, g):
+    """A TopologyTest.jl network as its constructor and makeConnect! build it."""
+    links = np.asfortranarray(np.array(g["links"], np.int64))
+    return (np.asfortranarray(g["coord"], np.float64), np.asfortranarray(g["nodeVel"], np.float64),
+            np.array(g["label"], np.int32), links, np.asfortranarray(g["bVec"], np.float64),
+            fixtures.make_connectivity(links, 4))
+
+
+@pytest.mark.parametrize("net_i", range(len(G_COL["networks"])))
+def test_detect_collision_matches_golden(oracle, fixtures, net_i):
+    """detectCollision (DislocationTopologyCollision.jl:1-221) against
+    test/TopologyTest.jl:5-92: every skip list, all ten returned values exactly."""
+    g = G_COL["networks"][net_i]
+    coord, vel, label, links, bvec, conn = collision_net(fixtures, g)
+    cd2 = G_COL["collisionDist"] * G_COL["collisionDist"]
+    for c in g["cases"]:
+        res, _ = oracle.detect_collision(cd2, coord, vel, label, links, bvec, conn, coord.shape[1], links.shape[1],
+                                         [tuple(p) for p in c["skip"]])
+        assert list(res) == c["expected"], (c["skip"], res)
+
+
+def test_minimum_distance_matches_golden(oracle):
+    """minimumDistance (Misc.jl:314-367) against test/MiscTest.jl:82-150."""
+    for c in G_COL["minimumDistance"]:
+        v = c["inputs"]
+        out = oracle.minimum_distance(*(np.array(v[k]) for k in ("x0", "x1", "y0", "y1", "vx0", "vx1", "vy0", "vy1")))
+        assert [float(o[0]) for o in out] == c["expected"], (v, out)
