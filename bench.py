@@ -29,6 +29,11 @@ collision: detectCollision on the workload network moving with the mobility
        step's velocities: pair scans/s of the kernels and of the host call, the
        oracle on a prefix of the network beside it, answers compared.
 
+u_tilde: calc_uTilde of the workload network at the displacement nodes of a
+       64^3-element cuboid mesh around its cube (Barnett triangles, FP64):
+       evaluations/s of the kernels and of the host call, the OpenMP oracle on a
+       sample of points beside it, values compared.
+
 node_rows: calcSelfForce and dlnMobility (BCC) on the workload network through
        their host-array C-ABI calls, node forces from the timed seg-seg step plus
        the self force: e2e and kernel times, the kernel's algorithmic GB/s, the
@@ -445,6 +450,57 @@ def run_collision(pkg, oracle, ctx, net, synth, p, b, cd, reps=5, cpu_target_s=1
     return out
 
 
+def run_u_tilde(pkg, oracle, ctx, net, cube, cells=64, reps=3, cpu_target_s=8.0, with_cpu=True):
+    """calc_uTilde on the workload network inside a cube^3 regular cuboid mesh
+    of cells^3 elements, at the cantilever's displacement nodes (the x0 face and
+    the x1/z1 edge): triangle-point evaluations/s of the kernels and of the host
+    call; beside it the oracle (OpenMP over points, all host threads) on a
+    sample of the points, its values compared with the GPU's."""
+    mesh = pkg.fem.RegularCuboidMesh(cube, cube, cube, cells, cells, cells)
+    bnd = pkg.fem.cantilever_boundaries(mesh)
+    mat = pkg.MaterialParameters(mu=1.0, nu=0.28)
+    pts = np.asfortranarray(mesh.coord[:, bnd.uGammaDln - 1])
+    M = pts.shape[1]
+    k = (mat.omνInv8π, mat.om2νomνInv8π)
+    u = ctx.u_tilde(*k, mesh, pts, net)
+    ts, ks = [], []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        u = ctx.u_tilde(*k, mesh, pts, net)
+        ts.append(time.perf_counter() - t0)
+        ks.append(ctx.last_kernel_ms)
+    evals = net.numSeg * M  # every segment is internal: one triangle each
+    ms_k, ms_e = min(ks), min(ts) * 1e3
+    out = {"segments": net.numSeg, "points": M, "mesh": "%g^3, %d^3 elements, cantilever uGammaDln" % (cube, cells),
+           "evals_per_call": evals, "kernel_ms": ms_k, "value": evals / (ms_k * 1e-3),
+           "unit": "triangle-point evaluations/s",
+           "e2e": {"ms": ms_e, "value": evals / (ms_e * 1e-3)}, "timing": "best of %d calls" % reps}
+    if not with_cpu:
+        return out
+    md = {"faceNorm": mesh.faceNorm, "faceMidPt": mesh.faceMidPt, "C": mesh.closure, "lo": mesh.lo, "hi": mesh.hi}
+    threads = cpu_threads()
+
+    def ref(idx):
+        return oracle.u_tilde(k, md, mesh.normals, np.asfortranarray(pts[:, idx]), net.coord, net.label, net.links,
+                              net.bVec, net.numNode, net.numSeg, nthreads=threads)[0]
+
+    probe = np.arange(0, M, max(1, M // threads))[:threads]
+    t0 = time.perf_counter()
+    ref(probe)
+    rate = len(probe) / max(time.perf_counter() - t0, 1e-6)
+    m = int(min(M, max(threads, rate * cpu_target_s)))
+    idx = np.linspace(0, M - 1, m).astype(np.int64)
+    t0 = time.perf_counter()
+    r = ref(idx)
+    dt = time.perf_counter() - t0
+    g = u.reshape(3, -1, order="F")[:, idx]
+    out["cpu_baseline"] = {"value": net.numSeg * m / dt, "unit": "triangle-point evaluations/s", "cores": threads,
+                           "kind": "port", "sample": "%d of the %d points, all segments, %.1f s" % (m, M, dt)}
+    out["parity_sample"] = {"points": m, "max_abs_diff_over_max": float(np.abs(g - r).max() / np.abs(r).max()),
+                            "rel_rms": float(np.linalg.norm(g - r) / np.linalg.norm(r))}
+    return out
+
+
 def run_reference(args, pkg, synth, oracle):
     ws, rank = _dist()
     if rank != 0:
@@ -738,6 +794,8 @@ def main():
     # collisionDist = minSegLen / 2 (the reference's default) with minSegLen =
     # 20 b, the workload's shortest segment.
     collision = run_collision(pkg, oracle, ctx, net, synth, p, b, 10.0, with_cpu=not args.no_cpu)
+    # Displacements at the FE boundary of a mesh around the workload's cube.
+    u_tilde = run_u_tilde(pkg, oracle, ctx, net, cfg["cube"], with_cpu=not args.no_cpu)
     achieved = flops_per_step / (statistics.mean(ms_kernel) * 1e-3)
     line = {
         "metric": "seg-seg pair interactions/s at 65k segs (FP64 plain vs FP32+surrogate) at stated error",
@@ -771,6 +829,7 @@ def main():
         "batched": batched,
         "node_rows": node_rows,
         "collision": collision,
+        "u_tilde": u_tilde,
         "kernel_ms_per_step": statistics.mean(ms_kernel),
     }
     cs = clocks.summary()

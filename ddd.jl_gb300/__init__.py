@@ -35,7 +35,7 @@ NOALLOC_MAX_SEGMENTS = 4096
 # Every symbol include/ddd_gb300.h declares.
 EXPORTED_SYMBOLS = (
     "ddd_create", "ddd_destroy", "ddd_last_error", "ddd_last_kernel_ms", "ddd_version",
-    "ddd_detect_collision", "ddd_minimum_distance",
+    "ddd_detect_collision", "ddd_minimum_distance", "ddd_u_tilde",
     "ddd_segseg_force", "ddd_segseg_force_inplace", "ddd_sigma_tilde",
     "ddd_segseg_force_device", "ddd_sigma_tilde_device", "ddd_set_mode", "ddd_get_mode", "ddd_probe_fma_peak",
     "ddd_segseg_force_device_noalloc",
@@ -99,6 +99,13 @@ class ddd_collision(ctypes.Structure):
                 ("n2s1", ctypes.c_int64), ("n1s2", ctypes.c_int64), ("n2s2", ctypes.c_int64), ("s1", ctypes.c_int64),
                 ("s2", ctypes.c_int64), ("L1", ctypes.c_double), ("L2", ctypes.c_double),
                 ("pairDistSq", ctypes.c_double), ("pairL1", ctypes.c_double), ("pairL2", ctypes.c_double)]
+
+
+class ddd_u_mesh(ctypes.Structure):
+    _fields_ = [("C", ctypes.c_double * 3), ("lo", ctypes.c_double * 3), ("hi", ctypes.c_double * 3),
+                ("tol", ctypes.c_double), ("faceNorm", ctypes.POINTER(ctypes.c_double)),
+                ("faceMidPt", ctypes.POINTER(ctypes.c_double)), ("numFaces", ctypes.c_int64),
+                ("normals", ctypes.POINTER(ctypes.c_double)), ("numNormals", ctypes.c_int64)]
 
 
 class ddd_sur_opts(ctypes.Structure):
@@ -204,6 +211,9 @@ def library():
                                            _i64, _ip, _i64, _dp, _i64, _ip, _i64, _i64, _i64, _i64, _ip, _i64,
                                            ctypes.POINTER(ddd_collision)]
         L.ddd_minimum_distance.argtypes = [_vp, _dp, _i64, _dp]
+        L.ddd_u_tilde.argtypes = [_vp, ctypes.c_double, ctypes.c_double, ctypes.POINTER(ddd_u_mesh), _dp, _i64, _dp,
+                                  _i64, ctypes.POINTER(ctypes.c_int32), _i64, _ip, _i64, _dp, _i64, _i64, _i64, _ip,
+                                  _dp, _i64]
         L.ddd_set_mode.argtypes = [_vp, ctypes.c_int]
         L.ddd_get_mode.argtypes = [_vp]
         L.ddd_probe_fma_peak.argtypes = [_vp, ctypes.c_int, _dp]
@@ -508,6 +518,37 @@ class Context:
         res = (bool(r.collision), ("null", "hinge", "twoLine")[r.type], r.n1s1, r.n2s1, r.n1s2, r.n2s2, r.s1, r.s2,
                r.L1, r.L2)
         return res, {"distSq": r.pairDistSq, "L1": r.pairL1, "L2": r.pairL2}
+
+    def u_tilde(self, omNuInv8pi, om2NuOmNuInv8pi, mesh, points, network, uDofs=None, out=None, tol=0.0):
+        """calc_uTilde's kernel: adds u of point p, component c to
+        out[uDofs[3p + c] - 1] (or out[3p + c]); returns out."""
+        pts = np.require(points, np.float64, ["F"])
+        M = pts.shape[1]
+        if out is None:
+            out = np.zeros(3 * M)
+        if out.dtype != np.float64 or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous float64 vector")
+        dofs = None if uDofs is None else np.ascontiguousarray(uDofs, np.int64)
+        if dofs is not None and dofs.shape[0] != 3 * M:
+            raise ValueError("uDofs must have 3 entries per point")
+        fn = np.require(mesh.faceNorm, np.float64, ["F"])
+        fm = np.require(mesh.faceMidPt, np.float64, ["F"])
+        nr = np.require(mesh.normals, np.float64, ["F"])
+        m = ddd_u_mesh()
+        for k in range(3):
+            m.C[k], m.lo[k], m.hi[k] = mesh.closure[k], mesh.lo[k], mesh.hi[k]
+        m.tol = float(tol)
+        m.faceNorm, m.faceMidPt, m.numFaces = fn.ctypes.data_as(_dp), fm.ctypes.data_as(_dp), fn.shape[1]
+        m.normals, m.numNormals = nr.ctypes.data_as(_dp), nr.shape[1]
+        net = network
+        lab = np.ascontiguousarray(net.label, np.int32)
+        self._check(self._L.ddd_u_tilde(
+            self._h, float(omNuInv8pi), float(om2NuOmNuInv8pi), ctypes.byref(m), pts.ctypes.data_as(_dp), M,
+            net.coord.ctypes.data_as(_dp), net.coord.shape[1], lab.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+            lab.shape[0], net.links.ctypes.data_as(_ip), net.links.shape[1], net.bVec.ctypes.data_as(_dp),
+            net.bVec.shape[1], net.numNode, net.numSeg, None if dofs is None else dofs.ctypes.data_as(_ip),
+            out.ctypes.data_as(_dp), out.shape[0]))
+        return out
 
     def minimum_distance(self, pts):
         """minimumDistance for pts (3 × 8 × n): 4 × n (distSq, dDistSqDt, L1, L2)."""
@@ -971,6 +1012,24 @@ def minimumDistance(x0, x1, y0, y1, vx0, vx1, vy0, vy1):
     return tuple(float(v[0]) for v in out) if single else tuple(out)
 
 
+def calc_uTilde(mesh, boundaries, matParams, network):
+    """calc_uTilde (DislocationFEM.jl:375-391): the displacements at the FE nodes
+    boundaries.uGammaDln, point-major (ux, uy, uz of each node in turn).  mesh:
+    fem.RegularCuboidMesh; boundaries: fem.Boundaries."""
+    pts = np.asfortranarray(mesh.coord[:, boundaries.uGammaDln - 1])
+    return get_context().u_tilde(matParams.omνInv8π, matParams.om2νomνInv8π, mesh, pts, network)
+
+
+def calc_uTilde_inplace(forceDisplacement, mesh, boundaries, matParams, network):
+    """calc_uTilde! (DislocationFEM.jl:362-373): zeroes forceDisplacement.uTilde
+    and adds point p's component c at uDofsDln[3p + c], the reference's indexing."""
+    forceDisplacement.uTilde[:] = 0.0
+    pts = np.asfortranarray(mesh.coord[:, boundaries.uGammaDln - 1])
+    get_context().u_tilde(matParams.omνInv8π, matParams.om2νomνInv8π, mesh, pts, network, boundaries.uDofsDln,
+                          forceDisplacement.uTilde)
+    return forceDisplacement
+
+
 def calc_σTilde(x0, dlnParams, matParams, network, idx=None):
     """calc_σTilde (DislocationFEM.jl:24-41): 6×M stresses, or a 6-vector for one point."""
     x0 = np.asarray(x0, dtype=np.float64)
@@ -992,3 +1051,6 @@ def calc_σTilde_inplace(σ, x0, dlnParams, matParams, network, idx=None):
 
 calc_sigmaTilde = calc_σTilde
 calc_sigmaTilde_inplace = calc_σTilde_inplace
+
+
+from . import fem  # noqa: E402  (RegularCuboidMesh, Boundaries, cantilever_boundaries, ForceDisplacement)

@@ -30,6 +30,7 @@ VARIANTS = {
     "self_force.cu": [("", ["--fmad=false"])],
     "mobility.cu": [("", ["--fmad=false"])],
     "collision.cu": [("", ["--fmad=false"])],
+    "u_tilde.cu": [("", ["--fmad=false", "-Xcompiler", "-ffp-contract=off"])],
 }
 
 

@@ -59,6 +59,8 @@ struct ddd_ctx {
   DevBuf links, conn, segforce;  // mobility inputs
   DevBuf vel, label, skippairs;  // collision inputs
   ddd::CollisionPlan* coll = nullptr;
+  DevBuf upoints;  // calc_uTilde evaluation points
+  ddd::UTildeScratch* ut = nullptr;
   std::vector<double> hostTmp;
   double lastKernelMs = 0.0;  // device time of the last self-force / mobility kernel
 };
@@ -312,6 +314,8 @@ void ddd_destroy(ddd_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (DevBuf* b : {&c->links, &c->conn, &c->segforce, &c->vel, &c->label, &c->skippairs}) b->release();
   if (c->coll) ddd::collision_plan_destroy(c->coll);
+  delete c->ut;
+  c->upoints.release();
   for (DevBuf* b : {&c->coord, &c->bvec, &c->segidx, &c->ext, &c->soa, &c->soadf, &c->skip, &c->partial, &c->out, &c->rows,
                     &c->x0, &c->sigma, &c->counters, &c->probe, &c->errflag})
     b->release();
@@ -1055,6 +1059,91 @@ int ddd_minimum_distance(ddd_ctx* ctx, const double* pts, int64_t n, double* out
   CK(ddd::launch_minimum_distance(ctx->x0.as<double>(), n, ctx->out.as<double>(), st), "minimum_distance");
   CK(cudaMemcpyAsync(out, ctx->out.p, (size_t)n * 4 * 8, cudaMemcpyDeviceToHost, st), "copy output");
   CK(cudaStreamSynchronize(st), "minimum_distance");
+  return DDD_OK;
+}
+
+int ddd_u_tilde(ddd_ctx* ctx, double omNuInv8pi, double om2NuOmNuInv8pi, const ddd_u_mesh* mesh,
+                const double* points, int64_t numPoints, const double* coord, int64_t coordCols, const int32_t* label,
+                int64_t labelLen, const int64_t* links, int64_t linkCols, const double* bVec, int64_t bVecCols,
+                int64_t numNode, int64_t numSeg, const int64_t* uDofs, double* uTilde, int64_t uLen) {
+  if (!ctx) return DDD_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (!mesh) return fail(ctx, DDD_EINVAL, "mesh is NULL");
+  if (numPoints < 0 || coordCols < 0 || labelLen < 0 || linkCols < 0 || bVecCols < 0 || numNode < 0 || numSeg < 0 ||
+      uLen < 0 || mesh->numFaces < 0 || mesh->numNormals < 0)
+    return fail(ctx, DDD_EINVAL, "negative size");
+  if (numNode > coordCols || numNode > labelLen) return fail(ctx, DDD_EINVAL, "numNode exceeds coord / label");
+  if (numSeg > linkCols || numSeg > bVecCols) return fail(ctx, DDD_EINVAL, "numSeg exceeds links / bVec");
+  if (!uDofs && uLen < 3 * numPoints) return fail(ctx, DDD_EINVAL, "uTilde shorter than 3 numPoints");
+  if (numPoints == 0) return DDD_OK;
+  if (!points || !uTilde || (numSeg > 0 && (!coord || !label || !links || !bVec)) ||
+      (mesh->numFaces > 0 && (!mesh->faceNorm || !mesh->faceMidPt)) || (mesh->numNormals > 0 && !mesh->normals))
+    return fail(ctx, DDD_EINVAL, "array is NULL");
+  char buf[160];
+  for (int64_t i = 0; i < numSeg; ++i)
+    for (int k = 0; k < 2; ++k)
+      if (links[2 * i + k] < 1 || links[2 * i + k] > numNode) {
+        snprintf(buf, sizeof buf, "links[%d, %lld] = %lld outside 1..numNode=%lld", k + 1, (long long)(i + 1),
+                 (long long)links[2 * i + k], (long long)numNode);
+        return fail(ctx, DDD_ERANGE, buf);
+      }
+  if (uDofs)
+    for (int64_t q = 0; q < 3 * numPoints; ++q)
+      if (uDofs[q] < 1 || uDofs[q] > uLen) {
+        snprintf(buf, sizeof buf, "uDofs[%lld] = %lld outside 1..%lld", (long long)(q + 1), (long long)uDofs[q],
+                 (long long)uLen);
+        return fail(ctx, DDD_ERANGE, buf);
+      }
+  for (int64_t q = 0; q < 3 * numPoints; ++q)
+    if (!std::isfinite(points[q])) return fail(ctx, DDD_ENONFINITE, "non-finite evaluation point");
+  for (int64_t q = 0; q < 3 * numNode; ++q)
+    if (!std::isfinite(coord[q])) return fail(ctx, DDD_ENONFINITE, "non-finite node coordinate");
+  ddd::UTildeArgs a{};
+  a.omNuInv8pi = omNuInv8pi;
+  a.om2NuOmNuInv8pi = om2NuOmNuInv8pi;
+  double ext = 0.0;
+  for (int k = 0; k < 3; ++k) {
+    a.C[k] = mesh->C[k];
+    a.lo[k] = mesh->lo[k];
+    a.hi[k] = mesh->hi[k];
+    ext = std::max(ext, mesh->hi[k] - mesh->lo[k]);
+  }
+  a.tol = mesh->tol > 0.0 ? mesh->tol : 1e-10 * ext;
+  a.faceNorm = mesh->faceNorm;
+  a.faceMidPt = mesh->faceMidPt;
+  a.numFaces = mesh->numFaces;
+  a.normals = mesh->normals;
+  a.numNormals = mesh->numNormals;
+  a.coord = coord;
+  a.label = label;
+  a.links = links;
+  a.bVec = bVec;
+  a.numNode = numNode;
+  a.numSeg = numSeg;
+  a.numPoints = numPoints;
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  if (!ctx->ut) ctx->ut = new ddd::UTildeScratch();
+  cudaStream_t st = ctx->stream;
+  const size_t cB = (size_t)std::max<int64_t>(numNode, 1) * 24, lB = (size_t)std::max<int64_t>(numSeg, 1) * 16;
+  const size_t bB = (size_t)std::max<int64_t>(numSeg, 1) * 24, pB = (size_t)numPoints * 24;
+  CK(ctx->coord.ensure(cB), "alloc coord");
+  CK(ctx->links.ensure(lB), "alloc links");
+  CK(ctx->bvec.ensure(bB), "alloc bVec");
+  CK(ctx->upoints.ensure(pB), "alloc points");
+  if (numNode > 0) CK(cudaMemcpyAsync(ctx->coord.p, coord, (size_t)numNode * 24, cudaMemcpyHostToDevice, st), "copy coord");
+  if (numSeg > 0) {
+    CK(cudaMemcpyAsync(ctx->links.p, links, (size_t)numSeg * 16, cudaMemcpyHostToDevice, st), "copy links");
+    CK(cudaMemcpyAsync(ctx->bvec.p, bVec, (size_t)numSeg * 24, cudaMemcpyHostToDevice, st), "copy bVec");
+  }
+  CK(cudaMemcpyAsync(ctx->upoints.p, points, pB, cudaMemcpyHostToDevice, st), "copy points");
+  a.coordDev = ctx->coord.as<double>();
+  a.linksDev = ctx->links.as<int64_t>();
+  a.bVecDev = ctx->bvec.as<double>();
+  a.pointsDev = ctx->upoints.as<double>();
+  ctx->hostTmp.assign((size_t)numPoints * 3, 0.0);
+  CK(ddd::u_tilde_compute(a, ctx->hostTmp.data(), ctx->ev[1], ctx->ev[2], st, *ctx->ut), "u_tilde");
+  ctx->lastKernelMs = elapsed(ctx->ev[1], ctx->ev[2]);
+  for (int64_t q = 0; q < 3 * numPoints; ++q) uTilde[uDofs ? uDofs[q] - 1 : q] += ctx->hostTmp[(size_t)q];
   return DDD_OK;
 }
 

@@ -4,6 +4,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <vector>
 
 struct ddd_ctx;
 
@@ -105,6 +106,60 @@ cudaError_t collision_detect(CollisionPlan* P, double cd2, const double* coord, 
                              double maxAbs, CollisionOut* out, cudaEvent_t e0, cudaEvent_t e1, cudaStream_t st);
 // pts: 3 x 8 x n (x0, x1, y0, y1, vx0, vx1, vy0, vy1), out 4 x n.
 cudaError_t launch_minimum_distance(const double* pts, int64_t n, double* out, cudaStream_t st);
+
+// Grow-only device buffer.
+struct GrowBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    const size_t want = bytes + bytes / 8 + 256;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) return e;
+    cap = want;
+    return cudaSuccess;
+  }
+  GrowBuf() = default;
+  GrowBuf(const GrowBuf&) = delete;
+  GrowBuf& operator=(const GrowBuf&) = delete;
+  ~GrowBuf() {
+    if (p) cudaFree(p);
+  }
+};
+
+// u_tilde.cu: calc_uTilde's displacements at numPoints points (u: host, 3 x
+// numPoints).  The host arrays drive the segment pass; the *Dev copies feed the
+// kernels.  Mesh: closure point C, volume box [lo, hi] widened by tol, face
+// normals / midpoints (3 x numFaces), projection directions (3 x numNormals).
+struct UTildeArgs {
+  double omNuInv8pi, om2NuOmNuInv8pi;
+  double C[3], lo[3], hi[3], tol;
+  const double* faceNorm;
+  const double* faceMidPt;
+  int64_t numFaces;
+  const double* normals;
+  int64_t numNormals;
+  const double* coord;
+  const int32_t* label;
+  const int64_t* links;
+  const double* bVec;
+  int64_t numNode, numSeg, numPoints;
+  const double* coordDev;
+  const int64_t* linksDev;
+  const double* bVecDev;
+  const double* pointsDev;
+};
+struct UTildeScratch {
+  std::vector<int64_t> order;
+  std::vector<double> explicitTri;
+  GrowBuf order_d, ex_d, tri_d, u_d;
+  int64_t lastTriangles = 0;
+};
+cudaError_t u_tilde_compute(const UTildeArgs& a, double* u, cudaEvent_t e0, cudaEvent_t e1, cudaStream_t st,
+                            UTildeScratch& S);
 
 // ddd_api.cu: context accessors for the other C-ABI files.
 int ctx_device(const ddd_ctx* c);

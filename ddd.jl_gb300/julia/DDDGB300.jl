@@ -11,10 +11,12 @@
 # Python mirror (ddd.jl_gb300/__init__.py) and its tests.
 module DDDGB300
 
+using Statistics: mean
+
 export calcSegSegForceGPU, calcSegSegForceGPU!, calc_σTildeGPU, calc_σTildeGPU!
 export calcSelfForceGPU, calcSelfForceGPU!, calcSegForceGPU, calcSegForceGPU!
 export Surrogate, loadSurrogate, calcSegSegForceSurrogateGPU
-export dlnMobilityGPU, dlnMobilityGPU!, detectCollisionGPU, minimumDistanceGPU
+export dlnMobilityGPU, dlnMobilityGPU!, detectCollisionGPU, minimumDistanceGPU, calc_uTildeGPU, calc_uTildeGPU!
 
 const libddd = joinpath(@__DIR__, "..", "libddd_gb300.so")
 
@@ -312,6 +314,58 @@ function minimumDistanceGPU(x0, x1, y0, y1, vx0, vx1, vy0, vy1)
     end
     check(rc)
     return out[1], out[2], out[3], out[4]
+end
+
+# ---------------------------------------------------------------------------
+# calc_uTilde / calc_uTilde! (DislocationFEM.jl:354-632): the mesh enters as
+# data (closure point, bounding box, face normals and midpoints, the normals
+# used for projections).
+
+struct DDDUMesh
+    C::NTuple{3, Float64}
+    lo::NTuple{3, Float64}
+    hi::NTuple{3, Float64}
+    tol::Float64
+    faceNorm::Ptr{Float64}
+    faceMidPt::Ptr{Float64}
+    numFaces::Int64
+    normals::Ptr{Float64}
+    numNormals::Int64
+end
+
+function _u_tilde!(uTilde, uDofs, mesh, boundaries, matParams, network)
+    C = Tuple(mean(mesh.vertices.vertices))
+    V = reduce(hcat, mesh.vertices.vertices)
+    lo, hi = Tuple(minimum(V, dims = 2)), Tuple(maximum(V, dims = 2))
+    faceNorm, faceMidPt = Matrix{Float64}(mesh.faceNorm), Matrix{Float64}(mesh.faceMidPt)
+    normals = mesh isa ..AbstractRegularCuboidMesh ? faceNorm[:, 1:2:5] : faceNorm  # DDD's mesh type (parent module)
+    points = Matrix{Float64}(mesh.coord[:, boundaries.uGammaDln])
+    coord, label, links, bVec = network.coord, network.label, network.links, network.bVec
+    dofs = uDofs === nothing ? C_NULL : convert(Vector{Int64}, uDofs)
+    GC.@preserve faceNorm faceMidPt normals points coord label links bVec dofs uTilde begin
+        m = Ref(DDDUMesh(C, lo, hi, 0.0, pointer(faceNorm), pointer(faceMidPt), size(faceNorm, 2), pointer(normals),
+                         size(normals, 2)))
+        rc = ccall((:ddd_u_tilde, libddd), Cint,
+            (Ptr{Cvoid}, Float64, Float64, Ref{DDDUMesh}, Ptr{Float64}, Int64, Ptr{Float64}, Int64, Ptr{Cvoid},
+             Int64, Ptr{Int64}, Int64, Ptr{Float64}, Int64, Int64, Int64, Ptr{Cvoid}, Ptr{Float64}, Int64),
+            context(), matParams.omνInv8π, matParams.om2νomνInv8π, m, points, size(points, 2), coord, size(coord, 2),
+            pointer(label), length(label), links, size(links, 2), bVec, size(bVec, 2), network.numNode[1],
+            network.numSeg[1], dofs === C_NULL ? C_NULL : pointer(dofs), uTilde, length(uTilde))
+    end
+    check(rc)
+    return uTilde
+end
+
+# calc_uTilde: point-major vector over boundaries.uGammaDln
+calc_uTildeGPU(mesh, boundaries, matParams, network) =
+    _u_tilde!(zeros(3 * length(boundaries.uGammaDln)), nothing, mesh, boundaries, matParams, network)
+
+# calc_uTilde!: zero forceDisplacement.uTilde, add through boundaries.uDofsDln
+function calc_uTildeGPU!(forceDisplacement, mesh, boundaries, matParams, network)
+    u = zeros(length(forceDisplacement.uTilde))
+    _u_tilde!(u, boundaries.uDofsDln, mesh, boundaries, matParams, network)
+    forceDisplacement.uTilde .= u
+    return nothing
 end
 
 # ---------------------------------------------------------------------------

@@ -96,8 +96,9 @@ ddd_ctx* ddd_create(int device);
 void ddd_destroy(ddd_ctx* ctx);
 /* Message of the last failed call on ctx (or of the last failed ddd_create when ctx is NULL). */
 const char* ddd_last_error(const ddd_ctx* ctx);
-/* Device time (ms, CUDA events around the launch) of the kernel of the last
- * successful ddd_self_force* / ddd_seg_force* / ddd_mobility_bcc* call on ctx.
+/* Device time (ms, CUDA events around the launches) of the kernels of the last
+ * successful ddd_self_force* / ddd_seg_force* / ddd_mobility_bcc* /
+ * ddd_detect_collision / ddd_u_tilde call on ctx.
  * No reference counterpart: measurement only. */
 double ddd_last_kernel_ms(const ddd_ctx* ctx);
 /* ABI version, 100 * major + minor. */
@@ -228,6 +229,39 @@ int ddd_detect_collision(ddd_ctx* ctx, double collisionDistSq, const double* coo
  * pts 3 × 8 × n (the eight points of each pair), out 4 × n (distSq,
  * dDistSqDt, L1, L2). */
 int ddd_minimum_distance(ddd_ctx* ctx, const double* pts, int64_t n, double* out);
+
+/* calc_uTilde(mesh, boundaries, matParams, network) and calc_uTilde!(...) —
+ * src/Processing/DislocationFEM.jl:354-632 (Barnett triangles :634-751): the
+ * displacement the network causes at the FE nodes with applied displacements.
+ * Each internal segment is closed on C (a full triangle, with the f and g
+ * terms); a segment with an external node (label extDln = 5) is closed through
+ * the points its nodes were projected out from (found on the mesh faces along
+ * `normals`, or by walking the face planes), five solid-angle triangles; a
+ * segment joining a surface node (labels 3, 4) to an external node only records
+ * that connection for the segments after it.  The mesh enters as data:
+ * mesh.vertices' mean (C), its bounding box (the "inside the volume" test,
+ * widened by tol; tol <= 0 means 1e-10 of the largest extent), faceNorm and
+ * faceMidPt (3 × numFaces) and the projection directions (3 × numNormals;
+ * faceNorm[:, 1:2:5] for a regular cuboid, as the reference uses).  points:
+ * mesh.coord[:, boundaries.uGammaDln] (3 × numPoints).  For point p and
+ * component c: uTilde[uDofs[3p + c] - 1] += u_c(p), or uTilde[3p + c] when
+ * uDofs is NULL (calc_uTilde's 1:3numPoints); calc_uTilde! passes
+ * boundaries.uDofsDln after zeroing uTilde, exactly the reference's indexing.
+ * Each point's sum runs over the triangles in the reference's order. */
+typedef struct ddd_u_mesh {
+  double C[3];
+  double lo[3], hi[3];
+  double tol;
+  const double* faceNorm;
+  const double* faceMidPt;
+  int64_t numFaces;
+  const double* normals;
+  int64_t numNormals;
+} ddd_u_mesh;
+int ddd_u_tilde(ddd_ctx* ctx, double omNuInv8pi, double om2NuOmNuInv8pi, const ddd_u_mesh* mesh,
+                const double* points, int64_t numPoints, const double* coord, int64_t coordCols, const int32_t* label,
+                int64_t labelLen, const int64_t* links, int64_t linkCols, const double* bVec, int64_t bVecCols,
+                int64_t numNode, int64_t numSeg, const int64_t* uDofs, double* uTilde, int64_t uLen);
 
 /* calc_σTilde(x0, dlnParams, matParams, network, idx = nothing) and
  * calc_σTilde!(σ, x0, ...) — src/Processing/DislocationFEM.jl:24-84, kernel

@@ -334,6 +334,58 @@ void oracle_detect_collision(double collisionDistSq, const double* coord, const 
   for (int k = 0; k < 5; ++k) dout[k] = dv[k];
 }
 
+// calc_uTilde (DislocationFEM.jl:354-632) at numPoints points (3 × M): u (3 × M)
+// summed over the triangles in the reference's order for each point.  k2 =
+// (omνInv8π, om2νomνInv8π); box = (lo xyz, hi xyz); C the closure point.  Points
+// are split over nthreads (each point's sum keeps its order).  Returns the
+// number of triangles.
+int64_t oracle_u_tilde(const double* k2, const double* C, const double* faceNorm, const double* faceMidPt,
+                       int64_t nF, const double* normals, int64_t nN, const double* box, double tol,
+                       const double* points, int64_t M, const double* coord, const int32_t* label,
+                       const int64_t* links, const double* bVec, int64_t numNode, int64_t numSeg, double* u,
+                       int nthreads) {
+  const UMesh<double> m{faceNorm, faceMidPt, nF, normals, nN, {box[0], box[1], box[2]}, {box[3], box[4], box[5]},
+                        {C[0], C[1], C[2]}, tol};
+  const std::vector<UTri<double>> tris = u_tilde_triangles<double>(m, coord, label, links, bVec, numNode, numSeg);
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
+  for (int64_t p = 0; p < M; ++p) {
+    const V3<double> P = {points[3 * p], points[3 * p + 1], points[3 * p + 2]};
+    V3<double> acc = {0.0, 0.0, 0.0};
+    for (const auto& t : tris) acc = acc + tri_u(t, k2[0], k2[1], P);
+    u[3 * p] = acc.x;
+    u[3 * p + 1] = acc.y;
+    u[3 * p + 2] = acc.z;
+  }
+  return (int64_t)tris.size();
+}
+
+// The same triangles (built in double, as the reference builds them) summed in
+// long double: the reference arithmetic's own error at each point is
+// |oracle_u_tilde - this|.
+int64_t oracle_u_tilde_ld(const double* k2, const double* C, const double* faceNorm, const double* faceMidPt,
+                          int64_t nF, const double* normals, int64_t nN, const double* box, double tol,
+                          const double* points, int64_t M, const double* coord, const int32_t* label,
+                          const int64_t* links, const double* bVec, int64_t numNode, int64_t numSeg, double* u,
+                          int nthreads) {
+  using LD = long double;
+  const UMesh<double> m{faceNorm, faceMidPt, nF, normals, nN, {box[0], box[1], box[2]}, {box[3], box[4], box[5]},
+                        {C[0], C[1], C[2]}, tol};
+  const std::vector<UTri<double>> tris = u_tilde_triangles<double>(m, coord, label, links, bVec, numNode, numSeg);
+  std::vector<UTri<LD>> tl;
+  auto up = [](const V3<double>& v) { return V3<LD>{(LD)v.x, (LD)v.y, (LD)v.z}; };
+  for (const auto& t : tris) tl.push_back(make_tri(up(t.A), up(t.B), up(t.C), up(t.b), t.full));
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads)
+  for (int64_t p = 0; p < M; ++p) {
+    const V3<LD> P = {(LD)points[3 * p], (LD)points[3 * p + 1], (LD)points[3 * p + 2]};
+    V3<LD> acc = {0, 0, 0};
+    for (const auto& t : tl) acc = acc + tri_u(t, (LD)k2[0], (LD)k2[1], P);
+    u[3 * p] = (double)acc.x;
+    u[3 * p + 1] = (double)acc.y;
+    u[3 * p + 2] = (double)acc.z;
+  }
+  return (int64_t)tris.size();
+}
+
 // PK forces (σ̂ b) × (n2 - n1) of the segments in idx (or 1:numSeg) from the
 // stresses sigmaHat (6 × n, one per entry, at the segment midpoints): PK
 // (3 × n, overwritten; 0 where extSeg[k]).

@@ -24,6 +24,7 @@
 //   src/Processing/DislocationFEM.jl:86-303       _calc_σTilde!
 //   src/Misc/Misc.jl:314-367                      minimumDistance
 //   src/Processing/DislocationTopologyCollision.jl:1-221  detectCollision
+//   src/Processing/DislocationFEM.jl:354-751      calc_uTilde, Barnett triangles
 #pragma once
 #include <cmath>
 #include <cstdint>
@@ -1102,6 +1103,189 @@ Collision detect_collision(T collisionDistSq, const T* coord, const T* nodeVel, 
   r.L1 = L1;
   r.L2 = L2;
   return r;
+}
+
+// ---------------------------------------------------------------------------
+// calc_uTilde (DislocationFEM.jl:354-632): displacements at FE nodes from
+// Barnett triangles (Bromage & Tarleton 2018) closing each segment on a point.
+
+// safeNorm (Misc.jl:289-300): returns |x| and normalises x, or eps and zero.
+template <class T> inline T safe_norm(V3<T>& x) {
+  const T eps = std::numeric_limits<T>::epsilon();
+  T n = norm(x);
+  if (n > eps) {
+    x = normalize(x);
+  } else {
+    x = {T(0), T(0), T(0)};
+    n = eps;
+  }
+  return n;
+}
+// π as the reference's Float64 arithmetic uses it, and to full precision for
+// the long double evaluation.
+template <class T> inline T pi_of() { return T(3.141592653589793); }
+template <> inline long double pi_of<long double>() { return 3.141592653589793238462643383279502884L; }
+template <class T> inline T jl_sign(T x) { return x > T(0) ? T(1) : (x < T(0) ? T(-1) : x); }
+// Julia's max(x, 0): -0.0 and negatives give +0.0, NaN stays.
+template <class T> inline T jl_max0(T x) { return std::isnan(x) ? x : ((x < T(0) || std::signbit(x)) ? T(0) : x); }
+template <class T> inline T clamp11(T x) { return x > T(1) ? T(1) : (x < T(-1) ? T(-1) : x); }
+
+// One triangle ABC with Burgers vector b; full = the form with matParams
+// (solid angle, f and g terms, DislocationFEM.jl:651-707), else the solid-angle
+// form (:708-751).  AB, BC, CA are the safeNorm'ed edge directions.
+template <class T> struct UTri {
+  V3<T> A, B, C, b, AB, BC, CA;
+  bool full;
+};
+
+template <class T> inline UTri<T> make_tri(const V3<T>& A, const V3<T>& B, const V3<T>& C, const V3<T>& b, bool full) {
+  UTri<T> t{A, B, C, b, B - A, C - B, A - C, full};
+  safe_norm(t.AB);
+  safe_norm(t.BC);
+  safe_norm(t.CA);
+  return t;
+}
+
+template <class T> inline V3<T> tri_u(const UTri<T>& t, T omNuInv8pi, T om2NuOmNuInv8pi, const V3<T>& P) {
+  using std::acos;
+  using std::atan;
+  using std::log;
+  using std::sqrt;
+  using std::tan;
+  const T fourPi = T(4) * pi_of<T>();
+  V3<T> RA = t.A - P, RB = t.B - P, RC = t.C - P;
+  const T RAn = safe_norm(RA), RBn = safe_norm(RB), RCn = safe_norm(RC);
+  const T RAdRB = clamp11(dot(RA, RB)), RBdRC = clamp11(dot(RB, RC)), RCdRA = clamp11(dot(RC, RA));
+  const T ta = acos(RAdRB), tb = acos(RBdRC), tc = acos(RCdRA);
+  const T th = (ta + tb + tc) / T(2);
+  const T factor = jl_max0(tan(th / T(2)) * tan((th - ta) / T(2)) * tan((th - tb) / T(2)) * tan((th - tc) / T(2)));
+  T omega = T(4) * atan(sqrt(factor));
+  omega = -jl_sign(dot(RA, cross(t.CA, t.AB))) * omega;
+  const V3<T> nb = -t.b;
+  V3<T> u = {nb.x * omega / fourPi, nb.y * omega / fourPi, nb.z * omega / fourPi};
+  if (!t.full) return u;
+  const V3<T> fAB = cross(t.b, t.AB) * log((RBn / RAn) * (T(1) + dot(RB, t.AB)) / (T(1) + dot(RA, t.AB)));
+  const V3<T> fBC = cross(t.b, t.BC) * log((RCn / RBn) * (T(1) + dot(RC, t.BC)) / (T(1) + dot(RB, t.BC)));
+  const V3<T> fCA = cross(t.b, t.CA) * log((RAn / RCn) * (T(1) + dot(RA, t.CA)) / (T(1) + dot(RC, t.CA)));
+  auto g = [](T s, const V3<T>& v, T den) { return V3<T>{s * v.x / den, s * v.y / den, s * v.z / den}; };
+  const V3<T> gAB = g(dot(t.b, cross(RA, RB)), RA + RB, T(1) + RAdRB);
+  const V3<T> gBC = g(dot(t.b, cross(RB, RC)), RB + RC, T(1) + RBdRC);
+  const V3<T> gCA = g(dot(t.b, cross(RC, RA)), RC + RA, T(1) + RCdRA);
+  return u - om2NuOmNuInv8pi * (fAB + fBC + fCA) + omNuInv8pi * (gAB + gBC + gCA);
+}
+
+// The mesh data calc_uTilde reads: face normals and midpoints (3 × nF), the
+// projection directions (3 × nN), the volume as a box [lo, hi] for the "inside
+// the mesh" test (LazySets' polytope membership in the reference, here an
+// inclusive box test widened by tol), and the closure point C.
+template <class T> struct UMesh {
+  const T* faceNorm;
+  const T* faceMidPt;
+  int64_t nF;
+  const T* normals;
+  int64_t nN;
+  V3<T> lo, hi, C;
+  T tol;
+};
+
+template <class T> inline bool inside_mesh(const UMesh<T>& m, const V3<T>& p) {
+  return p.x >= m.lo.x - m.tol && p.x <= m.hi.x + m.tol && p.y >= m.lo.y - m.tol && p.y <= m.hi.y + m.tol &&
+         p.z >= m.lo.z - m.tol && p.z <= m.hi.z + m.tol;
+}
+
+// findIntersectVolume (DislocationTopologySpecial.jl:7-34) with
+// linePlaneIntersect (Misc.jl:223-235): the smallest squared distance from l0
+// to the intersection of the line (l0, l) with a face plane inside the mesh.
+template <class T> inline T find_intersect_volume(const UMesh<T>& m, const V3<T>& l, const V3<T>& l0, V3<T>& node) {
+  T distMin = std::numeric_limits<T>::infinity();
+  node = {T(0), T(0), T(0)};
+  for (int64_t i = 0; i < m.nF; ++i) {
+    const V3<T> n = {m.faceNorm[3 * i], m.faceNorm[3 * i + 1], m.faceNorm[3 * i + 2]};
+    const V3<T> p0 = {m.faceMidPt[3 * i], m.faceMidPt[3 * i + 1], m.faceMidPt[3 * i + 2]};
+    const T den = dot(l, n);
+    const T num = dot(p0 - l0, n);
+    if (den == T(0)) continue;  // parallel: no point (or the Inf marker), skipped either way
+    const T d = num / den;
+    const V3<T> it = l0 + d * l;
+    if (std::isinf(it.x) || std::isinf(it.y) || std::isinf(it.z) || !inside_mesh(m, it)) continue;
+    const V3<T> dv = it - l0;
+    const T oldMin = distMin;
+    const T s = dv.x * dv.x + dv.y * dv.y + dv.z * dv.z;
+    distMin = s < oldMin ? s : oldMin;
+    if (distMin < oldMin) node = it;
+  }
+  return distMin;
+}
+
+// The triangles of _calc_uTilde! (DislocationFEM.jl:399-632) in the order the
+// reference evaluates them: one full triangle (A, B, C) per internal segment;
+// for a segment with an external node, five solid-angle triangles through the
+// points A' and B' the nodes were projected out from and C' = (A + B') / 2.
+// Segments joining a surface node to an external node only record that
+// connection (and only for the segments after them, as the reference's loop
+// builds the record as it goes).
+template <class T>
+std::vector<UTri<T>> u_tilde_triangles(const UMesh<T>& m, const T* coord, const int32_t* label, const int64_t* links,
+                                       const T* bVec, int64_t numNode, int64_t numSeg) {
+  auto srf = [](int32_t l) { return l == 3 || l == 4; };  // srfMobDln, srfFixDln
+  const int32_t ext = 5;                                  // extDln
+  std::vector<UTri<T>> tris;
+  std::vector<int64_t> surfNodeCons((size_t)numNode, 0);
+  auto X = [&](int64_t n) { return V3<T>{coord[3 * n], coord[3 * n + 1], coord[3 * n + 2]}; };
+  for (int64_t i = 0; i < numSeg; ++i) {
+    const int64_t l1 = links[2 * i], l2 = links[2 * i + 1];
+    if (srf(label[l1 - 1]) && label[l2 - 1] == ext) {
+      surfNodeCons[l2 - 1] = l1;
+      continue;
+    }
+    if (srf(label[l2 - 1]) && label[l1 - 1] == ext) {
+      surfNodeCons[l1 - 1] = l2;
+      continue;
+    }
+    const V3<T> A = X(l1 - 1), B = X(l2 - 1);
+    const V3<T> b = {bVec[3 * i], bVec[3 * i + 1], bVec[3 * i + 2]};
+    if (label[l1 - 1] != ext && label[l2 - 1] != ext) {
+      tris.push_back(make_tri(A, B, m.C, b, true));
+      continue;
+    }
+    const T inf = std::numeric_limits<T>::infinity();
+    T distMinA = inf, distMinB = inf, distMinC = inf;
+    V3<T> intersectA = {inf, inf, inf}, intersectB = {inf, inf, inf};
+    for (int64_t j = 0; j < m.nN; ++j) {
+      const V3<T> l = {m.normals[3 * j], m.normals[3 * j + 1], m.normals[3 * j + 2]};
+      V3<T> iA, iB;
+      const T dA = find_intersect_volume(m, l, A, iA);
+      const T dB = find_intersect_volume(m, l, B, iB);
+      if (dA < distMinA) distMinA = dA, intersectA = iA;
+      if (dB < distMinB) distMinB = dB, intersectB = iB;
+    }
+    // Out of an edge or a corner: walk the face planes towards the centre.
+    // distMinC is shared by the two walks, as in the reference.
+    auto walk = [&](V3<T> P) {
+      for (int64_t f = 0; f < m.nF; ++f) {
+        const V3<T> n = {m.faceNorm[3 * f], m.faceNorm[3 * f + 1], m.faceNorm[3 * f + 2]};
+        const V3<T> mp = {m.faceMidPt[3 * f], m.faceMidPt[3 * f + 1], m.faceMidPt[3 * f + 2]};
+        const T q = dot(P + mp, n);
+        const T dist = q * q;
+        const V3<T> it = P - n * std::sqrt(dist);
+        const T dc = norm(it - m.C);
+        if (dc <= distMinC) distMinC = dc, P = it;
+      }
+      return P;
+    };
+    if (std::isinf(distMinA)) intersectA = walk(A);
+    if (std::isinf(distMinB)) intersectB = walk(B);
+    V3<T> Ap = intersectA, Bp = intersectB;
+    if (surfNodeCons[l1 - 1] != 0) Ap = X(surfNodeCons[l1 - 1] - 1);
+    if (surfNodeCons[l2 - 1] != 0) Bp = X(surfNodeCons[l2 - 1] - 1);
+    const V3<T> Cp = {(A.x + Bp.x) / T(2), (A.y + Bp.y) / T(2), (A.z + Bp.z) / T(2)};
+    tris.push_back(make_tri(Ap, Bp, m.C, b, false));
+    tris.push_back(make_tri(Ap, A, Cp, b, false));
+    tris.push_back(make_tri(A, B, Cp, b, false));
+    tris.push_back(make_tri(B, Bp, Cp, b, false));
+    tris.push_back(make_tri(Bp, Ap, Cp, b, false));
+  }
+  return tris;
 }
 
 }  // namespace ddd_oracle

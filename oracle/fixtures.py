@@ -187,3 +187,57 @@ def make_connectivity(links, max_connect=4):
         conn[t1 - 1:t1 + 1, n1] = (i + 1, 1)
         conn[t2 - 1:t2 + 1, n2] = (i + 1, 2)
     return conn
+
+
+def cuboid_mesh(dx, dy, dz, mx, my, mz):
+    """The geometry of buildMesh for a regular cuboid (FEMConstructor.jl:130-480):
+    FE node coordinates (3 × (mx+1)(my+1)(mz+1), node i + (j-1)(mx+1) +
+    (k-1)(mx+1)(my+1) at ((i-1)w, (j-1)h, (k-1)d)), the 8 vertices, face normals
+    and face midpoints (3 × 6, faces xz@y0, yz@x1, xz@y1, yz@x0, xy@z0, xy@z1),
+    and the closure point mean(vertices) summed in order."""
+    w, h, d = dx / mx, dy / my, dz / mz
+    mx1, my1, mz1 = mx + 1, my + 1, mz + 1
+    coord = np.zeros((3, mx1 * my1 * mz1), order="F")
+    for k in range(mz1):
+        for j in range(my1):
+            for i in range(mx1):
+                g = i + j * mx1 + k * mx1 * my1
+                coord[:, g] = (i * w, j * h, k * d)
+    vtx = np.array([[0, 0, 0], [dx, 0, 0], [dx, dy, 0], [0, dy, 0], [0, 0, dz], [dx, 0, dz], [dx, dy, dz],
+                    [0, dy, dz]], np.float64).T
+    faces = np.array([[1, 2, 6, 5], [2, 3, 7, 6], [3, 4, 8, 7], [4, 1, 5, 8], [4, 3, 2, 1], [5, 6, 7, 8]]).T - 1
+    mid = np.zeros((3, 6))
+    for f in range(6):
+        s = vtx[:, faces[0, f]].copy()
+        for q in range(1, 4):
+            s = s + vtx[:, faces[q, f]]
+        mid[:, f] = s / 4
+    norm = np.array([[0, -1, 0], [1, 0, 0], [0, 1, 0], [-1, 0, 0], [0, 0, -1], [0, 0, 1]], np.float64).T
+    c = vtx[:, 0].copy()
+    for q in range(1, 8):
+        c = c + vtx[:, q]
+    return {"coord": coord, "vertices": vtx, "faceNorm": np.asfortranarray(norm), "faceMidPt": np.asfortranarray(mid),
+            "C": c / 8, "lo": vtx.min(axis=1), "hi": vtx.max(axis=1)}
+
+
+def cantilever_u_gamma(mx, my, mz):
+    """Boundaries(::CantileverLoad) (FEMConstructor.jl:761-850, 968-987):
+    uGammaDln = [uGamma nodes; mGamma nodes] from the mesh's surface node sets
+    (FEMConstructor.jl:274-300, 495-545) and uDofsDln = [3u-2; 3u-1; 3u]."""
+    mx1, my1, mz1 = mx + 1, my + 1, mz + 1
+    mxm1, mym1, mzm1 = mx - 1, my - 1, mz - 1
+    s = {
+        "x0y0z0": [1], "x0y1z0": [mx1 * my + 1], "x0y0z1": [1 + mx1 * my1 * mz],
+        "x0y1z1": [mx1 * my + 1 + mx1 * my1 * mz], "x1y0z1": [mx1 + mx1 * my1 * mz], "x1y1z1": [mx1 * my1 * mz1],
+        "y_x0z0": [i * mx1 + 1 for i in range(1, mym1 + 1)],
+        "y_x0z1": [i * mx1 + 1 + mx1 * my1 * mz for i in range(1, mym1 + 1)],
+        "y_x1z1": [i * mx1 + mx1 + mx1 * my1 * mz for i in range(1, mym1 + 1)],
+        "z_x0y0": [i * mx1 * my1 + 1 for i in range(1, mzm1 + 1)],
+        "z_x0y1": [i * mx1 * my1 + 1 + mx1 * my for i in range(1, mzm1 + 1)],
+        "yz_x0": [j * mx1 * my1 + 1 + i * mx1 for j in range(1, mzm1 + 1) for i in range(1, mym1 + 1)],
+    }
+    u = ["x0y0z0", "x0y1z0", "x0y0z1", "x0y1z1", "y_x0z0", "y_x0z1", "z_x0y0", "z_x0y1", "yz_x0"]
+    m = ["x1y0z1", "x1y1z1", "y_x1z1"]
+    nodes = np.array([n for k in u + m for n in s[k]], np.int64)
+    dofs = np.concatenate([3 * nodes - 2, 3 * nodes - 1, 3 * nodes])
+    return nodes, dofs

@@ -54,6 +54,12 @@ def lib():
         L.oracle_mobility_bcc.argtypes = [_dp, _dp, _dp, _ip, _ip, ctypes.c_int64, _dp, ctypes.c_int64, _ip,
                                           ctypes.c_int64, _dp, _dp]
         L.oracle_minimum_distance.argtypes = [_dp, ctypes.c_int64, _dp]
+        L.oracle_u_tilde.argtypes = [_dp, _dp, _dp, _dp, ctypes.c_int64, _dp, ctypes.c_int64, _dp, ctypes.c_double,
+                                     _dp, ctypes.c_int64, _dp, ctypes.POINTER(ctypes.c_int32), _ip, _dp,
+                                     ctypes.c_int64, ctypes.c_int64, _dp, ctypes.c_int]
+        L.oracle_u_tilde.restype = ctypes.c_int64
+        L.oracle_u_tilde_ld.argtypes = L.oracle_u_tilde.argtypes
+        L.oracle_u_tilde_ld.restype = ctypes.c_int64
         L.oracle_detect_collision.argtypes = [ctypes.c_double, _dp, _dp, ctypes.POINTER(ctypes.c_int32), _ip, _dp, _ip,
                                               ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, _ip, ctypes.c_int64,
                                               _ip, _dp]
@@ -194,6 +200,31 @@ def minimum_distance(x0, x1, y0, y1, vx0, vx1, vy0, vy1):
     out = np.zeros((4, n), np.float64, order="F")
     lib().oracle_minimum_distance(_d(pts), n, _d(out))
     return out[0], out[1], out[2], out[3]
+
+
+def u_tilde(k2, mesh, normals, points, coord, label, links, bvec, num_node, num_seg, tol=None, nthreads=1,
+            long_double=False):
+    """calc_uTilde's displacements (3 × M) at points (3 × M); mesh: the dict of
+    fixtures.cuboid_mesh (faceNorm, faceMidPt, C, lo, hi); normals 3 × K.
+    long_double: the same triangles summed in long double (the reference
+    arithmetic's error is the difference).  Returns (u, number of triangles)."""
+    pts = np.require(points, np.float64, ["F"])
+    M = pts.shape[1]
+    u = np.zeros((3, M), np.float64, order="F")
+    fn = np.require(mesh["faceNorm"], np.float64, ["F"])
+    fm = np.require(mesh["faceMidPt"], np.float64, ["F"])
+    nr = np.require(normals, np.float64, ["F"])
+    box = np.ascontiguousarray(np.r_[mesh["lo"], mesh["hi"]], np.float64)
+    if tol is None:
+        tol = 1e-10 * float(np.max(mesh["hi"] - mesh["lo"]))
+    lab = np.ascontiguousarray(label, np.int32)
+    fn_ = lib().oracle_u_tilde_ld if long_double else lib().oracle_u_tilde
+    nt = fn_(_d(np.ascontiguousarray(k2, np.float64)), _d(np.ascontiguousarray(mesh["C"], np.float64)),
+             _d(fn), _d(fm), fn.shape[1], _d(nr), nr.shape[1], _d(box), float(tol), _d(pts), M,
+             _d(np.require(coord, np.float64, ["F"])), lab.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+             _i(np.require(links, np.int64, ["F"])), _d(np.require(bvec, np.float64, ["F"])), int(num_node),
+             int(num_seg), _d(u), int(nthreads))
+    return u, int(nt)
 
 
 _COLLISION_TYPES = ("null", "hinge", "twoLine")

@@ -16,6 +16,11 @@ matrices they assert against into JSON fixtures beside this script:
                         triangle and a 4-node loop under 17 skip lists (hinge
                         and twoLine results), and test/MiscTest.jl:82-150 —
                         minimumDistance on 9 segment pairs
+  u_tilde_goldens.json  test/DislocationFEMTest.jl:270-1000 — calc_uTilde on a
+                        3 × 5 × 7 cuboid mesh (1013 × 1987 × 2999) with a
+                        prismatic and a shear octagon at its centre: ux, uy, uz at
+                        the cantilever's displacement nodes, and the full
+                        calc_uTilde! vector
   sigma_goldens.json    test/DislocationFEMTest.jl:5-155 — one edge and one
                         screw segment, σ̃ at a 3×3 grid (columns 5 and 6 of the
                         golden are (yz, xz), the code's order is (xz, yz))
@@ -88,6 +93,35 @@ def _safe_value(expr, env):
         raise ValueError("unsupported expression: " + ast.dump(n))
 
     return ev(expr)
+
+
+def _comma_vector(block, name):
+    m = re.search(r"\b" + re.escape(name) + r"\s*=\s*\[([^\]]*)\]", block)
+    return [float(v) for v in m.group(1).replace("\n", " ").split(",") if v.strip()]
+
+
+def u_tilde_goldens(ref):
+    """The "Calculate uTilde" testset of DislocationFEMTest.jl."""
+    t = open(os.path.join(ref, "test", "DislocationFEMTest.jl")).read()
+    blk = t[t.index('@testset "Calculate uTilde"'):]
+    num = lambda name: float(re.search(r"\b" + name + r"\s*=\s*([0-9.eE+-]+)", blk).group(1))
+    vec = lambda name: [float(v) for v in re.search(name + r"\s*=\s*Float64\[([^\]]*)\]", blk).group(1).split(";")]
+    dims = {k: num(k) for k in ("dx", "dy", "dz")}
+    cells = {k: int(num(k)) for k in ("mx", "my", "mz")}
+    seg_len = (dims["dx"] + dims["dy"] + dims["dz"]) / 30
+    loops = []
+    for kind in ("loopPrism", "loopShear"):
+        assert kind + "()" in blk
+        loops.append({"type": "prism" if kind == "loopPrism" else "shear", "numSides": 8, "nodeSide": 1,
+                      "numLoops": 1, "segLen": seg_len, "slipSystemIdx": 1, "label": [1] * 8})
+    centre = [dims["dx"] / 2, dims["dy"] / 2, dims["dz"] / 2]
+    json.dump({"mesh": dict(dims, **cells), "nu": num("ν"), "mu": 1.0,
+               "slipSystems": {"slipPlane": [vec("slipPlane")], "bVec": [vec("bVec")]},
+               "loops": loops, "range": [[c, c] for c in centre],
+               "ux": _comma_vector(blk, "uxTest"), "uy": _comma_vector(blk, "uyTest"),
+               "uz": _comma_vector(blk, "uzTest"), "uTildeFull": _comma_vector(blk, "uTildeTest"),
+               "rtol": 5e-5},
+              open(os.path.join(HERE, "u_tilde_goldens.json"), "w"), indent=1)
 
 
 def collision_goldens(ref):
@@ -243,6 +277,7 @@ def main(ref):
         c["golden_columns"] = ["xx", "yy", "zz", "xy", "yz", "xz"]
     json.dump({"cases": scases}, open(os.path.join(HERE, "sigma_goldens.json"), "w"), indent=1)
     collision_goldens(ref)
+    u_tilde_goldens(ref)
 
 
 if __name__ == "__main__":

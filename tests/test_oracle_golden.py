@@ -254,3 +254,40 @@ def test_minimum_distance_matches_golden(oracle):
         v = c["inputs"]
         out = oracle.minimum_distance(*(np.array(v[k]) for k in ("x0", "x1", "y0", "y1", "vx0", "vx1", "vy0", "vy1")))
         assert [float(o[0]) for o in out] == c["expected"], (v, out)
+
+
+G_U = json.load(open(os.path.join(GOLDEN, "u_tilde_goldens.json")))
+
+
+def u_tilde_case(fixtures):
+    """The DislocationFEMTest.jl "Calculate uTilde" setup: mesh, network, the
+    cantilever's displacement nodes and dofs, (omνInv8π, om2νomνInv8π)."""
+    g, m = G_U, G_U["mesh"]
+    mesh = fixtures.cuboid_mesh(m["dx"], m["dy"], m["dz"], m["mx"], m["my"], m["mz"])
+    net = fixtures.make_network(g["loops"], g["slipSystems"], g["range"])
+    nodes, dofs = fixtures.cantilever_u_gamma(m["mx"], m["my"], m["mz"])
+    nu = g["nu"]
+    om_nu_inv8pi = (1 / (1 - nu)) / (8 * np.pi)
+    return mesh, net, nodes, dofs, np.array([om_nu_inv8pi, (1 - 2 * nu) * om_nu_inv8pi])
+
+
+def test_u_tilde_matches_golden(oracle, fixtures):
+    """calc_uTilde (DislocationFEM.jl:354-751) against
+    test/DislocationFEMTest.jl:270-1000 (the test's rtol is 5e-5; the restatement
+    agrees to 1e-12), and calc_uTilde!'s full vector through uDofsDln."""
+    mesh, net, nodes, dofs, k2 = u_tilde_case(fixtures)
+    pts = np.asfortranarray(mesh["coord"][:, nodes - 1])
+    links = np.asfortranarray(net.segIdx[:, 1:3].T)
+    label = np.ones(net.coord.shape[1], np.int32)
+    u, ntri = oracle.u_tilde(k2, mesh, mesh["faceNorm"][:, 0:5:2], pts, net.coord, label, links, net.bVec,
+                             net.coord.shape[1], net.numSeg)
+    assert ntri == 16
+    for c, key in enumerate(("ux", "uy", "uz")):
+        gold = np.array(G_U[key])
+        assert np.linalg.norm(u[c] - gold) <= 1e-12 * np.linalg.norm(gold)
+    full = np.zeros(mesh["coord"].shape[1] * 3)
+    flat = u.ravel(order="F")
+    for k, d in enumerate(dofs):
+        full[d - 1] += flat[k]
+    gold = np.array(G_U["uTildeFull"])
+    assert np.linalg.norm(full - gold) <= 1e-12 * np.linalg.norm(gold)
