@@ -275,14 +275,16 @@ class DislocationNetwork:
     1-based), extSeg (linkBuf), segForce (3×2×linkBuf), numSeg; for the
     mobility also links (2×linkBuf), connectivity ((1+2 maxConnect)×nodeBuf),
     numNode, nodeForce and nodeVel (3×nodeBuf); for collision detection also
-    label (nodeBuf int32, the nodeTypeDln values; default 1 = intMobDln).
+    label (nodeBuf int32, the nodeTypeDln values; default 1 = intMobDln);
+    slipPlane and linksConnect are carried for the JSON files.
     links defaults to segIdx's node columns and connectivity to the one
     _makeConnect! builds from it.
     Stored Fortran-ordered, which is the Julia memory image.
     """
 
     def __init__(self, coord, bVec, segIdx, numSeg=None, extSeg=None, segForce=None, links=None,
-                 connectivity=None, numNode=None, nodeForce=None, nodeVel=None, maxConnect=4, label=None):
+                 connectivity=None, numNode=None, nodeForce=None, nodeVel=None, maxConnect=4, label=None,
+                 slipPlane=None, linksConnect=None):
         self.coord = np.asfortranarray(coord, dtype=np.float64)
         self.bVec = np.asfortranarray(bVec, dtype=np.float64)
         self.segIdx = np.asfortranarray(segIdx, dtype=np.int64)
@@ -304,6 +306,11 @@ class DislocationNetwork:
                         else np.asfortranarray(nodeVel, dtype=np.float64))
         self.label = (np.ones(nodes, np.int32) if label is None
                       else np.ascontiguousarray(np.asarray(label).astype(np.int32)))
+        nl = self.bVec.shape[1]
+        self.slipPlane = (np.zeros((3, nl), np.float64, order="F") if slipPlane is None
+                          else np.asfortranarray(slipPlane, dtype=np.float64))
+        self.linksConnect = (np.zeros((2, nl), np.int64, order="F") if linksConnect is None
+                             else np.asfortranarray(linksConnect, dtype=np.int64))
 
 
 def make_connectivity(links, num_node, max_connect=4):
@@ -1054,3 +1061,5 @@ calc_sigmaTilde_inplace = calc_σTilde_inplace
 
 
 from . import fem  # noqa: E402  (RegularCuboidMesh, Boundaries, cantilever_boundaries, ForceDisplacement)
+from . import json_io  # noqa: E402
+from .json_io import loadJSON, loadNetwork, saveJSON  # noqa: E402,F401

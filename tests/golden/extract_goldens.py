@@ -21,6 +21,10 @@ matrices they assert against into JSON fixtures beside this script:
                         prismatic and a shear octagon at its centre: ux, uy, uz at
                         the cantilever's displacement nodes, and the full
                         calc_uTilde! vector
+  sample_params.json    test/testData/sampleDislocationParameters.json,
+                        sampleMaterialParameters.json and BCC.json as parsed
+                        data (the JSON loaders' inputs; the material file also
+                        holds Julia-computed derived constants)
   sigma_goldens.json    test/DislocationFEMTest.jl:5-155 — one edge and one
                         screw segment, σ̃ at a 3×3 grid (columns 5 and 6 of the
                         golden are (yz, xz), the code's order is (xz, yz))
@@ -278,6 +282,11 @@ def main(ref):
     json.dump({"cases": scases}, open(os.path.join(HERE, "sigma_goldens.json"), "w"), indent=1)
     collision_goldens(ref)
     u_tilde_goldens(ref)
+    td = os.path.join(ref, "test", "testData")
+    json.dump({k: json.load(open(os.path.join(td, f))) for k, f in
+               (("dislocationParameters", "sampleDislocationParameters.json"),
+                ("materialParameters", "sampleMaterialParameters.json"), ("slipSystem", "BCC.json"))},
+              open(os.path.join(HERE, "sample_params.json"), "w"), indent=1, ensure_ascii=False)
 
 
 if __name__ == "__main__":
