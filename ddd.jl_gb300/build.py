@@ -31,6 +31,7 @@ VARIANTS = {
     "mobility.cu": [("", ["--fmad=false"])],
     "collision.cu": [("", ["--fmad=false"])],
     "u_tilde.cu": [("", ["--fmad=false", "-Xcompiler", "-ffp-contract=off"])],
+    "u_tilde_fast.cu": [("", ["--fmad=false"])],
 }
 
 

@@ -1099,6 +1099,7 @@ int ddd_u_tilde(ddd_ctx* ctx, double omNuInv8pi, double om2NuOmNuInv8pi, const d
   for (int64_t q = 0; q < 3 * numNode; ++q)
     if (!std::isfinite(coord[q])) return fail(ctx, DDD_ENONFINITE, "non-finite node coordinate");
   ddd::UTildeArgs a{};
+  a.fast = ctx->mode != DDD_MODE_FP64;
   a.omNuInv8pi = omNuInv8pi;
   a.om2NuOmNuInv8pi = om2NuOmNuInv8pi;
   double ext = 0.0;

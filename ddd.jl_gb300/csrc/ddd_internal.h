@@ -134,8 +134,11 @@ struct GrowBuf {
 // numPoints).  The host arrays drive the segment pass; the *Dev copies feed the
 // kernels.  Mesh: closure point C, volume box [lo, hi] widened by tol, face
 // normals / midpoints (3 x numFaces), projection directions (3 x numNormals).
+// Doubles per triangle in the field kernels' table (u_tilde.cu lays it out).
+constexpr int kUTriRows = 32;
 struct UTildeArgs {
   double omNuInv8pi, om2NuOmNuInv8pi;
+  bool fast;  // the reformulated FP64 kernel (u_tilde_fast.cu) instead of the reference's formulas
   double C[3], lo[3], hi[3], tol;
   const double* faceNorm;
   const double* faceMidPt;
@@ -155,11 +158,16 @@ struct UTildeArgs {
 struct UTildeScratch {
   std::vector<int64_t> order;
   std::vector<double> explicitTri;
-  GrowBuf order_d, ex_d, tri_d, u_d;
-  int64_t lastTriangles = 0;
+  GrowBuf order_d, ex_d, tri_d, u_d, part_d;
+  int64_t lastTriangles = 0, lastChunks = 0;
+  int sms = 0;
 };
 cudaError_t u_tilde_compute(const UTildeArgs& a, double* u, cudaEvent_t e0, cudaEvent_t e1, cudaStream_t st,
                             UTildeScratch& S);
+// Partial sums part[k][p] over triangle chunk k (K chunks of `chunk`).
+cudaError_t launch_u_field_fast(const double* tri, int64_t nTri, int64_t chunk, int64_t K, const double* points,
+                                int64_t M, double omNuInv8pi, double om2NuOmNuInv8pi, const double C[3], double* part,
+                                cudaStream_t st);
 
 // ddd_api.cu: context accessors for the other C-ABI files.
 int ctx_device(const ddd_ctx* c);

@@ -14,6 +14,7 @@
 // GPU: tri_prep builds every triangle's vertices and safeNorm'ed edges;
 // u_field gives each point one thread that sums the triangles in the
 // reference's order, triangles streamed through shared memory.
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstdint>
@@ -28,7 +29,7 @@ namespace {
 
 constexpr int PT = 128;   // points per CTA of the field kernel
 constexpr int TCH = 32;   // triangles per shared-memory chunk
-constexpr int TROW = 22;  // doubles per triangle: A, B, C, b, AB, BC, CA, full flag
+constexpr int TROW = kUTriRows;  // doubles per triangle (layout below)
 
 struct V {
   double x, y, z;
@@ -60,7 +61,11 @@ __device__ __forceinline__ double jl_sign(double x) { return x > 0.0 ? 1.0 : (x 
 __device__ __forceinline__ double jl_max0(double x) { return isnan(x) ? x : ((x < 0.0 || signbit(x)) ? 0.0 : x); }
 
 // Triangle rows (SoA, T columns): 0-2 A, 3-5 B, 6-8 C, 9-11 b, 12-14 AB,
-// 15-17 BC, 18-20 CA, 21 full (1) or solid angle only (0).
+// 15-17 BC, 18-20 CA, 21 full (1) or solid angle only (0), 22 link flags:
+// +1 when C is the closure point, +2 when A is the previous triangle's B (the
+// field kernel then reuses R = C - P and the previous R_B, bit for bit), +4 /
+// +8 when the BC / CA edge term cancels against the next / previous triangle's
+// (the reformulated kernel skips both), 23-31 b x AB, b x BC, b x CA.
 // order[t] >= 0: internal segment order[t] (A, B its nodes, C the closure
 // point); order[t] < 0: explicit triangle -1 - order[t] (rows A, B, C, b of
 // explicit, 13 doubles each, the last the full flag).
@@ -90,20 +95,89 @@ __global__ void tri_prep(const int64_t* __restrict__ order, int64_t nTri, const 
   safe_norm(AB);
   safe_norm(BC);
   safe_norm(CA);
-  const double r[TROW] = {A.x,  A.y,  A.z,  B.x,  B.y,  B.z,  C.x,  C.y,  C.z,  b.x,  b.y,
-                          b.z,  AB.x, AB.y, AB.z, BC.x, BC.y, BC.z, CA.x, CA.y, CA.z, full};
+  const bool closure = C.x == Cl.x && C.y == Cl.y && C.z == Cl.z;
+  double link = closure ? 1.0 : 0.0;
+  // A pair of consecutive full triangles closed on C with the same b, the
+  // second starting where the first ends, share the edge (B_t, C) in opposite
+  // directions: its g terms are exact negatives and its f terms cancel
+  // (both logs reduce to the distance from P to the same line).
+  auto node_of = [&](int64_t tt, int which, V& X, V& bb, bool& isFull, bool& isClosure) {
+    const int64_t o = order[tt];
+    if (o >= 0) {
+      X = ld3(coord, links[2 * o + which] - 1);
+      bb = ld3(bVec, o);
+      isFull = true;
+      isClosure = true;
+    } else {
+      const double* e = explicitTri + 13 * (-1 - o);
+      X = {e[3 * which], e[3 * which + 1], e[3 * which + 2]};
+      bb = {e[9], e[10], e[11]};
+      isFull = e[12] != 0.0;
+      isClosure = e[6] == Cl.x && e[7] == Cl.y && e[8] == Cl.z;
+    }
+  };
+  auto same = [](V x, V y) { return x.x == y.x && x.y == y.y && x.z == y.z; };
+  if (t > 0) {  // the previous triangle's B
+    V Bp, bp;
+    bool fp, cp;
+    node_of(t - 1, 1, Bp, bp, fp, cp);
+    if (same(Bp, A)) {
+      link += 2.0;
+      if (fp && cp && full != 0.0 && closure && same(bp, b)) link += 8.0;  // CA cancels the previous BC
+    }
+  }
+  if (t + 1 < nTri) {  // the next triangle's A
+    V An, bn;
+    bool fn, cn;
+    node_of(t + 1, 0, An, bn, fn, cn);
+    if (same(An, B) && fn && cn && full != 0.0 && closure && same(bn, b)) link += 4.0;  // BC cancels the next CA
+  }
+  const V bAB = cross(b, AB), bBC = cross(b, BC), bCA = cross(b, CA);
+  const double r[TROW] = {A.x,   A.y,   A.z,   B.x,   B.y,   B.z,   C.x,   C.y,   C.z,   b.x,   b.y,
+                          b.z,   AB.x,  AB.y,  AB.z,  BC.x,  BC.y,  BC.z,  CA.x,  CA.y,  CA.z,  full,
+                          link,  bAB.x, bAB.y, bAB.z, bBC.x, bBC.y, bBC.z, bCA.x, bCA.y, bCA.z};
 #pragma unroll
   for (int k = 0; k < TROW; ++k) tri[k * nTri + t] = r[k];
 }
 
+// What a point's previous triangle leaves for the next one (valid once a
+// triangle of the thread's range has been evaluated).
+struct Chain {
+  V RB;
+  double RBn, tb;
+  bool closure, valid;
+};
+
 // One triangle at point P (calcDisplacementDislocationTriangle!, both forms).
-__device__ __forceinline__ V tri_u(const double* s, double omNuInv8pi, double om2NuOmNuInv8pi, V P) {
+// RCc / RCcn: C - P safeNorm'ed for the closure point; ch: the previous
+// triangle's R_B, |R_B| and acos(R_B . R_C) (valid when the flags say so).
+__device__ __forceinline__ V tri_u(const double* s, double omNuInv8pi, double om2NuOmNuInv8pi, V P, V RCc,
+                                   double RCcn, Chain& ch) {
   const V A = {s[0], s[1], s[2]}, B = {s[3], s[4], s[5]}, C = {s[6], s[7], s[8]}, b = {s[9], s[10], s[11]};
   const V AB = {s[12], s[13], s[14]}, BC = {s[15], s[16], s[17]}, CA = {s[18], s[19], s[20]};
-  V RA = A - P, RB = B - P, RC = C - P;
-  const double RAn = safe_norm(RA), RBn = safe_norm(RB), RCn = safe_norm(RC);
+  const int link = (int)s[22];
+  const bool closure = link & 1, chained = (link & 2) && ch.valid;
+  V RA, RB = B - P, RC;
+  double RAn, RCn;
+  if (chained) {
+    RA = ch.RB;
+    RAn = ch.RBn;
+  } else {
+    RA = A - P;
+    RAn = safe_norm(RA);
+  }
+  const double RBn = safe_norm(RB);
+  if (closure) {
+    RC = RCc;
+    RCn = RCcn;
+  } else {
+    RC = C - P;
+    RCn = safe_norm(RC);
+  }
   const double RAdRB = clamp11(dot(RA, RB)), RBdRC = clamp11(dot(RB, RC)), RCdRA = clamp11(dot(RC, RA));
-  const double ta = acos(RAdRB), tb = acos(RBdRC), tc = acos(RCdRA);
+  // RC . RA here equals the previous triangle's RB . RC term by term.
+  const double ta = acos(RAdRB), tb = acos(RBdRC), tc = (chained && closure && ch.closure) ? ch.tb : acos(RCdRA);
+  ch = {RB, RBn, tb, closure, true};
   const double th = (ta + tb + tc) / 2.0;
   const double factor =
       jl_max0(tan(th / 2.0) * tan((th - ta) / 2.0) * tan((th - tb) / 2.0) * tan((th - tc) / 2.0));
@@ -112,9 +186,10 @@ __device__ __forceinline__ V tri_u(const double* s, double omNuInv8pi, double om
   const double fourPi = 4.0 * 3.141592653589793;
   V u = {-b.x * omega / fourPi, -b.y * omega / fourPi, -b.z * omega / fourPi};
   if (s[21] == 0.0) return u;
-  const V fAB = cross(b, AB) * log((RBn / RAn) * (1.0 + dot(RB, AB)) / (1.0 + dot(RA, AB)));
-  const V fBC = cross(b, BC) * log((RCn / RBn) * (1.0 + dot(RC, BC)) / (1.0 + dot(RB, BC)));
-  const V fCA = cross(b, CA) * log((RAn / RCn) * (1.0 + dot(RA, CA)) / (1.0 + dot(RC, CA)));
+  const V bAB = {s[23], s[24], s[25]}, bBC = {s[26], s[27], s[28]}, bCA = {s[29], s[30], s[31]};
+  const V fAB = bAB * log((RBn / RAn) * (1.0 + dot(RB, AB)) / (1.0 + dot(RA, AB)));
+  const V fBC = bBC * log((RCn / RBn) * (1.0 + dot(RC, BC)) / (1.0 + dot(RB, BC)));
+  const V fCA = bCA * log((RAn / RCn) * (1.0 + dot(RA, CA)) / (1.0 + dot(RC, CA)));
   const double sAB = dot(b, cross(RA, RB)), sBC = dot(b, cross(RB, RC)), sCA = dot(b, cross(RC, RA));
   const V vAB = RA + RB, vBC = RB + RC, vCA = RC + RA;
   const double dAB = 1.0 + RAdRB, dBC = 1.0 + RBdRC, dCA = 1.0 + RCdRA;
@@ -126,16 +201,22 @@ __device__ __forceinline__ V tri_u(const double* s, double omNuInv8pi, double om
          V{omNuInv8pi * gs.x, omNuInv8pi * gs.y, omNuInv8pi * gs.z};
 }
 
-__global__ void __launch_bounds__(PT) u_field(const double* __restrict__ tri, int64_t nTri,
+// Block (x, y): points x * PT.., triangles [y * chunk, (y + 1) * chunk), in
+// order; partial sums to part[y][p] (the reduce kernel adds them in y order).
+__global__ void __launch_bounds__(PT) u_field(const double* __restrict__ tri, int64_t nTri, int64_t chunk,
                                               const double* __restrict__ points, int64_t M, double omNuInv8pi,
-                                              double om2NuOmNuInv8pi, double* __restrict__ u) {
+                                              double om2NuOmNuInv8pi, V Cl, double* __restrict__ part) {
   __shared__ double sm[TCH][TROW + 1];
   const int64_t p = blockIdx.x * (int64_t)PT + threadIdx.x;
   const bool on = p < M;
   const V P = on ? ld3(points, p) : V{0.0, 0.0, 0.0};
+  V RCc = V{Cl.x, Cl.y, Cl.z} - P;
+  const double RCcn = safe_norm(RCc);
+  Chain ch = {{0.0, 0.0, 0.0}, 0.0, 0.0, false, false};
   V acc = {0.0, 0.0, 0.0};
-  for (int64_t t0 = 0; t0 < nTri; t0 += TCH) {
-    const int n = (int)(nTri - t0 < TCH ? nTri - t0 : TCH);
+  const int64_t tBeg = blockIdx.y * chunk, tEnd = tBeg + chunk < nTri ? tBeg + chunk : nTri;
+  for (int64_t t0 = tBeg; t0 < tEnd; t0 += TCH) {
+    const int n = (int)(tEnd - t0 < TCH ? tEnd - t0 : TCH);
     __syncthreads();
     for (int q = threadIdx.x; q < n * TROW; q += PT) {
       const int tt = q % n, k = q / n;
@@ -143,13 +224,23 @@ __global__ void __launch_bounds__(PT) u_field(const double* __restrict__ tri, in
     }
     __syncthreads();
     if (on)
-      for (int tt = 0; tt < n; ++tt) acc = acc + tri_u(sm[tt], omNuInv8pi, om2NuOmNuInv8pi, P);
+      for (int tt = 0; tt < n; ++tt) acc = acc + tri_u(sm[tt], omNuInv8pi, om2NuOmNuInv8pi, P, RCc, RCcn, ch);
   }
   if (on) {
-    u[3 * p] = acc.x;
-    u[3 * p + 1] = acc.y;
-    u[3 * p + 2] = acc.z;
+    double* u = part + 3 * (blockIdx.y * M + p);
+    u[0] = acc.x;
+    u[1] = acc.y;
+    u[2] = acc.z;
   }
+}
+
+// u[p] = sum over k of part[k][p], k in order.
+__global__ void u_reduce(const double* __restrict__ part, int64_t K, int64_t M, double* __restrict__ u) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= 3 * M) return;
+  double s = part[q];
+  for (int64_t k = 1; k < K; ++k) s += part[k * 3 * M + q];
+  u[q] = s;
 }
 
 // ---- host: the segment pass of _calc_uTilde! -------------------------------
@@ -274,7 +365,20 @@ cudaError_t u_tilde_compute(const UTildeArgs& a, double* u, cudaEvent_t e0, cuda
   if ((e = S.order_d.ensure((size_t)std::max<int64_t>(nTri, 1) * 8)) != cudaSuccess) return e;
   if ((e = S.ex_d.ensure(std::max<size_t>(ex.size(), 1) * 8)) != cudaSuccess) return e;
   if ((e = S.tri_d.ensure((size_t)std::max<int64_t>(nTri, 1) * TROW * 8)) != cudaSuccess) return e;
+  // Triangle chunks: enough CTAs to fill the GPU (about 4 per SM), at least
+  // 256 triangles each; one chunk keeps each point's sum strictly sequential.
+  if (!S.sms) {
+    int dev = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&S.sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  }
+  const int64_t bx = (a.numPoints + PT - 1) / PT;
+  const int64_t want = std::max<int64_t>(1, (4 * (int64_t)S.sms + bx - 1) / std::max<int64_t>(bx, 1));
+  const int64_t K = std::max<int64_t>(1, std::min<int64_t>({want, (nTri + 255) / 256, 65535}));
+  const int64_t chunk = std::max<int64_t>(1, (nTri + K - 1) / K);
+  S.lastChunks = K;
   if ((e = S.u_d.ensure((size_t)std::max<int64_t>(a.numPoints, 1) * 3 * 8)) != cudaSuccess) return e;
+  if ((e = S.part_d.ensure((size_t)std::max<int64_t>(a.numPoints, 1) * 3 * 8 * K)) != cudaSuccess) return e;
   if (nTri > 0 &&
       (e = cudaMemcpyAsync(S.order_d.p, order.data(), (size_t)nTri * 8, cudaMemcpyHostToDevice, st)) != cudaSuccess)
     return e;
@@ -288,10 +392,19 @@ cudaError_t u_tilde_compute(const UTildeArgs& a, double* u, cudaEvent_t e0, cuda
                                                         (const double*)S.ex_d.p, (double*)S.tri_d.p);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
+  if (a.numPoints > 0 && a.fast) {
+    if ((e = launch_u_field_fast((const double*)S.tri_d.p, nTri, chunk, K, a.pointsDev, a.numPoints, a.omNuInv8pi,
+                                 a.om2NuOmNuInv8pi, a.C, (double*)S.part_d.p, st)) != cudaSuccess)
+      return e;
+  } else if (a.numPoints > 0) {
+    u_field<<<dim3((unsigned)bx, (unsigned)K), PT, 0, st>>>((const double*)S.tri_d.p, nTri, chunk, a.pointsDev,
+                                                            a.numPoints, a.omNuInv8pi, a.om2NuOmNuInv8pi,
+                                                            V{a.C[0], a.C[1], a.C[2]}, (double*)S.part_d.p);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
   if (a.numPoints > 0) {
-    u_field<<<(int)((a.numPoints + PT - 1) / PT), PT, 0, st>>>((const double*)S.tri_d.p, nTri, a.pointsDev,
-                                                               a.numPoints, a.omNuInv8pi, a.om2NuOmNuInv8pi,
-                                                               (double*)S.u_d.p);
+    u_reduce<<<(int)((3 * a.numPoints + 255) / 256), 256, 0, st>>>((const double*)S.part_d.p, K, a.numPoints,
+                                                                   (double*)S.u_d.p);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   if (e1 && (e = cudaEventRecord(e1, st)) != cudaSuccess) return e;

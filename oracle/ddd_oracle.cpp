@@ -359,6 +359,24 @@ int64_t oracle_u_tilde(const double* k2, const double* C, const double* faceNorm
   return (int64_t)tris.size();
 }
 
+// The triangle list of calc_uTilde (13 doubles each: A, B, C, b, full), for
+// tests that look at single triangles.  Returns the count; writes at most cap.
+int64_t oracle_u_tilde_tris(const double* C, const double* faceNorm, const double* faceMidPt, int64_t nF,
+                            const double* normals, int64_t nN, const double* box, double tol, const double* coord,
+                            const int32_t* label, const int64_t* links, const double* bVec, int64_t numNode,
+                            int64_t numSeg, double* out, int64_t cap) {
+  const UMesh<double> m{faceNorm, faceMidPt, nF, normals, nN, {box[0], box[1], box[2]}, {box[3], box[4], box[5]},
+                        {C[0], C[1], C[2]}, tol};
+  const std::vector<UTri<double>> tris = u_tilde_triangles<double>(m, coord, label, links, bVec, numNode, numSeg);
+  for (int64_t t = 0; t < (int64_t)tris.size() && t < cap; ++t) {
+    const UTri<double>& q = tris[t];
+    const double r[13] = {q.A.x, q.A.y, q.A.z, q.B.x, q.B.y, q.B.z, q.C.x, q.C.y, q.C.z, q.b.x, q.b.y, q.b.z,
+                          q.full ? 1.0 : 0.0};
+    for (int k = 0; k < 13; ++k) out[13 * t + k] = r[k];
+  }
+  return (int64_t)tris.size();
+}
+
 // The same triangles (built in double, as the reference builds them) summed in
 // long double: the reference arithmetic's own error at each point is
 // |oracle_u_tilde - this|.

@@ -59,6 +59,10 @@ def lib():
                                      ctypes.c_int64, ctypes.c_int64, _dp, ctypes.c_int]
         L.oracle_u_tilde.restype = ctypes.c_int64
         L.oracle_u_tilde_ld.argtypes = L.oracle_u_tilde.argtypes
+        L.oracle_u_tilde_tris.argtypes = [_dp, _dp, _dp, ctypes.c_int64, _dp, ctypes.c_int64, _dp, ctypes.c_double,
+                                          _dp, ctypes.POINTER(ctypes.c_int32), _ip, _dp, ctypes.c_int64,
+                                          ctypes.c_int64, _dp, ctypes.c_int64]
+        L.oracle_u_tilde_tris.restype = ctypes.c_int64
         L.oracle_u_tilde_ld.restype = ctypes.c_int64
         L.oracle_detect_collision.argtypes = [ctypes.c_double, _dp, _dp, ctypes.POINTER(ctypes.c_int32), _ip, _dp, _ip,
                                               ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, _ip, ctypes.c_int64,
@@ -225,6 +229,25 @@ def u_tilde(k2, mesh, normals, points, coord, label, links, bvec, num_node, num_
              _i(np.require(links, np.int64, ["F"])), _d(np.require(bvec, np.float64, ["F"])), int(num_node),
              int(num_seg), _d(u), int(nthreads))
     return u, int(nt)
+
+
+def u_tilde_tris(mesh, normals, coord, label, links, bvec, num_node, num_seg, tol=None):
+    """calc_uTilde's triangles in the reference's order: (T × 13: A, B, C, b, full)."""
+    fn = np.require(mesh["faceNorm"], np.float64, ["F"])
+    fm = np.require(mesh["faceMidPt"], np.float64, ["F"])
+    nr = np.require(normals, np.float64, ["F"])
+    box = np.ascontiguousarray(np.r_[mesh["lo"], mesh["hi"]], np.float64)
+    if tol is None:
+        tol = 1e-10 * float(np.max(mesh["hi"] - mesh["lo"]))
+    lab = np.ascontiguousarray(label, np.int32)
+    args = [_d(np.ascontiguousarray(mesh["C"], np.float64)), _d(fn), _d(fm), fn.shape[1], _d(nr), nr.shape[1],
+            _d(box), float(tol), _d(np.require(coord, np.float64, ["F"])),
+            lab.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), _i(np.require(links, np.int64, ["F"])),
+            _d(np.require(bvec, np.float64, ["F"])), int(num_node), int(num_seg)]
+    n = lib().oracle_u_tilde_tris(*args, None, 0)
+    out = np.zeros((n, 13))
+    lib().oracle_u_tilde_tris(*args, _d(out), n)
+    return out
 
 
 _COLLISION_TYPES = ("null", "hinge", "twoLine")

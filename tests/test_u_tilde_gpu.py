@@ -113,6 +113,32 @@ def test_crossing_network_vs_oracle(pkg, oracle, seed):
     assert np.abs(u - ref).max() <= 1e-12 * scale + 4 * noise
 
 
+@pytest.mark.parametrize("seed", [1, 2])
+def test_fast_form(pkg, oracle, fixtures, seed):
+    """The reformulated FP64 kernel (one atan2 solid angle; selected by any mode
+    other than strict "fp64"): the goldens to 1e-11, and on the crossing
+    networks the same accuracy bound against long double as the strict form."""
+    ctx = pkg.get_context()
+    ctx.mode = "fp64_fma"
+    try:
+        mesh, bnd, mat, net = _golden(pkg, fixtures)
+        u = pkg.calc_uTilde(mesh, bnd, mat, net)
+        for c, key in enumerate(("ux", "uy", "uz")):
+            gold = np.array(G_U[key])
+            assert np.linalg.norm(u[c::3] - gold) <= 1e-11 * np.linalg.norm(gold)
+        mesh = pkg.fem.RegularCuboidMesh(1000.0, 1000.0, 1000.0, 5, 5, 5)
+        net = crossing_network(pkg, seed)
+        mat = pkg.MaterialParameters(mu=1.0, nu=0.3)
+        pts = np.asfortranarray(mesh.coord)
+        ref, _ = _oracle_u(oracle, mat, mesh, pts, net)
+        ld, _ = _oracle_u(oracle, mat, mesh, pts, net, long_double=True)
+        noise = np.abs(ref - ld).max()
+        u = ctx.u_tilde(mat.omνInv8π, mat.om2νomνInv8π, mesh, pts, net).reshape(3, -1, order="F")
+        assert np.abs(u - ld).max() <= 3 * noise + 1e-13 * np.abs(ref).max()
+    finally:
+        ctx.mode = "fp64"
+
+
 def test_dofs_scatter(pkg, fixtures):
     mesh, bnd, mat, net = _golden(pkg, fixtures)
     pts = np.asfortranarray(mesh.coord[:, bnd.uGammaDln - 1])
