@@ -561,6 +561,10 @@ def main():
     ap.add_argument("--cpu-target-s", type=float, default=15.0)
     ap.add_argument("--ref-step-s", type=float, default=4.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--rows-only", action="store_true",
+                    help="only the rows around the force (self force, mobility, collision, calc_uTilde) on the "
+                         "workload, seg-seg forces from one untimed call; prints their JSON and exits (the command "
+                         "the ncu captures of those kernels use)")
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-sigma", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
@@ -606,6 +610,20 @@ def main():
             _, rep = sur.force(k, segs, exact_mode="f32c", audit_fraction=0.0)
         torch.cuda.synchronize()
         print(json.dumps({"profile_surrogate": args.profile_surrogate, "segments": n, "report": rep}), flush=True)
+        return
+
+    if args.rows_only:
+        coord, bvec, seg = synth.network_arrays(p, b)
+        net = pkg.DislocationNetwork(coord, bvec, seg)
+        out = ctx.segseg_force(k, net)
+        dln_m = pkg.DislocationParameters(coreRad=synth.CORE_RAD, coreEnergy=1.0,
+                                          dragCoeffs=dict(edge=1.0, screw=2.0, climb=1e10, line=1e-4))
+        mat_m = pkg.MaterialParameters(mu=synth.MU, nu=synth.NU, sigmaPN=1e-4)
+        rows = {"node_rows": run_node_rows(pkg, oracle, ctx, net, dln_m, mat_m, out, with_cpu=not args.no_cpu),
+                "collision": run_collision(pkg, oracle, ctx, net, synth, p, b, 10.0, with_cpu=not args.no_cpu),
+                "u_tilde": run_u_tilde(pkg, oracle, ctx, net, cfg["cube"], with_cpu=not args.no_cpu),
+                "segments": n}
+        print(json.dumps(rows), flush=True)
         return
 
     stream = torch.cuda.Stream()

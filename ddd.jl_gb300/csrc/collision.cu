@@ -10,7 +10,7 @@
 //     reference's order (including the swap that keeps link1 on the longer
 //     connection for the rest of the k loop);
 //   * two-line pass: segments Morton-sorted into 128-segment tiles; a
-//     persistent kernel walks the tile pairs, rejects a pair of tiles whose
+//     persistent kernel takes the tile pairs from a counter, rejects a pair of tiles whose
 //     bounding boxes are farther apart than collisionDist and then, per pair of
 //     segments, rejects by bounding spheres in FP32 (radii rounded outward with
 //     a 1e-5 relative and 1e-5 * max|coord| margin, so no pair whose FP64
@@ -239,18 +239,27 @@ __device__ void block_best(Cand& c, Cand* sm) {
   c = sm[0];
 }
 
-// Two-line pass over the tile pairs (I <= J) of the sorted segments, persistent.
+// Two-line pass over the tile pairs (I <= J) of the sorted segments,
+// persistent; each CTA takes the next tile pair from a counter (most tile
+// pairs are rejected by their boxes at once, a few carry all the work).
 __global__ void __launch_bounds__(T) two_line(const float4* __restrict__ sph, const int4* __restrict__ meta,
                                                const float* __restrict__ tbox, int64_t nTP, float Rf, double cd2,
                                                const double* __restrict__ coord, const double* __restrict__ vel,
                                                const double* __restrict__ bVec, const int64_t* __restrict__ skip,
-                                               int64_t nSkip, Cand* __restrict__ part) {
+                                               int64_t nSkip, unsigned long long* __restrict__ next,
+                                               Cand* __restrict__ part) {
   __shared__ float4 s_sph[T];
   __shared__ int4 s_meta[T];
   __shared__ Cand s_red[T];
+  __shared__ unsigned long long s_tp;
   const int t = threadIdx.x;
   Cand best = {-1.0, INT64_MAX, INT64_MAX};
-  for (int64_t tp = blockIdx.x; tp < nTP; tp += gridDim.x) {
+  for (;;) {
+    __syncthreads();  // the previous tile pair's shared data and s_tp are no longer read
+    if (t == 0) s_tp = atomicAdd(next, 1ull);
+    __syncthreads();
+    const int64_t tp = (int64_t)s_tp;
+    if (tp >= nTP) break;
     int64_t J = (int64_t)((sqrt(8.0 * (double)tp + 1.0) - 1.0) * 0.5);
     while (J * (J + 1) / 2 > tp) --J;
     while ((J + 1) * (J + 2) / 2 <= tp) ++J;
@@ -262,7 +271,6 @@ __global__ void __launch_bounds__(T) two_line(const float4* __restrict__ sph, co
 #pragma unroll
     for (int k = 0; k < 3; ++k) gap = fmaxf(gap, fmaxf(__fsub_rd(bJ[k], bI[3 + k]), __fsub_rd(bI[k], bJ[3 + k])));
     if (gap > Rf) continue;  // uniform over the block: no pair of these tiles is within reach
-    __syncthreads();
     s_sph[t] = sph[J * T + t];
     s_meta[t] = meta[J * T + t];
     __syncthreads();
@@ -515,7 +523,7 @@ struct Buf {
 }  // namespace
 
 struct CollisionPlan {
-  Buf keysIn, keysOut, valsIn, valsOut, cub, ids, mob, sph, meta, tbox, hpart, tpart, rpart, out;
+  Buf keysIn, keysOut, valsIn, valsOut, cub, ids, mob, sph, meta, tbox, hpart, tpart, rpart, out, next;
   int twoLineGrid = 0;
 };
 
@@ -564,6 +572,7 @@ cudaError_t collision_detect(CollisionPlan* P, double cd2, const double* coord, 
   CCK(P->tpart.ensure((size_t)gT * sizeof(Cand)));
   CCK(P->rpart.ensure((size_t)nR * sizeof(int64_t)));
   CCK(P->out.ensure(sizeof(CollisionOut)));
+  CCK(P->next.ensure(sizeof(unsigned long long)));
 
   Box bx;
   const double ext = std::max(std::max(box[3] - box[0], box[4] - box[1]), box[5] - box[2]);
@@ -597,8 +606,9 @@ cudaError_t collision_detect(CollisionPlan* P, double cd2, const double* coord, 
     CCK(cudaGetLastError());
     tile_boxes<<<(int)nt, T, 0, st>>>(P->sph.as<float4>(), P->meta.as<int4>(), P->tbox.as<float>());
     CCK(cudaGetLastError());
+    CCK(cudaMemsetAsync(P->next.p, 0, sizeof(unsigned long long), st));
     two_line<<<gT, T, 0, st>>>(P->sph.as<float4>(), P->meta.as<int4>(), P->tbox.as<float>(), nTP, Rf, cd2, coord, vel,
-                               bVec, skip, nSkip, P->tpart.as<Cand>());
+                               bVec, skip, nSkip, P->next.as<unsigned long long>(), P->tpart.as<Cand>());
     CCK(cudaGetLastError());
     row_last<<<nR, RB, 0, st>>>(coord, bVec, P->ids.as<int2>(), P->mob.as<uint8_t>(), numSeg, skip, nSkip,
                                 P->rpart.as<int64_t>());

@@ -160,10 +160,11 @@ struct UTildeScratch {
   std::vector<double> explicitTri;
   GrowBuf order_d, ex_d, tri_d, u_d, part_d;
   int64_t lastTriangles = 0, lastChunks = 0;
-  int sms = 0;
+  int sms = 0, occStrict = 0, occFast = 0;
 };
 cudaError_t u_tilde_compute(const UTildeArgs& a, double* u, cudaEvent_t e0, cudaEvent_t e1, cudaStream_t st,
                             UTildeScratch& S);
+int u_field_fast_blocks_per_sm();
 // Partial sums part[k][p] over triangle chunk k (K chunks of `chunk`).
 cudaError_t launch_u_field_fast(const double* tri, int64_t nTri, int64_t chunk, int64_t K, const double* points,
                                 int64_t M, double omNuInv8pi, double om2NuOmNuInv8pi, const double C[3], double* part,

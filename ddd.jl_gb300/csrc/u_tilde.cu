@@ -365,15 +365,25 @@ cudaError_t u_tilde_compute(const UTildeArgs& a, double* u, cudaEvent_t e0, cuda
   if ((e = S.order_d.ensure((size_t)std::max<int64_t>(nTri, 1) * 8)) != cudaSuccess) return e;
   if ((e = S.ex_d.ensure(std::max<size_t>(ex.size(), 1) * 8)) != cudaSuccess) return e;
   if ((e = S.tri_d.ensure((size_t)std::max<int64_t>(nTri, 1) * TROW * 8)) != cudaSuccess) return e;
-  // Triangle chunks: enough CTAs to fill the GPU (about 4 per SM), at least
-  // 256 triangles each; one chunk keeps each point's sum strictly sequential.
+  // Triangle chunks of at least 256 triangles; one chunk keeps each point's
+  // sum strictly sequential.
   if (!S.sms) {
     int dev = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&S.sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
   }
+  int& occ = a.fast ? S.occFast : S.occStrict;
+  if (!occ) {
+    if (a.fast)
+      occ = u_field_fast_blocks_per_sm();
+    else if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, u_field, PT, 0)) != cudaSuccess)
+      return e;
+    occ = std::max(occ, 1);
+  }
+  // As many chunks as fit the resident slots in one wave (equal chunks then
+  // finish together); many points alone fill the GPU with one chunk.
   const int64_t bx = (a.numPoints + PT - 1) / PT;
-  const int64_t want = std::max<int64_t>(1, (4 * (int64_t)S.sms + bx - 1) / std::max<int64_t>(bx, 1));
+  const int64_t want = std::max<int64_t>(1, (int64_t)S.sms * occ / std::max<int64_t>(bx, 1));
   const int64_t K = std::max<int64_t>(1, std::min<int64_t>({want, (nTri + 255) / 256, 65535}));
   const int64_t chunk = std::max<int64_t>(1, (nTri + K - 1) / K);
   S.lastChunks = K;

@@ -149,6 +149,12 @@ __global__ void __launch_bounds__(PT) u_field_fast(const double* __restrict__ tr
 
 }  // namespace
 
+int u_field_fast_blocks_per_sm() {
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, u_field_fast, PT, 0) != cudaSuccess) return 1;
+  return occ;
+}
+
 cudaError_t launch_u_field_fast(const double* tri, int64_t nTri, int64_t chunk, int64_t K, const double* points,
                                 int64_t M, double omNuInv8pi, double om2NuOmNuInv8pi, const double C[3], double* part,
                                 cudaStream_t st) {
