@@ -7,13 +7,14 @@
 //      boxes are close enough to hold a pair outside the trust region;
 //   2. network pass (surrogate_infer.cu): every tile pair I <= J, far pairs
 //      through the MLP, partial forces written to the tile pair's slot;
-//   3. audit: a fixed, hashed ~audit_fraction of the tile pairs re-evaluated
-//      exactly on their far pairs (tile_body MODE 3), compared with the
-//      network's slot sums;
-//   4. near pass: the listed tile pairs, every pair outside the trust region
+//   3. near pass: the listed tile pairs, every pair outside the trust region
 //      evaluated exactly (tile_body MODE 2: the reference's general or
 //      near-parallel branch, the general branch in the caller's exact_mode
 //      arithmetic: strict FP64, df64 or f32c) and added to the slot;
+//   4. audit: a fixed, hashed ~audit_fraction of the tile pairs re-evaluated
+//      exactly over all their pairs (tile_body MODE 0, the all-pairs body in
+//      the same arithmetic), compared with their slots (network far pairs +
+//      exact near pairs): the difference is the network's error;
 //   5. reduction of each segment's slots in a fixed order, written back in the
 //      caller's order.
 // If the audited error exceeds the caller's bound, steps 2-5 are replaced by
@@ -622,9 +623,18 @@ int ddd_surrogate_force(ddd_surrogate* s, const ddd_consts* k, const double* seg
       "network pass");
   SCK(cudaEventRecord(P.ev[2], st), "event");
 
-  // 3. audit
+  // 3. near pass (in place)
+  SCK(launch_exact<2>(xm, A, P.nearItems.as<int4>(), &dv->nearCount, 0, &dv->next[2], P.partial.as<double>(),
+                      dv->counts, P.gridExact, st),
+      "near pass");
+  SCK(cudaEventRecord(P.ev[3], st), "event");
+
+  // 4. audit: the sampled tile pairs exactly over all their pairs (the plain
+  // all-pairs tile body), against their slots, which now hold the network's
+  // far pairs plus the exact near pairs: the difference is the network's
+  // error on the far pairs (the near pairs agree up to summation order).
   if (P.nAudit > 0) {
-    SCK(launch_exact<3>(xm, A, P.auditItems.as<int4>(), nullptr, P.nAudit, &dv->next[1], P.abuf.as<double>(), nullptr,
+    SCK(launch_exact<0>(xm, A, P.auditItems.as<int4>(), nullptr, P.nAudit, &dv->next[1], P.abuf.as<double>(), nullptr,
                         (int)std::min<int64_t>(P.gridExact, P.nAudit), st),
         "audit pass");
     sf::audit_compare<<<P.nAudit, sf::T, 0, st>>>(P.partial.as<double>(), P.abuf.as<double>(),
@@ -632,12 +642,6 @@ int ddd_surrogate_force(ddd_surrogate* s, const ddd_consts* k, const double* seg
     sf::audit_final<<<1, 256, 0, st>>>(P.astat.as<double>(), P.nAudit, dv->audit);
     SCK(cudaGetLastError(), "audit compare");
   }
-  SCK(cudaEventRecord(P.ev[3], st), "event");
-
-  // 4. near pass (in place)
-  SCK(launch_exact<2>(xm, A, P.nearItems.as<int4>(), &dv->nearCount, 0, &dv->next[2], P.partial.as<double>(),
-                      dv->counts, P.gridExact, st),
-      "near pass");
   SCK(cudaEventRecord(P.ev[4], st), "event");
 
   // 5. reduction into the caller's order
@@ -692,8 +696,8 @@ int ddd_surrogate_force(ddd_surrogate* s, const ddd_consts* k, const double* seg
       for (int i = 0; i < 5; ++i) cudaEventElapsedTime(&m[i], P.ev[i], P.ev[i + 1]);
     rep->ms_prep = m[0];
     rep->ms_network = m[1];
-    rep->ms_audit = m[2];
-    rep->ms_near = m[3];
+    rep->ms_near = m[2];
+    rep->ms_audit = m[3];
     rep->ms_reduce = m[4];
     rep->ms_total = fallback ? (double)msFallback : (double)(m[0] + m[1] + m[2] + m[3] + m[4]);
   }
