@@ -534,7 +534,7 @@ def run_reference(args, pkg, synth, oracle):
     out = {
         "impl": "reference",
         "metric": "seg-seg pair interactions/s at 65k segs (FP64 plain vs FP32+surrogate) at stated error",
-        "value": v, "unit": "pair-interactions/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "value": v, "unit": "pair-interactions/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * (n * (n - 1) / 2) / v, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
         "config": {"workload": "%s: %d segments, %d loops" % (args.workload, n, p.shape[0]),
