@@ -499,11 +499,17 @@ def run_u_tilde(pkg, oracle, ctx, net, cube, cells=64, reps=3, cpu_target_s=8.0,
         return oracle.u_tilde(k, md, mesh.normals, np.asfortranarray(pts[:, idx]), net.coord, net.label, net.links,
                               net.bVec, net.numNode, net.numSeg, nthreads=threads)[0]
 
-    probe = np.arange(0, M, max(1, M // threads))[:threads]
-    t0 = time.perf_counter()
-    ref(probe)
-    rate = len(probe) / max(time.perf_counter() - t0, 1e-6)
-    m = int(min(M, max(threads, rate * cpu_target_s)))
+    # Calibrate on a growing probe until it takes ~1/8 of the target (the
+    # triangle list is built once per call and dominates tiny probes).
+    m = threads
+    while True:
+        t0 = time.perf_counter()
+        ref(np.linspace(0, M - 1, m).astype(np.int64))
+        dt = time.perf_counter() - t0
+        if dt >= cpu_target_s / 8 or m >= M:
+            break
+        m = min(M, m * 4)
+    m = int(min(M, max(threads, m * cpu_target_s / max(dt, 1e-6))))
     idx = np.linspace(0, M - 1, m).astype(np.int64)
     t0 = time.perf_counter()
     r = ref(idx)
