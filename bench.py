@@ -194,8 +194,7 @@ def cpu_sigma_sample(pkg, synth, oracle, p, b, k5, cube, target_s):
 
 # DRAM bytes per tile pair of the strict tile kernel and of the network pass,
 # from one ncu capture each at 32,768 segments (32,896 tile pairs; the partial
-# slots exceed L2 there, so traffic grows with the tile-pair count):
-# profiles/dram_traffic_tile_mlp_32k.md.
+# slots exceed L2 there, so traffic grows with the tile-pair count).
 TILE_DRAM_BYTES_PER_TILE_PAIR = (31162112 + 376273664) // 32896
 MLP_DRAM_BYTES_PER_TILE_PAIR = (12404992 + 346662144) // 32896
 
@@ -851,7 +850,7 @@ def main():
                      "frac": achieved / fp64_peak,
                      "traffic": TILE_DRAM_BYTES_PER_TILE_PAIR * (n // 128) * (n // 128 + 1) // 2,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at 32,768 "
-                                       "segments, scaled by tile pairs (profiles/dram_traffic_tile_mlp_32k.md)",
+                                       "segments, scaled by tile pairs",
                      "kernel": "segseg_tile_f64<0>",
                      "peak_source": "measured FP64 FMA-chain probe on this GPU (ddd_probe_fma_peak); "
                                     "MEASURED_PEAKS.json holds no FP64 figure",

@@ -4,7 +4,9 @@
 # calc_σTilde / calc_σTilde! keep DDD.jl's signatures and array layouts; the
 # network's own arrays are passed to the library without copies.  Select it
 # with the existing DislocationParameters field parGPU (src/Type/DislocationType.jl:254):
-# the dispatch lines to add to DDD.jl are shown in INTEGRATION.md.
+# one line at the top of each replaced function, e.g. in calcSegSegForce
+# (src/Processing/DislocationForces.jl:470):
+#     dlnParams.parGPU && return DDDGB300.calcSegSegForceGPU(dlnParams, matParams, network, idx)
 #
 # Julia is not installed in the environment this library was built in, so this
 # file has not been executed there; the C ABI it binds is exercised by the

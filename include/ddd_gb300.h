@@ -350,8 +350,8 @@ int ddd_get_mode(const ddd_ctx* ctx);
  * 16-byte aligned.  Synchronous; DDD_ETIMEOUT if a bounded wait gave up. */
 int ddd_tc_gemm_bf16(ddd_ctx* ctx, int M, int N, int K, const void* A, const void* B, float* D, void* stream);
 
-/* Learned far-field surrogate (no reference counterpart; the north-star
- * extension).  A pair's four node forces, in the pair's own frame and scaled by
+/* Learned far-field surrogate (no reference counterpart: an extension of the
+ * seg-seg force).  A pair's four node forces, in the pair's own frame and scaled by
  * mu4pi L_i L_j / R^2, are bilinear in the two Burgers vectors; a small MLP
  * (16 -> 128 -> 128 -> 128 -> 112, GELU, FP16 operands, FP32 accumulation) maps
  * the pair geometry to the 108 coefficients of that bilinear form, and an exact

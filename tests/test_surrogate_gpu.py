@@ -57,7 +57,8 @@ def test_features_and_exact_targets(pkg, synth, oracle):
         c1, c2, cb = soa[0:3, j], soa[3:6, j], soa[6:9, j]
         ref = oracle.pair(k5, ab, a1, a2, cb, c1, c2).ravel()
         # Far pairs: the formula cancels strongly, so two correct FP64 evaluations
-        # agree to ~1e-6 of the largest component (long-double study in the design doc).
+        # agree to ~1e-6 of the largest component (measured against a long-double
+        # evaluation of the same pairs).
         assert np.allclose(Fh[q], ref, rtol=0, atol=1e-5 * np.abs(ref).max())
         li, lj = np.linalg.norm(a2 - a1), np.linalg.norm(c2 - c1)
         f, bp, (e1, e2, e3, scale) = M.features(0.5 * (c1 + c2) - 0.5 * (a1 + a2), (a2 - a1) / li, (c2 - c1) / lj,
