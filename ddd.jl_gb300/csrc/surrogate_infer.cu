@@ -11,9 +11,14 @@
 // thread t forms pair (row t, column (t + k) mod 128), writes its 8 geometric
 // features (hi and lo FP16 parts) as row t of a 128 x 16 FP16 operand, and the
 // layer chain runs as
-//   X (128x16) [W1|W1]^T -> TMEM (128x128 FP32) -> +b1, GELU (two per
-//   instruction, gelu_h2), FP16 -> H (smem)
-//   H W2^T -> TMEM -> ... -> H W3^T -> TMEM -> ... -> H W4^T -> TMEM (128x112)
+//   X (128x16) [W1|W1]^T -> TMEM (128x128 FP32) -> +b1, 2 GELU (two per
+//   instruction), FP16 -> H (smem)
+//   H (W2/2)^T -> TMEM -> ... -> H (W3/2)^T -> TMEM -> ... -> H (W4/2)^T -> TMEM
+// The activations are stored doubled (x (1 + tanh(.)), one instruction fewer
+// than 0.5 x (1 + tanh(.))) and W2..W4 are staged halved: both scalings are by
+// a power of two, so every product, and every accumulator, is bit-identical to
+// the plain GELU with the plain weights (weights below FP16's normal range
+// excepted, which lose their last bit).
 // one thread issuing the tcgen05.mma instructions, the warpgroup waiting on its
 // mbarrier (bounded), each thread reading back its own accumulator row
 // (tcgen05.ld) for the epilogue.  The 108 coefficients, contracted with the
@@ -146,7 +151,7 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t tm_row, const float* bi
     __half2 h[16];
 #pragma unroll
     for (int i = 0; i < 16; ++i)
-      h[i] = gelu_h2(__floats2half2_rn(__uint_as_float(r[2 * i]) + bias[c0 + 2 * i],
+      h[i] = gelu2_h2(__floats2half2_rn(__uint_as_float(r[2 * i]) + bias[c0 + 2 * i],
                                        __uint_as_float(r[2 * i + 1]) + bias[c0 + 2 * i + 1]));
     store_h16(H, t, c0, kHidden, h);
     store_h16(H, t, c0 + 16, kHidden, h + 8);
@@ -172,17 +177,23 @@ mlp_far_tiles(const float* __restrict__ ms, int64_t npad, const int4* __restrict
   unsigned char* H = smem + kH + wg * kHBytes;
 
   // Weights (K-major core-matrix layout) and biases into shared memory, once.
-  auto stage = [&](const __half* W, int rows, int K, int off) {
+  auto stage = [&](const __half* W, int rows, int K, int off, bool halve) {
+    const __half2 hf = __float2half2_rn(0.5f);
     for (int idx = tid; idx < rows * (K / 8); idx += kThreads) {
       const int r = idx / (K / 8), kb = idx % (K / 8);
-      *reinterpret_cast<uint4*>(smem + off + tc::kmajor_offset(r, kb * 8, K)) =
-          *reinterpret_cast<const uint4*>(W + (size_t)r * K + kb * 8);
+      uint4 v = *reinterpret_cast<const uint4*>(W + (size_t)r * K + kb * 8);
+      if (halve) {
+        __half2* h = reinterpret_cast<__half2*>(&v);
+#pragma unroll
+        for (int q2 = 0; q2 < 4; ++q2) h[q2] = __hmul2(h[q2], hf);
+      }
+      *reinterpret_cast<uint4*>(smem + off + tc::kmajor_offset(r, kb * 8, K)) = v;
     }
   };
-  stage(W1, kHidden, kFeatIn, kW1);
-  stage(W2, kHidden, kHidden, kW2);
-  stage(W3, kHidden, kHidden, kW3);
-  stage(W4, kOut, kHidden, kW4);
+  stage(W1, kHidden, kFeatIn, kW1, false);
+  stage(W2, kHidden, kHidden, kW2, true);
+  stage(W3, kHidden, kHidden, kW3, true);
+  stage(W4, kOut, kHidden, kW4, true);
   for (int i = tid; i < kHidden; i += kThreads) {
     sBias[i] = params[kOffB1 + i];
     sBias[kHidden + i] = params[kOffB2 + i];
