@@ -107,6 +107,31 @@ __device__ __forceinline__ void tmem_ld16_async(uint32_t taddr, uint32_t* r) {
       : "memory");
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t* r) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16};"
+      :
+      : "r"(taddr), "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]),
+        "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+      : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+// Columns c..c+15 of the thread's accumulator row set to bias[c..c+15]: the
+// next layer's MMAs then accumulate onto its bias.
+__device__ __forceinline__ void bias_to_tmem(uint32_t tm_row, const float* bias, int c) {
+  uint32_t v[16];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float4 b = *reinterpret_cast<const float4*>(bias + c + 4 * i);
+    v[4 * i] = __float_as_uint(b.x);
+    v[4 * i + 1] = __float_as_uint(b.y);
+    v[4 * i + 2] = __float_as_uint(b.z);
+    v[4 * i + 3] = __float_as_uint(b.w);
+  }
+  tmem_st16(tm_row + (uint32_t)c, v);
+}
 
 // 16 FP16 values (8 packed pairs) of row `row`, columns c0..c0+15, of a K-major tile.
 __device__ __forceinline__ void store_h16(unsigned char* base, int row, int c0, int KC, const __half2* p) {
@@ -126,9 +151,9 @@ __device__ __forceinline__ bool layer(uint32_t tm, const unsigned char* A, const
     const uint32_t a = tc::smem_addr(A), b = tc::smem_addr(B);
     const uint32_t sbo = (uint32_t)(K / 8) * 128u;
     const uint32_t idesc = tc::idesc_f16_f32(128, N);  // A and B both FP16
-    for (int kk = 0; kk < K; kk += 16)
+    for (int kk = 0; kk < K; kk += 16)  // onto the bias already in TMEM
       tc::mma_bf16(tm, tc::smem_desc(a + (uint32_t)(kk / 8) * 128u, 128u, sbo),
-                   tc::smem_desc(b + (uint32_t)(kk / 8) * 128u, 128u, sbo), idesc, kk > 0 ? 1u : 0u);
+                   tc::smem_desc(b + (uint32_t)(kk / 8) * 128u, 128u, sbo), idesc, 1u);
     tc::mma_commit(mbar);
   }
   bool ok = tc::mbar_wait(mbar, phase);
@@ -138,10 +163,13 @@ __device__ __forceinline__ bool layer(uint32_t tm, const unsigned char* A, const
   return ok;
 }
 
-// Row t of the warpgroup's 128-column accumulator + bias (FP32), GELU on FP16
-// pairs, into H (FP16): the same arithmetic as the training forward pass.  32
-// columns per tcgen05.wait::ld (64 measured 10% slower: register pressure).
-__device__ __forceinline__ void hidden_epilogue(uint32_t tm_row, const float* bias, unsigned char* H, int t) {
+// Row t of the warpgroup's 128-column accumulator (the layer's bias included:
+// the MMAs accumulated onto it), GELU on FP16 pairs, into H (FP16).  As each
+// 32-column chunk is read, the next layer's bias (nNext columns) takes its
+// place.  32 columns per tcgen05.wait::ld (64 measured 10% slower: register
+// pressure).
+__device__ __forceinline__ void hidden_epilogue(uint32_t tm_row, const float* biasNext, int nNext, unsigned char* H,
+                                                int t) {
 #pragma unroll 1
   for (int c0 = 0; c0 < kHidden; c0 += 32) {
     uint32_t r[32];
@@ -151,11 +179,13 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t tm_row, const float* bi
     __half2 h[16];
 #pragma unroll
     for (int i = 0; i < 16; ++i)
-      h[i] = gelu2_h2(__floats2half2_rn(__uint_as_float(r[2 * i]) + bias[c0 + 2 * i],
-                                       __uint_as_float(r[2 * i + 1]) + bias[c0 + 2 * i + 1]));
+      h[i] = gelu2_h2(__floats2half2_rn(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1])));
     store_h16(H, t, c0, kHidden, h);
     store_h16(H, t, c0 + 16, kHidden, h + 8);
+    if (c0 < nNext) bias_to_tmem(tm_row, biasNext, c0);
+    if (c0 + 16 < nNext) bias_to_tmem(tm_row, biasNext, c0 + 16);
   }
+  tmem_wait_st();
 }
 
 __global__ void __launch_bounds__(kThreads, 1)
@@ -211,6 +241,8 @@ mlp_far_tiles(const float* __restrict__ ms, int64_t npad, const int4* __restrict
   const uint32_t tm_row = tm + ((uint32_t)(q * 32) << 16);  // this warp's lanes
   uint32_t phase = 0;
   bool ok = true;
+  for (int c = 0; c < kHidden; c += 16) bias_to_tmem(tm_row, sBias, c);  // layer 1 of the first step
+  tmem_wait_st();
 
   for (;;) {
     __syncthreads();
@@ -263,14 +295,14 @@ mlp_far_tiles(const float* __restrict__ ms, int64_t npad, const int4* __restrict
       store_h16(H, t, 0, kFeatIn, x);
 
       if (!(ok = layer(tm, H, smem + kW1, kFeatIn, kHidden, &mbar[wg], phase, leader, bar))) break;
-      hidden_epilogue(tm_row, sBias, H, t);
+      hidden_epilogue(tm_row, sBias + kHidden, kHidden, H, t);
       if (!(ok = layer(tm, H, smem + kW2, kHidden, kHidden, &mbar[wg], phase, leader, bar))) break;
-      hidden_epilogue(tm_row, sBias + kHidden, H, t);
+      hidden_epilogue(tm_row, sBias + 2 * kHidden, kHidden, H, t);
       if (!(ok = layer(tm, H, smem + kW3, kHidden, kHidden, &mbar[wg], phase, leader, bar))) break;
-      hidden_epilogue(tm_row, sBias + 2 * kHidden, H, t);
+      hidden_epilogue(tm_row, sBias + 3 * kHidden, kOut, H, t);
       if (!(ok = layer(tm, H, smem + kW4, kHidden, kOut, &mbar[wg], phase, leader, bar))) break;
-      // Contraction: out[o] = sum_ac bp[ac] (Y[12 ac + o] + b4[12 ac + o]).
-      const float* b4 = sBias + 3 * kHidden;
+      // Contraction: out[o] = sum_ac bp[ac] Y[12 ac + o] (Y includes b4); then
+      // b1 into the columns for the next step's first layer.
       float out[kUsedOut];
 #pragma unroll
       for (int o = 0; o < kUsedOut; ++o) out[o] = 0.0f;
@@ -282,9 +314,12 @@ mlp_far_tiles(const float* __restrict__ ms, int64_t npad, const int4* __restrict
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
           const int j = c0 + i;
-          if (j < kCoef) out[j % kUsedOut] += bp[j / kUsedOut] * (__uint_as_float(yr[i]) + b4[j]);
+          if (j < kCoef) out[j % kUsedOut] += bp[j / kUsedOut] * __uint_as_float(yr[i]);
         }
       }
+#pragma unroll 1
+      for (int c = 0; c < kHidden; c += 16) bias_to_tmem(tm_row, sBias, c);
+      tmem_wait_st();
       float F[12];
 #pragma unroll
       for (int n = 0; n < 4; ++n) {
