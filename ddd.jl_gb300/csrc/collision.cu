@@ -500,25 +500,7 @@ __global__ void min_dist_batch(const double* __restrict__ pts, int64_t n, double
   out[4 * q + 3] = m.L2;
 }
 
-struct Buf {
-  void* p = nullptr;
-  size_t cap = 0;
-  cudaError_t ensure(size_t bytes) {
-    if (bytes <= cap) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-    const size_t want = bytes + bytes / 8 + 256;
-    cudaError_t e = cudaMalloc(&p, want);
-    if (e != cudaSuccess) return e;
-    cap = want;
-    return cudaSuccess;
-  }
-  template <class U> U* as() const { return reinterpret_cast<U*>(p); }
-  ~Buf() {
-    if (p) cudaFree(p);
-  }
-};
+using Buf = GrowBuf;
 
 }  // namespace
 

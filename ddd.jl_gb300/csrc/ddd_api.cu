@@ -21,30 +21,7 @@ namespace {
 std::string g_create_error;
 std::mutex g_create_mu;
 
-struct DevBuf {
-  void* p = nullptr;
-  size_t cap = 0;
-  cudaError_t ensure(size_t bytes) {
-    if (bytes <= cap) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-    size_t want = bytes + bytes / 8 + 256;
-    cudaError_t e = cudaMalloc(&p, want);
-    if (e != cudaSuccess) {
-      p = nullptr;
-      return e;
-    }
-    cap = want;
-    return cudaSuccess;
-  }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-  }
-  template <class T> T* as() const { return reinterpret_cast<T*>(p); }
-};
+using DevBuf = ddd::GrowBuf;
 
 }  // namespace
 

@@ -107,27 +107,33 @@ cudaError_t collision_detect(CollisionPlan* P, double cd2, const double* coord, 
 // pts: 3 x 8 x n (x0, x1, y0, y1, vx0, vx1, vy0, vy1), out 4 x n.
 cudaError_t launch_minimum_distance(const double* pts, int64_t n, double* out, cudaStream_t st);
 
-// Grow-only device buffer.
+// Grow-only device buffer (12.5 % headroom on growth), freed on release() or
+// destruction; used by every file that keeps device scratch between calls.
 struct GrowBuf {
   void* p = nullptr;
   size_t cap = 0;
   cudaError_t ensure(size_t bytes) {
     if (bytes <= cap) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
+    release();
     const size_t want = bytes + bytes / 8 + 256;
     cudaError_t e = cudaMalloc(&p, want);
-    if (e != cudaSuccess) return e;
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return e;
+    }
     cap = want;
     return cudaSuccess;
   }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <class X> X* as() const { return reinterpret_cast<X*>(p); }
   GrowBuf() = default;
   GrowBuf(const GrowBuf&) = delete;
   GrowBuf& operator=(const GrowBuf&) = delete;
-  ~GrowBuf() {
-    if (p) cudaFree(p);
-  }
+  ~GrowBuf() { release(); }
 };
 
 // u_tilde.cu: calc_uTilde's displacements at numPoints points (u: host, 3 x

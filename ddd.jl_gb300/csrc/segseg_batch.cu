@@ -127,24 +127,7 @@ namespace {
 using namespace ddd;
 using namespace ddd::batch;
 
-struct DBuf {
-  void* p = nullptr;
-  size_t cap = 0;
-  cudaError_t ensure(size_t n) {
-    if (n <= cap) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-    cudaError_t e = cudaMalloc(&p, n + 256);
-    if (e == cudaSuccess) cap = n + 256;
-    return e;
-  }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-  }
-};
+using DBuf = GrowBuf;
 
 // One (tile size, work order) layout of a batch.
 struct Layout {

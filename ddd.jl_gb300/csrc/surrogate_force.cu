@@ -340,28 +340,7 @@ __global__ void reduce_unpermute(const double* __restrict__ partial, const int32
 
 // Device buffers of the force path for one segment count.
 struct SurForcePlan {
-  struct Buf {
-    void* p = nullptr;
-    size_t cap = 0;
-    cudaError_t ensure(size_t n) {
-      if (n <= cap) return cudaSuccess;
-      if (p) cudaFree(p);
-      p = nullptr;
-      cap = 0;
-      cudaError_t e = cudaMalloc(&p, n + 256);
-      if (e == cudaSuccess) cap = n + 256;
-      return e;
-    }
-    template <class X>
-    X* as() const {
-      return reinterpret_cast<X*>(p);
-    }
-    void release() {
-      if (p) cudaFree(p);
-      p = nullptr;
-      cap = 0;
-    }
-  };
+  using Buf = GrowBuf;
   int64_t numSeg = -1, npad = 0, nt = 0, nItems = 0;
   int32_t nAudit = 0;
   double auditFraction = -1.0;
