@@ -4,7 +4,6 @@
 //   MODE  0 = unordered pairs i < j (both sides' forces), 1 = index rows (all
 //         j != i, forces on the row segment only), 2 = the pairs i < j outside
 //         the surrogate's trust region (near pairs; forces added to `p`),
-//         3 = the pairs i < j inside it (far pairs; forces written to `p`),
 //   P     arithmetic policy (FP64, df64, mixed FP32; pair_f64.cuh / pair_df.cuh).
 //
 // Thread t owns row segment i (registers); the column tile sits in shared
@@ -17,7 +16,7 @@
 // segment — are written to `p` as [side][component][T] doubles.  No
 // floating-point atomics: the result is deterministic.
 //
-// In MODES 2 and 3 every selected pair goes through the compacted dense pass:
+// In MODE 2 every selected pair goes through the compacted dense pass:
 // the branch is the reference's FP64 decision, the general branch uses the
 // policy's arithmetic (P::dense_general), the near-parallel branch FP64.
 //
@@ -85,7 +84,7 @@ __device__ __forceinline__ void tile_body(const TileArgs& A, const typename P::C
     gi = iActive ? rows[r] : 0;
     iActive = iActive && A.skip[gi] == 0;
   }
-  constexpr bool CLS = MODE >= 2;  // classified modes: dense pass only
+  constexpr bool CLS = MODE == 2;  // classified mode: dense pass only
   typename P::Seg si;
   if (!CLS) si = P::load_global(A, gi);
   float mi[3] = {0, 0, 0}, Li = 0.0f;
@@ -122,7 +121,7 @@ __device__ __forceinline__ void tile_body(const TileArgs& A, const typename P::C
         const bool far = sur::pair_is_far(mi[0], mi[1], mi[2], Li, A.ms[(sur::kMsM + 0) * n + gj],
                                           A.ms[(sur::kMsM + 1) * n + gj], A.ms[(sur::kMsM + 2) * n + gj],
                                           A.ms[sur::kMsL * n + gj], A.farK2, dx, dy, dz);
-        if (far == (MODE == 3)) pmask[jl >> 5] |= 1u << (jl & 31);
+        if (!far) pmask[jl >> 5] |= 1u << (jl & 31);
       }
     } else if (act) {
       typename P::Seg sj = P::template load_smem<T>(sm.pol, jl);
@@ -234,7 +233,7 @@ __device__ __forceinline__ void tile_body(const TileArgs& A, const typename P::C
   if (CLS) {
     const double v[12] = {fp1.x, fp1.y, fp1.z, fp2.x, fp2.y, fp2.z, fjp3.x, fjp3.y, fjp3.z, fjp4.x, fjp4.y, fjp4.z};
 #pragma unroll
-    for (int c = 0; c < 12; ++c) p[c * T + t] = (MODE == 2 ? p[c * T + t] : 0.0) + v[c];
+    for (int c = 0; c < 12; ++c) p[c * T + t] = p[c * T + t] + v[c];
   }
   if (counters && CLS) {
     unsigned long long g = nGeneral, pp = nDenseParallel, cc = nCore;
