@@ -206,3 +206,17 @@ def test_errors(pkg):
     bad.links[0, 2] = net.numNode + 5
     with pytest.raises(IndexError):
         ctx.detect_collision(1.0, bad, ())
+
+
+def test_edge_cases(pkg, oracle):
+    """No nodes, one segment, every node fixed: nothing to report, and the
+    oracle agrees field by field."""
+    ctx = pkg.get_context()
+    empty = pkg.DislocationNetwork(np.zeros((3, 0)), np.zeros((3, 0)), np.zeros((0, 3), np.int64))
+    assert ctx.detect_collision(1.0, empty)[0] == (False, "null", 0, 0, 0, 0, 0, 0, 0.0, 0.0)
+    one = pkg.DislocationNetwork(np.array([[0.0, 1.0], [0.0, 0.0], [0.0, 0.0]]), np.ones((3, 1)) / math.sqrt(3.0),
+                                 np.array([[1, 1, 2]]), nodeVel=np.array([[0.0, 1.0], [0.0, 0.0], [0.0, 0.0]]))
+    assert _compare(pkg, oracle, one, 100.0)[:2] == (False, "null")
+    fixed = polygons(pkg, 50, 5)
+    fixed.label[:] = 2  # intFixDln: no hinge, no two-line pair is evaluated
+    assert _compare(pkg, oracle, fixed, 1e6) == (False, "null", 0, 0, 0, 0, 0, 0, 0.0, 0.0)

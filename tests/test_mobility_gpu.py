@@ -89,3 +89,21 @@ def test_errors(pkg, synth):
     net.connectivity[1, 0] = 10 ** 6  # a link that does not exist
     with pytest.raises(IndexError):
         pkg.dlnMobility(dln, mat, net)
+
+
+def test_isolated_node(pkg, oracle):
+    """A node without connections has no force and a singular drag: its
+    velocity is NaN (0/0 in the 3x3 solve, as StaticArrays' Cramer solve in the
+    reference gives); the other nodes are unaffected."""
+    coord = np.array([[0.0, 100.0, 0.0, 500.0], [0.0, 0.0, 100.0, 500.0], [0.0, 0.0, 0.0, 500.0]])
+    seg = np.array([[1, 1, 2], [2, 2, 3], [3, 3, 1]])
+    b = np.ones((3, 3)) / np.sqrt(3.0)
+    net = pkg.DislocationNetwork(coord, b, seg, numNode=4)
+    net.segForce[...] = np.random.default_rng(2).normal(size=net.segForce.shape)
+    dln = pkg.DislocationParameters(coreRad=1.0, dragCoeffs=dict(edge=1.0, screw=2.0, climb=1e10, line=1e-4))
+    mat = pkg.MaterialParameters(mu=1.0, nu=0.28)
+    F, V = pkg.dlnMobility(dln, mat, net)
+    rF, rV = oracle.mobility_bcc(_mp(dln, mat), net.coord, net.bVec, net.links, net.connectivity, net.segForce,
+                                 net.numNode)
+    assert np.all(F[:, 3] == 0) and np.all(np.isnan(V[:, 3])) and np.all(np.isnan(rV[:, 3]))
+    assert np.array_equal(F, rF) and np.array_equal(V[:, :3], rV[:, :3])

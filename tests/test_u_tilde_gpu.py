@@ -165,3 +165,10 @@ def test_errors(pkg, fixtures):
     pts[0, 1] = np.inf
     with pytest.raises(ValueError):
         ctx.u_tilde(mat.omνInv8π, mat.om2νomνInv8π, mesh, pts, net)
+
+
+def test_no_segments(pkg, fixtures):
+    """A network without segments displaces nothing."""
+    mesh, bnd, mat, _ = _golden(pkg, fixtures)
+    empty = pkg.DislocationNetwork(np.zeros((3, 0)), np.zeros((3, 0)), np.zeros((0, 3), np.int64))
+    assert not np.any(pkg.calc_uTilde(mesh, bnd, mat, empty))
