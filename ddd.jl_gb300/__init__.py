@@ -38,6 +38,7 @@ EXPORTED_SYMBOLS = (
     "ddd_detect_collision", "ddd_minimum_distance", "ddd_u_tilde",
     "ddd_segseg_force", "ddd_segseg_force_inplace", "ddd_sigma_tilde",
     "ddd_segseg_force_device", "ddd_sigma_tilde_device", "ddd_set_mode", "ddd_get_mode", "ddd_probe_fma_peak",
+    "ddd_set_partial_limit", "ddd_get_partial_limit",
     "ddd_segseg_force_device_noalloc",
     "ddd_batch_create", "ddd_batch_run", "ddd_batch_info", "ddd_batch_last_error", "ddd_batch_destroy",
     "ddd_tc_gemm_bf16",
@@ -216,6 +217,9 @@ def library():
                                   _dp, _i64]
         L.ddd_set_mode.argtypes = [_vp, ctypes.c_int]
         L.ddd_get_mode.argtypes = [_vp]
+        L.ddd_set_partial_limit.argtypes = [_vp, ctypes.c_int64]
+        L.ddd_get_partial_limit.argtypes = [_vp]
+        L.ddd_get_partial_limit.restype = ctypes.c_int64
         L.ddd_probe_fma_peak.argtypes = [_vp, ctypes.c_int, _dp]
         _lib = L
     return _lib
@@ -648,6 +652,16 @@ class Context:
     @mode.setter
     def mode(self, m):
         self._check(self._L.ddd_set_mode(self._h, MODES.get(m, m) if isinstance(m, str) else int(m)))
+
+    @property
+    def partial_limit(self):
+        """Bytes of device memory for the all-pairs partial sums; past it the
+        tile pairs run in bands of tile columns (set 0 for the default)."""
+        return self._L.ddd_get_partial_limit(self._h)
+
+    @partial_limit.setter
+    def partial_limit(self, nbytes):
+        self._check(self._L.ddd_set_partial_limit(self._h, int(nbytes)))
 
     def tc_gemm_bf16(self, M, N, K, a_ptr, b_ptr, d_ptr, stream=None):
         """D[M×N] fp32 = A[M×K] · B[N×K]^T on tcgen05 (device pointers)."""

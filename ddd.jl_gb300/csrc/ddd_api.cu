@@ -40,6 +40,7 @@ struct ddd_ctx {
   ddd::UTildeScratch* ut = nullptr;
   std::vector<double> hostTmp;
   double lastKernelMs = 0.0;  // device time of the last self-force / mobility kernel
+  int64_t partialLimit = 0;   // bytes of all-pairs partial sums; 0: kDefaultPartialLimit
 };
 
 int ddd::ctx_device(const ddd_ctx* c) { return c->device; }
@@ -77,16 +78,36 @@ cudaError_t prep_df_if_needed(ddd_ctx* c, int64_t npad, cudaStream_t st) {
   return ddd::launch_prep_df(c->soa.as<double>(), npad, c->soadf.as<float>(), st);
 }
 
+// All-pairs partial sums: 16 GiB by default.  Below that every tile pair has
+// its slot (one tile launch, one reduction); above it the launchers run bands
+// of tile columns through a buffer of the limit's size.
+constexpr int64_t kDefaultPartialLimit = (int64_t)16 << 30;
+
+// Slots to allocate for npad segments: all nt(nt+1)/2 when they fit in the
+// context's limit, else as many as the limit holds, at least one column (nt).
+int64_t partial_slots(const ddd_ctx* c, int64_t npad) {
+  const int64_t tile = ddd::strict::segseg_npad(1);
+  const int64_t slotBytes = (int64_t)ddd::strict::segseg_partial_bytes_all(tile);
+  const int64_t nt = npad / tile, all = nt * (nt + 1) / 2;
+  const int64_t cap = (c->partialLimit ? c->partialLimit : kDefaultPartialLimit) / slotBytes;
+  return cap >= all ? all : (cap < nt ? nt : cap);
+}
+
+size_t partial_bytes(const ddd_ctx* c, int64_t npad) {
+  return (size_t)partial_slots(c, npad) * ddd::strict::segseg_partial_bytes_all(ddd::strict::segseg_npad(1));
+}
+
 cudaError_t run_segseg_all(ddd_ctx* c, const ddd::KConsts& K, const double* soa, const uint8_t* skip, int64_t npad,
                            double* partial, double* out, int64_t numSeg, unsigned long long* cnt, cudaStream_t st) {
+  const int64_t cap = partial_slots(c, npad);
   if (use_df(c)) {
     cudaError_t e = prep_df_if_needed(c, npad, st);
     if (e != cudaSuccess) return e;
     return ddd::launch_segseg_all_df(K, soa, c->soadf.as<float>(), skip, npad, partial, out, numSeg, cnt, st,
-                                     df_form(c));
+                                     df_form(c), cap);
   }
-  return use_fma(c) ? ddd::fast::launch_segseg_all_f64(K, soa, skip, npad, partial, out, numSeg, cnt, st)
-                    : ddd::strict::launch_segseg_all_f64(K, soa, skip, npad, partial, out, numSeg, cnt, st);
+  return use_fma(c) ? ddd::fast::launch_segseg_all_f64(K, soa, skip, npad, partial, out, numSeg, cnt, st, cap)
+                    : ddd::strict::launch_segseg_all_f64(K, soa, skip, npad, partial, out, numSeg, cnt, st, cap);
 }
 
 cudaError_t run_segseg_rows(ddd_ctx* c, const ddd::KConsts& K, const double* soa, const uint8_t* skip, int64_t npad,
@@ -216,7 +237,7 @@ int segseg_compute(ddd_ctx* ctx, const ddd_consts* k, const double* coord, int64
   CK(cudaMemsetAsync(ctx->counters.p, 0, 3 * sizeof(unsigned long long), ctx->stream), "memset counters");
   CK(ctx->out.ensure((size_t)nOut * 6 * sizeof(double)), "alloc output");
   if (!rowsMode) {
-    CK(ctx->partial.ensure(ddd::strict::segseg_partial_bytes_all(npad)), "alloc partial sums");
+    CK(ctx->partial.ensure(partial_bytes(ctx, npad)), "alloc partial sums");
     CK(cudaEventRecord(ctx->ev[1], ctx->stream), "event");
     CK(run_segseg_all(ctx, K, ctx->soa.as<double>(), ctx->skip.as<uint8_t>(), npad, ctx->partial.as<double>(),
                                   ctx->out.as<double>(), numSeg, ctx->counters.as<unsigned long long>(), ctx->stream),
@@ -773,7 +794,7 @@ int ddd_segseg_force_device(ddd_ctx* ctx, const ddd_consts* k, const double* seg
   const int64_t npad = ddd::strict::segseg_npad(numSeg);
   CK(ctx->soa.ensure(ddd::strict::segseg_soa_bytes(npad)), "alloc segment SoA");
   CK(ctx->skip.ensure((size_t)npad), "alloc skip flags");
-  CK(ctx->partial.ensure(ddd::strict::segseg_partial_bytes_all(npad)), "alloc partial sums");
+  CK(ctx->partial.ensure(partial_bytes(ctx, npad)), "alloc partial sums");
   CK(ctx->counters.ensure(3 * sizeof(unsigned long long)), "alloc counters");
   if (rep) CK(cudaMemsetAsync(ctx->counters.p, 0, 3 * sizeof(unsigned long long), st), "memset counters");
   if (rep) CK(cudaEventRecord(ctx->ev[1], st), "event");
@@ -843,6 +864,18 @@ int ddd_set_mode(ddd_ctx* ctx, int mode) {
 }
 
 int ddd_get_mode(const ddd_ctx* ctx) { return ctx ? ctx->mode : DDD_EINVAL; }
+
+int ddd_set_partial_limit(ddd_ctx* ctx, int64_t bytes) {
+  if (!ctx) return DDD_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (bytes < 0) return fail(ctx, DDD_EINVAL, "negative partial-sum limit");
+  ctx->partialLimit = bytes;
+  return DDD_OK;
+}
+
+int64_t ddd_get_partial_limit(const ddd_ctx* ctx) {
+  return ctx ? (ctx->partialLimit ? ctx->partialLimit : kDefaultPartialLimit) : DDD_EINVAL;
+}
 
 int ddd_surrogate_make_data(ddd_ctx* ctx, const ddd_consts* k, const double* segs, int64_t n, const int32_t* pairs,
                             int64_t P, void* X, float* Bp, float* T, double* F) {

@@ -12,6 +12,11 @@ namespace ddd {
 
 struct KConsts;
 
+// All-pairs partial sums: one slot (12 x TILE doubles) per tile pair I <= J,
+// slot J(J+1)/2 + I.  The all-pairs launchers take the partial buffer's size
+// in slots; when it is below nt(nt+1)/2 they run bands of J columns (each band
+// at most capSlots slots, at least one column, so capSlots >= nt is required).
+//
 // segseg_f64.cu and sigma_f64.cu, each compiled as two variants:
 //   strict: --fmad=false, every operation rounded as in the reference;
 //   fast:   FMA contraction.
@@ -25,15 +30,18 @@ struct KConsts;
                                    cudaStream_t st); \
   cudaError_t launch_prep_segments_packed(const double* in, int64_t ldIn, const uint8_t* extSeg, int64_t numSeg, \
                                           int64_t npad, double* soa, uint8_t* skip, cudaStream_t st); \
+  int64_t segseg_band_end(int64_t J0, int64_t nt, int64_t capSlots); \
   cudaError_t launch_segseg_all_f64(const KConsts& K, const double* soa, const uint8_t* skip, int64_t npad, \
                                     double* partial, double* out, int64_t numSeg, unsigned long long* counters, \
-                                    cudaStream_t st); \
+                                    cudaStream_t st, int64_t capSlots); \
   cudaError_t launch_segseg_rows_f64(const KConsts& K, const double* soa, const uint8_t* skip, int64_t npad, \
                                      const int64_t* rows, int64_t nRows, double* partial, double* out, \
                                      unsigned long long* counters, cudaStream_t st); \
   cudaError_t launch_sigma_f64(const KConsts& K, const double* soa, int64_t npad, int64_t nSeg, const double* x0, \
                                int64_t M, double* sigma, cudaStream_t st); \
   cudaError_t launch_reduce_all(const double* partial, int64_t npad, int64_t numSeg, double* out, cudaStream_t st); \
+  cudaError_t launch_reduce_band(const double* partial, int64_t J0, int64_t J1, int64_t numSeg, double* out, \
+                                 cudaStream_t st); \
   cudaError_t launch_reduce_rows(const double* partial, int64_t npad, int64_t nRows, double* out, cudaStream_t st);
 
 namespace strict {
@@ -50,7 +58,7 @@ size_t segseg_df_soa_bytes(int64_t npad);
 cudaError_t launch_prep_df(const double* soa, int64_t npad, float* soadf, cudaStream_t st);
 cudaError_t launch_segseg_all_df(const KConsts& K, const double* soa, const float* soadf, const uint8_t* skip,
                                  int64_t npad, double* partial, double* out, int64_t numSeg,
-                                 unsigned long long* counters, cudaStream_t st, int form);
+                                 unsigned long long* counters, cudaStream_t st, int form, int64_t capSlots);
 cudaError_t launch_segseg_rows_df(const KConsts& K, const double* soa, const float* soadf, const uint8_t* skip,
                                   int64_t npad, const int64_t* rows, int64_t nRows, double* partial, double* out,
                                   unsigned long long* counters, cudaStream_t st, int form);

@@ -49,12 +49,12 @@ __device__ __forceinline__ void tile_index_df(int64_t b, int64_t& I, int64_t& J)
 template <int MODE, int FORM>
 __global__ void __launch_bounds__(TILE, 2)
 segseg_tile_df(TileArgs A, typename PolDF<FORM>::Consts KP, const int64_t* __restrict__ rows, int64_t nRows,
-               int64_t nJt, double* __restrict__ partial, unsigned long long* __restrict__ counters) {
+               int64_t nJt, int64_t base, double* __restrict__ partial, unsigned long long* __restrict__ counters) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   auto& sm = *reinterpret_cast<TileSmemT<TILE, PolDF<FORM>>*>(smem_raw);
   int64_t I, J;
   if (MODE == 0) {
-    tile_index_df(blockIdx.x, I, J);
+    tile_index_df(base + blockIdx.x, I, J);  // slots base.. (a band of J columns)
   } else {
     I = blockIdx.x / nJt;
     J = blockIdx.x % nJt;
@@ -143,21 +143,31 @@ cudaError_t launch_prep_df(const double* soa, int64_t npad, float* soadf, cudaSt
 
 cudaError_t launch_segseg_all_df(const KConsts& K, const double* soa, const float* soadf, const uint8_t* skip,
                                  int64_t npad, double* partial, double* out, int64_t numSeg,
-                                 unsigned long long* counters, cudaStream_t st, int form) {
+                                 unsigned long long* counters, cudaStream_t st, int form, int64_t capSlots) {
   cudaError_t e = form ? set_attr_df<0, 1>() : set_attr_df<0, 0>();
   if (e != cudaSuccess) return e;
   const int64_t nt = npad / TILE;
   const int64_t nb = nt * (nt + 1) / 2;
   const TileArgs A{K, soa, skip, npad, soadf, nullptr};
-  if (form)
-    segseg_tile_df<0, 1><<<(unsigned)nb, TILE, sizeof(TileSmemT<TILE, PolDF<1>>), st>>>(
-        A, PolDF<1>::Consts{kconsts_df(K), kconsts_f(K)}, nullptr, 0, 0, partial, counters);
-  else
-    segseg_tile_df<0, 0><<<(unsigned)nb, TILE, sizeof(TileSmemT<TILE, PolDF<0>>), st>>>(
-        A, PolDF<0>::Consts{kconsts_df(K), kconsts_f(K)}, nullptr, 0, 0, partial, counters);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  return strict::launch_reduce_all(partial, npad, numSeg, out, st);
+  // One launch over all slots, or (partial sums larger than capSlots slots)
+  // bands of J columns in order, each reduced into the running output.
+  for (int64_t J0 = 0; J0 < nt;) {
+    const int64_t J1 = capSlots >= nb ? nt : strict::segseg_band_end(J0, nt, capSlots);
+    const int64_t b0 = J0 * (J0 + 1) / 2, nbb = J1 * (J1 + 1) / 2 - b0;
+    if (form)
+      segseg_tile_df<0, 1><<<(unsigned)nbb, TILE, sizeof(TileSmemT<TILE, PolDF<1>>), st>>>(
+          A, PolDF<1>::Consts{kconsts_df(K), kconsts_f(K)}, nullptr, 0, 0, b0, partial, counters);
+    else
+      segseg_tile_df<0, 0><<<(unsigned)nbb, TILE, sizeof(TileSmemT<TILE, PolDF<0>>), st>>>(
+          A, PolDF<0>::Consts{kconsts_df(K), kconsts_f(K)}, nullptr, 0, 0, b0, partial, counters);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    e = capSlots >= nb ? strict::launch_reduce_all(partial, npad, numSeg, out, st)
+                       : strict::launch_reduce_band(partial, J0, J1, numSeg, out, st);
+    if (e != cudaSuccess) return e;
+    J0 = J1;
+  }
+  return cudaSuccess;
 }
 
 cudaError_t launch_segseg_rows_df(const KConsts& K, const double* soa, const float* soadf, const uint8_t* skip,
@@ -171,10 +181,10 @@ cudaError_t launch_segseg_rows_df(const KConsts& K, const double* soa, const flo
   const TileArgs A{K, soa, skip, npad, soadf, nullptr};
   if (form)
     segseg_tile_df<1, 1><<<grid, TILE, sizeof(TileSmemT<TILE, PolDF<1>>), st>>>(
-        A, PolDF<1>::Consts{kconsts_df(K), kconsts_f(K)}, rows, nRows, nJt, partial, counters);
+        A, PolDF<1>::Consts{kconsts_df(K), kconsts_f(K)}, rows, nRows, nJt, 0, partial, counters);
   else
     segseg_tile_df<1, 0><<<grid, TILE, sizeof(TileSmemT<TILE, PolDF<0>>), st>>>(
-        A, PolDF<0>::Consts{kconsts_df(K), kconsts_f(K)}, rows, nRows, nJt, partial, counters);
+        A, PolDF<0>::Consts{kconsts_df(K), kconsts_f(K)}, rows, nRows, nJt, 0, partial, counters);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   return strict::launch_reduce_rows(partial, npad, nRows, out, st);

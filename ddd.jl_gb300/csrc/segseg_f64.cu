@@ -115,17 +115,19 @@ __device__ __forceinline__ void tile_index(int64_t b, int64_t& I, int64_t& J) {
   I = b - Jc * (Jc + 1) / 2;
 }
 
-// MODE 0: all pairs (symmetric, i < j), one CTA per tile pair I <= J.
+// MODE 0: all pairs (symmetric, i < j), one CTA per tile pair I <= J; the
+//         launch covers slots base.. (a band of J columns), its partial blocks
+//         indexed from base.
 // MODE 1: index rows (all j != i, F12 only), one CTA per (row tile, column tile).
 template <int MODE>
 __global__ void __launch_bounds__(TILE, 2)
-segseg_tile_f64(TileArgs A, const int64_t* __restrict__ rows, int64_t nRows, int64_t nJt, double* __restrict__ partial,
-                unsigned long long* __restrict__ counters) {
+segseg_tile_f64(TileArgs A, const int64_t* __restrict__ rows, int64_t nRows, int64_t nJt, int64_t base,
+                double* __restrict__ partial, unsigned long long* __restrict__ counters) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   auto& sm = *reinterpret_cast<TileSmemT<TILE, PolF64>*>(smem_raw);
   int64_t I, J;
   if (MODE == 0) {
-    tile_index(blockIdx.x, I, J);
+    tile_index(base + blockIdx.x, I, J);
   } else {
     I = blockIdx.x / nJt;
     J = blockIdx.x % nJt;
@@ -156,6 +158,41 @@ __global__ void segseg_reduce_all(const double* __restrict__ partial, int64_t nt
     const double* p = partial + b * 12 * TILE;
 #pragma unroll
     for (int c = 0; c < 6; ++c) acc[c] += p[(6 + c) * TILE + t];
+  }
+#pragma unroll
+  for (int c = 0; c < 6; ++c) out[6 * s + c] = acc[c];
+}
+
+// Banded all-pairs: one launch of the tile kernel covered the J columns
+// [J0, J1), slots J0(J0+1)/2 .. J1(J1+1)/2 - 1, stored from the band's first
+// slot.  Segment s in tile A < J1 adds its row blocks (A, J) for J in
+// [max(A, J0), J1), then, when A lies in the band, its column blocks (I, A)
+// for I = 0..A.  The band holding A starts the sum, later bands add to it: a
+// fixed order, so the result is deterministic (it is the unbanded sum
+// regrouped, equal to rounding).
+__global__ void segseg_reduce_band(const double* __restrict__ partial, int64_t J0, int64_t J1, int64_t numSeg,
+                                   double* __restrict__ out) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= numSeg) return;
+  const int64_t A = s / TILE;
+  if (A >= J1) return;
+  const int t = (int)(s % TILE);
+  const int64_t base = J0 * (J0 + 1) / 2;
+  const bool first = A >= J0;
+  double acc[6];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) acc[c] = first ? 0.0 : out[6 * s + c];
+  for (int64_t Jt = first ? A : J0; Jt < J1; ++Jt) {
+    const double* p = partial + (Jt * (Jt + 1) / 2 + A - base) * 12 * TILE;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) acc[c] += p[c * TILE + t];
+  }
+  if (first) {
+    for (int64_t It = 0; It <= A; ++It) {
+      const double* p = partial + (A * (A + 1) / 2 + It - base) * 12 * TILE;
+#pragma unroll
+      for (int c = 0; c < 6; ++c) acc[c] += p[(6 + c) * TILE + t];
+    }
   }
 #pragma unroll
   for (int c = 0; c < 6; ++c) out[6 * s + c] = acc[c];
@@ -223,6 +260,20 @@ cudaError_t launch_reduce_all(const double* partial, int64_t npad, int64_t numSe
   return cudaGetLastError();
 }
 
+int64_t segseg_band_end(int64_t J0, int64_t nt, int64_t capSlots) {
+  const int64_t b0 = J0 * (J0 + 1) / 2;
+  int64_t J1 = J0 + 1;
+  while (J1 < nt && (J1 + 1) * (J1 + 2) / 2 - b0 <= capSlots) ++J1;
+  return J1;
+}
+
+cudaError_t launch_reduce_band(const double* partial, int64_t J0, int64_t J1, int64_t numSeg, double* out,
+                               cudaStream_t st) {
+  const int64_t n = numSeg < J1 * TILE ? numSeg : J1 * TILE;
+  segseg_reduce_band<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(partial, J0, J1, n, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_reduce_rows(const double* partial, int64_t npad, int64_t nRows, double* out, cudaStream_t st) {
   segseg_reduce_rows<<<(unsigned)((nRows + 127) / 128), 128, 0, st>>>(partial, npad / TILE, nRows, out);
   return cudaGetLastError();
@@ -230,18 +281,33 @@ cudaError_t launch_reduce_rows(const double* partial, int64_t npad, int64_t nRow
 
 cudaError_t launch_segseg_all_f64(const KConsts& K, const double* soa, const uint8_t* skip, int64_t npad,
                                   double* partial, double* out, int64_t numSeg, unsigned long long* counters,
-                                  cudaStream_t st) {
+                                  cudaStream_t st, int64_t capSlots) {
   cudaError_t e = set_attr<0>();
   if (e != cudaSuccess) return e;
   const int64_t nt = npad / TILE;
   const int64_t nb = nt * (nt + 1) / 2;
   const TileArgs A{K, soa, skip, npad, nullptr, nullptr};
-  segseg_tile_f64<0><<<(unsigned)nb, TILE, sizeof(TileSmemT<TILE, PolF64>), st>>>(A, nullptr, 0, 0, partial,
-                                                                                  counters);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  segseg_reduce_all<<<(unsigned)((numSeg + 127) / 128), 128, 0, st>>>(partial, nt, numSeg, out);
-  return cudaGetLastError();
+  if (capSlots >= nb) {
+    segseg_tile_f64<0><<<(unsigned)nb, TILE, sizeof(TileSmemT<TILE, PolF64>), st>>>(A, nullptr, 0, 0, 0, partial,
+                                                                                    counters);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    segseg_reduce_all<<<(unsigned)((numSeg + 127) / 128), 128, 0, st>>>(partial, nt, numSeg, out);
+    return cudaGetLastError();
+  }
+  // Partial sums larger than capSlots slots: bands of J columns, in order.
+  for (int64_t J0 = 0; J0 < nt;) {
+    const int64_t J1 = segseg_band_end(J0, nt, capSlots);
+    const int64_t b0 = J0 * (J0 + 1) / 2, nbb = J1 * (J1 + 1) / 2 - b0;
+    segseg_tile_f64<0><<<(unsigned)nbb, TILE, sizeof(TileSmemT<TILE, PolF64>), st>>>(A, nullptr, 0, 0, b0, partial,
+                                                                                     counters);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    e = launch_reduce_band(partial, J0, J1, numSeg, out, st);
+    if (e != cudaSuccess) return e;
+    J0 = J1;
+  }
+  return cudaSuccess;
 }
 
 cudaError_t launch_segseg_rows_f64(const KConsts& K, const double* soa, const uint8_t* skip, int64_t npad,
@@ -252,7 +318,7 @@ cudaError_t launch_segseg_rows_f64(const KConsts& K, const double* soa, const ui
   const int64_t nJt = npad / TILE;
   const int64_t nrt = (nRows + TILE - 1) / TILE;
   const TileArgs A{K, soa, skip, npad, nullptr, nullptr};
-  segseg_tile_f64<1><<<(unsigned)(nrt * nJt), TILE, sizeof(TileSmemT<TILE, PolF64>), st>>>(A, rows, nRows, nJt,
+  segseg_tile_f64<1><<<(unsigned)(nrt * nJt), TILE, sizeof(TileSmemT<TILE, PolF64>), st>>>(A, rows, nRows, nJt, 0,
                                                                                            partial, counters);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;

@@ -94,7 +94,7 @@ int ddd_segseg_force_device_noalloc(const ddd_consts* k, const double* segs, int
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaError_t e = ddd::strict::launch_prep_segments_packed(segs, ldSegs, ext, numSeg, npad, soa, skip, st);
   if (e == cudaSuccess)
-    e = ddd::strict::launch_segseg_all_f64(K, soa, skip, npad, partial, force, numSeg, nullptr, st);
+    e = ddd::strict::launch_segseg_all_f64(K, soa, skip, npad, partial, force, numSeg, nullptr, st, INT64_MAX);
   return e == cudaSuccess ? DDD_OK : DDD_EDEVICE;
 }
 

@@ -343,6 +343,18 @@ void ddd_batch_destroy(ddd_batch* b);
 int ddd_set_mode(ddd_ctx* ctx, int mode);
 int ddd_get_mode(const ddd_ctx* ctx);
 
+/* Device memory for the all-pairs seg-seg partial sums of ctx, in bytes (0:
+ * the default, 16 GiB).  The all-pairs forms keep 12 x 128 doubles per pair
+ * of 128-segment tiles, nt(nt+1)/2 of them for nt tiles (6.4 GB at 131,072
+ * segments, 184 GB at 700,000).  When they exceed the limit the pairs run in
+ * bands of tile columns through a buffer of the limit's size (never below one
+ * column, nt slots), each band's sums added to the output in band order: the
+ * same deterministic result on every call, equal to the unbanded one to
+ * rounding.  No reference counterpart (the reference allocates per call).
+ * ddd_get_partial_limit returns the limit in force. */
+int ddd_set_partial_limit(ddd_ctx* ctx, int64_t bytes);
+int64_t ddd_get_partial_limit(const ddd_ctx* ctx);
+
 /* Tensor-core building block of the learned surrogate (no reference
  * counterpart): D[M x N] (FP32) = A[M x K] * B[N x K]^T with BF16 A and B,
  * row-major with K contiguous, on tcgen05 (accumulators in TMEM).  M a multiple

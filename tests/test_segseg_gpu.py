@@ -321,3 +321,43 @@ def test_f32c_mode(pkg, synth, oracle, num_loops, seed, pf, cube):
     assert np.all(nrm(F - ext) <= 1e-4 * nrm(ext) + 1e-6 * nrm(ext).max())
     exti = ext[:, :, [4, 8, 8]]
     assert np.all(nrm(Fi - exti) <= 1e-4 * nrm(exti) + 1e-6 * nrm(ext).max())
+
+
+@pytest.mark.parametrize("mode", ["fp64", "fp64_fma", "df64", "f32c"])
+def test_banded_partial_sums(pkg, synth, oracle, mode):
+    """A partial-sum limit below the all-pairs slot count (4,800 segments: 38
+    tiles, 741 tile pairs of 12,288 bytes) makes the launchers run bands of
+    tile columns: 100 slots (bands of 1-14 columns) and the minimum (one column
+    of 38 slots, 1 byte asked).  The band sums regroup the same FP64 additions,
+    so the forces equal the unbanded ones to rounding, repeat bit for bit, and
+    in the reference's arithmetic stay within the oracle bounds; the
+    device-resident entry point bands the same way."""
+    net = _synthetic(pkg, synth, 600, 7)
+    assert net.numSeg == 4800
+    dln, mat = _params(pkg)
+    ctx = pkg.get_context()
+    assert ctx.partial_limit == 16 << 30
+    ctx.mode = mode
+    try:
+        F = pkg.calcSegSegForce(dln, mat, net)
+        for limit in (100 * 12288, 1):
+            ctx.partial_limit = limit
+            Fb = pkg.calcSegSegForce(dln, mat, net)
+            assert np.linalg.norm(Fb - F) <= 1e-13 * np.linalg.norm(F)
+            assert np.array_equal(pkg.calcSegSegForce(dln, mat, net), Fb)
+            if mode == "fp64":
+                check_forces(Fb, oracle, k5_of(dln, mat), net)
+                torch = pytest.importorskip("torch")
+                rows9 = np.r_[net.coord[:, net.segIdx[:, 1] - 1], net.coord[:, net.segIdx[:, 2] - 1], net.bVec]
+                soa = torch.from_numpy(np.ascontiguousarray(rows9)).cuda()  # 9 x numSeg, row-major
+                out = torch.zeros(6 * net.numSeg, dtype=torch.float64, device="cuda")
+                ctx.segseg_force_device(pkg.consts_of(dln, mat), soa.data_ptr(), soa.shape[1], net.numSeg,
+                                        out.data_ptr(), stream=torch.cuda.current_stream().cuda_stream)
+                torch.cuda.synchronize()
+                assert np.array_equal(out.cpu().numpy().reshape(3, 2, -1, order="F"), Fb)
+    finally:
+        ctx.partial_limit = 0
+        ctx.mode = "fp64"
+    assert ctx.partial_limit == 16 << 30
+    with pytest.raises(ValueError):
+        ctx.partial_limit = -1
