@@ -19,6 +19,7 @@ export calcSegSegForceGPU, calcSegSegForceGPU!, calc_σTildeGPU, calc_σTildeGPU
 export calcSelfForceGPU, calcSelfForceGPU!, calcSegForceGPU, calcSegForceGPU!
 export Surrogate, loadSurrogate, calcSegSegForceSurrogateGPU
 export dlnMobilityGPU, dlnMobilityGPU!, detectCollisionGPU, minimumDistanceGPU, calc_uTildeGPU, calc_uTildeGPU!
+export setPartialLimitGPU, partialLimitGPU
 
 const libddd = joinpath(@__DIR__, "..", "libddd_gb300.so")
 
@@ -54,6 +55,13 @@ function check(rc)
 end
 
 idxvec(idx) = isnothing(idx) ? Int64[] : collect(Int64, idx)
+
+# Device memory for the all-pairs partial sums (bytes; 0 = the 16 GiB
+# default).  Networks whose tile pairs need more run in bands of tile columns
+# through a buffer of this size (same forces to rounding, deterministic).
+setPartialLimitGPU(bytes::Integer) =
+    check(ccall((:ddd_set_partial_limit, libddd), Cint, (Ptr{Cvoid}, Int64), context(), bytes))
+partialLimitGPU() = ccall((:ddd_get_partial_limit, libddd), Int64, (Ptr{Cvoid},), context())
 
 # calcSegSegForce (src/Processing/DislocationForces.jl:470-561)
 function calcSegSegForceGPU(dlnParams, matParams, network, idx = nothing)
