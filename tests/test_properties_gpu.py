@@ -115,3 +115,24 @@ def test_u_tilde_linear_in_burgers_vectors(pkg, synth):
     mat = pkg.MaterialParameters(mu=1.0, nu=0.28)
     u = pkg.calc_uTilde(mesh, bnd, mat, net)
     assert np.array_equal(pkg.calc_uTilde(mesh, bnd, mat, net2), 2.0 * u)
+
+
+def test_banded_65k(pkg, synth):
+    """The 65,536-segment workload (512 tiles, 131,328 tile pairs, 1.6 GB of
+    partial sums) in the f32c form with the partial-sum buffer capped at 256
+    MiB (7 bands of at most 21,845 tile pairs): the unbanded forces to
+    rounding, bilinear as exactly as the unbanded form."""
+    dln, mat = _params(pkg, synth)
+    ctx = pkg.get_context()
+    ctx.mode = "f32c"
+    try:
+        net = _net(pkg, synth, "gpu65k", 0)[0]
+        F = pkg.calcSegSegForce(dln, mat, net)
+        ctx.partial_limit = 256 << 20
+        Fb = pkg.calcSegSegForce(dln, mat, net)
+        F2 = pkg.calcSegSegForce(dln, mat, _net(pkg, synth, "gpu65k", 0, 2.0)[0])
+    finally:
+        ctx.partial_limit = 0
+        ctx.mode = "fp64"
+    assert np.linalg.norm(Fb - F) <= 1e-13 * np.linalg.norm(F)
+    assert np.array_equal(F2, 4.0 * Fb)
