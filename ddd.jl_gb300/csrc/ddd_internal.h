@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstddef>
 #include <cstdint>
 #include <vector>
@@ -11,6 +12,22 @@ struct ddd_ctx;
 namespace ddd {
 
 struct KConsts;
+
+// Raise a kernel's dynamic shared-memory limit on the current device, once per
+// device: the attribute lives in each device's context, so `done` keeps one bit
+// per device (devices past 63 set it on every call).  The bits are atomic, so
+// contexts on several host threads may race here; setting it twice is harmless.
+template <typename Kernel>
+cudaError_t set_smem_once(Kernel* kernel, int bytes, std::atomic<uint64_t>& done) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const uint64_t bit = dev < 64 ? (uint64_t)1 << dev : 0;
+  if (bit && (done.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess && bit) done.fetch_or(bit, std::memory_order_release);
+  return e;
+}
 
 // All-pairs partial sums: one slot (12 x TILE doubles) per tile pair I <= J,
 // slot J(J+1)/2 + I.  The all-pairs launchers take the partial buffer's size

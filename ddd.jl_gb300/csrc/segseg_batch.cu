@@ -263,15 +263,12 @@ KConsts kconsts(const ddd_consts* k) {
 // any stream capture.
 template <int T, class P>
 cudaError_t prepare_persistent(int device, Layout& L) {
-  static bool attr = false;
+  static std::atomic<uint64_t> attr{0};
   const int smem = (int)sizeof(TileSmemT<T, P>);
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(persistent_tiles<T, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  cudaError_t e = set_smem_once(persistent_tiles<T, P>, smem, attr);
+  if (e != cudaSuccess) return e;
   int sms = 0, per = 0;
-  cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   if (e != cudaSuccess) return e;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, persistent_tiles<T, P>, T, smem);
   if (e != cudaSuccess) return e;

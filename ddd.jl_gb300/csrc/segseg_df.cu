@@ -63,17 +63,10 @@ segseg_tile_df(TileArgs A, typename PolDF<FORM>::Consts KP, const int64_t* __res
                                      partial + (int64_t)blockIdx.x * (MODE == 0 ? 12 : 6) * TILE, counters);
 }
 
-bool g_attr_df[2][2] = {{false, false}, {false, false}};
-
 template <int MODE, int FORM>
 cudaError_t set_attr_df() {
-  if (!g_attr_df[MODE][FORM]) {
-    cudaError_t e = cudaFuncSetAttribute(segseg_tile_df<MODE, FORM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sizeof(TileSmemT<TILE, PolDF<FORM>>));
-    if (e != cudaSuccess) return e;
-    g_attr_df[MODE][FORM] = true;
-  }
-  return cudaSuccess;
+  static std::atomic<uint64_t> done{0};
+  return set_smem_once(segseg_tile_df<MODE, FORM>, (int)sizeof(TileSmemT<TILE, PolDF<FORM>>), done);
 }
 
 // σ̃ in the mixed form (sigma_point_mixed, pair_df.cuh): one thread per point,

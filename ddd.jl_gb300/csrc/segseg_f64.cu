@@ -242,17 +242,10 @@ cudaError_t launch_prep_segments_packed(const double* in, int64_t ldIn, const ui
   return cudaGetLastError();
 }
 
-static bool g_attr_set[2] = {false, false};
-
 template <int MODE>
 static cudaError_t set_attr() {
-  if (!g_attr_set[MODE]) {
-    cudaError_t e = cudaFuncSetAttribute(segseg_tile_f64<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sizeof(TileSmemT<TILE, PolF64>));
-    if (e != cudaSuccess) return e;
-    g_attr_set[MODE] = true;
-  }
-  return cudaSuccess;
+  static std::atomic<uint64_t> done{0};
+  return set_smem_once(segseg_tile_f64<MODE>, (int)sizeof(TileSmemT<TILE, PolF64>), done);
 }
 
 cudaError_t launch_reduce_all(const double* partial, int64_t npad, int64_t numSeg, double* out, cudaStream_t st) {

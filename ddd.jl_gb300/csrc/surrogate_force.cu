@@ -390,12 +390,8 @@ uint32_t slot_hash(uint32_t x) {
 
 template <int MODE, class P>
 cudaError_t set_exact_attr() {
-  static bool done = false;
-  if (done) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(sf::exact_tiles<MODE, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)sizeof(TileSmemT<sf::T, P>));
-  if (e == cudaSuccess) done = true;
-  return e;
+  static std::atomic<uint64_t> done{0};
+  return set_smem_once(sf::exact_tiles<MODE, P>, (int)sizeof(TileSmemT<sf::T, P>), done);
 }
 
 template <int MODE, class P>

@@ -376,11 +376,8 @@ cudaError_t launch_prep_mlp_seg(const double* soa, const uint8_t* skip, int64_t 
 }
 
 cudaError_t prepare_mlp_far_tiles() {
-  static bool attr = false;
-  if (attr) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(mlp_far_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
-  if (e == cudaSuccess) attr = true;
-  return e;
+  static std::atomic<uint64_t> attr{0};
+  return set_smem_once(mlp_far_tiles, kSmem, attr);
 }
 
 cudaError_t launch_mlp_far_tiles(const float* ms, int64_t npad, const int4* items, int32_t nItems, int32_t* next,

@@ -427,16 +427,18 @@ namespace {
 
 // CRC-32 (IEEE 802.3, reflected, polynomial 0xEDB88320; the zlib checksum).
 uint32_t crc32_bytes(const unsigned char* p, size_t n) {
-  static uint32_t table[256];
-  static bool init = false;
-  if (!init) {
-    for (uint32_t i = 0; i < 256; ++i) {
-      uint32_t c = i;
-      for (int k = 0; k < 8; ++k) c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
-      table[i] = c;
+  struct Table {
+    uint32_t v[256];
+    Table() {
+      for (uint32_t i = 0; i < 256; ++i) {
+        uint32_t c = i;
+        for (int k = 0; k < 8; ++k) c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
+        v[i] = c;
+      }
     }
-    init = true;
-  }
+  };
+  static const Table t;  // initialised once, thread-safe (C++11 static local)
+  const uint32_t* table = t.v;
   uint32_t c = 0xFFFFFFFFu;
   for (size_t i = 0; i < n; ++i) c = table[(c ^ p[i]) & 0xFF] ^ (c >> 8);
   return c ^ 0xFFFFFFFFu;

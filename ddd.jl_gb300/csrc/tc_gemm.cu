@@ -100,12 +100,9 @@ size_t tc_gemm_smem_bytes(int N) { return (size_t)(128 + N) * KC * 2; }
 static cudaError_t launch_tc_gemm(int M, int N, int K, const void* A, const void* B, float* D, int* err,
                                   cudaStream_t st, bool f16) {
   const int smem = (int)tc_gemm_smem_bytes(N);
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(tc_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  static std::atomic<uint64_t> attr{0};
+  cudaError_t e = set_smem_once(tc_gemm_tn, 64 * 1024, attr);
+  if (e != cudaSuccess) return e;
   tc_gemm_tn<<<M / 128, 128, smem, st>>>(M, N, K, (const uint16_t*)A, (const uint16_t*)B, D, err,
                                          tc::idesc_f32acc(128, N, f16));
   return cudaGetLastError();
