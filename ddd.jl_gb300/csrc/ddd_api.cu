@@ -110,17 +110,39 @@ cudaError_t run_segseg_all(ddd_ctx* c, const ddd::KConsts& K, const double* soa,
                     : ddd::strict::launch_segseg_all_f64(K, soa, skip, npad, partial, out, numSeg, cnt, st, cap);
 }
 
+// Index rows per launch: all of them when their partial sums (one block of
+// 6 x TILE doubles per row tile and column tile) fit in the context's limit,
+// else whole row tiles up to the limit, at least one.  Rows are independent,
+// so chunking changes no bit of the result.
+int64_t rows_per_chunk(const ddd_ctx* c, int64_t npad, int64_t nRows) {
+  const int64_t tile = ddd::strict::segseg_npad(1);
+  const int64_t perTile = (int64_t)ddd::strict::segseg_partial_bytes_rows(tile, npad);  // one row tile
+  const int64_t limit = c->partialLimit ? c->partialLimit : kDefaultPartialLimit;
+  const int64_t tiles = limit / perTile;
+  const int64_t chunk = (tiles < 1 ? 1 : tiles) * tile;
+  return chunk < nRows ? chunk : nRows;
+}
+
 cudaError_t run_segseg_rows(ddd_ctx* c, const ddd::KConsts& K, const double* soa, const uint8_t* skip, int64_t npad,
                             const int64_t* rows, int64_t nRows, double* partial, double* out,
                             unsigned long long* cnt, cudaStream_t st) {
   if (use_df(c)) {
     cudaError_t e = prep_df_if_needed(c, npad, st);
     if (e != cudaSuccess) return e;
-    return ddd::launch_segseg_rows_df(K, soa, c->soadf.as<float>(), skip, npad, rows, nRows, partial, out, cnt, st,
-                                      df_form(c));
   }
-  return use_fma(c) ? ddd::fast::launch_segseg_rows_f64(K, soa, skip, npad, rows, nRows, partial, out, cnt, st)
-                    : ddd::strict::launch_segseg_rows_f64(K, soa, skip, npad, rows, nRows, partial, out, cnt, st);
+  const int64_t chunk = rows_per_chunk(c, npad, nRows);
+  for (int64_t r0 = 0; r0 < nRows; r0 += chunk) {
+    const int64_t n = nRows - r0 < chunk ? nRows - r0 : chunk;
+    const cudaError_t e =
+        use_df(c) ? ddd::launch_segseg_rows_df(K, soa, c->soadf.as<float>(), skip, npad, rows + r0, n, partial,
+                                               out + 6 * r0, cnt, st, df_form(c))
+        : use_fma(c) ? ddd::fast::launch_segseg_rows_f64(K, soa, skip, npad, rows + r0, n, partial, out + 6 * r0, cnt,
+                                                         st)
+                     : ddd::strict::launch_segseg_rows_f64(K, soa, skip, npad, rows + r0, n, partial, out + 6 * r0,
+                                                           cnt, st);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 cudaError_t run_sigma(ddd_ctx* c, const ddd::KConsts& K, const double* soa, int64_t npad, int64_t nSeg,
@@ -250,7 +272,7 @@ int segseg_compute(ddd_ctx* ctx, const ddd_consts* k, const double* coord, int64
                        ctx->stream),
        "copy idx");
     h2d += nIdx * (int64_t)sizeof(int64_t);
-    CK(ctx->partial.ensure(ddd::strict::segseg_partial_bytes_rows(nIdx, npad)), "alloc partial sums");
+    CK(ctx->partial.ensure(ddd::strict::segseg_partial_bytes_rows(rows_per_chunk(ctx, npad, nIdx), npad)), "alloc partial sums");
     CK(cudaEventRecord(ctx->ev[1], ctx->stream), "event");
     CK(run_segseg_rows(ctx, K, ctx->soa.as<double>(), ctx->skip.as<uint8_t>(), npad, ctx->rows.as<int64_t>(),
                                    nIdx, ctx->partial.as<double>(), ctx->out.as<double>(),

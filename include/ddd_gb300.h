@@ -350,7 +350,10 @@ int ddd_get_mode(const ddd_ctx* ctx);
  * bands of tile columns through a buffer of the limit's size (never below one
  * column, nt slots), each band's sums added to the output in band order: the
  * same deterministic result on every call, equal to the unbanded one to
- * rounding.  No reference counterpart (the reference allocates per call).
+ * rounding.  The idx forms keep 6 x 128 doubles per pair of a 128-row tile
+ * of idx and a column tile; past the limit their rows run in chunks of whole
+ * row tiles (at least one), with results unchanged bit for bit.  No reference
+ * counterpart (the reference allocates per call).
  * ddd_get_partial_limit returns the limit in force. */
 int ddd_set_partial_limit(ddd_ctx* ctx, int64_t bytes);
 int64_t ddd_get_partial_limit(const ddd_ctx* ctx);

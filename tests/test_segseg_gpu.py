@@ -331,20 +331,26 @@ def test_banded_partial_sums(pkg, synth, oracle, mode):
     of 38 slots, 1 byte asked).  The band sums regroup the same FP64 additions,
     so the forces equal the unbanded ones to rounding, repeat bit for bit, and
     in the reference's arithmetic stay within the oracle bounds; the
-    device-resident entry point bands the same way."""
+    device-resident entry point bands the same way.  The idx form under the
+    same limits runs its rows in chunks of row tiles: bit-identical."""
     net = _synthetic(pkg, synth, 600, 7)
     assert net.numSeg == 4800
     dln, mat = _params(pkg)
     ctx = pkg.get_context()
     assert ctx.partial_limit == 16 << 30
     ctx.mode = mode
+    idx = np.random.default_rng(2).integers(1, net.numSeg + 1, 700)
     try:
         F = pkg.calcSegSegForce(dln, mat, net)
+        Fi = pkg.calcSegSegForce(dln, mat, net, idx)
         for limit in (100 * 12288, 1):
             ctx.partial_limit = limit
             Fb = pkg.calcSegSegForce(dln, mat, net)
             assert np.linalg.norm(Fb - F) <= 1e-13 * np.linalg.norm(F)
             assert np.array_equal(pkg.calcSegSegForce(dln, mat, net), Fb)
+            # The idx form in chunks of whole row tiles (5 and 1 of the 6):
+            # each row's sum is unchanged, bit for bit.
+            assert np.array_equal(pkg.calcSegSegForce(dln, mat, net, idx), Fi)
             if mode == "fp64":
                 check_forces(Fb, oracle, k5_of(dln, mat), net)
                 torch = pytest.importorskip("torch")
@@ -361,3 +367,44 @@ def test_banded_partial_sums(pkg, synth, oracle, mode):
     assert ctx.partial_limit == 16 << 30
     with pytest.raises(ValueError):
         ctx.partial_limit = -1
+
+
+def test_concurrent_host_threads(pkg, synth):
+    """Host threads calling at once (ctypes releases the GIL): four threads on
+    the shared context (its mutex serialises them) and two on contexts of their
+    own, each mixing the all-pairs, idx and σ̃ forms; every result is the
+    single-threaded one, bit for bit."""
+    import threading
+
+    net = _synthetic(pkg, synth, 300, 31)
+    dln, mat = _params(pkg)
+    pts = synth.grid_points(8, 20000.0)
+    idx = [3, 1, net.numSeg, 3]
+    want = (pkg.calcSegSegForce(dln, mat, net), pkg.calcSegSegForce(dln, mat, net, idx),
+            pkg.calc_σTilde(pts, dln, mat, net))
+    k = pkg.consts_of(dln, mat)
+    own = [pkg.Context(0), pkg.Context(0)]
+    ctxs = [pkg.get_context()] * 4 + own
+    got, errors = [None] * len(ctxs), []
+
+    def work(t):
+        try:
+            c = ctxs[t]
+            res = []
+            for _ in range(3):
+                res.append((c.segseg_force(k, net), c.segseg_force(k, net, idx), c.sigma_tilde(k, pts, net)))
+            got[t] = res
+        except Exception as e:  # reported below, on the main thread
+            errors.append(repr(e))
+
+    threads = [threading.Thread(target=work, args=(t,)) for t in range(len(ctxs))]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join(timeout=300)
+    for c in own:
+        c.close()
+    assert not errors, errors
+    for res in got:
+        for F, Fi, S in res:
+            assert np.array_equal(F, want[0]) and np.array_equal(Fi, want[1]) and np.array_equal(S, want[2])
