@@ -19,9 +19,15 @@
 namespace ddd {
 namespace DDD_VARIANT {
 
-constexpr int SIG_TILE = 128;
+// One warp per CTA: each thread owns a point and the CTA's 32 points share a
+// 32-segment tile in shared memory.  Small CTAs spread a small point set evenly
+// over the SMs (32,768 points: 1,024 CTAs, 6.7 per SM, where 128-thread CTAs
+// left 48 SMs with one CTA and 104 with two); each point still adds the
+// segments in order 0..nSeg-1.  24 resident CTAs per SM cap registers at 85,
+// the budget the 128-thread form ran at (80).
+constexpr int SIG_TILE = 32;
 
-__global__ void __launch_bounds__(SIG_TILE)
+__global__ void __launch_bounds__(SIG_TILE, 24)
 sigma_tilde_f64(KConsts K, const double* __restrict__ soa, int64_t npad, int64_t nSeg, const double* __restrict__ x0,
                 int64_t M, double* __restrict__ sigma) {
   __shared__ double seg[12][SIG_TILE];
