@@ -272,7 +272,8 @@ int segseg_compute(ddd_ctx* ctx, const ddd_consts* k, const double* coord, int64
                        ctx->stream),
        "copy idx");
     h2d += nIdx * (int64_t)sizeof(int64_t);
-    CK(ctx->partial.ensure(ddd::strict::segseg_partial_bytes_rows(rows_per_chunk(ctx, npad, nIdx), npad)), "alloc partial sums");
+    const int64_t chunkRows = rows_per_chunk(ctx, npad, nIdx);
+    CK(ctx->partial.ensure(ddd::strict::segseg_partial_bytes_rows(chunkRows, npad)), "alloc partial sums");
     CK(cudaEventRecord(ctx->ev[1], ctx->stream), "event");
     CK(run_segseg_rows(ctx, K, ctx->soa.as<double>(), ctx->skip.as<uint8_t>(), npad, ctx->rows.as<int64_t>(),
                                    nIdx, ctx->partial.as<double>(), ctx->out.as<double>(),
