@@ -687,7 +687,7 @@ int ddd_mobility_bcc(ddd_ctx* ctx, const ddd_mob_params* mp, const double* coord
   if (n > 0 && (!nodeForce || !nodeVel)) return fail(ctx, DDD_EINVAL, "nodeForce or nodeVel is NULL");
   int rc = mobility_compute(ctx, mp, coord, coordCols, bVec, bVecCols, links, linkCols, connectivity, ldConn, connCols,
                             segForce, segForceCols, numNode, idx, nIdx);
-  if (rc) return rc;
+  if (rc || n == 0) return rc;
   std::memcpy(nodeForce, ctx->hostTmp.data(), (size_t)n * 3 * sizeof(double));
   std::memcpy(nodeVel, ctx->hostTmp.data() + 3 * n, (size_t)n * 3 * sizeof(double));
   return DDD_OK;
@@ -1109,7 +1109,7 @@ int ddd_u_tilde(ddd_ctx* ctx, double omNuInv8pi, double om2NuOmNuInv8pi, const d
   if (numSeg > linkCols || numSeg > bVecCols) return fail(ctx, DDD_EINVAL, "numSeg exceeds links / bVec");
   if (!uDofs && uLen < 3 * numPoints) return fail(ctx, DDD_EINVAL, "uTilde shorter than 3 numPoints");
   if (numPoints == 0) return DDD_OK;
-  if (!points || !uTilde || (numSeg > 0 && (!coord || !label || !links || !bVec)) ||
+  if (!points || !uTilde || (numNode > 0 && (!coord || !label)) || (numSeg > 0 && (!links || !bVec)) ||
       (mesh->numFaces > 0 && (!mesh->faceNorm || !mesh->faceMidPt)) || (mesh->numNormals > 0 && !mesh->normals))
     return fail(ctx, DDD_EINVAL, "array is NULL");
   char buf[160];
