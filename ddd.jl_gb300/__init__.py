@@ -1051,16 +1051,40 @@ def calc_uTilde_inplace(forceDisplacement, mesh, boundaries, matParams, network)
     return forceDisplacement
 
 
+class ProductIterator:
+    """Iterators.product(xs, ys, zs), the grid form of calc_σTilde's points
+    (DislocationFEM.jl:33-37, :126-140): every (x, y, z) of xs × ys × zs, the
+    first factor varying fastest as Julia enumerates it."""
+
+    def __init__(self, xs, ys, zs):
+        self.factors = [np.asarray(f, dtype=np.float64).ravel() for f in (xs, ys, zs)]
+
+    def __len__(self):
+        return int(np.prod([len(f) for f in self.factors]))
+
+    @property
+    def ndim(self):
+        return 3
+
+    def points(self):
+        """The points as a 3 × M array, in the iterator's order."""
+        grids = np.meshgrid(*self.factors, indexing="ij")
+        return np.asfortranarray(np.stack([g.ravel(order="F") for g in grids]))
+
+
 def calc_σTilde(x0, dlnParams, matParams, network, idx=None):
-    """calc_σTilde (DislocationFEM.jl:24-41): 6×M stresses, or a 6-vector for one point."""
-    x0 = np.asarray(x0, dtype=np.float64)
+    """calc_σTilde (DislocationFEM.jl:24-41): 6×M stresses, or a 6-vector for
+    one point; x0 a 3×M array or a ProductIterator (a grid of points)."""
+    x0 = x0.points() if isinstance(x0, ProductIterator) else np.asarray(x0, dtype=np.float64)
     sig = get_context().sigma_tilde(consts_of(dlnParams, matParams), x0.reshape(3, -1, order="F"), network, idx)
     return sig[:, 0].copy() if sig.shape[1] == 1 else sig
 
 
 def calc_σTilde_inplace(σ, x0, dlnParams, matParams, network, idx=None):
-    """calc_σTilde! (DislocationFEM.jl:67-84): asserts the shapes, then overwrites σ."""
-    x0 = np.asarray(x0, dtype=np.float64)
+    """calc_σTilde! (DislocationFEM.jl:67-84): asserts the shapes, then overwrites σ.
+    A ProductIterator fails the assertion, as in the reference (ndims 3)."""
+    if not isinstance(x0, ProductIterator):
+        x0 = np.asarray(x0, dtype=np.float64)
     if not (σ.ndim == x0.ndim and σ.shape[0] == 6):
         raise AssertionError("ndims(σ) == ndims(x0) && size(σ, 1) == 6")
     if σ.ndim == 2 and σ.shape[1] != x0.shape[1]:

@@ -92,3 +92,17 @@ def test_near_parallel_neighbours_present(synth):
 def test_python_mirror_argument_checks(pkg):
     with pytest.raises(AssertionError):
         pkg.calc_σTilde_inplace(np.zeros((6, 3)), np.zeros((3, 4)), None, None, None)
+
+
+def test_product_iterator_points(pkg):
+    """Iterators.product(xs, ys, zs) enumerates the first factor fastest; the
+    mirror's ProductIterator gives calc_σTilde the points in that order, and
+    calc_σTilde! rejects it as the reference's ndims assertion does."""
+    xs, ys, zs = [0.0, 1.0, 2.0], [10.0, 20.0], [-5.0, 5.0, 7.0, 9.0]
+    it = pkg.ProductIterator(xs, ys, zs)
+    P = it.points()
+    assert P.shape == (3, 24) and len(it) == 24
+    want = [(x, y, z) for z in zs for y in ys for x in xs]  # Julia's order
+    assert [tuple(P[:, j]) for j in range(24)] == want
+    with pytest.raises(AssertionError):
+        pkg.calc_σTilde_inplace(np.zeros((6, 24)), it, None, None, None)

@@ -67,6 +67,11 @@ def test_line_of_49_segments(pkg, oracle, b):
     pkg.calc_σTilde_inplace(sig, pts, dln, mat, net)
     assert np.array_equal(sig, S)
     assert_sigma_close(S, oracle.sigma_tilde(k5_of(dln, mat), pts, net))
+    # The grid as Iterators.product(r, r, [0]) (DislocationFEM.jl:33-37): the
+    # first factor varies fastest, so y-major here is x-major there.
+    G = pkg.calc_σTilde(pkg.ProductIterator(r, r, [0.0]), dln, mat, net)
+    order = np.arange(51 * 51).reshape(51, 51).T.ravel()  # product index -> pts column
+    assert np.array_equal(G, S[:, order])
 
 
 @pytest.mark.parametrize("num_loops,npts", [(1, 1), (8, 100), (40, 1000), (64, 4096)])
