@@ -1,0 +1,59 @@
+// Host build of the precision forms' pair arithmetic: ddd.jl_gb300/csrc/
+// pair_df.cuh compiled as plain C++ (df64.cuh falls back to std:: functions),
+// so that the df64 and f32c general-branch formulas can be checked against the
+// FP64 oracle on a CPU.  Test infrastructure only; the product runs these
+// formulas on the GPU.  Build with -ffp-contract=off: the double-float
+// error-free transforms need every FP32 operation rounded on its own.
+//
+// Inputs per segment, 13 doubles, as the GPU's FP64 segment structure holds
+// them: n1 xyz, n2 xyz, b xyz, t xyz (unit direction), tN = 1/|n2 - n1|.
+// The GPU splits each into a (hi, lo) float pair; so does this file.
+#include <cstdint>
+
+#include "pair_df.cuh"
+
+using namespace ddd;
+
+namespace {
+
+DV3 dv3(const double* v) { return {df_from_double(v[0]), df_from_double(v[1]), df_from_double(v[2])}; }
+
+void store(const DV3& f, double* out) {
+  out[0] = df_to_double(f.x);
+  out[1] = df_to_double(f.y);
+  out[2] = df_to_double(f.z);
+}
+
+}  // namespace
+
+// k: aSq, mu4pi, mu8pi, mu4pinu (FP64, as ddd_consts).  form 0: df64 (every
+// general-pair operation in double-float); form 1: f32c (corner terms in
+// double-float, V-vector assembly in FP32).  For pair q (segments p[2q],
+// p[2q+1], 0-based rows of segs), out[12q ..] = F1, F2 (nodes of the first
+// segment), F3, F4 (nodes of the second).
+extern "C" void df_pair_forces(int form, const double* k, const double* segs, const int64_t* p, int64_t nPairs,
+                               double* out) {
+  const double aSq = k[0], mu4pi = k[1], mu8pi = k[2], mu4pinu = k[3];
+  const double mu8piaSq = aSq * mu8pi, mu4pinuaSq = aSq * mu4pinu;
+  const KConstsDF K{df_from_double(aSq), df_from_double(mu4pi), df_from_double(mu4pinu), df_from_double(mu8piaSq),
+                    df_from_double(mu4pinuaSq)};
+  const KConstsF KF{(float)mu4pi, (float)mu4pinu, (float)mu8piaSq, (float)mu4pinuaSq};
+  for (int64_t q = 0; q < nPairs; ++q) {
+    const double* a = segs + 13 * p[2 * q];
+    const double* b = segs + 13 * p[2 * q + 1];
+    const DV3 n11 = dv3(a), n12 = dv3(a + 3), b1 = dv3(a + 6), t1 = dv3(a + 9);
+    const DV3 n21 = dv3(b), n22 = dv3(b + 3), b2 = dv3(b + 6), t2 = dv3(b + 9);
+    const df64 t1N = df_from_double(a[12]), t2N = df_from_double(b[12]);
+    const df64 c = dot(t1, t2);
+    DV3 F1, F2, F3, F4;
+    if (form == 0)
+      general_pair_df<true, true>(K, b1, n11, n12, t1, t1N, b2, n21, n22, t2, t2N, c, F1, F2, F3, F4);
+    else
+      general_pair_mixed<true, true, true>(K, KF, f3(b1), n11, n12, t1, t1N.hi, f3(b2), n21, n22, t2, t2N.hi, c, F1,
+                                           F2, F3, F4);
+    store(F1, out + 12 * q);
+    store(F2, out + 12 * q + 3);
+    store(F3, out + 12 * q + 6);
+    store(F4, out + 12 * q + 9);
+  }
+}
