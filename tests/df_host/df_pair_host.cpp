@@ -57,3 +57,28 @@ extern "C" void df_pair_forces(int form, const double* k, const double* segs, co
     store(F4, out + 12 * q + 9);
   }
 }
+
+// The mixed σ̃ form (sigma_point_mixed): k5 = aSq, mu4pi, mu8pi, mu4pinu,
+// nuMu4pinu.  Each point's six components (xx, yy, zz, xy, xz, yz) summed
+// over the segments in order in df64, as the GPU kernel does; out[6j ..].
+extern "C" void df_sigma_points(const double* k5, const double* segs, int64_t nSeg, const double* x, int64_t M,
+                                double* out) {
+  KConstsSig K;
+  K.aSq = df_from_double(k5[0]);
+  K.mu4pi = (float)k5[1];
+  K.mu4pinu = (float)k5[3];
+  K.nuMu4pinu = (float)k5[4];
+  K.aSq32 = (float)k5[0];
+  K.aSqMu8pi = (float)(k5[0] * k5[2]);
+  for (int64_t j = 0; j < M; ++j) {
+    const DV3 xj = dv3(x + 3 * j);
+    df64 sig[6];
+    for (int c = 0; c < 6; ++c) sig[c] = df(0.0f);
+    for (int64_t s = 0; s < nSeg; ++s) {
+      const double* a = segs + 13 * s;
+      const F3 b = {(float)a[6], (float)a[7], (float)a[8]};
+      sigma_point_mixed(K, b, dv3(a), dv3(a + 3), dv3(a + 9), xj, sig);
+    }
+    for (int c = 0; c < 6; ++c) out[6 * j + c] = df_to_double(sig[c]);
+  }
+}

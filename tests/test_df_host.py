@@ -18,6 +18,9 @@ distances R ~ 50, 1,000 and 20,000 (lengths 20-200):
   median, and 2e-5 + 128x FP64's max;
 * plain FP32 (the oracle's FP32 restatement) is 13x worse than f32c near and
   1e4 to 1e7 times worse beyond. The compensated terms carry the accuracy.
+
+The mixed σ̃ form (sigma_point_mixed, same header) against the FP64 oracle
+per point: its error is flat in distance, ~1e-7.
 """
 import ctypes
 import os
@@ -48,6 +51,8 @@ def dfhost(tmp_path_factory):
     dp, ip = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)
     lib.df_pair_forces.argtypes = [ctypes.c_int, dp, dp, ip, ctypes.c_int64, dp]
     lib.df_pair_forces.restype = None
+    lib.df_sigma_points.argtypes = [dp, dp, ctypes.c_int64, dp, ctypes.c_int64, dp]
+    lib.df_sigma_points.restype = None
 
     def forces(form, n1, n2, b):
         """Forces (m × 4 × 3) of the pairs (segment 2q, segment 2q+1)."""
@@ -61,6 +66,18 @@ def dfhost(tmp_path_factory):
                            out_.ctypes.data_as(dp))
         return out_.reshape(m, 4, 3)
 
+    def sigma(n1, n2, b, x):
+        """Mixed-form σ̃ (6 × M) of one segment at the points x (M × 3)."""
+        t = n2 - n1
+        tN = 1.0 / np.sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2])
+        segs = np.ascontiguousarray(np.r_[n1, n2, b, t * tN, tN][None, :])
+        xs = np.ascontiguousarray(x)
+        out_ = np.zeros(6 * len(x))
+        lib.df_sigma_points(K5.ctypes.data_as(dp), segs.ctypes.data_as(dp), 1, xs.ctypes.data_as(dp), len(x),
+                            out_.ctypes.data_as(dp))
+        return out_.reshape(-1, 6).T
+
+    forces.sigma = sigma
     return forces
 
 
@@ -119,3 +136,28 @@ def test_precision_forms_vs_long_double(pkg, dfhost, oracle, dist, seed, f32_fac
     assert med(e_c) <= 1e-6 + 128 * med(e64), (med(e_c), med(e64))
     assert e_c.max() <= 2e-5 + 128 * e64.max(), (e_c.max(), e64.max())
     assert med(e_32) >= f32_factor * med(e_c), (med(e_32), med(e_c))
+
+
+@pytest.mark.parametrize("dist", [50.0, 1000.0, 20000.0])
+def test_mixed_sigma_per_point(pkg, dfhost, oracle, dist):
+    """The mixed σ̃ form (endpoint terms and their differences in df64,
+    assembly in FP32) against the FP64 oracle, per point relative to the
+    point's largest component: flat in distance (measured median 1.2e-7, max
+    5.9e-7 at R/L from 0.5 to 200), where the endpoint terms cancel as
+    (L/R)^2."""
+    rng = np.random.default_rng(int(dist))
+    errs = []
+    for _ in range(30):
+        n1 = rng.normal(size=3) * 100
+        d = rng.normal(size=3)
+        n2 = n1 + d / np.linalg.norm(d) * rng.uniform(20, 200)
+        b = rng.normal(size=3)
+        b /= np.linalg.norm(b)
+        x = n1 + rng.normal(size=(20, 3)) / np.sqrt(3) * dist
+        net = pkg.DislocationNetwork(np.asfortranarray(np.c_[n1, n2]), np.asfortranarray(b[:, None]),
+                                     np.array([[1, 1, 2]], np.int64))
+        ref = oracle.sigma_tilde(K5, np.asfortranarray(x.T), net)
+        S = dfhost.sigma(n1, n2, b, x)
+        errs.append(np.abs(S - ref).max(axis=0) / np.abs(ref).max(axis=0))
+    e = np.concatenate(errs)
+    assert np.median(e) <= 5e-7 and e.max() <= 5e-6, (np.median(e), e.max())
