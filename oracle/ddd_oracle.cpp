@@ -78,6 +78,51 @@ void oracle_segseg_pair(const double* k5, const double* b1, const double* n11, c
   }
 }
 
+// One pair by Gauss quadrature of the σ̃ field (not a reference function: the
+// restatement of a far-field form planned for the GPU, kept as its checker).
+// Segment 1's nodal forces are the integrals over s in [0, 1] of
+// N_k(s) (σ̃_2(x(s)) b1) × (n12 - n11), N_1 = 1 - s, N_2 = s, x(s) = n11 +
+// s (n12 - n11), where σ̃_2 is segment 2's non-singular stress (the reference's
+// formula, DislocationFEM.jl:86-303) and (σ b) × (n2 - n1) the force per unit
+// parameter (DislocationForces.jl:292-300).  nq-point Gauss-Legendre rule on
+// [0, 1], nq = 1..4.  Segment 2's nodal forces the same way with the roles
+// exchanged.  F[12] as oracle_segseg_pair.
+void oracle_segseg_pair_quad(const double* k5, const double* b1, const double* n11, const double* n12,
+                             const double* b2, const double* n21, const double* n22, int nq, double* F) {
+  static const double X[4][4] = {{0.0}, {-0.5773502691896257, 0.5773502691896257},
+                                 {-0.7745966692414834, 0.0, 0.7745966692414834},
+                                 {-0.8611363115940526, -0.3399810435848563, 0.3399810435848563, 0.8611363115940526}};
+  static const double W[4][4] = {{2.0}, {1.0, 1.0}, {0.5555555555555556, 0.8888888888888888, 0.5555555555555556},
+                                 {0.3478548451374538, 0.6521451548625461, 0.6521451548625461, 0.3478548451374538}};
+  for (int k = 0; k < 12; ++k) F[k] = 0.0;
+  if (nq < 1 || nq > 4) return;
+  const Consts<double> K = make_consts(k5);
+  const V3<double> B[2] = {{b1[0], b1[1], b1[2]}, {b2[0], b2[1], b2[2]}};
+  const V3<double> A[2] = {{n11[0], n11[1], n11[2]}, {n21[0], n21[1], n21[2]}};
+  const V3<double> E[2] = {{n12[0], n12[1], n12[2]}, {n22[0], n22[1], n22[2]}};
+  for (int side = 0; side < 2; ++side) {
+    const int o = 1 - side;  // the segment whose field acts
+    const V3<double> to = normalize(E[o] - A[o]);
+    const V3<double> l = E[side] - A[side];
+    V3<double> Fa = {0, 0, 0}, Fb = {0, 0, 0};
+    for (int q = 0; q < nq; ++q) {
+      const double sq = 0.5 * (1.0 + X[nq - 1][q]), wq = 0.5 * W[nq - 1][q];
+      const V3<double> x = A[side] + sq * l;
+      double sig[6] = {0, 0, 0, 0, 0, 0};
+      sigma_tilde_point<double>(K, B[o], A[o], E[o], to, x, sig);
+      const V3<double> f = pk_force<double>(sig, B[side], l);
+      Fa = Fa + (wq * (1.0 - sq)) * f;
+      Fb = Fb + (wq * sq) * f;
+    }
+    const V3<double> out[2] = {Fa, Fb};
+    for (int k = 0; k < 2; ++k) {
+      F[6 * side + 3 * k + 0] = out[k].x;
+      F[6 * side + 3 * k + 1] = out[k].y;
+      F[6 * side + 3 * k + 2] = out[k].z;
+    }
+  }
+}
+
 // Same pair in single precision (for the reduced-precision error studies).
 void oracle_segseg_pair_f32(const double* k5, const double* b1, const double* n11, const double* n12,
                             const double* b2, const double* n21, const double* n22, double* F) {

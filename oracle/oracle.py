@@ -42,6 +42,7 @@ def lib():
         L = ctypes.CDLL(LIB_PATH)
         L.oracle_segseg_pair.argtypes = [_dp] * 8
         L.oracle_segseg_pair_f32.argtypes = [_dp] * 8
+        L.oracle_segseg_pair_quad.argtypes = [_dp] * 7 + [ctypes.c_int, _dp]
         L.oracle_segseg_ser.argtypes = [_dp, _dp, _dp, _ip, ctypes.c_int64, _up, ctypes.c_int64, _dp]
         L.oracle_segseg_par_atomic.argtypes = [_dp, _dp, _dp, _ip, ctypes.c_int64, _up, ctypes.c_int64, _dp,
                                                ctypes.c_int]
@@ -107,6 +108,15 @@ def pair(k5, b1, n11, n12, b2, n21, n22, f32=False):
     F = np.zeros(12)
     fn = lib().oracle_segseg_pair_f32 if f32 else lib().oracle_segseg_pair
     fn(*[_d(a) for a in args], _d(F))
+    return F.reshape(4, 3)
+
+
+def pair_quad(k5, b1, n11, n12, b2, n21, n22, nq):
+    """Fnode1..4 (4×3) of one pair by nq-point Gauss quadrature of the σ̃ field
+    (the checker of a planned far-field form; not a reference function)."""
+    args = [np.ascontiguousarray(v, np.float64) for v in (k5, b1, n11, n12, b2, n21, n22)]
+    F = np.zeros(12)
+    lib().oracle_segseg_pair_quad(*[_d(a) for a in args], int(nq), _d(F))
     return F.reshape(4, 3)
 
 
