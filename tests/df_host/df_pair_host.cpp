@@ -82,3 +82,51 @@ extern "C" void df_sigma_points(const double* k5, const double* segs, int64_t nS
     for (int c = 0; c < 6; ++c) out[6 * j + c] = df_to_double(sig[c]);
   }
 }
+
+// The planned far-field form on the mixed arithmetic: a pair's nodal forces by
+// nq-point Gauss quadrature (nq = 2 or 3) of the partner's mixed-form σ̃, the
+// force per unit parameter (σ b) × l and the node sums in FP32 (l = n2 - n1).
+// Same statement as oracle_segseg_pair_quad, in the arithmetic a GPU kernel of
+// that form would use.  k5 and segs as df_sigma_points; pairs as
+// df_pair_forces.
+extern "C" void df_pair_quad_forces(const double* k5, const double* segs, const int64_t* p, int64_t nPairs, int nq,
+                                    double* out) {
+  static const float X[2][3] = {{0.21132486540518713f, 0.78867513459481287f, 0.0f},
+                                {0.11270166537925831f, 0.5f, 0.88729833462074169f}};
+  static const float W[2][3] = {{0.5f, 0.5f, 0.0f}, {0.27777777777777778f, 0.44444444444444444f, 0.27777777777777778f}};
+  KConstsSig K;
+  K.aSq = df_from_double(k5[0]);
+  K.mu4pi = (float)k5[1];
+  K.mu4pinu = (float)k5[3];
+  K.nuMu4pinu = (float)k5[4];
+  K.aSq32 = (float)k5[0];
+  K.aSqMu8pi = (float)(k5[0] * k5[2]);
+  const int r = nq == 3 ? 1 : 0;
+  for (int64_t q = 0; q < nPairs; ++q) {
+    const double* S[2] = {segs + 13 * p[2 * q], segs + 13 * p[2 * q + 1]};
+    for (int side = 0; side < 2; ++side) {
+      const double* me = S[side];
+      const double* ot = S[1 - side];
+      const DV3 n1 = dv3(me), l = dv3(me + 3) - dv3(me);
+      const F3 bm = {(float)me[6], (float)me[7], (float)me[8]};
+      const F3 lf = f3(l);
+      const F3 bo = {(float)ot[6], (float)ot[7], (float)ot[8]};
+      F3 Fa = {0.f, 0.f, 0.f}, Fb = {0.f, 0.f, 0.f};
+      for (int g = 0; g < (r ? 3 : 2); ++g) {
+        const DV3 x = n1 + df(X[r][g]) * l;
+        df64 sig[6];
+        for (int c = 0; c < 6; ++c) sig[c] = df(0.0f);
+        sigma_point_mixed(K, bo, dv3(ot), dv3(ot + 3), dv3(ot + 9), x, sig);
+        float s6[6];
+        for (int c = 0; c < 6; ++c) s6[c] = sig[c].hi + sig[c].lo;
+        const F3 sb = {s6[0] * bm.x + s6[3] * bm.y + s6[4] * bm.z, s6[3] * bm.x + s6[1] * bm.y + s6[5] * bm.z,
+                       s6[4] * bm.x + s6[5] * bm.y + s6[2] * bm.z};
+        const F3 f = cross(sb, lf);
+        Fa = Fa + (W[r][g] * (1.0f - X[r][g])) * f;
+        Fb = Fb + (W[r][g] * X[r][g]) * f;
+      }
+      double* o = out + 12 * q + 6 * side;
+      o[0] = Fa.x, o[1] = Fa.y, o[2] = Fa.z, o[3] = Fb.x, o[4] = Fb.y, o[5] = Fb.z;
+    }
+  }
+}
