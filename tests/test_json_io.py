@@ -117,3 +117,4 @@ def test_loaded_network_forces(pkg, fixtures, tmp_path):
     pkg.saveJSON(path, net)
     back = pkg.loadNetwork(path)
     assert np.array_equal(pkg.calcSegSegForce(dln, mat, back), pkg.calcSegSegForce(dln, mat, net))
+
