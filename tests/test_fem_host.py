@@ -1,6 +1,6 @@
-"""The product's mesh geometry for calc_uTilde (ddd.jl_gb300/fem.py) on a
-CPU, against the oracle's independent restatement of the reference's mesh
-and boundary constructors (oracle/fixtures.py)."""
+"""Host-side structures of the product on a CPU, against the oracle's
+independent restatements (oracle/fixtures.py): the mesh geometry calc_uTilde
+reads (ddd.jl_gb300/fem.py) and a network's node connectivity."""
 import numpy as np
 import pytest
 
@@ -22,3 +22,19 @@ def test_fem_mesh_matches_oracle_restatement(pkg, fixtures, dims):
     nodes, dofs = fixtures.cantilever_u_gamma(*dims[3:])
     bnd = pkg.fem.cantilever_boundaries(mesh)
     assert np.array_equal(bnd.uGammaDln, nodes) and np.array_equal(bnd.uDofsDln, dofs)
+
+
+def test_network_connectivity_matches_oracle_restatement(pkg, synth, fixtures):
+    """The product's default connectivity (what mobility and collision read),
+    built from the links, against the oracle's restatement of _makeConnect!
+    (DislocationUtil.jl:213-237), including nodes with three or four links."""
+    p, b = synth.square_loops(30, 8, 20.0, 200.0, 2000.0, 0.5, 0.1)
+    coord, bvec, seg = synth.network_arrays(p, b)
+    # Join a few loops at shared nodes: node 1 gains links from 9 and 17.
+    seg = seg.copy()
+    seg[8, 1] = 1
+    seg[16, 1] = 1
+    net = pkg.DislocationNetwork(coord, bvec, seg, maxConnect=4)
+    ref = fixtures.make_connectivity(net.links, 4)
+    assert np.array_equal(net.connectivity[:, :ref.shape[1]], ref)
+    assert net.connectivity[0, 0] == 4
