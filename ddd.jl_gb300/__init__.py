@@ -250,20 +250,35 @@ class MaterialParameters:
 
 
 class DislocationParameters:
-    """The DislocationParameters fields this path reads (src/Type/DislocationConstructor.jl:55-105)."""
+    """The DislocationParameters fields this path reads (src/Type/DislocationConstructor.jl:55-105).
+
+    Like the reference's constructor (:75-78) it asserts coreRad < minSegLen <
+    maxSegLen unless all three are 0, and minArea < maxArea unless both are 0
+    (AssertionError, as Julia's @assert raises)."""
 
     def __init__(self, *, coreRad=1.0, coreRadMag=1.0, coreEnergy=None, minSegLen=None, maxSegLen=None,
-                 collisionDist=None, parCPU=False, parGPU=True, dragCoeffs=None, **other):
+                 minArea=None, maxArea=None, collisionDist=None, parCPU=False, parGPU=True, dragCoeffs=None,
+                 **other):
         self.dragCoeffs = dict(edge=1.0, screw=2.0, climb=1e9, line=0.0)
         if dragCoeffs:
             self.dragCoeffs.update({k: float(v) for k, v in dict(dragCoeffs).items()})
         self.coreRad = float(coreRad)
         self.coreRadSq = self.coreRad * self.coreRad
-        self.coreEnergy = (1 / (4 * math.pi) * math.log(self.coreRad / 0.1) if coreEnergy is None
-                           else float(coreEnergy))
+        # Julia's log(0.0) is -Inf where Python's math.log raises.
+        self.coreEnergy = ((1 / (4 * math.pi) * math.log(self.coreRad / 0.1) if self.coreRad > 0 else -math.inf)
+                           if coreEnergy is None else float(coreEnergy))
         self.coreRadMag = float(coreRadMag)
         self.minSegLen = 2 * self.coreRad if minSegLen is None else float(minSegLen)
         self.maxSegLen = 20 * self.coreRad if maxSegLen is None else float(maxSegLen)
+        self.minArea = self.minSegLen ** 2 / math.sqrt(2) if minArea is None else float(minArea)
+        self.maxArea = 100 * self.minArea if maxArea is None else float(maxArea)
+        if not (self.coreRad == self.minSegLen == self.maxSegLen == 0):
+            assert self.coreRad < self.minSegLen < self.maxSegLen, \
+                "coreRad < minSegLen < maxSegLen does not hold (%g, %g, %g)" % (self.coreRad, self.minSegLen,
+                                                                                 self.maxSegLen)
+        if not (self.minArea == self.maxArea == 0):
+            assert self.minArea < self.maxArea, "minArea < maxArea does not hold (%g, %g)" % (self.minArea,
+                                                                                            self.maxArea)
         self.collisionDist = self.minSegLen / 2 if collisionDist is None else float(collisionDist)
         self.collisionDistSq = self.collisionDist * self.collisionDist
         self.parCPU = bool(parCPU)

@@ -290,4 +290,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python extract_goldens.py <DDD.jl checkout>")
+    main(sys.argv[1])

@@ -94,6 +94,20 @@ def test_python_mirror_argument_checks(pkg):
         pkg.calc_σTilde_inplace(np.zeros((6, 3)), np.zeros((3, 4)), None, None, None)
 
 
+def test_dislocation_parameters_assertions(pkg):
+    """DislocationConstructor.jl:75-78: coreRad < minSegLen < maxSegLen unless
+    all three are 0; minArea < maxArea unless both are 0."""
+    d = pkg.DislocationParameters(coreRad=2.0)  # defaults 4 and 40: accepted
+    assert (d.minSegLen, d.maxSegLen) == (4.0, 40.0)
+    assert d.minArea == 16.0 / np.sqrt(2) and d.maxArea == 100 * d.minArea
+    pkg.DislocationParameters(coreRad=0.0, minSegLen=0.0, maxSegLen=0.0, minArea=0.0, maxArea=0.0)
+    for kw in (dict(coreRad=5.0, minSegLen=5.0), dict(coreRad=1.0, minSegLen=10.0, maxSegLen=9.0),
+               dict(coreRad=1.0, minSegLen=2.0, maxSegLen=2.0), dict(coreRad=0.0, minSegLen=0.0, maxSegLen=1.0),
+               dict(coreRad=1.0, minArea=5.0, maxArea=5.0), dict(coreRad=1.0, minArea=0.0, maxArea=-1.0)):
+        with pytest.raises(AssertionError):
+            pkg.DislocationParameters(**kw)
+
+
 def test_product_iterator_points(pkg):
     """Iterators.product(xs, ys, zs) enumerates the first factor fastest; the
     mirror's ProductIterator gives calc_σTilde the points in that order, and
