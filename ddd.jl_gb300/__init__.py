@@ -38,6 +38,7 @@ EXPORTED_SYMBOLS = (
     "ddd_detect_collision", "ddd_minimum_distance", "ddd_u_tilde",
     "ddd_segseg_force", "ddd_segseg_force_inplace", "ddd_sigma_tilde",
     "ddd_segseg_force_device", "ddd_sigma_tilde_device", "ddd_set_mode", "ddd_get_mode", "ddd_probe_fma_peak",
+    "ddd_selftest_bounded_wait",
     "ddd_set_partial_limit", "ddd_get_partial_limit",
     "ddd_segseg_force_device_noalloc",
     "ddd_batch_create", "ddd_batch_run", "ddd_batch_info", "ddd_batch_last_error", "ddd_batch_destroy",
@@ -221,6 +222,7 @@ def library():
         L.ddd_get_partial_limit.argtypes = [_vp]
         L.ddd_get_partial_limit.restype = ctypes.c_int64
         L.ddd_probe_fma_peak.argtypes = [_vp, ctypes.c_int, _dp]
+        L.ddd_selftest_bounded_wait.argtypes = [_vp, ctypes.c_longlong, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -686,6 +688,15 @@ class Context:
         v = ctypes.c_double(0)
         self._check(self._L.ddd_probe_fma_peak(self._h, int(precision), ctypes.byref(v)))
         return v.value
+
+    @property
+    def last_error(self):
+        """ddd_last_error: the message of this context's last failed call."""
+        return self._L.ddd_last_error(self._h).decode()
+
+    def selftest_bounded_wait(self, max_clocks, arrive):
+        """ddd_selftest_bounded_wait: the return code (DDD_OK or DDD_ETIMEOUT), not raised."""
+        return self._L.ddd_selftest_bounded_wait(self._h, int(max_clocks), 1 if arrive else 0)
 
 
 class Batch:

@@ -83,7 +83,7 @@ def build(verbose=False, ptxas_info=False):
     logs = "".join(l for _, l in results)
     if _stale(LIB, objs):
         tmp = LIB + ".tmp"
-        cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs
+        cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-ldl"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))

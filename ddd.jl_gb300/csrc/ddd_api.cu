@@ -356,6 +356,7 @@ double ddd_last_kernel_ms(const ddd_ctx* c) { return c ? c->lastKernelMs : 0.0; 
 int ddd_segseg_force(ddd_ctx* ctx, const ddd_consts* k, const double* coord, int64_t coordCols, const double* bVec,
                      int64_t bVecCols, const int64_t* segIdx, int64_t ldSegIdx, const uint8_t* extSeg,
                      int64_t numSeg, const int64_t* idx, int64_t nIdx, double* force, ddd_report* rep) {
+  DDD_NVTX("ddd_segseg_force");
   if (!ctx) return DDD_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
   const int64_t nOut = idx ? nIdx : numSeg;
@@ -474,6 +475,7 @@ extern "C" {
 int ddd_self_force(ddd_ctx* ctx, const ddd_consts* k, const ddd_self_params* sp, const double* coord,
                    int64_t coordCols, const double* bVec, int64_t bVecCols, const int64_t* segIdx, int64_t ldSegIdx,
                    const uint8_t* extSeg, int64_t numSeg, const int64_t* idx, int64_t nIdx, double* F1, double* F2) {
+  DDD_NVTX("ddd_self_force");
   if (!ctx) return DDD_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
   const int64_t n = idx ? nIdx : numSeg;
@@ -493,6 +495,7 @@ int ddd_self_force_inplace(ddd_ctx* ctx, const ddd_consts* k, const ddd_self_par
                            int64_t coordCols, const double* bVec, int64_t bVecCols, const int64_t* segIdx,
                            int64_t ldSegIdx, const uint8_t* extSeg, int64_t numSeg, const int64_t* idx, int64_t nIdx,
                            double* segForce, int64_t segForceCols) {
+  DDD_NVTX("ddd_self_force_inplace");
   if (!ctx) return DDD_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
   if (segForceCols < numSeg) return fail(ctx, DDD_EINVAL, "segForce has fewer columns than numSeg");
@@ -517,6 +520,7 @@ int ddd_seg_force(ddd_ctx* ctx, const ddd_consts* k, const ddd_self_params* sp, 
                   int64_t coordCols, const double* bVec, int64_t bVecCols, const int64_t* segIdx, int64_t ldSegIdx,
                   const uint8_t* extSeg, int64_t numSeg, const double* sigmaHat, const int64_t* idx, int64_t nIdx,
                   double* force, ddd_report* rep) {
+  DDD_NVTX("ddd_seg_force");
   if (!ctx) return DDD_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
   const int64_t n = idx ? nIdx : numSeg;
@@ -542,6 +546,7 @@ int ddd_seg_force_inplace(ddd_ctx* ctx, const ddd_consts* k, const ddd_self_para
                           int64_t coordCols, const double* bVec, int64_t bVecCols, const int64_t* segIdx,
                           int64_t ldSegIdx, const uint8_t* extSeg, int64_t numSeg, const double* sigmaHat,
                           const int64_t* idx, int64_t nIdx, double* segForce, int64_t segForceCols, ddd_report* rep) {
+  DDD_NVTX("ddd_seg_force_inplace");
   if (!ctx) return DDD_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
   if (segForceCols < numSeg) return fail(ctx, DDD_EINVAL, "segForce has fewer columns than numSeg");
@@ -681,6 +686,7 @@ int ddd_mobility_bcc(ddd_ctx* ctx, const ddd_mob_params* mp, const double* coord
                      const int64_t* connectivity, int64_t ldConn, int64_t connCols, const double* segForce,
                      int64_t segForceCols, int64_t numNode, const int64_t* idx, int64_t nIdx, double* nodeForce,
                      double* nodeVel) {
+  DDD_NVTX("ddd_mobility_bcc");
   if (!ctx) return DDD_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
   const int64_t n = idx ? nIdx : numNode;
@@ -698,6 +704,7 @@ int ddd_mobility_bcc_inplace(ddd_ctx* ctx, const ddd_mob_params* mp, const doubl
                              const int64_t* connectivity, int64_t ldConn, int64_t connCols, const double* segForce,
                              int64_t segForceCols, int64_t numNode, const int64_t* idx, int64_t nIdx,
                              double* nodeForce, double* nodeVel, int64_t nodeCols) {
+  DDD_NVTX("ddd_mobility_bcc_inplace");
   if (!ctx) return DDD_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
   const int64_t n = idx ? nIdx : numNode;
@@ -721,6 +728,7 @@ int ddd_segseg_force_inplace(ddd_ctx* ctx, const ddd_consts* k, const double* co
                              const double* bVec, int64_t bVecCols, const int64_t* segIdx, int64_t ldSegIdx,
                              const uint8_t* extSeg, int64_t numSeg, const int64_t* idx, int64_t nIdx,
                              double* segForce, int64_t segForceCols, ddd_report* rep) {
+  DDD_NVTX("ddd_segseg_force_inplace");
   if (!ctx) return DDD_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
   if (segForceCols < numSeg) return fail(ctx, DDD_EINVAL, "segForce has fewer columns than numSeg");
@@ -736,6 +744,7 @@ int ddd_sigma_tilde(ddd_ctx* ctx, const ddd_consts* k, const double* x0, int64_t
                     int64_t coordCols, const double* bVec, int64_t bVecCols, const int64_t* segIdx,
                     int64_t ldSegIdx, int64_t numSeg, const int64_t* idx, int64_t nIdx, double* sigma,
                     ddd_report* rep) {
+  DDD_NVTX("ddd_sigma_tilde");
   if (!ctx) return DDD_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
   ddd::KConsts K;
@@ -803,6 +812,7 @@ int ddd_sigma_tilde(ddd_ctx* ctx, const ddd_consts* k, const double* x0, int64_t
 
 int ddd_segseg_force_device(ddd_ctx* ctx, const ddd_consts* k, const double* segs, int64_t ldSegs,
                             const uint8_t* ext, int64_t numSeg, double* force, void* stream, ddd_report* rep) {
+  DDD_NVTX("ddd_segseg_force_device");
   if (!ctx) return DDD_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
   ddd::KConsts K;
@@ -844,6 +854,7 @@ int ddd_segseg_force_device(ddd_ctx* ctx, const ddd_consts* k, const double* seg
 int ddd_sigma_tilde_device(ddd_ctx* ctx, const ddd_consts* k, const double* x0, int64_t numPoints,
                            const double* segs, int64_t ldSegs, int64_t numSeg, double* sigma, void* stream,
                            ddd_report* rep) {
+  DDD_NVTX("ddd_sigma_tilde_device");
   if (!ctx) return DDD_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
   ddd::KConsts K;
@@ -902,6 +913,7 @@ int64_t ddd_get_partial_limit(const ddd_ctx* ctx) {
 
 int ddd_surrogate_make_data(ddd_ctx* ctx, const ddd_consts* k, const double* segs, int64_t n, const int32_t* pairs,
                             int64_t P, void* X, float* Bp, float* T, double* F) {
+  DDD_NVTX("ddd_surrogate_make_data");
   if (!ctx) return DDD_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
   ddd::KConsts K;
@@ -922,6 +934,7 @@ int ddd_surrogate_make_data(ddd_ctx* ctx, const ddd_consts* k, const double* seg
 }
 
 int ddd_tc_gemm_bf16(ddd_ctx* ctx, int M, int N, int K, const void* A, const void* B, float* D, void* stream) {
+  DDD_NVTX("ddd_tc_gemm_bf16");
   if (!ctx) return DDD_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
   if (M <= 0 || M % 128 || N < 16 || N > 256 || N % 16 || K <= 0 || K % 16)
@@ -940,7 +953,25 @@ int ddd_tc_gemm_bf16(ddd_ctx* ctx, int M, int N, int K, const void* A, const voi
   return DDD_OK;
 }
 
+int ddd_selftest_bounded_wait(ddd_ctx* ctx, long long max_clocks, int arrive) {
+  DDD_NVTX("ddd_selftest_bounded_wait");
+  if (!ctx) return DDD_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (max_clocks < 1 || max_clocks > 2000000000LL)
+    return fail(ctx, DDD_EINVAL, "max_clocks must be in [1, 2e9] (about a second at most)");
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  CK(ctx->errflag.ensure(sizeof(int)), "alloc error flag");
+  CK(cudaMemsetAsync(ctx->errflag.p, 0, sizeof(int), ctx->stream), "memset");
+  CK(ddd::launch_bounded_wait_probe(max_clocks, arrive, ctx->errflag.as<int>(), ctx->stream), "bounded_wait_probe");
+  int flag = 0;
+  CK(cudaMemcpyAsync(&flag, ctx->errflag.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "copy flag");
+  CK(cudaStreamSynchronize(ctx->stream), "bounded_wait_probe");
+  if (flag) return fail(ctx, DDD_ETIMEOUT, "bounded mbarrier wait timed out (self-test)");
+  return DDD_OK;
+}
+
 int ddd_probe_fma_peak(ddd_ctx* ctx, int precision, double* flops_per_s) {
+  DDD_NVTX("ddd_probe_fma_peak");
   if (!ctx || !flops_per_s) return DDD_EINVAL;
   if (precision != 64 && precision != 32) return fail(ctx, DDD_EINVAL, "precision must be 64 or 32");
   std::lock_guard<std::mutex> g(ctx->mu);
@@ -948,19 +979,28 @@ int ddd_probe_fma_peak(ddd_ctx* ctx, int precision, double* flops_per_s) {
   int sms = 0;
   CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device), "attr");
   const int threads = 256, blocks = sms * 8;
-  const int iters = precision == 64 ? 4096 : 65536;
   CK(ctx->probe.ensure((size_t)blocks * threads * sizeof(double)), "alloc probe");
+  auto run = [&](int iters, float* ms) -> cudaError_t {
+    cudaError_t e = cudaEventRecord(ctx->ev[0], ctx->stream);
+    if (e == cudaSuccess)
+      e = precision == 64 ? ddd::launch_fp64_peak_probe(ctx->probe.as<double>(), iters, blocks, threads, ctx->stream)
+                          : ddd::launch_fp32_peak_probe(ctx->probe.as<float>(), iters, blocks, threads, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->ev[1], ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e == cudaSuccess) *ms = elapsed(ctx->ev[0], ctx->ev[1]);
+    return e;
+  };
+  // Calibrate the chain length so one timed run lasts about a second.
+  int iters = precision == 64 ? 4096 : 65536;
+  float ms = 0.0f;
+  CK(run(iters, &ms), "probe");
+  CK(run(iters, &ms), "probe");
+  const double want = (double)iters * 1100.0 / (ms > 1e-3f ? ms : 1e-3f);
+  iters = (int)std::min(want, 1.0e9);
   float best = 1e30f;
-  for (int rep = 0; rep < 4; ++rep) {
-    CK(cudaEventRecord(ctx->ev[0], ctx->stream), "event");
-    if (precision == 64)
-      CK(ddd::launch_fp64_peak_probe(ctx->probe.as<double>(), iters, blocks, threads, ctx->stream), "probe");
-    else
-      CK(ddd::launch_fp32_peak_probe(ctx->probe.as<float>(), iters, blocks, threads, ctx->stream), "probe");
-    CK(cudaEventRecord(ctx->ev[1], ctx->stream), "event");
-    CK(cudaStreamSynchronize(ctx->stream), "probe");
-    float ms = elapsed(ctx->ev[0], ctx->ev[1]);
-    if (rep > 0 && ms < best) best = ms;
+  for (int rep = 0; rep < 3; ++rep) {
+    CK(run(iters, &ms), "probe");
+    if (ms < best) best = ms;
   }
   *flops_per_s = 2.0 * 8.0 * (double)iters * (double)threads * (double)blocks / (best * 1e-3);
   return DDD_OK;
@@ -975,6 +1015,7 @@ int ddd_detect_collision(ddd_ctx* ctx, double collisionDistSq, const double* coo
                          const int64_t* links, int64_t linkCols, const double* bVec, int64_t bVecCols,
                          const int64_t* connectivity, int64_t ldConn, int64_t connCols, int64_t numNode,
                          int64_t numSeg, const int64_t* skipSegs, int64_t nSkip, ddd_collision* out) {
+  DDD_NVTX("ddd_detect_collision");
   if (!ctx) return DDD_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
   if (!out) return fail(ctx, DDD_EINVAL, "out is NULL");
@@ -1079,6 +1120,7 @@ int ddd_detect_collision(ddd_ctx* ctx, double collisionDistSq, const double* coo
 }
 
 int ddd_minimum_distance(ddd_ctx* ctx, const double* pts, int64_t n, double* out) {
+  DDD_NVTX("ddd_minimum_distance");
   if (!ctx) return DDD_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
   if (n < 0) return fail(ctx, DDD_EINVAL, "negative size");
@@ -1099,6 +1141,7 @@ int ddd_u_tilde(ddd_ctx* ctx, double omNuInv8pi, double om2NuOmNuInv8pi, const d
                 const double* points, int64_t numPoints, const double* coord, int64_t coordCols, const int32_t* label,
                 int64_t labelLen, const int64_t* links, int64_t linkCols, const double* bVec, int64_t bVecCols,
                 int64_t numNode, int64_t numSeg, const int64_t* uDofs, double* uTilde, int64_t uLen) {
+  DDD_NVTX("ddd_u_tilde");
   if (!ctx) return DDD_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
   if (!mesh) return fail(ctx, DDD_EINVAL, "mesh is NULL");

@@ -1,6 +1,7 @@
 // Internal declarations shared by the kernel files and the C-ABI layer.
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <atomic>
 #include <cstddef>
@@ -10,6 +11,17 @@
 struct ddd_ctx;
 
 namespace ddd {
+
+// An NVTX range for the life of a C-ABI call: profilers (Nsight Systems, ncu's
+// NVTX filters) show each entry point's span on the host timeline.  NVTX is
+// header-only and costs a function-pointer check when no tool is attached.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+#define DDD_NVTX(name) ::ddd::NvtxRange ddd_nvtx_range_(name)
 
 struct KConsts;
 
@@ -59,7 +71,8 @@ cudaError_t set_smem_once(Kernel* kernel, int bytes, std::atomic<uint64_t>& done
   cudaError_t launch_reduce_all(const double* partial, int64_t npad, int64_t numSeg, double* out, cudaStream_t st); \
   cudaError_t launch_reduce_band(const double* partial, int64_t J0, int64_t J1, int64_t numSeg, double* out, \
                                  cudaStream_t st); \
-  cudaError_t launch_reduce_rows(const double* partial, int64_t npad, int64_t nRows, double* out, cudaStream_t st);
+  cudaError_t launch_reduce_rows(const double* partial, int64_t npad, int64_t nRows, double* out, cudaStream_t st); \
+  cudaError_t preload_all_f64();
 
 namespace strict {
 DDD_F64_DECLS
@@ -89,6 +102,9 @@ cudaError_t launch_tc_gemm_bf16(int M, int N, int K, const void* A, const void* 
                                 cudaStream_t st);
 cudaError_t launch_tc_gemm_f16(int M, int N, int K, const void* A, const void* B, float* D, int* err,
                                cudaStream_t st);
+// One warp waiting (bounded by max_clocks) on an mbarrier that receives its
+// arrival only when `arrive` != 0; *err = 1 when the wait ran out.
+cudaError_t launch_bounded_wait_probe(long long max_clocks, int arrive, int* err, cudaStream_t st);
 
 // surrogate_data.cu: features and exact scaled targets of a pair list.
 cudaError_t launch_pair_data(const KConsts& K, const double* soa, int64_t npad, const int32_t* pairs, int64_t P,

@@ -355,6 +355,7 @@ int fail(ddd_batch* b, int code, const std::string& m) {
 extern "C" {
 
 ddd_batch* ddd_batch_create(ddd_ctx* ctx, int64_t nNet, const int64_t* numSeg, int mode, int tune) {
+  DDD_NVTX("ddd_batch_create");
   if (!ctx || nNet < 0 || (nNet > 0 && !numSeg)) return nullptr;
   if (mode != DDD_MODE_FP64 && mode != DDD_MODE_DF64 && mode != DDD_MODE_F32C) return nullptr;
   ddd_batch* b = new ddd_batch();
@@ -404,6 +405,7 @@ const char* ddd_batch_last_error(const ddd_batch* b) { return b ? b->err.c_str()
 
 int ddd_batch_run(ddd_batch* b, const ddd_consts* k, const double* segs, const uint8_t* ext, double* force,
                   void* stream) {
+  DDD_NVTX("ddd_batch_run");
   if (!b || !k) return DDD_EINVAL;
   if (b->totalSeg > 0 && (!segs || !force)) return fail(b, DDD_EINVAL, "segs or force is NULL");
   if (!(k->aSq > 0.0)) return fail(b, DDD_EINVAL, "aSq must be > 0");

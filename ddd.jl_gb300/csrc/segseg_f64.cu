@@ -248,6 +248,18 @@ static cudaError_t set_attr() {
   return set_smem_once(segseg_tile_f64<MODE>, (int)sizeof(TileSmemT<TILE, PolF64>), done);
 }
 
+// Loads the all-pairs kernels on the current device (under lazy module loading
+// the driver loads a kernel, and reserves its memory, at first use) and sets
+// the tile kernel's shared-memory attribute, without launching anything.
+cudaError_t preload_all_f64() {
+  cudaError_t e = set_attr<0>();
+  cudaFuncAttributes fa;
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, prep_segments_packed);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, segseg_reduce_all);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, segseg_reduce_band);
+  return e;
+}
+
 cudaError_t launch_reduce_all(const double* partial, int64_t npad, int64_t numSeg, double* out, cudaStream_t st) {
   segseg_reduce_all<<<(unsigned)((numSeg + 127) / 128), 128, 0, st>>>(partial, npad / TILE, numSeg, out);
   return cudaGetLastError();

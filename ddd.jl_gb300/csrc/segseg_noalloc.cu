@@ -12,8 +12,17 @@
 //
 // Limits and sharing:
 //   * at most DDD_NOALLOC_MAX_SEGMENTS segments (larger sizes are rejected);
-//   * the scratch array (about 6.9 MB) exists on every GPU that loads this
-//     library, for the life of the process;
+//   * the scratch array (about 6.9 MB) is device memory that the CUDA driver
+//     reserves when it loads this file's module on a device, and the force
+//     kernels' code is loaded the same way.  Under CUDA's default lazy module
+//     loading that happens inside the first call on that device (the
+//     cudaGetSymbolAddress and kernel look-ups below), not when the library
+//     loads; with CUDA_MODULE_LOADING=EAGER it happens when the device's
+//     context is created.  The memory stays reserved until the process exits.
+//     A caller whose pool reserves the GPU should therefore make one call on
+//     each device during set-up, before the pool reserves its memory: a call
+//     with numSeg = 0 does only that set-up (module loads, kernel attribute,
+//     address lookup) and launches nothing;
 //   * every call shares the array and it keeps the last call's contents; every
 //     scratch element this call reads is written earlier in the same call, so
 //     nothing needs clearing, and calls that overlap on the GPU (two streams,
@@ -23,6 +32,7 @@
 //     capture that contains later calls.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <mutex>
 
 #include "../../include/ddd_gb300.h"
@@ -48,7 +58,7 @@ void* g_scratch_ptr[kMaxDevices] = {};
 std::mutex g_mu;
 
 // Device address of g_scratch on the current device (looked up once per device,
-// with that device current).
+// with that device current), the force kernels loaded there.
 int scratch_for_current_device(unsigned char** out) {
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return DDD_EDEVICE;
@@ -57,6 +67,7 @@ int scratch_for_current_device(unsigned char** out) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
     if (e != cudaSuccess || !p) return DDD_EDEVICE;
+    if (ddd::strict::preload_all_f64() != cudaSuccess) return DDD_EDEVICE;
     g_scratch_ptr[dev] = p;
   }
   *out = static_cast<unsigned char*>(g_scratch_ptr[dev]);
@@ -72,8 +83,15 @@ int ddd_segseg_force_device_noalloc(const ddd_consts* k, const double* segs, int
   if (!k || numSeg < 0 || ldSegs < numSeg) return DDD_EINVAL;
   if (numSeg > kMaxSeg) return DDD_ETOOBIG;
   if (numSeg > 0 && (!segs || !force)) return DDD_EINVAL;
-  if (numSeg == 0) return DDD_OK;
+  const double v[5] = {k->aSq, k->mu4pi, k->mu8pi, k->mu4pinu, k->nuMu4pinu};
+  for (double x : v)
+    if (!std::isfinite(x)) return DDD_ENONFINITE;
   if (!(k->aSq > 0.0)) return DDD_EINVAL;
+  // Per-device set-up first, so that a numSeg = 0 call loads the scratch.
+  unsigned char* base = nullptr;
+  int rc = scratch_for_current_device(&base);
+  if (rc) return rc;
+  if (numSeg == 0) return DDD_OK;
   ddd::KConsts K;
   K.aSq = k->aSq;
   K.mu4pi = k->mu4pi;
@@ -83,9 +101,6 @@ int ddd_segseg_force_device_noalloc(const ddd_consts* k, const double* segs, int
   K.mu8piaSq = k->aSq * k->mu8pi;
   K.mu4pinuaSq = k->aSq * k->mu4pinu;
 
-  unsigned char* base = nullptr;
-  int rc = scratch_for_current_device(&base);
-  if (rc) return rc;
   double* soa = reinterpret_cast<double*>(base);
   uint8_t* skip = base + kSoaBytes;
   double* partial = reinterpret_cast<double*>(base + kSoaBytes + kSkipBytes);

@@ -525,6 +525,7 @@ const char* ddd_surrogate_last_error(const ddd_surrogate* s) { return s ? s->las
 int ddd_surrogate_force(ddd_surrogate* s, const ddd_consts* k, const double* segs, int64_t ldSegs,
                         const uint8_t* ext, int64_t numSeg, double* force, void* stream, const ddd_sur_opts* opts,
                         ddd_sur_report* rep) {
+  DDD_NVTX("ddd_surrogate_force");
   if (!s) return DDD_EINVAL;
   ddd_sur_opts o{20.0, 0.01, 1e-3, DDD_MODE_FP64};
   if (opts) o = *opts;
@@ -686,6 +687,7 @@ int ddd_surrogate_force_host(ddd_surrogate* s, const ddd_consts* k, const double
                              const double* bVec, int64_t bVecCols, const int64_t* segIdx, int64_t ldSegIdx,
                              const uint8_t* extSeg, int64_t numSeg, double* force, const ddd_sur_opts* opts,
                              ddd_sur_report* rep) {
+  DDD_NVTX("ddd_surrogate_force_host");
   if (!s) return DDD_EINVAL;
   if (numSeg < 0 || coordCols < 0 || bVecCols < 0 || ldSegIdx < numSeg)
     return sfail(s, DDD_EINVAL, "negative size or numSeg exceeds the rows of segIdx");

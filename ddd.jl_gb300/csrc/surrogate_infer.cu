@@ -241,6 +241,7 @@ mlp_far_tiles(const float* __restrict__ ms, int64_t npad, const int4* __restrict
   const uint32_t tm_row = tm + ((uint32_t)(q * 32) << 16);  // this warp's lanes
   uint32_t phase = 0;
   bool ok = true;
+  bool pending = false;  // this warpgroup's last commit did not arrive in time
   for (int c = 0; c < kHidden; c += 16) bias_to_tmem(tm_row, sBias, c);  // layer 1 of the first step
   tmem_wait_st();
 
@@ -294,13 +295,25 @@ mlp_far_tiles(const float* __restrict__ ms, int64_t npad, const int4* __restrict
       for (int i = 0; i < 8; ++i) x[i] = __floats2half2_rn(row[2 * i], row[2 * i + 1]);
       store_h16(H, t, 0, kFeatIn, x);
 
-      if (!(ok = layer(tm, H, smem + kW1, kFeatIn, kHidden, &mbar[wg], phase, leader, bar))) break;
+      if (!(ok = layer(tm, H, smem + kW1, kFeatIn, kHidden, &mbar[wg], phase, leader, bar))) {
+        pending = true;
+        break;
+      }
       hidden_epilogue(tm_row, sBias + kHidden, kHidden, H, t);
-      if (!(ok = layer(tm, H, smem + kW2, kHidden, kHidden, &mbar[wg], phase, leader, bar))) break;
+      if (!(ok = layer(tm, H, smem + kW2, kHidden, kHidden, &mbar[wg], phase, leader, bar))) {
+        pending = true;
+        break;
+      }
       hidden_epilogue(tm_row, sBias + 2 * kHidden, kHidden, H, t);
-      if (!(ok = layer(tm, H, smem + kW3, kHidden, kHidden, &mbar[wg], phase, leader, bar))) break;
+      if (!(ok = layer(tm, H, smem + kW3, kHidden, kHidden, &mbar[wg], phase, leader, bar))) {
+        pending = true;
+        break;
+      }
       hidden_epilogue(tm_row, sBias + 3 * kHidden, kOut, H, t);
-      if (!(ok = layer(tm, H, smem + kW4, kHidden, kOut, &mbar[wg], phase, leader, bar))) break;
+      if (!(ok = layer(tm, H, smem + kW4, kHidden, kOut, &mbar[wg], phase, leader, bar))) {
+        pending = true;
+        break;
+      }
       // Contraction: out[o] = sum_ac bp[ac] Y[12 ac + o] (Y includes b4); then
       // b1 into the columns for the next step's first layer.
       float out[kUsedOut];
@@ -361,6 +374,12 @@ mlp_far_tiles(const float* __restrict__ ms, int64_t npad, const int4* __restrict
     }
   }
   if (!ok && tid == 0) atomicExch(err, 1);
+  // A warpgroup whose wait ran out may still have MMAs writing its TMEM
+  // columns; they retire only through the commit's arrival on its mbarrier
+  // (the phase `layer` already stepped past), so wait for it, bounded again,
+  // before the CTA frees the columns.  If that wait also runs out the columns
+  // are freed anyway: a CTA must release its TMEM before it exits.
+  if (pending) tc::mbar_wait(&mbar[wg], phase ^ 1u);
   tc::fence_before_sync();
   __syncthreads();
   if (tid < 32) tc::tmem_dealloc(s_tm, 512);

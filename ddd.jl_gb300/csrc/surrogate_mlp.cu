@@ -346,6 +346,7 @@ cudaError_t backward(ddd_surrogate* s, const __half* X, const float* Bp, const f
 extern "C" {
 
 ddd_surrogate* ddd_surrogate_create(ddd_ctx* ctx, uint64_t seed) {
+  DDD_NVTX("ddd_surrogate_create");
   if (!ctx) return nullptr;
   ddd_surrogate* s = new ddd_surrogate();
   s->device = ddd::ctx_device(ctx);
@@ -467,6 +468,7 @@ T get(const std::vector<unsigned char>& b, size_t off) {
 extern "C" {
 
 int ddd_surrogate_save(ddd_surrogate* s, const char* path, double kappa, double nu, double aSq) {
+  DDD_NVTX("ddd_surrogate_save");
   if (!s || !path) return DDD_EINVAL;
   std::vector<unsigned char> b(kHeader + (size_t)kNumParams * 4 + 4);
   std::memcpy(b.data(), kMagic, 8);
@@ -492,6 +494,7 @@ int ddd_surrogate_save(ddd_surrogate* s, const char* path, double kappa, double 
 }
 
 int ddd_surrogate_load(ddd_surrogate* s, const char* path, double* kappa, double* nu, double* aSq) {
+  DDD_NVTX("ddd_surrogate_load");
   if (!s || !path) return DDD_EINVAL;
   FILE* f = std::fopen(path, "rb");
   if (!f) {
@@ -526,6 +529,7 @@ int ddd_surrogate_load(ddd_surrogate* s, const char* path, double* kappa, double
 // gradients (flat FP32 layout) copied to the host.
 int ddd_surrogate_grads(ddd_surrogate* s, const void* X, const float* Bp, const float* T, int64_t B, double* loss,
                         float* grads) {
+  DDD_NVTX("ddd_surrogate_grads");
   if (!s || !X || !Bp || !T || B <= 0 || B % 128) return DDD_EINVAL;
   cudaSetDevice(s->device);
   if (cudaDeviceSynchronize() != cudaSuccess) return DDD_EDEVICE;  // caller's inputs are ready
@@ -550,6 +554,7 @@ int ddd_surrogate_grads(ddd_surrogate* s, const void* X, const float* Bp, const 
 // fixed order; the mean loss of each epoch goes to lossHistory (host, may be NULL).
 int ddd_surrogate_train(ddd_surrogate* s, const void* X, const float* Bp, const float* T, int64_t P, int64_t B,
                         int epochs, float lr, float weightDecay, double* lossHistory) {
+  DDD_NVTX("ddd_surrogate_train");
   if (!s || !X || !Bp || !T || B <= 0 || B % 128 || P < B || P % B || epochs <= 0) return DDD_EINVAL;
   cudaSetDevice(s->device);
   if (cudaDeviceSynchronize() != cudaSuccess) return DDD_EDEVICE;  // caller's inputs are ready
@@ -592,6 +597,7 @@ int ddd_surrogate_train(ddd_surrogate* s, const void* X, const float* Bp, const 
 // Batched evaluation (P % 128 == 0): O [P x 16] FP32 (device, 12 used) = the
 // contracted scaled node forces of the rows of X and Bp.
 int ddd_surrogate_forward(ddd_surrogate* s, const void* X, const float* Bp, int64_t P, float* O) {
+  DDD_NVTX("ddd_surrogate_forward");
   if (!s || !X || !Bp || !O || P <= 0 || P % 128) return DDD_EINVAL;
   cudaSetDevice(s->device);
   if (cudaDeviceSynchronize() != cudaSuccess) return DDD_EDEVICE;  // caller's inputs are ready

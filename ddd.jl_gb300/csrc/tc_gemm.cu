@@ -71,10 +71,11 @@ tc_gemm_tn(int M, int N, int K, const uint16_t* __restrict__ A, const uint16_t* 
       }
       tc::mma_commit(&mbar);
     }
-    ok = tc::mbar_wait(&mbar, phase);
+    // Every thread leaves with the same verdict: a thread whose wait ran out
+    // makes the whole CTA stop.
+    ok = __syncthreads_and(tc::mbar_wait(&mbar, phase)) != 0;
     phase ^= 1u;
     tc::fence_after_sync();
-    __syncthreads();
   }
 
   if (ok) {
@@ -85,15 +86,46 @@ tc_gemm_tn(int M, int N, int K, const uint16_t* __restrict__ A, const uint16_t* 
 #pragma unroll
       for (int i = 0; i < 16; ++i) D[(size_t)row * N + c0 + i] = v[i];
     }
-  } else if (lane == 0) {
-    atomicExch(err, 1);
+  } else {
+    if (t == 0) atomicExch(err, 1);
+    // The MMAs of the abandoned chunk may still be writing these TMEM columns:
+    // an MMA retires only through its commit's arrival on the mbarrier, so wait
+    // (bounded again) for that arrival before the columns are freed.  If this
+    // wait also runs out, the columns are freed anyway: a CTA must release its
+    // TMEM before it exits.
+    tc::mbar_wait(&mbar, phase ^ 1u);
   }
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(taddr, ncols);
 }
 
+// Self-test of the bounded mbarrier wait that every tcgen05 kernel here uses:
+// one warp, one mbarrier expecting one arrival.  With arrive != 0 thread 0
+// arrives before the wait (the wait must succeed); with arrive == 0 nothing
+// ever arrives, so every thread's wait runs out after max_clocks SM clocks and
+// the kernel records the timeout in *err and returns.  No MMA is issued and no
+// TMEM is held, so nothing is left in flight when the wait gives up.
+__global__ void bounded_wait_probe(long long max_clocks, int arrive, int* __restrict__ err) {
+  __shared__ uint64_t mbar;
+  if (threadIdx.x == 0) tc::mbar_init(&mbar, 1);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  __syncwarp();
+  if (arrive && threadIdx.x == 0) {
+    uint64_t state;
+    asm volatile("mbarrier.arrive.shared::cta.b64 %0, [%1];" : "=l"(state) : "r"(tc::smem_addr(&mbar)) : "memory");
+    (void)state;
+  }
+  const bool ok = tc::mbar_wait(&mbar, 0u, max_clocks);
+  if (!ok) atomicExch(err, 1);
+}
+
 }  // namespace
+
+cudaError_t launch_bounded_wait_probe(long long max_clocks, int arrive, int* err, cudaStream_t st) {
+  bounded_wait_probe<<<1, 32, 0, st>>>(max_clocks, arrive, err);
+  return cudaGetLastError();
+}
 
 size_t tc_gemm_smem_bytes(int N) { return (size_t)(128 + N) * KC * 2; }
 

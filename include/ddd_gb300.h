@@ -297,13 +297,20 @@ int ddd_sigma_tilde_device(ddd_ctx* ctx, const ddd_consts* k, const double* x0, 
  * cudaStream_t; NULL = the legacy default stream), in DDD_MODE_FP64 arithmetic,
  * and the call returns without waiting.  It calls no cudaMalloc, cudaFree or
  * other allocating routine: its scratch is a fixed device array of about
- * 6.9 MB that exists on every GPU that loads the library, for the life of the
- * process.  Limits: numSeg <= DDD_NOALLOC_MAX_SEGMENTS, else DDD_ETOOBIG.
+ * 6.9 MB.  The CUDA driver reserves that array, and loads the force kernels,
+ * when it loads the library's modules on a device: under CUDA's default lazy
+ * module loading that is inside the first call on each device (with
+ * CUDA_MODULE_LOADING=EAGER, at context creation), and the memory stays
+ * reserved until the process exits.  So make one call on each device during
+ * set-up, before a pool allocator reserves the GPU: a call with numSeg = 0
+ * does only this set-up (module loads, address lookup) and launches nothing.
+ * Make that first call before any stream capture that contains later calls.
+ * Limits: numSeg <= DDD_NOALLOC_MAX_SEGMENTS, else DDD_ETOOBIG.
  * Every call shares that array (it keeps the last call's contents; each call
  * writes every element it reads first), so calls that overlap on the GPU race:
- * serialise them.  The first call on each device looks up the array's device
- * address; make it before any stream capture that contains later calls.
- * Returns DDD_OK, DDD_EINVAL, DDD_ETOOBIG or DDD_EDEVICE (no message). */
+ * serialise them.
+ * Returns DDD_OK, DDD_EINVAL, DDD_ENONFINITE (a non-finite constant in k),
+ * DDD_ETOOBIG or DDD_EDEVICE (no message). */
 #define DDD_NOALLOC_MAX_SEGMENTS 4096
 int ddd_segseg_force_device_noalloc(const ddd_consts* k, const double* segs, int64_t ldSegs, const uint8_t* ext,
                                     int64_t numSeg, double* force, void* stream);
@@ -469,8 +476,21 @@ const char* ddd_surrogate_last_error(const ddd_surrogate* s);
 
 /* Measurement utility (no reference counterpart): FP64 or FP32 FMA-pipe
  * throughput of this GPU in FLOP/s, measured with CUDA events over an
- * FMA-chain kernel filling every SM.  precision: 64 or 32. */
+ * FMA-chain kernel filling every SM; the chain length is calibrated so each
+ * timed run lasts about a second (clocks and power settle), best of three.
+ * precision: 64 or 32. */
 int ddd_probe_fma_peak(ddd_ctx* ctx, int precision, double* flops_per_s);
+
+/* Failure-detection self-test (no reference counterpart: the reference has no
+ * device code).  Runs, on the context's device, the bounded mbarrier wait that
+ * the tensor-core kernels (ddd_tc_gemm_bf16, the surrogate's network pass) use
+ * for every wait, in a one-warp kernel that issues no MMA and holds no tensor
+ * memory: with arrive != 0 the barrier receives its arrival and the call
+ * returns DDD_OK; with arrive == 0 nothing arrives, the wait gives up after
+ * max_clocks SM clocks (1 <= max_clocks <= 2e9, about a second at most), the
+ * kernel records the timeout and returns, and the call returns DDD_ETIMEOUT
+ * with the context still usable.  Synchronous. */
+int ddd_selftest_bounded_wait(ddd_ctx* ctx, long long max_clocks, int arrive);
 
 #ifdef __cplusplus
 }
