@@ -168,9 +168,35 @@ def cpu_par_sample(pkg, synth, oracle, p, b, k5, target_s, variant="atomic"):
     dt = time.perf_counter() - t0
     n = net.numSeg
     return {"value": n * (n - 1) / 2 / dt, "unit": "pair-interactions/s", "cores": threads, "kind": "port",
-            "variant": variant,
+            "variant": variant, "seconds": dt,
             "sample": "all %d pairs of the first %d segments (%d loops) of the workload, %.1f s" %
                       (n * (n - 1) // 2, n, n_loops, dt)}
+
+
+def parity_sample(oracle, k5, net, F, rows):
+    """The parity check of the GPU forces F (3 x 2 x numSeg) on the given
+    0-based rows: the oracle's Float64 rows (the reference's arithmetic) and the
+    same rows in long double.  noise = the largest node-force error of the
+    reference's own Float64 arithmetic on these rows (against long double).
+    The bound, per node force vector: |F_gpu - F_ref| <= 1e-10 |F_ref| + 4 noise
+    + 4 ulps of the largest force; bound_excess = the largest left side minus
+    right side (<= 0 when the bound holds); accuracy: the kernel's own error
+    against long double <= 3 noise."""
+    rows = np.sort(np.asarray(rows))
+    nt_ = cpu_threads()
+    ref_rows = oracle.segseg_rows(k5, net, rows, nt_)
+    ext_rows = oracle.segseg_ser_ld(k5, net, rows, nthreads=nt_)
+    nrm = lambda a: np.linalg.norm(a, axis=0)
+    G = F[:, :, rows]
+    d = nrm(G - ref_rows)
+    noise = float(nrm(ref_rows - ext_rows).max())
+    ulps = 4 * np.finfo(np.float64).eps * float(nrm(ext_rows).max())
+    gpu_err = float(nrm(G - ext_rows).max())
+    return {"rows": len(rows), "fp64_max_rel_node": float(np.max(d / nrm(ref_rows))),
+            "fp64_err_vs_longdouble": gpu_err, "reference_arith_err_vs_longdouble": noise,
+            "bound": "|dF| <= 1e-10 |F| + 4 noise + 4 ulp(max|F|) per node",
+            "bound_excess": float(np.max(d - (1e-10 * nrm(ref_rows) + 4 * noise + ulps))),
+            "accuracy_excess": gpu_err - (3 * noise + ulps)}
 
 
 def cpu_sigma_sample(pkg, synth, oracle, p, b, k5, cube, target_s):
@@ -331,6 +357,54 @@ def run_precision_131k(pkg, synth, ctx, k, stream, sptr, flush):
                             "max_rel_point": (ds / ns).max().item(),
                             "max_point_over_max": (ds.max() / ns.max()).item()}},
     }
+
+
+def run_sigma_32k(pkg, synth, oracle, ctx, k, stream, sptr, flush, fp64_peak, with_cpu=True):
+    """σ̃ of the 32,768-segment GPU workload (same generator, seed 0) at every
+    point of the 128^3-point grid over its cube (2,097,152 points: the workload
+    names "2^20 points on a 128^3 grid", and the whole grid is evaluated), FP64
+    strict: one warm-up
+    on 4,096 points, then one timed full evaluation (CUDA events, L2 flushed
+    before it); 256 sampled points checked against the oracle (the reference's
+    segment order per point)."""
+    import torch
+    p, b, cfg = synth.make("gpu32k", seed=0)
+    n = p.shape[0] * 8
+    pts = synth.grid_points(cfg["grid"], cfg["cube"])
+    M = pts.shape[1]
+    soa = torch.from_numpy(synth.packed_soa(p, b)).cuda()
+    x0 = torch.from_numpy(np.ascontiguousarray(pts.T)).cuda()
+    sig = torch.zeros(6 * M, dtype=torch.float64, device="cuda")
+    with torch.cuda.stream(stream):
+        ctx.sigma_tilde_device(k, x0.data_ptr(), 4096, soa.data_ptr(), n, n, sig.data_ptr(), stream=sptr)
+        torch.cuda.synchronize()
+        flush.zero_()
+        a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a_.record(stream)
+        ctx.sigma_tilde_device(k, x0.data_ptr(), M, soa.data_ptr(), n, n, sig.data_ptr(), stream=sptr)
+        b_.record(stream)
+        torch.cuda.synchronize()
+    ms = a_.elapsed_time(b_)
+    evals = n * M
+    out = {"config": "gpu32k: %d segments x %d points (%d^3 grid over the %g^3 b cube), FP64 strict"
+                     % (n, M, cfg["grid"], cfg["cube"]),
+           "value": evals / (ms * 1e-3), "unit": "seg-point evaluations/s", "points_per_s": M / (ms * 1e-3),
+           "ms": ms, "frac_fp64_peak": evals * OPS_SIGMA_EVAL / (ms * 1e-3) / fp64_peak,
+           "kernel": "sigma_tilde_f64"}
+    if with_cpu:
+        coord, bvec, seg = synth.network_arrays(p, b)
+        net = pkg.DislocationNetwork(coord, bvec, seg)
+        pick = np.sort(np.random.default_rng(1).choice(M, 256, replace=False))
+        k5 = np.array([k.aSq, k.mu4pi, k.mu8pi, k.mu4pinu, k.nuMu4pinu])
+        ref = oracle.sigma_tilde(k5, np.asfortranarray(pts[:, pick]), net, nthreads=cpu_threads())
+        S = sig.view(M, 6)[torch.from_numpy(pick).cuda()].cpu().numpy().T
+        d = np.linalg.norm(S - ref, axis=0)
+        r = np.linalg.norm(ref, axis=0)
+        smax = torch.linalg.norm(sig.view(M, 6), dim=1).max().item()
+        out["parity_sample"] = {"points": len(pick), "max_rel_point": float(np.max(d / r)),
+                                "bound": "|dσ| <= 1e-10 |σ| + 1e-12 max|σ| per point",
+                                "bound_excess": float(np.max(d - (1e-10 * r + 1e-12 * smax)))}
+    return out
 
 
 def run_node_rows(pkg, oracle, ctx, net, dln, mat, segseg, reps=5, with_cpu=True):
@@ -521,6 +595,48 @@ def run_u_tilde(pkg, oracle, ctx, net, cube, cells=64, reps=3, cpu_target_s=8.0,
     return out
 
 
+def _r(x, d=4):
+    return None if x is None else float("%.*g" % (d, x))
+
+
+def summary(line, variants, surrogate, sigma32k, batched):
+    """The headline figures in a few hundred characters, printed last on the
+    JSON line so that a reader of the line's end sees both halves of the metric
+    (FP64 plain and FP32 + surrogate), their errors and roofline fractions."""
+    rf = line["roofline"]
+    out = {"fp64": {"pairs_per_s": _r(line["value"]), "e2e": _r(line["e2e"]["value"]), "frac_probe": _r(rf["frac"], 3),
+                    "frac_pipe_rate": _r(rf["frac_pipe_rate"], 3), "probe_tflops": _r(rf["peak"]),
+                    "pipe_rate_tflops": _r(rf["pipe_rate_peak"])}}
+    par = line.get("parity_sample")
+    if par:
+        out["fp64"]["parity"] = {"rows": par["rows"], "max_rel_node": _r(par["fp64_max_rel_node"], 3),
+                                 "bound_excess": _r(par["bound_excess"], 3),
+                                 "accuracy_excess": _r(par["accuracy_excess"], 3)}
+    for m, v in (variants or {}).items():
+        out[m] = {"pairs_per_s": _r(v["value"]), "x_fp64": _r(v["speedup_vs_fp64"], 3),
+                  "rel_rms": _r(v["error_vs_fp64"]["rel_rms"], 3)}
+        if v.get("frac_pipe_rate_algorithmic") is not None:
+            out[m]["frac_pipe_rate"] = _r(v["frac_pipe_rate_algorithmic"], 3)
+    if surrogate:
+        sv = surrogate["f32c"]
+        f32c = (variants or {}).get("f32c")
+        out["surrogate_f32c"] = {
+            "pairs_per_s": _r(sv["value"]), "x_fp64": _r(sv["speedup_vs_fp64"], 3),
+            "x_f32c_exact": _r(f32c["ms_per_step"] / sv["ms_per_step"], 3) if f32c else None,
+            "rel_rms": _r(sv["error_vs_fp64"]["rel_rms"], 3),
+            "max_node_over_max": _r(sv["error_vs_fp64"]["max_node_over_max_force"], 3),
+            "tensor_frac": _r(sv["network_kernel"]["frac"], 3), "kappa": surrogate["kappa"],
+            "arch": "MLP 16-128-128-128-112 GELU, FP16 fwd / FP32 acc, exact bilinear b contraction"}
+    if sigma32k:
+        out["sigma_32k_grid128"] = {"evals_per_s": _r(sigma32k["value"]), "frac_probe": _r(sigma32k["frac_fp64_peak"], 3),
+                                 "bound_excess": _r(sigma32k.get("parity_sample", {}).get("bound_excess"), 3)}
+    if batched:
+        out["batched"] = {m: {"pairs_per_s": _r(batched[m]["value"]),
+                              "rel_rms": _r(batched[m]["error_vs_fp64"]["rel_rms"], 3)}
+                          for m in ("f32c", "fp64") if m in batched}
+    return out
+
+
 def run_reference(args, pkg, synth, oracle):
     ws, rank = _dist()
     if rank != 0:
@@ -534,16 +650,19 @@ def run_reference(args, pkg, synth, oracle):
         info = cpu_par_sample(pkg, synth, oracle, p, b, k5, args.ref_step_s)
         if it >= args.warmup:
             vals.append(info["value"])
+            times.append(info["seconds"])
     v = statistics.median(vals)
     n = p.shape[0] * 8
     out = {
         "impl": "reference",
         "metric": "seg-seg pair interactions/s at 65k segs (FP64 plain vs FP32+surrogate) at stated error",
         "value": v, "unit": "pair-interactions/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * (n * (n - 1) / 2) / v, "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
         "config": {"workload": "%s: %d segments, %d loops" % (args.workload, n, p.shape[0]),
-                   "ms_per_step_note": "extrapolated to the full workload from the sampled pairs/s"},
+                   "step": "all pairs of a prefix of the workload sized to about %g s (%s); ms_per_step is that "
+                           "sampled step's wall time" % (args.ref_step_s, info["sample"]),
+                   "ms_per_full_workload_step_extrapolated": 1e3 * (n * (n - 1) / 2) / v},
         "cpu_baseline": {"kind": "port", "cores": info["cores"], "sample": info["sample"], "value": v,
                          "unit": "pair-interactions/s",
                          "what": "C++/OpenMP restatement of calcSegSegForcePar (DislocationForces.jl:719-777); "
@@ -566,6 +685,8 @@ def main():
     ap.add_argument("--cpu-target-s", type=float, default=15.0)
     ap.add_argument("--ref-step-s", type=float, default=4.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--parity-rows", type=int, default=64, help="segments of the timed result checked against the "
+                    "oracle (and long double)")
     ap.add_argument("--rows-only", action="store_true",
                     help="only the rows around the force (self force, mobility, collision, calc_uTilde) on the "
                          "workload, seg-seg forces from one untimed call; prints their JSON and exits (the command "
@@ -641,7 +762,12 @@ def main():
     rep = ctx.segseg_force_device(k, soa.data_ptr(), n, n, force.data_ptr(), stream=sptr, report=True)
     flops_per_step = (rep["pairs_general"] * OPS_GENERAL_PAIR + rep["pairs_parallel"] * OPS_PARALLEL_PAIR
                       + rep["core_sides"] * 2 * OPS_GENERAL_PAIR)
-    fp64_peak = ctx.probe_fma_peak(64)
+    # FP64 peak, measured: an FMA-chain kernel on every SM, calibrated to run
+    # about a second per timing (best of three), clocks sampled meanwhile.
+    with ClockSampler(local) as probe_clocks:
+        fp64_peak = ctx.probe_fma_peak(64)
+    probe_clock = probe_clocks.summary()
+    n_sm = torch.cuda.get_device_properties(local).multi_processor_count
 
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -674,8 +800,10 @@ def main():
     # error against the strict FP64 result (itself parity-checked).
     variants = {}
     ref_force = force.cpu().numpy().reshape(3, 2, -1, order="F")
+    cs_v = clocks.summary()
+    pipe_peak_v = 4.0 * n_sm * cs_v["sm_mhz"] * 1e6 if cs_v else None
     if not args.no_variants:
-        for mode in ("fp64_fma", "df64", "f32c"):
+        for mode in ("fp64_fast", "fp64_fma", "df64", "f32c"):
             ctx.mode = mode
             out_v = torch.zeros_like(force)
             with torch.cuda.stream(stream):
@@ -698,6 +826,8 @@ def main():
                 "ms_per_step": statistics.mean(vms),
                 "speedup_vs_fp64": ms_step / statistics.mean(vms),
                 "frac_fp64_peak_algorithmic": flops_per_step / (statistics.mean(vms) * 1e-3) / fp64_peak,
+                "frac_pipe_rate_algorithmic": (flops_per_step / (statistics.mean(vms) * 1e-3) / pipe_peak_v
+                                               if pipe_peak_v else None),
                 "error_vs_fp64": {"rel_rms": float(np.linalg.norm(Fv - ref_force) / np.linalg.norm(ref_force)),
                                   "max_node_over_max_force": float(dn.max() / fn.max()),
                                   "max_rel_node": float(np.max(dn / np.maximum(fn, 1e-300)))},
@@ -721,6 +851,10 @@ def main():
     precision131k = None
     if not args.no_precision131k and args.loops is None:
         precision131k = run_precision_131k(pkg, synth, ctx, k, stream, sptr, flush)
+
+    sigma32k = None
+    if not args.no_sigma and args.loops is None:
+        sigma32k = run_sigma_32k(pkg, synth, oracle, ctx, k, stream, sptr, flush, fp64_peak, with_cpu=not args.no_cpu)
 
     # Field-point stress σ̃ of the same network on a 32^3 grid over the cube.
     sigma = None
@@ -785,6 +919,17 @@ def main():
         bforce = torch.zeros(6 * bsegs.shape[1], dtype=torch.float64, device="cuda")
         bpairs = sum(n_ * (n_ - 1) // 2 for n_ in sizes)
         batched = {"networks": len(sizes), "segments": int(sum(sizes)), "pairs_per_run": int(bpairs)}
+        # Reference for the errors: every network through the single-network
+        # FP64 kernel (itself parity-checked against the oracle).
+        tot = bsegs.shape[1]
+        bref = torch.zeros(6 * tot, dtype=torch.float64, device="cuda")
+        off_ = 0
+        for n_ in sizes:
+            ctx.segseg_force_device(k, bsegs.data_ptr() + 8 * off_, tot, n_, bref.data_ptr() + 8 * 6 * off_,
+                                    stream=sptr)
+            off_ += n_
+        torch.cuda.synchronize()
+        bref_n = torch.linalg.norm(bref.view(tot, 2, 3), dim=2)
         for mode, tune in (("f32c", True), ("fp64", False)):
             plan = pkg.Batch(ctx, sizes, mode=mode, tune=tune)
             with torch.cuda.stream(stream):
@@ -798,9 +943,16 @@ def main():
                 torch.cuda.synchronize()
             ms_b = a_.elapsed_time(b_) / 2
             inf = plan.info()
+            dn_ = torch.linalg.norm((bforce - bref).view(tot, 2, 3), dim=2)
             batched[mode] = {"value": bpairs / (ms_b * 1e-3), "unit": "pair-interactions/s", "ms_per_run": ms_b,
                              "tile": inf["tile"], "order": inf["order"], "work_items": inf["work_items"],
-                             "tune_ms": inf["tune_ms"] if tune else None, "graph_launches": inf["graph_launches"]}
+                             "tune_ms": inf["tune_ms"] if tune else None, "graph_launches": inf["graph_launches"],
+                             "error_vs_fp64": {
+                                 "against": "each network through the single-network FP64 kernel",
+                                 "rel_rms": (torch.linalg.norm(bforce - bref) / torch.linalg.norm(bref)).item(),
+                                 "max_rel_node": (dn_ / bref_n.clamp_min(1e-300)).max().item(),
+                                 "max_node_over_max_force": (dn_.max() / bref_n.max()).item(),
+                                 "bit_equal": bool(torch.equal(bforce, bref))}}
             plan.close()
 
     # End to end through the reference-facing C-ABI call with host arrays.
@@ -835,6 +987,12 @@ def main():
     # Displacements at the FE boundary of a mesh around the workload's cube.
     u_tilde = run_u_tilde(pkg, oracle, ctx, net, cfg["cube"], with_cpu=not args.no_cpu)
     achieved = flops_per_step / (statistics.mean(ms_kernel) * 1e-3)
+    cs = clocks.summary()
+    # The FP64 pipe's own rate: 2 DFMA per SM per clock (ncu's FP64 pipe peak:
+    # 304 DFMA per cycle on 152 SMs), 2 FLOPs each, at the median SM clock
+    # sampled during the timed steps.
+    step_mhz = cs["sm_mhz"] if cs else None
+    pipe_peak = 4.0 * n_sm * step_mhz * 1e6 if step_mhz else None
     line = {
         "metric": "seg-seg pair interactions/s at 65k segs (FP64 plain vs FP32+surrogate) at stated error",
         "value": value, "unit": "pair-interactions/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -852,8 +1010,12 @@ def main():
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at 32,768 "
                                        "segments, scaled by tile pairs",
                      "kernel": "segseg_tile_f64<0>",
-                     "peak_source": "measured FP64 FMA-chain probe on this GPU (ddd_probe_fma_peak); "
-                                    "MEASURED_PEAKS.json holds no FP64 figure",
+                     "peak_source": "measured FP64 FMA-chain probe on this GPU (ddd_probe_fma_peak, ~1 s per "
+                                    "timing, best of 3); MEASURED_PEAKS.json holds no FP64 figure",
+                     "probe_clock": probe_clock,
+                     "pipe_rate_peak": pipe_peak / 1e12 if pipe_peak else None,
+                     "frac_pipe_rate": achieved / pipe_peak if pipe_peak else None,
+                     "pipe_rate_source": "2 DFMA/SM/clock x %d SMs x median SM clock of the timed steps" % n_sm,
                      "flops_per_step": flops_per_step,
                      "branches": {k_: rep[k_] for k_ in ("pairs_general", "pairs_parallel", "core_sides")}},
         "e2e": {"value": e2e_value, "unit": "pair-interactions/s", "h2d_bytes_per_step": erep["h2d_bytes"],
@@ -864,13 +1026,13 @@ def main():
         "surrogate": surrogate,
         "precision_131k": precision131k,
         "sigma_tilde": sigma,
+        "sigma_tilde_32k_grid128": sigma32k,
         "batched": batched,
         "node_rows": node_rows,
         "collision": collision,
         "u_tilde": u_tilde,
         "kernel_ms_per_step": statistics.mean(ms_kernel),
     }
-    cs = clocks.summary()
     if cs:
         line["clocks"] = cs
     if not args.no_cpu:
@@ -882,16 +1044,9 @@ def main():
             sigma["cpu_baseline"] = cpu_sigma_sample(pkg, synth, oracle, p, b, k5, cfg["cube"], 5.0)
         # Parity of the timed result on sampled segments: the oracle's Float64 rows
         # and the same rows in long double (the reference arithmetic's own error).
-        rows = np.sort(np.random.default_rng(0).choice(n, 16, replace=False))
-        nt_ = cpu_threads()
-        ref_rows = oracle.segseg_rows(k5, net, rows, nt_)
-        ext_rows = oracle.segseg_ser_ld(k5, net, rows, nthreads=nt_)
-        nrm = lambda a: np.linalg.norm(a, axis=0)
-        par = {"rows": len(rows), "fp64_max_rel_node": float(np.max(nrm(ref_force[:, :, rows] - ref_rows) /
-                                                                   nrm(ref_rows))),
-               "fp64_err_vs_longdouble": float(nrm(ref_force[:, :, rows] - ext_rows).max()),
-               "reference_arith_err_vs_longdouble": float(nrm(ref_rows - ext_rows).max())}
-        line["parity_sample"] = par
+        line["parity_sample"] = parity_sample(oracle, k5, net, ref_force, np.random.default_rng(0).choice(
+            n, args.parity_rows, replace=False))
+    line["summary"] = summary(line, variants, surrogate, sigma32k, batched)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

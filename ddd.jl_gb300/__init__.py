@@ -52,8 +52,9 @@ EXPORTED_SYMBOLS = (
 )
 
 # Arithmetic modes (ddd_set_mode).
-MODE_FP64, MODE_FP64_FMA, MODE_DF64, MODE_F32C = 0, 1, 2, 3
-MODES = {"fp64": MODE_FP64, "fp64_fma": MODE_FP64_FMA, "df64": MODE_DF64, "f32c": MODE_F32C}
+MODE_FP64, MODE_FP64_FMA, MODE_DF64, MODE_F32C, MODE_FP64_FAST = 0, 1, 2, 3, 4
+MODES = {"fp64": MODE_FP64, "fp64_fma": MODE_FP64_FMA, "df64": MODE_DF64, "f32c": MODE_F32C,
+         "fp64_fast": MODE_FP64_FAST}
 
 
 class DDDError(RuntimeError):

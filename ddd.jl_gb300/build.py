@@ -24,6 +24,8 @@ VARIANTS = {
     "sigma_f64.cu": [("strict", ["-DDDD_VARIANT=strict", "--fmad=false"]), ("fast", ["-DDDD_VARIANT=fast"])],
     # df64 needs exact error-free transformations: no contraction.
     "segseg_df.cu": [("", ["--fmad=false"])],
+    # explicit fused multiply-adds only (host builds of its header give the same bits)
+    "segseg_f64fast.cu": [("", ["--fmad=false"])],
     "segseg_batch.cu": [("", ["--fmad=false"])],
     "surrogate_data.cu": [("", ["--fmad=false"])],
     "surrogate_force.cu": [("", ["--fmad=false"])],

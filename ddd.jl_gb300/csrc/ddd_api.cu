@@ -67,6 +67,7 @@ int cuda_fail(ddd_ctx* c, cudaError_t e, const char* where) {
 // and inverse length) always uses the strict build, so t and 1/|l| are the
 // reference's values in both modes.
 bool use_fma(const ddd_ctx* c) { return c->mode == DDD_MODE_FP64_FMA; }
+bool use_fx(const ddd_ctx* c) { return c->mode == DDD_MODE_FP64_FAST; }
 bool use_df(const ddd_ctx* c) { return c->mode == DDD_MODE_DF64 || c->mode == DDD_MODE_F32C; }
 int df_form(const ddd_ctx* c) { return c->mode == DDD_MODE_F32C ? 1 : 0; }
 
@@ -106,6 +107,7 @@ cudaError_t run_segseg_all(ddd_ctx* c, const ddd::KConsts& K, const double* soa,
     return ddd::launch_segseg_all_df(K, soa, c->soadf.as<float>(), skip, npad, partial, out, numSeg, cnt, st,
                                      df_form(c), cap);
   }
+  if (use_fx(c)) return ddd::launch_segseg_all_fx(K, soa, skip, npad, partial, out, numSeg, cnt, st, cap);
   return use_fma(c) ? ddd::fast::launch_segseg_all_f64(K, soa, skip, npad, partial, out, numSeg, cnt, st, cap)
                     : ddd::strict::launch_segseg_all_f64(K, soa, skip, npad, partial, out, numSeg, cnt, st, cap);
 }
@@ -136,6 +138,7 @@ cudaError_t run_segseg_rows(ddd_ctx* c, const ddd::KConsts& K, const double* soa
     const cudaError_t e =
         use_df(c) ? ddd::launch_segseg_rows_df(K, soa, c->soadf.as<float>(), skip, npad, rows + r0, n, partial,
                                                out + 6 * r0, cnt, st, df_form(c))
+        : use_fx(c)  ? ddd::launch_segseg_rows_fx(K, soa, skip, npad, rows + r0, n, partial, out + 6 * r0, cnt, st)
         : use_fma(c) ? ddd::fast::launch_segseg_rows_f64(K, soa, skip, npad, rows + r0, n, partial, out + 6 * r0, cnt,
                                                          st)
                      : ddd::strict::launch_segseg_rows_f64(K, soa, skip, npad, rows + r0, n, partial, out + 6 * r0,
@@ -152,8 +155,8 @@ cudaError_t run_sigma(ddd_ctx* c, const ddd::KConsts& K, const double* soa, int6
     if (e != cudaSuccess) return e;
     return ddd::launch_sigma_mixed(K, c->soadf.as<float>(), npad, nSeg, x0, M, sigma, st);
   }
-  return use_fma(c) ? ddd::fast::launch_sigma_f64(K, soa, npad, nSeg, x0, M, sigma, st)
-                    : ddd::strict::launch_sigma_f64(K, soa, npad, nSeg, x0, M, sigma, st);
+  return use_fma(c) || use_fx(c) ? ddd::fast::launch_sigma_f64(K, soa, npad, nSeg, x0, M, sigma, st)
+                                 : ddd::strict::launch_sigma_f64(K, soa, npad, nSeg, x0, M, sigma, st);
 }
 
 
@@ -891,7 +894,8 @@ int ddd_sigma_tilde_device(ddd_ctx* ctx, const ddd_consts* k, const double* x0, 
 int ddd_set_mode(ddd_ctx* ctx, int mode) {
   if (!ctx) return DDD_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
-  if (mode != DDD_MODE_FP64 && mode != DDD_MODE_FP64_FMA && mode != DDD_MODE_DF64 && mode != DDD_MODE_F32C)
+  if (mode != DDD_MODE_FP64 && mode != DDD_MODE_FP64_FMA && mode != DDD_MODE_DF64 && mode != DDD_MODE_F32C &&
+      mode != DDD_MODE_FP64_FAST)
     return fail(ctx, DDD_EINVAL, "unknown mode");
   ctx->mode = mode;
   return DDD_OK;

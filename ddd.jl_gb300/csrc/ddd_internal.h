@@ -96,6 +96,16 @@ cudaError_t launch_segseg_rows_df(const KConsts& K, const double* soa, const flo
 cudaError_t launch_sigma_mixed(const KConsts& K, const float* soadf, int64_t npad, int64_t nSeg, const double* x0,
                                int64_t M, double* sigma, cudaStream_t st);
 
+// segseg_f64fast.cu: the FP64 tile kernels with the fast general branch
+// (pair_f64fast.cuh: fewer divisions, table-driven log/atan, explicit FMAs);
+// near-parallel branch, segment preparation and reductions strict.
+cudaError_t launch_segseg_all_fx(const KConsts& K, const double* soa, const uint8_t* skip, int64_t npad,
+                                 double* partial, double* out, int64_t numSeg, unsigned long long* counters,
+                                 cudaStream_t st, int64_t capSlots);
+cudaError_t launch_segseg_rows_fx(const KConsts& K, const double* soa, const uint8_t* skip, int64_t npad,
+                                  const int64_t* rows, int64_t nRows, double* partial, double* out,
+                                  unsigned long long* counters, cudaStream_t st);
+
 // tc_gemm.cu: tcgen05 GEMM, D = A * B^T (both K-major), A and B both BF16 or both F16.
 size_t tc_gemm_smem_bytes(int N);
 cudaError_t launch_tc_gemm_bf16(int M, int N, int K, const void* A, const void* B, float* D, int* err,

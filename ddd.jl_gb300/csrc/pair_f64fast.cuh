@@ -1,0 +1,325 @@
+// The general branch (1 - c^2 > sqrt(eps)) of the non-singular seg-seg force in
+// a reformulated FP64 form that issues fewer FP64 instructions than the
+// reference's literal evaluation (pair_f64.cuh), for DDD_MODE_FP64_FAST.
+// Same formulas (Arsenlis et al. 2007, App. A.1, as written in DDD.jl
+// src/Processing/DislocationForces.jl:879-1165 and :1480-1561); differences:
+//   * per corner, one IEEE division instead of four: with R1 = Ra + y + x c,
+//     R2 = Ra + x + y c and Q = 1 / (Ra R1 R2), 1/(Ra R1) = Q R2,
+//     1/(Ra R2) = Q R1 and 1/Ra = Q (R1 R2); the division by a^2 + d^2(1 - c^2)
+//     becomes a product with its reciprocal, taken once per pair;
+//   * the logarithms and arctangents are the table-driven fm::log / fm::atan
+//     (fastmath_f64.cuh), or CUDA's, by the template flag FMATH;
+//   * explicit fused multiply-adds (fma_) in the corner terms and the force
+//     assembly.  Quantities that cancel keep the reference's separate rounding:
+//     c, 1 - c^2, the cross products and dots of the pair's geometry, the
+//     local coordinates d, x1, x2, y1, y2, the argument of Ra, and
+//     Ra + y + x c, Ra + x + y c — the terms whose rounding sets the
+//     reference's own error.
+// Everything else is plain IEEE arithmetic, so the same header compiled for a
+// CPU (no contraction) gives the GPU's results bit for bit when FMATH = true.
+#pragma once
+#include "fastmath_f64.cuh"
+
+namespace ddd {
+namespace fx {
+
+struct X3 {
+  double x, y, z;
+};
+FM_HD X3 operator+(X3 a, X3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+FM_HD X3 operator-(X3 a, X3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+FM_HD X3 operator-(X3 a) { return {-a.x, -a.y, -a.z}; }
+FM_HD X3 operator*(double s, X3 a) { return {s * a.x, s * a.y, s * a.z}; }
+FM_HD X3 operator*(X3 a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+FM_HD double dot(X3 a, X3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+FM_HD X3 cross(X3 a, X3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+// s a + v, fused per component.
+FM_HD X3 fmv(double s, X3 a, X3 v) { return {fm::fma_(s, a.x, v.x), fm::fma_(s, a.y, v.y), fm::fma_(s, a.z, v.z)}; }
+// v with its sign flipped when sm is the sign-bit mask (integer operations).
+FM_HD double sgn(double v, long long sm) { return fm::as_d(fm::as_ll(v) ^ sm); }
+
+struct KFast {
+  double aSq, mu4pi, mu8pi, mu4pinu, mu8piaSq, mu4pinuaSq;
+};
+
+template <bool FMATH>
+FM_HD double lg(double v) {
+  if (FMATH) return fm::log(v);
+  return fm::std_log(v);
+}
+template <bool FMATH>
+FM_HD double at(double v) {
+  if (FMATH) return fm::atan(v);
+  return fm::std_atan(v);
+}
+
+// SegSegInteg at one corner (DislocationForces.jl:1480-1561), added (sm = 0) or
+// subtracted (sm = sign bit) into integ[19].  aSq_dSq, aSq_dSqI = 1/aSq_dSq and
+// den = 1/sqrt((1 - c^2) aSq_dSq) are per pair.
+template <bool FMATH>
+FM_HD void corner(double aSq_dSq, double aSq_dSqI, double den, double c, double cSq, double omcSqI, double x, double y,
+                  long long sm, double* integ) {
+  const double xSq = x * x;
+  const double ySq = y * y;
+  const double Ra = sqrt(aSq_dSq + xSq + ySq + 2.0 * x * y * c);
+  const double R1 = Ra + y + x * c;  // Ra_Rd_t1
+  const double R2 = Ra + x + y * c;  // Ra_Rd_t2
+  const double L1 = lg<FMATH>(R1);
+  const double L2 = lg<FMATH>(R2);
+  const double R12 = R1 * R2;
+  const double Q = 1.0 / (Ra * R12);
+  const double RaInv = Q * R12;
+  const double S1 = Q * R2;  // RaSq_R_t1_I = 1/(Ra R1)
+  const double S2 = Q * R1;  // RaSq_R_t2_I = 1/(Ra R2)
+  const double xS1 = x * S1, xxS1 = x * xS1;
+  const double yS2 = y * S2, yyS2 = y * yS2;
+
+  const double integ1 = -2.0 * den * at<FMATH>((1.0 + c) * (Ra + x + y) * den);
+  const double c_1 = aSq_dSq * integ1;
+  const double c_5_6 = fm::fma_(c, Ra, -c_1) * omcSqI;
+  const double integ2 = fm::fma_(c, L2, -L1) * omcSqI;
+  const double integ3 = fm::fma_(c, L1, -L2) * omcSqI;
+  const double integ4 = fm::fma_(c, c_1, -Ra) * omcSqI;
+  const double integ5 = fm::fma_(y, L2, c_5_6);
+  const double integ6 = fm::fma_(x, L1, c_5_6);
+
+  const double c_11_12 = fm::fma_(-c, RaInv, integ1);
+  const double c_15_18 = fm::fma_(c, xS1, -RaInv);
+  const double x_13_14 = x * c_15_18;
+  const double c_19 = fm::fma_(c, yS2, -RaInv);
+  const double y_13_14 = y * c_19;
+  const double c_16 = fm::fma_(-cSq, yyS2, fm::fma_(-(x - c * y), RaInv, L2));
+  const double z_15_18 = y * c_16;
+  const double c_17_19 = fm::fma_(-cSq, xxS1, fm::fma_(-(y - c * x), RaInv, L1));
+  const double c15_18_19 = 2.0 * integ4;
+
+  integ[0] += sgn(integ1, sm);
+  integ[1] += sgn(integ2, sm);
+  integ[2] += sgn(integ3, sm);
+  integ[3] += sgn(integ4, sm);
+  integ[4] += sgn(integ5, sm);
+  integ[5] += sgn(integ6, sm);
+  integ[6] += sgn((integ1 - xS1 - yS2) * aSq_dSqI, sm);
+  integ[7] += sgn(fm::fma_(-c, S2, S1) * omcSqI, sm);
+  integ[8] += sgn(fm::fma_(-c, S1, S2) * omcSqI, sm);
+  integ[9] += sgn(fm::fma_(-c, xS1 + yS2 + integ1, RaInv) * omcSqI, sm);
+  integ[10] += sgn(fm::fma_(cSq, yS2, xS1 + c_11_12) * omcSqI, sm);
+  integ[11] += sgn(fm::fma_(cSq, xS1, yS2 + c_11_12) * omcSqI, sm);
+  integ[12] += sgn(fm::fma_(c, y_13_14 - integ2, integ3 - x_13_14) * omcSqI, sm);
+  integ[13] += sgn(fm::fma_(c, x_13_14 - integ3, integ2 - y_13_14) * omcSqI, sm);
+  integ[14] += sgn(fm::fma_(c, fm::fma_(xSq, c_15_18, -c15_18_19), integ5 - z_15_18) * omcSqI, sm);
+  integ[15] += sgn(fm::fma_(c, c_16, fm::fma_(2.0, integ2, xxS1)) * omcSqI, sm);
+  integ[16] += sgn(fm::fma_(c, c_17_19, fm::fma_(2.0, integ3, yyS2)) * omcSqI, sm);
+  integ[17] += sgn(fm::fma_(c, z_15_18 - integ5, fm::fma_(-xSq, c_15_18, c15_18_19)) * omcSqI, sm);
+  integ[18] += sgn(fm::fma_(c, fm::fma_(x, c_17_19, -integ6), fm::fma_(-ySq, c_19, c15_18_19)) * omcSqI, sm);
+}
+
+// sum_k V[k] F[k] with fused products.
+FM_HD X3 fsum11(const X3* V, const double* F) {
+  X3 s = V[0] * F[0];
+#pragma unroll
+  for (int k = 1; k < 11; ++k) s = fmv(F[k], V[k], s);
+  return s;
+}
+
+// General branch of calcSegSegForce; NEED12 / NEED34 as in pair_f64.cuh.
+template <bool NEED12, bool NEED34, bool FMATH>
+FM_HD void general_pair(const KFast& K, X3 b1, X3 n11, X3 n12, X3 t1, double t1N, X3 b2, X3 n21, X3 n22, X3 t2,
+                        double t2N, double c, X3& F1, X3& F2, X3& F3, X3& F4) {
+  const double mu4pi = K.mu4pi, mu4pinu = K.mu4pinu, mu8piaSq = K.mu8piaSq, mu4pinuaSq = K.mu4pinuaSq;
+  const double cSq = c * c;
+  const double omcSq = 1.0 - cSq;
+  const double omcSqI = 1.0 / omcSq;
+
+  const X3 t2ct1 = cross(t2, t1);
+  const X3 t1ct2 = -t2ct1;
+  const X3 b2ct2 = cross(b2, t2);
+  const X3 b1ct1 = cross(b1, t1);
+
+  const double t2db2 = dot(t2, b2);
+  const double t2db1 = dot(t2, b1);
+  const double t1db2 = dot(t1, b2);
+  const double t1db1 = dot(t1, b1);
+
+  const double t2ct1db2 = dot(t2ct1, b2);
+  const double t1ct2db1 = dot(t1ct2, b1);
+  const double b1ct1db2 = dot(b1ct1, b2);
+  const double b2ct2db1 = dot(b2ct2, b1);
+
+  const X3 t2ct1ct2 = t1 - c * t2;
+  const X3 t1ct2ct1 = t2 - c * t1;
+  const X3 t2cb1ct2 = b1 - t2db1 * t2;
+  const X3 t1cb2ct1 = b2 - t1db2 * t1;
+  const X3 b1ct1ct2 = t2db1 * t1 - c * b1;
+  const X3 b2ct2ct1 = t1db2 * t2 - c * b2;
+
+  const double t2ct1cb1dt1 = t2db1 - t1db1 * c;
+  const double t1ct2cb2dt2 = t1db2 - t2db2 * c;
+  const double t2ct1cb1db2 = t2db1 * t1db2 - t1db1 * t2db2;
+
+  const X3 R1 = n21 - n11;
+  const X3 R2 = n22 - n12;
+  const double d = dot(R2, t2ct1) * omcSqI;
+
+  const double mu4pid = mu4pi * d;
+  const double mu4pinud = mu4pinu * d;
+  const double mu4pinudSq = mu4pinud * d;
+  const double mu4pinudCu = mu4pinudSq * d;
+  const double mu4pinuaSqd = mu4pinuaSq * d;
+  const double mu8piaSqd = mu8piaSq * d;
+
+  const double lim11 = dot(R1, t1);
+  const double lim12 = dot(R1, t2);
+  const double lim21 = dot(R2, t1);
+  const double lim22 = dot(R2, t2);
+
+  const double x1 = (lim12 - c * lim11) * omcSqI;
+  const double x2 = (lim22 - c * lim21) * omcSqI;
+  const double y1 = (lim11 - c * lim12) * omcSqI;
+  const double y2 = (lim21 - c * lim22) * omcSqI;
+
+  double integ[19];
+#pragma unroll
+  for (int k = 0; k < 19; ++k) integ[k] = 0.0;
+  const double aSq_dSq = K.aSq + d * d * omcSq;
+  const double aSq_dSqI = 1.0 / aSq_dSq;
+  const double den = 1.0 / sqrt(omcSq * aSq_dSq);
+  // ((I(x1,y1) - I(x1,y2)) - I(x2,y1)) + I(x2,y2), DislocationForces.jl:948-951.
+#pragma unroll 1
+  for (int q = 0; q < 4; ++q) {
+    const double x = (q & 2) ? x2 : x1;
+    const double y = (q & 1) ? y2 : y1;
+    const long long sm = (q == 1 || q == 2) ? (long long)0x8000000000000000ULL : 0LL;
+    corner<FMATH>(aSq_dSq, aSq_dSqI, den, c, cSq, omcSqI, x, y, sm, integ);
+  }
+
+  X3 V[11];
+  double Fi[11];
+  if (NEED12) {
+    double tmp1 = fm::fma_(t1db2, t2db1, t2ct1cb1db2);
+    const X3 V1 = tmp1 * t2ct1;
+    const X3 V2 = b1ct1 * t1ct2cb2dt2;
+    const X3 V3 = fmv(-t2db1, t1cb2ct1, t1ct2 * b1ct1db2);
+    const X3 V4 = -b1ct1 * t2ct1db2;
+    const X3 V5 = fmv(-b2ct2db1, t1ct2, b2ct2ct1 * t2db1);
+
+    double tmp2;
+    tmp1 = mu4pinud * t1ct2db1;
+    tmp2 = mu4pinud * b2ct2db1;
+    V[0] = fmv(tmp2, t1ct2ct1, fmv(tmp1, b2ct2ct1, fmv(-mu4pinud, V2, mu4pid * V1)));
+    tmp1 = mu4pinu * t2db1;
+    tmp2 = mu4pinu * b2ct2db1;
+    V[1] = fmv(tmp2, t1ct2, fmv(-tmp1, b2ct2ct1, mu4pi * V5));
+    tmp1 = mu4pinu * t1db1;
+    V[2] = fmv(-mu4pinu, V4, fmv(mu4pi, V3, -tmp1 * b2ct2ct1));
+    tmp1 = mu4pinudCu * t1ct2cb2dt2 * t1ct2db1;
+    V[3] = fmv(-tmp1, t1ct2ct1, fmv(-mu4pinuaSqd, V2, mu8piaSqd * V1));
+    tmp1 = mu4pinudSq * t1ct2cb2dt2 * t2db1;
+    tmp2 = mu4pinudSq * t1ct2cb2dt2 * t1ct2db1;
+    V[4] = fmv(-tmp2, t1ct2, fmv(tmp1, t1ct2ct1, mu8piaSq * V5));
+    tmp1 = mu4pinudSq * fm::fma_(t2ct1db2, t1ct2db1, t1ct2cb2dt2 * t1db1);
+    V[5] = fmv(tmp1, t1ct2ct1, fmv(-mu4pinuaSq, V4, mu8piaSq * V3));
+    tmp1 = mu4pinud * fm::fma_(t1ct2cb2dt2, t1db1, t2ct1db2 * t1ct2db1);
+    tmp2 = mu4pinud * t2ct1db2 * t2db1;
+    V[6] = fmv(-tmp2, t1ct2ct1, tmp1 * t1ct2);
+    tmp1 = mu4pinud * t1ct2cb2dt2 * t2db1;
+    V[7] = tmp1 * t1ct2;
+    tmp1 = mu4pinud * t2ct1db2 * t1db1;
+    V[8] = -tmp1 * t1ct2ct1;
+    const X3 tv = mu4pinu * t2ct1db2 * t1ct2;
+    V[9] = -tv * t2db1;
+    V[10] = -tv * t1db1;
+
+    const double y2_ = -y2;
+    Fi[0] = fm::fma_(y2_, integ[0], integ[2]);
+    Fi[1] = fm::fma_(y2_, integ[1], integ[3]);
+    Fi[2] = fm::fma_(y2_, integ[2], integ[5]);
+    Fi[3] = fm::fma_(y2_, integ[6], integ[8]);
+    Fi[4] = fm::fma_(y2_, integ[7], integ[9]);
+    Fi[5] = fm::fma_(y2_, integ[8], integ[11]);
+    Fi[6] = fm::fma_(y2_, integ[9], integ[13]);
+    Fi[7] = fm::fma_(y2_, integ[10], integ[12]);
+    Fi[8] = fm::fma_(y2_, integ[11], integ[16]);
+    Fi[9] = fm::fma_(y2_, integ[12], integ[14]);
+    Fi[10] = fm::fma_(y2_, integ[13], integ[18]);
+    F1 = fsum11(V, Fi) * t1N;
+
+    Fi[0] = fm::fma_(y1, integ[0], -integ[2]);
+    Fi[1] = fm::fma_(y1, integ[1], -integ[3]);
+    Fi[2] = fm::fma_(y1, integ[2], -integ[5]);
+    Fi[3] = fm::fma_(y1, integ[6], -integ[8]);
+    Fi[4] = fm::fma_(y1, integ[7], -integ[9]);
+    Fi[5] = fm::fma_(y1, integ[8], -integ[11]);
+    Fi[6] = fm::fma_(y1, integ[9], -integ[13]);
+    Fi[7] = fm::fma_(y1, integ[10], -integ[12]);
+    Fi[8] = fm::fma_(y1, integ[11], -integ[16]);
+    Fi[9] = fm::fma_(y1, integ[12], -integ[14]);
+    Fi[10] = fm::fma_(y1, integ[13], -integ[18]);
+    F2 = fsum11(V, Fi) * t1N;
+  }
+  if (NEED34) {
+    double tmp1 = fm::fma_(t2db1, t1db2, t2ct1cb1db2);
+    const X3 V1 = tmp1 * t1ct2;
+    const X3 V2 = b2ct2 * t2ct1cb1dt1;
+    const X3 V3 = fmv(-t1db2, b1ct1ct2, t2ct1 * b1ct1db2);
+    const X3 V5 = fmv(-b2ct2db1, t2ct1, t2cb1ct2 * t1db2);
+    const X3 V6 = b2ct2 * t1ct2db1;
+
+    double tmp2;
+    tmp1 = mu4pinud * t2ct1db2;
+    tmp2 = mu4pinud * b1ct1db2;
+    V[0] = fmv(tmp2, t2ct1ct2, fmv(tmp1, b1ct1ct2, fmv(-mu4pinud, V2, mu4pid * V1)));
+    tmp1 = mu4pinu * t2db2;
+    V[1] = fmv(-mu4pinu, V6, fmv(mu4pi, V5, tmp1 * b1ct1ct2));
+    tmp1 = mu4pinu * t1db2;
+    tmp2 = mu4pinu * b1ct1db2;
+    V[2] = fmv(-tmp2, t2ct1, fmv(tmp1, b1ct1ct2, mu4pi * V3));
+    tmp1 = mu4pinudCu * t2ct1cb1dt1 * t2ct1db2;
+    V[3] = fmv(-tmp1, t2ct1ct2, fmv(-mu4pinuaSqd, V2, mu8piaSqd * V1));
+    tmp1 = mu4pinudSq * fm::fma_(t1ct2db1, t2ct1db2, t2ct1cb1dt1 * t2db2);
+    V[4] = fmv(-tmp1, t2ct1ct2, fmv(-mu4pinuaSq, V6, mu8piaSq * V5));
+    tmp1 = mu4pinudSq * t2ct1cb1dt1 * t1db2;
+    tmp2 = mu4pinudSq * t2ct1cb1dt1 * t2ct1db2;
+    V[5] = fmv(tmp2, t2ct1, fmv(-tmp1, t2ct1ct2, mu8piaSq * V3));
+    tmp1 = mu4pinud * fm::fma_(t2ct1cb1dt1, t2db2, t1ct2db1 * t2ct1db2);
+    tmp2 = mu4pinud * t1ct2db1 * t1db2;
+    V[6] = fmv(-tmp2, t2ct1ct2, tmp1 * t2ct1);
+    tmp1 = mu4pinud * t1ct2db1 * t2db2;
+    V[7] = -tmp1 * t2ct1ct2;
+    tmp1 = mu4pinud * t2ct1cb1dt1 * t1db2;
+    V[8] = tmp1 * t2ct1;
+    const X3 tv = mu4pinu * t1ct2db1 * t2ct1;
+    V[9] = tv * t2db2;
+    V[10] = tv * t1db2;
+
+    Fi[0] = fm::fma_(x2, integ[0], -integ[1]);
+    Fi[1] = fm::fma_(x2, integ[1], -integ[4]);
+    Fi[2] = fm::fma_(x2, integ[2], -integ[3]);
+    Fi[3] = fm::fma_(x2, integ[6], -integ[7]);
+    Fi[4] = fm::fma_(x2, integ[7], -integ[10]);
+    Fi[5] = fm::fma_(x2, integ[8], -integ[9]);
+    Fi[6] = fm::fma_(x2, integ[9], -integ[12]);
+    Fi[7] = fm::fma_(x2, integ[10], -integ[15]);
+    Fi[8] = fm::fma_(x2, integ[11], -integ[13]);
+    Fi[9] = fm::fma_(x2, integ[12], -integ[17]);
+    Fi[10] = fm::fma_(x2, integ[13], -integ[14]);
+    F3 = fsum11(V, Fi) * t2N;
+
+    const double x1_ = -x1;
+    Fi[0] = fm::fma_(x1_, integ[0], integ[1]);
+    Fi[1] = fm::fma_(x1_, integ[1], integ[4]);
+    Fi[2] = fm::fma_(x1_, integ[2], integ[3]);
+    Fi[3] = fm::fma_(x1_, integ[6], integ[7]);
+    Fi[4] = fm::fma_(x1_, integ[7], integ[10]);
+    Fi[5] = fm::fma_(x1_, integ[8], integ[9]);
+    Fi[6] = fm::fma_(x1_, integ[9], integ[12]);
+    Fi[7] = fm::fma_(x1_, integ[10], integ[15]);
+    Fi[8] = fm::fma_(x1_, integ[11], integ[13]);
+    Fi[9] = fm::fma_(x1_, integ[12], integ[17]);
+    Fi[10] = fm::fma_(x1_, integ[13], integ[14]);
+    F4 = fsum11(V, Fi) * t2N;
+  }
+}
+
+}  // namespace fx
+}  // namespace ddd

@@ -68,6 +68,16 @@ typedef struct ddd_ctx ddd_ctx;
  * branch, branch decision and per-node accumulation in FP64 as in
  * DDD_MODE_DF64.  Measured node-force error ~5e-8 relative RMS. */
 #define DDD_MODE_F32C 3
+/* DDD_MODE_FP64_FAST, FP64 throughout with fewer FP64 instructions per pair:
+ * the general branch with one division per corner instead of four, table-
+ * driven logarithms and arctangents (about 1 ulp), and fused multiply-adds
+ * wherever the reference's terms do not cancel; the quantities whose rounding
+ * sets the reference's own error (c, 1 - c^2, the pair geometry, the local
+ * coordinates, Ra and Ra + y + x c) are rounded as the reference rounds them,
+ * and the near-parallel branch is the strict code.  Its node forces stay
+ * within the reference arithmetic's own rounding noise (the same parity bound
+ * as DDD_MODE_FP64).  The field stress runs the FMA build in this mode. */
+#define DDD_MODE_FP64_FAST 4
 
 /* Constants of the path.  The reference computes them in
  * MaterialParameters (src/Type/MaterialConstructor.jl:66-82) and

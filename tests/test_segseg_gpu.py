@@ -263,6 +263,41 @@ def test_fma_mode(pkg, synth, oracle, num_loops, seed):
     assert not np.array_equal(F, S)  # a different kernel ran
 
 
+@pytest.mark.parametrize("num_loops,seed,pf,cube", [(1, 0, 0.05, 3000.0), (17, 2, 0.05, 3000.0),
+                                                    (64, 4, 0.05, 3000.0), (150, 5, 0.05, 3000.0),
+                                                    (96, 21, 0.5, 1500.0), (300, 7, 0.05, 20000.0)])
+def test_fp64_fast_mode(pkg, synth, oracle, num_loops, seed, pf, cube):
+    """DDD_MODE_FP64_FAST (one division per corner, table-driven log/atan,
+    explicit FMAs where the terms do not cancel; near-parallel branch strict)
+    under the same parity bound as the strict kernel: per node
+    |ΔF| <= 1e-10 |F| + 4 noise and kernel error <= 3 noise.  The same
+    header built for a CPU measures its error at 1.0-1.1x the reference
+    arithmetic's own on these networks.  Also: same branch counts as the
+    strict kernel, idx and in-place forms, external segments skipped."""
+    net = _synthetic(pkg, synth, num_loops, seed, parallel_fraction=pf, cube=cube)
+    net.extSeg[::29] = 1
+    dln, mat = _params(pkg)
+    ctx = pkg.get_context()
+    S = pkg.calcSegSegForce(dln, mat, net)
+    rep_s = dict(ctx.last_report)
+    idx = np.array([1, 5, 5, net.numSeg])
+    ctx.mode = "fp64_fast"
+    try:
+        F = pkg.calcSegSegForce(dln, mat, net)
+        rep_f = dict(ctx.last_report)
+        Fi = pkg.calcSegSegForce(dln, mat, net, idx)
+        assert np.array_equal(pkg.calcSegSegForce(dln, mat, net), F)
+    finally:
+        ctx.mode = "fp64"
+    assert (rep_f["pairs_general"], rep_f["pairs_parallel"]) == (rep_s["pairs_general"], rep_s["pairs_parallel"])
+    assert np.all(F[:, :, net.extSeg[:net.numSeg] == 1] == 0)
+    k5 = k5_of(dln, mat)
+    check_forces(F, oracle, k5, net)
+    check_forces(Fi, oracle, k5, net, rows=idx - 1, ref=oracle.segseg_idx(k5, net, idx))
+    if num_loops > 1:
+        assert not np.array_equal(F, S)  # a different kernel ran
+
+
 @pytest.mark.parametrize("num_loops,seed,pf", [(64, 4, 0.05), (150, 5, 0.05), (96, 21, 0.5)])
 def test_df64_mode(pkg, synth, oracle, num_loops, seed, pf):
     """DDD_MODE_DF64 (double-float general branch, FP64 near-parallel branch and
@@ -323,7 +358,7 @@ def test_f32c_mode(pkg, synth, oracle, num_loops, seed, pf, cube):
     assert np.all(nrm(Fi - exti) <= 1e-4 * nrm(exti) + 1e-6 * nrm(ext).max())
 
 
-@pytest.mark.parametrize("mode", ["fp64", "fp64_fma", "df64", "f32c"])
+@pytest.mark.parametrize("mode", ["fp64", "fp64_fma", "fp64_fast", "df64", "f32c"])
 def test_banded_partial_sums(pkg, synth, oracle, mode):
     """A partial-sum limit below the all-pairs slot count (4,800 segments: 38
     tiles, 741 tile pairs of 12,288 bytes) makes the launchers run bands of
