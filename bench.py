@@ -604,7 +604,8 @@ def summary(line, variants, surrogate, sigma32k, batched):
     JSON line so that a reader of the line's end sees both halves of the metric
     (FP64 plain and FP32 + surrogate), their errors and roofline fractions."""
     rf = line["roofline"]
-    out = {"fp64": {"pairs_per_s": _r(line["value"]), "e2e": _r(line["e2e"]["value"]), "frac_probe": _r(rf["frac"], 3),
+    out = {"fp64": {"mode": line.get("mode", "fp64").split(" ")[0],
+                    "pairs_per_s": _r(line["value"]), "e2e": _r(line["e2e"]["value"]), "frac_probe": _r(rf["frac"], 3),
                     "frac_pipe_rate": _r(rf["frac_pipe_rate"], 3), "probe_tflops": _r(rf["peak"]),
                     "pipe_rate_tflops": _r(rf["pipe_rate_peak"])}}
     par = line.get("parity_sample")
@@ -692,6 +693,12 @@ def main():
                          "workload, seg-seg forces from one untimed call; prints their JSON and exits (the command "
                          "the ncu captures of those kernels use)")
     ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--mode", default="fp64", choices=["fp64", "fp64_fast"],
+                    help="arithmetic of the timed FP64 steps: fp64 = the reference's rounding (strict), fp64_fast = "
+                         "the reformulated FP64 form (same parity bound)")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="only the timed steps (no e2e, variants or other rows): the command ncu captures of the "
+                         "FP64 tile kernel use")
     ap.add_argument("--no-sigma", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--sigma-grid", type=int, default=32)
@@ -759,6 +766,7 @@ def main():
     sptr = stream.cuda_stream
 
     # One reported call: branch statistics for the algorithmic FLOP count.
+    ctx.mode = args.mode
     rep = ctx.segseg_force_device(k, soa.data_ptr(), n, n, force.data_ptr(), stream=sptr, report=True)
     flops_per_step = (rep["pairs_general"] * OPS_GENERAL_PAIR + rep["pairs_parallel"] * OPS_PARALLEL_PAIR
                       + rep["core_sides"] * 2 * OPS_GENERAL_PAIR)
@@ -794,16 +802,30 @@ def main():
     if dist:
         dist.barrier()
     value = ws * pairs / (ms_step * 1e-3)
+    if args.headline_only:
+        if rank == 0:
+            print(json.dumps({"mode": args.mode, "value": value, "unit": "pair-interactions/s", "ms_per_step": ms_step,
+                              "segments": n, "steps": args.steps}), flush=True)
+        return
 
     # Other arithmetic modes of the same path, same workload and timing: the FMA
     # build of the FP64 kernel and the df64 precision form.  Each reports its
     # error against the strict FP64 result (itself parity-checked).
     variants = {}
-    ref_force = force.cpu().numpy().reshape(3, 2, -1, order="F")
+    ref_force = force.cpu().numpy().reshape(3, 2, -1, order="F")  # the timed mode's result
+    # The strict FP64 result (the reference's rounding): the errors of every
+    # other form are taken against it.
+    strict = force
+    if args.mode != "fp64":
+        ctx.mode = "fp64"
+        strict = torch.zeros_like(force)
+        ctx.segseg_force_device(k, soa.data_ptr(), n, n, strict.data_ptr(), stream=sptr)
+        torch.cuda.synchronize()
+    strict_force = strict.cpu().numpy().reshape(3, 2, -1, order="F")
     cs_v = clocks.summary()
     pipe_peak_v = 4.0 * n_sm * cs_v["sm_mhz"] * 1e6 if cs_v else None
     if not args.no_variants:
-        for mode in ("fp64_fast", "fp64_fma", "df64", "f32c"):
+        for mode in [m for m in ("fp64", "fp64_fast", "fp64_fma", "df64", "f32c") if m != args.mode]:
             ctx.mode = mode
             out_v = torch.zeros_like(force)
             with torch.cuda.stream(stream):
@@ -817,10 +839,10 @@ def main():
                     b_.record(stream)
                     torch.cuda.synchronize()
                     vms.append(a_.elapsed_time(b_))
-            ctx.mode = "fp64"
+            ctx.mode = args.mode
             Fv = out_v.cpu().numpy().reshape(3, 2, -1, order="F")
-            dn = np.linalg.norm(Fv - ref_force, axis=0)
-            fn = np.linalg.norm(ref_force, axis=0)
+            dn = np.linalg.norm(Fv - strict_force, axis=0)
+            fn = np.linalg.norm(strict_force, axis=0)
             variants[mode] = {
                 "value": pairs / (statistics.mean(vms) * 1e-3), "unit": "pair-interactions/s",
                 "ms_per_step": statistics.mean(vms),
@@ -828,17 +850,21 @@ def main():
                 "frac_fp64_peak_algorithmic": flops_per_step / (statistics.mean(vms) * 1e-3) / fp64_peak,
                 "frac_pipe_rate_algorithmic": (flops_per_step / (statistics.mean(vms) * 1e-3) / pipe_peak_v
                                                if pipe_peak_v else None),
-                "error_vs_fp64": {"rel_rms": float(np.linalg.norm(Fv - ref_force) / np.linalg.norm(ref_force)),
+                "error_vs_fp64": {"rel_rms": float(np.linalg.norm(Fv - strict_force) / np.linalg.norm(strict_force)),
                                   "max_node_over_max_force": float(dn.max() / fn.max()),
                                   "max_rel_node": float(np.max(dn / np.maximum(fn, 1e-300)))},
                 "branches_match_fp64": (rep_v["pairs_general"], rep_v["pairs_parallel"]) ==
                                        (rep["pairs_general"], rep["pairs_parallel"]),
             }
 
+    # The rows below run in the reference's rounding unless they set a mode.
+    ctx.mode = "fp64"
+    ms_strict = ms_step if args.mode == "fp64" else variants.get("fp64", {}).get("ms_per_step")
+
     # Learned far-field surrogate ("FP32+surrogate"), same workload and timing.
     surrogate = None
     if not args.no_surrogate:
-        surrogate = run_surrogate(args, pkg, ctx, k, soa, force, pairs, ms_step, stream, sptr, flush)
+        surrogate = run_surrogate(args, pkg, ctx, k, soa, strict, pairs, ms_strict or ms_step, stream, sptr, flush)
         peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
         if os.path.exists(peaks_path):
             tp = json.load(open(peaks_path)).get("bf16_tflops")
@@ -955,9 +981,11 @@ def main():
                                  "bit_equal": bool(torch.equal(bforce, bref))}}
             plan.close()
 
-    # End to end through the reference-facing C-ABI call with host arrays.
+    # End to end through the reference-facing C-ABI call with host arrays, in
+    # the timed steps' mode.
     coord, bvec, seg = synth.network_arrays(p, b)
     net = pkg.DislocationNetwork(coord, bvec, seg)
+    ctx.mode = args.mode
     e2e_steps = args.e2e_steps if args.e2e_steps is not None else max(1, min(args.steps, 3))
     pkg_ctx = ctx
     pkg_ctx.segseg_force(k, net)  # warm-up
@@ -970,6 +998,7 @@ def main():
     e2e_value = ws * pairs / t_e2e
     # Same forces as the device-resident path.
     same = bool(np.array_equal(out.ravel(order="F"), force.cpu().numpy()))
+    ctx.mode = "fp64"
 
     if rank != 0:
         return
@@ -1009,7 +1038,7 @@ def main():
                      "traffic": TILE_DRAM_BYTES_PER_TILE_PAIR * (n // 128) * (n // 128 + 1) // 2,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at 32,768 "
                                        "segments, scaled by tile pairs",
-                     "kernel": "segseg_tile_f64<0>",
+                     "kernel": "segseg_tile_f64<0>" if args.mode == "fp64" else "segseg_tile_fx<0>",
                      "peak_source": "measured FP64 FMA-chain probe on this GPU (ddd_probe_fma_peak, ~1 s per "
                                     "timing, best of 3); MEASURED_PEAKS.json holds no FP64 figure",
                      "probe_clock": probe_clock,
@@ -1021,7 +1050,10 @@ def main():
         "e2e": {"value": e2e_value, "unit": "pair-interactions/s", "h2d_bytes_per_step": erep["h2d_bytes"],
                 "d2h_bytes_per_step": erep["d2h_bytes"], "steps": e2e_steps, "matches_device_path": same},
         "gpu_launches": 3 * args.steps,
-        "mode": "fp64 (strict: every multiply and add rounded separately, as the reference)",
+        "mode": {"fp64": "fp64 (strict: every multiply and add rounded separately, as the reference)",
+                 "fp64_fast": "fp64_fast (FP64 throughout, reformulated: one division per corner, table-driven "
+                              "log/atan, explicit FMAs where the reference's terms do not cancel; same parity bound "
+                              "as the strict form, checked below)"}[args.mode],
         "variants": variants,
         "surrogate": surrogate,
         "precision_131k": precision131k,

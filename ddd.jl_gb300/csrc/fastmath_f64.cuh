@@ -130,7 +130,11 @@ FM_HD double atan(double z) {
   if (!(a <= 1.0e300)) return std_atan(z);  // inf, NaN
   const bool big = a > 1.0;
   const float af = (float)a;
+#if defined(__CUDA_ARCH__)
+  const float w = big ? __frcp_rn(af) : af;  // correctly rounded: the host's 1.0f / af
+#else
   const float w = big ? 1.0f / af : af;
+#endif
   const int j = (int)(w * 16.0f + 0.5f);    // 0..16
   const fm_d3 T = big ? ld(&kAtanCompC[j]) : ld(&kAtanC[j]);
   const double num = big ? fma_(-a, T.c, 1.0) : a - T.c;

@@ -211,6 +211,62 @@ def test_trained_surrogate_accuracy_and_gain(pkg, synth, trained):
     assert torch.equal(F, F2)  # deterministic
 
 
+def test_committed_checkpoint_gain_over_f32c_exact(pkg, synth):
+    """What the learned part gains over the method without it.  The committed
+    checkpoint (trained on four other networks of the workload's generator)
+    on a 32,768-segment network of that generator: the surrogate with f32c
+    exact passes must beat the f32c exact kernel alone (the same arithmetic
+    for every pair, no network) in device time, at <= 1e-4 node-force relative
+    RMS error against the strict FP64 forces (the bench measures ~3x at 65,536
+    segments, 2.5e-5)."""
+    import ddd_gb300
+
+    path = os.path.join(os.path.dirname(ddd_gb300.__file__), "data", "surrogate_gpu65k_nu028.bin")
+    ctx = pkg.get_context()
+    sur = pkg.Surrogate(ctx, seed=0).load(path)
+    net, segs = _network(pkg, synth, 4096, seed=0)
+    k = _k(pkg)
+    n = segs.shape[1]
+    d = torch.from_numpy(segs).cuda()
+    ref = torch.zeros((n, 6), dtype=torch.float64, device="cuda")
+    ctx.segseg_force_device(k, d.data_ptr(), n, n, ref.data_ptr())
+    ex = torch.zeros_like(ref)
+    st = torch.cuda.current_stream()
+
+    def timed(fn, reps=2):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        for _ in range(reps):
+            fn()
+        b.record(st)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    ctx.mode = "f32c"
+    try:
+        ms_f32c = timed(lambda: ctx.segseg_force_device(k, d.data_ptr(), n, n, ex.data_ptr(),
+                                                        stream=st.cuda_stream))
+    finally:
+        ctx.mode = "fp64"
+    out = {}
+
+    def run_sur():
+        out["F"], out["rep"] = sur.force(k, d, exact_mode="f32c", stream=st.cuda_stream)
+
+    ms_sur = timed(run_sur)
+    err = (torch.linalg.norm(out["F"] - ref) / torch.linalg.norm(ref)).item()
+    err_f32c = (torch.linalg.norm(ex - ref) / torch.linalg.norm(ref)).item()
+    if os.environ.get("DDD_TEST_STATS"):
+        with open(os.environ["DDD_TEST_STATS"], "a") as fh:
+            fh.write("gain over f32c exact: %.1f ms vs %.1f ms, err %.3e (f32c %.3e)\n" % (ms_sur, ms_f32c, err,
+                                                                                         err_f32c))
+    assert out["rep"]["fallback"] == 0
+    assert err <= 1e-4, err
+    assert ms_sur < ms_f32c, (ms_sur, ms_f32c)
+
+
 def test_host_array_entry_matches_device_form(pkg, synth, trained):
     # ddd_surrogate_force_host takes the network's own arrays (the
     # ddd_segseg_force layout, extSeg per segment row): same result, bit for bit.
