@@ -54,11 +54,11 @@ FM_HD double at(double v) {
 }
 
 // SegSegInteg at one corner (DislocationForces.jl:1480-1561), added (sm = 0) or
-// subtracted (sm = sign bit) into integ[19].  aSq_dSq, aSq_dSqI = 1/aSq_dSq and
-// den = 1/sqrt((1 - c^2) aSq_dSq) are per pair.
+// subtracted (sm = sign bit) into integ[19].  aSq_dSq and den =
+// 1/sqrt((1 - c^2) aSq_dSq) are per pair.
 template <bool FMATH>
-FM_HD void corner(double aSq_dSq, double aSq_dSqI, double den, double c, double cSq, double omcSqI, double x, double y,
-                  long long sm, double* integ) {
+FM_HD void corner(double aSq_dSq, double den, double c, double cSq, double omcSqI, double x, double y, long long sm,
+                  double* integ) {
   const double xSq = x * x;
   const double ySq = y * y;
   const double Ra = sqrt(aSq_dSq + xSq + ySq + 2.0 * x * y * c);
@@ -99,27 +99,21 @@ FM_HD void corner(double aSq_dSq, double aSq_dSqI, double den, double c, double 
   integ[3] += sgn(integ4, sm);
   integ[4] += sgn(integ5, sm);
   integ[5] += sgn(integ6, sm);
-  integ[6] += sgn((integ1 - xS1 - yS2) * aSq_dSqI, sm);
-  integ[7] += sgn(fm::fma_(-c, S2, S1) * omcSqI, sm);
-  integ[8] += sgn(fm::fma_(-c, S1, S2) * omcSqI, sm);
-  integ[9] += sgn(fm::fma_(-c, xS1 + yS2 + integ1, RaInv) * omcSqI, sm);
-  integ[10] += sgn(fm::fma_(cSq, yS2, xS1 + c_11_12) * omcSqI, sm);
-  integ[11] += sgn(fm::fma_(cSq, xS1, yS2 + c_11_12) * omcSqI, sm);
-  integ[12] += sgn(fm::fma_(c, y_13_14 - integ2, integ3 - x_13_14) * omcSqI, sm);
-  integ[13] += sgn(fm::fma_(c, x_13_14 - integ3, integ2 - y_13_14) * omcSqI, sm);
-  integ[14] += sgn(fm::fma_(c, fm::fma_(xSq, c_15_18, -c15_18_19), integ5 - z_15_18) * omcSqI, sm);
-  integ[15] += sgn(fm::fma_(c, c_16, fm::fma_(2.0, integ2, xxS1)) * omcSqI, sm);
-  integ[16] += sgn(fm::fma_(c, c_17_19, fm::fma_(2.0, integ3, yyS2)) * omcSqI, sm);
-  integ[17] += sgn(fm::fma_(c, z_15_18 - integ5, fm::fma_(-xSq, c_15_18, c15_18_19)) * omcSqI, sm);
-  integ[18] += sgn(fm::fma_(c, fm::fma_(x, c_17_19, -integ6), fm::fma_(-ySq, c_19, c15_18_19)) * omcSqI, sm);
-}
-
-// sum_k V[k] F[k] with fused products.
-FM_HD X3 fsum11(const X3* V, const double* F) {
-  X3 s = V[0] * F[0];
-#pragma unroll
-  for (int k = 1; k < 11; ++k) s = fmv(F[k], V[k], s);
-  return s;
+  // integ[6] and integ[7..18] accumulate their numerators: the caller scales
+  // the four-corner sums by 1/aSq_dSq and 1/(1 - c^2) once.
+  integ[6] += sgn(integ1 - xS1 - yS2, sm);
+  integ[7] += sgn(fm::fma_(-c, S2, S1), sm);
+  integ[8] += sgn(fm::fma_(-c, S1, S2), sm);
+  integ[9] += sgn(fm::fma_(-c, xS1 + yS2 + integ1, RaInv), sm);
+  integ[10] += sgn(fm::fma_(cSq, yS2, xS1 + c_11_12), sm);
+  integ[11] += sgn(fm::fma_(cSq, xS1, yS2 + c_11_12), sm);
+  integ[12] += sgn(fm::fma_(c, y_13_14 - integ2, integ3 - x_13_14), sm);
+  integ[13] += sgn(fm::fma_(c, x_13_14 - integ3, integ2 - y_13_14), sm);
+  integ[14] += sgn(fm::fma_(c, fm::fma_(xSq, c_15_18, -c15_18_19), integ5 - z_15_18), sm);
+  integ[15] += sgn(fm::fma_(c, c_16, fm::fma_(2.0, integ2, xxS1)), sm);
+  integ[16] += sgn(fm::fma_(c, c_17_19, fm::fma_(2.0, integ3, yyS2)), sm);
+  integ[17] += sgn(fm::fma_(c, z_15_18 - integ5, fm::fma_(-xSq, c_15_18, c15_18_19)), sm);
+  integ[18] += sgn(fm::fma_(c, fm::fma_(x, c_17_19, -integ6), fm::fma_(-ySq, c_19, c15_18_19)), sm);
 }
 
 // General branch of calcSegSegForce; NEED12 / NEED34 as in pair_f64.cuh.
@@ -190,45 +184,82 @@ FM_HD void general_pair(const KFast& K, X3 b1, X3 n11, X3 n12, X3 t1, double t1N
     const double x = (q & 2) ? x2 : x1;
     const double y = (q & 1) ? y2 : y1;
     const long long sm = (q == 1 || q == 2) ? (long long)0x8000000000000000ULL : 0LL;
-    corner<FMATH>(aSq_dSq, aSq_dSqI, den, c, cSq, omcSqI, x, y, sm, integ);
+    corner<FMATH>(aSq_dSq, den, c, cSq, omcSqI, x, y, sm, integ);
   }
+  integ[6] *= aSq_dSqI;
+#pragma unroll
+  for (int k = 7; k < 19; ++k) integ[k] *= omcSqI;
 
-  X3 V[11];
+  // Force assembly.  The reference forms 11 vectors V[k] per side and sums
+  // V[k] Fi[k] (DislocationForces.jl:953-1145); every V[k] is a combination of
+  // five vectors (side 1: A = t2 x t1, B = b1 x t1, C = b2 - (t1.b2) t1,
+  // D = (t1.b2) t2 - c b2, E = t2 - c t1; side 2: A, B = b2 x t2,
+  // G = (t2.b1) t1 - c b1, H = t1 - c t2, K = b1 - (t2.b1) t2), so each node's
+  // force is sum_m e_m (sum_k s_km Fi[k]): the scalar coefficients s_km first,
+  // then five vector terms.
   double Fi[11];
   if (NEED12) {
-    double tmp1 = fm::fma_(t1db2, t2db1, t2ct1cb1db2);
-    const X3 V1 = tmp1 * t2ct1;
-    const X3 V2 = b1ct1 * t1ct2cb2dt2;
-    const X3 V3 = fmv(-t2db1, t1cb2ct1, t1ct2 * b1ct1db2);
-    const X3 V4 = -b1ct1 * t2ct1db2;
-    const X3 V5 = fmv(-b2ct2db1, t1ct2, b2ct2ct1 * t2db1);
-
-    double tmp2;
-    tmp1 = mu4pinud * t1ct2db1;
-    tmp2 = mu4pinud * b2ct2db1;
-    V[0] = fmv(tmp2, t1ct2ct1, fmv(tmp1, b2ct2ct1, fmv(-mu4pinud, V2, mu4pid * V1)));
-    tmp1 = mu4pinu * t2db1;
-    tmp2 = mu4pinu * b2ct2db1;
-    V[1] = fmv(tmp2, t1ct2, fmv(-tmp1, b2ct2ct1, mu4pi * V5));
-    tmp1 = mu4pinu * t1db1;
-    V[2] = fmv(-mu4pinu, V4, fmv(mu4pi, V3, -tmp1 * b2ct2ct1));
-    tmp1 = mu4pinudCu * t1ct2cb2dt2 * t1ct2db1;
-    V[3] = fmv(-tmp1, t1ct2ct1, fmv(-mu4pinuaSqd, V2, mu8piaSqd * V1));
-    tmp1 = mu4pinudSq * t1ct2cb2dt2 * t2db1;
-    tmp2 = mu4pinudSq * t1ct2cb2dt2 * t1ct2db1;
-    V[4] = fmv(-tmp2, t1ct2, fmv(tmp1, t1ct2ct1, mu8piaSq * V5));
-    tmp1 = mu4pinudSq * fm::fma_(t2ct1db2, t1ct2db1, t1ct2cb2dt2 * t1db1);
-    V[5] = fmv(tmp1, t1ct2ct1, fmv(-mu4pinuaSq, V4, mu8piaSq * V3));
-    tmp1 = mu4pinud * fm::fma_(t1ct2cb2dt2, t1db1, t2ct1db2 * t1ct2db1);
-    tmp2 = mu4pinud * t2ct1db2 * t2db1;
-    V[6] = fmv(-tmp2, t1ct2ct1, tmp1 * t1ct2);
-    tmp1 = mu4pinud * t1ct2cb2dt2 * t2db1;
-    V[7] = tmp1 * t1ct2;
-    tmp1 = mu4pinud * t2ct1db2 * t1db1;
-    V[8] = -tmp1 * t1ct2ct1;
-    const X3 tv = mu4pinu * t2ct1db2 * t1ct2;
-    V[9] = -tv * t2db1;
-    V[10] = -tv * t1db1;
+    const X3& A = t2ct1;
+    const X3& B = b1ct1;
+    const X3& C = t1cb2ct1;
+    const X3& D = b2ct2ct1;
+    const X3& E = t1ct2ct1;
+    const double p1 = fm::fma_(t1db2, t2db1, t2ct1cb1db2);  // V1 = p1 A
+    const double p2 = t1ct2cb2dt2;                           // V2 = p2 B
+    const double p3a = -b1ct1db2, p3c = -t2db1;              // V3 = p3a A + p3c C
+    const double p4 = -t2ct1db2;                             // V4 = p4 B
+    const double p5d = t2db1, p5a = b2ct2db1;                // V5 = p5d D + p5a A
+    const double r3 = mu4pinudCu * t1ct2cb2dt2 * t1ct2db1;
+    const double r4a = mu4pinudSq * t1ct2cb2dt2 * t2db1;
+    const double r4b = mu4pinudSq * t1ct2cb2dt2 * t1ct2db1;
+    const double r5 = mu4pinudSq * fm::fma_(t2ct1db2, t1ct2db1, t1ct2cb2dt2 * t1db1);
+    const double r6a = mu4pinud * fm::fma_(t1ct2cb2dt2, t1db1, t2ct1db2 * t1ct2db1);
+    const double r6b = mu4pinud * t2ct1db2 * t2db1;
+    const double r7 = mu4pinud * t1ct2cb2dt2 * t2db1;
+    const double r8 = mu4pinud * t2ct1db2 * t1db1;
+    const double r9 = mu4pinu * t2ct1db2 * t2db1;
+    const double r10 = mu4pinu * t2ct1db2 * t1db1;
+    // s_km of V[0..10] on A, B, C, D, E.
+    const double a0 = mu4pid * p1, a1 = fm::fma_(mu4pi, p5a, -mu4pinu * b2ct2db1), a2 = mu4pi * p3a,
+                 a3 = mu8piaSqd * p1, a4 = fm::fma_(mu8piaSq, p5a, r4b), a5 = mu8piaSq * p3a;
+    const double b0 = -mu4pinud * p2, b2 = -mu4pinu * p4, b3 = -mu4pinuaSqd * p2, b5 = -mu4pinuaSq * p4;
+    const double c2 = mu4pi * p3c, c5 = mu8piaSq * p3c;
+    const double d0 = mu4pinud * t1ct2db1, d1 = fm::fma_(mu4pi, p5d, -mu4pinu * t2db1), d2 = -mu4pinu * t1db1,
+                 d4 = mu8piaSq * p5d;
+    const double e0 = mu4pinud * b2ct2db1;
+    auto node = [&](double tN) {
+      double al = Fi[0] * a0;
+      al = fm::fma_(Fi[1], a1, al);
+      al = fm::fma_(Fi[2], a2, al);
+      al = fm::fma_(Fi[3], a3, al);
+      al = fm::fma_(Fi[4], a4, al);
+      al = fm::fma_(Fi[5], a5, al);
+      al = fm::fma_(Fi[6], -r6a, al);
+      al = fm::fma_(Fi[7], -r7, al);
+      al = fm::fma_(Fi[9], r9, al);
+      al = fm::fma_(Fi[10], r10, al);
+      double be = Fi[0] * b0;
+      be = fm::fma_(Fi[2], b2, be);
+      be = fm::fma_(Fi[3], b3, be);
+      be = fm::fma_(Fi[5], b5, be);
+      const double ga = fm::fma_(Fi[2], c2, Fi[5] * c5);
+      double de = Fi[0] * d0;
+      de = fm::fma_(Fi[1], d1, de);
+      de = fm::fma_(Fi[2], d2, de);
+      de = fm::fma_(Fi[4], d4, de);
+      double ep = Fi[0] * e0;
+      ep = fm::fma_(Fi[3], -r3, ep);
+      ep = fm::fma_(Fi[4], r4a, ep);
+      ep = fm::fma_(Fi[5], r5, ep);
+      ep = fm::fma_(Fi[6], -r6b, ep);
+      ep = fm::fma_(Fi[8], -r8, ep);
+      X3 f = al * A;
+      f = fmv(be, B, f);
+      f = fmv(ga, C, f);
+      f = fmv(de, D, f);
+      f = fmv(ep, E, f);
+      return f * tN;
+    };
 
     const double y2_ = -y2;
     Fi[0] = fm::fma_(y2_, integ[0], integ[2]);
@@ -242,7 +273,7 @@ FM_HD void general_pair(const KFast& K, X3 b1, X3 n11, X3 n12, X3 t1, double t1N
     Fi[8] = fm::fma_(y2_, integ[11], integ[16]);
     Fi[9] = fm::fma_(y2_, integ[12], integ[14]);
     Fi[10] = fm::fma_(y2_, integ[13], integ[18]);
-    F1 = fsum11(V, Fi) * t1N;
+    F1 = node(t1N);
 
     Fi[0] = fm::fma_(y1, integ[0], -integ[2]);
     Fi[1] = fm::fma_(y1, integ[1], -integ[3]);
@@ -255,42 +286,70 @@ FM_HD void general_pair(const KFast& K, X3 b1, X3 n11, X3 n12, X3 t1, double t1N
     Fi[8] = fm::fma_(y1, integ[11], -integ[16]);
     Fi[9] = fm::fma_(y1, integ[12], -integ[14]);
     Fi[10] = fm::fma_(y1, integ[13], -integ[18]);
-    F2 = fsum11(V, Fi) * t1N;
+    F2 = node(t1N);
   }
   if (NEED34) {
-    double tmp1 = fm::fma_(t2db1, t1db2, t2ct1cb1db2);
-    const X3 V1 = tmp1 * t1ct2;
-    const X3 V2 = b2ct2 * t2ct1cb1dt1;
-    const X3 V3 = fmv(-t1db2, b1ct1ct2, t2ct1 * b1ct1db2);
-    const X3 V5 = fmv(-b2ct2db1, t2ct1, t2cb1ct2 * t1db2);
-    const X3 V6 = b2ct2 * t1ct2db1;
-
-    double tmp2;
-    tmp1 = mu4pinud * t2ct1db2;
-    tmp2 = mu4pinud * b1ct1db2;
-    V[0] = fmv(tmp2, t2ct1ct2, fmv(tmp1, b1ct1ct2, fmv(-mu4pinud, V2, mu4pid * V1)));
-    tmp1 = mu4pinu * t2db2;
-    V[1] = fmv(-mu4pinu, V6, fmv(mu4pi, V5, tmp1 * b1ct1ct2));
-    tmp1 = mu4pinu * t1db2;
-    tmp2 = mu4pinu * b1ct1db2;
-    V[2] = fmv(-tmp2, t2ct1, fmv(tmp1, b1ct1ct2, mu4pi * V3));
-    tmp1 = mu4pinudCu * t2ct1cb1dt1 * t2ct1db2;
-    V[3] = fmv(-tmp1, t2ct1ct2, fmv(-mu4pinuaSqd, V2, mu8piaSqd * V1));
-    tmp1 = mu4pinudSq * fm::fma_(t1ct2db1, t2ct1db2, t2ct1cb1dt1 * t2db2);
-    V[4] = fmv(-tmp1, t2ct1ct2, fmv(-mu4pinuaSq, V6, mu8piaSq * V5));
-    tmp1 = mu4pinudSq * t2ct1cb1dt1 * t1db2;
-    tmp2 = mu4pinudSq * t2ct1cb1dt1 * t2ct1db2;
-    V[5] = fmv(tmp2, t2ct1, fmv(-tmp1, t2ct1ct2, mu8piaSq * V3));
-    tmp1 = mu4pinud * fm::fma_(t2ct1cb1dt1, t2db2, t1ct2db1 * t2ct1db2);
-    tmp2 = mu4pinud * t1ct2db1 * t1db2;
-    V[6] = fmv(-tmp2, t2ct1ct2, tmp1 * t2ct1);
-    tmp1 = mu4pinud * t1ct2db1 * t2db2;
-    V[7] = -tmp1 * t2ct1ct2;
-    tmp1 = mu4pinud * t2ct1cb1dt1 * t1db2;
-    V[8] = tmp1 * t2ct1;
-    const X3 tv = mu4pinu * t1ct2db1 * t2ct1;
-    V[9] = tv * t2db2;
-    V[10] = tv * t1db2;
+    const X3& A = t2ct1;
+    const X3& B = b2ct2;
+    const X3& G = b1ct1ct2;
+    const X3& H = t2ct1ct2;
+    const X3& Kv = t2cb1ct2;
+    const double p1 = -fm::fma_(t2db1, t1db2, t2ct1cb1db2);  // V1 = p1 A
+    const double p2 = t2ct1cb1dt1;                            // V2 = p2 B
+    const double p3a = b1ct1db2, p3g = -t1db2;                // V3 = p3a A + p3g G
+    const double p5k = t1db2, p5a = -b2ct2db1;                // V5 = p5k K + p5a A
+    const double p6 = t1ct2db1;                               // V6 = p6 B
+    const double r3 = mu4pinudCu * t2ct1cb1dt1 * t2ct1db2;
+    const double r4 = mu4pinudSq * fm::fma_(t1ct2db1, t2ct1db2, t2ct1cb1dt1 * t2db2);
+    const double r5a = mu4pinudSq * t2ct1cb1dt1 * t1db2;
+    const double r5b = mu4pinudSq * t2ct1cb1dt1 * t2ct1db2;
+    const double r6a = mu4pinud * fm::fma_(t2ct1cb1dt1, t2db2, t1ct2db1 * t2ct1db2);
+    const double r6b = mu4pinud * t1ct2db1 * t1db2;
+    const double r7 = mu4pinud * t1ct2db1 * t2db2;
+    const double r8 = mu4pinud * t2ct1cb1dt1 * t1db2;
+    const double r9 = mu4pinu * t1ct2db1 * t2db2;
+    const double r10 = mu4pinu * t1ct2db1 * t1db2;
+    // s_km of V[0..10] on A, B, G, H, K.
+    const double a0 = mu4pid * p1, a1 = mu4pi * p5a, a2 = fm::fma_(mu4pi, p3a, -mu4pinu * b1ct1db2),
+                 a3 = mu8piaSqd * p1, a4 = mu8piaSq * p5a, a5 = fm::fma_(mu8piaSq, p3a, r5b);
+    const double b0 = -mu4pinud * p2, b1 = -mu4pinu * p6, b3 = -mu4pinuaSqd * p2, b4 = -mu4pinuaSq * p6;
+    const double g0 = mu4pinud * t2ct1db2, g1 = mu4pinu * t2db2, g2 = fm::fma_(mu4pi, p3g, mu4pinu * t1db2),
+                 g5 = mu8piaSq * p3g;
+    const double h0 = mu4pinud * b1ct1db2;
+    const double k1 = mu4pi * p5k, k4 = mu8piaSq * p5k;
+    auto node = [&](double tN) {
+      double al = Fi[0] * a0;
+      al = fm::fma_(Fi[1], a1, al);
+      al = fm::fma_(Fi[2], a2, al);
+      al = fm::fma_(Fi[3], a3, al);
+      al = fm::fma_(Fi[4], a4, al);
+      al = fm::fma_(Fi[5], a5, al);
+      al = fm::fma_(Fi[6], r6a, al);
+      al = fm::fma_(Fi[8], r8, al);
+      al = fm::fma_(Fi[9], r9, al);
+      al = fm::fma_(Fi[10], r10, al);
+      double be = Fi[0] * b0;
+      be = fm::fma_(Fi[1], b1, be);
+      be = fm::fma_(Fi[3], b3, be);
+      be = fm::fma_(Fi[4], b4, be);
+      double ge = Fi[0] * g0;
+      ge = fm::fma_(Fi[1], g1, ge);
+      ge = fm::fma_(Fi[2], g2, ge);
+      ge = fm::fma_(Fi[5], g5, ge);
+      double he = Fi[0] * h0;
+      he = fm::fma_(Fi[3], -r3, he);
+      he = fm::fma_(Fi[4], -r4, he);
+      he = fm::fma_(Fi[5], -r5a, he);
+      he = fm::fma_(Fi[6], -r6b, he);
+      he = fm::fma_(Fi[7], -r7, he);
+      const double ka = fm::fma_(Fi[1], k1, Fi[4] * k4);
+      X3 f = al * A;
+      f = fmv(be, B, f);
+      f = fmv(ge, G, f);
+      f = fmv(he, H, f);
+      f = fmv(ka, Kv, f);
+      return f * tN;
+    };
 
     Fi[0] = fm::fma_(x2, integ[0], -integ[1]);
     Fi[1] = fm::fma_(x2, integ[1], -integ[4]);
@@ -303,7 +362,7 @@ FM_HD void general_pair(const KFast& K, X3 b1, X3 n11, X3 n12, X3 t1, double t1N
     Fi[8] = fm::fma_(x2, integ[11], -integ[13]);
     Fi[9] = fm::fma_(x2, integ[12], -integ[17]);
     Fi[10] = fm::fma_(x2, integ[13], -integ[14]);
-    F3 = fsum11(V, Fi) * t2N;
+    F3 = node(t2N);
 
     const double x1_ = -x1;
     Fi[0] = fm::fma_(x1_, integ[0], integ[1]);
@@ -317,7 +376,7 @@ FM_HD void general_pair(const KFast& K, X3 b1, X3 n11, X3 n12, X3 t1, double t1N
     Fi[8] = fm::fma_(x1_, integ[11], integ[13]);
     Fi[9] = fm::fma_(x1_, integ[12], integ[17]);
     Fi[10] = fm::fma_(x1_, integ[13], integ[14]);
-    F4 = fsum11(V, Fi) * t2N;
+    F4 = node(t2N);
   }
 }
 

@@ -1,6 +1,6 @@
 // Displacements of the FE nodes from the dislocation network (calc_uTilde /
-// calc_uTilde!, DislocationFEM.jl:354-632) by Barnett triangles
-// (calcDisplacementDislocationTriangle!, :634-751; Bromage & Tarleton 2018),
+// calc_uTilde!, DislocationFEM.jl:355-581) by Barnett triangles
+// (calcDisplacementDislocationTriangle!, :600-707; Bromage & Tarleton 2018),
 // strict FP64 (compiled with --fmad=false; the host part with
 // -ffp-contract=off).
 //

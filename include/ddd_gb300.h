@@ -241,7 +241,7 @@ int ddd_detect_collision(ddd_ctx* ctx, double collisionDistSq, const double* coo
 int ddd_minimum_distance(ddd_ctx* ctx, const double* pts, int64_t n, double* out);
 
 /* calc_uTilde(mesh, boundaries, matParams, network) and calc_uTilde!(...) —
- * src/Processing/DislocationFEM.jl:354-632 (Barnett triangles :634-751): the
+ * src/Processing/DislocationFEM.jl:355-581 (Barnett triangles :600-707): the
  * displacement the network causes at the FE nodes with applied displacements.
  * Each internal segment is closed on C (a full triangle, with the f and g
  * terms); a segment with an external node (label extDln = 5) is closed through

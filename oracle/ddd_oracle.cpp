@@ -379,7 +379,7 @@ void oracle_detect_collision(double collisionDistSq, const double* coord, const 
   for (int k = 0; k < 5; ++k) dout[k] = dv[k];
 }
 
-// calc_uTilde (DislocationFEM.jl:354-632) at numPoints points (3 × M): u (3 × M)
+// calc_uTilde (DislocationFEM.jl:355-581) at numPoints points (3 × M): u (3 × M)
 // summed over the triangles in the reference's order for each point.  k2 =
 // (omνInv8π, om2νomνInv8π); box = (lo xyz, hi xyz); C the closure point.  Points
 // are split over nthreads (each point's sum keeps its order).  Returns the

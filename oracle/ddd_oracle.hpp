@@ -24,7 +24,7 @@
 //   src/Processing/DislocationFEM.jl:86-303       _calc_σTilde!
 //   src/Misc/Misc.jl:314-367                      minimumDistance
 //   src/Processing/DislocationTopologyCollision.jl:1-221  detectCollision
-//   src/Processing/DislocationFEM.jl:354-751      calc_uTilde, Barnett triangles
+//   src/Processing/DislocationFEM.jl:355-707      calc_uTilde, Barnett triangles
 #pragma once
 #include <cmath>
 #include <cstdint>
@@ -1106,7 +1106,7 @@ Collision detect_collision(T collisionDistSq, const T* coord, const T* nodeVel, 
 }
 
 // ---------------------------------------------------------------------------
-// calc_uTilde (DislocationFEM.jl:354-632): displacements at FE nodes from
+// calc_uTilde (DislocationFEM.jl:355-581): displacements at FE nodes from
 // Barnett triangles (Bromage & Tarleton 2018) closing each segment on a point.
 
 // safeNorm (Misc.jl:289-300): returns |x| and normalises x, or eps and zero.
@@ -1131,8 +1131,8 @@ template <class T> inline T jl_max0(T x) { return std::isnan(x) ? x : ((x < T(0)
 template <class T> inline T clamp11(T x) { return x > T(1) ? T(1) : (x < T(-1) ? T(-1) : x); }
 
 // One triangle ABC with Burgers vector b; full = the form with matParams
-// (solid angle, f and g terms, DislocationFEM.jl:651-707), else the solid-angle
-// form (:708-751).  AB, BC, CA are the safeNorm'ed edge directions.
+// (solid angle, f and g terms, DislocationFEM.jl:600-660), else the solid-angle
+// form (:661-707).  AB, BC, CA are the safeNorm'ed edge directions.
 template <class T> struct UTri {
   V3<T> A, B, C, b, AB, BC, CA;
   bool full;

@@ -272,7 +272,7 @@ def u_tilde_case(fixtures):
 
 
 def test_u_tilde_matches_golden(oracle, fixtures):
-    """calc_uTilde (DislocationFEM.jl:354-751) against
+    """calc_uTilde (DislocationFEM.jl:355-707) against
     test/DislocationFEMTest.jl:270-1000 (the test's rtol is 5e-5; the restatement
     agrees to 1e-12), and calc_uTilde!'s full vector through uDofsDln."""
     mesh, net, nodes, dofs, k2 = u_tilde_case(fixtures)
