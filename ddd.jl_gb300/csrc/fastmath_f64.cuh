@@ -8,19 +8,19 @@
 // Methods (published, restated):
 //   log: P. T. P. Tang, "Table-driven implementation of the logarithm function
 //        in IEEE floating-point arithmetic", ACM TOMS 16 (1990): v = 2^k m,
-//        m reduced by a table point c_j = 1 + j/128 to r = (m - c_j)/c_j with
-//        |r| <= 2^-8, log v = k ln2 + ln c_j + log1p(r), log1p by its Taylor
-//        series to r^7 (truncation < 2^-59 relative).  m is kept in
+//        m reduced by a table point c_j = 1 + j/256 to r = (m - c_j)/c_j with
+//        |r| <= 2^-9, log v = k ln2 + ln c_j + log1p(r), log1p by its Taylor
+//        series to r^6 (truncation < 2^-56 relative).  m is kept in
 //        [sqrt(1/2), sqrt(2)) (the table then holds ln(c_j / 2) for the upper
 //        half) so that k ln2 and ln c_j never cancel near v = 1.  The part of
 //        (m - c_j)/c_j lost by rounding r is recovered with one FMA
 //        (remainder m - c_j - c_j r) and added to the tail.
 //   atan: |z| > 1 by atan z = pi/2 - atan(1/z); the argument (z or 1/z) is
-//        reduced by a table point c_j = j/16 through the addition formula
+//        reduced by a table point c_j = j/64 through the addition formula
 //        atan w = atan c_j + atan((w - c_j)/(1 + w c_j)), written for the
 //        |z| > 1 case as (1 - |z| c_j)/(|z| + c_j) so that one division serves
-//        both; |u| <= 1/32 and the odd Taylor series to u^11 (truncation
-//        < 2^-63 relative).  The table index comes from an FP32 estimate: any
+//        both; |u| <= 1/128 and the odd Taylor series to u^7 (truncation
+//        < 2^-59 relative).  The table index comes from an FP32 estimate: any
 //        nearby index is exact algebra, only |u| depends on it.
 // Out-of-range arguments (log of a non-positive, subnormal, infinite or NaN
 // value; atan of an infinity or NaN) go to the standard functions.
@@ -100,11 +100,11 @@ FM_HD double log(double v) {
   const int hi = (int)(bits >> 32);
   if (hi < 0x00100000 || hi >= 0x7ff00000) return std_log(v);  // <= 0, subnormal, inf, NaN
   const int mh = hi & 0x000FFFFF;
-  const int j = (mh + 0x1000) >> 13;       // c_j = 1 + j/128 nearest to m = 1 + f
+  const int j = (mh + 0x800) >> 12;        // c_j = 1 + j/256 nearest to m = 1 + f
   const bool half = mh >= 0x6A09E;          // m >= sqrt(2): log(m/2) + (k + 1) ln2
   const int k = (hi >> 20) - 1023 + (half ? 1 : 0);
   const double m = as_d((bits & 0x000FFFFFFFFFFFFFLL) | 0x3FF0000000000000LL);
-  const double c = as_d(0x3FF0000000000000LL + ((long long)j << 45));
+  const double c = as_d(0x3FF0000000000000LL + ((long long)j << 44));
   const double ic = ld(&kLogInvC[j]);
   const double mc = m - c;                  // exact (Sterbenz)
   const double r = mc * ic;
@@ -113,8 +113,7 @@ FM_HD double log(double v) {
   const double kd = (double)k;
   const double hiP = fma_(kd, FM_LN2_HI, T.hi);  // k * LN2_HI exact
   const double loP = fma_(kd, FM_LN2_LO, T.lo);
-  double q = 1.0 / 7.0;
-  q = fma_(q, r, -1.0 / 6.0);
+  double q = -1.0 / 6.0;
   q = fma_(q, r, 1.0 / 5.0);
   q = fma_(q, r, -0.25);
   q = fma_(q, r, 1.0 / 3.0);
@@ -135,16 +134,13 @@ FM_HD double atan(double z) {
 #else
   const float w = big ? 1.0f / af : af;
 #endif
-  const int j = (int)(w * 16.0f + 0.5f);    // 0..16
+  const int j = (int)(w * 64.0f + 0.5f);    // 0..64
   const fm_d3 T = big ? ld(&kAtanCompC[j]) : ld(&kAtanC[j]);
   const double num = big ? fma_(-a, T.c, 1.0) : a - T.c;
   const double den = big ? a + T.c : fma_(a, T.c, 1.0);
   const double u = num / den;
   const double u2 = u * u;
-  double p = -1.0 / 11.0;
-  p = fma_(p, u2, 1.0 / 9.0);
-  p = fma_(p, u2, -1.0 / 7.0);
-  p = fma_(p, u2, 0.2);
+  double p = fma_(u2, -1.0 / 7.0, 0.2);
   p = fma_(p, u2, -1.0 / 3.0);
   const double s = fma_(u * u2, p, u);      // atan(u)
   const double r = big ? T.hi + (T.lo - s) : T.hi + (T.lo + s);

@@ -9,12 +9,17 @@
 //     becomes a product with its reciprocal, taken once per pair;
 //   * the logarithms and arctangents are the table-driven fm::log / fm::atan
 //     (fastmath_f64.cuh), or CUDA's, by the template flag FMATH;
-//   * explicit fused multiply-adds (fma_) in the corner terms and the force
-//     assembly.  Quantities that cancel keep the reference's separate rounding:
-//     c, 1 - c^2, the cross products and dots of the pair's geometry, the
-//     local coordinates d, x1, x2, y1, y2, the argument of Ra, and
-//     Ra + y + x c, Ra + x + y c — the terms whose rounding sets the
-//     reference's own error.
+//   * explicit fused multiply-adds (fma_) in the corner terms, the products of
+//     unit and Burgers vectors, and the force assembly, which is regrouped on
+//     five vectors per side;
+//   * the terms whose rounding sets the reference's own error keep its
+//     separate rounding: c, 1 - c^2, d, the local coordinates x1, x2, y1, y2
+//     (R.t and (lim - c lim) / (1 - c^2)), the argument of Ra, and
+//     Ra + y + x c, Ra + x + y c.  Measured on a CPU against long double: with
+//     these kept, the node-force error is the reference arithmetic's own
+//     (1.00-1.01x); fusing the local coordinates as well makes the result
+//     more accurate than the reference (0.6x its error on sparse networks) but
+//     moves it ~3e-10 away from the reference's values, past the parity bound.
 // Everything else is plain IEEE arithmetic, so the same header compiled for a
 // CPU (no contraction) gives the GPU's results bit for bit when FMATH = true.
 #pragma once
@@ -33,6 +38,11 @@ FM_HD X3 operator*(double s, X3 a) { return {s * a.x, s * a.y, s * a.z}; }
 FM_HD X3 operator*(X3 a, double s) { return {a.x * s, a.y * s, a.z * s}; }
 FM_HD double dot(X3 a, X3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 FM_HD X3 cross(X3 a, X3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+// Fused forms: a.b with two FMAs; a x b with one FMA per component.
+FM_HD double dotf(X3 a, X3 b) { return fm::fma_(a.z, b.z, fm::fma_(a.y, b.y, a.x * b.x)); }
+FM_HD X3 crossf(X3 a, X3 b) {
+  return {fm::fma_(a.y, b.z, -(a.z * b.y)), fm::fma_(a.z, b.x, -(a.x * b.z)), fm::fma_(a.x, b.y, -(a.y * b.x))};
+}
 // s a + v, fused per component.
 FM_HD X3 fmv(double s, X3 a, X3 v) { return {fm::fma_(s, a.x, v.x), fm::fma_(s, a.y, v.y), fm::fma_(s, a.z, v.z)}; }
 // v with its sign flipped when sm is the sign-bit mask (integer operations).
@@ -53,15 +63,22 @@ FM_HD double at(double v) {
   return fm::std_atan(v);
 }
 
+// Per-pair constants of the corners: aSq_dSq = a^2 + d^2 (1 - c^2),
+// den = 1/sqrt((1 - c^2) aSq_dSq), c2 = 2c, cden = (1 + c) den, m2den = -2 den.
+struct CornerK {
+  double aSq_dSq, c, cSq, omcSqI, c2, cden, m2den;
+};
+
 // SegSegInteg at one corner (DislocationForces.jl:1480-1561), added (sm = 0) or
-// subtracted (sm = sign bit) into integ[19].  aSq_dSq and den =
-// 1/sqrt((1 - c^2) aSq_dSq) are per pair.
-template <bool FMATH>
-FM_HD void corner(double aSq_dSq, double den, double c, double cSq, double omcSqI, double x, double y, long long sm,
-                  double* integ) {
+// subtracted (sm = sign bit) into integ[19]; the first corner (FIRST, sm = 0)
+// writes instead of adding to zero.
+template <bool FMATH, bool FIRST>
+FM_HD void corner(const CornerK& P, double x, double y, long long sm, double* integ) {
+  const double aSq_dSq = P.aSq_dSq, c = P.c, cSq = P.cSq, omcSqI = P.omcSqI;
   const double xSq = x * x;
   const double ySq = y * y;
-  const double Ra = sqrt(aSq_dSq + xSq + ySq + 2.0 * x * y * c);
+  // (x y) (2c) equals the reference's ((2x) y) c bit for bit (scaling by 2 is exact).
+  const double Ra = sqrt(aSq_dSq + xSq + ySq + x * y * P.c2);
   const double R1 = Ra + y + x * c;  // Ra_Rd_t1
   const double R2 = Ra + x + y * c;  // Ra_Rd_t2
   const double L1 = lg<FMATH>(R1);
@@ -74,7 +91,7 @@ FM_HD void corner(double aSq_dSq, double den, double c, double cSq, double omcSq
   const double xS1 = x * S1, xxS1 = x * xS1;
   const double yS2 = y * S2, yyS2 = y * yS2;
 
-  const double integ1 = -2.0 * den * at<FMATH>((1.0 + c) * (Ra + x + y) * den);
+  const double integ1 = P.m2den * at<FMATH>((Ra + x + y) * P.cden);
   const double c_1 = aSq_dSq * integ1;
   const double c_5_6 = fm::fma_(c, Ra, -c_1) * omcSqI;
   const double integ2 = fm::fma_(c, L2, -L1) * omcSqI;
@@ -93,27 +110,34 @@ FM_HD void corner(double aSq_dSq, double den, double c, double cSq, double omcSq
   const double c_17_19 = fm::fma_(-cSq, xxS1, fm::fma_(-(y - c * x), RaInv, L1));
   const double c15_18_19 = 2.0 * integ4;
 
-  integ[0] += sgn(integ1, sm);
-  integ[1] += sgn(integ2, sm);
-  integ[2] += sgn(integ3, sm);
-  integ[3] += sgn(integ4, sm);
-  integ[4] += sgn(integ5, sm);
-  integ[5] += sgn(integ6, sm);
-  // integ[6] and integ[7..18] accumulate their numerators: the caller scales
-  // the four-corner sums by 1/aSq_dSq and 1/(1 - c^2) once.
-  integ[6] += sgn(integ1 - xS1 - yS2, sm);
-  integ[7] += sgn(fm::fma_(-c, S2, S1), sm);
-  integ[8] += sgn(fm::fma_(-c, S1, S2), sm);
-  integ[9] += sgn(fm::fma_(-c, xS1 + yS2 + integ1, RaInv), sm);
-  integ[10] += sgn(fm::fma_(cSq, yS2, xS1 + c_11_12), sm);
-  integ[11] += sgn(fm::fma_(cSq, xS1, yS2 + c_11_12), sm);
-  integ[12] += sgn(fm::fma_(c, y_13_14 - integ2, integ3 - x_13_14), sm);
-  integ[13] += sgn(fm::fma_(c, x_13_14 - integ3, integ2 - y_13_14), sm);
-  integ[14] += sgn(fm::fma_(c, fm::fma_(xSq, c_15_18, -c15_18_19), integ5 - z_15_18), sm);
-  integ[15] += sgn(fm::fma_(c, c_16, fm::fma_(2.0, integ2, xxS1)), sm);
-  integ[16] += sgn(fm::fma_(c, c_17_19, fm::fma_(2.0, integ3, yyS2)), sm);
-  integ[17] += sgn(fm::fma_(c, z_15_18 - integ5, fm::fma_(-xSq, c_15_18, c15_18_19)), sm);
-  integ[18] += sgn(fm::fma_(c, fm::fma_(x, c_17_19, -integ6), fm::fma_(-ySq, c_19, c15_18_19)), sm);
+  // integ[6] and integ[7..18] take their numerators: the caller scales the
+  // four-corner sums by 1/aSq_dSq and 1/(1 - c^2) once.
+  const double v[19] = {integ1,
+                        integ2,
+                        integ3,
+                        integ4,
+                        integ5,
+                        integ6,
+                        integ1 - xS1 - yS2,
+                        fm::fma_(-c, S2, S1),
+                        fm::fma_(-c, S1, S2),
+                        fm::fma_(-c, xS1 + yS2 + integ1, RaInv),
+                        fm::fma_(cSq, yS2, xS1 + c_11_12),
+                        fm::fma_(cSq, xS1, yS2 + c_11_12),
+                        fm::fma_(c, y_13_14 - integ2, integ3 - x_13_14),
+                        fm::fma_(c, x_13_14 - integ3, integ2 - y_13_14),
+                        fm::fma_(c, fm::fma_(xSq, c_15_18, -c15_18_19), integ5 - z_15_18),
+                        fm::fma_(c, c_16, fm::fma_(2.0, integ2, xxS1)),
+                        fm::fma_(c, c_17_19, fm::fma_(2.0, integ3, yyS2)),
+                        fm::fma_(c, z_15_18 - integ5, fm::fma_(-xSq, c_15_18, c15_18_19)),
+                        fm::fma_(c, fm::fma_(x, c_17_19, -integ6), fm::fma_(-ySq, c_19, c15_18_19))};
+#pragma unroll
+  for (int k = 0; k < 19; ++k) {
+    if (FIRST)
+      integ[k] = v[k];
+    else
+      integ[k] += sgn(v[k], sm);
+  }
 }
 
 // General branch of calcSegSegForce; NEED12 / NEED34 as in pair_f64.cuh.
@@ -125,31 +149,31 @@ FM_HD void general_pair(const KFast& K, X3 b1, X3 n11, X3 n12, X3 t1, double t1N
   const double omcSq = 1.0 - cSq;
   const double omcSqI = 1.0 / omcSq;
 
-  const X3 t2ct1 = cross(t2, t1);
+  const X3 t2ct1 = crossf(t2, t1);
   const X3 t1ct2 = -t2ct1;
-  const X3 b2ct2 = cross(b2, t2);
-  const X3 b1ct1 = cross(b1, t1);
+  const X3 b2ct2 = crossf(b2, t2);
+  const X3 b1ct1 = crossf(b1, t1);
 
-  const double t2db2 = dot(t2, b2);
-  const double t2db1 = dot(t2, b1);
-  const double t1db2 = dot(t1, b2);
-  const double t1db1 = dot(t1, b1);
+  const double t2db2 = dotf(t2, b2);
+  const double t2db1 = dotf(t2, b1);
+  const double t1db2 = dotf(t1, b2);
+  const double t1db1 = dotf(t1, b1);
 
-  const double t2ct1db2 = dot(t2ct1, b2);
-  const double t1ct2db1 = dot(t1ct2, b1);
-  const double b1ct1db2 = dot(b1ct1, b2);
-  const double b2ct2db1 = dot(b2ct2, b1);
+  const double t2ct1db2 = dotf(t2ct1, b2);
+  const double t1ct2db1 = dotf(t1ct2, b1);
+  const double b1ct1db2 = dotf(b1ct1, b2);
+  const double b2ct2db1 = dotf(b2ct2, b1);
 
-  const X3 t2ct1ct2 = t1 - c * t2;
-  const X3 t1ct2ct1 = t2 - c * t1;
-  const X3 t2cb1ct2 = b1 - t2db1 * t2;
-  const X3 t1cb2ct1 = b2 - t1db2 * t1;
-  const X3 b1ct1ct2 = t2db1 * t1 - c * b1;
-  const X3 b2ct2ct1 = t1db2 * t2 - c * b2;
+  const X3 t2ct1ct2 = fmv(-c, t2, t1);
+  const X3 t1ct2ct1 = fmv(-c, t1, t2);
+  const X3 t2cb1ct2 = fmv(-t2db1, t2, b1);
+  const X3 t1cb2ct1 = fmv(-t1db2, t1, b2);
+  const X3 b1ct1ct2 = fmv(-c, b1, t2db1 * t1);
+  const X3 b2ct2ct1 = fmv(-c, b2, t1db2 * t2);
 
-  const double t2ct1cb1dt1 = t2db1 - t1db1 * c;
-  const double t1ct2cb2dt2 = t1db2 - t2db2 * c;
-  const double t2ct1cb1db2 = t2db1 * t1db2 - t1db1 * t2db2;
+  const double t2ct1cb1dt1 = fm::fma_(-t1db1, c, t2db1);
+  const double t1ct2cb2dt2 = fm::fma_(-t2db2, c, t1db2);
+  const double t2ct1cb1db2 = fm::fma_(t2db1, t1db2, -(t1db1 * t2db2));
 
   const X3 R1 = n21 - n11;
   const X3 R2 = n22 - n12;
@@ -173,18 +197,18 @@ FM_HD void general_pair(const KFast& K, X3 b1, X3 n11, X3 n12, X3 t1, double t1N
   const double y2 = (lim21 - c * lim22) * omcSqI;
 
   double integ[19];
-#pragma unroll
-  for (int k = 0; k < 19; ++k) integ[k] = 0.0;
   const double aSq_dSq = K.aSq + d * d * omcSq;
   const double aSq_dSqI = 1.0 / aSq_dSq;
   const double den = 1.0 / sqrt(omcSq * aSq_dSq);
+  const CornerK P{aSq_dSq, c, cSq, omcSqI, 2.0 * c, (1.0 + c) * den, -2.0 * den};
   // ((I(x1,y1) - I(x1,y2)) - I(x2,y1)) + I(x2,y2), DislocationForces.jl:948-951.
+  corner<FMATH, true>(P, x1, y1, 0LL, integ);
 #pragma unroll 1
-  for (int q = 0; q < 4; ++q) {
+  for (int q = 1; q < 4; ++q) {
     const double x = (q & 2) ? x2 : x1;
     const double y = (q & 1) ? y2 : y1;
     const long long sm = (q == 1 || q == 2) ? (long long)0x8000000000000000ULL : 0LL;
-    corner<FMATH>(aSq_dSq, den, c, cSq, omcSqI, x, y, sm, integ);
+    corner<FMATH, false>(P, x, y, sm, integ);
   }
   integ[6] *= aSq_dSqI;
 #pragma unroll

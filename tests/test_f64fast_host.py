@@ -73,6 +73,7 @@ def test_fast_form_within_reference_noise(pkg, synth, oracle, fasthost, num_loop
     ulps = 4 * np.finfo(np.float64).eps * nrm(ext).max()
     noise = nrm(ref - ext).max()
     F = fasthost(k5, net)
+    assert np.linalg.norm(F - ref) <= 1e-10 * np.linalg.norm(ref) + ulps
     assert nrm(F - ext).max() <= 1.5 * noise + ulps
     assert np.max(nrm(F - ref) - (1e-10 * nrm(ref) + 4 * noise + ulps)) <= 0
     assert not np.array_equal(F, ref)
