@@ -122,13 +122,28 @@ FM_HD double log(double v) {
   return hiP + (r + tail);
 }
 
+FM_HD float as_f(int v) {
+#if defined(__CUDA_ARCH__)
+  return __int_as_float(v);
+#else
+  float r;
+  std::memcpy(&r, &v, sizeof r);
+  return r;
+#endif
+}
+
 FM_HD double atan(double z) {
   const long long bits = as_ll(z);
   const long long sgn = bits & (long long)0x8000000000000000ULL;
-  const double a = as_d(bits ^ sgn);
-  if (!(a <= 1.0e300)) return std_atan(z);  // inf, NaN
-  const bool big = a > 1.0;
-  const float af = (float)a;
+  const long long ab = bits ^ sgn;              // |z|; positive doubles order as integers
+  if (ab >= 0x7FF0000000000000LL) return std_atan(z);  // inf, NaN
+  const double a = as_d(ab);
+  const bool big = ab > 0x3FF0000000000000LL;   // |z| > 1
+  // FP32 estimate of |z| from its high word (exponent re-biased, 20 mantissa
+  // bits, truncated): 0 below the FP32 normal range, infinity above it.
+  const int hi = (int)(ab >> 32);
+  const int e = (hi >> 20) - 1023;
+  const float af = e < -126 ? 0.0f : (e > 127 ? as_f(0x7F800000) : as_f(((e + 127) << 23) | ((hi & 0xFFFFF) << 3)));
 #if defined(__CUDA_ARCH__)
   const float w = big ? __frcp_rn(af) : af;  // correctly rounded: the host's 1.0f / af
 #else
