@@ -254,15 +254,16 @@ def run_surrogate(args, pkg, ctx, k, soa, ref, pairs, ms_fp64, stream, sptr, flu
     F = torch.empty((n, 6), dtype=torch.float64, device="cuda")
     refv = ref.view(n, 6)
     out = {"source": source, "kappa": sur.kappa, "audit_fraction": 0.01}
-    for xm in ("f32c", "fp64"):
+    for key, xm, far in (("f32c", "f32c", "network"), ("fp64", "fp64", "network"), ("quad3_f32c", "f32c", "quad3"),
+                         ("quad3_fp64", "fp64", "quad3")):
         with torch.cuda.stream(stream):
-            sur.force(k, soa, out=F, exact_mode=xm, stream=sptr)  # plan set-up
+            sur.force(k, soa, out=F, exact_mode=xm, stream=sptr, far=far)  # plan set-up
             ts, rep = [], None
             for _ in range(max(1, min(args.steps, 3))):
                 flush.zero_()
                 a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 a_.record(stream)
-                _, rep = sur.force(k, soa, out=F, exact_mode=xm, stream=sptr)
+                _, rep = sur.force(k, soa, out=F, exact_mode=xm, stream=sptr, far=far)
                 b_.record(stream)
                 torch.cuda.synchronize()
                 ts.append(a_.elapsed_time(b_))
@@ -271,7 +272,23 @@ def run_surrogate(args, pkg, ctx, k, soa, ref, pairs, ms_fp64, stream, sptr, flu
         fn = torch.linalg.norm(refv.view(n, 2, 3), dim=2)
         slots = rep["tiles_total"] * 128 * 128
         tfl = slots * OPS_MLP_PAIR / (rep["ms_network"] * 1e-3) / 1e12
-        out[xm] = {
+        far_pairs = rep["pairs_total"] - rep["pairs_near_general"] - rep["pairs_near_parallel"]
+        if far != "network":
+            out[key] = {
+                "value": pairs / (ms * 1e-3), "unit": "pair-interactions/s", "ms_per_step": ms,
+                "speedup_vs_fp64": ms_fp64 / ms, "far": "FP32 Gauss-Legendre quadrature, 3 points per segment",
+                "exact_passes": xm,
+                "error_vs_fp64": {"rel_rms": (torch.linalg.norm(F - refv) / torch.linalg.norm(refv)).item(),
+                                  "median_rel_node": (dn / fn).median().item(),
+                                  "max_node_over_max_force": (dn.max() / fn.max()).item()},
+                "audit_estimate_rel_rms": rep["audit_node_rel_rms"], "fallback": rep["fallback"],
+                "pairs_far": far_pairs,
+                "ms": {kk: rep[kk] for kk in ("ms_prep", "ms_network", "ms_audit", "ms_near", "ms_reduce")},
+                "far_kernel": {"kernel": "quad_far_tiles<3>", "far_pairs_per_s": far_pairs / (rep["ms_network"] * 1e-3),
+                               "bound": "fp32"},
+            }
+            continue
+        out[key] = {
             "value": pairs / (ms * 1e-3), "unit": "pair-interactions/s", "ms_per_step": ms,
             "speedup_vs_fp64": ms_fp64 / ms,
             "error_vs_fp64": {"rel_rms": (torch.linalg.norm(F - refv) / torch.linalg.norm(refv)).item(),
@@ -279,7 +296,7 @@ def run_surrogate(args, pkg, ctx, k, soa, ref, pairs, ms_fp64, stream, sptr, flu
                               "max_node_over_max_force": (dn.max() / fn.max()).item()},
             "audit_estimate_rel_rms": rep["audit_node_rel_rms"], "fallback": rep["fallback"],
             "pairs_near_exact": rep["pairs_near_general"] + rep["pairs_near_parallel"],
-            "pairs_network": rep["pairs_total"] - rep["pairs_near_general"] - rep["pairs_near_parallel"],
+            "pairs_network": far_pairs,
             "ms": {kk: rep[kk] for kk in ("ms_prep", "ms_network", "ms_audit", "ms_near", "ms_reduce")},
             "network_kernel": {"kernel": "mlp_far_tiles", "tensor_tflops": tfl, "bound": "tensor",
                                "peak_tflops": None, "frac": None,
@@ -628,6 +645,12 @@ def summary(line, variants, surrogate, sigma32k, batched):
             "max_node_over_max": _r(sv["error_vs_fp64"]["max_node_over_max_force"], 3),
             "tensor_frac": _r(sv["network_kernel"]["frac"], 3), "kappa": surrogate["kappa"],
             "arch": "MLP 16-128-128-128-112 GELU, FP16 fwd / FP32 acc, exact bilinear b contraction"}
+    if surrogate and "quad3_f32c" in surrogate:
+        qv = surrogate["quad3_f32c"]
+        out["quad3_f32c"] = {"pairs_per_s": _r(qv["value"]), "x_fp64": _r(qv["speedup_vs_fp64"], 3),
+                             "rel_rms": _r(qv["error_vs_fp64"]["rel_rms"], 3),
+                             "max_node_over_max": _r(qv["error_vs_fp64"]["max_node_over_max_force"], 3),
+                             "far": "FP32 Gauss-Legendre, 3 points per segment, no network"}
     if sigma32k:
         out["sigma_32k_grid128"] = {"evals_per_s": _r(sigma32k["value"]), "frac_probe": _r(sigma32k["frac_fp64_peak"], 3),
                                  "bound_excess": _r(sigma32k.get("parity_sample", {}).get("bound_excess"), 3)}
@@ -708,6 +731,8 @@ def main():
                     help="only run N surrogate force calls on the workload (f32c exact passes, no audit) and exit: "
                          "the command the ncu captures of the surrogate kernels use")
     ap.add_argument("--surrogate", default=SURROGATE_CKPT, help="surrogate checkpoint (trained here when missing)")
+    ap.add_argument("--far", default="network", choices=["network", "quad2", "quad3"],
+                    help="far pass of --profile-surrogate: the network or FP32 Gauss-Legendre quadrature")
     args = ap.parse_args()
 
     import __graft_entry__ as graft
@@ -740,7 +765,7 @@ def main():
         sur = pkg.Surrogate(ctx, seed=0).load(args.surrogate)
         segs = torch.from_numpy(synth.packed_soa(p, b)).cuda()
         for _ in range(args.profile_surrogate):
-            _, rep = sur.force(k, segs, exact_mode="f32c", audit_fraction=0.0)
+            _, rep = sur.force(k, segs, exact_mode="f32c", audit_fraction=0.0, far=args.far)
         torch.cuda.synchronize()
         print(json.dumps({"profile_surrogate": args.profile_surrogate, "segments": n, "report": rep}), flush=True)
         return

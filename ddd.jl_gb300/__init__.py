@@ -113,7 +113,11 @@ class ddd_u_mesh(ctypes.Structure):
 
 class ddd_sur_opts(ctypes.Structure):
     _fields_ = [("kappa", ctypes.c_double), ("audit_fraction", ctypes.c_double), ("audit_tol", ctypes.c_double),
-                ("exact_mode", ctypes.c_int)]
+                ("exact_mode", ctypes.c_int), ("far_mode", ctypes.c_int)]
+
+
+# Far-pair passes of ddd_surrogate_force (ddd_sur_opts.far_mode).
+FAR_MODES = {"network": 0, "quad2": 2, "quad3": 3}
 
 
 class ddd_sur_report(ctypes.Structure):
@@ -863,13 +867,15 @@ class Surrogate:
 
     # -- forces ---------------------------------------------------------------
     def force(self, k, segs, ext=None, kappa=None, audit_fraction=0.01, audit_tol=1e-3, exact_mode="fp64", out=None,
-              stream=None):
+              stream=None, far="network"):
         """ddd_surrogate_force on packed 9 × n segments (a CUDA float64 tensor or
         a numpy array); exact_mode: arithmetic of the exact near / audit passes
-        ("fp64", "df64" or "f32c").  Returns (forces as a CUDA tensor n × 6 = the
-        3 × 2 × n column-major array, report dict)."""
+        ("fp64", "df64" or "f32c"); far: "network", or "quad2" / "quad3" for
+        the far pairs by FP32 Gauss-Legendre quadrature (no network used).
+        Returns (forces as a CUDA tensor n × 6 = the 3 × 2 × n column-major
+        array, report dict)."""
         import torch
-        o = self._opts(k, kappa, audit_fraction, audit_tol, exact_mode)
+        o = self._opts(k, kappa, audit_fraction, audit_tol, exact_mode, far)
         if not isinstance(segs, torch.Tensor):
             segs = torch.from_numpy(np.ascontiguousarray(segs, dtype=np.float64)).cuda()
         assert segs.dtype == torch.float64 and segs.is_cuda and segs.dim() == 2 and segs.shape[0] == 9
@@ -886,19 +892,21 @@ class Surrogate:
                                              ctypes.byref(o), ctypes.byref(rep)), "surrogate force")
         return out, rep.as_dict()
 
-    def _opts(self, k, kappa, audit_fraction, audit_tol, exact_mode):
-        if self.nu is not None and abs(_nu_of(k) - self.nu) > 1e-9:
+    def _opts(self, k, kappa, audit_fraction, audit_tol, exact_mode, far="network"):
+        fm = FAR_MODES.get(far, far) if isinstance(far, str) else int(far)
+        if fm == 0 and self.nu is not None and abs(_nu_of(k) - self.nu) > 1e-9:
             raise DDDError(DDD_EINVAL, "surrogate trained for nu = %.6g, called with nu = %.6g"
                            % (self.nu, _nu_of(k)))
         return ddd_sur_opts(self.kappa if kappa is None else float(kappa), float(audit_fraction), float(audit_tol),
-                            MODES.get(exact_mode, exact_mode) if isinstance(exact_mode, str) else int(exact_mode))
+                            MODES.get(exact_mode, exact_mode) if isinstance(exact_mode, str) else int(exact_mode),
+                            fm)
 
     def force_network(self, dlnParams, matParams, network, kappa=None, audit_fraction=0.01, audit_tol=1e-3,
-                      exact_mode="fp64"):
+                      exact_mode="fp64", far="network"):
         """The surrogate's calcSegSegForce on a DislocationNetwork's own host arrays
         (ddd_surrogate_force_host): a fresh 3×2×numSeg array and the report."""
         k = consts_of(dlnParams, matParams)
-        o = self._opts(k, kappa, audit_fraction, audit_tol, exact_mode)
+        o = self._opts(k, kappa, audit_fraction, audit_tol, exact_mode, far)
         n = network.numSeg
         F = np.zeros((3, 2, n), np.float64, order="F")
         rep = ddd_sur_report()

@@ -1,0 +1,153 @@
+// Far-pair pass of the seg-seg force by Gauss-Legendre quadrature in FP32
+// (farfield_quad.cuh): the alternative to the network pass in the surrogate
+// force path (ddd_surrogate_force with far_mode = 2 or 3).  Same routing: the
+// Morton-sorted segments, every tile pair I <= J, the FP32 trust test
+// pair_is_far deciding which pairs are far (the near pass takes the others),
+// and the same per-tile-pair slot of 12 x 128 partial forces (row segments'
+// then column segments' node forces), so the near pass, audit and reduction
+// run unchanged after it.
+//
+// One CTA of 128 threads per tile pair (grid-stride over the items).  Thread t
+// owns row segment i in registers; the column tile sits in shared memory; at
+// step k thread t pairs with column (t + k) mod 128, so a warp's lanes never
+// share a column and column forces accumulate race-free in per-warp arrays.
+// Per-segment FP32 data (qs, built by prep_quad_seg from the sorted FP64
+// segments): the low part of the midpoint (the FP32 midpoint of the trust test
+// plus this part gives the midpoint to ~2^-48), the segment vector n2 - n1,
+// the unit direction, the length and the Burgers vector.
+#include <cuda_runtime.h>
+
+#include "ddd_internal.h"
+#include "farfield_quad.cuh"
+#include "pair_f64.cuh"
+#include "surrogate.cuh"
+
+namespace ddd {
+
+namespace {
+
+constexpr int TQ = 128;
+constexpr int kQsRows = 13;  // midpoint low part xyz, segment vector xyz, direction xyz, length, Burgers xyz
+constexpr int kQLo = 0, kQL = 3, kQT = 6, kQLen = 9, kQB = 10;
+
+__global__ void prep_quad_seg(const double* __restrict__ soa, const float* __restrict__ ms, int64_t npad,
+                              float* __restrict__ qs) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= npad) return;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double n1 = soa[k * npad + i], n2 = soa[(3 + k) * npad + i];
+    const double m = 0.5 * (n1 + n2);
+    qs[(kQLo + k) * npad + i] = (float)(m - (double)ms[(sur::kMsM + k) * npad + i]);
+    qs[(kQL + k) * npad + i] = (float)(n2 - n1);
+    qs[(kQT + k) * npad + i] = (float)soa[(9 + k) * npad + i];
+    qs[(kQB + k) * npad + i] = (float)soa[(6 + k) * npad + i];
+  }
+  qs[kQLen * npad + i] = (float)(1.0 / soa[12 * npad + i]);
+}
+
+template <int NQ>
+__global__ void __launch_bounds__(TQ)
+quad_far_tiles(const float* __restrict__ ms, const float* __restrict__ qs, int64_t npad, const int4* __restrict__ items,
+               int32_t nItems, qf::QConst K, float kappa2, double* __restrict__ partial) {
+  __shared__ float cM[3][TQ], cLen[TQ];        // trust-test data of the column tile
+  __shared__ float cQ[kQsRows][TQ];            // quadrature data of the column tile
+  __shared__ float sFJ[TQ / 32][6][TQ];        // per-warp column forces
+  const int t = threadIdx.x, warp = t >> 5;
+  for (int32_t w = blockIdx.x; w < nItems; w += gridDim.x) {
+    const int4 it = items[w];
+    const int64_t i = it.y + t, j0 = it.z;
+    const bool diag = it.w != 0;
+    __syncthreads();  // the previous item's readers are done with the tile
+#pragma unroll
+    for (int k = 0; k < 3; ++k) cM[k][t] = ms[(sur::kMsM + k) * npad + j0 + t];
+    cLen[t] = ms[sur::kMsL * npad + j0 + t];
+#pragma unroll
+    for (int k = 0; k < kQsRows; ++k) cQ[k][t] = qs[k * npad + j0 + t];
+#pragma unroll
+    for (int q = 0; q < TQ / 32; ++q)
+#pragma unroll
+      for (int c = 0; c < 6; ++c) sFJ[q][c][t] = 0.0f;
+    const float mi[3] = {ms[(sur::kMsM + 0) * npad + i], ms[(sur::kMsM + 1) * npad + i],
+                         ms[(sur::kMsM + 2) * npad + i]};
+    const float Li = ms[sur::kMsL * npad + i];
+    const float loi[3] = {qs[(kQLo + 0) * npad + i], qs[(kQLo + 1) * npad + i], qs[(kQLo + 2) * npad + i]};
+    const qf::V3f li = {qs[(kQL + 0) * npad + i], qs[(kQL + 1) * npad + i], qs[(kQL + 2) * npad + i]};
+    const qf::V3f ti = {qs[(kQT + 0) * npad + i], qs[(kQT + 1) * npad + i], qs[(kQT + 2) * npad + i]};
+    const float Lni = qs[kQLen * npad + i];
+    const qf::V3f bi = {qs[(kQB + 0) * npad + i], qs[(kQB + 1) * npad + i], qs[(kQB + 2) * npad + i]};
+    __syncthreads();
+    qf::V3f f1 = {0.f, 0.f, 0.f}, f2 = {0.f, 0.f, 0.f};
+    for (int k = 0; k < TQ; ++k) {
+      const int jl = (t + k) & (TQ - 1);
+      float dx, dy, dz;
+      const bool far = sur::pair_is_far(mi[0], mi[1], mi[2], Li, cM[0][jl], cM[1][jl], cM[2][jl], cLen[jl], kappa2,
+                                        dx, dy, dz);
+      if (far && (!diag || jl > t)) {
+        // m_i - m_j from the FP32 midpoints and their low parts.
+        const qf::V3f dm = {(mi[0] - cM[0][jl]) + (loi[0] - cQ[kQLo + 0][jl]),
+                            (mi[1] - cM[1][jl]) + (loi[1] - cQ[kQLo + 1][jl]),
+                            (mi[2] - cM[2][jl]) + (loi[2] - cQ[kQLo + 2][jl])};
+        const qf::V3f lj = {cQ[kQL + 0][jl], cQ[kQL + 1][jl], cQ[kQL + 2][jl]};
+        const qf::V3f tj = {cQ[kQT + 0][jl], cQ[kQT + 1][jl], cQ[kQT + 2][jl]};
+        const qf::V3f bj = {cQ[kQB + 0][jl], cQ[kQB + 1][jl], cQ[kQB + 2][jl]};
+        const float Lnj = cQ[kQLen][jl];
+        qf::V3f Fa, Fb, Fc, Fd;
+        qf::side<NQ>(K, dm, li, bi, tj, Lnj, bj, Fa, Fb);
+        qf::side<NQ>(K, {-dm.x, -dm.y, -dm.z}, lj, bj, ti, Lni, bi, Fc, Fd);
+        f1 = f1 + Fa;
+        f2 = f2 + Fb;
+        float* fj = &sFJ[warp][0][0];
+        fj[0 * TQ + jl] += Fc.x;
+        fj[1 * TQ + jl] += Fc.y;
+        fj[2 * TQ + jl] += Fc.z;
+        fj[3 * TQ + jl] += Fd.x;
+        fj[4 * TQ + jl] += Fd.y;
+        fj[5 * TQ + jl] += Fd.z;
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+    double* p = partial + (int64_t)it.x * 12 * TQ;
+    const float row[6] = {f1.x, f1.y, f1.z, f2.x, f2.y, f2.z};
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      p[c * TQ + t] = (double)row[c];
+      double v = 0.0;
+#pragma unroll
+      for (int q = 0; q < TQ / 32; ++q) v += (double)sFJ[q][c][t];
+      p[(6 + c) * TQ + t] = v;
+    }
+  }
+}
+
+}  // namespace
+
+size_t quad_seg_bytes(int64_t npad) { return (size_t)npad * kQsRows * sizeof(float); }
+
+cudaError_t launch_prep_quad_seg(const double* soa, const float* ms, int64_t npad, float* qs, cudaStream_t st) {
+  prep_quad_seg<<<(unsigned)((npad + 255) / 256), 256, 0, st>>>(soa, ms, npad, qs);
+  return cudaGetLastError();
+}
+
+int quad_far_blocks_per_sm(int nq) {
+  int per = 0;
+  if (nq == 2)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, quad_far_tiles<2>, TQ, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, quad_far_tiles<3>, TQ, 0);
+  return per > 0 ? per : 1;
+}
+
+cudaError_t launch_quad_far_tiles(const float* ms, const float* qs, int64_t npad, const int4* items, int32_t nItems,
+                                  int nq, const KConsts& K, float kappa2, double* partial, int grid, cudaStream_t st) {
+  if (nItems <= 0) return cudaSuccess;
+  const qf::QConst Q{(float)K.aSq, (float)K.mu4pi, (float)K.mu4pinu, (float)K.nuMu4pinu, (float)(K.aSq * K.mu8pi)};
+  if (nq == 2)
+    quad_far_tiles<2><<<grid, TQ, 0, st>>>(ms, qs, npad, items, nItems, Q, kappa2, partial);
+  else
+    quad_far_tiles<3><<<grid, TQ, 0, st>>>(ms, qs, npad, items, nItems, Q, kappa2, partial);
+  return cudaGetLastError();
+}
+
+}  // namespace ddd

@@ -47,6 +47,12 @@ cudaError_t launch_prep_mlp_seg(const double* soa, const uint8_t* skip, int64_t 
 cudaError_t launch_mlp_far_tiles(const float* ms, int64_t npad, const int4* items, int32_t nItems, int32_t* next,
                                  const void* const* W, const float* params, float mu4pi, float kappa2,
                                  double* partial, int32_t* err, int grid, cudaStream_t st);
+// farfield_quad.cu: the far pairs by Gauss-Legendre quadrature in FP32 instead of the network.
+size_t quad_seg_bytes(int64_t npad);
+cudaError_t launch_prep_quad_seg(const double* soa, const float* ms, int64_t npad, float* qs, cudaStream_t st);
+int quad_far_blocks_per_sm(int nq);
+cudaError_t launch_quad_far_tiles(const float* ms, const float* qs, int64_t npad, const int4* items, int32_t nItems,
+                                  int nq, const KConsts& K, float kappa2, double* partial, int grid, cudaStream_t st);
 
 namespace sf {
 
@@ -345,13 +351,13 @@ struct SurForcePlan {
   int32_t nAudit = 0;
   double auditFraction = -1.0;
   size_t cubBytes = 0;
-  int sms = 0, gridExact = 0;
-  Buf soa, soadf, skip, ms, keysIn, keysOut, valsIn, perm, src, cubTmp, minmaxPart, box, tbox, allItems, nearItems, partial,
+  int sms = 0, gridExact = 0, gridQuad = 0;
+  Buf soa, soadf, skip, ms, qs, keysIn, keysOut, valsIn, perm, src, cubTmp, minmaxPart, box, tbox, allItems, nearItems, partial,
       auditItems, auditSlots, abuf, astat, small;
   Buf hostSegs, hostExt, hostForce;  // device copies for the host-array entry point
   cudaEvent_t ev[6] = {};
   ~SurForcePlan() {
-    for (Buf* b : {&soa, &soadf, &skip, &ms, &keysIn, &keysOut, &valsIn, &perm, &src, &cubTmp, &minmaxPart, &box, &tbox,
+    for (Buf* b : {&soa, &soadf, &skip, &ms, &qs, &keysIn, &keysOut, &valsIn, &perm, &src, &cubTmp, &minmaxPart, &box, &tbox,
                    &allItems, &nearItems, &partial, &auditItems, &auditSlots, &abuf, &astat, &small, &hostSegs,
                    &hostExt, &hostForce})
       b->release();
@@ -437,6 +443,7 @@ cudaError_t ensure_plan(ddd_surrogate* s, int64_t numSeg, double auditFraction) 
                                                            sizeof(TileSmemT<sf::T, PolF64>))) != cudaSuccess)
       return e;
     P.gridExact = P.sms * std::max(1, per);
+    P.gridQuad = P.sms * quad_far_blocks_per_sm(3);
     const size_t n = (size_t)numSeg, np = (size_t)P.npad;
     if ((e = P.soa.ensure(np * 13 * sizeof(double))) != cudaSuccess) return e;
     if ((e = P.skip.ensure(np)) != cudaSuccess) return e;
@@ -527,10 +534,12 @@ int ddd_surrogate_force(ddd_surrogate* s, const ddd_consts* k, const double* seg
                         ddd_sur_report* rep) {
   DDD_NVTX("ddd_surrogate_force");
   if (!s) return DDD_EINVAL;
-  ddd_sur_opts o{20.0, 0.01, 1e-3, DDD_MODE_FP64};
+  ddd_sur_opts o{20.0, 0.01, 1e-3, DDD_MODE_FP64, 0};
   if (opts) o = *opts;
   if (o.exact_mode != DDD_MODE_FP64 && o.exact_mode != DDD_MODE_DF64 && o.exact_mode != DDD_MODE_F32C)
     return sfail(s, DDD_EINVAL, "exact_mode must be DDD_MODE_FP64, DDD_MODE_DF64 or DDD_MODE_F32C");
+  if (o.far_mode != 0 && o.far_mode != 2 && o.far_mode != 3)
+    return sfail(s, DDD_EINVAL, "far_mode must be 0 (network) or 2 / 3 (Gauss points of the quadrature)");
   if (!k) return sfail(s, DDD_EINVAL, "consts is NULL");
   const double kv[5] = {k->aSq, k->mu4pi, k->mu8pi, k->mu4pinu, k->nuMu4pinu};
   for (double x : kv)
@@ -563,6 +572,7 @@ int ddd_surrogate_force(ddd_surrogate* s, const ddd_consts* k, const double* seg
   const float kappa = (float)o.kappa;
   const int xm = o.exact_mode;
   if (xm != DDD_MODE_FP64) SCK(P.soadf.ensure((size_t)npad * 26 * sizeof(float)), "allocate df64 segments");
+  if (o.far_mode) SCK(P.qs.ensure(quad_seg_bytes(npad)), "allocate quadrature segment data");
   TileArgs A{K, P.soa.as<double>(), P.skip.as<uint8_t>(), npad, P.soadf.as<float>(), nullptr};
   A.ms = P.ms.as<float>();
   A.farK2 = kappa * kappa;
@@ -584,6 +594,8 @@ int ddd_surrogate_force(ddd_surrogate* s, const ddd_consts* k, const double* seg
                                         P.skip.as<uint8_t>(), P.src.as<int32_t>(), &dv->active);
   SCK(cudaGetLastError(), "gather");
   SCK(launch_prep_mlp_seg(P.soa.as<double>(), P.skip.as<uint8_t>(), npad, P.ms.as<float>(), st), "prep_mlp_seg");
+  if (o.far_mode)
+    SCK(launch_prep_quad_seg(P.soa.as<double>(), P.ms.as<float>(), npad, P.qs.as<float>(), st), "prep_quad_seg");
   if (xm != DDD_MODE_FP64) SCK(launch_prep_df(P.soa.as<double>(), npad, P.soadf.as<float>(), st), "prep_df");
   sf::tile_boxes<<<(unsigned)nt, sf::T, 0, st>>>(P.ms.as<float>(), npad, P.tbox.as<float>());
   sf::near_items<<<(unsigned)((P.nItems + 255) / 256), 256, 0, st>>>(
@@ -591,12 +603,19 @@ int ddd_surrogate_force(ddd_surrogate* s, const ddd_consts* k, const double* seg
   SCK(cudaGetLastError(), "tile classification");
   SCK(cudaEventRecord(P.ev[1], st), "event");
 
-  // 2. network pass over every tile pair
-  const void* W[4] = {s->W1, s->W2, s->W3, s->W4};
-  const int gridNet = (int)std::min<int64_t>(P.sms, P.nItems);
-  SCK(launch_mlp_far_tiles(P.ms.as<float>(), npad, P.allItems.as<int4>(), (int32_t)P.nItems, &dv->next[0], W, s->P,
-                           (float)k->mu4pi, kappa * kappa, P.partial.as<double>(), &dv->err, gridNet, st),
-      "network pass");
+  // 2. far pass over every tile pair: the network, or Gauss-Legendre quadrature
+  if (o.far_mode) {
+    SCK(launch_quad_far_tiles(P.ms.as<float>(), P.qs.as<float>(), npad, P.allItems.as<int4>(), (int32_t)P.nItems,
+                              o.far_mode, K, kappa * kappa, P.partial.as<double>(),
+                              (int)std::min<int64_t>(P.gridQuad, P.nItems), st),
+        "quadrature pass");
+  } else {
+    const void* W[4] = {s->W1, s->W2, s->W3, s->W4};
+    const int gridNet = (int)std::min<int64_t>(P.sms, P.nItems);
+    SCK(launch_mlp_far_tiles(P.ms.as<float>(), npad, P.allItems.as<int4>(), (int32_t)P.nItems, &dv->next[0], W, s->P,
+                             (float)k->mu4pi, kappa * kappa, P.partial.as<double>(), &dv->err, gridNet, st),
+        "network pass");
+  }
   SCK(cudaEventRecord(P.ev[2], st), "event");
 
   // 3. near pass (in place)

@@ -446,8 +446,14 @@ int ddd_surrogate_load(ddd_surrogate* s, const char* path, double* kappa, double
  * (sqrt(sum of squared slot errors / sampled fraction) / ||F||); when that
  * exceeds audit_tol, the whole call is recomputed with the exact FP64 kernel
  * (fallback = 1).
+ * Far pairs may instead go to Gauss-Legendre quadrature of the non-singular
+ * stress on both segments (far_mode 2 or 3, FP32): the endpoint differences
+ * of the analytic form are replaced by integrals of their derivatives, which
+ * do not cancel, so a far pair's force carries ~2e-7 relative error (3 points,
+ * R >= 20 max(L_i, L_j)) where the analytic FP64 formula loses up to ~1e-3 to
+ * cancellation; the near pass, audit and fallback are unchanged.
  * opts may be NULL (kappa 20, audit_fraction 0.01, audit_tol 1e-3, exact_mode
- * DDD_MODE_FP64); rep may be
+ * DDD_MODE_FP64, far_mode 0); rep may be
  * NULL.  Synchronous: the work is queued on `stream` (NULL: the surrogate's own
  * stream, after waiting for all work already queued on the device) and the
  * call returns when the forces are complete. */
@@ -457,6 +463,9 @@ typedef struct {
   double audit_tol;      /* bound of the estimated node-force relative RMS error; <= 0: no fallback */
   int exact_mode;        /* arithmetic of the exact passes (near, audit, fallback): DDD_MODE_FP64 (strict),
                             DDD_MODE_DF64 or DDD_MODE_F32C for the general branch */
+  int far_mode;          /* 0: far pairs through the network; 2 or 3: through Gauss-Legendre quadrature with
+                            that many points on each segment, in FP32 (no network involved: the surrogate's
+                            weights and trained Poisson ratio are not used) */
 } ddd_sur_opts;
 typedef struct {
   int64_t pairs_total;          /* unordered pairs of active segments */

@@ -1,0 +1,79 @@
+"""The far-field quadrature's arithmetic on a CPU.
+
+tests/quad_host/quad_host.cpp compiles ddd.jl_gb300/csrc/farfield_quad.cuh
+(the FP32 Gauss-Legendre form of the far-pair force that ddd_surrogate_force
+runs with far_mode 2 or 3) as plain C++, with inputs rounded to FP32 as the GPU
+pass rounds them.  Against the long-double evaluation of the reference's
+analytic pair force (the oracle on two-segment networks), relative to each
+pair's largest node force, at midpoint separations R = 20-1000 max(L):
+* 3 points: median ~2e-7, max < 1e-6 (the FP32 arithmetic; the quadrature
+  itself is ~1e-9 at R/L = 20);
+* 2 points: ~5e-6 at R/L = 20 (quadrature error), ~2e-7 from R/L = 100.
+The analytic FP64 formula of the reference is off by up to ~3e-2 at
+R/L = 1000 on the same pairs (its four-corner cancellation), which the test
+records as the comparison.
+"""
+import ctypes
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+SRC = os.path.join(ROOT, "tests", "quad_host", "quad_host.cpp")
+K5 = np.array([1.0, 1 / (4 * np.pi), 1 / (8 * np.pi), 1 / (4 * np.pi) / 0.72, 0.28 / (4 * np.pi) / 0.72])
+
+
+@pytest.fixture(scope="module")
+def quadhost(tmp_path_factory):
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    out = str(tmp_path_factory.mktemp("quadhost") / "libquadhost.so")
+    cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-I",
+           os.path.join(ROOT, "ddd.jl_gb300", "csrc"), SRC, "-o", out]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    lib = ctypes.CDLL(out)
+    dp, ip = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)
+    lib.quad_pair_forces.argtypes = [dp, dp, ip, ctypes.c_int64, ctypes.c_int, dp]
+    lib.quad_pair_forces.restype = None
+    return lib
+
+
+def _pairs(rng, RL, n):
+    def unit():
+        v = rng.normal(size=3)
+        return v / np.linalg.norm(v)
+    out = []
+    for _ in range(n):
+        L1, L2 = rng.uniform(20, 200, 2)
+        c1 = rng.uniform(0, 20000, 3)
+        c2 = c1 + unit() * RL * max(L1, L2)
+        t1, t2, b1, b2 = unit(), unit(), unit(), unit()
+        out.append((c1 - t1 * L1 / 2, c1 + t1 * L1 / 2, b1, c2 - t2 * L2 / 2, c2 + t2 * L2 / 2, b2))
+    return out
+
+
+@pytest.mark.parametrize("RL,nq,med,mx", [(20, 3, 5e-7, 2e-6), (30, 3, 5e-7, 2e-6), (100, 3, 5e-7, 2e-6),
+                                          (1000, 3, 5e-7, 2e-6), (20, 2, 1e-5, 5e-5), (100, 2, 5e-7, 5e-6)])
+def test_quadrature_against_long_double(pkg, oracle, quadhost, RL, nq, med, mx):
+    rng = np.random.default_rng(RL + nq)
+    dp, ip = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)
+    errs = []
+    for n11, n12, b1, n21, n22, b2 in _pairs(rng, RL, 30):
+        segs = np.ascontiguousarray(np.r_[n11, n12, b1, n21, n22, b2])
+        out = np.zeros(12)
+        pr = np.array([0, 1], dtype=np.int64)
+        quadhost.quad_pair_forces(K5.ctypes.data_as(dp), segs.ctypes.data_as(dp), pr.ctypes.data_as(ip), 1, nq,
+                                  out.ctypes.data_as(dp))
+        net = pkg.DislocationNetwork(np.asfortranarray(np.stack([n11, n12, n21, n22], 1)),
+                                     np.asfortranarray(np.stack([b1, b2], 1)),
+                                     np.asfortranarray(np.array([[1, 1, 2], [2, 3, 4]], dtype=np.int64)))
+        ext = oracle.segseg_ser_ld(K5, net)
+        q = out.reshape(2, 2, 3).transpose(2, 1, 0)  # (xyz, node, segment)
+        errs.append(np.abs(q - ext).max() / np.abs(ext).max())
+    assert np.median(errs) <= med and np.max(errs) <= mx, (np.median(errs), np.max(errs))

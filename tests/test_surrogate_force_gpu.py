@@ -266,6 +266,53 @@ def test_committed_checkpoint_gain_over_f32c_exact(pkg, synth):
     assert err <= 1e-4, err
     assert ms_sur < ms_f32c, (ms_sur, ms_f32c)
 
+    # The far pairs by quadrature instead of the network (3 points): faster than
+    # f32c exact as well, and closer to the strict FP64 forces.
+    def run_quad():
+        out["Fq"], out["repq"] = sur.force(k, d, exact_mode="f32c", stream=st.cuda_stream, far="quad3")
+
+    ms_quad = timed(run_quad)
+    err_q = (torch.linalg.norm(out["Fq"] - ref) / torch.linalg.norm(ref)).item()
+    assert out["repq"]["fallback"] == 0
+    assert err_q <= 2e-6, err_q
+    assert ms_quad < ms_f32c, (ms_quad, ms_f32c)
+
+
+@pytest.mark.parametrize("exact_mode,far", [("fp64", "quad3"), ("f32c", "quad3"), ("fp64", "quad2")])
+def test_quadrature_far_field(pkg, synth, oracle, exact_mode, far):
+    """far = "quad3" / "quad2": far pairs by FP32 Gauss-Legendre quadrature on
+    both segments (no network), near pairs exact.  On a 12,000-segment network of
+    the workload's generator (mostly far pairs), against the long-double
+    evaluation of the reference's formulas on 96 sampled segments: relative RMS
+    <= 1e-6 (3 points) / 1e-5 (2 points), per node <= 1e-4 |F| + 1e-6 max|F|
+    (measured on a CPU: a far pair's force to ~2e-7 with 3 points).  The result
+    does not depend on the network's weights, every pair is counted once, and
+    repeats are bit-equal."""
+    dln, mat = _params(pkg)
+    net, segs = _network(pkg, synth, 1500, seed=41)
+    n = segs.shape[1]
+    k, k5 = _k(pkg), k5_of(dln, mat)
+    sur = pkg.Surrogate(pkg.get_context(), seed=0)  # untrained: not used by the quadrature
+    F, rep = sur.force(k, segs, far=far, exact_mode=exact_mode, audit_fraction=0.02)
+    assert rep["fallback"] == 0 and rep["pairs_total"] == n * (n - 1) // 2
+    assert rep["pairs_near_general"] + rep["pairs_near_parallel"] < rep["pairs_total"] // 10
+    flat = sur.params()
+    sur.set_params(np.full_like(flat, 3.0))
+    F2, _ = sur.force(k, segs, far=far, exact_mode=exact_mode, audit_fraction=0.02)
+    assert torch.equal(F, F2)
+    F3 = np.asfortranarray(F.cpu().numpy().reshape(n, 2, 3).transpose(2, 1, 0))
+    rows = np.sort(np.random.default_rng(5).choice(n, 96, replace=False))
+    ext = oracle.segseg_ser_ld(k5, net, rows, nthreads=os.cpu_count() or 1)
+    G = F3[:, :, rows]
+    nrm = lambda a: np.linalg.norm(a, axis=0)
+    rel = np.linalg.norm(G - ext) / np.linalg.norm(ext)
+    if os.environ.get("DDD_TEST_STATS"):
+        with open(os.environ["DDD_TEST_STATS"], "a") as fh:
+            fh.write("quadrature %s %s: rel rms %.3e max node %.3e audit %.3e %s\n" % (
+                far, exact_mode, rel, (nrm(G - ext) / nrm(ext)).max(), rep["audit_node_rel_rms"], rep))
+    assert rel <= (1e-6 if far == "quad3" else 1e-5), rel
+    assert np.all(nrm(G - ext) <= 1e-4 * nrm(ext) + 1e-6 * nrm(ext).max())
+
 
 def test_host_array_entry_matches_device_form(pkg, synth, trained):
     # ddd_surrogate_force_host takes the network's own arrays (the
