@@ -15,6 +15,15 @@
 // segments): the low part of the midpoint (the FP32 midpoint of the trust test
 // plus this part gives the midpoint to ~2^-48), the segment vector n2 - n1,
 // the unit direction, the length and the Burgers vector.
+//
+// Near-parallel pairs (1 - c^2 <= sqrt(eps) by the reference's FP64 test on
+// the FP64 directions; an FP32 pre-test with a wide margin picks the
+// candidates) take the reference's construction of calcParSegSegForce
+// (DislocationForces.jl:1167-1442): each side's source segment projected onto
+// the field segment's direction and pulled in by the critical angle, plus the
+// two connector segments where its core-correction test holds
+// (qf::par_sources); the quadrature then integrates that geometry, so these
+// pairs get the force the reference assigns them.
 #include <cuda_runtime.h>
 
 #include "ddd_internal.h"
@@ -46,10 +55,34 @@ __global__ void prep_quad_seg(const double* __restrict__ soa, const float* __res
   qs[kQLen * npad + i] = (float)(1.0 / soa[12 * npad + i]);
 }
 
+// FP64 record of segment g of the sorted SoA (rows n1, n2, b, t).
+__device__ __forceinline__ qf::SegD seg_d(const double* __restrict__ soa, int64_t npad, int64_t g) {
+  qf::SegD d;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    d.n1[k] = soa[k * npad + g];
+    d.l[k] = soa[(3 + k) * npad + g] - d.n1[k];
+    d.b[k] = soa[(6 + k) * npad + g];
+    d.t[k] = soa[(9 + k) * npad + g];
+  }
+  return d;
+}
+
+// The near-parallel path out of line: rare, and its registers should not
+// count against the common path's.
 template <int NQ>
-__global__ void __launch_bounds__(TQ)
-quad_far_tiles(const float* __restrict__ ms, const float* __restrict__ qs, int64_t npad, const int4* __restrict__ items,
-               int32_t nItems, qf::QConst K, float kappa2, double* __restrict__ partial) {
+__device__ __noinline__ void par_pair_dev(const qf::QConst& K, const double* __restrict__ soa, int64_t npad, int64_t i,
+                                          int64_t j, double c, qf::V3f dm, qf::V3f li, qf::V3f bi, qf::V3f lj,
+                                          qf::V3f bj, qf::V3f& Fa, qf::V3f& Fb, qf::V3f& Fc, qf::V3f& Fd) {
+  qf::par_pair<NQ>(K, seg_d(soa, npad, i), seg_d(soa, npad, j), c, dm, li, bi, lj, bj, Fa, Fb, Fc, Fd);
+}
+
+// Five CTAs per SM: the rare near-parallel path (par_pair) spills rather than
+// lowering the occupancy of the common path.
+template <int NQ>
+__global__ void __launch_bounds__(TQ, 5)
+quad_far_tiles(const float* __restrict__ ms, const float* __restrict__ qs, const double* __restrict__ soa, int64_t npad,
+               const int4* __restrict__ items, int32_t nItems, qf::QConst K, float kappa2, double* __restrict__ partial) {
   __shared__ float cM[3][TQ], cLen[TQ];        // trust-test data of the column tile
   __shared__ float cQ[kQsRows][TQ];            // quadrature data of the column tile
   __shared__ float sFJ[TQ / 32][6][TQ];        // per-warp column forces
@@ -93,8 +126,21 @@ quad_far_tiles(const float* __restrict__ ms, const float* __restrict__ qs, int64
         const qf::V3f bj = {cQ[kQB + 0][jl], cQ[kQB + 1][jl], cQ[kQB + 2][jl]};
         const float Lnj = cQ[kQLen][jl];
         qf::V3f Fa, Fb, Fc, Fd;
-        qf::side<NQ>(K, dm, li, bi, tj, Lnj, bj, Fa, Fb);
-        qf::side<NQ>(K, {-dm.x, -dm.y, -dm.z}, lj, bj, ti, Lni, bi, Fc, Fd);
+        const float c32 = qf::dot(ti, tj);
+        bool par = false;
+        double c64 = 0.0;
+        if (1.0f - c32 * c32 <= 1e-5f) {  // FP32 error of 1 - c^2 < 1e-6: only these can be near-parallel
+          const int64_t gj = j0 + jl;
+          const double ti64[3] = {soa[9 * npad + i], soa[10 * npad + i], soa[11 * npad + i]};
+          const double tj64[3] = {soa[9 * npad + gj], soa[10 * npad + gj], soa[11 * npad + gj]};
+          par = qf::par_decision(ti64, tj64, c64);
+        }
+        if (!par) {
+          qf::side<NQ>(K, dm, li, bi, tj, Lnj, bj, Fa, Fb);
+          qf::side<NQ>(K, {-dm.x, -dm.y, -dm.z}, lj, bj, ti, Lni, bi, Fc, Fd);
+        } else {
+          par_pair_dev<NQ>(K, soa, npad, i, j0 + jl, c64, dm, li, bi, lj, bj, Fa, Fb, Fc, Fd);
+        }
         f1 = f1 + Fa;
         f2 = f2 + Fb;
         float* fj = &sFJ[warp][0][0];
@@ -139,14 +185,15 @@ int quad_far_blocks_per_sm(int nq) {
   return per > 0 ? per : 1;
 }
 
-cudaError_t launch_quad_far_tiles(const float* ms, const float* qs, int64_t npad, const int4* items, int32_t nItems,
-                                  int nq, const KConsts& K, float kappa2, double* partial, int grid, cudaStream_t st) {
+cudaError_t launch_quad_far_tiles(const float* ms, const float* qs, const double* soa, int64_t npad, const int4* items,
+                                  int32_t nItems, int nq, const KConsts& K, float kappa2, double* partial, int grid,
+                                  cudaStream_t st) {
   if (nItems <= 0) return cudaSuccess;
   const qf::QConst Q{(float)K.aSq, (float)K.mu4pi, (float)K.mu4pinu, (float)K.nuMu4pinu, (float)(K.aSq * K.mu8pi)};
   if (nq == 2)
-    quad_far_tiles<2><<<grid, TQ, 0, st>>>(ms, qs, npad, items, nItems, Q, kappa2, partial);
+    quad_far_tiles<2><<<grid, TQ, 0, st>>>(ms, qs, soa, npad, items, nItems, Q, kappa2, partial);
   else
-    quad_far_tiles<3><<<grid, TQ, 0, st>>>(ms, qs, npad, items, nItems, Q, kappa2, partial);
+    quad_far_tiles<3><<<grid, TQ, 0, st>>>(ms, qs, soa, npad, items, nItems, Q, kappa2, partial);
   return cudaGetLastError();
 }
 

@@ -128,5 +128,144 @@ QF_HD void side(const QConst& K, V3f dm, V3f lf, V3f bf, V3f to, float Lo, V3f b
   }
 }
 
+// sqrt(eps(Float64)) and hCotanθc of the reference's near-parallel branch
+// (DislocationForces.jl:892,1194).
+constexpr double kParEps = 1.4901161193847656e-08;
+constexpr double kParHCot = 4075.672300430329;
+
+// A source segment of a near-parallel pair as the reference rebuilds it:
+// offset of its midpoint from the original source segment's midpoint,
+// direction, length and Burgers vector (FP32).
+struct Src {
+  V3f off, to;
+  float Lo;
+  V3f bo;
+};
+
+QF_HD void vset(double* d, const double* a) { d[0] = a[0], d[1] = a[1], d[2] = a[2]; }
+QF_HD double dotd(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+// One segment from p to p + v (FP64, relative to the original source
+// midpoint) with Burgers b, as a Src; false when it has zero length.
+QF_HD bool make_src(const double* p, const double* v, const double* b, Src& s) {
+  const double L = sqrt(dotd(v, v));
+  if (!(L > 0.0)) return false;
+  s.off = {(float)(p[0] + 0.5 * v[0]), (float)(p[1] + 0.5 * v[1]), (float)(p[2] + 0.5 * v[2])};
+  s.to = {(float)(v[0] / L), (float)(v[1] / L), (float)(v[2] / L)};
+  s.Lo = (float)L;
+  s.bo = {(float)b[0], (float)b[1], (float)b[2]};
+  return true;
+}
+
+// One side of calcParSegSegForce (DislocationForces.jl:1204-1317, :1319-1433):
+// the source segment nb1 -> nb1 + lb (Burgers bb; FP64, nb1 relative to the
+// source's midpoint, nb1abs its absolute position) is projected onto the field
+// segment's direction ta and pulled in by the critical angle: with
+// proj = (lb.ta) ta, diff = lb - proj, the segment nbm1 = nb1 + diff/2 +
+// hCot |diff| ta -> nbm2 = nb1 + proj + diff/2 - hCot |diff| ta.  When the
+// rejection is not negligible against the positions (magDiffSq >
+// sqrt(eps) (|nbm1|^2 + |nbm2|^2), absolute coordinates; SIDE 1 takes
+// magDiffSq = diff.diff, SIDE 2 |diff|^2) the two connectors nb1 -> nbm1 and
+// nbm2 -> nb1 + lb are sources too.  Writes up to three sources; returns how
+// many.  The force on the field segment is the sum of their quadratures: the
+// reference evaluates the same geometry analytically.
+template <int SIDE>
+QF_HD int par_sources(const double* ta, const double* nb1, const double* nb1abs, const double* lb, const double* bb,
+                      Src* out) {
+  const double tmp = dotd(lb, ta);
+  const double proj[3] = {tmp * ta[0], tmp * ta[1], tmp * ta[2]};
+  const double diff[3] = {lb[0] - proj[0], lb[1] - proj[1], lb[2] - proj[2]};
+  const double dd = dotd(diff, diff);
+  const double magDiff = sqrt(dd);
+  const double tv1[3] = {0.5 * diff[0], 0.5 * diff[1], 0.5 * diff[2]};
+  const double tv2[3] = {kParHCot * magDiff * ta[0], kParHCot * magDiff * ta[1], kParHCot * magDiff * ta[2]};
+  double m1[3], m2[3];  // nbm1, nbm2 relative to the source midpoint
+  for (int k = 0; k < 3; ++k) {
+    m1[k] = nb1[k] + tv1[k] + tv2[k];
+    m2[k] = nb1[k] + proj[k] + tv1[k] - tv2[k];
+  }
+  int n = 0;
+  const double v[3] = {m2[0] - m1[0], m2[1] - m1[1], m2[2] - m1[2]};
+  if (make_src(m1, v, bb, out[n])) ++n;
+  double a1[3], a2[3];  // absolute nbm1, nbm2
+  for (int k = 0; k < 3; ++k) {
+    a1[k] = nb1abs[k] + tv1[k] + tv2[k];
+    a2[k] = nb1abs[k] + proj[k] + tv1[k] - tv2[k];
+  }
+  const double magDiffSq = SIDE == 1 ? dd : magDiff * magDiff;
+  if (magDiffSq > kParEps * (dotd(a1, a1) + dotd(a2, a2))) {
+    const double c1[3] = {tv1[0] + tv2[0], tv1[1] + tv2[1], tv1[2] + tv2[2]};  // nb1 -> nbm1
+    double e2[3], c2[3];                                                          // nbm2 -> nb1 + lb
+    for (int k = 0; k < 3; ++k) {
+      e2[k] = nb1[k] + lb[k];
+      c2[k] = e2[k] - m2[k];
+    }
+    if (make_src(nb1, c1, bb, out[n])) ++n;
+    if (make_src(m2, c2, bb, out[n])) ++n;
+  }
+  return n;
+}
+
+// FP64 record of one segment for the near-parallel path: node 1, n2 - n1,
+// Burgers vector and unit direction (the values the FP64 kernels use).
+struct SegD {
+  double n1[3], l[3], b[3], t[3];
+};
+
+// The reference's branch decision on the FP64 directions (c = t_i.t_j and
+// 1 - c^2 rounded as DislocationForces.jl:888-892 rounds them): true for the
+// near-parallel branch.
+QF_HD bool par_decision(const double* ti, const double* tj, double& c) {
+#if defined(__CUDA_ARCH__)
+  c = __dadd_rn(__dadd_rn(__dmul_rn(ti[0], tj[0]), __dmul_rn(ti[1], tj[1])), __dmul_rn(ti[2], tj[2]));
+  return !(__dsub_rn(1.0, __dmul_rn(c, c)) > kParEps);
+#else
+  c = ti[0] * tj[0] + ti[1] * tj[1] + ti[2] * tj[2];
+  return !(1.0 - c * c > kParEps);
+#endif
+}
+
+// A near-parallel pair (segment i = seg 1, j = seg 2 of calcParSegSegForce):
+// forces on i (Fa, Fb) and on j (Fc, Fd) from the reference's rebuilt sources,
+// dm = m_i - m_j and the FP32 segment vectors and Burgers vectors as the
+// general path takes them.  Seg 1 is flipped when c < 0, as the reference
+// does: side 1 then projects onto -t_i, and side 2's source is seg 1 reversed
+// (its Burgers vector negated).
+template <int NQ>
+QF_HD void par_pair(const QConst& K, const SegD& si, const SegD& sj, double c, V3f dm, V3f li, V3f bi, V3f lj, V3f bj,
+                    V3f& Fa, V3f& Fb, V3f& Fc, V3f& Fd) {
+  const bool flip = c < 0.0;
+  Src src[3];
+  Fa = Fb = Fc = Fd = {0.f, 0.f, 0.f};
+  {  // side 1: field i (direction t_i, or -t_i when flipped), source j
+    const double ta[3] = {flip ? -si.t[0] : si.t[0], flip ? -si.t[1] : si.t[1], flip ? -si.t[2] : si.t[2]};
+    const double nb1[3] = {-0.5 * sj.l[0], -0.5 * sj.l[1], -0.5 * sj.l[2]};
+    const int n = par_sources<1>(ta, nb1, sj.n1, sj.l, sj.b, src);
+    for (int q = 0; q < n; ++q) {
+      V3f a, b;
+      side<NQ>(K, dm - src[q].off, li, bi, src[q].to, src[q].Lo, src[q].bo, a, b);
+      Fa = Fa + a;
+      Fb = Fb + b;
+    }
+  }
+  {  // side 2: field j (direction t_j), source i (reversed when flipped)
+    double nb1abs[3], lb[3], bb[3], nb1[3];
+    for (int k = 0; k < 3; ++k) {
+      nb1abs[k] = flip ? si.n1[k] + si.l[k] : si.n1[k];
+      lb[k] = flip ? -si.l[k] : si.l[k];
+      bb[k] = flip ? -si.b[k] : si.b[k];
+      nb1[k] = -0.5 * lb[k];
+    }
+    const int n = par_sources<2>(sj.t, nb1, nb1abs, lb, bb, src);
+    const V3f dmj = {-dm.x, -dm.y, -dm.z};
+    for (int q = 0; q < n; ++q) {
+      V3f a, b;
+      side<NQ>(K, dmj - src[q].off, lj, bj, src[q].to, src[q].Lo, src[q].bo, a, b);
+      Fc = Fc + a;
+      Fd = Fd + b;
+    }
+  }
+}
+
 }  // namespace qf
 }  // namespace ddd

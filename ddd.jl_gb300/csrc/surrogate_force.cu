@@ -51,8 +51,9 @@ cudaError_t launch_mlp_far_tiles(const float* ms, int64_t npad, const int4* item
 size_t quad_seg_bytes(int64_t npad);
 cudaError_t launch_prep_quad_seg(const double* soa, const float* ms, int64_t npad, float* qs, cudaStream_t st);
 int quad_far_blocks_per_sm(int nq);
-cudaError_t launch_quad_far_tiles(const float* ms, const float* qs, int64_t npad, const int4* items, int32_t nItems,
-                                  int nq, const KConsts& K, float kappa2, double* partial, int grid, cudaStream_t st);
+cudaError_t launch_quad_far_tiles(const float* ms, const float* qs, const double* soa, int64_t npad, const int4* items,
+                                  int32_t nItems, int nq, const KConsts& K, float kappa2, double* partial, int grid,
+                                  cudaStream_t st);
 
 namespace sf {
 
@@ -605,7 +606,8 @@ int ddd_surrogate_force(ddd_surrogate* s, const ddd_consts* k, const double* seg
 
   // 2. far pass over every tile pair: the network, or Gauss-Legendre quadrature
   if (o.far_mode) {
-    SCK(launch_quad_far_tiles(P.ms.as<float>(), P.qs.as<float>(), npad, P.allItems.as<int4>(), (int32_t)P.nItems,
+    SCK(launch_quad_far_tiles(P.ms.as<float>(), P.qs.as<float>(), P.soa.as<double>(), npad, P.allItems.as<int4>(),
+                              (int32_t)P.nItems,
                               o.far_mode, K, kappa * kappa, P.partial.as<double>(),
                               (int)std::min<int64_t>(P.gridQuad, P.nItems), st),
         "quadrature pass");

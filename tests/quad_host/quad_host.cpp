@@ -3,8 +3,13 @@
 // difference from FP32 (hi, lo) midpoints, the segment vector, direction,
 // length and Burgers vector rounded to FP32.  Test infrastructure only: it
 // checks the form's accuracy on a CPU; the product runs the header on the GPU.
+// Near pairs of the network-level function take the oracle's restatement of the
+// reference (tests may use the oracle).
+#include <cmath>
 #include <cstdint>
+#include <vector>
 
+#include "../../oracle/ddd_oracle.hpp"
 #include "farfield_quad.cuh"
 
 using ddd::qf::V3f;
@@ -62,5 +67,98 @@ extern "C" void quad_pair_forces(const double* k5, const double* segs, const int
       out[12 * q + 3 * k + 1] = F[k].y;
       out[12 * q + 3 * k + 2] = F[k].z;
     }
+  }
+}
+
+// Forces on the given rows of a whole network (segs: n x 9 doubles, n1, n2, b)
+// as ddd_surrogate_force with far_mode = nq computes them: far pairs (the FP32
+// trust test R^2 >= kappa^2 max(L_i, L_j)^2 on FP32 midpoints and lengths) by
+// the quadrature, taking the reference's near-parallel construction where its
+// FP64 branch test says so (qf::par_pair, the kernel's own code), near pairs by
+// the oracle's FP64 restatement of the reference.  out: 6 per row (node 1,
+// node 2).  Summation in j order, FP64.
+extern "C" void quad_network_rows(const double* k5, const double* segs, int64_t n, double kappa, int nq,
+                                  const int64_t* rows, int64_t nRows, double* out) {
+  using namespace ddd::qf;
+  const QConst K{(float)k5[0], (float)k5[1], (float)k5[3], (float)k5[4], (float)(k5[0] * k5[2])};
+  ddd_oracle::Consts<double> KO;
+  KO.aSq = k5[0];
+  KO.mu4pi = k5[1];
+  KO.mu8pi = k5[2];
+  KO.mu4pinu = k5[3];
+  KO.nuMu4pinu = k5[4];
+  KO.mu8piaSq = KO.aSq * KO.mu8pi;
+  KO.mu4pinuaSq = KO.aSq * KO.mu4pinu;
+  std::vector<Prep> P(n);
+  std::vector<SegD> D(n);
+  std::vector<float> Lf(n);
+  for (int64_t i = 0; i < n; ++i) {
+    const double* s = segs + 9 * i;
+    P[i] = prep(s);
+    double l2 = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      D[i].n1[k] = s[k];
+      D[i].l[k] = s[3 + k] - s[k];
+      D[i].b[k] = s[6 + k];
+      l2 += D[i].l[k] * D[i].l[k];
+    }
+    const double tN = 1.0 / std::sqrt(l2);  // the FP64 kernels' direction and inverse length
+    for (int k = 0; k < 3; ++k) D[i].t[k] = D[i].l[k] * tN;
+    Lf[i] = (float)(1.0 / tN);
+    P[i].t = {(float)D[i].t[0], (float)D[i].t[1], (float)D[i].t[2]};
+    P[i].L = Lf[i];
+  }
+  const float k2 = (float)(kappa * kappa);
+  for (int64_t r = 0; r < nRows; ++r) {
+    const int64_t i = rows[r];
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    for (int64_t j = 0; j < n; ++j) {
+      if (j == i) continue;
+      const Prep &a = P[i], &b = P[j];
+      const float dx = b.mhi[0] - a.mhi[0], dy = b.mhi[1] - a.mhi[1], dz = b.mhi[2] - a.mhi[2];
+      const float R2 = (dx * dx + dy * dy) + dz * dz;
+      const float Lm = a.L > b.L ? a.L : b.L;
+      double F[6];
+      if (R2 >= k2 * (Lm * Lm)) {
+        const V3f dm = {(a.mhi[0] - b.mhi[0]) + (a.mlo[0] - b.mlo[0]), (a.mhi[1] - b.mhi[1]) + (a.mlo[1] - b.mlo[1]),
+                        (a.mhi[2] - b.mhi[2]) + (a.mlo[2] - b.mlo[2])};
+        V3f Fa, Fb, Fc, Fd;
+        double c = 0.0;
+        const float c32 = dot(a.t, b.t);
+        const bool par = 1.0f - c32 * c32 <= 1e-5f && par_decision(D[i].t, D[j].t, c);
+        if (!par) {
+          if (nq == 3)
+            side<3>(K, dm, a.l, a.b, b.t, b.L, b.b, Fa, Fb);
+          else
+            side<2>(K, dm, a.l, a.b, b.t, b.L, b.b, Fa, Fb);
+        } else if (i < j) {  // segment i is the reference's seg 1
+          if (nq == 3)
+            par_pair<3>(K, D[i], D[j], c, dm, a.l, a.b, b.l, b.b, Fa, Fb, Fc, Fd);
+          else
+            par_pair<2>(K, D[i], D[j], c, dm, a.l, a.b, b.l, b.b, Fa, Fb, Fc, Fd);
+        } else {  // segment i is seg 2: its forces are the pair's Fc, Fd
+          const V3f dmr = {-dm.x, -dm.y, -dm.z};
+          if (nq == 3)
+            par_pair<3>(K, D[j], D[i], c, dmr, b.l, b.b, a.l, a.b, Fc, Fd, Fa, Fb);
+          else
+            par_pair<2>(K, D[j], D[i], c, dmr, b.l, b.b, a.l, a.b, Fc, Fd, Fa, Fb);
+        }
+        F[0] = Fa.x, F[1] = Fa.y, F[2] = Fa.z, F[3] = Fb.x, F[4] = Fb.y, F[5] = Fb.z;
+      } else {
+        const double *s = segs + 9 * i, *q = segs + 9 * j;
+        ddd_oracle::V3<double> o[4];
+        if (i < j) {
+          ddd_oracle::seg_seg_force<double>(KO, {s[6], s[7], s[8]}, {s[0], s[1], s[2]}, {s[3], s[4], s[5]},
+                                            {q[6], q[7], q[8]}, {q[0], q[1], q[2]}, {q[3], q[4], q[5]}, o);
+          F[0] = o[0].x, F[1] = o[0].y, F[2] = o[0].z, F[3] = o[1].x, F[4] = o[1].y, F[5] = o[1].z;
+        } else {
+          ddd_oracle::seg_seg_force<double>(KO, {q[6], q[7], q[8]}, {q[0], q[1], q[2]}, {q[3], q[4], q[5]},
+                                            {s[6], s[7], s[8]}, {s[0], s[1], s[2]}, {s[3], s[4], s[5]}, o);
+          F[0] = o[2].x, F[1] = o[2].y, F[2] = o[2].z, F[3] = o[3].x, F[4] = o[3].y, F[5] = o[3].z;
+        }
+      }
+      for (int k = 0; k < 6; ++k) acc[k] += F[k];
+    }
+    for (int k = 0; k < 6; ++k) out[6 * r + k] = acc[k];
   }
 }

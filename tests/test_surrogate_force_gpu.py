@@ -231,17 +231,21 @@ def test_committed_checkpoint_gain_over_f32c_exact(pkg, synth):
     ref = torch.zeros((n, 6), dtype=torch.float64, device="cuda")
     ctx.segseg_force_device(k, d.data_ptr(), n, n, ref.data_ptr())
     ex = torch.zeros_like(ref)
-    st = torch.cuda.current_stream()
+    # A stream of its own: torch's default stream has handle 0, which the
+    # library reads as "its own stream", and the events would time nothing.
+    st = torch.cuda.Stream()
+    torch.cuda.synchronize()
 
     def timed(fn, reps=2):
-        fn()
-        torch.cuda.synchronize()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(st)
-        for _ in range(reps):
+        with torch.cuda.stream(st):
             fn()
-        b.record(st)
-        torch.cuda.synchronize()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            for _ in range(reps):
+                fn()
+            b.record(st)
+            torch.cuda.synchronize()
         return a.elapsed_time(b) / reps
 
     ctx.mode = "f32c"
@@ -274,20 +278,23 @@ def test_committed_checkpoint_gain_over_f32c_exact(pkg, synth):
     ms_quad = timed(run_quad)
     err_q = (torch.linalg.norm(out["Fq"] - ref) / torch.linalg.norm(ref)).item()
     assert out["repq"]["fallback"] == 0
-    assert err_q <= 2e-6, err_q
+    assert err_q <= 1e-6, err_q
     assert ms_quad < ms_f32c, (ms_quad, ms_f32c)
 
 
-@pytest.mark.parametrize("exact_mode,far", [("fp64", "quad3"), ("f32c", "quad3"), ("fp64", "quad2")])
-def test_quadrature_far_field(pkg, synth, oracle, exact_mode, far):
+@pytest.mark.parametrize("exact_mode,far,rel_max", [("fp64", "quad3", 1e-8), ("f32c", "quad3", 1e-6),
+                                                   ("fp64", "quad2", 1e-6)])
+def test_quadrature_far_field(pkg, synth, oracle, exact_mode, far, rel_max):
     """far = "quad3" / "quad2": far pairs by FP32 Gauss-Legendre quadrature on
-    both segments (no network), near pairs exact.  On a 12,000-segment network of
+    both segments (no network), near pairs exact; near-parallel far pairs take
+    the reference's projected geometry first.  On a 12,000-segment network of
     the workload's generator (mostly far pairs), against the long-double
-    evaluation of the reference's formulas on 96 sampled segments: relative RMS
-    <= 1e-6 (3 points) / 1e-5 (2 points), per node <= 1e-4 |F| + 1e-6 max|F|
-    (measured on a CPU: a far pair's force to ~2e-7 with 3 points).  The result
-    does not depend on the network's weights, every pair is counted once, and
-    repeats are bit-equal."""
+    evaluation of the reference's formulas on 96 sampled segments: relative
+    RMS <= 1e-8 with 3 points and FP64 near pairs (the CPU build of the same
+    code measures ~3e-10), <= 1e-6 with f32c near pairs (their own ~2e-7) or 2
+    points; per node <= 1e-4 |F| + 1e-6 max|F|.  The result does not depend on
+    the network's weights, every pair is counted once, and repeats are
+    bit-equal."""
     dln, mat = _params(pkg)
     net, segs = _network(pkg, synth, 1500, seed=41)
     n = segs.shape[1]
@@ -310,7 +317,7 @@ def test_quadrature_far_field(pkg, synth, oracle, exact_mode, far):
         with open(os.environ["DDD_TEST_STATS"], "a") as fh:
             fh.write("quadrature %s %s: rel rms %.3e max node %.3e audit %.3e %s\n" % (
                 far, exact_mode, rel, (nrm(G - ext) / nrm(ext)).max(), rep["audit_node_rel_rms"], rep))
-    assert rel <= (1e-6 if far == "quad3" else 1e-5), rel
+    assert rel <= rel_max, rel
     assert np.all(nrm(G - ext) <= 1e-4 * nrm(ext) + 1e-6 * nrm(ext).max())
 
 
