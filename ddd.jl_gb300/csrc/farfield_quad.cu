@@ -18,7 +18,9 @@
 //
 // Near-parallel pairs (1 - c^2 <= sqrt(eps) by the reference's FP64 test on
 // the FP64 directions; an FP32 pre-test with a wide margin picks the
-// candidates) take the reference's construction of calcParSegSegForce
+// candidates) are flagged during the sweep and evaluated afterwards in a
+// compacted dense pass (fixed order, so the sums stay deterministic), with the
+// reference's construction of calcParSegSegForce
 // (DislocationForces.jl:1167-1442): each side's source segment projected onto
 // the field segment's direction and pulled in by the critical angle, plus the
 // two connector segments where its core-correction test holds
@@ -68,39 +70,43 @@ __device__ __forceinline__ qf::SegD seg_d(const double* __restrict__ soa, int64_
   return d;
 }
 
-// The near-parallel path out of line: rare, and its registers should not
-// count against the common path's.
-template <int NQ>
-__device__ __noinline__ void par_pair_dev(const qf::QConst& K, const double* __restrict__ soa, int64_t npad, int64_t i,
-                                          int64_t j, double c, qf::V3f dm, qf::V3f li, qf::V3f bi, qf::V3f lj,
-                                          qf::V3f bj, qf::V3f& Fa, qf::V3f& Fb, qf::V3f& Fc, qf::V3f& Fd) {
-  qf::par_pair<NQ>(K, seg_d(soa, npad, i), seg_d(soa, npad, j), c, dm, li, bi, lj, bj, Fa, Fb, Fc, Fd);
-}
+// Shared memory of one CTA: the column tile, per-warp column forces, and the
+// compaction state of the near-parallel pairs.
+struct QuadSmem {
+  float cM[3][TQ], cLen[TQ];      // trust-test data of the column tile
+  float cQ[kQsRows][TQ];          // quadrature data of the column tile
+  float sFJ[TQ / 32][6][TQ];      // per-warp column forces
+  float cf[TQ][12];               // dense pass: one pair's four node forces per thread
+  uint16_t plist[TQ * TQ];        // near-parallel pairs (row << 8 | column), by row then step
+  int cnt[TQ];
+  int total;
+};
 
-// Five CTAs per SM: the rare near-parallel path (par_pair) spills rather than
-// lowering the occupancy of the common path.
+// Five CTAs of 128 threads per SM fit the registers; the near-parallel pairs
+// run in a dense pass after the sweep (as in tile_body.cuh), so a warp never
+// waits on one lane's FP64 branch.
 template <int NQ>
-__global__ void __launch_bounds__(TQ, 5)
+__global__ void __launch_bounds__(TQ)
 quad_far_tiles(const float* __restrict__ ms, const float* __restrict__ qs, const double* __restrict__ soa, int64_t npad,
                const int4* __restrict__ items, int32_t nItems, qf::QConst K, float kappa2, double* __restrict__ partial) {
-  __shared__ float cM[3][TQ], cLen[TQ];        // trust-test data of the column tile
-  __shared__ float cQ[kQsRows][TQ];            // quadrature data of the column tile
-  __shared__ float sFJ[TQ / 32][6][TQ];        // per-warp column forces
+  extern __shared__ __align__(16) unsigned char qsm_raw[];
+  QuadSmem& sm = *reinterpret_cast<QuadSmem*>(qsm_raw);
+  constexpr int NW = TQ / 32;
   const int t = threadIdx.x, warp = t >> 5;
   for (int32_t w = blockIdx.x; w < nItems; w += gridDim.x) {
     const int4 it = items[w];
-    const int64_t i = it.y + t, j0 = it.z;
+    const int64_t i0 = it.y, i = it.y + t, j0 = it.z;
     const bool diag = it.w != 0;
     __syncthreads();  // the previous item's readers are done with the tile
 #pragma unroll
-    for (int k = 0; k < 3; ++k) cM[k][t] = ms[(sur::kMsM + k) * npad + j0 + t];
-    cLen[t] = ms[sur::kMsL * npad + j0 + t];
+    for (int k = 0; k < 3; ++k) sm.cM[k][t] = ms[(sur::kMsM + k) * npad + j0 + t];
+    sm.cLen[t] = ms[sur::kMsL * npad + j0 + t];
 #pragma unroll
-    for (int k = 0; k < kQsRows; ++k) cQ[k][t] = qs[k * npad + j0 + t];
+    for (int k = 0; k < kQsRows; ++k) sm.cQ[k][t] = qs[k * npad + j0 + t];
 #pragma unroll
-    for (int q = 0; q < TQ / 32; ++q)
+    for (int q = 0; q < NW; ++q)
 #pragma unroll
-      for (int c = 0; c < 6; ++c) sFJ[q][c][t] = 0.0f;
+      for (int c = 0; c < 6; ++c) sm.sFJ[q][c][t] = 0.0f;
     const float mi[3] = {ms[(sur::kMsM + 0) * npad + i], ms[(sur::kMsM + 1) * npad + i],
                          ms[(sur::kMsM + 2) * npad + i]};
     const float Li = ms[sur::kMsL * npad + i];
@@ -110,61 +116,156 @@ quad_far_tiles(const float* __restrict__ ms, const float* __restrict__ qs, const
     const float Lni = qs[kQLen * npad + i];
     const qf::V3f bi = {qs[(kQB + 0) * npad + i], qs[(kQB + 1) * npad + i], qs[(kQB + 2) * npad + i]};
     __syncthreads();
+
+    // ---- Sweep: general far pairs by quadrature; near-parallel ones flagged. ----
     qf::V3f f1 = {0.f, 0.f, 0.f}, f2 = {0.f, 0.f, 0.f};
+    uint32_t pmask[NW];
+#pragma unroll
+    for (int q = 0; q < NW; ++q) pmask[q] = 0;
     for (int k = 0; k < TQ; ++k) {
       const int jl = (t + k) & (TQ - 1);
       float dx, dy, dz;
-      const bool far = sur::pair_is_far(mi[0], mi[1], mi[2], Li, cM[0][jl], cM[1][jl], cM[2][jl], cLen[jl], kappa2,
-                                        dx, dy, dz);
+      const bool far = sur::pair_is_far(mi[0], mi[1], mi[2], Li, sm.cM[0][jl], sm.cM[1][jl], sm.cM[2][jl],
+                                        sm.cLen[jl], kappa2, dx, dy, dz);
       if (far && (!diag || jl > t)) {
-        // m_i - m_j from the FP32 midpoints and their low parts.
-        const qf::V3f dm = {(mi[0] - cM[0][jl]) + (loi[0] - cQ[kQLo + 0][jl]),
-                            (mi[1] - cM[1][jl]) + (loi[1] - cQ[kQLo + 1][jl]),
-                            (mi[2] - cM[2][jl]) + (loi[2] - cQ[kQLo + 2][jl])};
-        const qf::V3f lj = {cQ[kQL + 0][jl], cQ[kQL + 1][jl], cQ[kQL + 2][jl]};
-        const qf::V3f tj = {cQ[kQT + 0][jl], cQ[kQT + 1][jl], cQ[kQT + 2][jl]};
-        const qf::V3f bj = {cQ[kQB + 0][jl], cQ[kQB + 1][jl], cQ[kQB + 2][jl]};
-        const float Lnj = cQ[kQLen][jl];
-        qf::V3f Fa, Fb, Fc, Fd;
+        const qf::V3f tj = {sm.cQ[kQT + 0][jl], sm.cQ[kQT + 1][jl], sm.cQ[kQT + 2][jl]};
         const float c32 = qf::dot(ti, tj);
         bool par = false;
-        double c64 = 0.0;
         if (1.0f - c32 * c32 <= 1e-5f) {  // FP32 error of 1 - c^2 < 1e-6: only these can be near-parallel
           const int64_t gj = j0 + jl;
           const double ti64[3] = {soa[9 * npad + i], soa[10 * npad + i], soa[11 * npad + i]};
           const double tj64[3] = {soa[9 * npad + gj], soa[10 * npad + gj], soa[11 * npad + gj]};
+          double c64;
           par = qf::par_decision(ti64, tj64, c64);
         }
-        if (!par) {
+        if (par) {
+          pmask[jl >> 5] |= 1u << (jl & 31);
+        } else {
+          // m_i - m_j from the FP32 midpoints and their low parts.
+          const qf::V3f dm = {(mi[0] - sm.cM[0][jl]) + (loi[0] - sm.cQ[kQLo + 0][jl]),
+                              (mi[1] - sm.cM[1][jl]) + (loi[1] - sm.cQ[kQLo + 1][jl]),
+                              (mi[2] - sm.cM[2][jl]) + (loi[2] - sm.cQ[kQLo + 2][jl])};
+          const qf::V3f lj = {sm.cQ[kQL + 0][jl], sm.cQ[kQL + 1][jl], sm.cQ[kQL + 2][jl]};
+          const qf::V3f bj = {sm.cQ[kQB + 0][jl], sm.cQ[kQB + 1][jl], sm.cQ[kQB + 2][jl]};
+          const float Lnj = sm.cQ[kQLen][jl];
+          qf::V3f Fa, Fb, Fc, Fd;
           qf::side<NQ>(K, dm, li, bi, tj, Lnj, bj, Fa, Fb);
           qf::side<NQ>(K, {-dm.x, -dm.y, -dm.z}, lj, bj, ti, Lni, bi, Fc, Fd);
-        } else {
-          par_pair_dev<NQ>(K, soa, npad, i, j0 + jl, c64, dm, li, bi, lj, bj, Fa, Fb, Fc, Fd);
+          f1 = f1 + Fa;
+          f2 = f2 + Fb;
+          float* fj = &sm.sFJ[warp][0][0];
+          fj[0 * TQ + jl] += Fc.x;
+          fj[1 * TQ + jl] += Fc.y;
+          fj[2 * TQ + jl] += Fc.z;
+          fj[3 * TQ + jl] += Fd.x;
+          fj[4 * TQ + jl] += Fd.y;
+          fj[5 * TQ + jl] += Fd.z;
         }
-        f1 = f1 + Fa;
-        f2 = f2 + Fb;
-        float* fj = &sFJ[warp][0][0];
-        fj[0 * TQ + jl] += Fc.x;
-        fj[1 * TQ + jl] += Fc.y;
-        fj[2 * TQ + jl] += Fc.z;
-        fj[3 * TQ + jl] += Fd.x;
-        fj[4 * TQ + jl] += Fd.y;
-        fj[5 * TQ + jl] += Fd.z;
       }
       __syncwarp();
     }
+
+    // ---- Near-parallel pairs: compact in a fixed order, evaluate densely. ----
+    int myCnt = 0;
+#pragma unroll
+    for (int q = 0; q < NW; ++q) myCnt += __popc(pmask[q]);
+    sm.cnt[t] = myCnt;
     __syncthreads();
+    if (warp == 0) {  // exclusive prefix sum over the 128 counts, 4 per lane
+      int v[NW], s4 = 0;
+#pragma unroll
+      for (int q = 0; q < NW; ++q) {
+        v[q] = sm.cnt[NW * t + q];
+        s4 += v[q];
+      }
+      int incl = s4;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int nb = __shfl_up_sync(0xffffffffu, incl, o);
+        if ((t & 31) >= o) incl += nb;
+      }
+      int excl = incl - s4;
+#pragma unroll
+      for (int q = 0; q < NW; ++q) {
+        sm.cnt[NW * t + q] = excl;
+        excl += v[q];
+      }
+    }
+    __syncthreads();
+    const int myOff = sm.cnt[t];
+    if (t == TQ - 1) sm.total = myOff + myCnt;
+    {
+      int o = myOff;
+      for (int k = 0; k < TQ; ++k) {
+        const int jl = (t + k) & (TQ - 1);
+        if (pmask[jl >> 5] & (1u << (jl & 31))) sm.plist[o++] = (uint16_t)((t << 8) | jl);
+      }
+    }
+    __syncthreads();
+    const int nPar = sm.total;
+    qf::V3f fc3 = {0.f, 0.f, 0.f}, fc4 = {0.f, 0.f, 0.f};  // this thread's column segment
+    for (int base = 0; base < nPar; base += TQ) {
+      const int e = base + t;
+      if (e < nPar) {
+        const int il = sm.plist[e] >> 8, jl = sm.plist[e] & 0xff;
+        const int64_t gi = i0 + il, gj = j0 + jl;
+        const qf::SegD si = seg_d(soa, npad, gi), sj = seg_d(soa, npad, gj);
+        double c;
+        qf::par_decision(si.t, sj.t, c);
+        const float mi2[3] = {ms[(sur::kMsM + 0) * npad + gi], ms[(sur::kMsM + 1) * npad + gi],
+                              ms[(sur::kMsM + 2) * npad + gi]};
+        const qf::V3f dm = {(mi2[0] - sm.cM[0][jl]) + (qs[(kQLo + 0) * npad + gi] - sm.cQ[kQLo + 0][jl]),
+                            (mi2[1] - sm.cM[1][jl]) + (qs[(kQLo + 1) * npad + gi] - sm.cQ[kQLo + 1][jl]),
+                            (mi2[2] - sm.cM[2][jl]) + (qs[(kQLo + 2) * npad + gi] - sm.cQ[kQLo + 2][jl])};
+        const qf::V3f la = {qs[(kQL + 0) * npad + gi], qs[(kQL + 1) * npad + gi], qs[(kQL + 2) * npad + gi]};
+        const qf::V3f ba = {qs[(kQB + 0) * npad + gi], qs[(kQB + 1) * npad + gi], qs[(kQB + 2) * npad + gi]};
+        const qf::V3f lb = {sm.cQ[kQL + 0][jl], sm.cQ[kQL + 1][jl], sm.cQ[kQL + 2][jl]};
+        const qf::V3f bb = {sm.cQ[kQB + 0][jl], sm.cQ[kQB + 1][jl], sm.cQ[kQB + 2][jl]};
+        qf::V3f Fa, Fb, Fc, Fd;
+        qf::par_pair<NQ>(K, si, sj, c, dm, la, ba, lb, bb, Fa, Fb, Fc, Fd);
+        const float v[12] = {Fa.x, Fa.y, Fa.z, Fb.x, Fb.y, Fb.z, Fc.x, Fc.y, Fc.z, Fd.x, Fd.y, Fd.z};
+#pragma unroll
+        for (int c2 = 0; c2 < 12; ++c2) sm.cf[t][c2] = v[c2];
+      }
+      __syncthreads();
+      const int lim = min(TQ, nPar - base);
+      // Row forces: this thread's own entries, in list order.
+      const int lo = max(myOff, base), hi = min(myOff + myCnt, base + lim);
+      for (int e2 = lo; e2 < hi; ++e2) {
+        const float* f = sm.cf[e2 - base];
+        f1 = f1 + qf::V3f{f[0], f[1], f[2]};
+        f2 = f2 + qf::V3f{f[3], f[4], f[5]};
+      }
+      // Column forces: the entries whose column is this thread's, in list order.
+      for (int q = 0; q < lim; ++q) {
+        if ((sm.plist[base + q] & 0xff) == t) {
+          const float* f = sm.cf[q];
+          fc3 = fc3 + qf::V3f{f[6], f[7], f[8]};
+          fc4 = fc4 + qf::V3f{f[9], f[10], f[11]};
+        }
+      }
+      __syncthreads();
+    }
+
+    // ---- Partials: row segments' then column segments' node forces. ----
     double* p = partial + (int64_t)it.x * 12 * TQ;
     const float row[6] = {f1.x, f1.y, f1.z, f2.x, f2.y, f2.z};
+    const float colp[6] = {fc3.x, fc3.y, fc3.z, fc4.x, fc4.y, fc4.z};
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
       p[c * TQ + t] = (double)row[c];
-      double v = 0.0;
+      double v = (double)colp[c];
 #pragma unroll
-      for (int q = 0; q < TQ / 32; ++q) v += (double)sFJ[q][c][t];
+      for (int q = 0; q < NW; ++q) v += (double)sm.sFJ[q][c][t];
       p[(6 + c) * TQ + t] = v;
     }
   }
+}
+
+template <int NQ>
+cudaError_t set_attr_quad() {
+  static std::atomic<uint64_t> done{0};
+  return set_smem_once(quad_far_tiles<NQ>, (int)sizeof(QuadSmem), done);
 }
 
 }  // namespace
@@ -178,10 +279,13 @@ cudaError_t launch_prep_quad_seg(const double* soa, const float* ms, int64_t npa
 
 int quad_far_blocks_per_sm(int nq) {
   int per = 0;
-  if (nq == 2)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, quad_far_tiles<2>, TQ, 0);
-  else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, quad_far_tiles<3>, TQ, 0);
+  if (nq == 2) {
+    if (set_attr_quad<2>() == cudaSuccess)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, quad_far_tiles<2>, TQ, sizeof(QuadSmem));
+  } else {
+    if (set_attr_quad<3>() == cudaSuccess)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, quad_far_tiles<3>, TQ, sizeof(QuadSmem));
+  }
   return per > 0 ? per : 1;
 }
 
@@ -190,10 +294,12 @@ cudaError_t launch_quad_far_tiles(const float* ms, const float* qs, const double
                                   cudaStream_t st) {
   if (nItems <= 0) return cudaSuccess;
   const qf::QConst Q{(float)K.aSq, (float)K.mu4pi, (float)K.mu4pinu, (float)K.nuMu4pinu, (float)(K.aSq * K.mu8pi)};
+  cudaError_t e = nq == 2 ? set_attr_quad<2>() : set_attr_quad<3>();
+  if (e != cudaSuccess) return e;
   if (nq == 2)
-    quad_far_tiles<2><<<grid, TQ, 0, st>>>(ms, qs, soa, npad, items, nItems, Q, kappa2, partial);
+    quad_far_tiles<2><<<grid, TQ, sizeof(QuadSmem), st>>>(ms, qs, soa, npad, items, nItems, Q, kappa2, partial);
   else
-    quad_far_tiles<3><<<grid, TQ, 0, st>>>(ms, qs, soa, npad, items, nItems, Q, kappa2, partial);
+    quad_far_tiles<3><<<grid, TQ, sizeof(QuadSmem), st>>>(ms, qs, soa, npad, items, nItems, Q, kappa2, partial);
   return cudaGetLastError();
 }
 
