@@ -870,7 +870,7 @@ class Surrogate:
               stream=None, far="network"):
         """ddd_surrogate_force on packed 9 × n segments (a CUDA float64 tensor or
         a numpy array); exact_mode: arithmetic of the exact near / audit passes
-        ("fp64", "df64" or "f32c"); far: "network", or "quad2" / "quad3" for
+        ("fp64", "fp64_fast", "df64" or "f32c"); far: "network", or "quad2" / "quad3" for
         the far pairs by FP32 Gauss-Legendre quadrature (no network used).
         Returns (forces as a CUDA tensor n × 6 = the 3 × 2 × n column-major
         array, report dict)."""

@@ -13,40 +13,13 @@
 
 #include "ddd_internal.h"
 #include "pair_f64.cuh"
-#include "pair_f64fast.cuh"
-#include "tile_body.cuh"
+#include "tile_pol_fx.cuh"
 
 namespace ddd {
 
 namespace {
 
 constexpr int TILE = 128;
-
-__device__ __forceinline__ fx::X3 x3(const D3& v) { return {v.x, v.y, v.z}; }
-__device__ __forceinline__ D3 d3(const fx::X3& v) { return {v.x, v.y, v.z}; }
-
-// The FP64 policy with the fast general branch.
-struct PolF64Fast : PolF64 {
-  template <bool BOTH>
-  static __device__ __forceinline__ void general(const Consts&, const TileArgs& A, const Seg& a, const Seg& b,
-                                                 double c, D3& F1, D3& F2, D3& F3, D3& F4) {
-    const fx::KFast K{A.K.aSq, A.K.mu4pi, A.K.mu8pi, A.K.mu4pinu, A.K.mu8piaSq, A.K.mu4pinuaSq};
-    fx::X3 G1, G2, G3, G4;
-    fx::general_pair<true, BOTH, true>(K, x3(a.b), x3(a.n1), x3(a.n2), x3(a.t), a.tN, x3(b.b), x3(b.n1), x3(b.n2),
-                                       x3(b.t), b.tN, c, G1, G2, G3, G4);
-    F1 = d3(G1);
-    F2 = d3(G2);
-    if (BOTH) {
-      F3 = d3(G3);
-      F4 = d3(G4);
-    }
-  }
-  static __device__ __forceinline__ void dense_general(const Consts& KP, const TileArgs& A, int64_t gi, int64_t gj,
-                                                       D3& F1, D3& F2, D3& F3, D3& F4) {
-    const SegF64 a = tb_load_seg64(A.soa, A.npad, gi), b = tb_load_seg64(A.soa, A.npad, gj);
-    general<true>(KP, A, a, b, dot(a.t, b.t), F1, F2, F3, F4);
-  }
-};
 
 __device__ __forceinline__ void tile_index_fx(int64_t b, int64_t& I, int64_t& J) {
   int64_t Jc = (int64_t)((sqrt(8.0 * (double)b + 1.0) - 1.0) * 0.5);

@@ -39,6 +39,7 @@
 #include "surrogate_state.h"
 #include "tile_body.cuh"
 #include "tile_pol_df.cuh"
+#include "tile_pol_fx.cuh"
 
 namespace ddd {
 
@@ -413,12 +414,15 @@ cudaError_t launch_exact_p(const TileArgs& A, const typename P::Consts& KP, cons
 }
 
 // The exact tile pass in the arithmetic of `mode` (DDD_MODE_FP64 strict,
-// DDD_MODE_DF64 or DDD_MODE_F32C for the general branch).
+// DDD_MODE_FP64_FAST, DDD_MODE_DF64 or DDD_MODE_F32C for the general branch).
 template <int MODE>
 cudaError_t launch_exact(int mode, const TileArgs& A, const int4* items, const int32_t* nDev, int32_t nHost,
                          int32_t* next, double* partial, unsigned long long* counters, int grid, cudaStream_t st) {
   if (mode == DDD_MODE_FP64)
     return launch_exact_p<MODE, PolF64>(A, PolF64::Consts{}, items, nDev, nHost, next, partial, counters, grid, st);
+  if (mode == DDD_MODE_FP64_FAST)
+    return launch_exact_p<MODE, PolF64Fast>(A, PolF64Fast::Consts{}, items, nDev, nHost, next, partial, counters, grid,
+                                            st);
   const typename PolDF<0>::Consts KP{kconsts_df(A.K), kconsts_f(A.K)};
   if (mode == DDD_MODE_DF64)
     return launch_exact_p<MODE, PolDF<0>>(A, KP, items, nDev, nHost, next, partial, counters, grid, st);
@@ -537,8 +541,9 @@ int ddd_surrogate_force(ddd_surrogate* s, const ddd_consts* k, const double* seg
   if (!s) return DDD_EINVAL;
   ddd_sur_opts o{20.0, 0.01, 1e-3, DDD_MODE_FP64, 0};
   if (opts) o = *opts;
-  if (o.exact_mode != DDD_MODE_FP64 && o.exact_mode != DDD_MODE_DF64 && o.exact_mode != DDD_MODE_F32C)
-    return sfail(s, DDD_EINVAL, "exact_mode must be DDD_MODE_FP64, DDD_MODE_DF64 or DDD_MODE_F32C");
+  if (o.exact_mode != DDD_MODE_FP64 && o.exact_mode != DDD_MODE_FP64_FAST && o.exact_mode != DDD_MODE_DF64 &&
+      o.exact_mode != DDD_MODE_F32C)
+    return sfail(s, DDD_EINVAL, "exact_mode must be DDD_MODE_FP64, DDD_MODE_FP64_FAST, DDD_MODE_DF64 or DDD_MODE_F32C");
   if (o.far_mode != 0 && o.far_mode != 2 && o.far_mode != 3)
     return sfail(s, DDD_EINVAL, "far_mode must be 0 (network) or 2 / 3 (Gauss points of the quadrature)");
   if (!k) return sfail(s, DDD_EINVAL, "consts is NULL");
@@ -572,7 +577,8 @@ int ddd_surrogate_force(ddd_surrogate* s, const ddd_consts* k, const double* seg
   K.mu4pinuaSq = k->aSq * k->mu4pinu;
   const float kappa = (float)o.kappa;
   const int xm = o.exact_mode;
-  if (xm != DDD_MODE_FP64) SCK(P.soadf.ensure((size_t)npad * 26 * sizeof(float)), "allocate df64 segments");
+  const bool dfx = xm == DDD_MODE_DF64 || xm == DDD_MODE_F32C;  // the exact passes read df64 segment data
+  if (dfx) SCK(P.soadf.ensure((size_t)npad * 26 * sizeof(float)), "allocate df64 segments");
   if (o.far_mode) SCK(P.qs.ensure(quad_seg_bytes(npad)), "allocate quadrature segment data");
   TileArgs A{K, P.soa.as<double>(), P.skip.as<uint8_t>(), npad, P.soadf.as<float>(), nullptr};
   A.ms = P.ms.as<float>();
@@ -597,7 +603,7 @@ int ddd_surrogate_force(ddd_surrogate* s, const ddd_consts* k, const double* seg
   SCK(launch_prep_mlp_seg(P.soa.as<double>(), P.skip.as<uint8_t>(), npad, P.ms.as<float>(), st), "prep_mlp_seg");
   if (o.far_mode)
     SCK(launch_prep_quad_seg(P.soa.as<double>(), P.ms.as<float>(), npad, P.qs.as<float>(), st), "prep_quad_seg");
-  if (xm != DDD_MODE_FP64) SCK(launch_prep_df(P.soa.as<double>(), npad, P.soadf.as<float>(), st), "prep_df");
+  if (dfx) SCK(launch_prep_df(P.soa.as<double>(), npad, P.soadf.as<float>(), st), "prep_df");
   sf::tile_boxes<<<(unsigned)nt, sf::T, 0, st>>>(P.ms.as<float>(), npad, P.tbox.as<float>());
   sf::near_items<<<(unsigned)((P.nItems + 255) / 256), 256, 0, st>>>(
       P.allItems.as<int4>(), (int32_t)P.nItems, P.tbox.as<float>(), kappa, P.nearItems.as<int4>(), &dv->nearCount);

@@ -462,7 +462,7 @@ typedef struct {
   double audit_fraction; /* in [0, 1]; 0 disables the audit */
   double audit_tol;      /* bound of the estimated node-force relative RMS error; <= 0: no fallback */
   int exact_mode;        /* arithmetic of the exact passes (near, audit, fallback): DDD_MODE_FP64 (strict),
-                            DDD_MODE_DF64 or DDD_MODE_F32C for the general branch */
+                            DDD_MODE_FP64_FAST, DDD_MODE_DF64 or DDD_MODE_F32C for the general branch */
   int far_mode;          /* 0: far pairs through the network; 2 or 3: through Gauss-Legendre quadrature with
                             that many points on each segment, in FP32 (no network involved: the surrogate's
                             weights and trained Poisson ratio are not used) */
