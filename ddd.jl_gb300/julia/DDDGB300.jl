@@ -17,9 +17,9 @@ using Statistics: mean
 
 export calcSegSegForceGPU, calcSegSegForceGPU!, calc_σTildeGPU, calc_σTildeGPU!
 export calcSelfForceGPU, calcSelfForceGPU!, calcSegForceGPU, calcSegForceGPU!
-export Surrogate, loadSurrogate, calcSegSegForceSurrogateGPU
+export Surrogate, loadSurrogate, quadratureFarField, calcSegSegForceSurrogateGPU
 export dlnMobilityGPU, dlnMobilityGPU!, detectCollisionGPU, minimumDistanceGPU, calc_uTildeGPU, calc_uTildeGPU!
-export setPartialLimitGPU, partialLimitGPU
+export setPartialLimitGPU, partialLimitGPU, setModeGPU, modeGPU
 
 const libddd = joinpath(@__DIR__, "..", "libddd_gb300.so")
 
@@ -62,6 +62,13 @@ idxvec(idx) = isnothing(idx) ? Int64[] : collect(Int64, idx)
 setPartialLimitGPU(bytes::Integer) =
     check(ccall((:ddd_set_partial_limit, libddd), Cint, (Ptr{Cvoid}, Int64), context(), bytes))
 partialLimitGPU() = ccall((:ddd_get_partial_limit, libddd), Int64, (Ptr{Cvoid},), context())
+
+# Arithmetic of the context's kernels (ddd_set_mode): 0 = strict FP64, the
+# reference's formulas and rounding (default); 4 = the fast FP64 form (same
+# formulas, fewer FP64 instructions, within the strict form's parity bound);
+# 1 = FP64 with FMA contraction; 2 = df64; 3 = f32c.
+setModeGPU(mode::Integer) = check(ccall((:ddd_set_mode, libddd), Cint, (Ptr{Cvoid}, Cint), context(), mode))
+modeGPU() = ccall((:ddd_get_mode, libddd), Cint, (Ptr{Cvoid},), context())
 
 # calcSegSegForce (src/Processing/DislocationForces.jl:470-561)
 function calcSegSegForceGPU(dlnParams, matParams, network, idx = nothing)
@@ -389,6 +396,7 @@ struct DDDSurOpts
     audit_fraction::Float64
     audit_tol::Float64
     exact_mode::Cint
+    far_mode::Cint
 end
 
 struct DDDSurReport
@@ -436,15 +444,28 @@ function loadSurrogate(path::AbstractString)
     return s
 end
 
-# exact_mode: 0 = strict FP64 (DDD_MODE_FP64), 2 = df64, 3 = f32c.
+# A handle without a checkpoint, for far_mode = 2 or 3 (the quadrature reads
+# no weights); kappa is the near/far threshold R >= kappa max(L_i, L_j).
+function quadratureFarField(; kappa = 20.0)
+    p = ccall((:ddd_surrogate_create, libddd), Ptr{Cvoid}, (Ptr{Cvoid}, UInt64), context(), 0)
+    p == C_NULL && error("ddd_surrogate_create failed")
+    s = Surrogate(p, kappa, NaN)
+    finalizer(x -> ccall((:ddd_surrogate_destroy, libddd), Cvoid, (Ptr{Cvoid},), x.ptr), s)
+    return s
+end
+
+# exact_mode: 0 = strict FP64 (DDD_MODE_FP64), 4 = fast FP64, 2 = df64, 3 = f32c.
+# far_mode: 0 = far pairs through the network; 2 or 3 = Gauss-Legendre
+# quadrature with that many points per segment (no weights read).
 function calcSegSegForceSurrogateGPU(s::Surrogate, dlnParams, matParams, network;
-                                     audit_fraction = 0.01, audit_tol = 1e-3, exact_mode = 0)
+                                     audit_fraction = 0.01, audit_tol = 1e-3, exact_mode = 0, far_mode = 0)
     nu = 1 - matParams.μ4π / matParams.μ4πν
-    isnan(s.nu) || abs(nu - s.nu) <= 1e-9 || throw(ArgumentError("surrogate trained for nu = $(s.nu), not $nu"))
+    far_mode != 0 || isnan(s.nu) || abs(nu - s.nu) <= 1e-9 ||
+        throw(ArgumentError("surrogate trained for nu = $(s.nu), not $nu"))
     numSeg = network.numSeg[1]
     out = zeros(3, 2, numSeg)
     k = Ref(consts(dlnParams, matParams))
-    opts = Ref(DDDSurOpts(s.kappa, audit_fraction, audit_tol, exact_mode))
+    opts = Ref(DDDSurOpts(s.kappa, audit_fraction, audit_tol, exact_mode, far_mode))
     rep = Ref{DDDSurReport}()
     coord, bVec, segIdx, extSeg = network.coord, network.bVec, network.segIdx, network.extSeg
     GC.@preserve coord bVec segIdx extSeg out begin

@@ -120,3 +120,51 @@ def test_product_iterator_points(pkg):
     assert [tuple(P[:, j]) for j in range(24)] == want
     with pytest.raises(AssertionError):
         pkg.calc_σTilde_inplace(np.zeros((6, 24)), it, None, None, None)
+
+
+# Julia struct of the shim -> C struct of the header.
+JULIA_STRUCTS = {"DDDConsts": "ddd_consts", "DDDSelfParams": "ddd_self_params", "DDDMobParams": "ddd_mob_params",
+                 "DDDCollision": "ddd_collision", "DDDUMesh": "ddd_u_mesh", "DDDSurOpts": "ddd_sur_opts",
+                 "DDDSurReport": "ddd_sur_report"}
+_C_TYPES = {"double": "f64", "int": "i32", "int32_t": "i32", "int64_t": "i64", "const double*": "ptr"}
+_JL_TYPES = {"Float64": "f64", "Cint": "i32", "Int32": "i32", "Int64": "i64", "Ptr{Float64}": "ptr"}
+
+
+def _c_struct_fields(text, name):
+    m = re.search(r"typedef struct(?: \w+)? \{([^{}]*)\} " + name + ";", text)
+    assert m, name
+    body = re.sub(r"/\*.*?\*/", "", m.group(1), flags=re.S)
+    fields = []
+    for decl in body.split(";"):
+        decl = " ".join(decl.split())
+        if not decl:
+            continue
+        t = re.match(r"(const double\*|double|int64_t|int32_t|int)\s+(.*)", decl)
+        assert t, decl
+        for var in t.group(2).split(","):
+            var = var.strip()
+            a = re.match(r"(\w+)\[(\d+)\]$", var)
+            fields.append((a.group(1), _C_TYPES[t.group(1)], int(a.group(2))) if a else
+                          (var, _C_TYPES[t.group(1)], 1))
+    return fields
+
+
+def _jl_struct_fields(text, name):
+    m = re.search(r"^struct " + name + r"\n(.*?)^end", text, re.S | re.M)
+    assert m, name
+    fields = []
+    for line in m.group(1).strip().splitlines():
+        var, typ = [x.strip() for x in line.split("::")]
+        a = re.match(r"NTuple\{(\d+), (\w+)\}", typ)
+        fields.append((var, _JL_TYPES[a.group(2)], int(a.group(1))) if a else (var, _JL_TYPES[typ], 1))
+    return fields
+
+
+def test_julia_shim_structs_match_header():
+    """Every struct the Julia binding passes by reference has the header's
+    fields, in order, with the same widths (a missing trailing field would let
+    the library read past the caller's struct)."""
+    jl = open(os.path.join(ROOT, "ddd.jl_gb300", "julia", "DDDGB300.jl")).read()
+    c = open(HEADER).read()
+    for jname, cname in JULIA_STRUCTS.items():
+        assert _jl_struct_fields(jl, jname) == _c_struct_fields(c, cname), jname
