@@ -1084,8 +1084,8 @@ def main():
                 "d2h_bytes_per_step": erep["d2h_bytes"], "steps": e2e_steps, "matches_device_path": same},
         "gpu_launches": 3 * args.steps,
         "mode": {"fp64": "fp64 (strict: every multiply and add rounded separately, as the reference)",
-                 "fp64_fast": "fp64_fast (FP64 throughout, reformulated: one division per corner, table-driven "
-                              "log/atan, explicit FMAs where the reference's terms do not cancel; same parity bound "
+                 "fp64_fast": "fp64_fast (FP64 throughout, reformulated: one division per corner, log/atan in "
+                              "integer fixed point on the integer pipes, explicit FMAs where the reference's terms do not cancel; same parity bound "
                               "as the strict form, checked below)"}[args.mode],
         "variants": variants,
         "surrogate": surrogate,

@@ -7,8 +7,11 @@
 //     R2 = Ra + x + y c and Q = 1 / (Ra R1 R2), 1/(Ra R1) = Q R2,
 //     1/(Ra R2) = Q R1 and 1/Ra = Q (R1 R2); the division by a^2 + d^2(1 - c^2)
 //     becomes a product with its reciprocal, taken once per pair;
-//   * the logarithms and arctangents are the table-driven fm::log / fm::atan
-//     (fastmath_f64.cuh), or CUDA's, by the template flag FMATH;
+//   * the logarithms and arctangents are, by the template argument FMATH:
+//     the integer-pipe im::log / im::atan (intmath_f64.cuh, kMathInt: they
+//     take no FP64 pipe slots and are correctly rounded but for ~1 case in
+//     10^3), the FP64 table-driven fm::log / fm::atan (fastmath_f64.cuh,
+//     kMathTable) or CUDA's (kMathCuda);
 //   * explicit fused multiply-adds (fma_) in the corner terms, the products of
 //     unit and Burgers vectors, and the force assembly, which is regrouped on
 //     five vectors per side;
@@ -21,9 +24,11 @@
 //     more accurate than the reference (0.6x its error on sparse networks) but
 //     moves it ~3e-10 away from the reference's values, past the parity bound.
 // Everything else is plain IEEE arithmetic, so the same header compiled for a
-// CPU (no contraction) gives the GPU's results bit for bit when FMATH = true.
+// CPU (no contraction) gives the GPU's results bit for bit when FMATH is
+// kMathInt or kMathTable.
 #pragma once
 #include "fastmath_f64.cuh"
+#include "intmath_f64.cuh"
 
 namespace ddd {
 namespace fx {
@@ -52,14 +57,18 @@ struct KFast {
   double aSq, mu4pi, mu8pi, mu4pinu, mu8piaSq, mu4pinuaSq;
 };
 
-template <bool FMATH>
+constexpr int kMathCuda = 0, kMathTable = 1, kMathInt = 2;
+
+template <int FMATH>
 FM_HD double lg(double v) {
-  if (FMATH) return fm::log(v);
+  if (FMATH == kMathInt) return im::log(v);
+  if (FMATH == kMathTable) return fm::log(v);
   return fm::std_log(v);
 }
-template <bool FMATH>
+template <int FMATH>
 FM_HD double at(double v) {
-  if (FMATH) return fm::atan(v);
+  if (FMATH == kMathInt) return im::atan(v);
+  if (FMATH == kMathTable) return fm::atan(v);
   return fm::std_atan(v);
 }
 
@@ -72,7 +81,7 @@ struct CornerK {
 // SegSegInteg at one corner (DislocationForces.jl:1480-1561), added (sm = 0) or
 // subtracted (sm = sign bit) into integ[19]; the first corner (FIRST, sm = 0)
 // writes instead of adding to zero.
-template <bool FMATH, bool FIRST>
+template <int FMATH, bool FIRST>
 FM_HD void corner(const CornerK& P, double x, double y, long long sm, double* integ) {
   const double aSq_dSq = P.aSq_dSq, c = P.c, cSq = P.cSq, omcSqI = P.omcSqI;
   const double xSq = x * x;
@@ -141,7 +150,7 @@ FM_HD void corner(const CornerK& P, double x, double y, long long sm, double* in
 }
 
 // General branch of calcSegSegForce; NEED12 / NEED34 as in pair_f64.cuh.
-template <bool NEED12, bool NEED34, bool FMATH>
+template <bool NEED12, bool NEED34, int FMATH>
 FM_HD void general_pair(const KFast& K, X3 b1, X3 n11, X3 n12, X3 t1, double t1N, X3 b2, X3 n21, X3 n22, X3 t2,
                         double t2N, double c, X3& F1, X3& F2, X3& F3, X3& F4) {
   const double mu4pi = K.mu4pi, mu4pinu = K.mu4pinu, mu8piaSq = K.mu8piaSq, mu4pinuaSq = K.mu4pinuaSq;

@@ -2,7 +2,8 @@
 // (DDD_MODE_FP64_FAST): the FP64 kernel's tiles, schedule, near-parallel
 // compaction and deterministic reduction (tile_body.cuh, segseg_f64.cu) with
 // the general branch of pair_f64fast.cuh — one division per corner instead of
-// four, table-driven logarithms and arctangents, explicit fused multiply-adds
+// four, logarithms and arctangents in integer fixed point on the integer pipes
+// (intmath_f64.cuh, off the FP64 pipe), explicit fused multiply-adds
 // where the reference's terms do not cancel.  The near-parallel branch, the
 // branch decision and the segment preparation stay the strict FP64 code.
 //

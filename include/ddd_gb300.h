@@ -69,8 +69,9 @@ typedef struct ddd_ctx ddd_ctx;
  * DDD_MODE_DF64.  Measured node-force error ~5e-8 relative RMS. */
 #define DDD_MODE_F32C 3
 /* DDD_MODE_FP64_FAST, FP64 throughout with fewer FP64 instructions per pair:
- * the general branch with one division per corner instead of four, table-
- * driven logarithms and arctangents (about 1 ulp), and fused multiply-adds
+ * the general branch with one division per corner instead of four,
+ * logarithms and arctangents computed in integer fixed point on the integer
+ * pipes (within 0.51 ulp; they take no FP64 pipe time), and fused multiply-adds
  * wherever the reference's terms do not cancel; the quantities whose rounding
  * sets the reference's own error (c, 1 - c^2, the pair geometry, the local
  * coordinates, Ra and Ra + y + x c) are rounded as the reference rounds them,

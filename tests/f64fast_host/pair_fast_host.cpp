@@ -1,7 +1,7 @@
 // Host build of the fast FP64 form of the seg-seg force (DDD_MODE_FP64_FAST):
 // ddd.jl_gb300/csrc/pair_f64fast.cuh compiled as plain C++ without contraction,
 // so its general branch gives the GPU's values bit for bit (with the
-// table-driven logarithm and arctangent).  Pairs that take the near-parallel
+// integer-pipe or table-driven logarithm and arctangent).  Pairs that take the near-parallel
 // branch, which the GPU form evaluates in the reference's strict arithmetic,
 // use the oracle's restatement here.  Test infrastructure only: it measures the
 // form's accuracy against long double on a CPU; the product runs the header on
@@ -23,8 +23,8 @@ struct HostSeg {
 
 // All-pairs forces in calcSegSegForceSer!'s order (DislocationForces.jl:778-829):
 // F (3 x 2 x numSeg, zeroed here) += the four node forces of every pair i < j,
-// external segments skipped on both sides.  fmath != 0: the table-driven
-// log/atan (the GPU form); 0: the C library's.
+// external segments skipped on both sides.  fmath 2: the integer-pipe log/atan,
+// 1: the FP64 table-driven ones, 0: the C library's.
 extern "C" void fast_segseg_ser(int fmath, const double* k5, const double* coord, const double* bVec,
                                 const int64_t* segIdx, int64_t ld, const uint8_t* extSeg, int64_t numSeg,
                                 double* F) {
@@ -64,12 +64,15 @@ extern "C" void fast_segseg_ser(int fmath, const double* k5, const double* coord
       const double c = ddd::fx::dot(a.t, b.t);
       X3 F1, F2, F3, F4;
       if (1.0 - c * c > 1.4901161193847656e-08) {
-        if (fmath)
-          ddd::fx::general_pair<true, true, true>(K, a.b, a.n1, a.n2, a.t, a.tN, b.b, b.n1, b.n2, b.t, b.tN, c, F1,
-                                                  F2, F3, F4);
+        if (fmath == 2)
+          ddd::fx::general_pair<true, true, ddd::fx::kMathInt>(K, a.b, a.n1, a.n2, a.t, a.tN, b.b, b.n1, b.n2, b.t,
+                                                               b.tN, c, F1, F2, F3, F4);
+        else if (fmath == 1)
+          ddd::fx::general_pair<true, true, ddd::fx::kMathTable>(K, a.b, a.n1, a.n2, a.t, a.tN, b.b, b.n1, b.n2, b.t,
+                                                                 b.tN, c, F1, F2, F3, F4);
         else
-          ddd::fx::general_pair<true, true, false>(K, a.b, a.n1, a.n2, a.t, a.tN, b.b, b.n1, b.n2, b.t, b.tN, c, F1,
-                                                   F2, F3, F4);
+          ddd::fx::general_pair<true, true, ddd::fx::kMathCuda>(K, a.b, a.n1, a.n2, a.t, a.tN, b.b, b.n1, b.n2, b.t,
+                                                                b.tN, c, F1, F2, F3, F4);
       } else {
         ddd_oracle::V3<double> out[4];
         ddd_oracle::seg_seg_force<double>(KO, {a.b.x, a.b.y, a.b.z}, {a.n1.x, a.n1.y, a.n1.z}, {a.n2.x, a.n2.y, a.n2.z},
@@ -87,10 +90,11 @@ extern "C" void fast_segseg_ser(int fmath, const double* k5, const double* coord
   }
 }
 
-// The table-driven logarithm and arctangent at n points.
-extern "C" void fast_log_atan(const double* x, int64_t n, double* lg, double* at) {
+// The logarithm and arctangent at n points: kind 2 the integer-pipe ones
+// (intmath_f64.cuh), 1 the FP64 table-driven ones (fastmath_f64.cuh).
+extern "C" void fast_log_atan(int kind, const double* x, int64_t n, double* lg, double* at) {
   for (int64_t i = 0; i < n; ++i) {
-    lg[i] = ddd::fm::log(x[i]);
-    at[i] = ddd::fm::atan(x[i]);
+    lg[i] = kind == 2 ? ddd::im::log(x[i]) : ddd::fm::log(x[i]);
+    at[i] = kind == 2 ? ddd::im::atan(x[i]) : ddd::fm::atan(x[i]);
   }
 }
