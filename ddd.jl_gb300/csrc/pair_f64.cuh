@@ -8,13 +8,19 @@
 // Differences from a literal transcription, all below 1e-13 relative:
 //   * t = (n2 - n1)/|n2 - n1| and 1/|n2 - n1| are computed once per segment
 //     (same operations the reference repeats per pair);
-//   * nvcc contracts a*b + c into FMA;
+//   * nvcc contracts a*b + c into FMA in the FMA build (the strict build keeps
+//     every multiply and add separate);
+//   * log and atan are the integer-pipe functions of intmath_f64.cuh: within
+//     0.51 ulp (correctly rounded but for ~1 case in 10^3, like the C library
+//     the reference calls), and they take no FP64 pipe time;
 //   * the core-correction calls of the near-parallel branch evaluate the general
 //     branch directly: their segments make 1 - c^2 = 1.01 sqrt(eps) with the
 //     other segment by construction (DislocationForces.jl:1194), so the
 //     reference's own branch test always takes the general branch there.
 #pragma once
 #include <cstdint>
+
+#include "intmath_f64.cuh"
 
 namespace ddd {
 
@@ -71,9 +77,9 @@ __device__ __forceinline__ void seg_seg_integ_acc(double aSq_dSq, double den, do
   double Ra_Rd_t1 = Ra + y + x * c;
   double Ra_Rd_t2 = Ra + x + y * c;
 
-  double log_Ra_Rd_t1 = log(Ra_Rd_t1);
+  double log_Ra_Rd_t1 = im::log(Ra_Rd_t1);
   double xlog_Ra_Rd_t1 = x * log_Ra_Rd_t1;
-  double log_Ra_Rd_t2 = log(Ra_Rd_t2);
+  double log_Ra_Rd_t2 = im::log(Ra_Rd_t2);
   double ylog_Ra_Rd_t2 = y * log_Ra_Rd_t2;
 
   double RaSq_R_t1_I = RaInv / Ra_Rd_t1;
@@ -84,7 +90,7 @@ __device__ __forceinline__ void seg_seg_integ_acc(double aSq_dSq, double den, do
   double yRaSq_R_t2_I = y * RaSq_R_t2_I;
   double ySqRaSq_R_t2_I = y * yRaSq_R_t2_I;
 
-  double integ1 = -2.0 * den * atan((1.0 + c) * (Ra + x + y) * den);
+  double integ1 = -2.0 * den * im::atan((1.0 + c) * (Ra + x + y) * den);
 
   double c_1 = aSq_dSq * integ1;
   double c_5_6 = (c * Ra - c_1) * omcSqI;
@@ -337,7 +343,7 @@ __device__ __forceinline__ void par_seg_seg_integ_acc(double aSq_dSq, double aSq
   double xmy = x - y;
   double Ra = sqrt(aSq_dSq + xpy * xpy);
   double RaInv = 1.0 / Ra;
-  double Log_Ra_ypz = log(Ra + xpy);
+  double Log_Ra_ypz = im::log(Ra + xpy);
   double tmp = xmy * Ra * aSq_dSqI;
   double i10 = -aSq_dSqI * xpy * RaInv;
   integ[0] += sgn((Ra * aSq_dSqI), sm);
