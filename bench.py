@@ -225,10 +225,12 @@ def cpu_sigma_sample(pkg, synth, oracle, p, b, k5, cube, target_s):
             "sample": "%d segments x %d points of the 32^3 grid, %.1f s" % (net.numSeg, m, dt)}
 
 
-# DRAM bytes per tile pair of the strict tile kernel and of the network pass,
-# from one ncu capture each at 32,768 segments (32,896 tile pairs; the partial
-# slots exceed L2 there, so traffic grows with the tile-pair count).
+# DRAM bytes per tile pair of the strict and fast FP64 tile kernels and of the
+# network pass, from one ncu capture each at 32,768 segments (32,896 tile
+# pairs; the partial slots exceed L2 there, so traffic grows with the tile-pair
+# count).
 TILE_DRAM_BYTES_PER_TILE_PAIR = (31162112 + 376273664) // 32896
+TILE_FX_DRAM_BYTES_PER_TILE_PAIR = (27079168 + 366944512) // 32896
 MLP_DRAM_BYTES_PER_TILE_PAIR = (12404992 + 346662144) // 32896
 
 # Tensor-core FLOPs of the surrogate network per pair slot (one row of the
@@ -1068,7 +1070,8 @@ def main():
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
                      "frac": achieved / fp64_peak,
-                     "traffic": TILE_DRAM_BYTES_PER_TILE_PAIR * (n // 128) * (n // 128 + 1) // 2,
+                     "traffic": (TILE_DRAM_BYTES_PER_TILE_PAIR if args.mode == "fp64" else
+                                 TILE_FX_DRAM_BYTES_PER_TILE_PAIR) * (n // 128) * (n // 128 + 1) // 2,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at 32,768 "
                                        "segments, scaled by tile pairs",
                      "kernel": "segseg_tile_f64<0>" if args.mode == "fp64" else "segseg_tile_fx<0>",

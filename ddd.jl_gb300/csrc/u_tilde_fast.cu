@@ -1,6 +1,7 @@
 // calc_uTilde's field kernel, reformulated FP64 (compiled with --fmad=false):
 // the same triangles, unit vectors and sums as u_tilde.cu's reference-order
 // kernel, with
+//   * log and atan on the integer pipes (intmath_f64.cuh);
 //   * the solid angle's magnitude from one atan2 (Van Oosterom & Strackee
 //     1983: tan(Ω/2) = R_A·(R_B×R_C) / (1 + R_A·R_B + R_B·R_C + R_C·R_A) for
 //     unit R) instead of l'Huilier's three acos, four tan and one atan, its
@@ -23,11 +24,21 @@
 #include <cuda_runtime.h>
 
 #include "ddd_internal.h"
+#include "intmath_f64.cuh"
 
 namespace ddd {
 namespace {
 
 constexpr int PT = 128;
+
+// atan2(y, x) for y > 0 on the integer pipes: the quotient rounded once, then
+// im::atan (within ~1 ulp; CUDA documents 2 ulp for its atan2).
+__device__ __forceinline__ double atan2_pos(double y, double x) {
+  const double pi = 3.141592653589793;
+  if (x > 0.0) return im::atan(y / x);
+  if (x < 0.0) return pi - im::atan(y / -x);
+  return 0.5 * pi;
+}
 constexpr int TCH = 32;
 constexpr int TROW = kUTriRows;
 
@@ -111,28 +122,28 @@ __global__ void __launch_bounds__(PT) u_field_fast(const double* __restrict__ tr
       const double sgn = -jl_sign(dot(RA, cross(CA, AB)));
       double om;
       if (fabs(num) > 1e-10) {
-        om = sgn * (2.0 * atan2(fabs(num), 1.0 + ab + bc + ca));
+        om = sgn * (2.0 * atan2_pos(fabs(num), 1.0 + ab + bc + ca));
       } else {  // (nearly) in the triangle's plane: the reference's expression
         const double ta = acos(clamp11(ab)), tb = acos(clamp11(bc)), tc = acos(clamp11(ca));
         const double th = (ta + tb + tc) / 2.0;
         const double f =
             jl_max0(tan(th / 2.0) * tan((th - ta) / 2.0) * tan((th - tb) / 2.0) * tan((th - tc) / 2.0));
-        om = sgn * (4.0 * atan(sqrt(f)));
+        om = sgn * (4.0 * im::atan(sqrt(f)));
       }
       const double fourPi = 4.0 * 3.141592653589793;
       acc = acc + V{-s[9] * om / fourPi, -s[10] * om / fourPi, -s[11] * om / fourPi};
       if (s[21] == 0.0) continue;
       const V b = {s[9], s[10], s[11]};
-      const double lAB = log((RBn * (1.0 + dot(RB, AB))) / (RAn * (1.0 + dot(RA, AB))));
+      const double lAB = im::log((RBn * (1.0 + dot(RB, AB))) / (RAn * (1.0 + dot(RA, AB))));
       V fs = V{s[23], s[24], s[25]} * lAB;
       V gs = (RA + RB) * (dot(b, cross(RA, RB)) / (1.0 + clamp11(ab)));
       if (!(link & 4)) {
-        const double lBC = log((RCn * (1.0 + dot(RC, BC))) / (RBn * (1.0 + dot(RB, BC))));
+        const double lBC = im::log((RCn * (1.0 + dot(RC, BC))) / (RBn * (1.0 + dot(RB, BC))));
         fs = fs + V{s[26], s[27], s[28]} * lBC;
         gs = gs + (RB + RC) * (dot(b, cross(RB, RC)) / (1.0 + clamp11(bc)));
       }
       if (!(link & 8)) {
-        const double lCA = log((RAn * (1.0 + dot(RA, CA))) / (RCn * (1.0 + dot(RC, CA))));
+        const double lCA = im::log((RAn * (1.0 + dot(RA, CA))) / (RCn * (1.0 + dot(RC, CA))));
         fs = fs + V{s[29], s[30], s[31]} * lCA;
         gs = gs + (RC + RA) * (dot(b, cross(RC, RA)) / (1.0 + clamp11(ca)));
       }
