@@ -738,11 +738,13 @@ def main():
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--no-precision131k", action="store_true")
     ap.add_argument("--profile-surrogate", type=int, default=0, metavar="N",
-                    help="only run N surrogate force calls on the workload (f32c exact passes, no audit) and exit: "
+                    help="only run N surrogate force calls on the workload (no audit) and exit: "
                          "the command the ncu captures of the surrogate kernels use")
     ap.add_argument("--surrogate", default=SURROGATE_CKPT, help="surrogate checkpoint (trained here when missing)")
     ap.add_argument("--far", default="network", choices=["network", "quad2", "quad3"],
                     help="far pass of --profile-surrogate: the network or FP32 Gauss-Legendre quadrature")
+    ap.add_argument("--exact-mode", default="f32c", choices=["f32c", "fp64_fast", "fp64"],
+                    help="arithmetic of the near pass of --profile-surrogate")
     args = ap.parse_args()
 
     import __graft_entry__ as graft
@@ -775,7 +777,7 @@ def main():
         sur = pkg.Surrogate(ctx, seed=0).load(args.surrogate)
         segs = torch.from_numpy(synth.packed_soa(p, b)).cuda()
         for _ in range(args.profile_surrogate):
-            _, rep = sur.force(k, segs, exact_mode="f32c", audit_fraction=0.0, far=args.far)
+            _, rep = sur.force(k, segs, exact_mode=args.exact_mode, audit_fraction=0.0, far=args.far)
         torch.cuda.synchronize()
         print(json.dumps({"profile_surrogate": args.profile_surrogate, "segments": n, "report": rep}), flush=True)
         return

@@ -142,20 +142,7 @@ struct Src {
   V3f bo;
 };
 
-QF_HD void vset(double* d, const double* a) { d[0] = a[0], d[1] = a[1], d[2] = a[2]; }
 QF_HD double dotd(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
-
-// One segment from p to p + v (FP64, relative to the original source
-// midpoint) with Burgers b, as a Src; false when it has zero length.
-QF_HD bool make_src(const double* p, const double* v, const double* b, Src& s) {
-  const double L = sqrt(dotd(v, v));
-  if (!(L > 0.0)) return false;
-  s.off = {(float)(p[0] + 0.5 * v[0]), (float)(p[1] + 0.5 * v[1]), (float)(p[2] + 0.5 * v[2])};
-  s.to = {(float)(v[0] / L), (float)(v[1] / L), (float)(v[2] / L)};
-  s.Lo = (float)L;
-  s.bo = {(float)b[0], (float)b[1], (float)b[2]};
-  return true;
-}
 
 // One side of calcParSegSegForce (DislocationForces.jl:1204-1317, :1319-1433):
 // the source segment nb1 -> nb1 + lb (Burgers bb; FP64, nb1 relative to the
@@ -169,6 +156,14 @@ QF_HD bool make_src(const double* p, const double* v, const double* b, Src& s) {
 // nbm2 -> nb1 + lb are sources too.  Writes up to three sources; returns how
 // many.  The force on the field segment is the sum of their quadratures: the
 // reference evaluates the same geometry analytically.
+//
+// Only the rejection needs FP64 (it is |lb| sin(angle), far below |lb|): lb.ta,
+// diff and diff.diff are formed as the reference forms them.  The sources are
+// FP32 quantities, and they simplify exactly: the main source runs along ta
+// with signed length lb.ta - 2 hCot |diff| and its midpoint is the source's own
+// (nb1 + lb/2), and both connectors are the vector diff/2 + hCot |diff| ta.  The
+// connector test is decided in FP32 unless it falls within 1e-5 of its
+// threshold, where it is evaluated in FP64 exactly as written above.
 template <int SIDE>
 QF_HD int par_sources(const double* ta, const double* nb1, const double* nb1abs, const double* lb, const double* bb,
                       Src* out) {
@@ -176,32 +171,50 @@ QF_HD int par_sources(const double* ta, const double* nb1, const double* nb1abs,
   const double proj[3] = {tmp * ta[0], tmp * ta[1], tmp * ta[2]};
   const double diff[3] = {lb[0] - proj[0], lb[1] - proj[1], lb[2] - proj[2]};
   const double dd = dotd(diff, diff);
-  const double magDiff = sqrt(dd);
-  const double tv1[3] = {0.5 * diff[0], 0.5 * diff[1], 0.5 * diff[2]};
-  const double tv2[3] = {kParHCot * magDiff * ta[0], kParHCot * magDiff * ta[1], kParHCot * magDiff * ta[2]};
-  double m1[3], m2[3];  // nbm1, nbm2 relative to the source midpoint
-  for (int k = 0; k < 3; ++k) {
-    m1[k] = nb1[k] + tv1[k] + tv2[k];
-    m2[k] = nb1[k] + proj[k] + tv1[k] - tv2[k];
-  }
+  const V3f t = {(float)ta[0], (float)ta[1], (float)ta[2]};
+  const V3f d = {(float)diff[0], (float)diff[1], (float)diff[2]};
+  const V3f n1 = {(float)nb1[0], (float)nb1[1], (float)nb1[2]};
+  const V3f lv = {(float)lb[0], (float)lb[1], (float)lb[2]};
+  const V3f b = {(float)bb[0], (float)bb[1], (float)bb[2]};
+  const float h = (float)kParHCot * std::sqrt((float)dd);  // hCot |diff|
   int n = 0;
-  const double v[3] = {m2[0] - m1[0], m2[1] - m1[1], m2[2] - m1[2]};
-  if (make_src(m1, v, bb, out[n])) ++n;
-  double a1[3], a2[3];  // absolute nbm1, nbm2
-  for (int k = 0; k < 3; ++k) {
-    a1[k] = nb1abs[k] + tv1[k] + tv2[k];
-    a2[k] = nb1abs[k] + proj[k] + tv1[k] - tv2[k];
+  const float Lm = (float)tmp - 2.0f * h;  // signed length of nbm1 -> nbm2 along ta
+  if (Lm != 0.0f) {
+    out[n].off = n1 + 0.5f * lv;
+    out[n].to = Lm > 0.0f ? t : V3f{-t.x, -t.y, -t.z};
+    out[n].Lo = std::fabs(Lm);
+    out[n].bo = b;
+    ++n;
   }
-  const double magDiffSq = SIDE == 1 ? dd : magDiff * magDiff;
-  if (magDiffSq > kParEps * (dotd(a1, a1) + dotd(a2, a2))) {
-    const double c1[3] = {tv1[0] + tv2[0], tv1[1] + tv2[1], tv1[2] + tv2[2]};  // nb1 -> nbm1
-    double e2[3], c2[3];                                                          // nbm2 -> nb1 + lb
+  // Connector test: |nbm1|^2 + |nbm2|^2 in FP32, FP64 next to the threshold.
+  const V3f c = 0.5f * d + h * t;  // nb1 -> nbm1, and nbm2 -> nb1 + lb
+  const V3f a0 = {(float)nb1abs[0], (float)nb1abs[1], (float)nb1abs[2]};
+  const V3f a1 = a0 + c, a2 = a0 + (float)tmp * t + 0.5f * d - h * t;
+  const float thr = (float)kParEps * (dot(a1, a1) + dot(a2, a2));
+  const float ddf = (float)dd;
+  bool conn;
+  if (ddf > thr * 1.00001f) {
+    conn = true;
+  } else if (ddf < thr * 0.99999f) {
+    conn = false;
+  } else {
+    const double magDiff = sqrt(dd);
+    double e1[3], e2[3];
     for (int k = 0; k < 3; ++k) {
-      e2[k] = nb1[k] + lb[k];
-      c2[k] = e2[k] - m2[k];
+      const double tv1 = 0.5 * diff[k], tv2 = kParHCot * magDiff * ta[k];
+      e1[k] = nb1abs[k] + tv1 + tv2;
+      e2[k] = nb1abs[k] + proj[k] + tv1 - tv2;
     }
-    if (make_src(nb1, c1, bb, out[n])) ++n;
-    if (make_src(m2, c2, bb, out[n])) ++n;
+    const double magDiffSq = SIDE == 1 ? dd : magDiff * magDiff;
+    conn = magDiffSq > kParEps * (dotd(e1, e1) + dotd(e2, e2));
+  }
+  const float Lc = std::sqrt(dot(c, c));
+  if (conn && Lc > 0.0f) {
+    const V3f tc = (1.0f / Lc) * c;
+    out[n] = {n1 + 0.5f * c, tc, Lc, b};
+    ++n;
+    out[n] = {n1 + (float)tmp * t + 0.5f * d - h * t + 0.5f * c, tc, Lc, b};
+    ++n;
   }
   return n;
 }
