@@ -16,9 +16,11 @@
 // segment — are written to `p` as [side][component][T] doubles.  No
 // floating-point atomics: the result is deterministic.
 //
-// In MODE 2 every selected pair goes through the compacted dense pass:
-// the branch is the reference's FP64 decision, the general branch uses the
-// policy's arithmetic (P::dense_general), the near-parallel branch FP64.
+// In MODE 2 every selected pair goes through the compacted dense pass.  The
+// sweep takes the reference's FP64 branch decision for each selected pair and
+// compacts the general-branch pairs (policy arithmetic, P::dense_general) and
+// the near-parallel ones (FP64) into two runs of the list, so that no warp runs
+// both branches.
 //
 // Data: `soa` is the FP64 structure of arrays (13 rows of npad doubles: n1xyz,
 // n2xyz, bxyz, txyz, 1/|l|), `skip` one byte per segment (external or padding).
@@ -88,12 +90,14 @@ __device__ __forceinline__ void tile_body(const TileArgs& A, const typename P::C
   typename P::Seg si;
   if (!CLS) si = P::load_global(A, gi);
   float mi[3] = {0, 0, 0}, Li = 0.0f;
+  D3 ti = {0, 0, 0};  // MODE 2: the row's FP64 direction for the branch decision
   if (CLS) {
     const int64_t n = A.npad;
     mi[0] = A.ms[(sur::kMsM + 0) * n + gi];
     mi[1] = A.ms[(sur::kMsM + 1) * n + gi];
     mi[2] = A.ms[(sur::kMsM + 2) * n + gi];
     Li = A.ms[sur::kMsL * n + gi];
+    ti = {A.soa[9 * n + gi], A.soa[10 * n + gi], A.soa[11 * n + gi]};
   }
 
   if (!CLS) {
@@ -104,9 +108,9 @@ __device__ __forceinline__ void tile_body(const TileArgs& A, const typename P::C
   __syncthreads();
 
   typename P::Acc fi1 = P::acc_zero(), fi2 = P::acc_zero();
-  uint32_t pmask[NW];
+  uint32_t pmask[NW], gmask[NW];  // near-parallel pairs; MODE 2: general-branch pairs
 #pragma unroll
-  for (int w = 0; w < NW; ++w) pmask[w] = 0;
+  for (int w = 0; w < NW; ++w) pmask[w] = gmask[w] = 0;
   unsigned long long nGeneral = 0, nDenseParallel = 0;
 
   for (int k = 0; k < T; ++k) {
@@ -121,7 +125,14 @@ __device__ __forceinline__ void tile_body(const TileArgs& A, const typename P::C
         const bool far = sur::pair_is_far(mi[0], mi[1], mi[2], Li, A.ms[(sur::kMsM + 0) * n + gj],
                                           A.ms[(sur::kMsM + 1) * n + gj], A.ms[(sur::kMsM + 2) * n + gj],
                                           A.ms[sur::kMsL * n + gj], A.farK2, dx, dy, dz);
-        if (!far) pmask[jl >> 5] |= 1u << (jl & 31);
+        if (!far) {
+          const D3 tj = {A.soa[9 * n + gj], A.soa[10 * n + gj], A.soa[11 * n + gj]};
+          const double c = dot(ti, tj);
+          if (1.0 - c * c > kSqrtEps)
+            gmask[jl >> 5] |= 1u << (jl & 31);
+          else
+            pmask[jl >> 5] |= 1u << (jl & 31);
+        }
       }
     } else if (act) {
       typename P::Seg sj = P::template load_smem<T>(sm.pol, jl);
@@ -144,65 +155,89 @@ __device__ __forceinline__ void tile_body(const TileArgs& A, const typename P::C
     __syncwarp();
   }
 
-  // ---- Near-parallel pairs: compact (fixed order), evaluate densely in FP64. ----
-  int myCnt = 0;
+  // ---- Compact the listed pairs (fixed order: by row, then by step) and
+  // evaluate them densely: MODE 2 lists its general-branch pairs first, then its
+  // near-parallel ones; the other modes list only near-parallel pairs. ----
+  int myCntG = 0, myCnt = 0;
 #pragma unroll
-  for (int w = 0; w < NW; ++w) myCnt += __popc(pmask[w]);
-  sm.cnt[t] = myCnt;
-  __syncthreads();
-  if (warp == 0) {
-    constexpr int PER = T / 32;
-    int v[PER];
-    int s = 0;
-#pragma unroll
-    for (int q = 0; q < PER; ++q) {
-      v[q] = sm.cnt[PER * t + q];
-      s += v[q];
-    }
-    int incl = s;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      int n = __shfl_up_sync(0xffffffffu, incl, o);
-      if ((t & 31) >= o) incl += n;
-    }
-    int excl = incl - s;
-#pragma unroll
-    for (int q = 0; q < PER; ++q) {
-      sm.cnt[PER * t + q] = excl;
-      excl += v[q];
-    }
+  for (int w = 0; w < NW; ++w) {
+    myCntG += __popc(gmask[w]);
+    myCnt += __popc(pmask[w]);
   }
+  int myOffG = 0, myOff = 0;
+#pragma unroll
+  for (int run = CLS ? 0 : 1; run < 2; ++run) {
+    sm.cnt[t] = run == 0 ? myCntG : myCnt;
+    __syncthreads();
+    if (warp == 0) {
+      constexpr int PER = T / 32;
+      int v[PER];
+      int s = 0;
+#pragma unroll
+      for (int q = 0; q < PER; ++q) {
+        v[q] = sm.cnt[PER * t + q];
+        s += v[q];
+      }
+      int incl = s;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        int n = __shfl_up_sync(0xffffffffu, incl, o);
+        if ((t & 31) >= o) incl += n;
+      }
+      int excl = incl - s;
+#pragma unroll
+      for (int q = 0; q < PER; ++q) {
+        sm.cnt[PER * t + q] = excl;
+        excl += v[q];
+      }
+    }
+    __syncthreads();
+    if (run == 0) {
+      myOffG = sm.cnt[t];
+      if (t == T - 1) sm.total = myOffG + myCntG;
+    } else {
+      myOff = sm.cnt[t];
+    }
+    __syncthreads();
+  }
+  const int nGen = CLS ? sm.total : 0;  // the general run, then the near-parallel run
+  myOff += nGen;
   __syncthreads();
-  const int myOff = sm.cnt[t];
   if (t == T - 1) sm.total = myOff + myCnt;
   {
-    int o = myOff;
+    int og = myOffG, o = myOff;
     for (int k = 0; k < T; ++k) {
       const int jl = (t + k) & (T - 1);
-      if (pmask[jl >> 5] & (1u << (jl & 31))) sm.plist[o++] = (uint16_t)((t << 8) | jl);
+      const uint32_t bit = 1u << (jl & 31);
+      if (CLS && (gmask[jl >> 5] & bit)) sm.plist[og++] = (uint16_t)((t << 8) | jl);
+      if (pmask[jl >> 5] & bit) sm.plist[o++] = (uint16_t)((t << 8) | jl);
     }
   }
   __syncthreads();
   const int nPar = sm.total;
   D3 fp1 = {0, 0, 0}, fp2 = {0, 0, 0}, fjp3 = {0, 0, 0}, fjp4 = {0, 0, 0};
   unsigned long long nCore = 0;
-  for (int base = 0; base < nPar; base += CH) {
+  // Chunks of CH never straddle the two runs, so a warp runs one branch.
+  for (int base = 0; base < nPar;) {
+    const bool genRun = base < nGen;
+    const int end = genRun ? nGen : nPar;
     const int e = base + t;
-    if (e < nPar) {
+    if (e < end) {
       const int il = sm.plist[e] >> 8, jl = sm.plist[e] & 0xff;
-      SegF64 a = tb_load_seg64(A.soa, A.npad, MODE != 1 ? iBase + il : rows[iBase + il]);
-      SegF64 b = tb_load_seg64(A.soa, A.npad, j0 + jl);
-      double c = dot(a.t, b.t);
       D3 F1, F2, F3 = {0, 0, 0}, F4 = {0, 0, 0};
-      if (CLS && 1.0 - c * c > kSqrtEps) {
-        // The reference's branch decision in FP64; the policy's general-branch arithmetic.
+      if (genRun) {
         P::dense_general(KP, A, iBase + il, j0 + jl, F1, F2, F3, F4);
         ++nGeneral;
-      } else if (MODE != 1) {
-        ++nDenseParallel;
-        nCore += parallel_pair<true>(A.K, a.b, a.n1, a.n2, a.t, a.tN, b.b, b.n1, b.n2, b.t, b.tN, c, F1, F2, F3, F4);
       } else {
-        nCore += parallel_pair<false>(A.K, a.b, a.n1, a.n2, a.t, a.tN, b.b, b.n1, b.n2, b.t, b.tN, c, F1, F2, F3, F4);
+        SegF64 a = tb_load_seg64(A.soa, A.npad, MODE != 1 ? iBase + il : rows[iBase + il]);
+        SegF64 b = tb_load_seg64(A.soa, A.npad, j0 + jl);
+        double c = dot(a.t, b.t);
+        if (MODE != 1) {
+          ++nDenseParallel;
+          nCore += parallel_pair<true>(A.K, a.b, a.n1, a.n2, a.t, a.tN, b.b, b.n1, b.n2, b.t, b.tN, c, F1, F2, F3, F4);
+        } else {
+          nCore += parallel_pair<false>(A.K, a.b, a.n1, a.n2, a.t, a.tN, b.b, b.n1, b.n2, b.t, b.tN, c, F1, F2, F3, F4);
+        }
       }
       sm.cf[t][0] = F1.x; sm.cf[t][1] = F1.y; sm.cf[t][2] = F1.z;
       sm.cf[t][3] = F2.x; sm.cf[t][4] = F2.y; sm.cf[t][5] = F2.z;
@@ -210,12 +245,23 @@ __device__ __forceinline__ void tile_body(const TileArgs& A, const typename P::C
       sm.cf[t][9] = F4.x; sm.cf[t][10] = F4.y; sm.cf[t][11] = F4.z;
     }
     __syncthreads();
-    const int lim = min(CH, nPar - base);
-    const int lo = max(myOff, base), hi = min(myOff + myCnt, base + lim);
-    for (int e2 = lo; e2 < hi; ++e2) {
-      const double* f = sm.cf[e2 - base];
-      fp1 = fp1 + D3{f[0], f[1], f[2]};
-      fp2 = fp2 + D3{f[3], f[4], f[5]};
+    const int lim = min(CH, end - base);
+    // This thread's own entries of the chunk: its general run, then its near-parallel run.
+    {
+      const int lo = max(myOffG, base), hi = min(myOffG + myCntG, base + lim);
+      for (int e2 = lo; e2 < hi; ++e2) {
+        const double* f = sm.cf[e2 - base];
+        fp1 = fp1 + D3{f[0], f[1], f[2]};
+        fp2 = fp2 + D3{f[3], f[4], f[5]};
+      }
+    }
+    {
+      const int lo = max(myOff, base), hi = min(myOff + myCnt, base + lim);
+      for (int e2 = lo; e2 < hi; ++e2) {
+        const double* f = sm.cf[e2 - base];
+        fp1 = fp1 + D3{f[0], f[1], f[2]};
+        fp2 = fp2 + D3{f[3], f[4], f[5]};
+      }
     }
     if (MODE != 1) {
       for (int q = 0; q < lim; ++q) {
@@ -227,6 +273,7 @@ __device__ __forceinline__ void tile_body(const TileArgs& A, const typename P::C
       }
     }
     __syncthreads();
+    base += lim;
   }
 
   // ---- Partials: [side][component][T]; side 0 = row segments, 1 = column segments. ----
