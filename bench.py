@@ -389,10 +389,10 @@ def run_sigma_32k(pkg, synth, oracle, ctx, k, stream, sptr, flush, fp64_peak, wi
     """σ̃ of the 32,768-segment GPU workload (same generator, seed 0) at every
     point of the 128^3-point grid over its cube (2,097,152 points: the workload
     names "2^20 points on a 128^3 grid", and the whole grid is evaluated), FP64
-    strict: one warm-up
-    on 4,096 points, then one timed full evaluation (CUDA events, L2 flushed
-    before it); 256 sampled points checked against the oracle (the reference's
-    segment order per point)."""
+    strict and the fast FP64 form: each one warm-up on 4,096 points, then one
+    timed full evaluation (CUDA events, L2 flushed before it); 256 sampled
+    points checked against the oracle (the reference's segment order per
+    point) for both."""
     import torch
     p, b, cfg = synth.make("gpu32k", seed=0)
     n = p.shape[0] * 8
@@ -401,22 +401,35 @@ def run_sigma_32k(pkg, synth, oracle, ctx, k, stream, sptr, flush, fp64_peak, wi
     soa = torch.from_numpy(synth.packed_soa(p, b)).cuda()
     x0 = torch.from_numpy(np.ascontiguousarray(pts.T)).cuda()
     sig = torch.zeros(6 * M, dtype=torch.float64, device="cuda")
-    with torch.cuda.stream(stream):
-        ctx.sigma_tilde_device(k, x0.data_ptr(), 4096, soa.data_ptr(), n, n, sig.data_ptr(), stream=sptr)
-        torch.cuda.synchronize()
-        flush.zero_()
-        a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a_.record(stream)
-        ctx.sigma_tilde_device(k, x0.data_ptr(), M, soa.data_ptr(), n, n, sig.data_ptr(), stream=sptr)
-        b_.record(stream)
-        torch.cuda.synchronize()
-    ms = a_.elapsed_time(b_)
+    sig_fx = torch.zeros(6 * M, dtype=torch.float64, device="cuda")
+
+    def timed(out, mode):
+        ctx.mode = mode
+        try:
+            with torch.cuda.stream(stream):
+                ctx.sigma_tilde_device(k, x0.data_ptr(), 4096, soa.data_ptr(), n, n, out.data_ptr(), stream=sptr)
+                torch.cuda.synchronize()
+                flush.zero_()
+                a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a_.record(stream)
+                ctx.sigma_tilde_device(k, x0.data_ptr(), M, soa.data_ptr(), n, n, out.data_ptr(), stream=sptr)
+                b_.record(stream)
+                torch.cuda.synchronize()
+        finally:
+            ctx.mode = "fp64"
+        return a_.elapsed_time(b_)
+
+    ms = timed(sig, "fp64")
+    ms_fx = timed(sig_fx, "fp64_fast")
     evals = n * M
     out = {"config": "gpu32k: %d segments x %d points (%d^3 grid over the %g^3 b cube), FP64 strict"
                      % (n, M, cfg["grid"], cfg["cube"]),
            "value": evals / (ms * 1e-3), "unit": "seg-point evaluations/s", "points_per_s": M / (ms * 1e-3),
            "ms": ms, "frac_fp64_peak": evals * OPS_SIGMA_EVAL / (ms * 1e-3) / fp64_peak,
-           "kernel": "sigma_tilde_f64"}
+           "kernel": "sigma_tilde_f64",
+           "fast": {"value": evals / (ms_fx * 1e-3), "ms": ms_fx, "speedup_vs_fp64": ms / ms_fx,
+                    "frac_fp64_peak": evals * OPS_SIGMA_EVAL / (ms_fx * 1e-3) / fp64_peak,
+                    "kernel": "sigma_tilde_fx"}}
     if with_cpu:
         coord, bvec, seg = synth.network_arrays(p, b)
         net = pkg.DislocationNetwork(coord, bvec, seg)
@@ -430,6 +443,10 @@ def run_sigma_32k(pkg, synth, oracle, ctx, k, stream, sptr, flush, fp64_peak, wi
         out["parity_sample"] = {"points": len(pick), "max_rel_point": float(np.max(d / r)),
                                 "bound": "|dσ| <= 1e-10 |σ| + 1e-12 max|σ| per point",
                                 "bound_excess": float(np.max(d - (1e-10 * r + 1e-12 * smax)))}
+        Sf = sig_fx.view(M, 6)[torch.from_numpy(pick).cuda()].cpu().numpy().T
+        df = np.linalg.norm(Sf - ref, axis=0)
+        out["fast"]["parity_sample"] = {"points": len(pick), "max_rel_point": float(np.max(df / r)),
+                                        "bound_excess": float(np.max(df - (1e-10 * r + 1e-12 * smax)))}
     return out
 
 
@@ -661,8 +678,11 @@ def summary(line, variants, surrogate, sigma32k, batched):
                        "rel_rms": _r(qv["error_vs_fp64"]["rel_rms"], 3),
                        "max_node_over_max": _r(qv["error_vs_fp64"]["max_node_over_max_force"], 3)}
     if sigma32k:
+        fx = sigma32k.get("fast", {})
         out["sigma_32k_grid128"] = {"evals_per_s": _r(sigma32k["value"]), "frac_probe": _r(sigma32k["frac_fp64_peak"], 3),
-                                 "bound_excess": _r(sigma32k.get("parity_sample", {}).get("bound_excess"), 3)}
+                                 "bound_excess": _r(sigma32k.get("parity_sample", {}).get("bound_excess"), 3),
+                                 "fast_evals_per_s": _r(fx.get("value")), "fast_frac_probe": _r(fx.get("frac_fp64_peak"), 3),
+                                 "fast_bound_excess": _r(fx.get("parity_sample", {}).get("bound_excess"), 3)}
     if batched:
         out["batched"] = {m: {"pairs_per_s": _r(batched[m]["value"]),
                               "rel_rms": _r(batched[m]["error_vs_fp64"]["rel_rms"], 3)}
@@ -968,6 +988,30 @@ def main():
                           "error_vs_fp64": {"rel_rms": (torch.linalg.norm(sig - sig_ref) /
                                                         torch.linalg.norm(sig_ref)).item(),
                                             "max_point_over_max": (dp.max() / rp.max()).item()}}
+        # The fast FP64 form (sigma_fx.cuh): throughput, and its distance from
+        # the strict result against the strict form's per-point bound.
+        ctx.mode = "fp64_fast"
+        with torch.cuda.stream(stream):
+            ctx.sigma_tilde_device(k, x0.data_ptr(), M, soa.data_ptr(), n, n, sig.data_ptr(), stream=sptr)
+            torch.cuda.synchronize()
+            sms = []
+            for _ in range(2):
+                flush.zero_()
+                a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a_.record(stream)
+                ctx.sigma_tilde_device(k, x0.data_ptr(), M, soa.data_ptr(), n, n, sig.data_ptr(), stream=sptr)
+                b_.record(stream)
+                torch.cuda.synchronize()
+                sms.append(a_.elapsed_time(b_))
+        ctx.mode = "fp64"
+        ms_fx = statistics.mean(sms)
+        dp = torch.linalg.norm((sig - sig_ref).view(M, 6), dim=1)
+        sigma["fast"] = {"value": evals / (ms_fx * 1e-3), "ms": ms_fx, "speedup_vs_fp64": ms_sig / ms_fx,
+                         "frac_fp64_peak": evals * OPS_SIGMA_EVAL / (ms_fx * 1e-3) / fp64_peak,
+                         "kernel": "sigma_tilde_fx",
+                         "error_vs_fp64": {"rel_rms": (torch.linalg.norm(sig - sig_ref) /
+                                                       torch.linalg.norm(sig_ref)).item(),
+                                           "bound_excess": (dp - (1e-10 * rp + 1e-12 * rp.max())).max().item()}}
 
     # Batched form: 256 independent networks (segment counts log-uniform in
     # [64, 8192], own seeds, cubes 2000-20000 b, slip-system subsets) in one

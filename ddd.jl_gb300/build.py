@@ -26,6 +26,7 @@ VARIANTS = {
     "segseg_df.cu": [("", ["--fmad=false"])],
     # explicit fused multiply-adds only (host builds of its header give the same bits)
     "segseg_f64fast.cu": [("", ["--fmad=false"])],
+    "sigma_fx.cu": [("", ["--fmad=false"])],
     "segseg_batch.cu": [("", ["--fmad=false"])],
     "surrogate_data.cu": [("", ["--fmad=false"])],
     "surrogate_force.cu": [("", ["--fmad=false"])],

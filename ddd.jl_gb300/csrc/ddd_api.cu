@@ -155,8 +155,9 @@ cudaError_t run_sigma(ddd_ctx* c, const ddd::KConsts& K, const double* soa, int6
     if (e != cudaSuccess) return e;
     return ddd::launch_sigma_mixed(K, c->soadf.as<float>(), npad, nSeg, x0, M, sigma, st);
   }
-  return use_fma(c) || use_fx(c) ? ddd::fast::launch_sigma_f64(K, soa, npad, nSeg, x0, M, sigma, st)
-                                 : ddd::strict::launch_sigma_f64(K, soa, npad, nSeg, x0, M, sigma, st);
+  if (use_fx(c)) return ddd::launch_sigma_fx(K, soa, npad, nSeg, x0, M, sigma, st);
+  return use_fma(c) ? ddd::fast::launch_sigma_f64(K, soa, npad, nSeg, x0, M, sigma, st)
+                    : ddd::strict::launch_sigma_f64(K, soa, npad, nSeg, x0, M, sigma, st);
 }
 
 

@@ -99,6 +99,9 @@ cudaError_t launch_sigma_mixed(const KConsts& K, const float* soadf, int64_t npa
 // segseg_f64fast.cu: the FP64 tile kernels with the fast general branch
 // (pair_f64fast.cuh: fewer divisions, table-driven log/atan, explicit FMAs);
 // near-parallel branch, segment preparation and reductions strict.
+// The fast FP64 form of σ̃ (sigma_fx.cu).
+cudaError_t launch_sigma_fx(const KConsts& K, const double* soa, int64_t npad, int64_t nSeg, const double* x0,
+                            int64_t M, double* sigma, cudaStream_t st);
 cudaError_t launch_segseg_all_fx(const KConsts& K, const double* soa, const uint8_t* skip, int64_t npad,
                                  double* partial, double* out, int64_t numSeg, unsigned long long* counters,
                                  cudaStream_t st, int64_t capSlots);

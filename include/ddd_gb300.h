@@ -77,7 +77,10 @@ typedef struct ddd_ctx ddd_ctx;
  * coordinates, Ra and Ra + y + x c) are rounded as the reference rounds them,
  * and the near-parallel branch is the strict code.  Its node forces stay
  * within the reference arithmetic's own rounding noise (the same parity bound
- * as DDD_MODE_FP64).  The field stress runs the FMA build in this mode. */
+ * as DDD_MODE_FP64).  The field stress runs its own fast form in this mode:
+ * the six components regrouped on four vectors and seven scalars, 1/Ra by a
+ * reciprocal square root, fused multiply-adds (about half the FP64
+ * instructions; within the strict form's per-point bound). */
 #define DDD_MODE_FP64_FAST 4
 
 /* Constants of the path.  The reference computes them in

@@ -580,6 +580,34 @@ void oracle_opcount_sigma(const double* k5, const double* b, const double* n1, c
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
+// σ̃ with every operation in long double (rounded to double at the end): its
+// distance from the Float64 result is the reference arithmetic's own error
+// (_calc_σTilde!, DislocationFEM.jl:129-299, as oracle_sigma_tilde).
+extern "C" void oracle_sigma_tilde_ld(const double* k5, const double* x0, int64_t M, const double* coord,
+                                      const double* bVec, const int64_t* segIdx, int64_t ld, int64_t numSeg,
+                                      double* sigma, int nthreads) {
+  typedef long double L;
+  Consts<L> K;
+  K.aSq = k5[0];
+  K.mu4pi = k5[1];
+  K.mu8pi = k5[2];
+  K.mu4pinu = k5[3];
+  K.nuMu4pinu = k5[4];
+  K.mu8piaSq = (L)k5[0] * (L)k5[2];
+  K.mu4pinuaSq = (L)k5[0] * (L)k5[3];
+  std::vector<Seg> s = gather(coord, bVec, segIdx, ld, numSeg);
+  auto cv = [](const V3<double>& v) { return V3<L>{(L)v.x, (L)v.y, (L)v.z}; };
+  std::vector<V3<L>> t(numSeg);
+  for (int64_t q = 0; q < numSeg; ++q) t[q] = normalize(cv(s[q].n2) - cv(s[q].n1));
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+  for (int64_t j = 0; j < M; ++j) {
+    L sig[6] = {0, 0, 0, 0, 0, 0};
+    const V3<L> x = {(L)x0[3 * j], (L)x0[3 * j + 1], (L)x0[3 * j + 2]};
+    for (int64_t q = 0; q < numSeg; ++q) sigma_tilde_point<L>(K, cv(s[q].b), cv(s[q].n1), cv(s[q].n2), t[q], x, sig);
+    for (int k = 0; k < 6; ++k) sigma[6 * j + k] = (double)sig[k];
+  }
+}
+
 // Extended-precision all-pairs (long double), to measure the rounding noise of
 // the Float64 algorithm itself: |F_f64 - F_ld| is the reference's own error.
 // rows (0-based, may be NULL = all) selects the segments returned; F is 3×2×nRows.

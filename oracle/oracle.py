@@ -74,6 +74,8 @@ def lib():
                                         ctypes.c_int64, _dp, ctypes.c_int]
         L.oracle_sigma_tilde.argtypes = [_dp, _dp, ctypes.c_int64, _dp, _dp, _ip, ctypes.c_int64, ctypes.c_int64,
                                          _ip, ctypes.c_int64, _dp, ctypes.c_int]
+        L.oracle_sigma_tilde_ld.argtypes = [_dp, _dp, ctypes.c_int64, _dp, _dp, _ip, ctypes.c_int64, ctypes.c_int64,
+                                            _dp, ctypes.c_int]
         L.oracle_segseg_ser_ld.argtypes = [_dp, _dp, _dp, _ip, ctypes.c_int64, _up, ctypes.c_int64, _ip,
                                            ctypes.c_int64, _dp, ctypes.c_int]
         L.oracle_opcount_pair.argtypes = [_dp] * 7 + [_llp, _dp]
@@ -316,6 +318,18 @@ def sigma_tilde(k5, x0, net, idx=None, nthreads=1):
         ip, n = _i(idx), len(idx)
     lib().oracle_sigma_tilde(_d(np.ascontiguousarray(k5, np.float64)), _d(x0), M, _d(coord), _d(bvec), _i(seg), ld,
                              net.numSeg, ip, n, _d(sig), int(nthreads))
+    return sig
+
+
+def sigma_tilde_ld(k5, x0, net, nthreads=1):
+    """σ̃ (6×M) with every operation in long double, rounded to double at the
+    end; its distance from sigma_tilde is the Float64 algorithm's own error."""
+    coord, bvec, seg, ext, ld = _net_arrays(net)
+    x0 = np.require(x0, np.float64, ["F"])
+    M = x0.shape[1]
+    sig = np.zeros((6, M), np.float64, order="F")
+    lib().oracle_sigma_tilde_ld(_d(np.ascontiguousarray(k5, np.float64)), _d(x0), M, _d(coord), _d(bvec), _i(seg), ld,
+                                net.numSeg, _d(sig), int(nthreads))
     return sig
 
 

@@ -98,3 +98,28 @@ extern "C" void fast_log_atan(int kind, const double* x, int64_t n, double* lg, 
     at[i] = kind == 2 ? ddd::im::atan(x[i]) : ddd::fm::atan(x[i]);
   }
 }
+
+// σ̃ at M points (x0 3×M) by the fast form of sigma_fx.cuh: each point's sum
+// over the segments in list order, as calc_σTilde.  sigma is 6×M.
+#include "sigma_fx.cuh"
+extern "C" void fast_sigma(const double* k5, const double* x0, int64_t M, const double* coord, const double* bVec,
+                           const int64_t* segIdx, int64_t ld, int64_t numSeg, double* sigma) {
+  using ddd::sx::X3;
+  const ddd::sx::KS K{k5[0], k5[1], k5[3], k5[4], k5[0] * k5[2]};
+  std::vector<ddd::sx::SegS> s(numSeg);
+  for (int64_t i = 0; i < numSeg; ++i) {
+    const int64_t l = segIdx[i] - 1, a = segIdx[i + ld] - 1, b = segIdx[i + 2 * ld] - 1;
+    const X3 n1 = {coord[3 * a], coord[3 * a + 1], coord[3 * a + 2]};
+    const X3 v = {coord[3 * b] - n1.x, coord[3 * b + 1] - n1.y, coord[3 * b + 2] - n1.z};
+    const double L = std::sqrt(v.x * v.x + v.y * v.y + v.z * v.z), iL = 1.0 / L;
+    const X3 t = {iL * v.x, iL * v.y, iL * v.z};
+    const X3 bb = {bVec[3 * l], bVec[3 * l + 1], bVec[3 * l + 2]};
+    s[i] = {n1, t, bb, {t.y * bb.z - t.z * bb.y, t.z * bb.x - t.x * bb.z, t.x * bb.y - t.y * bb.x}, L};
+  }
+  for (int64_t j = 0; j < M; ++j) {
+    double sig[6] = {0, 0, 0, 0, 0, 0};
+    const X3 x = {x0[3 * j], x0[3 * j + 1], x0[3 * j + 2]};
+    for (int64_t q = 0; q < numSeg; ++q) ddd::sx::sigma_point(K, s[q], x, sig);
+    for (int k = 0; k < 6; ++k) sigma[6 * j + k] = sig[k];
+  }
+}

@@ -41,6 +41,8 @@ def fasthost(tmp_path_factory):
     lib.fast_segseg_ser.argtypes = [ctypes.c_int, dp, dp, dp, ip, ctypes.c_int64, up, ctypes.c_int64, dp]
     lib.fast_segseg_ser.restype = None
     lib.fast_log_atan.argtypes = [ctypes.c_int, dp, ctypes.c_int64, dp, dp]
+    lib.fast_sigma.argtypes = [dp, dp, ctypes.c_int64, dp, dp, ip, ctypes.c_int64, ctypes.c_int64, dp]
+    lib.fast_sigma.restype = None
     lib.fast_log_atan.restype = None
 
     def forces(k5, net, fmath=1):
@@ -56,7 +58,16 @@ def fasthost(tmp_path_factory):
         lib.fast_log_atan(kind, x.ctypes.data_as(dp), len(x), lo.ctypes.data_as(dp), at.ctypes.data_as(dp))
         return lo, at
 
+    def sigma(k5, pts, net):
+        pts = np.asfortranarray(pts, np.float64)
+        S = np.zeros((6, pts.shape[1]), order="F")
+        lib.fast_sigma(np.ascontiguousarray(k5).ctypes.data_as(dp), pts.ctypes.data_as(dp), pts.shape[1],
+                       net.coord.ctypes.data_as(dp), net.bVec.ctypes.data_as(dp), net.segIdx.ctypes.data_as(ip),
+                       net.segIdx.shape[0], net.numSeg, S.ctypes.data_as(dp))
+        return S
+
     forces.log_atan = log_atan
+    forces.sigma = sigma
     return forces
 
 
@@ -125,3 +136,21 @@ def test_integer_log_atan_ulps(fasthost):
     assert lo_s[0] == -np.inf and lo_s[1] == np.inf and lo_s[2] == 0.0 and np.isclose(lo_s[3], np.log(5e-320))
     assert at_s[1] == np.pi / 2 and at_s[0] == 0.0 and at_s[4] == -np.pi / 2 and np.isnan(at_s[5])
     assert at_s[6] == 1e-30
+
+
+@pytest.mark.parametrize("num_loops,cube", [(64, 2000.0), (300, 20000.0), (96, 1500.0)])
+def test_fast_sigma_within_bound(pkg, synth, oracle, fasthost, num_loops, cube):
+    """The fast σ̃ form (sigma_fx.cuh, the header the GPU runs) against long
+    double: normwise within 4x the reference arithmetic's own error (measured
+    2-2.3x; both ~1e-15), and the strict form's per-point bound
+    |Δσ| <= 1e-10 |σ| + 1e-12 max|σ| against the reference arithmetic."""
+    p, b = synth.square_loops(num_loops, 3, 20.0, 200.0, cube, 0.5, 0.1)
+    net = pkg.DislocationNetwork(*synth.network_arrays(p, b))
+    k5 = k5_of(pkg.DislocationParameters(coreRad=1.0), pkg.MaterialParameters(mu=1.0, nu=0.28))
+    pts = np.asfortranarray(np.random.default_rng(1).uniform(0, cube, (3, 1500)))
+    ref = oracle.sigma_tilde(k5, pts, net, nthreads=os.cpu_count() or 1)
+    ld = oracle.sigma_tilde_ld(k5, pts, net, nthreads=os.cpu_count() or 1)
+    F = fasthost.sigma(k5, pts, net)
+    assert np.linalg.norm(F - ld) <= 4 * np.linalg.norm(ref - ld) + 1e-16 * np.linalg.norm(ld)
+    d, n = np.linalg.norm(F - ref, axis=0), np.linalg.norm(ref, axis=0)
+    assert np.all(d <= 1e-10 * n + 1e-12 * n.max())
