@@ -514,7 +514,9 @@ __device__ __forceinline__ int parallel_pair(const KConsts& K, D3 b1, D3 n11, D3
 }
 
 // σ̃ of one segment at one point, added into sig[6] (xx, yy, zz, xy, xz, yz).
-__device__ __forceinline__ void sigma_point(const KConsts& K, D3 b, D3 n1, D3 n2, D3 t, D3 x, double* sig) {
+// txb = t x b depends on the segment only: the caller computes it once per
+// segment with the same operations (the same bits as computing it here).
+__device__ __forceinline__ void sigma_point(const KConsts& K, D3 b, D3 n1, D3 n2, D3 t, D3 txb, D3 x, double* sig) {
   const double mu4pi = K.mu4pi, mu4pinu = K.mu4pinu, nuMu4pinu = K.nuMu4pinu, a2 = K.aSq;
   const double a2mu8pi = a2 * K.mu8pi;
   D3 R = x - n1;
@@ -552,7 +554,6 @@ __device__ __forceinline__ void sigma_point(const KConsts& K, D3 b, D3 n1, D3 n2
   double s_15 = s_15b - s_15a;
   double s_25 = s_25b - s_25a;
 
-  D3 txb = cross(t, b);
   D3 dxb = cross(nd, b);
   double dxbdt = dot(dxb, t);
   double common = mu4pinu * dxbdt;

@@ -30,7 +30,7 @@ constexpr int SIG_TILE = 32;
 __global__ void __launch_bounds__(SIG_TILE, 24)
 sigma_tilde_f64(KConsts K, const double* __restrict__ soa, int64_t npad, int64_t nSeg, const double* __restrict__ x0,
                 int64_t M, double* __restrict__ sigma) {
-  __shared__ double seg[12][SIG_TILE];
+  __shared__ double seg[15][SIG_TILE];  // n1, n2, b, t, t x b
   const int t = threadIdx.x;
   const int64_t j = blockIdx.x * (int64_t)SIG_TILE + t;
   D3 x = {0, 0, 0};
@@ -40,6 +40,12 @@ sigma_tilde_f64(KConsts K, const double* __restrict__ soa, int64_t npad, int64_t
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < 12; ++k) seg[k][t] = soa[k * npad + s0 + t];
+    {
+      const D3 tx = cross(D3{seg[9][t], seg[10][t], seg[11][t]}, D3{seg[6][t], seg[7][t], seg[8][t]});
+      seg[12][t] = tx.x;
+      seg[13][t] = tx.y;
+      seg[14][t] = tx.z;
+    }
     __syncthreads();
     const int n = (int)min((int64_t)SIG_TILE, nSeg - s0);
     if (j < M) {
@@ -48,7 +54,8 @@ sigma_tilde_f64(KConsts K, const double* __restrict__ soa, int64_t npad, int64_t
         D3 n2 = {seg[3][q], seg[4][q], seg[5][q]};
         D3 b = {seg[6][q], seg[7][q], seg[8][q]};
         D3 tt = {seg[9][q], seg[10][q], seg[11][q]};
-        sigma_point(K, b, n1, n2, tt, x, sig);
+        D3 txb = {seg[12][q], seg[13][q], seg[14][q]};
+        sigma_point(K, b, n1, n2, tt, txb, x, sig);
       }
     }
   }
