@@ -266,13 +266,14 @@ def run_surrogate(args, pkg, ctx, k, soa, ref, pairs, ms_fp64, stream, sptr, flu
     for key, xm, far in (("f32c", "f32c", "network"), ("fp64", "fp64", "network"), ("quad3_f32c", "f32c", "quad3"),
                          ("quad3_fp64fast", "fp64_fast", "quad3"), ("quad3_fp64", "fp64", "quad3")):
         with torch.cuda.stream(stream):
-            sur.force(k, soa, out=F, exact_mode=xm, stream=sptr, far=far)  # plan set-up
+            kap = None if far == "network" else pkg.QUAD_KAPPA  # the network's own kappa, or the quadrature's
+            sur.force(k, soa, out=F, exact_mode=xm, stream=sptr, far=far, kappa=kap)  # plan set-up
             ts, rep = [], None
             for _ in range(max(1, min(args.steps, 3))):
                 flush.zero_()
                 a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 a_.record(stream)
-                _, rep = sur.force(k, soa, out=F, exact_mode=xm, stream=sptr, far=far)
+                _, rep = sur.force(k, soa, out=F, exact_mode=xm, stream=sptr, far=far, kappa=kap)
                 b_.record(stream)
                 torch.cuda.synchronize()
                 ts.append(a_.elapsed_time(b_))
@@ -286,7 +287,7 @@ def run_surrogate(args, pkg, ctx, k, soa, ref, pairs, ms_fp64, stream, sptr, flu
             out[key] = {
                 "value": pairs / (ms * 1e-3), "unit": "pair-interactions/s", "ms_per_step": ms,
                 "speedup_vs_fp64": ms_fp64 / ms, "far": "FP32 Gauss-Legendre quadrature, 3 points per segment",
-                "exact_passes": xm,
+                "kappa": pkg.QUAD_KAPPA, "exact_passes": xm,
                 "error_vs_fp64": {"rel_rms": (torch.linalg.norm(F - refv) / torch.linalg.norm(refv)).item(),
                                   "median_rel_node": (dn / fn).median().item(),
                                   "max_node_over_max_force": (dn.max() / fn.max()).item()},

@@ -118,6 +118,13 @@ class ddd_sur_opts(ctypes.Structure):
 
 # Far-pair passes of ddd_surrogate_force (ddd_sur_opts.far_mode).
 FAR_MODES = {"network": 0, "quad2": 2, "quad3": 3}
+# Default trust factor of the quadrature far field: the 3-point rule (far_mode
+# 3) stays at its FP32 noise level (~2e-7 per pair) down to R = 8 max(L_i, L_j),
+# so the near pass can stop at 10 lengths; the 2-point rule (far_mode 2) needs
+# 20 (4e-6 per pair there, 3e-5 at 10).  The network's factor is its training
+# range (the checkpoint's kappa).
+QUAD_KAPPA = 10.0
+QUAD2_KAPPA = 20.0
 
 
 class ddd_sur_report(ctypes.Structure):
@@ -897,7 +904,9 @@ class Surrogate:
         if fm == 0 and self.nu is not None and abs(_nu_of(k) - self.nu) > 1e-9:
             raise DDDError(DDD_EINVAL, "surrogate trained for nu = %.6g, called with nu = %.6g"
                            % (self.nu, _nu_of(k)))
-        return ddd_sur_opts(self.kappa if kappa is None else float(kappa), float(audit_fraction), float(audit_tol),
+        if kappa is None:
+            kappa = QUAD_KAPPA if fm == 3 else (QUAD2_KAPPA if fm == 2 else self.kappa)
+        return ddd_sur_opts(float(kappa), float(audit_fraction), float(audit_tol),
                             MODES.get(exact_mode, exact_mode) if isinstance(exact_mode, str) else int(exact_mode),
                             fm)
 

@@ -445,8 +445,10 @@ function loadSurrogate(path::AbstractString)
 end
 
 # A handle without a checkpoint, for far_mode = 2 or 3 (the quadrature reads
-# no weights); kappa is the near/far threshold R >= kappa max(L_i, L_j).
-function quadratureFarField(; kappa = 20.0)
+# no weights); kappa is the near/far threshold R >= kappa max(L_i, L_j).  The
+# 3-point rule (far_mode 3) is at its FP32 noise level (~2e-7 per pair) from
+# R = 8 max(L) on, so 10 suffices; the 2-point rule needs 20.
+function quadratureFarField(; kappa = 10.0)
     p = ccall((:ddd_surrogate_create, libddd), Ptr{Cvoid}, (Ptr{Cvoid}, UInt64), context(), 0)
     p == C_NULL && error("ddd_surrogate_create failed")
     s = Surrogate(p, kappa, NaN)

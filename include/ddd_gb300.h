@@ -462,7 +462,10 @@ int ddd_surrogate_load(ddd_surrogate* s, const char* path, double* kappa, double
  * stream, after waiting for all work already queued on the device) and the
  * call returns when the forces are complete. */
 typedef struct {
-  double kappa;          /* trust-region factor; the network's training range sets it (> 0) */
+  double kappa;          /* trust-region factor R >= kappa max(L_i, L_j) for far pairs (> 0): the network's
+                            training range sets it for far_mode 0 (the checkpoint's kappa); for the
+                            3-point quadrature 10 suffices (at the FP32 noise level from 8), for the
+                            2-point rule 20 */
   double audit_fraction; /* in [0, 1]; 0 disables the audit */
   double audit_tol;      /* bound of the estimated node-force relative RMS error; <= 0: no fallback */
   int exact_mode;        /* arithmetic of the exact passes (near, audit, fallback): DDD_MODE_FP64 (strict),
