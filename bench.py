@@ -687,7 +687,7 @@ def summary(line, variants, surrogate, sigma32k, batched):
     if batched:
         out["batched"] = {m: {"pairs_per_s": _r(batched[m]["value"]),
                               "rel_rms": _r(batched[m]["error_vs_fp64"]["rel_rms"], 3)}
-                          for m in ("f32c", "fp64") if m in batched}
+                          for m in ("f32c", "fp64", "fp64_fast") if m in batched}
     return out
 
 
@@ -1017,7 +1017,8 @@ def main():
     # Batched form: 256 independent networks (segment counts log-uniform in
     # [64, 8192], own seeds, cubes 2000-20000 b, slip-system subsets) in one
     # persistent launch replayed from a CUDA graph.  The f32c plan is autotuned
-    # (tile 64/128 x work order); the FP64 plan uses the default tile 128.
+    # (tile 64/128 x work order); the FP64 plans (strict and fast) use the
+    # default tile 128.
     batched = None
     if not args.no_batched:
         nets = synth.batch_networks(256, seed=0)
@@ -1038,7 +1039,7 @@ def main():
             off_ += n_
         torch.cuda.synchronize()
         bref_n = torch.linalg.norm(bref.view(tot, 2, 3), dim=2)
-        for mode, tune in (("f32c", True), ("fp64", False)):
+        for mode, tune in (("f32c", True), ("fp64", False), ("fp64_fast", False)):
             plan = pkg.Batch(ctx, sizes, mode=mode, tune=tune)
             with torch.cuda.stream(stream):
                 plan.run(k, bsegs.data_ptr(), bforce.data_ptr(), stream=sptr)  # tune (if asked) + graph capture

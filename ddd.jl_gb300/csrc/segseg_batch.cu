@@ -13,8 +13,10 @@
 // in a fixed order.  Results are deterministic and equal, bit for bit, to the
 // per-network launches with the same tile size and arithmetic.
 //
-// Arithmetic: DDD_MODE_FP64 (strict), DDD_MODE_DF64, DDD_MODE_F32C.  The file
-// is compiled with --fmad=false (strict FP64 rounding, exact df64 transforms).
+// Arithmetic: DDD_MODE_FP64 (strict), DDD_MODE_FP64_FAST (tile_pol_fx.cuh),
+// DDD_MODE_DF64, DDD_MODE_F32C.  The file is compiled with --fmad=false (strict
+// FP64 rounding, the fast form's explicit fused operations only, exact df64
+// transforms).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -30,12 +32,16 @@
 #include "pair_f64.cuh"
 #include "tile_body.cuh"
 #include "tile_pol_df.cuh"
+#include "tile_pol_fx.cuh"
 
 namespace ddd {
 namespace batch {
 
 template <int FORM>
 using PolDFb = PolDF<FORM>;  // tile_pol_df.cuh
+
+// The precision forms read the df64 SoA as well.
+bool uses_df(int mode) { return mode == DDD_MODE_DF64 || mode == DDD_MODE_F32C; }
 
 // Padded SoA from the caller's packed 9 × ld array; src[g] = source column or -1.
 __global__ void prep_batched(const double* __restrict__ in, int64_t ldIn, const uint8_t* __restrict__ ext,
@@ -224,7 +230,7 @@ cudaError_t build_layout(ddd_batch* b, Layout& L, int T, int order) {
   cudaError_t e;
   if ((e = L.soa.ensure((size_t)ntot * 13 * sizeof(double))) != cudaSuccess) return e;
   if ((e = L.skip.ensure((size_t)ntot)) != cudaSuccess) return e;
-  if (b->mode != DDD_MODE_FP64 && (e = L.soadf.ensure((size_t)ntot * 26 * sizeof(float))) != cudaSuccess) return e;
+  if (uses_df(b->mode) && (e = L.soadf.ensure((size_t)ntot * 26 * sizeof(float))) != cudaSuccess) return e;
   if ((e = L.partial.ensure((size_t)slots * 12 * T * sizeof(double))) != cudaSuccess) return e;
   if ((e = L.items.ensure(items.size() * sizeof(int4))) != cudaSuccess) return e;
   if ((e = L.src.ensure(src.size() * sizeof(int32_t))) != cudaSuccess) return e;
@@ -296,7 +302,7 @@ cudaError_t enqueue(ddd_batch* b, Layout& L, const ddd_consts* k, const double* 
   prep_batched<<<(unsigned)((ntot + 255) / 256), 256, 0, st>>>(segs, b->totalSeg, ext, (const int32_t*)L.src.p, ntot,
                                                                (double*)L.soa.p, (uint8_t*)L.skip.p);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  if (b->mode != DDD_MODE_FP64) {
+  if (uses_df(b->mode)) {
     if ((e = launch_prep_df((const double*)L.soa.p, ntot, (float*)L.soadf.p, st)) != cudaSuccess) return e;
   }
   const KConsts K = kconsts(k);
@@ -305,6 +311,9 @@ cudaError_t enqueue(ddd_batch* b, Layout& L, const ddd_consts* k, const double* 
   if (b->mode == DDD_MODE_FP64) {
     e = L.T == 64 ? launch_persistent<64, PolF64>(A, PolF64::Consts{}, L, next, counters, st)
                   : launch_persistent<128, PolF64>(A, PolF64::Consts{}, L, next, counters, st);
+  } else if (b->mode == DDD_MODE_FP64_FAST) {
+    e = L.T == 64 ? launch_persistent<64, PolF64Fast>(A, PolF64Fast::Consts{}, L, next, counters, st)
+                  : launch_persistent<128, PolF64Fast>(A, PolF64Fast::Consts{}, L, next, counters, st);
   } else if (b->mode == DDD_MODE_DF64) {
     const PolDFb<0>::Consts KP{kconsts_df(K), kconsts_f(K)};
     e = L.T == 64 ? launch_persistent<64, PolDFb<0>>(A, KP, L, next, counters, st)
@@ -333,6 +342,8 @@ Layout& layout_of(ddd_batch* b, const Config& c) { return b->lay[c.T == 64 ? 0 :
 cudaError_t prepare(ddd_batch* b, Layout& L) {
   if (b->mode == DDD_MODE_FP64) return L.T == 64 ? prepare_persistent<64, PolF64>(b->device, L)
                                                  : prepare_persistent<128, PolF64>(b->device, L);
+  if (b->mode == DDD_MODE_FP64_FAST) return L.T == 64 ? prepare_persistent<64, PolF64Fast>(b->device, L)
+                                                      : prepare_persistent<128, PolF64Fast>(b->device, L);
   if (b->mode == DDD_MODE_DF64) return L.T == 64 ? prepare_persistent<64, PolDFb<0>>(b->device, L)
                                                  : prepare_persistent<128, PolDFb<0>>(b->device, L);
   return L.T == 64 ? prepare_persistent<64, PolDFb<1>>(b->device, L)
@@ -357,7 +368,8 @@ extern "C" {
 ddd_batch* ddd_batch_create(ddd_ctx* ctx, int64_t nNet, const int64_t* numSeg, int mode, int tune) {
   DDD_NVTX("ddd_batch_create");
   if (!ctx || nNet < 0 || (nNet > 0 && !numSeg)) return nullptr;
-  if (mode != DDD_MODE_FP64 && mode != DDD_MODE_DF64 && mode != DDD_MODE_F32C) return nullptr;
+  if (mode != DDD_MODE_FP64 && mode != DDD_MODE_FP64_FAST && mode != DDD_MODE_DF64 && mode != DDD_MODE_F32C)
+    return nullptr;
   ddd_batch* b = new ddd_batch();
   b->device = ddd::ctx_device(ctx);
   b->mode = mode;

@@ -332,7 +332,8 @@ int ddd_segseg_force_device_noalloc(const ddd_consts* k, const double* segs, int
 /* Batched form (no reference counterpart: the reference evaluates one network
  * per call).  Many independent networks of uneven sizes in one persistent
  * launch replayed from a captured CUDA graph.  A batch plan is made for a list
- * of network sizes and a mode (DDD_MODE_FP64, DDD_MODE_DF64 or DDD_MODE_F32C);
+ * of network sizes and a mode (DDD_MODE_FP64, DDD_MODE_FP64_FAST, DDD_MODE_DF64 or
+ * DDD_MODE_F32C);
  * with tune != 0 its first run times the candidate tile sizes (64, 128) and
  * work orders on the actual inputs and keeps the fastest (remembered per size
  * list and mode for the rest of the process).  Inputs: all networks

@@ -41,7 +41,7 @@ def _per_network(pkg, ctx, k, torch, sizes, segs, ext):
     return np.concatenate(out)
 
 
-@pytest.mark.parametrize("mode", ["fp64", "df64", "f32c"])
+@pytest.mark.parametrize("mode", ["fp64", "fp64_fast", "df64", "f32c"])
 def test_batched_equals_per_network(pkg, synth, mode):
     ctx = pkg.get_context()
     k = pkg.consts_of(pkg.DislocationParameters(coreRad=1.0), pkg.MaterialParameters(mu=1.0, nu=0.28))

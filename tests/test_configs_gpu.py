@@ -9,8 +9,8 @@
   oracle; all pairs on the GPU, 128 sampled segments against the oracle's rows.
 * The batched workload (many networks of 64 to 8,192 segments, each with its
   own seed, cube and slip-system subset, one persistent launch): every
-  network's forces against the oracle, in FP64 under the parity bound and in
-  the df64 / f32c precision forms under their error bounds.
+  network's forces against the oracle, in FP64 (strict and fast) under the
+  parity bound and in the df64 / f32c precision forms under their error bounds.
 
 Bounds are those of tests/test_segseg_gpu.py (forces: per node
 |ΔF| <= 1e-10 |F| + 4 noise, noise being the reference arithmetic's own worst
@@ -108,7 +108,7 @@ def _batch(synth, seed):
     return nets
 
 
-@pytest.mark.parametrize("mode", ["fp64", "df64", "f32c"])
+@pytest.mark.parametrize("mode", ["fp64", "fp64_fast", "df64", "f32c"])
 def test_batched_networks_against_oracle(pkg, synth, oracle, mode):
     torch = pytest.importorskip("torch")
     nets = _batch(synth, 7)
@@ -132,7 +132,7 @@ def test_batched_networks_against_oracle(pkg, synth, oracle, mode):
         # Networks above 1,024 segments: 96 sampled rows of the oracle.
         rows = None if n <= 1024 else np.sort(np.random.default_rng(n).choice(n, 96, replace=False))
         Fc = F if rows is None else F[:, :, rows]
-        if mode == "fp64":
+        if mode in ("fp64", "fp64_fast"):
             check_forces(Fc, oracle, k5, net, rows=rows)
             continue
         ext = oracle.segseg_ser_ld(k5, net, rows, nthreads=NT)
