@@ -82,13 +82,23 @@ QF_HD V3f cross(V3f a, V3f b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x *
 // Forces on the field segment's two nodes (Fa on n1f, Fb on n2f) from the
 // source segment o.  dm = m_f - m_o (midpoint difference, FP32 to ~1e-7
 // relative), lf = n2f - n1f, bf its Burgers vector; to, Lo, bo of the source.
+//
+// sigma b_f at a field point is Lo sum_term S_term V_term (S_term the weighted
+// source integrals of the s-derivatives).  Expanding the five V_term, the sum
+// is a combination of five vectors only, b_f, nd, t x b, t and nd x b:
+//   beta_b   = c (S03 + a^2 S05)
+//   beta_nd  = mu4pinu S03 (txb.b_f) + c (S05 (nd.b_f) - S15 (t.b_f))
+//   beta_txb = mu4pinu S03 (nd.b_f) + (t.b_f) h
+//   beta_t   = -(dxb.b_f) g + (txb.b_f) h + c (S25 (t.b_f) - S15 (nd.b_f))
+//   beta_dxb = -(t.b_f) g
+// with g = mu4pi S03 + a^2 mu8pi S05 and h = a^2 mu8pi S15 - nu mu4pinu S13
+// (V15's t-only part and V13 both fold into h).  Lo is folded into the source
+// weights.
 template <int NQ>
 QF_HD void side(const QConst& K, V3f dm, V3f lf, V3f bf, V3f to, float Lo, V3f bo, V3f& Fa, V3f& Fb) {
   const V3f txb = cross(to, bo);
   const float tb = dot(to, bf), txbb = dot(txb, bf);
-  const V3f V13 = (-K.nuMu4pinu) * (txbb * to + tb * txb);
-  const V3f T15 = K.a2mu8pi * (txbb * to + tb * txb);  // the t-only part of V15
-  const V3f R0 = dm + (0.5f * Lo) * to;              // x - n1o at xi = 1/2
+  const V3f R0 = dm + (0.5f * Lo) * to;  // x - n1o at xi = 1/2
   Fa = {0.f, 0.f, 0.f};
   Fb = {0.f, 0.f, 0.f};
 #pragma unroll
@@ -102,25 +112,29 @@ QF_HD void side(const QConst& K, V3f dm, V3f lf, V3f bf, V3f to, float Lo, V3f b
     const V3f dxb = cross(nd, bo);
     const float c = K.mu4pinu * dot(dxb, to);
     const float ndb = dot(nd, bf), dxbb = dot(dxb, bf);
-    const V3f tdx = dxbb * to + tb * dxb;
-    const V3f V03 = c * bf + K.mu4pinu * (txbb * nd + ndb * txb) - K.mu4pi * tdx;
-    const V3f V05 = c * (K.a2 * bf + ndb * nd) - K.a2mu8pi * tdx;
-    const V3f V15 = T15 - c * (ndb * to + tb * nd);
-    const V3f V25 = (c * tb) * to;
     float S03 = 0.f, S13 = 0.f, S05 = 0.f, S15 = 0.f, S25 = 0.f;
 #pragma unroll
     for (int h = 0; h < NQ; ++h) {
       const float s = s1 + Lo * Rule<NQ>::x(h);
       const float ri = rsqrt_(A + s * s);
-      const float w3 = Rule<NQ>::w(h) * ri * ri * ri;
-      const float w5 = 3.0f * w3 * ri * ri;
+      const float ri2 = ri * ri;
+      const float w3 = (Lo * Rule<NQ>::w(h)) * ri2 * ri;
+      const float w5 = 3.0f * w3 * ri2;
       S03 += w3;
       S13 += w3 * s;
       S05 += w5;
       S15 += w5 * s;
       S25 += w5 * s * s;
     }
-    const V3f sb = Lo * (S03 * V03 + S13 * V13 + S05 * V05 + S15 * V15 + S25 * V25);
+    const float gq = K.mu4pi * S03 + K.a2mu8pi * S05;
+    const float hq = K.a2mu8pi * S15 - K.nuMu4pinu * S13;
+    const float m03 = K.mu4pinu * S03;
+    const float bb = c * (S03 + K.a2 * S05);
+    const float bn = m03 * txbb + c * (S05 * ndb - S15 * tb);
+    const float bx = m03 * ndb + tb * hq;
+    const float bt = txbb * hq - dxbb * gq + c * (S25 * tb - S15 * ndb);
+    const float bd = -tb * gq;
+    const V3f sb = bb * bf + bn * nd + bx * txb + bt * to + bd * dxb;
     const V3f f = cross(sb, lf);
     const float w = Rule<NQ>::w(g);
     Fa = Fa + (w * (1.0f - xi)) * f;
