@@ -70,6 +70,10 @@ __device__ __forceinline__ qf::SegD seg_d(const double* __restrict__ soa, int64_
   return d;
 }
 
+// Near-parallel pairs listed per round: a tile pair with more (up to 128 x 128)
+// takes several rounds.  The cap keeps the shared memory at four CTAs per SM.
+constexpr int kPCap = 8192;
+
 // Shared memory of one CTA: the column tile, per-warp column forces, and the
 // compaction state of the near-parallel pairs.
 struct QuadSmem {
@@ -77,16 +81,16 @@ struct QuadSmem {
   float cQ[kQsRows][TQ];          // quadrature data of the column tile
   float sFJ[TQ / 32][6][TQ];      // per-warp column forces
   float cf[TQ][12];               // dense pass: one pair's four node forces per thread
-  uint16_t plist[TQ * TQ];        // near-parallel pairs (row << 8 | column), by row then step
+  uint16_t plist[kPCap];          // near-parallel pairs (row << 8 | column), by row then step: one round
   int cnt[TQ];
   int total;
 };
 
-// Five CTAs of 128 threads per SM fit the registers; the near-parallel pairs
-// run in a dense pass after the sweep (as in tile_body.cuh), so a warp never
-// waits on one lane's FP64 branch.
+// Four CTAs of 128 threads per SM (128 registers per thread, 43 KB of shared
+// memory each); the near-parallel pairs run in a dense pass after the sweep (as
+// in tile_body.cuh), so a warp never waits on one lane's FP64 branch.
 template <int NQ>
-__global__ void __launch_bounds__(TQ)
+__global__ void __launch_bounds__(TQ, 4)
 quad_far_tiles(const float* __restrict__ ms, const float* __restrict__ qs, const double* __restrict__ soa, int64_t npad,
                const int4* __restrict__ items, int32_t nItems, qf::QConst K, float kappa2, double* __restrict__ partial) {
   extern __shared__ __align__(16) unsigned char qsm_raw[];
@@ -194,57 +198,64 @@ quad_far_tiles(const float* __restrict__ ms, const float* __restrict__ qs, const
     __syncthreads();
     const int myOff = sm.cnt[t];
     if (t == TQ - 1) sm.total = myOff + myCnt;
-    {
-      int o = myOff;
-      for (int k = 0; k < TQ; ++k) {
-        const int jl = (t + k) & (TQ - 1);
-        if (pmask[jl >> 5] & (1u << (jl & 31))) sm.plist[o++] = (uint16_t)((t << 8) | jl);
-      }
-    }
     __syncthreads();
     const int nPar = sm.total;
     qf::V3f fc3 = {0.f, 0.f, 0.f}, fc4 = {0.f, 0.f, 0.f};  // this thread's column segment
-    for (int base = 0; base < nPar; base += TQ) {
-      const int e = base + t;
-      if (e < nPar) {
-        const int il = sm.plist[e] >> 8, jl = sm.plist[e] & 0xff;
-        const int64_t gi = i0 + il, gj = j0 + jl;
-        const qf::SegD si = seg_d(soa, npad, gi), sj = seg_d(soa, npad, gj);
-        double c;
-        qf::par_decision(si.t, sj.t, c);
-        const float mi2[3] = {ms[(sur::kMsM + 0) * npad + gi], ms[(sur::kMsM + 1) * npad + gi],
-                              ms[(sur::kMsM + 2) * npad + gi]};
-        const qf::V3f dm = {(mi2[0] - sm.cM[0][jl]) + (qs[(kQLo + 0) * npad + gi] - sm.cQ[kQLo + 0][jl]),
-                            (mi2[1] - sm.cM[1][jl]) + (qs[(kQLo + 1) * npad + gi] - sm.cQ[kQLo + 1][jl]),
-                            (mi2[2] - sm.cM[2][jl]) + (qs[(kQLo + 2) * npad + gi] - sm.cQ[kQLo + 2][jl])};
-        const qf::V3f la = {qs[(kQL + 0) * npad + gi], qs[(kQL + 1) * npad + gi], qs[(kQL + 2) * npad + gi]};
-        const qf::V3f ba = {qs[(kQB + 0) * npad + gi], qs[(kQB + 1) * npad + gi], qs[(kQB + 2) * npad + gi]};
-        const qf::V3f lb = {sm.cQ[kQL + 0][jl], sm.cQ[kQL + 1][jl], sm.cQ[kQL + 2][jl]};
-        const qf::V3f bb = {sm.cQ[kQB + 0][jl], sm.cQ[kQB + 1][jl], sm.cQ[kQB + 2][jl]};
-        qf::V3f Fa, Fb, Fc, Fd;
-        qf::par_pair<NQ>(K, si, sj, c, dm, la, ba, lb, bb, Fa, Fb, Fc, Fd);
-        const float v[12] = {Fa.x, Fa.y, Fa.z, Fb.x, Fb.y, Fb.z, Fc.x, Fc.y, Fc.z, Fd.x, Fd.y, Fd.z};
-#pragma unroll
-        for (int c2 = 0; c2 < 12; ++c2) sm.cf[t][c2] = v[c2];
-      }
-      __syncthreads();
-      const int lim = min(TQ, nPar - base);
-      // Row forces: this thread's own entries, in list order.
-      const int lo = max(myOff, base), hi = min(myOff + myCnt, base + lim);
-      for (int e2 = lo; e2 < hi; ++e2) {
-        const float* f = sm.cf[e2 - base];
-        f1 = f1 + qf::V3f{f[0], f[1], f[2]};
-        f2 = f2 + qf::V3f{f[3], f[4], f[5]};
-      }
-      // Column forces: the entries whose column is this thread's, in list order.
-      for (int q = 0; q < lim; ++q) {
-        if ((sm.plist[base + q] & 0xff) == t) {
-          const float* f = sm.cf[q];
-          fc3 = fc3 + qf::V3f{f[6], f[7], f[8]};
-          fc4 = fc4 + qf::V3f{f[9], f[10], f[11]};
+    for (int r0 = 0; r0 < nPar; r0 += kPCap) {  // rounds of at most kPCap listed pairs
+      const int rEnd = min(nPar, r0 + kPCap);
+      {
+        int o = myOff;
+        for (int k = 0; k < TQ; ++k) {
+          const int jl = (t + k) & (TQ - 1);
+          if (pmask[jl >> 5] & (1u << (jl & 31))) {
+            if (o >= r0 && o < rEnd) sm.plist[o - r0] = (uint16_t)((t << 8) | jl);
+            ++o;
+          }
         }
       }
       __syncthreads();
+      for (int base = r0; base < rEnd; base += TQ) {
+        const int e = base + t;
+        if (e < rEnd) {
+          const int il = sm.plist[e - r0] >> 8, jl = sm.plist[e - r0] & 0xff;
+          const int64_t gi = i0 + il, gj = j0 + jl;
+          const qf::SegD si = seg_d(soa, npad, gi), sj = seg_d(soa, npad, gj);
+          double c;
+          qf::par_decision(si.t, sj.t, c);
+          const float mi2[3] = {ms[(sur::kMsM + 0) * npad + gi], ms[(sur::kMsM + 1) * npad + gi],
+                                ms[(sur::kMsM + 2) * npad + gi]};
+          const qf::V3f dm = {(mi2[0] - sm.cM[0][jl]) + (qs[(kQLo + 0) * npad + gi] - sm.cQ[kQLo + 0][jl]),
+                              (mi2[1] - sm.cM[1][jl]) + (qs[(kQLo + 1) * npad + gi] - sm.cQ[kQLo + 1][jl]),
+                              (mi2[2] - sm.cM[2][jl]) + (qs[(kQLo + 2) * npad + gi] - sm.cQ[kQLo + 2][jl])};
+          const qf::V3f la = {qs[(kQL + 0) * npad + gi], qs[(kQL + 1) * npad + gi], qs[(kQL + 2) * npad + gi]};
+          const qf::V3f ba = {qs[(kQB + 0) * npad + gi], qs[(kQB + 1) * npad + gi], qs[(kQB + 2) * npad + gi]};
+          const qf::V3f lb = {sm.cQ[kQL + 0][jl], sm.cQ[kQL + 1][jl], sm.cQ[kQL + 2][jl]};
+          const qf::V3f bb = {sm.cQ[kQB + 0][jl], sm.cQ[kQB + 1][jl], sm.cQ[kQB + 2][jl]};
+          qf::V3f Fa, Fb, Fc, Fd;
+          qf::par_pair<NQ>(K, si, sj, c, dm, la, ba, lb, bb, Fa, Fb, Fc, Fd);
+          const float v[12] = {Fa.x, Fa.y, Fa.z, Fb.x, Fb.y, Fb.z, Fc.x, Fc.y, Fc.z, Fd.x, Fd.y, Fd.z};
+#pragma unroll
+          for (int c2 = 0; c2 < 12; ++c2) sm.cf[t][c2] = v[c2];
+        }
+        __syncthreads();
+        const int lim = min(TQ, rEnd - base);
+        // Row forces: this thread's own entries, in list order.
+        const int lo = max(myOff, base), hi = min(myOff + myCnt, base + lim);
+        for (int e2 = lo; e2 < hi; ++e2) {
+          const float* f = sm.cf[e2 - base];
+          f1 = f1 + qf::V3f{f[0], f[1], f[2]};
+          f2 = f2 + qf::V3f{f[3], f[4], f[5]};
+        }
+        // Column forces: the entries whose column is this thread's, in list order.
+        for (int q = 0; q < lim; ++q) {
+          if ((sm.plist[base - r0 + q] & 0xff) == t) {
+            const float* f = sm.cf[q];
+            fc3 = fc3 + qf::V3f{f[6], f[7], f[8]};
+            fc4 = fc4 + qf::V3f{f[9], f[10], f[11]};
+          }
+        }
+        __syncthreads();
+      }
     }
 
     // ---- Partials: row segments' then column segments' node forces. ----

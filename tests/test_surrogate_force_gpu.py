@@ -363,3 +363,38 @@ def test_checkpoint_round_trip(pkg, synth, trained, tmp_path):
     k = pkg.consts_of(pkg.DislocationParameters(coreRad=1.0), pkg.MaterialParameters(mu=1.0, nu=0.3))
     with pytest.raises(pkg.DDDError):
         trained.force(k, segs)
+
+
+def test_quadrature_many_near_parallel_far_pairs(pkg, oracle):
+    """256 exactly parallel 20 b segments on two ladders (y = 300 b k, z = 0
+    and 400 b): every pair is far (R >= 15 L) and near-parallel, so every
+    force comes from the quadrature of the reference's projected geometry, and
+    the tile pair between the two sorted tiles holds 16,384 such pairs, more
+    than one round of the far pass's near-parallel list (8,192).  Against the
+    oracle's FP64 forces: relative RMS <= 1e-6, per node <= 1e-4 |F| + 1e-6
+    max |F|, no near pair, every pair counted once."""
+    n = 256
+    coord = np.zeros((3, 2 * n))
+    for s in range(n):
+        y, z = 300.0 * (s % 128), (0.0 if s < 128 else 400.0)
+        coord[:, 2 * s] = [0.0, y, z]
+        coord[:, 2 * s + 1] = [20.0, y, z]
+    bv = np.array([1.0, 1.0, 0.0]) / np.sqrt(2.0)
+    bvec = np.asfortranarray(np.tile(bv[:, None], (1, n)))
+    seg = np.asfortranarray(np.array([[s + 1, 2 * s + 1, 2 * s + 2] for s in range(n)], dtype=np.int64))
+    net = pkg.DislocationNetwork(np.asfortranarray(coord), bvec, seg)
+    segs = np.zeros((9, n))
+    for s in range(n):
+        segs[0:3, s] = coord[:, 2 * s]
+        segs[3:6, s] = coord[:, 2 * s + 1]
+        segs[6:9, s] = bv
+    dln, mat = _params(pkg)
+    sur = pkg.Surrogate(pkg.get_context(), seed=0)
+    F, rep = sur.force(_k(pkg), np.ascontiguousarray(segs), far="quad3", exact_mode="fp64", audit_fraction=0.0)
+    assert rep["pairs_total"] == n * (n - 1) // 2
+    assert rep["pairs_near_general"] + rep["pairs_near_parallel"] == 0
+    G = np.asfortranarray(F.cpu().numpy().reshape(n, 2, 3).transpose(2, 1, 0))
+    ref = oracle.segseg_ser(k5_of(dln, mat), net)
+    nrm = lambda a: np.linalg.norm(a, axis=0)
+    assert np.linalg.norm(G - ref) <= 1e-6 * np.linalg.norm(ref)
+    assert np.all(nrm(G - ref) <= 1e-4 * nrm(ref) + 1e-6 * nrm(ref).max())
