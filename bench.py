@@ -263,17 +263,22 @@ def run_surrogate(args, pkg, ctx, k, soa, ref, pairs, ms_fp64, stream, sptr, flu
     F = torch.empty((n, 6), dtype=torch.float64, device="cuda")
     refv = ref.view(n, 6)
     out = {"source": source, "kappa": sur.kappa, "audit_fraction": 0.01}
-    for key, xm, far in (("f32c", "f32c", "network"), ("fp64", "fp64", "network"), ("quad3_f32c", "f32c", "quad3"),
-                         ("quad3_fp64fast", "fp64_fast", "quad3"), ("quad3_fp64", "fp64", "quad3")):
+    # quad3_*: 3-point rule, switched to 2 points on 32-pair steps beyond QUAD_KAPPA_TWO lengths (the
+    # default); quad3_f32c_no_switch: 3 points everywhere.
+    for key, xm, far, k2 in (("f32c", "f32c", "network", None), ("fp64", "fp64", "network", None),
+                             ("quad3_f32c", "f32c", "quad3", pkg.QUAD_KAPPA_TWO),
+                             ("quad3_f32c_no_switch", "f32c", "quad3", 0.0),
+                             ("quad3_fp64fast", "fp64_fast", "quad3", pkg.QUAD_KAPPA_TWO),
+                             ("quad3_fp64", "fp64", "quad3", pkg.QUAD_KAPPA_TWO)):
         with torch.cuda.stream(stream):
             kap = None if far == "network" else pkg.QUAD_KAPPA  # the network's own kappa, or the quadrature's
-            sur.force(k, soa, out=F, exact_mode=xm, stream=sptr, far=far, kappa=kap)  # plan set-up
+            sur.force(k, soa, out=F, exact_mode=xm, stream=sptr, far=far, kappa=kap, kappa_two=k2)  # plan set-up
             ts, rep = [], None
             for _ in range(max(1, min(args.steps, 3))):
                 flush.zero_()
                 a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 a_.record(stream)
-                _, rep = sur.force(k, soa, out=F, exact_mode=xm, stream=sptr, far=far, kappa=kap)
+                _, rep = sur.force(k, soa, out=F, exact_mode=xm, stream=sptr, far=far, kappa=kap, kappa_two=k2)
                 b_.record(stream)
                 torch.cuda.synchronize()
                 ts.append(a_.elapsed_time(b_))
@@ -286,8 +291,10 @@ def run_surrogate(args, pkg, ctx, k, soa, ref, pairs, ms_fp64, stream, sptr, flu
         if far != "network":
             out[key] = {
                 "value": pairs / (ms * 1e-3), "unit": "pair-interactions/s", "ms_per_step": ms,
-                "speedup_vs_fp64": ms_fp64 / ms, "far": "FP32 Gauss-Legendre quadrature, 3 points per segment",
-                "kappa": pkg.QUAD_KAPPA, "exact_passes": xm,
+                "speedup_vs_fp64": ms_fp64 / ms,
+                "far": "FP32 Gauss-Legendre quadrature, 3 points per segment" + (
+                    ", 2 on 32-pair steps whose far pairs all lie beyond %g lengths" % k2 if k2 else ""),
+                "kappa": pkg.QUAD_KAPPA, "kappa_two": k2, "exact_passes": xm,
                 "error_vs_fp64": {"rel_rms": (torch.linalg.norm(F - refv) / torch.linalg.norm(refv)).item(),
                                   "median_rel_node": (dn / fn).median().item(),
                                   "max_node_over_max_force": (dn.max() / fn.max()).item()},
@@ -672,7 +679,7 @@ def summary(line, variants, surrogate, sigma32k, batched):
             "max_node_over_max": _r(sv["error_vs_fp64"]["max_node_over_max_force"], 3),
             "tensor_frac": _r(sv["network_kernel"]["frac"], 3), "kappa": surrogate["kappa"],
             "arch": "MLP 16-128-128-128-112 GELU, FP16 fwd / FP32 acc, exact bilinear b contraction"}
-    for qk in ("quad3_f32c", "quad3_fp64fast"):
+    for qk in ("quad3_f32c", "quad3_f32c_no_switch", "quad3_fp64fast"):
         if surrogate and qk in surrogate:
             qv = surrogate[qk]
             out[qk] = {"pairs_per_s": _r(qv["value"]), "x_fp64": _r(qv["speedup_vs_fp64"], 3),
@@ -762,6 +769,8 @@ def main():
                     help="only run N surrogate force calls on the workload (no audit) and exit: "
                          "the command the ncu captures of the surrogate kernels use")
     ap.add_argument("--surrogate", default=SURROGATE_CKPT, help="surrogate checkpoint (trained here when missing)")
+    ap.add_argument("--kappa-two", type=float, default=None,
+                    help="--far quad3: 2-point switch threshold in lengths (default the package's, 0 = off)")
     ap.add_argument("--far", default="network", choices=["network", "quad2", "quad3"],
                     help="far pass of --profile-surrogate: the network or FP32 Gauss-Legendre quadrature")
     ap.add_argument("--exact-mode", default="f32c", choices=["f32c", "fp64_fast", "fp64"],
@@ -798,7 +807,8 @@ def main():
         sur = pkg.Surrogate(ctx, seed=0).load(args.surrogate)
         segs = torch.from_numpy(synth.packed_soa(p, b)).cuda()
         for _ in range(args.profile_surrogate):
-            _, rep = sur.force(k, segs, exact_mode=args.exact_mode, audit_fraction=0.0, far=args.far)
+            _, rep = sur.force(k, segs, exact_mode=args.exact_mode, audit_fraction=0.0, far=args.far,
+                               kappa_two=args.kappa_two)
         torch.cuda.synchronize()
         print(json.dumps({"profile_surrogate": args.profile_surrogate, "segments": n, "report": rep}), flush=True)
         return

@@ -113,7 +113,7 @@ class ddd_u_mesh(ctypes.Structure):
 
 class ddd_sur_opts(ctypes.Structure):
     _fields_ = [("kappa", ctypes.c_double), ("audit_fraction", ctypes.c_double), ("audit_tol", ctypes.c_double),
-                ("exact_mode", ctypes.c_int), ("far_mode", ctypes.c_int)]
+                ("exact_mode", ctypes.c_int), ("far_mode", ctypes.c_int), ("kappa_two", ctypes.c_double)]
 
 
 # Far-pair passes of ddd_surrogate_force (ddd_sur_opts.far_mode).
@@ -125,6 +125,11 @@ FAR_MODES = {"network": 0, "quad2": 2, "quad3": 3}
 # range (the checkpoint's kappa).
 QUAD_KAPPA = 10.0
 QUAD2_KAPPA = 20.0
+# The 3-point far pass switches a warp's step of 32 pairs to the 2-point rule
+# when each of its far pairs lies beyond this many lengths: the 2-point rule's
+# truncation (~5e-6 per pair at 20 lengths, falling as (L/R)^4) is then below
+# the far pairs' FP32 noise.
+QUAD_KAPPA_TWO = 30.0
 
 
 class ddd_sur_report(ctypes.Structure):
@@ -874,15 +879,17 @@ class Surrogate:
 
     # -- forces ---------------------------------------------------------------
     def force(self, k, segs, ext=None, kappa=None, audit_fraction=0.01, audit_tol=1e-3, exact_mode="fp64", out=None,
-              stream=None, far="network"):
+              stream=None, far="network", kappa_two=None):
         """ddd_surrogate_force on packed 9 × n segments (a CUDA float64 tensor or
         a numpy array); exact_mode: arithmetic of the exact near / audit passes
         ("fp64", "fp64_fast", "df64" or "f32c"); far: "network", or "quad2" / "quad3" for
-        the far pairs by FP32 Gauss-Legendre quadrature (no network used).
+        the far pairs by FP32 Gauss-Legendre quadrature (no network used);
+        kappa_two: "quad3"'s switch to 2 points beyond that many lengths
+        (default QUAD_KAPPA_TWO, 0 = off).
         Returns (forces as a CUDA tensor n × 6 = the 3 × 2 × n column-major
         array, report dict)."""
         import torch
-        o = self._opts(k, kappa, audit_fraction, audit_tol, exact_mode, far)
+        o = self._opts(k, kappa, audit_fraction, audit_tol, exact_mode, far, kappa_two)
         if not isinstance(segs, torch.Tensor):
             segs = torch.from_numpy(np.ascontiguousarray(segs, dtype=np.float64)).cuda()
         assert segs.dtype == torch.float64 and segs.is_cuda and segs.dim() == 2 and segs.shape[0] == 9
@@ -899,23 +906,25 @@ class Surrogate:
                                              ctypes.byref(o), ctypes.byref(rep)), "surrogate force")
         return out, rep.as_dict()
 
-    def _opts(self, k, kappa, audit_fraction, audit_tol, exact_mode, far="network"):
+    def _opts(self, k, kappa, audit_fraction, audit_tol, exact_mode, far="network", kappa_two=None):
         fm = FAR_MODES.get(far, far) if isinstance(far, str) else int(far)
         if fm == 0 and self.nu is not None and abs(_nu_of(k) - self.nu) > 1e-9:
             raise DDDError(DDD_EINVAL, "surrogate trained for nu = %.6g, called with nu = %.6g"
                            % (self.nu, _nu_of(k)))
         if kappa is None:
             kappa = QUAD_KAPPA if fm == 3 else (QUAD2_KAPPA if fm == 2 else self.kappa)
+        if kappa_two is None:
+            kappa_two = QUAD_KAPPA_TWO if fm == 3 else 0.0
         return ddd_sur_opts(float(kappa), float(audit_fraction), float(audit_tol),
                             MODES.get(exact_mode, exact_mode) if isinstance(exact_mode, str) else int(exact_mode),
-                            fm)
+                            fm, float(kappa_two))
 
     def force_network(self, dlnParams, matParams, network, kappa=None, audit_fraction=0.01, audit_tol=1e-3,
-                      exact_mode="fp64", far="network"):
+                      exact_mode="fp64", far="network", kappa_two=None):
         """The surrogate's calcSegSegForce on a DislocationNetwork's own host arrays
         (ddd_surrogate_force_host): a fresh 3×2×numSeg array and the report."""
         k = consts_of(dlnParams, matParams)
-        o = self._opts(k, kappa, audit_fraction, audit_tol, exact_mode, far)
+        o = self._opts(k, kappa, audit_fraction, audit_tol, exact_mode, far, kappa_two)
         n = network.numSeg
         F = np.zeros((3, 2, n), np.float64, order="F")
         rep = ddd_sur_report()

@@ -16,6 +16,15 @@
 // plus this part gives the midpoint to ~2^-48), the segment vector n2 - n1,
 // the unit direction, the length and the Burgers vector.
 //
+// With 3 points (far_mode 3) a warp's step of 32 pairs takes the 2-point rule
+// instead when each far pair it holds lies beyond kappaTwo max(L_i, L_j)
+// (ddd_sur_opts.kappa_two): the 2-point rule's truncation error falls as
+// (L/R)^4 and is below the FP32 arithmetic's ~2e-7 per pair from ~30 lengths,
+// and it costs 4 + 2 instead of 9 + 3 stress evaluations per side.  The choice
+// is a warp vote on values fixed by the tile layout, so results stay
+// deterministic; the dense near-parallel pass votes the same way over its
+// listed pairs.
+//
 // Near-parallel pairs (1 - c^2 <= sqrt(eps) by the reference's FP64 test on
 // the FP64 directions; an FP32 pre-test with a wide margin picks the
 // candidates) are flagged during the sweep and evaluated afterwards in a
@@ -70,6 +79,15 @@ __device__ __forceinline__ qf::SegD seg_d(const double* __restrict__ soa, int64_
   return d;
 }
 
+// R^2 >= kappaTwo2 max(L_i, L_j)^2 for the midpoint difference d, rounded as
+// the trust test (sur::pair_is_far) rounds it; false when kappaTwo2 is
+// infinite (rule switch off).
+__device__ __forceinline__ bool beyond(float dx, float dy, float dz, float Li, float Lj, float kappaTwo2) {
+  const float R2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+  const float Lm = fmaxf(Li, Lj);
+  return R2 >= __fmul_rn(kappaTwo2, __fmul_rn(Lm, Lm));
+}
+
 // Near-parallel pairs listed per round: a tile pair with more (up to 128 x 128)
 // takes several rounds.  The cap keeps the shared memory at four CTAs per SM.
 constexpr int kPCap = 8192;
@@ -92,7 +110,8 @@ struct QuadSmem {
 template <int NQ>
 __global__ void __launch_bounds__(TQ, 4)
 quad_far_tiles(const float* __restrict__ ms, const float* __restrict__ qs, const double* __restrict__ soa, int64_t npad,
-               const int4* __restrict__ items, int32_t nItems, qf::QConst K, float kappa2, double* __restrict__ partial) {
+               const int4* __restrict__ items, int32_t nItems, qf::QConst K, float kappa2, float kappaTwo2,
+               double* __restrict__ partial) {
   extern __shared__ __align__(16) unsigned char qsm_raw[];
   QuadSmem& sm = *reinterpret_cast<QuadSmem*>(qsm_raw);
   constexpr int NW = TQ / 32;
@@ -128,10 +147,14 @@ quad_far_tiles(const float* __restrict__ ms, const float* __restrict__ qs, const
     for (int q = 0; q < NW; ++q) pmask[q] = 0;
     for (int k = 0; k < TQ; ++k) {
       const int jl = (t + k) & (TQ - 1);
-      float dx, dy, dz;
+      float dx, dy, dz, R2, Lm2;
       const bool far = sur::pair_is_far(mi[0], mi[1], mi[2], Li, sm.cM[0][jl], sm.cM[1][jl], sm.cM[2][jl],
-                                        sm.cLen[jl], kappa2, dx, dy, dz);
-      if (far && (!diag || jl > t)) {
+                                        sm.cLen[jl], kappa2, dx, dy, dz, R2, Lm2);
+      const bool take = far && (!diag || jl > t);
+      // 2-point rule for this step when every pair the warp takes lies beyond
+      // kappaTwo max(L_i, L_j) (a warp-uniform choice, fixed by the tile layout).
+      const bool two = NQ == 2 || !__any_sync(0xffffffffu, take && !(R2 >= __fmul_rn(kappaTwo2, Lm2)));
+      if (take) {
         const qf::V3f tj = {sm.cQ[kQT + 0][jl], sm.cQ[kQT + 1][jl], sm.cQ[kQT + 2][jl]};
         const float c32 = qf::dot(ti, tj);
         bool par = false;
@@ -153,8 +176,13 @@ quad_far_tiles(const float* __restrict__ ms, const float* __restrict__ qs, const
           const qf::V3f bj = {sm.cQ[kQB + 0][jl], sm.cQ[kQB + 1][jl], sm.cQ[kQB + 2][jl]};
           const float Lnj = sm.cQ[kQLen][jl];
           qf::V3f Fa, Fb, Fc, Fd;
-          qf::side<NQ>(K, dm, li, bi, tj, Lnj, bj, Fa, Fb);
-          qf::side<NQ>(K, {-dm.x, -dm.y, -dm.z}, lj, bj, ti, Lni, bi, Fc, Fd);
+          if (two) {
+            qf::side<2>(K, dm, li, bi, tj, Lnj, bj, Fa, Fb);
+            qf::side<2>(K, {-dm.x, -dm.y, -dm.z}, lj, bj, ti, Lni, bi, Fc, Fd);
+          } else {
+            qf::side<NQ>(K, dm, li, bi, tj, Lnj, bj, Fa, Fb);
+            qf::side<NQ>(K, {-dm.x, -dm.y, -dm.z}, lj, bj, ti, Lni, bi, Fc, Fd);
+          }
           f1 = f1 + Fa;
           f2 = f2 + Fb;
           float* fj = &sm.sFJ[warp][0][0];
@@ -216,14 +244,21 @@ quad_far_tiles(const float* __restrict__ ms, const float* __restrict__ qs, const
       __syncthreads();
       for (int base = r0; base < rEnd; base += TQ) {
         const int e = base + t;
-        if (e < rEnd) {
-          const int il = sm.plist[e - r0] >> 8, jl = sm.plist[e - r0] & 0xff;
-          const int64_t gi = i0 + il, gj = j0 + jl;
+        const bool has = e < rEnd;
+        const int il = has ? sm.plist[e - r0] >> 8 : 0, jl = has ? sm.plist[e - r0] & 0xff : 0;
+        const int64_t gi = i0 + il, gj = j0 + jl;
+        const float mi2[3] = {ms[(sur::kMsM + 0) * npad + gi], ms[(sur::kMsM + 1) * npad + gi],
+                              ms[(sur::kMsM + 2) * npad + gi]};
+        // The same warp-uniform choice of rule as the sweep's, over this warp's listed pairs.
+        const bool two =
+            NQ == 2 || !__any_sync(0xffffffffu, has && !beyond(__fsub_rn(sm.cM[0][jl], mi2[0]),
+                                                               __fsub_rn(sm.cM[1][jl], mi2[1]),
+                                                               __fsub_rn(sm.cM[2][jl], mi2[2]),
+                                                               ms[sur::kMsL * npad + gi], sm.cLen[jl], kappaTwo2));
+        if (has) {
           const qf::SegD si = seg_d(soa, npad, gi), sj = seg_d(soa, npad, gj);
           double c;
           qf::par_decision(si.t, sj.t, c);
-          const float mi2[3] = {ms[(sur::kMsM + 0) * npad + gi], ms[(sur::kMsM + 1) * npad + gi],
-                                ms[(sur::kMsM + 2) * npad + gi]};
           const qf::V3f dm = {(mi2[0] - sm.cM[0][jl]) + (qs[(kQLo + 0) * npad + gi] - sm.cQ[kQLo + 0][jl]),
                               (mi2[1] - sm.cM[1][jl]) + (qs[(kQLo + 1) * npad + gi] - sm.cQ[kQLo + 1][jl]),
                               (mi2[2] - sm.cM[2][jl]) + (qs[(kQLo + 2) * npad + gi] - sm.cQ[kQLo + 2][jl])};
@@ -232,7 +267,10 @@ quad_far_tiles(const float* __restrict__ ms, const float* __restrict__ qs, const
           const qf::V3f lb = {sm.cQ[kQL + 0][jl], sm.cQ[kQL + 1][jl], sm.cQ[kQL + 2][jl]};
           const qf::V3f bb = {sm.cQ[kQB + 0][jl], sm.cQ[kQB + 1][jl], sm.cQ[kQB + 2][jl]};
           qf::V3f Fa, Fb, Fc, Fd;
-          qf::par_pair<NQ>(K, si, sj, c, dm, la, ba, lb, bb, Fa, Fb, Fc, Fd);
+          if (two)
+            qf::par_pair<2>(K, si, sj, c, dm, la, ba, lb, bb, Fa, Fb, Fc, Fd);
+          else
+            qf::par_pair<NQ>(K, si, sj, c, dm, la, ba, lb, bb, Fa, Fb, Fc, Fd);
           const float v[12] = {Fa.x, Fa.y, Fa.z, Fb.x, Fb.y, Fb.z, Fc.x, Fc.y, Fc.z, Fd.x, Fd.y, Fd.z};
 #pragma unroll
           for (int c2 = 0; c2 < 12; ++c2) sm.cf[t][c2] = v[c2];
@@ -301,16 +339,18 @@ int quad_far_blocks_per_sm(int nq) {
 }
 
 cudaError_t launch_quad_far_tiles(const float* ms, const float* qs, const double* soa, int64_t npad, const int4* items,
-                                  int32_t nItems, int nq, const KConsts& K, float kappa2, double* partial, int grid,
-                                  cudaStream_t st) {
+                                  int32_t nItems, int nq, const KConsts& K, float kappa2, float kappaTwo2,
+                                  double* partial, int grid, cudaStream_t st) {
   if (nItems <= 0) return cudaSuccess;
   const qf::QConst Q{(float)K.aSq, (float)K.mu4pi, (float)K.mu4pinu, (float)K.nuMu4pinu, (float)(K.aSq * K.mu8pi)};
   cudaError_t e = nq == 2 ? set_attr_quad<2>() : set_attr_quad<3>();
   if (e != cudaSuccess) return e;
   if (nq == 2)
-    quad_far_tiles<2><<<grid, TQ, sizeof(QuadSmem), st>>>(ms, qs, soa, npad, items, nItems, Q, kappa2, partial);
+    quad_far_tiles<2><<<grid, TQ, sizeof(QuadSmem), st>>>(ms, qs, soa, npad, items, nItems, Q, kappa2, kappaTwo2,
+                                                                 partial);
   else
-    quad_far_tiles<3><<<grid, TQ, sizeof(QuadSmem), st>>>(ms, qs, soa, npad, items, nItems, Q, kappa2, partial);
+    quad_far_tiles<3><<<grid, TQ, sizeof(QuadSmem), st>>>(ms, qs, soa, npad, items, nItems, Q, kappa2, kappaTwo2,
+                                                                 partial);
   return cudaGetLastError();
 }
 

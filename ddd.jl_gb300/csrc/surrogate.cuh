@@ -186,13 +186,20 @@ constexpr int kMsM = 0, kMsT = 3, kMsL = 6, kMsB = 7;
 // the result identical whatever the contraction flags of the translation unit,
 // so each pair is counted by exactly one of the network and the exact pass.
 __device__ __forceinline__ bool pair_is_far(float mix, float miy, float miz, float Li, float mjx, float mjy,
-                                            float mjz, float Lj, float kappa2, float& dx, float& dy, float& dz) {
+                                            float mjz, float Lj, float kappa2, float& dx, float& dy, float& dz,
+                                            float& R2, float& Lm2) {
   dx = __fsub_rn(mjx, mix);
   dy = __fsub_rn(mjy, miy);
   dz = __fsub_rn(mjz, miz);
-  const float R2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+  R2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
   const float Lm = fmaxf(Li, Lj);
-  return Li > 0.0f && Lj > 0.0f && R2 >= __fmul_rn(kappa2, __fmul_rn(Lm, Lm));
+  Lm2 = __fmul_rn(Lm, Lm);
+  return Li > 0.0f && Lj > 0.0f && R2 >= __fmul_rn(kappa2, Lm2);
+}
+__device__ __forceinline__ bool pair_is_far(float mix, float miy, float miz, float Li, float mjx, float mjy,
+                                            float mjz, float Lj, float kappa2, float& dx, float& dy, float& dz) {
+  float R2, Lm2;
+  return pair_is_far(mix, miy, miz, Li, mjx, mjy, mjz, Lj, kappa2, dx, dy, dz, R2, Lm2);
 }
 
 // Flat parameter layout (FP32 master copy): W1 [128 x 8], b1 [128],

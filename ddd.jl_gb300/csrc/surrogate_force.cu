@@ -53,8 +53,8 @@ size_t quad_seg_bytes(int64_t npad);
 cudaError_t launch_prep_quad_seg(const double* soa, const float* ms, int64_t npad, float* qs, cudaStream_t st);
 int quad_far_blocks_per_sm(int nq);
 cudaError_t launch_quad_far_tiles(const float* ms, const float* qs, const double* soa, int64_t npad, const int4* items,
-                                  int32_t nItems, int nq, const KConsts& K, float kappa2, double* partial, int grid,
-                                  cudaStream_t st);
+                                  int32_t nItems, int nq, const KConsts& K, float kappa2, float kappaTwo2,
+                                  double* partial, int grid, cudaStream_t st);
 
 namespace sf {
 
@@ -539,7 +539,7 @@ int ddd_surrogate_force(ddd_surrogate* s, const ddd_consts* k, const double* seg
                         ddd_sur_report* rep) {
   DDD_NVTX("ddd_surrogate_force");
   if (!s) return DDD_EINVAL;
-  ddd_sur_opts o{20.0, 0.01, 1e-3, DDD_MODE_FP64, 0};
+  ddd_sur_opts o{20.0, 0.01, 1e-3, DDD_MODE_FP64, 0, 0.0};
   if (opts) o = *opts;
   if (o.exact_mode != DDD_MODE_FP64 && o.exact_mode != DDD_MODE_FP64_FAST && o.exact_mode != DDD_MODE_DF64 &&
       o.exact_mode != DDD_MODE_F32C)
@@ -552,6 +552,8 @@ int ddd_surrogate_force(ddd_surrogate* s, const ddd_consts* k, const double* seg
     if (!std::isfinite(x)) return sfail(s, DDD_ENONFINITE, "non-finite material/core constant");
   if (!(k->aSq > 0.0)) return sfail(s, DDD_EINVAL, "aSq (coreRadSq) must be > 0");
   if (!(o.kappa > 0.0) || !std::isfinite(o.kappa)) return sfail(s, DDD_EINVAL, "kappa must be > 0");
+  if (!(o.kappa_two >= 0.0) || !std::isfinite(o.kappa_two))
+    return sfail(s, DDD_EINVAL, "kappa_two must be >= 0 (0: no 2-point switch)");
   if (!(o.audit_fraction >= 0.0 && o.audit_fraction <= 1.0)) return sfail(s, DDD_EINVAL, "audit_fraction in [0, 1]");
   if (numSeg < 0 || ldSegs < numSeg) return sfail(s, DDD_EINVAL, "numSeg < 0 or ldSegs < numSeg");
   if (numSeg > ((int64_t)1 << 24)) return sfail(s, DDD_ETOOBIG, "numSeg above 2^24");
@@ -612,9 +614,11 @@ int ddd_surrogate_force(ddd_surrogate* s, const ddd_consts* k, const double* seg
 
   // 2. far pass over every tile pair: the network, or Gauss-Legendre quadrature
   if (o.far_mode) {
+    const float kappaTwo = (float)o.kappa_two;
+    const float kappaTwo2 = o.far_mode == 3 && o.kappa_two > 0.0 ? kappaTwo * kappaTwo : INFINITY;
     SCK(launch_quad_far_tiles(P.ms.as<float>(), P.qs.as<float>(), P.soa.as<double>(), npad, P.allItems.as<int4>(),
                               (int32_t)P.nItems,
-                              o.far_mode, K, kappa * kappa, P.partial.as<double>(),
+                              o.far_mode, K, kappa * kappa, kappaTwo2, P.partial.as<double>(),
                               (int)std::min<int64_t>(P.gridQuad, P.nItems), st),
         "quadrature pass");
   } else {

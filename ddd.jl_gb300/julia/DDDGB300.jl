@@ -397,6 +397,7 @@ struct DDDSurOpts
     audit_tol::Float64
     exact_mode::Cint
     far_mode::Cint
+    kappa_two::Float64
 end
 
 struct DDDSurReport
@@ -459,15 +460,18 @@ end
 # exact_mode: 0 = strict FP64 (DDD_MODE_FP64), 4 = fast FP64, 2 = df64, 3 = f32c.
 # far_mode: 0 = far pairs through the network; 2 or 3 = Gauss-Legendre
 # quadrature with that many points per segment (no weights read).
+# kappa_two (far_mode 3): 32-pair steps whose far pairs all lie beyond that many
+# lengths take the 2-point rule; 0 = always 3 points.
 function calcSegSegForceSurrogateGPU(s::Surrogate, dlnParams, matParams, network;
-                                     audit_fraction = 0.01, audit_tol = 1e-3, exact_mode = 0, far_mode = 0)
+                                     audit_fraction = 0.01, audit_tol = 1e-3, exact_mode = 0, far_mode = 0,
+                                     kappa_two = far_mode == 3 ? 30.0 : 0.0)
     nu = 1 - matParams.μ4π / matParams.μ4πν
     far_mode != 0 || isnan(s.nu) || abs(nu - s.nu) <= 1e-9 ||
         throw(ArgumentError("surrogate trained for nu = $(s.nu), not $nu"))
     numSeg = network.numSeg[1]
     out = zeros(3, 2, numSeg)
     k = Ref(consts(dlnParams, matParams))
-    opts = Ref(DDDSurOpts(s.kappa, audit_fraction, audit_tol, exact_mode, far_mode))
+    opts = Ref(DDDSurOpts(s.kappa, audit_fraction, audit_tol, exact_mode, far_mode, kappa_two))
     rep = Ref{DDDSurReport}()
     coord, bVec, segIdx, extSeg = network.coord, network.bVec, network.segIdx, network.extSeg
     GC.@preserve coord bVec segIdx extSeg out begin

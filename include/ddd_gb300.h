@@ -458,7 +458,7 @@ int ddd_surrogate_load(ddd_surrogate* s, const char* path, double* kappa, double
  * R >= 20 max(L_i, L_j)) where the analytic FP64 formula loses up to ~1e-3 to
  * cancellation; the near pass, audit and fallback are unchanged.
  * opts may be NULL (kappa 20, audit_fraction 0.01, audit_tol 1e-3, exact_mode
- * DDD_MODE_FP64, far_mode 0); rep may be
+ * DDD_MODE_FP64, far_mode 0, kappa_two 0); rep may be
  * NULL.  Synchronous: the work is queued on `stream` (NULL: the surrogate's own
  * stream, after waiting for all work already queued on the device) and the
  * call returns when the forces are complete. */
@@ -474,6 +474,10 @@ typedef struct {
   int far_mode;          /* 0: far pairs through the network; 2 or 3: through Gauss-Legendre quadrature with
                             that many points on each segment, in FP32 (no network involved: the surrogate's
                             weights and trained Poisson ratio are not used) */
+  double kappa_two;      /* far_mode 3 only, >= 0: the far pass takes the 2-point rule for a warp's step of
+                            32 pairs when each far pair in it lies beyond kappa_two max(L_i, L_j) (the
+                            2-point rule's truncation is below the FP32 noise there from ~30); 0: always
+                            3 points */
 } ddd_sur_opts;
 typedef struct {
   int64_t pairs_total;          /* unordered pairs of active segments */

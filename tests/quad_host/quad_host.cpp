@@ -75,10 +75,12 @@ extern "C" void quad_pair_forces(const double* k5, const double* segs, const int
 // trust test R^2 >= kappa^2 max(L_i, L_j)^2 on FP32 midpoints and lengths) by
 // the quadrature, taking the reference's near-parallel construction where its
 // FP64 branch test says so (qf::par_pair, the kernel's own code), near pairs by
-// the oracle's FP64 restatement of the reference.  out: 6 per row (node 1,
-// node 2).  Summation in j order, FP64.
+// the oracle's FP64 restatement of the reference.  two (nRows x n bytes, or
+// NULL): far pairs flagged there take the 2-point rule whatever nq is (the
+// kernel's per-tile-pair switch, decided by the caller).  out: 6 per row
+// (node 1, node 2).  Summation in j order, FP64.
 extern "C" void quad_network_rows(const double* k5, const double* segs, int64_t n, double kappa, int nq,
-                                  const int64_t* rows, int64_t nRows, double* out) {
+                                  const int64_t* rows, int64_t nRows, const uint8_t* two, double* out) {
   using namespace ddd::qf;
   const QConst K{(float)k5[0], (float)k5[1], (float)k5[3], (float)k5[4], (float)(k5[0] * k5[2])};
   ddd_oracle::Consts<double> KO;
@@ -126,19 +128,20 @@ extern "C" void quad_network_rows(const double* k5, const double* segs, int64_t 
         double c = 0.0;
         const float c32 = dot(a.t, b.t);
         const bool par = 1.0f - c32 * c32 <= 1e-5f && par_decision(D[i].t, D[j].t, c);
+        const int nqp = two && two[r * n + j] ? 2 : nq;
         if (!par) {
-          if (nq == 3)
+          if (nqp == 3)
             side<3>(K, dm, a.l, a.b, b.t, b.L, b.b, Fa, Fb);
           else
             side<2>(K, dm, a.l, a.b, b.t, b.L, b.b, Fa, Fb);
         } else if (i < j) {  // segment i is the reference's seg 1
-          if (nq == 3)
+          if (nqp == 3)
             par_pair<3>(K, D[i], D[j], c, dm, a.l, a.b, b.l, b.b, Fa, Fb, Fc, Fd);
           else
             par_pair<2>(K, D[i], D[j], c, dm, a.l, a.b, b.l, b.b, Fa, Fb, Fc, Fd);
         } else {  // segment i is seg 2: its forces are the pair's Fc, Fd
           const V3f dmr = {-dm.x, -dm.y, -dm.z};
-          if (nq == 3)
+          if (nqp == 3)
             par_pair<3>(K, D[j], D[i], c, dmr, b.l, b.b, a.l, a.b, Fc, Fd, Fa, Fb);
           else
             par_pair<2>(K, D[j], D[i], c, dmr, b.l, b.b, a.l, a.b, Fc, Fd, Fa, Fb);

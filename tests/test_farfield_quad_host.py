@@ -79,9 +79,9 @@ def test_quadrature_against_long_double(pkg, oracle, quadhost, RL, nq, med, mx):
     assert np.median(errs) <= med and np.max(errs) <= mx, (np.median(errs), np.max(errs))
 
 
-@pytest.mark.parametrize("kappa", [20.0, 10.0])
+@pytest.mark.parametrize("kappa,kappa_two", [(20.0, 0.0), (10.0, 0.0), (10.0, 30.0)])
 @pytest.mark.parametrize("loops,seed,cube,pf", [(600, 41, 20000.0, 0.05), (300, 7, 3000.0, 0.2)])
-def test_network_rows_against_long_double(pkg, synth, oracle, quadhost, loops, seed, cube, pf, kappa):
+def test_network_rows_against_long_double(pkg, synth, oracle, quadhost, loops, seed, cube, pf, kappa, kappa_two):
     """A whole network as the far-field mode computes it (quad_network_rows:
     the kernel's own decisions and near-parallel construction, near pairs from
     the oracle), 48 sampled segments against the long-double evaluation of the
@@ -91,27 +91,39 @@ def test_network_rows_against_long_double(pkg, synth, oracle, quadhost, loops, s
     Measured with 3 points: normwise ~3e-10, worst node ~4e-9 relative (far
     pairs' forces are small beside the near pairs', so their FP32 error of
     ~2e-7 each stays small in the node sums), at the trust factor 20 and at
-    10 (the quadrature's default).  Bounds: normwise 1e-8, per node
-    1e-6 |F| + 1e-8 max |F|."""
+    10 (the quadrature's default).  kappa_two > 0: every pair beyond
+    kappa_two max(L_i, L_j) takes the 2-point rule, more pairs than the GPU
+    pass's switch (a 32-pair step only when all its far pairs are that far);
+    at 30 the errors stay where they are (measured ~7.5e-10 normwise with 96 %
+    of the pairs on 2 points on 32,768 segments of the workload).  Bounds:
+    normwise 1e-8, per node 1e-6 |F| + 1e-8 max |F|."""
     dp, ip = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)
     quadhost.quad_network_rows.argtypes = [dp, dp, ctypes.c_int64, ctypes.c_double, ctypes.c_int, ip, ctypes.c_int64,
-                                           dp]
+                                           ctypes.c_void_p, dp]
     quadhost.quad_network_rows.restype = None
     p, b = synth.square_loops(loops, seed, 20.0, 200.0, cube, 0.5, pf)
     net = pkg.DislocationNetwork(*synth.network_arrays(p, b))
     n = net.numSeg
     segs = np.ascontiguousarray(synth.packed_soa(p, b).T)
     rows = np.sort(np.random.default_rng(seed).choice(n, 48, replace=False)).astype(np.int64)
+    two = None
+    if kappa_two > 0:
+        m = 0.5 * (segs[:, 0:3] + segs[:, 3:6])
+        L = np.linalg.norm(segs[:, 3:6] - segs[:, 0:3], axis=1)
+        R = np.linalg.norm(m[rows][:, None] - m[None], axis=2)
+        two = np.ascontiguousarray(R >= kappa_two * np.maximum(L[rows][:, None], L[None]), dtype=np.uint8)
+        assert two.mean() > 0.05
     out = np.zeros((len(rows), 6))
     quadhost.quad_network_rows(K5.ctypes.data_as(dp), segs.ctypes.data_as(dp), n, kappa, 3, rows.ctypes.data_as(ip),
-                               len(rows), out.ctypes.data_as(dp))
+                               len(rows), None if two is None else two.ctypes.data_as(ctypes.c_void_p),
+                               out.ctypes.data_as(dp))
     ext = oracle.segseg_ser_ld(K5, net, rows, nthreads=os.cpu_count() or 1)
     G = out.reshape(-1, 2, 3).transpose(2, 1, 0)
     nrm = lambda a: np.linalg.norm(a, axis=0)
     rel = np.linalg.norm(G - ext) / np.linalg.norm(ext)
     if os.environ.get("DDD_TEST_STATS"):
         with open(os.environ["DDD_TEST_STATS"], "a") as fh:
-            fh.write("quad network rows %d loops cube %g kappa %g: rel %.3e max node rel %.3e\n" % (
-                loops, cube, kappa, rel, np.max(nrm(G - ext) / nrm(ext))))
+            fh.write("quad network rows %d loops cube %g kappa %g kappa_two %g: rel %.3e max node rel %.3e\n" % (
+                loops, cube, kappa, kappa_two, rel, np.max(nrm(G - ext) / nrm(ext))))
     assert rel <= 1e-8, rel
     assert np.all(nrm(G - ext) <= 1e-6 * nrm(ext) + 1e-8 * nrm(ext).max())

@@ -282,11 +282,13 @@ def test_committed_checkpoint_gain_over_f32c_exact(pkg, synth):
     assert ms_quad < ms_f32c, (ms_quad, ms_f32c)
 
 
-@pytest.mark.parametrize("exact_mode,far,kappa,rel_max", [("fp64", "quad3", None, 1e-8),
-                                                         ("fp64_fast", "quad3", None, 1e-8),
-                                                         ("fp64_fast", "quad3", 20.0, 1e-8),
-                                                         ("f32c", "quad3", None, 1e-6), ("fp64", "quad2", None, 1e-6)])
-def test_quadrature_far_field(pkg, synth, oracle, exact_mode, far, kappa, rel_max):
+@pytest.mark.parametrize("exact_mode,far,kappa,kappa_two,rel_max", [("fp64", "quad3", None, None, 1e-8),
+                                                                   ("fp64", "quad3", None, 0.0, 1e-8),
+                                                                   ("fp64_fast", "quad3", None, None, 1e-8),
+                                                                   ("fp64_fast", "quad3", 20.0, None, 1e-8),
+                                                                   ("f32c", "quad3", None, None, 1e-6),
+                                                                   ("fp64", "quad2", None, None, 1e-6)])
+def test_quadrature_far_field(pkg, synth, oracle, exact_mode, far, kappa, kappa_two, rel_max):
     """far = "quad3" / "quad2": far pairs by FP32 Gauss-Legendre quadrature on
     both segments (no network), near pairs exact; near-parallel far pairs take
     the reference's projected geometry first.  On a 12,000-segment network of
@@ -296,7 +298,9 @@ def test_quadrature_far_field(pkg, synth, oracle, exact_mode, far, kappa, rel_ma
     build of the same code measures ~3e-10), <= 1e-6 with f32c near pairs (their own ~2e-7) or 2
     points; per node <= 1e-4 |F| + 1e-6 max|F|.  The default trust factor is
     10 lengths for 3 points and 20 for 2 (the 3-point rule is at its FP32
-    noise level from 8); 20 with 3 points is checked too.  The result does not
+    noise level from 8); 20 with 3 points is checked too.  "quad3" switches
+    32-pair steps whose far pairs all lie beyond 30 lengths to 2 points by
+    default (kappa_two); 0 keeps 3 points everywhere.  The result does not
     depend on the network's weights, every pair is counted once, and repeats
     are bit-equal."""
     dln, mat = _params(pkg)
@@ -304,12 +308,12 @@ def test_quadrature_far_field(pkg, synth, oracle, exact_mode, far, kappa, rel_ma
     n = segs.shape[1]
     k, k5 = _k(pkg), k5_of(dln, mat)
     sur = pkg.Surrogate(pkg.get_context(), seed=0)  # untrained: not used by the quadrature
-    F, rep = sur.force(k, segs, far=far, exact_mode=exact_mode, audit_fraction=0.02, kappa=kappa)
+    F, rep = sur.force(k, segs, far=far, exact_mode=exact_mode, audit_fraction=0.02, kappa=kappa, kappa_two=kappa_two)
     assert rep["fallback"] == 0 and rep["pairs_total"] == n * (n - 1) // 2
     assert rep["pairs_near_general"] + rep["pairs_near_parallel"] < rep["pairs_total"] // 10
     flat = sur.params()
     sur.set_params(np.full_like(flat, 3.0))
-    F2, _ = sur.force(k, segs, far=far, exact_mode=exact_mode, audit_fraction=0.02, kappa=kappa)
+    F2, _ = sur.force(k, segs, far=far, exact_mode=exact_mode, audit_fraction=0.02, kappa=kappa, kappa_two=kappa_two)
     assert torch.equal(F, F2)
     F3 = np.asfortranarray(F.cpu().numpy().reshape(n, 2, 3).transpose(2, 1, 0))
     rows = np.sort(np.random.default_rng(5).choice(n, 96, replace=False))
@@ -323,6 +327,30 @@ def test_quadrature_far_field(pkg, synth, oracle, exact_mode, far, kappa, rel_ma
                 far, exact_mode, rel, (nrm(G - ext) / nrm(ext)).max(), rep["audit_node_rel_rms"], rep))
     assert rel <= rel_max, rel
     assert np.all(nrm(G - ext) <= 1e-4 * nrm(ext) + 1e-6 * nrm(ext).max())
+
+
+def test_quadrature_two_point_switch(pkg, synth):
+    """The 3-point far pass's switch to 2 points (kappa_two): with the default
+    30 lengths it changes the forces (some 32-pair steps lie that far out on
+    this 12,000-segment network) by far less than the quadrature's own error
+    (relative RMS <= 1e-8 against kappa_two = 0); a threshold no pair reaches
+    gives the 3-point result bit for bit, and 2-point-only runs (far_mode 2)
+    do not depend on it.  A negative or non-finite kappa_two is refused."""
+    net, segs = _network(pkg, synth, 1500, seed=41)
+    k = _k(pkg)
+    sur = pkg.Surrogate(pkg.get_context(), seed=0)
+    F0, _ = sur.force(k, segs, far="quad3", exact_mode="fp64", audit_fraction=0.0, kappa_two=0.0)
+    F30, _ = sur.force(k, segs, far="quad3", exact_mode="fp64", audit_fraction=0.0, kappa_two=30.0)
+    Fbig, _ = sur.force(k, segs, far="quad3", exact_mode="fp64", audit_fraction=0.0, kappa_two=1e12)
+    assert torch.equal(F0, Fbig)
+    assert not torch.equal(F0, F30)
+    assert (torch.linalg.norm(F30 - F0) / torch.linalg.norm(F0)).item() <= 1e-8
+    G0, _ = sur.force(k, segs, far="quad2", exact_mode="fp64", audit_fraction=0.0, kappa_two=0.0)
+    G1, _ = sur.force(k, segs, far="quad2", exact_mode="fp64", audit_fraction=0.0, kappa_two=30.0)
+    assert torch.equal(G0, G1)
+    for bad in (-1.0, float("inf"), float("nan")):
+        with pytest.raises(pkg.DDDError):
+            sur.force(k, segs, far="quad3", exact_mode="fp64", audit_fraction=0.0, kappa_two=bad)
 
 
 def test_host_array_entry_matches_device_form(pkg, synth, trained):
