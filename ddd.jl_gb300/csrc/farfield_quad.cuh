@@ -61,9 +61,14 @@ struct Rule<3> {
   static QF_HD float w(int i) { return i == 1 ? 0.44444444444444444f : 0.27777777777777778f; }
 };
 
+// The argument is a squared distance between points of a far pair's segments
+// (>= ((kappa - 1) L)^2 > 0), never subnormal, so the flush-to-zero form of the
+// hardware approximation gives the same value without the subnormal handling
+// that rsqrtf carries.
 QF_HD float rsqrt_(float v) {
 #if defined(__CUDA_ARCH__)
-  const float y = rsqrtf(v);
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(v));
 #else
   const float y = 1.0f / std::sqrt(v);
 #endif
