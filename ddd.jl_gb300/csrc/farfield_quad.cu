@@ -257,8 +257,6 @@ quad_far_tiles(const float* __restrict__ ms, const float* __restrict__ qs, const
                                                                ms[sur::kMsL * npad + gi], sm.cLen[jl], kappaTwo2));
         if (has) {
           const qf::SegD si = seg_d(soa, npad, gi), sj = seg_d(soa, npad, gj);
-          double c;
-          qf::par_decision(si.t, sj.t, c);
           const qf::V3f dm = {(mi2[0] - sm.cM[0][jl]) + (qs[(kQLo + 0) * npad + gi] - sm.cQ[kQLo + 0][jl]),
                               (mi2[1] - sm.cM[1][jl]) + (qs[(kQLo + 1) * npad + gi] - sm.cQ[kQLo + 1][jl]),
                               (mi2[2] - sm.cM[2][jl]) + (qs[(kQLo + 2) * npad + gi] - sm.cQ[kQLo + 2][jl])};
@@ -266,11 +264,15 @@ quad_far_tiles(const float* __restrict__ ms, const float* __restrict__ qs, const
           const qf::V3f ba = {qs[(kQB + 0) * npad + gi], qs[(kQB + 1) * npad + gi], qs[(kQB + 2) * npad + gi]};
           const qf::V3f lb = {sm.cQ[kQL + 0][jl], sm.cQ[kQL + 1][jl], sm.cQ[kQL + 2][jl]};
           const qf::V3f bb = {sm.cQ[kQB + 0][jl], sm.cQ[kQB + 1][jl], sm.cQ[kQB + 2][jl]};
+          const qf::V3f ta = {qs[(kQT + 0) * npad + gi], qs[(kQT + 1) * npad + gi], qs[(kQT + 2) * npad + gi]};
+          const qf::V3f tb = {sm.cQ[kQT + 0][jl], sm.cQ[kQT + 1][jl], sm.cQ[kQT + 2][jl]};
+          const qf::V3f ma = {mi2[0], mi2[1], mi2[2]}, mb = {sm.cM[0][jl], sm.cM[1][jl], sm.cM[2][jl]};
+          const bool flip = qf::dot(ta, tb) < 0.0f;  // the sign of the FP64 t_i.t_j (|c| > 1 - 1e-8 here)
           qf::V3f Fa, Fb, Fc, Fd;
           if (two)
-            qf::par_pair<2>(K, si, sj, c, dm, la, ba, lb, bb, Fa, Fb, Fc, Fd);
+            qf::par_pair<2>(K, si, sj, flip, dm, ma, mb, ta, tb, la, ba, lb, bb, Fa, Fb, Fc, Fd);
           else
-            qf::par_pair<NQ>(K, si, sj, c, dm, la, ba, lb, bb, Fa, Fb, Fc, Fd);
+            qf::par_pair<NQ>(K, si, sj, flip, dm, ma, mb, ta, tb, la, ba, lb, bb, Fa, Fb, Fc, Fd);
           const float v[12] = {Fa.x, Fa.y, Fa.z, Fb.x, Fb.y, Fb.z, Fc.x, Fc.y, Fc.z, Fd.x, Fd.y, Fd.z};
 #pragma unroll
           for (int c2 = 0; c2 < 12; ++c2) sm.cf[t][c2] = v[c2];

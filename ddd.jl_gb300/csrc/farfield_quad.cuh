@@ -164,8 +164,8 @@ struct Src {
 QF_HD double dotd(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
 
 // One side of calcParSegSegForce (DislocationForces.jl:1204-1317, :1319-1433):
-// the source segment nb1 -> nb1 + lb (Burgers bb; FP64, nb1 relative to the
-// source's midpoint, nb1abs its absolute position) is projected onto the field
+// the source segment nb1 -> nb1 + lb (nb1 = -lb/2 relative to the source's
+// midpoint, nb1abs its absolute position) is projected onto the field
 // segment's direction ta and pulled in by the critical angle: with
 // proj = (lb.ta) ta, diff = lb - proj, the segment nbm1 = nb1 + diff/2 +
 // hCot |diff| ta -> nbm2 = nb1 + proj + diff/2 - hCot |diff| ta.  When the
@@ -177,24 +177,25 @@ QF_HD double dotd(const double* a, const double* b) { return a[0] * b[0] + a[1] 
 // reference evaluates the same geometry analytically.
 //
 // Only the rejection needs FP64 (it is |lb| sin(angle), far below |lb|): lb.ta,
-// diff and diff.diff are formed as the reference forms them.  The sources are
-// FP32 quantities, and they simplify exactly: the main source runs along ta
-// with signed length lb.ta - 2 hCot |diff| and its midpoint is the source's own
-// (nb1 + lb/2), and both connectors are the vector diff/2 + hCot |diff| ta.  The
-// connector test is decided in FP32 unless it falls within 1e-5 of its
-// threshold, where it is evaluated in FP64 exactly as written above.
-template <int SIDE>
-QF_HD int par_sources(const double* ta, const double* nb1, const double* nb1abs, const double* lb, const double* bb,
+// diff and diff.diff are formed from the FP64 ta and lb as the reference forms
+// them.  Everything else comes in FP32, as the general path already holds it:
+// t and lv (ta and lb rounded), the Burgers vector b, and a0, the source's
+// first node in absolute coordinates to ~1e-7 relative.  The sources simplify
+// exactly: the main source runs along ta with signed length lb.ta - 2 hCot
+// |diff| and its midpoint is the source's own (nb1 + lb/2), and both
+// connectors are the vector diff/2 + hCot |diff| ta.  The connector test is
+// decided in FP32 (a0's error is far inside the margin) unless it falls within
+// 1e-5 of its threshold, where it is evaluated in FP64 exactly as written
+// above, on nb1abs(k), the FP64 node.
+template <int SIDE, class Abs>
+QF_HD int par_sources(const double* ta, const double* lb, V3f t, V3f lv, V3f b, V3f a0, const Abs& nb1abs,
                       Src* out) {
   const double tmp = dotd(lb, ta);
   const double proj[3] = {tmp * ta[0], tmp * ta[1], tmp * ta[2]};
   const double diff[3] = {lb[0] - proj[0], lb[1] - proj[1], lb[2] - proj[2]};
   const double dd = dotd(diff, diff);
-  const V3f t = {(float)ta[0], (float)ta[1], (float)ta[2]};
   const V3f d = {(float)diff[0], (float)diff[1], (float)diff[2]};
-  const V3f n1 = {(float)nb1[0], (float)nb1[1], (float)nb1[2]};
-  const V3f lv = {(float)lb[0], (float)lb[1], (float)lb[2]};
-  const V3f b = {(float)bb[0], (float)bb[1], (float)bb[2]};
+  const V3f n1 = -0.5f * lv;  // the FP32 rounding of -lb/2 (exact scaling)
   const float h = (float)kParHCot * std::sqrt((float)dd);  // hCot |diff|
   int n = 0;
   const float Lm = (float)tmp - 2.0f * h;  // signed length of nbm1 -> nbm2 along ta
@@ -207,7 +208,6 @@ QF_HD int par_sources(const double* ta, const double* nb1, const double* nb1abs,
   }
   // Connector test: |nbm1|^2 + |nbm2|^2 in FP32, FP64 next to the threshold.
   const V3f c = 0.5f * d + h * t;  // nb1 -> nbm1, and nbm2 -> nb1 + lb
-  const V3f a0 = {(float)nb1abs[0], (float)nb1abs[1], (float)nb1abs[2]};
   const V3f a1 = a0 + c, a2 = a0 + (float)tmp * t + 0.5f * d - h * t;
   const float thr = (float)kParEps * (dot(a1, a1) + dot(a2, a2));
   const float ddf = (float)dd;
@@ -220,9 +220,10 @@ QF_HD int par_sources(const double* ta, const double* nb1, const double* nb1abs,
     const double magDiff = sqrt(dd);
     double e1[3], e2[3];
     for (int k = 0; k < 3; ++k) {
+      const double na = nb1abs(k);
       const double tv1 = 0.5 * diff[k], tv2 = kParHCot * magDiff * ta[k];
-      e1[k] = nb1abs[k] + tv1 + tv2;
-      e2[k] = nb1abs[k] + proj[k] + tv1 - tv2;
+      e1[k] = na + tv1 + tv2;
+      e2[k] = na + proj[k] + tv1 - tv2;
     }
     const double magDiffSq = SIDE == 1 ? dd : magDiff * magDiff;
     conn = magDiffSq > kParEps * (dotd(e1, e1) + dotd(e2, e2));
@@ -257,22 +258,33 @@ QF_HD bool par_decision(const double* ti, const double* tj, double& c) {
 #endif
 }
 
+// FP64 node 1 of a segment, or its node 2 (n1 + l, as the reference forms
+// the reversed segment's start) when flipped: the connector test's operand.
+struct NodeAbs {
+  const SegD* s;
+  bool end2;
+  QF_HD double operator()(int k) const { return end2 ? s->n1[k] + s->l[k] : s->n1[k]; }
+};
+
 // A near-parallel pair (segment i = seg 1, j = seg 2 of calcParSegSegForce):
-// forces on i (Fa, Fb) and on j (Fc, Fd) from the reference's rebuilt sources,
-// dm = m_i - m_j and the FP32 segment vectors and Burgers vectors as the
-// general path takes them.  Seg 1 is flipped when c < 0, as the reference
-// does: side 1 then projects onto -t_i, and side 2's source is seg 1 reversed
-// (its Burgers vector negated).
+// forces on i (Fa, Fb) and on j (Fc, Fd) from the reference's rebuilt sources.
+// FP64 from si, sj: the directions t and segment vectors l (the rejection's
+// operands) and the nodes (the connector test near its threshold).  FP32 as
+// the general path takes them: dm = m_i - m_j, the midpoints mi, mj, the unit
+// directions ti, tj (the FP64 ones rounded), segment vectors and Burgers
+// vectors.  Seg 1 is flipped when c = t_i.t_j < 0 (flip; for a near-parallel
+// pair |c| > 1 - 1e-8, so the FP32 dot product has the same sign), as the
+// reference does: side 1 then projects onto -t_i, and side 2's source is
+// seg 1 reversed (its Burgers vector negated).
 template <int NQ>
-QF_HD void par_pair(const QConst& K, const SegD& si, const SegD& sj, double c, V3f dm, V3f li, V3f bi, V3f lj, V3f bj,
-                    V3f& Fa, V3f& Fb, V3f& Fc, V3f& Fd) {
-  const bool flip = c < 0.0;
+QF_HD void par_pair(const QConst& K, const SegD& si, const SegD& sj, bool flip, V3f dm, V3f mi, V3f mj, V3f ti,
+                    V3f tj, V3f li, V3f bi, V3f lj, V3f bj, V3f& Fa, V3f& Fb, V3f& Fc, V3f& Fd) {
   Src src[3];
   Fa = Fb = Fc = Fd = {0.f, 0.f, 0.f};
   {  // side 1: field i (direction t_i, or -t_i when flipped), source j
     const double ta[3] = {flip ? -si.t[0] : si.t[0], flip ? -si.t[1] : si.t[1], flip ? -si.t[2] : si.t[2]};
-    const double nb1[3] = {-0.5 * sj.l[0], -0.5 * sj.l[1], -0.5 * sj.l[2]};
-    const int n = par_sources<1>(ta, nb1, sj.n1, sj.l, sj.b, src);
+    const V3f t = flip ? V3f{-ti.x, -ti.y, -ti.z} : ti;
+    const int n = par_sources<1>(ta, sj.l, t, lj, bj, mj - 0.5f * lj, NodeAbs{&sj, false}, src);
     for (int q = 0; q < n; ++q) {
       V3f a, b;
       side<NQ>(K, dm - src[q].off, li, bi, src[q].to, src[q].Lo, src[q].bo, a, b);
@@ -281,20 +293,16 @@ QF_HD void par_pair(const QConst& K, const SegD& si, const SegD& sj, double c, V
     }
   }
   {  // side 2: field j (direction t_j), source i (reversed when flipped)
-    double nb1abs[3], lb[3], bb[3], nb1[3];
-    for (int k = 0; k < 3; ++k) {
-      nb1abs[k] = flip ? si.n1[k] + si.l[k] : si.n1[k];
-      lb[k] = flip ? -si.l[k] : si.l[k];
-      bb[k] = flip ? -si.b[k] : si.b[k];
-      nb1[k] = -0.5 * lb[k];
-    }
-    const int n = par_sources<2>(sj.t, nb1, nb1abs, lb, bb, src);
+    const double lb[3] = {flip ? -si.l[0] : si.l[0], flip ? -si.l[1] : si.l[1], flip ? -si.l[2] : si.l[2]};
+    const V3f lv = flip ? V3f{-li.x, -li.y, -li.z} : li;
+    const V3f b = flip ? V3f{-bi.x, -bi.y, -bi.z} : bi;
+    const int n = par_sources<2>(sj.t, lb, tj, lv, b, mi - 0.5f * lv, NodeAbs{&si, flip}, src);
     const V3f dmj = {-dm.x, -dm.y, -dm.z};
     for (int q = 0; q < n; ++q) {
-      V3f a, b;
-      side<NQ>(K, dmj - src[q].off, lj, bj, src[q].to, src[q].Lo, src[q].bo, a, b);
+      V3f a, bq;
+      side<NQ>(K, dmj - src[q].off, lj, bj, src[q].to, src[q].Lo, src[q].bo, a, bq);
       Fc = Fc + a;
-      Fd = Fd + b;
+      Fd = Fd + bq;
     }
   }
 }

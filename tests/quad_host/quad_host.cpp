@@ -135,16 +135,20 @@ extern "C" void quad_network_rows(const double* k5, const double* segs, int64_t 
           else
             side<2>(K, dm, a.l, a.b, b.t, b.L, b.b, Fa, Fb);
         } else if (i < j) {  // segment i is the reference's seg 1
+          const V3f ma = {a.mhi[0], a.mhi[1], a.mhi[2]}, mb = {b.mhi[0], b.mhi[1], b.mhi[2]};
+          const bool flip = dot(a.t, b.t) < 0.0f;
           if (nqp == 3)
-            par_pair<3>(K, D[i], D[j], c, dm, a.l, a.b, b.l, b.b, Fa, Fb, Fc, Fd);
+            par_pair<3>(K, D[i], D[j], flip, dm, ma, mb, a.t, b.t, a.l, a.b, b.l, b.b, Fa, Fb, Fc, Fd);
           else
-            par_pair<2>(K, D[i], D[j], c, dm, a.l, a.b, b.l, b.b, Fa, Fb, Fc, Fd);
+            par_pair<2>(K, D[i], D[j], flip, dm, ma, mb, a.t, b.t, a.l, a.b, b.l, b.b, Fa, Fb, Fc, Fd);
         } else {  // segment i is seg 2: its forces are the pair's Fc, Fd
           const V3f dmr = {-dm.x, -dm.y, -dm.z};
+          const V3f ma = {a.mhi[0], a.mhi[1], a.mhi[2]}, mb = {b.mhi[0], b.mhi[1], b.mhi[2]};
+          const bool flip = dot(a.t, b.t) < 0.0f;
           if (nqp == 3)
-            par_pair<3>(K, D[j], D[i], c, dmr, b.l, b.b, a.l, a.b, Fc, Fd, Fa, Fb);
+            par_pair<3>(K, D[j], D[i], flip, dmr, mb, ma, b.t, a.t, b.l, b.b, a.l, a.b, Fc, Fd, Fa, Fb);
           else
-            par_pair<2>(K, D[j], D[i], c, dmr, b.l, b.b, a.l, a.b, Fc, Fd, Fa, Fb);
+            par_pair<2>(K, D[j], D[i], flip, dmr, mb, ma, b.t, a.t, b.l, b.b, a.l, a.b, Fc, Fd, Fa, Fb);
         }
         F[0] = Fa.x, F[1] = Fa.y, F[2] = Fa.z, F[3] = Fb.x, F[4] = Fb.y, F[5] = Fb.z;
       } else {
