@@ -2,6 +2,8 @@
 import ctypes
 import os
 import re
+import shutil
+import subprocess
 
 import numpy as np
 import pytest
@@ -168,3 +170,59 @@ def test_julia_shim_structs_match_header():
     c = open(HEADER).read()
     for jname, cname in JULIA_STRUCTS.items():
         assert _jl_struct_fields(jl, jname) == _c_struct_fields(c, cname), jname
+
+
+def _ctypes_fields(cls):
+    kinds = {ctypes.c_double: "f64", ctypes.c_int: "i32", ctypes.c_int32: "i32", ctypes.c_int64: "i64",
+             ctypes.POINTER(ctypes.c_double): "ptr"}
+    out = []
+    for name, typ in cls._fields_:
+        if issubclass(typ, ctypes.Array):
+            out.append((name, kinds[typ._type_], typ._length_))
+        else:
+            out.append((name, kinds[typ], 1))
+    return out
+
+
+_ABI_STRUCTS = ("ddd_consts", "ddd_report", "ddd_self_params", "ddd_mob_params", "ddd_collision", "ddd_u_mesh",
+                "ddd_batch_info_t", "ddd_sur_opts", "ddd_sur_report")
+
+
+def test_python_structs_match_header(pkg, tmp_path):
+    """Every ctypes struct of the Python mirror has the header's fields, in
+    order, with the same widths, and the size the C compiler gives the
+    header's struct (the ABI these pointers cross)."""
+    c = open(HEADER).read()
+    for cname in _ABI_STRUCTS:
+        assert _ctypes_fields(getattr(pkg, cname)) == _c_struct_fields(c, cname), cname
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "sizes.c"
+    src.write_text('#include <stdio.h>\n#include "ddd_gb300.h"\nint main(void) {\n' + "".join(
+        '  printf("%%zu\\n", sizeof(%s));\n' % n for n in _ABI_STRUCTS) + "  return 0;\n}\n")
+    exe = str(tmp_path / "sizes")
+    r = subprocess.run([cc, "-std=c99", "-I", os.path.dirname(HEADER), str(src), "-o", exe], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+    sizes = [int(x) for x in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
+    assert sizes == [ctypes.sizeof(getattr(pkg, n)) for n in _ABI_STRUCTS]
+
+
+def test_quadrature_option_defaults(pkg):
+    """The Python mirror's far-field options: the quadrature's own trust
+    factors (QUAD_KAPPA for 3 points, QUAD2_KAPPA for 2), the 2-point switch
+    at QUAD_KAPPA_TWO lengths for 3 points only, the network's checkpoint
+    kappa otherwise; explicit values pass through."""
+    import types
+    k = pkg.consts_of(pkg.DislocationParameters(coreRad=1.0), pkg.MaterialParameters(mu=1.0, nu=0.28))
+    me = types.SimpleNamespace(kappa=20.0, nu=None)
+    o = pkg.Surrogate._opts(me, k, None, 0.01, 1e-3, "f32c", "quad3")
+    assert (o.kappa, o.kappa_two, o.far_mode, o.exact_mode) == (pkg.QUAD_KAPPA, pkg.QUAD_KAPPA_TWO, 3,
+                                                                  pkg.MODES["f32c"])
+    o = pkg.Surrogate._opts(me, k, None, 0.01, 1e-3, "fp64", "quad2")
+    assert (o.kappa, o.kappa_two, o.far_mode) == (pkg.QUAD2_KAPPA, 0.0, 2)
+    o = pkg.Surrogate._opts(me, k, None, 0.01, 1e-3, "fp64", "network")
+    assert (o.kappa, o.kappa_two, o.far_mode) == (20.0, 0.0, 0)
+    o = pkg.Surrogate._opts(me, k, 12.0, 0.0, 0.0, "fp64_fast", "quad3", 0.0)
+    assert (o.kappa, o.kappa_two, o.audit_fraction) == (12.0, 0.0, 0.0)
