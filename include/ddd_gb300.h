@@ -476,8 +476,8 @@ typedef struct {
                             weights and trained Poisson ratio are not used) */
   double kappa_two;      /* far_mode 3 only, >= 0: the far pass takes the 2-point rule for a warp's step of
                             32 pairs when each far pair in it lies beyond kappa_two max(L_i, L_j) (the
-                            2-point rule's truncation is below the FP32 noise there from ~30); 0: always
-                            3 points */
+                            2-point rule's truncation, ~5e-6 per pair at 20 lengths, falls as (L/R)^4;
+                            from 30 the node-force errors are those of 3 points); 0: always 3 points */
 } ddd_sur_opts;
 typedef struct {
   int64_t pairs_total;          /* unordered pairs of active segments */
