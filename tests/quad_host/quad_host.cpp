@@ -169,3 +169,27 @@ extern "C" void quad_network_rows(const double* k5, const double* segs, int64_t 
     for (int k = 0; k < 6; ++k) out[6 * r + k] = acc[k];
   }
 }
+
+// The near-parallel construction's source count (qf::par_sources) for n
+// configurations (FP64 rows: ta xyz, lb xyz, nb1abs xyz), with the FP32 inputs
+// formed as the far pass forms them: ta and lb rounded, and the source's node
+// from its FP32 midpoint minus half its FP32 vector.  nsrc[q] = the returned
+// count (bit 1 set when the connectors were added).
+extern "C" void quad_par_sources(int side, const double* cfg, int64_t n, int* nsrc) {
+  for (int64_t q = 0; q < n; ++q) {
+    const double* ta = cfg + 9 * q;
+    const double* lb = ta + 3;
+    const double* na = ta + 6;
+    const V3f t = {(float)ta[0], (float)ta[1], (float)ta[2]};
+    const V3f lv = {(float)lb[0], (float)lb[1], (float)lb[2]};
+    const V3f m = {(float)(na[0] + 0.5 * lb[0]), (float)(na[1] + 0.5 * lb[1]), (float)(na[2] + 0.5 * lb[2])};
+    const V3f a0 = m - 0.5f * lv;
+    struct Abs {
+      const double* p;
+      double operator()(int k) const { return p[k]; }
+    } abs{na};
+    ddd::qf::Src src[3];
+    nsrc[q] = side == 1 ? ddd::qf::par_sources<1>(ta, lb, t, lv, V3f{0.f, 0.f, 1.f}, a0, abs, src)
+                        : ddd::qf::par_sources<2>(ta, lb, t, lv, V3f{0.f, 0.f, 1.f}, a0, abs, src);
+  }
+}

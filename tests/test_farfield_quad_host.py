@@ -127,3 +127,78 @@ def test_network_rows_against_long_double(pkg, synth, oracle, quadhost, loops, s
                 loops, cube, kappa, kappa_two, rel, np.max(nrm(G - ext) / nrm(ext))))
     assert rel <= 1e-8, rel
     assert np.all(nrm(G - ext) <= 1e-6 * nrm(ext) + 1e-8 * nrm(ext).max())
+
+
+@pytest.mark.parametrize("side", [1, 2])
+def test_near_parallel_connector_test_matches_fp64(quadhost, side):
+    """The near-parallel construction decides the reference's connector test
+    (magDiffSq > sqrt(eps) (|nbm1|^2 + |nbm2|^2), DislocationForces.jl:1204-1317
+    and :1319-1433) in FP32 from approximate node positions, and in FP64 within
+    1e-5 of the threshold.  Over 20,000 near-parallel configurations (tilts
+    1e-7 to 1.2e-4 rad, segment lengths 20-200, positions 1 to 3e4 from the
+    origin, a third of them placed within 1e-3 relative of the threshold, half
+    of those within 5e-6), the decision equals the FP64 formula's evaluated in
+    the reference's order."""
+    dp = ctypes.POINTER(ctypes.c_double)
+    quadhost.quad_par_sources.argtypes = [ctypes.c_int, dp, ctypes.c_int64, ctypes.POINTER(ctypes.c_int)]
+    quadhost.quad_par_sources.restype = None
+    rng = np.random.default_rng(11 + side)
+    eps, hcot = 1.4901161193847656e-08, 4075.672300430329
+    n = 20000
+
+    def unit(v):
+        return v / np.linalg.norm(v, axis=-1, keepdims=True)
+
+    L = rng.uniform(20, 200, n)
+    u = unit(rng.normal(size=(n, 3)))
+    w = unit(np.cross(u, rng.normal(size=(n, 3))))
+    th = np.exp(rng.uniform(np.log(1e-7), np.log(1.2e-4), n))
+    ta = unit(np.cos(th)[:, None] * u + np.sin(th)[:, None] * w)
+    lb = L[:, None] * u
+    pos = unit(rng.normal(size=(n, 3))) * np.exp(rng.uniform(0, np.log(3e4), n))[:, None]
+
+    def ref_conn(ta, lb, na):
+        tmp = lb[:, 0] * ta[:, 0] + lb[:, 1] * ta[:, 1] + lb[:, 2] * ta[:, 2]
+        proj = tmp[:, None] * ta
+        diff = lb - proj
+        dd = diff[:, 0] * diff[:, 0] + diff[:, 1] * diff[:, 1] + diff[:, 2] * diff[:, 2]
+        mag = np.sqrt(dd)
+        tv1 = 0.5 * diff
+        tv2 = (hcot * mag)[:, None] * ta
+        e1 = na + tv1 + tv2
+        e2 = na + proj + tv1 - tv2
+        s1 = e1[:, 0] * e1[:, 0] + e1[:, 1] * e1[:, 1] + e1[:, 2] * e1[:, 2]
+        s2 = e2[:, 0] * e2[:, 0] + e2[:, 1] * e2[:, 1] + e2[:, 2] * e2[:, 2]
+        msq = dd if side == 1 else mag * mag
+        return msq > eps * (s1 + s2), msq, s1 + s2
+
+    # A third placed within 1e-3, relative, of the threshold: tilts of 9e-5 to
+    # 1.2e-4 rad (below ~8.6e-5 no position reaches it) and the node at
+    # -lb/2 + r v, r solving |r v + a|^2 + |r v + b|^2 = magDiffSq / (eps target)
+    # for the offsets a, b of nbm1 and nbm2 from that point.
+    k = np.arange(n) % 3 == 0
+    th[k] = rng.uniform(9e-5, 1.2e-4, k.sum())
+    ta = unit(np.cos(th)[:, None] * u + np.sin(th)[:, None] * w)
+    target = 1 + np.where(np.arange(n) % 2 == 0, rng.uniform(-1e-3, 1e-3, n), rng.uniform(-5e-6, 5e-6, n))
+    tmp = np.sum(lb * ta, axis=1)
+    diff = lb - tmp[:, None] * ta
+    dd = np.sum(diff * diff, axis=1)
+    h = (hcot * np.sqrt(dd))[:, None] * ta
+    a = -0.5 * lb + 0.5 * diff + h
+    b = -0.5 * lb + tmp[:, None] * ta + 0.5 * diff - h
+    v = unit(rng.normal(size=(n, 3)))
+    T = dd / (eps * target)
+    pb = np.sum(v * (a + b), axis=1)
+    disc = pb ** 2 - 2 * (np.sum(a * a, axis=1) + np.sum(b * b, axis=1) - T)
+    ok = k & (disc > 0)
+    r = (-pb + np.sqrt(np.where(disc > 0, disc, 0))) / 2
+    pos[ok] = -0.5 * lb[ok] + r[ok, None] * v[ok]
+    _, msq, ssum = ref_conn(ta, lb, pos)
+    close = ok & (np.abs(msq / (eps * ssum) - 1) < 2e-3)
+    want, _, _ = ref_conn(ta, lb, pos)
+    cfg = np.ascontiguousarray(np.concatenate([ta, lb, pos], axis=1))
+    got = np.zeros(n, dtype=np.int32)
+    quadhost.quad_par_sources(side, cfg.ctypes.data_as(dp), n, got.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    band = close & (np.abs(msq / (eps * ssum) - 1) < 1e-5)  # decided by the FP64 evaluation
+    assert close.sum() > n // 5 and band.sum() > n // 20 and 0.3 < want[close].mean() < 0.7
+    assert np.array_equal(got >= 2, want)
