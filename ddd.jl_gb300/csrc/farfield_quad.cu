@@ -66,14 +66,13 @@ __global__ void prep_quad_seg(const double* __restrict__ soa, const float* __res
   qs[kQLen * npad + i] = (float)(1.0 / soa[12 * npad + i]);
 }
 
-// FP64 record of segment g of the sorted SoA (rows n1, n2, b, t).
+// FP64 record of segment g of the sorted SoA (rows n1, n2, t).
 __device__ __forceinline__ qf::SegD seg_d(const double* __restrict__ soa, int64_t npad, int64_t g) {
   qf::SegD d;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     d.n1[k] = soa[k * npad + g];
     d.l[k] = soa[(3 + k) * npad + g] - d.n1[k];
-    d.b[k] = soa[(6 + k) * npad + g];
     d.t[k] = soa[(9 + k) * npad + g];
   }
   return d;

@@ -239,10 +239,10 @@ QF_HD int par_sources(const double* ta, const double* lb, V3f t, V3f lv, V3f b, 
   return n;
 }
 
-// FP64 record of one segment for the near-parallel path: node 1, n2 - n1,
-// Burgers vector and unit direction (the values the FP64 kernels use).
+// FP64 record of one segment for the near-parallel path: node 1, n2 - n1 and
+// the unit direction (the values the FP64 kernels use).
 struct SegD {
-  double n1[3], l[3], b[3], t[3];
+  double n1[3], l[3], t[3];
 };
 
 // The reference's branch decision on the FP64 directions (c = t_i.t_j and

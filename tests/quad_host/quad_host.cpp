@@ -101,7 +101,6 @@ extern "C" void quad_network_rows(const double* k5, const double* segs, int64_t 
     for (int k = 0; k < 3; ++k) {
       D[i].n1[k] = s[k];
       D[i].l[k] = s[3 + k] - s[k];
-      D[i].b[k] = s[6 + k];
       l2 += D[i].l[k] * D[i].l[k];
     }
     const double tN = 1.0 / std::sqrt(l2);  // the FP64 kernels' direction and inverse length
