@@ -19,8 +19,9 @@
 // With 3 points (far_mode 3) a warp's step of 32 pairs takes the 2-point rule
 // instead when each far pair it holds lies beyond kappaTwo max(L_i, L_j)
 // (ddd_sur_opts.kappa_two): the 2-point rule's truncation error falls as
-// (L/R)^4 and is below the FP32 arithmetic's ~2e-7 per pair from ~30 lengths,
-// and it costs 4 + 2 instead of 9 + 3 stress evaluations per side.  The choice
+// (L/R)^4 (~5e-6 per pair at 20 lengths, ~1e-6 at 30; from 30 the node-force
+// errors measure as with 3 points everywhere), and it costs 4 + 2 instead of
+// 9 + 3 stress evaluations per side.  The choice
 // is a warp vote on values fixed by the tile layout, so results stay
 // deterministic; the dense near-parallel pass votes the same way over its
 // listed pairs.
