@@ -127,8 +127,8 @@ QUAD_KAPPA = 10.0
 QUAD2_KAPPA = 20.0
 # The 3-point far pass switches a warp's step of 32 pairs to the 2-point rule
 # when each of its far pairs lies beyond this many lengths: the 2-point rule's
-# truncation (~5e-6 per pair at 20 lengths, falling as (L/R)^4) is then below
-# the far pairs' FP32 noise.
+# truncation (~5e-6 per pair at 20 lengths, falling as (L/R)^4) is then small
+# enough that the node-force errors measure as with 3 points everywhere.
 QUAD_KAPPA_TWO = 30.0
 
 
